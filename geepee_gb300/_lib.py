@@ -1,0 +1,102 @@
+"""ctypes binding of libgpk.so (the C ABI declared in include/gpk.h).
+
+The library is built in-tree by ``geepee_gb300.build``.  There is no fallback: if
+the shared object is missing or no CUDA device is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libgpk.so')
+
+GPK_DF64 = 0
+GPK_FP32 = 1
+
+_c_int = ctypes.c_int
+_c_dbl = ctypes.c_double
+_vp = ctypes.c_void_p
+
+# name -> argtypes (all return int)
+_SIGS = {
+    'gpk_version': [],
+    'gpk_kern': [_c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _c_int, _vp, _vp, _c_dbl, _vp, _c_int, _vp],
+    'gpk_psi_fwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                    _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_psi_bwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                    _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_psi_bwd_ex': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                       _vp, _vp, _vp, _vp, ctypes.c_long, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_det_fwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _vp, _vp, _vp, _vp,
+                    _vp, _vp, _vp, _vp, _vp],
+    'gpk_det_bwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _vp, _vp, _vp, _vp,
+                    _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_gram': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
+    'gpk_wsum': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
+    'gpk_gemm': [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_dbl, _vp, _c_int,
+                 ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp],
+    'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
+}
+
+_lib = None
+
+
+def lib():
+    """Load libgpk.so once (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f'{LIB_PATH} is missing: build it with `python -m geepee_gb300.build`')
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _c_int
+        L.gpk_last_error.restype = ctypes.c_char_p
+        L.gpk_last_error.argtypes = []
+        _lib = L
+    return _lib
+
+
+def declared_symbols():
+    return list(_SIGS) + ['gpk_last_error']
+
+
+class GpkError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__(f'{what}: status {code}: {lib().gpk_last_error().decode()}')
+        self.code = code
+
+
+def call(name, *args):
+    rc = getattr(lib(), name)(*args)
+    if rc != 0:
+        raise GpkError(rc, name)
+    return rc
+
+
+def ptr(t):
+    """Device pointer of a CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError('libgpk needs CUDA tensors')
+    if not t.is_contiguous():
+        raise ValueError('libgpk needs contiguous tensors')
+    return t.data_ptr()
+
+
+def stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def prec_of(dtype):
+    if dtype == torch.float64:
+        return GPK_DF64
+    if dtype == torch.float32:
+        return GPK_FP32
+    raise TypeError(f'unsupported dtype {dtype}')

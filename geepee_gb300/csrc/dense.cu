@@ -1,0 +1,310 @@
+// Small dense linear algebra for the M x M sparse-GP algebra (M <= 256), double-float.
+//   gpk_gemm      batched C = alpha op(A) op(B) + beta C
+//   gpk_chol_inv  batched SPD Cholesky + inverse + log-determinant (M <= 128, one CTA each)
+//   gpk_trace_kzz gradient of tr(M Kzz) w.r.t. log sf^2, log ell^2 and Z
+#include "common.cuh"
+
+namespace {
+
+constexpr int TB = 32;   // GEMM tile
+constexpr int TK = 16;   // GEMM k-chunk
+
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, int tA, int tB, double alpha,
+                                                   const typename Num<T>::store_t* A, int lda, long sA,
+                                                   const typename Num<T>::store_t* B, int ldb, long sB,
+                                                   double beta, typename Num<T>::store_t* C, int ldc, long sC) {
+  typedef typename Num<T>::store_t S;
+  __shared__ T As[TK][TB + 1];
+  __shared__ T Bs[TK][TB + 1];
+  const int bz = blockIdx.z;
+  A += bz * sA;
+  B += bz * sB;
+  C += bz * sC;
+  const int i0 = blockIdx.y * TB, j0 = blockIdx.x * TB;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 2 x 2 outputs each
+  T acc[2][2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) acc[r][c] = Num<T>::zero();
+  for (int k0 = 0; k0 < k; k0 += TK) {
+    for (int e = threadIdx.x; e < TK * TB; e += 256) {
+      int kk = e / TB, ii = e % TB;
+      int gi = i0 + ii, gk = k0 + kk;
+      T av = Num<T>::zero();
+      if (gi < m && gk < k) av = Num<T>::ld(tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk]);
+      As[kk][ii] = av;
+      int gj = j0 + ii;
+      T bv = Num<T>::zero();
+      if (gj < n && gk < k) bv = Num<T>::ld(tB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj]);
+      Bs[kk][ii] = bv;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < TK; ++kk) {
+      T a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
+      T b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
+      acc[0][0] = fma_(a0, b0, acc[0][0]);
+      acc[0][1] = fma_(a0, b1, acc[0][1]);
+      acc[1][0] = fma_(a1, b0, acc[1][0]);
+      acc[1][1] = fma_(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  const T al = Num<T>::ld(static_cast<S>(alpha));
+  const T be = Num<T>::ld(static_cast<S>(beta));
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      int gi = i0 + ty * 2 + r, gj = j0 + tx * 2 + c;
+      if (gi < m && gj < n) {
+        T v = mul(al, acc[r][c]);
+        if (beta != 0.0) v = fma_(be, Num<T>::ld(C[(size_t)gi * ldc + gj]), v);
+        C[(size_t)gi * ldc + gj] = Num<T>::st(v);
+      }
+    }
+}
+
+// ---- SPD Cholesky + inverse, one 1024-thread CTA per matrix, matrix in shared memory ----
+template <typename T>
+__global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Num<T>::store_t* A, long sA,
+                                                        typename Num<T>::store_t* Ainv, long sI,
+                                                        typename Num<T>::store_t* Lout, long sL, double* logdet,
+                                                        int* info) {
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  const int ld = M + 1;
+  T* S = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][M+1]
+  T* dg = S + M * ld;                                              // [M] diagonal of L
+  T* di = dg + M;                                                  // [M] 1/diag
+  T* tmp = di + M;                                                 // [M]
+  T* red = tmp + M;                                                // [32]
+  __shared__ int s_info;
+  const int b = blockIdx.x;
+  A += b * sA;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  load_exp_table(tab);
+  for (int e = tid; e < M * M; e += blockDim.x) {
+    int i = e / M, j = e % M;
+    S[i * ld + j] = Num<T>::ld(A[(size_t)i * M + j]);
+  }
+  if (tid == 0) s_info = 0;
+  __syncthreads();
+  // right-looking Cholesky on the lower triangle
+  for (int kk = 0; kk < M; ++kk) {
+    T piv = S[kk * ld + kk];
+    if (!(Num<T>::approx(piv) > 0.f)) {   // uniform: every thread read the same value
+      if (tid == 0) s_info = kk + 1;
+      break;
+    }
+    T d = sqrt_(piv);
+    T inv = recip(d);
+    if (tid == 0) {
+      dg[kk] = d;
+      di[kk] = inv;
+    }
+    for (int i = kk + 1 + tid; i < M; i += blockDim.x) S[i * ld + kk] = mul(S[i * ld + kk], inv);
+    __syncthreads();
+    for (int i = kk + 1 + ty; i < M; i += 32) {
+      T lik = S[i * ld + kk];
+      for (int j = kk + 1 + tx; j <= i; j += 32) S[i * ld + j] = sub(S[i * ld + j], mul(lik, S[j * ld + kk]));
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  int bad = s_info;
+  if (info && tid == 0) info[b] = bad;
+  if (bad) return;
+  if (Lout) {
+    Lout += b * sL;
+    for (int e = tid; e < M * M; e += blockDim.x) {
+      int i = e / M, j = e % M;
+      T v = i == j ? dg[i] : (i > j ? S[i * ld + j] : Num<T>::zero());
+      Lout[(size_t)i * M + j] = Num<T>::st(v);
+    }
+  }
+  if (logdet) {
+    T l = tid < M ? log_tab(dg[tid], tab) : Num<T>::zero();
+    l = warp_sum(l);
+    if (tx == 0) red[ty] = l;
+    __syncthreads();
+    if (ty == 0) {
+      T s = tx < 32 ? red[tx] : Num<T>::zero();
+      s = warp_sum(s);
+      if (tx == 0) logdet[b] = (double)Num<T>::st(scale2(s, 1));
+    }
+  }
+  if (!Ainv) return;
+  // in-place inverse of the unit-scaled lower factor, columns right to left:
+  //   X_jj = 1/L_jj,  X_ij = -X_jj sum_{k=j+1..i} X_ik L_kj   (i > j)
+  for (int j = M - 1; j >= 0; --j) {
+    for (int k = j + 1 + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + j];
+    __syncthreads();
+    // 8 threads per row
+    int i = j + 1 + (tid >> 3), sl = tid & 7;
+    T s = Num<T>::zero();
+    if (i < M)
+      for (int k = j + 1 + sl; k <= i; k += 8) s = fma_(S[i * ld + k], tmp[k], s);
+#pragma unroll
+    for (int m = 1; m < 8; m <<= 1) s = add(s, shfl_xor(s, m));
+    __syncthreads();
+    if (i < M && sl == 0) S[i * ld + j] = neg(mul(di[j], s));
+    if (tid == 0) S[j * ld + j] = di[j];
+    __syncthreads();
+  }
+  // Ainv = X^T X  (X lower): Ainv_ij = sum_{k >= max(i,j)} X_ki X_kj
+  Ainv += b * sI;
+  for (int e = tid; e < M * (M + 1) / 2; e += blockDim.x) {
+    int i = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+    if ((i + 1) * (i + 2) / 2 <= e) ++i;
+    if (i * (i + 1) / 2 > e) --i;
+    int j = e - i * (i + 1) / 2;   // j <= i
+    T s = Num<T>::zero();
+    for (int kk = i; kk < M; ++kk) s = fma_(S[kk * ld + i], S[kk * ld + j], s);
+    typename Num<T>::store_t v = Num<T>::st(s);
+    Ainv[(size_t)i * M + j] = v;
+    Ainv[(size_t)j * M + i] = v;
+  }
+}
+
+// gradient of tr(Mm Kzz), Kzz_ab = sf2 exp(-1/2 sum_q (z_aq - z_bq)^2 / l_q) (no jitter):
+//   d/dlog sf2 = sum_ab Mm_ab K_ab;  d/dlog l_q = 1/2 sum_ab Mm_ab K_ab (z_aq-z_bq)^2 / l_q
+//   d/dz_aq = sum_b (Mm_ab + Mm_ba) K_ab (z_bq - z_aq) / l_q
+// (geepee/kernels.py:447-475).  Results are ADDED, scaled: g_sf += s_sf * ., g_ls += s_ls * ., g_z += .
+template <typename T>
+__global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
+                                                        const typename Num<T>::store_t* Z, const double* lls2,
+                                                        const double* lsf2, double s_sf, double s_ls,
+                                                        double* g_sf, double* g_ls, double* g_z) {
+  typedef typename Num<T>::store_t S;
+  __shared__ float2 tab[256];
+  __shared__ T il[8], lsf;
+  __shared__ T red[8][9];
+  load_exp_table(tab);
+  __syncthreads();
+  if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
+  if (threadIdx.x == 0) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
+  __syncthreads();
+  T gs = Num<T>::zero();
+  T gl[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) gl[q] = Num<T>::zero();
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
+    T gz[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) gz[q] = Num<T>::zero();
+    for (int b = 0; b < M; ++b) {
+      T r = Num<T>::zero();
+      for (int q = 0; q < Q; ++q) {
+        T d = sub(Num<T>::ld(Z[a * Q + q]), Num<T>::ld(Z[b * Q + q]));
+        r = fma_(mul(d, d), il[q], r);
+      }
+      T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
+      T mab = Num<T>::ld(Mm[(size_t)a * M + b]);
+      T w = mul(mab, k);
+      T ws = mul(add(mab, Num<T>::ld(Mm[(size_t)b * M + a])), k);
+      gs = add(gs, w);
+      for (int q = 0; q < Q; ++q) {
+        T d = sub(Num<T>::ld(Z[b * Q + q]), Num<T>::ld(Z[a * Q + q]));
+        T dil = mul(d, il[q]);
+        gl[q] = fma_(mul(w, d), dil, gl[q]);
+        gz[q] = fma_(ws, dil, gz[q]);
+      }
+    }
+    for (int q = 0; q < Q; ++q) atomicAdd(&g_z[a * Q + q], (double)Num<T>::st(gz[q]));
+  }
+  // reduce gs and gl over the CTA
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T v[9];
+  v[0] = gs;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[1 + q] = gl[q];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    T s = warp_sum(v[i]);
+    if (lane == 0) red[warp][i] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 9; ++i) {
+      T s = red[0][i];
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = add(s, red[w][i]);
+      v[i] = s;
+    }
+    atomicAdd(g_sf, s_sf * (double)Num<T>::st(v[0]));
+    for (int q = 0; q < Q; ++q) atomicAdd(&g_ls[q], s_ls * 0.5 * (double)Num<T>::st(v[1 + q]));
+  }
+}
+
+template <typename T>
+int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
+                const void* B, int ldb, long sB, double beta, void* C, int ldc, long sC, cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  dim3 grid(gpk::ceil_div(n, TB), gpk::ceil_div(m, TB), batch);
+  gemm_kernel<T><<<grid, 256, 0, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB, beta,
+                                       (S*)C, ldc, sC);
+  return gpk::check_launch("gemm");
+}
+
+}  // namespace
+
+extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
+                        const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
+                        void* C, int ldc, long strideC, void* stream) {
+  GPK_REQUIRE(batch >= 0 && m >= 0 && n >= 0 && k >= 0, "gemm: negative size");
+  GPK_REQUIRE(batch <= 65535, "gemm: batch %d > 65535", batch);
+  GPK_REQUIRE(A && B && C, "gemm: null pointer");
+  GPK_REQUIRE(lda >= (transA ? m : k) && ldb >= (transB ? k : n) && ldc >= n, "gemm: bad leading dimension");
+  if (batch == 0 || m == 0 || n == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64)
+    return gemm_launch<df64>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc,
+                             strideC, st);
+  if (prec == GPK_FP32)
+    return gemm_launch<float>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc,
+                              strideC, st);
+  return gpk::fail(GPK_EINVAL, "gemm: unknown precision %d", prec);
+}
+
+extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
+                            void* stream) {
+  GPK_REQUIRE(batch >= 0 && M >= 1 && M <= 128, "chol_inv: M=%d outside [1,128]", M);
+  GPK_REQUIRE(A, "chol_inv: null input");
+  if (batch == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  long s = (long)M * M;
+  if (prec == GPK_DF64) {
+    size_t sm = 256 * 8 + ((size_t)M * (M + 1) + 3 * M + 32) * sizeof(df64);
+    auto k = chol_inv_kernel<df64>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<batch, 1024, sm, st>>>(M, (const double*)A, s, (double*)Ainv, s, (double*)L, s, logdet, info);
+  } else if (prec == GPK_FP32) {
+    size_t sm = 256 * 8 + ((size_t)M * (M + 1) + 3 * M + 32) * sizeof(float);
+    auto k = chol_inv_kernel<float>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<batch, 1024, sm, st>>>(M, (const float*)A, s, (float*)Ainv, s, (float*)L, s, logdet, info);
+  } else {
+    return gpk::fail(GPK_EINVAL, "chol_inv: unknown precision %d", prec);
+  }
+  return gpk::check_launch("chol_inv");
+}
+
+extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
+                             const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
+                             void* stream) {
+  GPK_REQUIRE(M >= 1 && Q >= 1 && Q <= 8, "trace_kzz: bad sizes M=%d Q=%d", M, Q);
+  GPK_REQUIRE(Mm && Z && lls2 && lsf2 && g_sf && g_ls && g_z, "trace_kzz: null pointer");
+  cudaStream_t st = gpk::as_stream(stream);
+  int grid = gpk::ceil_div(M, 128);
+  if (prec == GPK_DF64)
+    trace_kzz_kernel<df64><<<grid, 128, 0, st>>>(M, Q, (const double*)Mm, (const double*)Z, lls2, lsf2, s_sf, s_ls,
+                                                 g_sf, g_ls, g_z);
+  else if (prec == GPK_FP32)
+    trace_kzz_kernel<float><<<grid, 128, 0, st>>>(M, Q, (const float*)Mm, (const float*)Z, lls2, lsf2, s_sf, s_ls,
+                                                  g_sf, g_ls, g_z);
+  else
+    return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);
+  return gpk::check_launch("trace_kzz");
+}

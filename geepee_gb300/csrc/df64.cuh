@@ -1,0 +1,187 @@
+// Double-float ("df64") arithmetic on the FP32 pipes of sm_103a.
+//
+// A value is the unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving
+// about 48 significant bits.  GB300 issues FP32 FMAs at ~60x its FP64 rate, so the
+// error-free transformations below (Knuth two-sum, FMA two-product) buy FP64-class
+// accuracy for the ill-conditioned parts of the sparse-GP path at a fraction of the
+// cost of native double.  Algorithms: Dekker/Knuth error-free transforms and the
+// double-double scheme of Hida, Li & Bailey ("Algorithms for quad-double precision
+// floating point arithmetic", ARITH 2001), specialised to float pairs.
+//
+// The same kernels are instantiated for plain `float`; the overload set below lets
+// templated code be written once (add/mul/fma_/exp_/...).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+struct df64 {
+  float hi, lo;
+};
+
+__host__ __device__ __forceinline__ df64 make_df(float h, float l = 0.f) { df64 r; r.hi = h; r.lo = l; return r; }
+
+__device__ __forceinline__ df64 df_from_double(double x) {
+  float h = __double2float_rn(x);
+  float l = __double2float_rn(x - (double)h);
+  return make_df(h, l);
+}
+__device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+
+// ---- error-free transforms ----
+__device__ __forceinline__ df64 two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return make_df(s, e);
+}
+__device__ __forceinline__ df64 quick_two_sum(float a, float b) {  // |a| >= |b|
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return make_df(s, e);
+}
+__device__ __forceinline__ df64 two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  float e = __fmaf_rn(a, b, -p);
+  return make_df(p, e);
+}
+
+// ---- arithmetic ----
+// "sloppy" double-float add (Hida-Li-Bailey): error <= ~2^-47 (|a| + |b|), the same
+// shape of bound as an FP64 add; 11 FP32 ops.
+__device__ __forceinline__ df64 add(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 neg(df64 a) { return make_df(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 sub(df64 a, df64 b) { return add(a, neg(b)); }
+__device__ __forceinline__ df64 add(df64 a, float b) {
+  df64 s = two_sum(a.hi, b);
+  s.lo = __fadd_rn(s.lo, a.lo);
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 mul(df64 a, df64 b) {
+  df64 p = two_prod(a.hi, b.hi);
+  p.lo = __fmaf_rn(a.hi, b.lo, p.lo);
+  p.lo = __fmaf_rn(a.lo, b.hi, p.lo);
+  return quick_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df64 mul(df64 a, float b) {
+  df64 p = two_prod(a.hi, b);
+  p.lo = __fmaf_rn(a.lo, b, p.lo);
+  return quick_two_sum(p.hi, p.lo);
+}
+// a*b + c
+__device__ __forceinline__ df64 fma_(df64 a, df64 b, df64 c) { return add(mul(a, b), c); }
+__device__ __forceinline__ df64 scale2(df64 a, int e) { return make_df(ldexpf(a.hi, e), ldexpf(a.lo, e)); }
+
+__device__ __forceinline__ df64 div(df64 a, df64 b) {
+  float q1 = __fdiv_rn(a.hi, b.hi);
+  df64 r = sub(a, mul(b, q1));
+  float q2 = __fdiv_rn(r.hi, b.hi);
+  r = sub(r, mul(b, q2));
+  float q3 = __fdiv_rn(r.hi, b.hi);
+  df64 q = quick_two_sum(q1, q2);
+  return add(q, q3);
+}
+__device__ __forceinline__ df64 recip(df64 b) { return div(make_df(1.f), b); }
+
+// sqrt by one Newton correction of the float root: s + (a - s^2) / (2 s)
+__device__ __forceinline__ df64 sqrt_(df64 a) {
+  if (a.hi <= 0.f) return make_df(0.f);
+  float s = sqrtf(a.hi);
+  df64 r = sub(a, two_prod(s, s));
+  float c = __fdiv_rn(r.hi, 2.f * s);
+  return quick_two_sum(s, c);
+}
+
+// ---- exp: table-driven reduction x = k ln2/256 + r, |r| <= ln2/512 ----
+// Table T[j] = 2^(j/256) stored as df64 (exp2_table.cuh); copied into shared memory
+// once per CTA by load_exp_table().
+#define GPK_EXP_TABLE 256
+#include "exp2_table.cuh"
+
+// ln2/256 = 0.0027076061740622863 as a df64 (hi + lo exact to 3.4e-19)
+__device__ __forceinline__ df64 ln2_over_256() { return make_df(2.707606182e-03f, -7.440055516e-12f); }
+
+template <typename Tab>
+__device__ __forceinline__ df64 exp_tab(df64 x, const Tab& tab) {
+  if (x.hi < -103.0f) return make_df(0.f);
+  if (x.hi > 88.0f) return make_df(__int_as_float(0x7f800000), 0.f);
+  const float inv = 369.32993f;  // 256 / ln 2
+  float kf = rintf(x.hi * inv);
+  int k = (int)kf;
+  df64 r = sub(x, mul(ln2_over_256(), kf));
+  // exp(r) - 1 = r + r^2/2 + r^3/6 + r^4/24  (|r| < 1.4e-3; next term < 4e-17)
+  df64 r2 = mul(r, r);
+  float t = r.hi * r2.hi * (0.16666667f + r.hi * 0.041666668f);
+  df64 p = add(add(r, scale2(r2, -1)), t);
+  df64 e = add(p, 1.0f);
+  int j = k & (GPK_EXP_TABLE - 1);
+  int m = k >> 8;  // arithmetic shift: floor(k / 256)
+  float2 tj = tab[j];
+  df64 res = mul(make_df(tj.x, tj.y), e);
+  return scale2(res, m);
+}
+
+// log by one Newton step on exp: y1 = y0 + x exp(-y0) - 1
+template <typename Tab>
+__device__ __forceinline__ df64 log_tab(df64 x, const Tab& tab) {
+  float y0 = logf(x.hi);
+  df64 ey = exp_tab(make_df(-y0), tab);
+  df64 c = sub(mul(x, ey), make_df(1.f));
+  return add(make_df(y0), c);
+}
+
+// ---- warp reductions ----
+__device__ __forceinline__ df64 shfl_xor(df64 a, int m) {
+  return make_df(__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m));
+}
+__device__ __forceinline__ float shfl_xor(float a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+__device__ __forceinline__ df64 warp_sum(df64 a) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) a = add(a, shfl_xor(a, m));
+  return a;
+}
+__device__ __forceinline__ float warp_sum(float a) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) a += __shfl_xor_sync(0xffffffffu, a, m);
+  return a;
+}
+
+// ---- float overloads so templated kernels compile for T = float ----
+__device__ __forceinline__ float add(float a, float b) { return a + b; }
+__device__ __forceinline__ float sub(float a, float b) { return a - b; }
+__device__ __forceinline__ float mul(float a, float b) { return a * b; }
+__device__ __forceinline__ float neg(float a) { return -a; }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float recip(float b) { return __fdiv_rn(1.f, b); }
+__device__ __forceinline__ float sqrt_(float a) { return sqrtf(fmaxf(a, 0.f)); }
+__device__ __forceinline__ float scale2(float a, int e) { return ldexpf(a, e); }
+template <typename Tab> __device__ __forceinline__ float exp_tab(float x, const Tab&) { return expf(x); }
+template <typename Tab> __device__ __forceinline__ float log_tab(float x, const Tab&) { return logf(x); }
+
+// conversions between storage (double / float) and compute (df64 / float) types
+template <typename T> struct Num;
+template <> struct Num<df64> {
+  typedef double store_t;
+  __device__ static __forceinline__ df64 ld(double x) { return df_from_double(x); }
+  __device__ static __forceinline__ double st(df64 x) { return df_to_double(x); }
+  __device__ static __forceinline__ df64 c(float x) { return make_df(x); }
+  __device__ static __forceinline__ df64 zero() { return make_df(0.f); }
+  __device__ static __forceinline__ float approx(df64 x) { return x.hi; }
+};
+template <> struct Num<float> {
+  typedef float store_t;
+  __device__ static __forceinline__ float ld(float x) { return x; }
+  __device__ static __forceinline__ float st(float x) { return x; }
+  __device__ static __forceinline__ float c(float x) { return x; }
+  __device__ static __forceinline__ float zero() { return 0.f; }
+  __device__ static __forceinline__ float approx(float x) { return x; }
+};
+
+// the exp table lives in shared memory; every kernel that calls exp_tab loads it first
+__device__ __forceinline__ void load_exp_table(float2* s_tab) {
+  for (int i = threadIdx.x; i < GPK_EXP_TABLE; i += blockDim.x) s_tab[i] = kExp2Tab[i];
+}

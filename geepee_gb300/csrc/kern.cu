@@ -1,0 +1,463 @@
+// ARD exponentiated-quadratic kernel matrices and the deterministic-input sparse-GP
+// layer (first DGP layer / SGPR): fused forward contractions and the per-row backward.
+#include "common.cuh"
+
+namespace {
+
+constexpr int DMAXK = 64;   // max input dimension
+constexpr int DO_MAX = 4;   // max output dimension of a layer
+constexpr int RR = 4;       // rows per CTA pass in the layer kernels
+
+template <typename T>
+struct Hyp {
+  T inv_l2[DMAXK];   // 1/ell^2
+  T lsf;             // log sf^2
+  T sf2;
+};
+
+template <typename T>
+__device__ void load_hyp(Hyp<T>& h, const double* lls2, const double* lsf2, int D, const float2* tab) {
+  typedef typename Num<T>::store_t S;
+  for (int d = threadIdx.x; d < D; d += blockDim.x)
+    h.inv_l2[d] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[d]))), tab);
+  if (threadIdx.x == 0) {
+    h.lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
+    h.sf2 = exp_tab(h.lsf, tab);
+  }
+}
+
+// K[n,m] = exp(lsf - 1/2 sum_d (x-z)^2 / l_d) (+ jitter on the diagonal)
+template <typename T>
+__global__ void __launch_bounds__(256) kern_matrix_kernel(int N, int M, int D, const typename Num<T>::store_t* x,
+                                                          int ldx, const typename Num<T>::store_t* z, int ldz,
+                                                          const double* lls2, const double* lsf2, double jitter,
+                                                          typename Num<T>::store_t* K, int ldk) {
+  __shared__ float2 tab[256];
+  __shared__ Hyp<T> h;
+  load_exp_table(tab);
+  __syncthreads();
+  load_hyp(h, lls2, lsf2, D, tab);
+  __syncthreads();
+  int m = blockIdx.x * 32 + threadIdx.x;
+  int n = blockIdx.y * 8 + threadIdx.y;
+  if (m >= M || n >= N) return;
+  T r = Num<T>::zero();
+  for (int d = 0; d < D; ++d) {
+    T df = sub(Num<T>::ld(x[(size_t)n * ldx + d]), Num<T>::ld(z[(size_t)m * ldz + d]));
+    r = fma_(mul(df, df), h.inv_l2[d], r);
+  }
+  T k = exp_tab(sub(h.lsf, scale2(r, -1)), tab);
+  if (jitter != 0.0 && n == m) k = add(k, Num<T>::ld(static_cast<typename Num<T>::store_t>(jitter)));
+  K[(size_t)n * ldk + m] = Num<T>::st(k);
+}
+
+// Deterministic-input layer forward for rows n:
+//   k_n = K(x_n, Z);  m_nd = k_n . A_d;  Bk_ndb = sum_a B_d[a,b] k_na;  v_nd = sf2 + k_n . Bk_nd
+// (geepee/aep_models.py:142-158, base_models.py:265-284).
+template <typename T>
+__global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int Dout,
+                                                      const typename Num<T>::store_t* x, int ldx,
+                                                      const typename Num<T>::store_t* z, const double* lls2,
+                                                      const double* lsf2, const typename Num<T>::store_t* A,
+                                                      const typename Num<T>::store_t* B,
+                                                      typename Num<T>::store_t* kfu,
+                                                      typename Num<T>::store_t* Bk,
+                                                      typename Num<T>::store_t* m_out,
+                                                      typename Num<T>::store_t* v_out) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
+  T* kr = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [RR][M]
+  T* red = kr + RR * M;                                                              // [32][64]
+  load_exp_table(tab);
+  __syncthreads();
+  load_hyp(*h, lls2, lsf2, D, tab);
+  __syncthreads();
+  for (int n0 = blockIdx.x * RR; n0 < N; n0 += gridDim.x * RR) {
+    for (int i = threadIdx.x; i < RR * M; i += blockDim.x) {
+      int r = i / M, mm = i % M, n = n0 + r;
+      T k = Num<T>::zero();
+      if (n < N) {
+        T rr = Num<T>::zero();
+        for (int d = 0; d < D; ++d) {
+          T df = sub(Num<T>::ld(x[(size_t)n * ldx + d]), Num<T>::ld(z[(size_t)mm * D + d]));
+          rr = fma_(mul(df, df), h->inv_l2[d], rr);
+        }
+        k = exp_tab(sub(h->lsf, scale2(rr, -1)), tab);
+        if (kfu) kfu[(size_t)n * M + mm] = Num<T>::st(k);
+      }
+      kr[i] = k;
+    }
+    __syncthreads();
+    T vals[2 * DO_MAX * RR];
+#pragma unroll
+    for (int i = 0; i < 2 * DO_MAX * RR; ++i) vals[i] = Num<T>::zero();
+    for (int b = threadIdx.x; b < M; b += blockDim.x) {
+      for (int d = 0; d < Dout; ++d) {
+        const S* Bd = B + (size_t)d * M * M;
+        T acc[RR];
+#pragma unroll
+        for (int r = 0; r < RR; ++r) acc[r] = Num<T>::zero();
+        for (int a = 0; a < M; ++a) {
+          T bab = Num<T>::ld(Bd[(size_t)a * M + b]);
+#pragma unroll
+          for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
+        }
+        T ad = Num<T>::ld(A[(size_t)d * M + b]);
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+          int n = n0 + r;
+          if (n < N && Bk) Bk[((size_t)n * Dout + d) * M + b] = Num<T>::st(acc[r]);
+          T kb = kr[r * M + b];
+          vals[(r * DO_MAX + d) * 2] = fma_(kb, ad, vals[(r * DO_MAX + d) * 2]);
+          vals[(r * DO_MAX + d) * 2 + 1] = fma_(kb, acc[r], vals[(r * DO_MAX + d) * 2 + 1]);
+        }
+      }
+    }
+    // CTA reduction of RR*Dout*(m, v) values
+    {
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      const int K = 2 * DO_MAX * RR;
+      for (int i = 0; i < K; ++i) {
+        T s = warp_sum(vals[i]);
+        if (lane == 0) red[warp * 64 + i] = s;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        for (int i = 0; i < K; ++i) {
+          T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
+          s = warp_sum(s);
+          if (lane == 0) red[32 * 64 + i] = s;
+        }
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < RR * Dout; i += blockDim.x) {
+        int r = i / Dout, d = i % Dout, n = n0 + r;
+        if (n < N) {
+          T mm = red[32 * 64 + (r * DO_MAX + d) * 2];
+          T vv = add(h->sf2, red[32 * 64 + (r * DO_MAX + d) * 2 + 1]);
+          if (m_out) m_out[(size_t)n * Dout + d] = Num<T>::st(mm);
+          if (v_out) v_out[(size_t)n * Dout + d] = Num<T>::st(vv);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Deterministic-input layer backward, per row (geepee/aep_models.py:451-460 with
+// kfucompDer, kernels.py:381-399):
+//   dkfu_nb = sum_d dm_nd A_db + 2 sum_d dv_nd Bk_ndb,   L_nb = dkfu_nb kfu_nb
+//   dsf2 += sum L / sf2;  dl_q += sum L (x-z)^2 / l^{3/2};  dZ_bq += sum_n L (x_nq - z_bq)/l_q
+//   dA_db += sum_n dm_nd kfu_nb;   dx_nq = -sum_b L_nb (x_nq - z_bq)/l_q   (optional)
+template <typename T>
+__global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int Dout,
+                                                      const typename Num<T>::store_t* x, int ldx,
+                                                      const typename Num<T>::store_t* z, const double* lls2,
+                                                      const double* lsf2, const typename Num<T>::store_t* A,
+                                                      const typename Num<T>::store_t* kfu,
+                                                      const typename Num<T>::store_t* Bk,
+                                                      const typename Num<T>::store_t* dm,
+                                                      const typename Num<T>::store_t* dv,
+                                                      const typename Num<T>::store_t* dkfu, double* dsf2,
+                                                      double* dl, double* dZ, double* dA,
+                                                      typename Num<T>::store_t* dx) {
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
+  T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));  // [D]
+  T* red = xs + DMAXK;                                                                // [32][64]
+  load_exp_table(tab);
+  __syncthreads();
+  load_hyp(*h, lls2, lsf2, D, tab);
+  __syncthreads();
+  const int b = threadIdx.x;  // one pseudo-input per thread (M <= blockDim)
+  T gsf = Num<T>::zero();
+  T gl[16];
+  T gz[16];
+  T ga[DO_MAX];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) gl[q] = gz[q] = Num<T>::zero();
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d) ga[d] = Num<T>::zero();
+  for (int n = blockIdx.x; n < N; n += gridDim.x) {
+    for (int d = threadIdx.x; d < D; d += blockDim.x) xs[d] = Num<T>::ld(x[(size_t)n * ldx + d]);
+    __syncthreads();
+    T L = Num<T>::zero();
+    if (b < M) {
+      T k = Num<T>::ld(kfu[(size_t)n * M + b]);
+      T g = Num<T>::zero();
+      if (dkfu) {
+        g = Num<T>::ld(dkfu[(size_t)n * M + b]);
+      } else {
+        for (int d = 0; d < Dout; ++d) {
+          T dmd = Num<T>::ld(dm[(size_t)n * Dout + d]);
+          T dvd = Num<T>::ld(dv[(size_t)n * Dout + d]);
+          g = fma_(dmd, Num<T>::ld(A[(size_t)d * M + b]), g);
+          g = fma_(scale2(dvd, 1), Num<T>::ld(Bk[((size_t)n * Dout + d) * M + b]), g);
+          if (d < DO_MAX) ga[d] = fma_(dmd, k, ga[d]);
+        }
+      }
+      L = mul(g, k);
+      gsf = add(gsf, L);
+      for (int q = 0; q < D && q < 16; ++q) {
+        T df = sub(xs[q], Num<T>::ld(z[(size_t)b * D + q]));
+        T t = mul(L, df);
+        gz[q] = fma_(t, h->inv_l2[q], gz[q]);
+        gl[q] = fma_(t, df, gl[q]);
+      }
+    }
+    if (dx) {
+      // dx_nq = -sum_b L (x - z)/l : CTA reduction per dimension
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      for (int q = 0; q < D; ++q) {
+        T t = Num<T>::zero();
+        if (b < M) t = mul(L, mul(sub(xs[q], Num<T>::ld(z[(size_t)b * D + q])), h->inv_l2[q]));
+        t = warp_sum(t);
+        if (lane == 0) red[warp * 64 + (q & 63)] = t;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        for (int q = 0; q < D; ++q) {
+          T s = lane < nw ? red[lane * 64 + q] : Num<T>::zero();
+          s = warp_sum(s);
+          if (lane == 0) dx[(size_t)n * D + q] = Num<T>::st(neg(s));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (b < M) {
+    for (int q = 0; q < D && q < 16; ++q) atomicAdd(&dZ[(size_t)b * D + q], (double)Num<T>::st(gz[q]));
+    if (dA && !dkfu)
+      for (int d = 0; d < Dout && d < DO_MAX; ++d) atomicAdd(&dA[(size_t)d * M + b], (double)Num<T>::st(ga[d]));
+  }
+  // dsf2 and dl: CTA reductions
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T vals[17];
+  vals[0] = gsf;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) vals[1 + q] = gl[q];
+  for (int i = 0; i < 17; ++i) {
+    T s = warp_sum(vals[i]);
+    if (lane == 0) red[warp * 64 + i] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    for (int i = 0; i < 17; ++i) {
+      T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
+      vals[i] = warp_sum(s);
+    }
+    if (lane == 0) {
+      atomicAdd(dsf2, (double)Num<T>::st(div(vals[0], h->sf2)));
+      for (int q = 0; q < D && q < 16; ++q) {
+        // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
+        T il = h->inv_l2[q];
+        atomicAdd(&dl[q], (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il)))));
+      }
+    }
+  }
+}
+
+// Weighted Gram reduction:  C[d] += sum_n w[n,d] u_n v_n^T  (u, v: [N,M] rows; C: [Dout,M,M] f64)
+// 32x32 output tile per CTA, n split across gridDim.z.  (The dBhat / dSucav einsums of
+// geepee/aep_models.py:463-464, 490-493.)
+template <typename T>
+__global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
+                                                   const typename Num<T>::store_t* v,
+                                                   const typename Num<T>::store_t* w, double* C, int nchunk) {
+  __shared__ T su[32], sv[32], sw[DO_MAX];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of threads, 4 outputs each
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  T acc[DO_MAX][4];
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[d][r] = Num<T>::zero();
+  int nbeg = (int)((long)N * blockIdx.z / gridDim.z), nend = (int)((long)N * (blockIdx.z + 1) / gridDim.z);
+  for (int n = nbeg; n < nend; ++n) {
+    if (threadIdx.x < 32) {
+      int i = i0 + threadIdx.x;
+      su[threadIdx.x] = i < M ? Num<T>::ld(u[(size_t)n * M + i]) : Num<T>::zero();
+    } else if (threadIdx.x < 64) {
+      int j = j0 + threadIdx.x - 32;
+      sv[threadIdx.x - 32] = j < M ? Num<T>::ld(v[(size_t)n * M + j]) : Num<T>::zero();
+    } else if (threadIdx.x < 64 + Dout) {
+      sw[threadIdx.x - 64] = Num<T>::ld(w[(size_t)n * Dout + threadIdx.x - 64]);
+    }
+    __syncthreads();
+    T vj = sv[tx];
+#pragma unroll
+    for (int d = 0; d < DO_MAX; ++d) {
+      if (d < Dout) {
+        T wv = mul(sw[d], vj);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[d][r] = fma_(su[ty * 4 + r], wv, acc[d][r]);
+      }
+    }
+    __syncthreads();
+  }
+  (void)nchunk;
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d) {
+    if (d < Dout) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        int i = i0 + ty * 4 + r, j = j0 + tx;
+        if (i < M && j < M) atomicAdd(&C[((size_t)d * M + i) * M + j], (double)Num<T>::st(acc[d][r]));
+      }
+    }
+  }
+}
+
+// c[d] += sum_n w[n,d] u_n   (u: [N,M]; c: [Dout,M] f64)
+template <typename T>
+__global__ void __launch_bounds__(256) wsum_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
+                                                   const typename Num<T>::store_t* w, double* c) {
+  const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int part = threadIdx.x >> 5;  // 8 n-partitions per CTA
+  __shared__ T red[8][32][DO_MAX];
+  T acc[DO_MAX];
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d) acc[d] = Num<T>::zero();
+  if (j < M) {
+    for (int n = blockIdx.y * 8 + part; n < N; n += gridDim.y * 8) {
+      T uv = Num<T>::ld(u[(size_t)n * M + j]);
+      for (int d = 0; d < Dout && d < DO_MAX; ++d) acc[d] = fma_(Num<T>::ld(w[(size_t)n * Dout + d]), uv, acc[d]);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d) red[part][threadIdx.x & 31][d] = acc[d];
+  __syncthreads();
+  if (part == 0 && j < M) {
+    for (int d = 0; d < Dout && d < DO_MAX; ++d) {
+      T s = red[0][threadIdx.x][d];
+      for (int p = 1; p < 8; ++p) s = add(s, red[p][threadIdx.x][d]);
+      atomicAdd(&c[(size_t)d * M + j], (double)Num<T>::st(s));
+    }
+  }
+}
+
+size_t det_fwd_smem(int M, size_t tsz) { return 256 * 8 + sizeof(Hyp<df64>) + (RR * M + 33 * 64) * tsz; }
+size_t det_bwd_smem(size_t tsz) { return 256 * 8 + sizeof(Hyp<df64>) + (DMAXK + 32 * 64) * tsz; }
+
+template <typename T>
+int kern_launch(int N, int M, int D, const void* x, int ldx, const void* z, int ldz, const double* lls2,
+                const double* lsf2, double jitter, void* K, int ldk, cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  dim3 grid(gpk::ceil_div(M, 32), gpk::ceil_div(N, 8));
+  kern_matrix_kernel<T><<<grid, dim3(32, 8), 0, st>>>(N, M, D, (const S*)x, ldx, (const S*)z, ldz, lls2, lsf2,
+                                                    jitter, (S*)K, ldk);
+  return gpk::check_launch("kern");
+}
+
+}  // namespace
+
+extern "C" int gpk_kern(int prec, int N, int M, int D, const void* x, int ldx, const void* z, int ldz,
+                        const double* lls2, const double* lsf2, double jitter, void* K, int ldk, void* stream) {
+  GPK_REQUIRE(N >= 0 && M >= 0 && D >= 1 && D <= DMAXK, "kern: bad sizes N=%d M=%d D=%d", N, M, D);
+  GPK_REQUIRE(x && z && lls2 && lsf2 && K, "kern: null pointer");
+  GPK_REQUIRE(ldx >= D && ldz >= D && ldk >= M, "kern: bad leading dimension");
+  if (N == 0 || M == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64) return kern_launch<df64>(N, M, D, x, ldx, z, ldz, lls2, lsf2, jitter, K, ldk, st);
+  if (prec == GPK_FP32) return kern_launch<float>(N, M, D, x, ldx, z, ldz, lls2, lsf2, jitter, K, ldk, st);
+  return gpk::fail(GPK_EINVAL, "kern: unknown precision %d", prec);
+}
+
+extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                           const double* lls2, const double* lsf2, const void* A, const void* B, void* kfu,
+                           void* Bk, void* m_out, void* v_out, void* stream) {
+  GPK_REQUIRE(N >= 0 && M >= 1 && M <= 1024 && D >= 1 && D <= DMAXK, "det_fwd: bad sizes N=%d M=%d D=%d", N, M, D);
+  GPK_REQUIRE(Dout >= 1 && Dout <= DO_MAX, "det_fwd: Dout=%d outside [1,%d]", Dout, DO_MAX);
+  GPK_REQUIRE(x && Z && lls2 && lsf2 && A && B, "det_fwd: null input");
+  if (N == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  int grid = gpk::ceil_div(N, RR);
+  int cap = gpk::sm_count() * 4;
+  if (grid > cap) grid = cap;
+  if (prec == GPK_DF64) {
+    size_t sm = det_fwd_smem(M, sizeof(df64));
+    auto k = det_fwd_kernel<df64>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
+                             (const double*)A, (const double*)B, (double*)kfu, (double*)Bk, (double*)m_out,
+                             (double*)v_out);
+  } else if (prec == GPK_FP32) {
+    size_t sm = det_fwd_smem(M, sizeof(float));
+    auto k = det_fwd_kernel<float>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
+                             (const float*)B, (float*)kfu, (float*)Bk, (float*)m_out, (float*)v_out);
+  } else {
+    return gpk::fail(GPK_EINVAL, "det_fwd: unknown precision %d", prec);
+  }
+  return gpk::check_launch("det_fwd");
+}
+
+extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                           const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
+                           const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
+                           double* dA, void* dx, void* stream) {
+  GPK_REQUIRE(N >= 0 && M >= 1 && M <= 256 && D >= 1 && D <= 16, "det_bwd: bad sizes N=%d M=%d D=%d (M<=256, D<=16)", N, M, D);
+  GPK_REQUIRE(dkfu || (Dout >= 1 && Dout <= DO_MAX), "det_bwd: Dout=%d outside [1,%d]", Dout, DO_MAX);
+  GPK_REQUIRE(x && Z && lls2 && lsf2 && kfu && dsf2 && dl && dZ, "det_bwd: null");
+  GPK_REQUIRE(dkfu || (A && Bk && dm && dv), "det_bwd: need dkfu or (A, Bk, dm, dv)");
+  if (N == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  int threads = M <= 128 ? 128 : 256;
+  int grid = N < gpk::sm_count() * 2 ? N : gpk::sm_count() * 2;
+  size_t smd = det_bwd_smem(sizeof(df64)), smf = det_bwd_smem(sizeof(float));
+  if (prec == GPK_DF64) {
+    det_bwd_kernel<df64><<<grid, threads, smd, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2,
+                                                     lsf2, (const double*)A, (const double*)kfu,
+                                                     (const double*)Bk, (const double*)dm, (const double*)dv, (const double*)dkfu, dsf2,
+                                                     dl, dZ, dA, (double*)dx);
+  } else if (prec == GPK_FP32) {
+    det_bwd_kernel<float><<<grid, threads, smf, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2,
+                                                      lsf2, (const float*)A, (const float*)kfu, (const float*)Bk,
+                                                      (const float*)dm, (const float*)dv, (const float*)dkfu, dsf2, dl, dZ, dA,
+                                                      (float*)dx);
+  } else {
+    return gpk::fail(GPK_EINVAL, "det_bwd: unknown precision %d", prec);
+  }
+  return gpk::check_launch("det_bwd");
+}
+
+extern "C" int gpk_gram(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
+                        void* stream) {
+  GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1 && Dout <= DO_MAX, "gram: bad sizes");
+  GPK_REQUIRE(u && v && w && C, "gram: null pointer");
+  if (N == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  int tiles = gpk::ceil_div(M, 32) * gpk::ceil_div(M, 32);
+  int chunks = gpk::ceil_div(gpk::sm_count() * 2, tiles);
+  if (chunks > gpk::ceil_div(N, 16)) chunks = gpk::ceil_div(N, 16);
+  if (chunks < 1) chunks = 1;
+  dim3 grid(gpk::ceil_div(M, 32), gpk::ceil_div(M, 32), chunks);
+  if (prec == GPK_DF64)
+    gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C, chunks);
+  else if (prec == GPK_FP32)
+    gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C, chunks);
+  else
+    return gpk::fail(GPK_EINVAL, "gram: unknown precision %d", prec);
+  return gpk::check_launch("gram");
+}
+
+extern "C" int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const void* w, double* c, void* stream) {
+  GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1 && Dout <= DO_MAX, "wsum: bad sizes");
+  GPK_REQUIRE(u && w && c, "wsum: null pointer");
+  if (N == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  int gy = gpk::ceil_div(N, 256);
+  if (gy > 64) gy = 64;
+  dim3 grid(gpk::ceil_div(M, 32), gy);
+  if (prec == GPK_DF64)
+    wsum_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)w, c);
+  else if (prec == GPK_FP32)
+    wsum_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)w, c);
+  else
+    return gpk::fail(GPK_EINVAL, "wsum: unknown precision %d", prec);
+  return gpk::check_launch("wsum");
+}

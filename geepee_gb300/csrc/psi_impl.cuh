@@ -1,0 +1,613 @@
+// Psi statistics of the ARD kernel under Gaussian inputs, fused with the
+// moment-matching contractions of a sparse-GP layer, and their backward pass.
+//
+// Work decomposition (both kernels): a CTA walks a strided sequence of data points
+// n; for each point its threads first build per-point tables in shared memory
+// (per-dimension constants, per-pseudo-input terms u_a, h_aq), then sweep the
+// M(M+1)/2 unordered pairs (a <= b) of pseudo-inputs.  Each thread owns a fixed set of
+// pairs (p = tid + k*blockDim) across all of its points, so sums over n of per-pair
+// quantities (sum_n psi2, dB = sum_n dv psi2) stay in registers until one atomic
+// flush per CTA.  psi2 per point is never materialised in HBM (unless requested).
+//
+// log psi2[n,a,b] = u_a + u_b + G_ab - sum_q h_aq z_bq   with
+//   G_ab = -sum_q (z_aq - z_bq)^2 / (4 l_q)                      (per call)
+//   u_a  = k_n/2 + sum_q c_q z_aq (mu_q - z_aq/4),  h_aq = c_q z_aq / 2   (per point)
+//   k_n  = 2 log sf2 + 1/2 sum_q log(l_q / (l_q + 2 S_q)) - sum_q c_q mu_q^2,
+//   c_q  = 1 / (l_q + 2 S_q)
+// which is the reference's exponent (geepee/kernels.py:219-225) regrouped so that the
+// inner loop costs Q multiply-adds plus one exp.
+#pragma once
+#include "common.cuh"
+
+namespace psi_impl {
+
+constexpr int QMAX = 8;
+constexpr int DMAX = 4;
+constexpr int NT = 512;        // threads per CTA
+constexpr int PPT_MAX = 16;    // pairs per thread for register-resident per-pair sums
+
+template <typename S>
+struct PsiArgs {
+  int N, M, Q, Dout;
+  const S* mu;
+  const S* var;
+  const S* Z;
+  const double* lls2;
+  const double* lsf2;
+  const S* A;
+  const S* B;
+  S* psi1;
+  S* psi2;
+  double* psi2_sum;
+  S* m_out;
+  S* v_out;
+  const S* m;
+  const S* dm;
+  const S* dv;
+  const S* dpsi1;    // optional [N,M]: replaces dm_all A
+  long b_stride;     // != 0: B is per point (B + n*b_stride), dv treated as 1
+  double* dsf2;
+  double* dl;
+  double* dZ;
+  double* dA;
+  double* dB;
+  S* dmu;
+  S* dvar;
+};
+
+__device__ __forceinline__ void pair_of(int p, int& a, int& b) {
+  // row-major lower triangle: p = a(a+1)/2 + b, 0 <= b <= a
+  int r = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
+  if ((r + 1) * (r + 2) / 2 <= p) ++r;
+  if (r * (r + 1) / 2 > p) --r;
+  a = r;
+  b = p - r * (r + 1) / 2;
+}
+
+template <typename T>
+struct Smem {
+  float2* tab;   // [256]
+  T* z;          // [M*Q]
+  T* ell2;       // [Q]
+  T* lnl;        // [Q]   log ell2
+  T* inv4l;      // [Q]   1/(4 ell2)
+  T* misc;       // [4]   log sf2, sf2, ...
+  T* pmu;        // [Q]   per point
+  T* pis1;       // [Q]   1/(l+S)
+  T* pc;         // [Q]   1/(l+2S)
+  T* pld1;       // [Q]   1/2 log(l/(l+S))
+  T* pld2;       // [Q]   1/2 log(l/(l+2S))
+  T* pd;         // [2*DMAX] per-point dm_all, dv
+  T* u;          // [M]
+  T* h;          // [M*Q]
+  T* ps1;        // [M]
+  T* G;          // [P]
+  T* red;        // [32 * 64]
+  T* L;          // [P]   (backward only)
+  T* rows;       // [M*(1+Q)] row statistics (backward only)
+};
+
+template <typename T>
+__device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd) {
+  Smem<T> s;
+  s.tab = reinterpret_cast<float2*>(base);
+  T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
+  s.z = t; t += M * Q;
+  s.ell2 = t; t += QMAX;
+  s.lnl = t; t += QMAX;
+  s.inv4l = t; t += QMAX;
+  s.misc = t; t += 4;
+  s.pmu = t; t += QMAX;
+  s.pis1 = t; t += QMAX;
+  s.pc = t; t += QMAX;
+  s.pld1 = t; t += QMAX;
+  s.pld2 = t; t += QMAX;
+  s.pd = t; t += 2 * DMAX;
+  s.u = t; t += M;
+  s.h = t; t += M * Q;
+  s.ps1 = t; t += M;
+  s.G = t; t += P;
+  s.red = t; t += 32 * 64;
+  if (bwd) {
+    s.L = t; t += P;
+    s.rows = t; t += M * (1 + QMAX);
+  } else {
+    s.L = nullptr;
+    s.rows = nullptr;
+  }
+  return s;
+}
+
+__host__ __device__ inline size_t smem_bytes(int M, int Q, int P, bool bwd, size_t tsz) {
+  size_t n = (size_t)M * Q + 5 * QMAX + 4 + 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + M + P + 32 * 64;
+  if (bwd) n += P + (size_t)M * (1 + QMAX);
+  return 256 * 8 + n * tsz;
+}
+
+// CTA-wide sum of K values per thread (K <= 64); result valid in thread 0.
+template <typename T>
+__device__ __forceinline__ void block_sum(T* vals, int K, T* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = 0; i < K; ++i) {
+    T s = warp_sum(vals[i]);
+    if (lane == 0) red[warp * 64 + i] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    for (int i = 0; i < K; ++i) {
+      T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
+      vals[i] = warp_sum(s);
+    }
+  }
+}
+
+// common per-CTA setup: exp table, Z, lengthscales, signal variance, G table
+template <typename T, typename S>
+__device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
+  const int M = a.M, Q = a.Q;
+  load_exp_table(s.tab);
+  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) s.z[i] = Num<T>::ld(a.Z[i]);
+  __syncthreads();
+  if (threadIdx.x < Q) {
+    int q = threadIdx.x;
+    T lnl = Num<T>::ld(static_cast<S>(a.lls2[q]));
+    T l2 = exp_tab(lnl, s.tab);
+    s.lnl[q] = lnl;
+    s.ell2[q] = l2;
+    s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
+  }
+  if (threadIdx.x == 32) {
+    T lsf = Num<T>::ld(static_cast<S>(a.lsf2[0]));
+    s.misc[0] = lsf;
+    s.misc[1] = exp_tab(lsf, s.tab);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    int ia, ib;
+    pair_of(p, ia, ib);
+    T g = Num<T>::zero();
+    for (int q = 0; q < Q; ++q) {
+      T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
+      g = fma_(mul(d, d), s.inv4l[q], g);
+    }
+    s.G[p] = neg(g);
+  }
+}
+
+// per-point constants for dimension q (threads q < Q)
+template <typename T, typename S>
+__device__ __forceinline__ void point_dims(const PsiArgs<S>& a, Smem<T>& s, int n) {
+  if (threadIdx.x < a.Q) {
+    int q = threadIdx.x;
+    T mu = Num<T>::ld(a.mu[(size_t)n * a.Q + q]);
+    T var = Num<T>::ld(a.var[(size_t)n * a.Q + q]);
+    T s1 = add(s.ell2[q], var);
+    T s2 = add(s.ell2[q], add(var, var));
+    s.pmu[q] = mu;
+    s.pis1[q] = recip(s1);
+    s.pc[q] = recip(s2);
+    s.pld1[q] = scale2(sub(s.lnl[q], log_tab(s1, s.tab)), -1);
+    s.pld2[q] = scale2(sub(s.lnl[q], log_tab(s2, s.tab)), -1);
+  }
+}
+
+// per-pseudo-input terms for point n: psi1_a, u_a, h_aq (threads over a)
+template <typename T>
+__device__ __forceinline__ T point_rows(Smem<T>& s, int M, int Q, int ia) {
+  const T lsf = s.misc[0];
+  T e1 = lsf;
+  T kap = add(lsf, lsf);
+  for (int q = 0; q < Q; ++q) {
+    T d = sub(s.pmu[q], s.z[ia * Q + q]);
+    e1 = add(e1, sub(s.pld1[q], scale2(mul(mul(d, d), s.pis1[q]), -1)));
+    kap = add(kap, sub(s.pld2[q], mul(mul(s.pmu[q], s.pmu[q]), s.pc[q])));
+  }
+  T u = scale2(kap, -1);
+  for (int q = 0; q < Q; ++q) {
+    T zq = s.z[ia * Q + q];
+    T czq = mul(s.pc[q], zq);
+    u = add(u, mul(czq, sub(s.pmu[q], scale2(zq, -2))));
+    s.h[ia * Q + q] = scale2(czq, -1);
+  }
+  s.u[ia] = u;
+  T p1 = exp_tab(e1, s.tab);
+  s.ps1[ia] = p1;
+  return p1;
+}
+
+template <typename T>
+__device__ __forceinline__ T pair_psi2(const Smem<T>& s, int Q, int p, int ia, int ib) {
+  T x = add(add(s.u[ia], s.u[ib]), s.G[p]);
+  T cr = Num<T>::zero();
+  for (int q = 0; q < Q; ++q) cr = fma_(s.h[ia * Q + q], s.z[ib * Q + q], cr);
+  return exp_tab(sub(x, cr), s.tab);
+}
+
+// ---------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a, const Smem<T>& s, int n,
+                                      int p, bool contract, T* vals) {
+  typedef typename Num<T>::store_t S;
+  const int M = a.M;
+  int ia, ib;
+  pair_of(p, ia, ib);
+  T ps = pair_psi2(s, a.Q, p, ia, ib);
+  if (a.psi2) {
+    S v = Num<T>::st(ps);
+    a.psi2[((size_t)n * M + ia) * M + ib] = v;
+    a.psi2[((size_t)n * M + ib) * M + ia] = v;
+  }
+  if (contract) {
+    for (int d = 0; d < a.Dout; ++d) {
+      const S* Bd = a.B + (size_t)d * M * M;
+      T w = Num<T>::ld(Bd[ia * M + ib]);
+      if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+      vals[DMAX + d] = fma_(w, ps, vals[DMAX + d]);
+    }
+  }
+  return ps;
+}
+
+// PPT > 0: each thread owns pairs tid + k*NT (k < PPT) and keeps sum_n psi2 in registers.
+// PPT == 0: plain strided sweep over any number of pairs (no psi2_sum).
+template <typename T, int PPT>
+__global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  const int M = a.M, Q = a.Q, D = a.Dout;
+  const int P = M * (M + 1) / 2;
+  Smem<T> s = carve<T>(smem_raw, M, Q, P, false);
+  cta_setup<T, S>(a, s, P);
+  const bool contract = (a.A != nullptr) && (a.B != nullptr) && (a.m_out != nullptr || a.v_out != nullptr);
+  T acc[PPT > 0 ? PPT : 1];
+#pragma unroll
+  for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) acc[k] = Num<T>::zero();
+  __syncthreads();
+
+  for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
+    point_dims<T, S>(a, s, n);
+    __syncthreads();
+    T vals[2 * DMAX];
+#pragma unroll
+    for (int i = 0; i < 2 * DMAX; ++i) vals[i] = Num<T>::zero();
+    for (int ia = threadIdx.x; ia < M; ia += blockDim.x) {
+      T p1 = point_rows(s, M, Q, ia);
+      if (a.psi1) a.psi1[(size_t)n * M + ia] = Num<T>::st(p1);
+      if (contract)
+        for (int d = 0; d < D; ++d) vals[d] = fma_(p1, Num<T>::ld(a.A[d * M + ia]), vals[d]);
+    }
+    __syncthreads();
+    if (PPT > 0) {
+#pragma unroll
+      for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) {
+        int p = threadIdx.x + k * NT;
+        if (p < P) acc[k] = add(acc[k], fwd_pair<T>(a, s, n, p, contract, vals));
+      }
+    } else {
+      for (int p = threadIdx.x; p < P; p += NT) fwd_pair<T>(a, s, n, p, contract, vals);
+    }
+    if (contract) {
+      block_sum(vals, 2 * DMAX, s.red);
+      if (threadIdx.x == 0) {
+        for (int d = 0; d < D; ++d) {
+          T mm = vals[d];
+          T vv = sub(add(s.misc[1], vals[DMAX + d]), mul(mm, mm));
+          if (a.m_out) a.m_out[(size_t)n * D + d] = Num<T>::st(mm);
+          if (a.v_out) a.v_out[(size_t)n * D + d] = Num<T>::st(vv);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (PPT > 0 && a.psi2_sum) {
+#pragma unroll
+    for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) {
+      int p = threadIdx.x + k * NT;
+      if (p < P) {
+        int ia, ib;
+        pair_of(p, ia, ib);
+        double v = (double)Num<T>::st(acc[k]);
+        atomicAdd(&a.psi2_sum[ia * M + ib], v);
+        if (ia != ib) atomicAdd(&a.psi2_sum[ib * M + ia], v);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Backward.  Per point: psi1 terms per pseudo-input; per pair L = W psi2 with
+// W = sum_d dv_d (B_d[a,b] + B_d[b,a]) (the symmetrised upstream gradient, as
+// psi2compDer does, geepee/kernels.py:415-418) staged in shared memory; then per row
+// a the full-square sums R_a = sum_b L~_ab, S_aq = sum_b L~_ab z_bq (L~ the symmetric
+// half-weight matrix).  Every psi2 gradient is an affine function of R and S:
+//   dZ_aq += R_a(-z_aq/l + 2 c mu - c z_aq) + S_aq (1/l - c)
+//   dmu_q  = -2c (mu Rt - St)                    (Rt = sum_a R_a, St = sum_a S_a)
+//   dS_q   = -c Rt + 2c^2 (mu^2 Rt - 2 mu St + Z2R/2 + ZS/2)
+//   dl_q  += 2 ell (Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 (mu^2 Rt - 2 mu St + Z2R/2 + ZS/2))
+// with Z2R = sum_a z_a^2 R_a, ZS = sum_a z_a S_a; these restate psi2compDer
+// (geepee/kernels.py:402-444) without its N x M x M temporaries.
+template <typename T, int PPT, int DB>
+__global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  const int M = a.M, Q = a.Q, D = a.Dout;
+  const int P = M * (M + 1) / 2;
+  Smem<T> s = carve<T>(smem_raw, M, Q, P, true);
+  cta_setup<T, S>(a, s, P);
+  const int lane = threadIdx.x & 31;
+
+  T accB[PPT][DB];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k)
+#pragma unroll
+    for (int d = 0; d < DB; ++d) accB[k][d] = Num<T>::zero();
+  // per-thread accumulators over points
+  T g_sf = Num<T>::zero();                 // sum L1 + 2 sum L (for dsf2 * sf2)
+  T g_l[QMAX];                             // dl (before the ell factor)
+  T g_z[2][QMAX];                          // dZ of the rows this thread owns (row phase, M <= 128)
+  T g_zp[QMAX];                            // dZ psi1 part (pseudo-input a = tid)
+  T g_A[DB];
+#pragma unroll
+  for (int q = 0; q < QMAX; ++q) g_l[q] = g_z[0][q] = g_z[1][q] = g_zp[q] = Num<T>::zero();
+#pragma unroll
+  for (int d = 0; d < DB; ++d) g_A[d] = Num<T>::zero();
+  // rows owned in the row phase: 8 threads per row, rows a = tid/8 + k*(NT/8), k < 2
+  __syncthreads();
+
+  for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
+    point_dims<T, S>(a, s, n);
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + D) {
+      int d = threadIdx.x - 32;
+      T dvv = a.b_stride ? Num<T>::c(1.f) : Num<T>::ld(a.dv[(size_t)n * D + d]);
+      if (!a.dpsi1) {
+        T mm = Num<T>::ld(a.m[(size_t)n * D + d]);
+        T dmv = Num<T>::ld(a.dm[(size_t)n * D + d]);
+        s.pd[d] = sub(dmv, mul(scale2(dvv, 1), mm));     // dm_all
+      }
+      s.pd[DMAX + d] = dvv;
+    }
+    __syncthreads();
+    // ---- psi1 terms, one pseudo-input per thread
+    T pv[2 * QMAX];     // per-point dmu, dS partials (psi1 part)
+#pragma unroll
+    for (int i = 0; i < 2 * QMAX; ++i) pv[i] = Num<T>::zero();
+    for (int ia = threadIdx.x; ia < M; ia += blockDim.x) {
+      T p1 = point_rows(s, M, Q, ia);
+      T dp1 = Num<T>::zero();
+      if (a.dpsi1) {
+        dp1 = Num<T>::ld(a.dpsi1[(size_t)n * M + ia]);
+      } else {
+#pragma unroll
+        for (int d = 0; d < DB; ++d) {
+          if (d < D) {
+            dp1 = fma_(s.pd[d], Num<T>::ld(a.A[d * M + ia]), dp1);
+            g_A[d] = fma_(s.pd[d], p1, g_A[d]);
+          }
+        }
+      }
+      T L1 = mul(dp1, p1);
+      g_sf = add(g_sf, L1);
+      for (int q = 0; q < Q; ++q) {
+        T dd = sub(s.pmu[q], s.z[ia * Q + q]);
+        T ds = mul(dd, s.pis1[q]);                       // (mu - z)/s1
+        T ds2 = mul(ds, ds);
+        pv[q] = sub(pv[q], mul(L1, ds));                 // dmu
+        pv[QMAX + q] = add(pv[QMAX + q], scale2(mul(L1, sub(ds2, s.pis1[q])), -1));  // dS
+        g_zp[q] = add(g_zp[q], mul(L1, ds));             // dZ (psi1)
+        // dl/ell: 1/l - 1/s1 + d^2/s1^2
+        g_l[q] = add(g_l[q], mul(L1, add(sub(recip(s.ell2[q]), s.pis1[q]), ds2)));
+      }
+    }
+    __syncthreads();
+    // ---- pairs: L = W psi2 -> shared memory; dB accumulation
+    T dvr[DB];
+#pragma unroll
+    for (int d = 0; d < DB; ++d) dvr[d] = d < D ? s.pd[DMAX + d] : Num<T>::zero();
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      int p = threadIdx.x + k * blockDim.x;
+      if (p < P) {
+        int ia, ib;
+        pair_of(p, ia, ib);
+        T ps = pair_psi2(s, Q, p, ia, ib);
+        T w = Num<T>::zero();
+#pragma unroll
+        for (int d = 0; d < DB; ++d) {
+          if (d < D) {
+            const S* Bd = a.B + (size_t)d * M * M + (size_t)n * a.b_stride;
+            T bb = Num<T>::ld(Bd[ia * M + ib]);
+            if (ia != ib) bb = add(bb, Num<T>::ld(Bd[ib * M + ia]));
+            w = fma_(dvr[d], bb, w);
+            accB[k][d] = fma_(dvr[d], ps, accB[k][d]);
+          }
+        }
+        // L~ (half weight off the diagonal: the symmetric matrix entry)
+        T l = mul(w, ps);
+        s.L[p] = ia == ib ? l : scale2(l, -1);
+      }
+    }
+    __syncthreads();
+    // ---- row sums, 8 threads per row
+#pragma unroll
+    for (int rk = 0; rk < 2; ++rk) {
+      int ia = rk * (NT / 8) + (threadIdx.x >> 3);
+      int sl = threadIdx.x & 7;
+      T R = Num<T>::zero();
+      T Sq[QMAX];
+#pragma unroll
+      for (int q = 0; q < QMAX; ++q) Sq[q] = Num<T>::zero();
+      if (ia < M) {
+        for (int ib = sl; ib < M; ib += 8) {
+          int p = ia >= ib ? ia * (ia + 1) / 2 + ib : ib * (ib + 1) / 2 + ia;
+          T l = s.L[p];
+          R = add(R, l);
+          for (int q = 0; q < Q; ++q) Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
+        }
+      }
+#pragma unroll
+      for (int m = 1; m < 8; m <<= 1) {
+        R = add(R, shfl_xor(R, m));
+        for (int q = 0; q < Q; ++q) Sq[q] = add(Sq[q], shfl_xor(Sq[q], m));
+      }
+      if (ia < M && sl == 0) {
+        T* row = s.rows + ia * (1 + QMAX);
+        row[0] = R;
+        for (int q = 0; q < Q; ++q) {
+          row[1 + q] = Sq[q];
+          T zq = s.z[ia * Q + q];
+          T il = recip(s.ell2[q]);
+          T cq = s.pc[q];
+          // R(-z/l + 2 c mu - c z) + S (1/l - c)
+          T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, s.pmu[q]), 1)), mul(cq, zq));
+          g_z[rk][q] = add(g_z[rk][q], add(mul(R, t), mul(Sq[q], sub(il, cq))));
+        }
+      }
+    }
+    (void)lane;
+    __syncthreads();
+    // ---- per-point totals (warp 0), combined with the psi1 partials
+    // pv partials live in threads < M; reduce them with the row statistics
+    T vals[2 * QMAX];
+#pragma unroll
+    for (int i = 0; i < 2 * QMAX; ++i) vals[i] = pv[i];
+    block_sum(vals, 2 * QMAX, s.red);   // thread 0 holds psi1 part of dmu, dS
+    if (threadIdx.x < 32) {
+      T Rt = Num<T>::zero();
+      T St[QMAX], Z2R[QMAX], ZS[QMAX];
+#pragma unroll
+      for (int q = 0; q < QMAX; ++q) St[q] = Z2R[q] = ZS[q] = Num<T>::zero();
+      for (int ia = threadIdx.x; ia < M; ia += 32) {
+        const T* row = s.rows + ia * (1 + QMAX);
+        Rt = add(Rt, row[0]);
+        for (int q = 0; q < Q; ++q) {
+          T zq = s.z[ia * Q + q];
+          St[q] = add(St[q], row[1 + q]);
+          Z2R[q] = fma_(mul(zq, zq), row[0], Z2R[q]);
+          ZS[q] = fma_(zq, row[1 + q], ZS[q]);
+        }
+      }
+      Rt = warp_sum(Rt);
+      for (int q = 0; q < Q; ++q) {
+        St[q] = warp_sum(St[q]);
+        Z2R[q] = warp_sum(Z2R[q]);
+        ZS[q] = warp_sum(ZS[q]);
+      }
+      if (threadIdx.x == 0) {
+        g_sf = add(g_sf, scale2(Rt, 1));
+        for (int q = 0; q < Q; ++q) {
+          T mu = s.pmu[q], cq = s.pc[q], il = recip(s.ell2[q]);
+          T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St[q]), 1)), scale2(add(Z2R[q], ZS[q]), -1));
+          T dmu = add(vals[q], mul(scale2(cq, 1), sub(St[q], mul(mu, Rt))));
+          T dS = add(vals[QMAX + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
+          // (dl / 2 ell) accumulates: Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 e2
+          T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R[q], ZS[q]), mul(il, il)), -1)),
+                    mul(mul(cq, cq), e2));
+          g_l[q] = add(g_l[q], scale2(t, 1));
+          a.dmu[(size_t)n * Q + q] = Num<T>::st(dmu);
+          a.dvar[(size_t)n * Q + q] = Num<T>::st(dS);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- flush CTA accumulators
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    int p = threadIdx.x + k * NT;
+    if (p < P) {
+      int ia, ib;
+      pair_of(p, ia, ib);
+#pragma unroll
+      for (int d = 0; d < DB; ++d) {
+        if (d < D && a.dB) {
+          double v = (double)Num<T>::st(accB[k][d]);
+          atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
+          if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
+        }
+      }
+    }
+  }
+  if (threadIdx.x < M) {
+#pragma unroll
+    for (int d = 0; d < DB; ++d)
+      if (d < D && a.dA) atomicAdd(&a.dA[d * M + threadIdx.x], (double)Num<T>::st(g_A[d]));
+    for (int q = 0; q < Q; ++q) atomicAdd(&a.dZ[threadIdx.x * Q + q], (double)Num<T>::st(g_zp[q]));
+  }
+#pragma unroll
+  for (int rk = 0; rk < 2; ++rk) {
+    int ia = rk * (NT / 8) + (threadIdx.x >> 3);
+    if (ia < M && (threadIdx.x & 7) == 0)
+      for (int q = 0; q < Q; ++q) atomicAdd(&a.dZ[ia * Q + q], (double)Num<T>::st(g_z[rk][q]));
+  }
+  // dsf2 and dl need the ell / sf2 factors: (sum L1 + 2 sum L) / sf2 and ell * g_l
+  T vals[1 + QMAX];
+  vals[0] = g_sf;
+#pragma unroll
+  for (int q = 0; q < QMAX; ++q) vals[1 + q] = g_l[q];
+  __syncthreads();
+  block_sum(vals, 1 + QMAX, s.red);
+  if (threadIdx.x == 0) {
+    atomicAdd(a.dsf2, (double)Num<T>::st(div(vals[0], s.misc[1])));
+    for (int q = 0; q < Q; ++q) {
+      T ell = sqrt_(s.ell2[q]);
+      atomicAdd(&a.dl[q], (double)Num<T>::st(mul(vals[1 + q], ell)));
+    }
+  }
+}
+
+template <typename T, int PPT>
+int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
+  auto k = psi_fwd_kernel<T, PPT>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, NT, sm, st>>>(a);
+  return gpk::check_launch("psi_fwd");
+}
+
+template <typename T>
+int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a, cudaStream_t st) {
+  const int P = a.M * (a.M + 1) / 2;
+  size_t sm = smem_bytes(a.M, a.Q, P, false, sizeof(T));
+  if (sm > 227 * 1024) return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: M=%d needs %zu B of shared memory", a.M, sm);
+  const bool sum = a.psi2_sum != nullptr;
+  if (sum && P > PPT_MAX * NT)
+    return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: psi2_sum needs M(M+1)/2 <= %d (M=%d)", PPT_MAX * NT, a.M);
+  int per_sm = (int)((227 * 1024) / (sm + 1024));
+  if (per_sm < 1) per_sm = 1;
+  if (per_sm > 2) per_sm = 2;
+  int grid = gpk::sm_count() * per_sm;
+  if (grid > a.N) grid = a.N;
+  if (grid < 1) return GPK_OK;
+  if (!sum) return run_fwd<T, 0>(a, grid, sm, st);
+  if (P <= 4 * NT) return run_fwd<T, 4>(a, grid, sm, st);
+  return run_fwd<T, 16>(a, grid, sm, st);
+}
+
+template <typename T, int PPT, int DB>
+int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
+  auto k = psi_bwd_kernel<T, PPT, DB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, NT, sm, st>>>(a);
+  return gpk::check_launch("psi_bwd");
+}
+
+template <typename T, int DB>
+int bwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t sm, cudaStream_t st) {
+  if (P <= 4 * NT) return run_bwd<T, 4, DB>(a, grid, sm, st);
+  return run_bwd<T, 16, DB>(a, grid, sm, st);
+}
+
+template <typename T>
+int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a, cudaStream_t st) {
+  const int P = a.M * (a.M + 1) / 2;
+  size_t sm = smem_bytes(a.M, a.Q, P, true, sizeof(T));
+  if (a.M > 128 || sm > 227 * 1024)
+    return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d unsupported (M <= 128)", a.M);
+  int grid = gpk::sm_count();
+  if (grid > a.N) grid = a.N;
+  if (grid < 1) return GPK_OK;
+  if (a.Dout == 1) return bwd_ppt<T, 1>(a, P, grid, sm, st);
+  if (a.Dout == 2) return bwd_ppt<T, 2>(a, P, grid, sm, st);
+  return bwd_ppt<T, 4>(a, P, grid, sm, st);
+}
+
+}  // namespace psi_impl

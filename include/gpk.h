@@ -1,0 +1,150 @@
+/* gpk.h - C ABI of libgpk.so, the GB300 (sm_103a) kernels behind geepee_gb300.
+ *
+ * Every entry point takes caller-owned DEVICE buffers (plain pointers, row-major,
+ * explicit sizes), a cudaStream_t passed as void*, and returns an int status:
+ *   GPK_OK (0) on success, >0 a LAPACK-style info (e.g. the failing pivot of a
+ *   Cholesky), <0 an argument / support / CUDA error (see gpk_last_error()).
+ * Launches are asynchronous on `stream`; nothing allocates device memory, so every
+ * call can be captured in a CUDA graph.
+ *
+ * Precision `prec`: GPK_DF64 - buffers are float64 and the arithmetic is
+ * double-float (two FP32 words, ~48-bit significand) on the FP32 pipes;
+ * GPK_FP32 - buffers are float32 and the arithmetic is FP32.  Accumulated outputs
+ * (sums over data points) are always float64 and are ADDED INTO (the caller zeroes
+ * them first), so results of several launches can be combined.
+ *
+ * Hyperparameters are device pointers in the reference's log parameterisation:
+ * lls2[q] = log ell_q^2 = 2*ls[q], lsf2[0] = log sf^2 = 2*sf
+ * (the arguments geepee passes to compute_kernel / compute_psi_weave, e.g.
+ * geepee/aep_models.py:154,194).
+ */
+#ifndef GPK_H
+#define GPK_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPK_OK 0
+#define GPK_EINVAL (-1)
+#define GPK_EUNSUPPORTED (-2)
+#define GPK_ECUDA (-3)
+
+#define GPK_DF64 0
+#define GPK_FP32 1
+
+/* Library version and the text of the last error on this thread. */
+int gpk_version(void);
+const char* gpk_last_error(void);
+
+/* ARD exponentiated-quadratic kernel matrix
+ *   K[n,m] = sf2 * exp(-1/2 sum_d (x[n,d]-z[m,d])^2 / ell2[d])  (+ jitter if n == m)
+ * x: [N,D] (row stride ldx), z: [M,D] (row stride ldz), K: [N,M] (row stride ldk).
+ * Replaces geepee/kernels.py:10-22 compute_kernel(lls, lsf, x, z) (and the jittered
+ * Kuu of base_models.py:454-464 when jitter > 0). */
+int gpk_kern(int prec, int N, int M, int D, const void* x, int ldx, const void* z, int ldz,
+             const double* lls2, const double* lsf2, double jitter, void* K, int ldk, void* stream);
+
+/* Psi statistics of the ARD kernel under Gaussian inputs N(mu, var), fused with the
+ * moment-matching contractions of one sparse-GP layer.
+ *   psi1[n,m]   = sf2 prod_q sqrt(l/(l+S)) exp(-(mu-z_m)^2 / (2(l+S)))
+ *   psi2[n,a,b] = sf2^2 prod_q sqrt(l/(l+2S)) exp(-(z_a-z_b)^2/(4l) - (mu-(z_a+z_b)/2)^2/(l+2S))
+ * Inputs: mu, var [N,Q]; Z [M,Q]; optional A [Dout,M] and B [Dout,M,M].
+ * Outputs (each optional, NULL to skip):
+ *   psi1 [N,M]; psi2 [N,M,M] (full symmetric, per point); psi2_sum [M,M] += sum_n psi2
+ *   (float64); m_out, v_out [N,Dout]:  m = psi1 A^T,  v = sf2 + sum_ab B[d,a,b] psi2[n,a,b] - m^2
+ *   (A and B required for m_out / v_out).
+ * Replaces geepee/kernels.py:181-240 compute_psi_weave and the contraction in
+ * SGP_Layer._forward_prop_random_thru_cav_mm, geepee/aep_models.py:182-199
+ * (base_models.py:286-307 for the posterior). */
+int gpk_psi_fwd(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
+                const void* Z, const double* lls2, const double* lsf2, const void* A,
+                const void* B, void* psi1, void* psi2, double* psi2_sum, void* m_out,
+                void* v_out, void* stream);
+
+/* Backward of gpk_psi_fwd's m/v outputs, recomputing psi1/psi2 (nothing N*M*M is stored).
+ * Given m [N,Dout] and upstream gradients dm, dv [N,Dout]:
+ *   dm_all = dm - 2 dv m;  dpsi1 = dm_all A;  dpsi2[n] = sum_d dv[n,d] B[d]
+ * and returns the gradients of  sum(dpsi1*psi1) + sum(dpsi2*psi2):
+ *   dsf2 [1] (w.r.t. sf^2), dl [Q] (w.r.t. ell, not ell^2), dZ [M,Q]   (+=, float64)
+ *   dA [Dout,M] += sum_n dm_all[n,d] psi1[n,:];  dB [Dout,M,M] += sum_n dv[n,d] psi2[n]
+ *   dmu, dvar [N,Q] (overwritten, buffer precision).
+ * Replaces geepee/kernels.py:302-309 compute_psi_derivatives (psi1compDer :355-378,
+ * psi2compDer :402-444) together with the dAhat/dBhat/dpsi einsums of
+ * SGP_Layer.backprop_grads_lvm_mm, geepee/aep_models.py:238-245. */
+int gpk_psi_bwd(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
+                const void* Z, const double* lls2, const double* lsf2, const void* A,
+                const void* B, const void* m, const void* dm, const void* dv, double* dsf2,
+                double* dl, double* dZ, double* dA, double* dB, void* dmu, void* dvar,
+                void* stream);
+
+
+/* As gpk_psi_bwd, with two generic modes used by the drop-in compute_psi_derivatives:
+ *   dpsi1 != NULL : an arbitrary upstream gradient dL/dpsi1 [N,M] replaces dm_all A
+ *                   (A, m, dm may then be NULL; dA is not touched);
+ *   b_stride != 0 : B holds a per-point dL/dpsi2 (point n at B + n*b_stride, Dout = 1,
+ *                   dv ignored, dB not touched).
+ * Replaces geepee/kernels.py:302-309 for arbitrary (dL_dpsi1, dL_dpsi2). */
+int gpk_psi_bwd_ex(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
+                   const void* Z, const double* lls2, const double* lsf2, const void* A,
+                   const void* B, const void* m, const void* dm, const void* dv, const void* dpsi1,
+                   long b_stride, double* dsf2, double* dl, double* dZ, double* dA, double* dB,
+                   void* dmu, void* dvar, void* stream);
+
+/* Deterministic-input sparse-GP layer, forward (fused):
+ *   kfu = K(x, Z) [N,M];  m[n,d] = kfu_n . A_d;  Bk[n,d,b] = sum_a B[d,a,b] kfu[n,a];
+ *   v[n,d] = sf2 + kfu_n . Bk[n,d]
+ * x [N,D] (row stride ldx), Z [M,D], A [Dout,M], B [Dout,M,M].  kfu/Bk/m/v optional.
+ * Replaces SGP_Layer._forward_prop_deterministic_thru_cav, geepee/aep_models.py:142-158
+ * (and _thru_post, base_models.py:265-284). */
+int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                const double* lls2, const double* lsf2, const void* A, const void* B, void* kfu,
+                void* Bk, void* m_out, void* v_out, void* stream);
+
+/* Deterministic-input layer, backward through kfu:
+ *   dkfu = dm A + 2 dv Bk   (or the given dkfu [N,M] when dkfu != NULL)
+ * returns (+=, float64) dsf2 [1], dl [D] (w.r.t. ell), dZ [M,D], dA [Dout,M] += dm^T kfu,
+ * and optionally dx [N,D] (overwritten).  Replaces kfucompDer / compute_kfu_derivatives,
+ * geepee/kernels.py:312-313,381-399, with the dkfu einsums of aep_models.py:452-454. */
+int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
+                const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
+                double* dA, void* dx, void* stream);
+
+/* Weighted Gram reduction over rows:  C[d] += sum_n w[n,d] u_n v_n^T  (u, v [N,M], w [N,Dout],
+ * C [Dout,M,M] float64).  The einsum('nd,na,nb->dab') / einsum('na,nd,nb->dab') reductions of
+ * geepee/aep_models.py:464,493. */
+int gpk_gram(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
+             void* stream);
+
+/* c[d] += sum_n w[n,d] u_n  (u [N,M], w [N,Dout], c [Dout,M] float64);
+ * einsum('nd,nm->dm') of geepee/aep_models.py:239,463,490. */
+int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const void* w, double* c, void* stream);
+
+/* Batched GEMM  C[b] = alpha op(A[b]) op(B[b]) + beta C[b]  (row-major; op = transpose when
+ * transA/transB != 0; batch strides in elements, 0 broadcasts).  In the df64 precision the
+ * products of the M x M AEP algebra (np.einsum chains such as 'ab,dbc,ce->dae',
+ * geepee/aep_models.py:252,258, base_models.py:480-488) run on the FP32 pipes. */
+int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
+             const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
+             void* C, int ldc, long strideC, void* stream);
+
+/* Batched SPD factorisation of A[b] (M x M, M <= 128): writes (each optional) the inverse
+ * Ainv, the lower Cholesky factor L, logdet = log det A, and info[b] = 0 or the 1-based
+ * pivot where A[b] stopped being positive definite (LAPACK potrf convention).
+ * Replaces np.linalg.inv / slogdet on Kuu, Su^-1, Suhat^-1 (geepee/base_models.py:464,471,
+ * aep_models.py:68,78,91,525). */
+int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
+                 void* stream);
+
+/* Gradient of tr(Mm Kzz), Kzz = K(Z, Z) without jitter, w.r.t. log sf^2, log ell^2 and Z,
+ * added with scales: g_sf += s_sf * d/dlog sf^2, g_ls += s_ls * d/dlog ell^2, g_z += d/dZ.
+ * Replaces geepee/kernels.py:447-475 d_trace_MKzz_dhypers. */
+int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
+                  const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
+                  void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPK_H */

@@ -1,0 +1,681 @@
+"""float64 numpy restatement of the geepee AEP sparse-GP path (the oracle).
+
+TEST INFRASTRUCTURE ONLY - see ``oracle/__init__.py``.  Never imported by the
+product package.
+
+Each function names the reference lines (thangbui/geepee, paths relative to the
+project root) whose arithmetic it restates.  The structure is functional: a
+layer is a plain dict of arrays, models are functions of (data, params).
+Derivatives of the psi statistics are derived afresh from the closed forms
+(below) rather than transcribed; they agree with the reference's hand-derived
+routines to rounding (pinned by ``tests/test_oracle_golden.py``).
+
+Notation: ell2 = exp(2 ls) (squared lengthscales), sf2 = exp(2 sf) (signal
+variance), mu/S the Gaussian input means/variances [N,Q], Z the pseudo-inputs
+[M,Q].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+JITTER = 1e-5  # geepee/config.py:11
+
+
+def _scalar(a) -> float:
+    return float(np.ravel(a)[0])
+
+
+# --------------------------------------------------------------------------
+# kernels.py
+# --------------------------------------------------------------------------
+
+def ard_kernel(lls, lsf, x, z):
+    """ARD exponentiated quadratic; ``compute_kernel`` geepee/kernels.py:10-22.
+
+    lls = log ell^2 (per dim), lsf = log sf^2.
+    """
+    x = np.atleast_2d(x)
+    z = np.atleast_2d(z)
+    ell2 = np.exp(np.asarray(lls, dtype=float))
+    sq = (((x[:, None, :] - z[None, :, :]) ** 2) / ell2).sum(-1)
+    return np.exp(np.asarray(lsf, dtype=float)) * np.exp(-0.5 * sq)
+
+
+def psi_stats(lls2, lsf2, mu, S, Z):
+    """psi1 [N,M] and per-point psi2 [N,M,M]; ``compute_psi_weave`` kernels.py:181-240.
+
+    psi1[n,m]   = sf2 prod_q sqrt(l/(l+S)) exp(-(mu-z_m)^2 / (2 (l+S)))
+    psi2[n,a,b] = sf2^2 prod_q sqrt(l/(l+2S)) exp(-(z_a-z_b)^2/(4l) - (mu-(z_a+z_b)/2)^2/(l+2S))
+    """
+    ell2 = np.exp(np.asarray(lls2, dtype=float))
+    sf2 = np.exp(_scalar(lsf2))
+    s1 = ell2 + S                                             # [N,Q]
+    log1 = 0.5 * np.log(ell2 / s1).sum(-1)                   # [N]
+    d1 = mu[:, None, :] - Z[None, :, :]                      # [N,M,Q]
+    psi1 = sf2 * np.exp(log1[:, None] - 0.5 * (d1 ** 2 / s1[:, None, :]).sum(-1))
+    s2 = ell2 + 2.0 * S
+    log2 = 0.5 * np.log(ell2 / s2).sum(-1)
+    dz2 = (((Z[:, None, :] - Z[None, :, :]) ** 2) / (4.0 * ell2)).sum(-1)   # [M,M]
+    zbar = 0.5 * (Z[:, None, :] + Z[None, :, :])                          # [M,M,Q]
+    e = mu[:, None, None, :] - zbar[None]                                 # [N,M,M,Q]
+    arg = log2[:, None, None] - dz2[None] - (e ** 2 / s2[:, None, None, :]).sum(-1)
+    psi2 = sf2 * sf2 * np.exp(arg)
+    return psi1, psi2
+
+
+def psi_derivatives(dpsi1, psi1, dpsi2, psi2, ell, sf2, mu, S, Z):
+    """Gradients of sum(dpsi1*psi1) + sum(dpsi2*psi2).
+
+    Restates ``compute_psi_derivatives`` (kernels.py:302-309 -> psi1compDer :355-378,
+    psi2compDer :402-444): returns (d sf2, d ell [Q] w.r.t. ell (not ell^2), dZ [M,Q],
+    dmu [N,Q], dS [N,Q]).  dpsi2 may be [M,M] (shared) or [N,M,M]; it is symmetrised.
+    """
+    ell = np.asarray(ell, dtype=float)
+    ell2 = ell ** 2
+    N = mu.shape[0]
+    # ---- psi1 part: log psi1 = log sf2 + sum_q [1/2 log l - 1/2 log s - d^2/(2s)]
+    s1 = ell2 + S
+    L1 = dpsi1 * psi1                                  # [N,M]
+    d1 = mu[:, None, :] - Z[None, :, :]                # [N,M,Q]
+    g_mu1 = -d1 / s1[:, None, :]
+    g_S1 = -0.5 / s1[:, None, :] + 0.5 * d1 ** 2 / s1[:, None, :] ** 2
+    g_l1 = ell * (1.0 / ell2 - 1.0 / s1[:, None, :] + d1 ** 2 / s1[:, None, :] ** 2)
+    dsf2 = L1.sum() / sf2
+    dmu = np.einsum('nm,nmq->nq', L1, g_mu1)
+    dS = np.einsum('nm,nmq->nq', L1, g_S1)
+    dZ = -np.einsum('nm,nmq->mq', L1, g_mu1)
+    dl = np.einsum('nm,nmq->q', L1, g_l1)
+    # ---- psi2 part
+    G = np.asarray(dpsi2, dtype=float)
+    if G.ndim == 2:
+        G = 0.5 * (G + G.T)
+        L2 = G[None] * psi2
+    else:
+        G = 0.5 * (G + np.swapaxes(G, 1, 2))
+        L2 = G * psi2                                  # [N,M,M]
+    s2 = ell2 + 2.0 * S                                # [N,Q]
+    delta = Z[:, None, :] - Z[None, :, :]              # [M,M,Q]
+    e = mu[:, None, None, :] - 0.5 * (Z[:, None, :] + Z[None, :, :])[None]
+    r = s2[:, None, None, :]
+    dsf2 += 2.0 * L2.sum() / sf2
+    dmu += np.einsum('nab,nabq->nq', L2, -2.0 * e / r)
+    dS += np.einsum('nab,nabq->nq', L2, -1.0 / r + 2.0 * e ** 2 / r ** 2)
+    dl += 2.0 * ell * np.einsum('nab,nabq->q', L2,
+                                0.5 / ell2 - 0.5 / r + delta[None] ** 2 / (4.0 * ell2 ** 2) + e ** 2 / r ** 2)
+    # d/dz_a of the (a,b) term: -delta/(2l) + e/r ; symmetric G doubles the row sum
+    dZ += 2.0 * np.einsum('nab,nabq->aq', L2, -delta[None] / (2.0 * ell2) + e / r)
+    del N
+    return dsf2, dl, dZ, dmu, dS
+
+
+def kfu_derivatives(dkfu, kfu, ell, sf2, x, Z, grad_x=False):
+    """``compute_kfu_derivatives`` kernels.py:312-313 -> kfucompDer :381-399."""
+    ell2 = np.asarray(ell, dtype=float) ** 2
+    L = dkfu * kfu
+    diff = x[:, None, :] - Z[None, :, :]              # x - z
+    dsf2 = L.sum() / sf2
+    dZ = np.einsum('nm,nmq->mq', L, diff) / ell2
+    dl = np.einsum('nm,nmq->q', L, diff ** 2) / np.asarray(ell, dtype=float) ** 3
+    if grad_x:
+        dx = -np.einsum('nm,nmq->nq', L, diff) / ell2
+        return dsf2, dl, dZ, dx
+    return dsf2, dl, dZ
+
+
+def trace_kzz_grads(lls, lsf, z, Mmat, Kzz):
+    """Gradient of tr(M Kzz) w.r.t. (log sf^2, log ell^2 [Q], Z [M,Q]).
+
+    ``d_trace_MKzz_dhypers`` kernels.py:447-475 (same quantities, derived directly).
+    """
+    ell2 = np.exp(np.asarray(lls, dtype=float))
+    W = Mmat * Kzz                                       # elementwise
+    g_lsf = W.sum()
+    delta = z[:, None, :] - z[None, :, :]
+    g_lls = 0.5 * np.einsum('ab,abq->q', W, delta ** 2) / ell2
+    Ws = Mmat + Mmat.T
+    g_z = np.einsum('ab,abq->aq', Ws * Kzz, -delta) / ell2
+    return g_lsf, g_lls, g_z
+
+
+# --------------------------------------------------------------------------
+# the sparse GP layer (base_models.py Base_SGP_Layer, aep_models.py SGP_Layer)
+# --------------------------------------------------------------------------
+
+def _triu(M):
+    return np.triu_indices(M)
+
+
+def layer_unpack(p, suffix, M, Dout, nat_param=True):
+    """``update_hypers`` + ``compute_kuu`` + ``update_posterior``, base_models.py:630-658,454-488."""
+    ls = np.asarray(p['ls' + suffix], dtype=float)
+    sf = p['sf' + suffix]
+    Z = np.asarray(p['zu' + suffix], dtype=float)
+    eta1 = np.asarray(p['eta1_R' + suffix], dtype=float)
+    eta2 = np.asarray(p['eta2' + suffix], dtype=float)
+    iu = _triu(M)
+    R = np.zeros((Dout, M, M))
+    for d in range(Dout):
+        R[d][iu] = eta1[d]
+        R[d][np.diag_indices(M)] = np.exp(np.diag(R[d]))
+    th1 = np.einsum('dba,dbc->dac', R, R)            # R^T R
+    th2 = eta2.copy()
+    Kuu = ard_kernel(2 * ls, 2 * _scalar(sf), Z, Z) + JITTER * np.eye(M)
+    Kinv = np.linalg.inv(Kuu)
+    L = dict(ls=ls, sf=_scalar(sf), Z=Z, R=R, th1=th1, th2=th2, Kuu=Kuu, Kinv=Kinv,
+             M=M, Dout=Dout, nat=nat_param)
+    if nat_param:
+        Suinv = Kinv[None] + th1
+        Su = np.linalg.inv(Suinv)
+        mu = np.einsum('dab,db->da', Su, th2)
+    else:
+        Su = th1.copy()
+        Suinv = np.linalg.inv(Su)
+        mu = th2.copy()
+    Spmm = Su + np.einsum('da,db->dab', mu, mu)
+    L.update(Su=Su, Suinv=Suinv, mu=mu, Spmm=Spmm,
+             A=np.einsum('ab,db->da', Kinv, mu),
+             B_sto=-Kinv[None] + Kinv[None] @ Spmm @ Kinv[None],
+             B_det=-Kinv[None] + Kinv[None] @ Su @ Kinv[None])
+    return L
+
+
+def layer_cavity(L, N, alpha):
+    """``SGP_Layer.compute_cavity`` aep_models.py:513-546."""
+    beta = (N - alpha) / N
+    K = L['Kinv'][None]
+    if L['nat']:
+        Shinv = K + beta * L['th1']
+        Sh = np.linalg.inv(Shinv)
+        mh = np.einsum('dab,db->da', Sh, beta * L['th2'])
+    else:
+        f1 = L['Suinv'] - K
+        f2 = np.einsum('dab,db->da', L['Suinv'], L['mu'])
+        Shinv = K + beta * f1
+        Sh = np.linalg.inv(Shinv)
+        mh = np.einsum('dab,db->da', Sh, beta * f2)
+    Smm_h = Sh + np.einsum('da,db->dab', mh, mh)
+    L.update(beta=beta, Shinv=Shinv, Sh=Sh, mh=mh, Smm_h=Smm_h,
+             Ah=np.einsum('ab,db->da', L['Kinv'], mh),
+             Bh_sto=-K + K @ Smm_h @ K,
+             Bh_det=-K + K @ Sh @ K)
+    return L
+
+
+def _half_logdet_quad(S, m):
+    sign, logdet = np.linalg.slogdet(S)
+    return 0.5 * logdet.sum() + 0.5 * np.sum(m * np.linalg.solve(S, m[..., None])[..., 0])
+
+
+def layer_phi(L, N, alpha):
+    """``compute_phi`` aep_models.py:62-114 (prior, posterior, cavity log-partitions)."""
+    _, ld = np.linalg.slogdet(L['Kuu'])
+    phi_prior = L['Dout'] * 0.5 * ld
+    phi_post = _half_logdet_quad(L['Su'], L['mu'])
+    phi_cav = _half_logdet_quad(L['Sh'], L['mh'])
+    return phi_prior + (N / alpha - 1.0) * phi_post - (N / alpha) * phi_cav
+
+
+def fwd_det(L, x, cav=True):
+    """Deterministic inputs: aep_models.py:142-158 (cavity) / base_models.py:265-284 (posterior)."""
+    kfu = ard_kernel(2 * L['ls'], 2 * L['sf'], x, L['Z'])
+    A, B = (L['Ah'], L['Bh_det']) if cav else (L['A'], L['B_det'])
+    m = kfu @ A.T
+    v = np.exp(2 * L['sf']) + np.einsum('dab,na,nb->nd', B, kfu, kfu)
+    return m, v, kfu
+
+
+def fwd_mm(L, mx, vx, cav=True):
+    """Gaussian inputs, moment matching: aep_models.py:182-199 / base_models.py:286-307."""
+    psi1, psi2 = psi_stats(2 * L['ls'], 2 * L['sf'], mx, vx, L['Z'])
+    A, B = (L['Ah'], L['Bh_sto']) if cav else (L['A'], L['B_sto'])
+    m = psi1 @ A.T
+    v = np.exp(2 * L['sf']) + np.einsum('dab,nab->nd', B, psi2) - m ** 2
+    return m, v, psi1, psi2
+
+
+def _pack_eta1(L, dth1):
+    """d theta_1 -> d eta1_R (upper-triangular, log-diagonal packing).
+
+    Chain rule of theta_1 = R^T R with R's diagonal stored as a log
+    (the packing loop at aep_models.py:275-287, base_models.py:506-514).
+    """
+    M, Dout = L['M'], L['Dout']
+    dR = L['R'] @ (dth1 + np.swapaxes(dth1, 1, 2))
+    out = np.zeros((Dout, M * (M + 1) // 2))
+    iu, di = _triu(M), np.diag_indices(M)
+    for d in range(Dout):
+        g = dR[d].copy()
+        g[di] = g[di] * L['R'][d][di]
+        out[d] = g[iu]
+    return out
+
+
+def _cav_grad_u(L, dmu, dSu):
+    """``compute_cav_grad_u`` aep_models.py:548-586."""
+    beta = L['beta']
+    if L['nat']:
+        dSu = dSu + np.einsum('da,db->dab', dmu, beta * L['th2'])
+        dSinv = -L['Sh'] @ dSu @ L['Sh']
+        dKinv = dSinv.sum(0)
+        dth1 = beta * dSinv
+        deta2 = beta * np.einsum('dab,db->da', L['Sh'], dmu)
+    else:
+        f2 = np.einsum('dab,db->da', L['Suinv'], L['mu'])
+        dSh = dSu + np.einsum('da,db->dab', dmu, beta * f2)
+        dShinv = -L['Sh'] @ dSh @ L['Sh']
+        dSinv1 = beta * dShinv
+        Shdmu = np.einsum('dab,db->da', L['Sh'], dmu)
+        dSinv = dSinv1 + beta * np.einsum('da,db->dab', Shdmu, L['mu'])
+        dth1 = -L['Suinv'] @ dSinv @ L['Suinv']
+        deta2 = beta * np.einsum('dab,db->da', L['Suinv'], Shdmu)
+        dKinv = (1 - beta) / beta * dSinv1.sum(0)
+    return _pack_eta1(L, dth1), deta2, dKinv
+
+
+def _post_grad_u(L, dmu, dSu):
+    """``compute_posterior_grad_u`` base_models.py:490-516."""
+    if L['nat']:
+        dSu = dSu + np.einsum('da,db->dab', dmu, L['th2'])
+        dSinv = -L['Su'] @ dSu @ L['Su']
+        dKinv = dSinv.sum(0)
+        dth1 = dSinv
+        deta2 = np.einsum('dab,db->da', L['Su'], dmu)
+    else:
+        deta2 = dmu
+        dth1 = dSu
+        dKinv = 0.0
+    return _pack_eta1(L, dth1), deta2, dKinv
+
+
+def _finish_hyp(L, g_sf, g_ls, g_z, Minner):
+    lsf = 2 * L['sf']
+    gl_sf, gl_lls, gl_z = trace_kzz_grads(2 * L['ls'], lsf, L['Z'], Minner,
+                                          L['Kuu'] - JITTER * np.eye(L['M']))
+    return g_sf + 2 * gl_sf, g_ls + 2 * gl_lls, g_z + gl_z
+
+
+def bwd_mm(L, N, alpha, m, dm, dv, psi1, psi2, mx, vx):
+    """``backprop_grads_lvm_mm`` aep_models.py:201-304 (includes the phi gradients)."""
+    ell = np.exp(L['ls'])
+    sf2 = np.exp(2 * L['sf'])
+    beta = L['beta']
+    s_post, s_cav = N / alpha - 1.0, -N / alpha
+    K = L['Kinv']
+    dm_all = dm - 2 * dv * m
+    dAh = dm_all.T @ psi1
+    dBh = np.einsum('nd,nab->dab', dv, psi2)
+    dpsi1 = dm_all @ L['Ah']
+    dpsi2 = np.einsum('nd,dab->nab', dv, L['Bh_sto'])
+    dsf2, dl, dz, dmx, dvx = psi_derivatives(dpsi1, psi1, dpsi2, psi2, ell, sf2, mx, vx, L['Z'])
+    dls = dl * ell
+    dsf = 2 * sf2 * (dsf2 + dv.sum())
+    dvcav = K[None] @ dBh @ K[None]
+    dmcav = 2 * np.einsum('dab,db->da', dvcav, L['mh']) + dAh @ K.T
+    dvcav = dvcav + beta * np.einsum('da,db->dab', dmcav, L['th2'])
+    dvcavinv = -L['Sh'] @ dvcav @ L['Sh']
+    dth1 = beta * dvcavinv
+    dth2 = beta * np.einsum('dab,db->da', L['Sh'], dmcav)
+    dK = (dvcavinv.sum(0) + dAh.T @ L['mh']
+          + 2 * np.einsum('dab,dac->bc', K[None] @ L['Smm_h'], dBh) - dBh.sum(0))
+    Minner = s_post * L['Spmm'].sum(0) + s_cav * L['Smm_h'].sum(0) - 2.0 * dK
+    dth1 = -0.5 * s_post * L['Spmm'] - 0.5 * s_cav * beta * L['Smm_h'] + dth1
+    dth2 = s_post * L['mu'] + s_cav * beta * L['mh'] + dth2
+    Mall = 0.5 * (L['Dout'] * K + K @ Minner @ K)
+    dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, Mall)
+    return ({'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': _pack_eta1(L, dth1), 'eta2': dth2},
+            {'mx': dmx, 'vx': dvx})
+
+
+def bwd_det(L, N, alpha, dm, dv, kfu, x):
+    """``backprop_grads_reg`` aep_models.py:412-511 (includes the phi gradients)."""
+    ell = np.exp(L['ls'])
+    sf2 = np.exp(2 * L['sf'])
+    s_post, s_cav = N / alpha - 1.0, -N / alpha
+    K = L['Kinv']
+    kK = kfu @ K
+    dkfu = dm @ L['Ah'] + 2 * np.einsum('nd,dab,na->nb', dv, L['Bh_det'], kfu)
+    dsf2, dl, dz = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'])
+    dls = dl * ell
+    dsf = 2 * sf2 * (dsf2 + dv.sum())
+    dmucav = dm.T @ kK
+    dSucav = np.einsum('na,nd,nb->dab', kK, dv, kK)
+    Sinv_mh = np.einsum('dab,db->da', L['Shinv'], L['mh'])
+    dmucav = dmucav + s_cav * Sinv_mh
+    dSucav = dSucav + s_cav * (0.5 * L['Shinv'] - 0.5 * np.einsum('da,db->dab', Sinv_mh, Sinv_mh))
+    e1c, e2c, dKc = _cav_grad_u(L, dmucav, dSucav)
+    Sinv_mu = np.einsum('dab,db->da', L['Suinv'], L['mu'])
+    dmu = s_post * Sinv_mu
+    dSu = s_post * (0.5 * L['Suinv'] - 0.5 * np.einsum('da,db->dab', Sinv_mu, Sinv_mu))
+    e1p, e2p, dKp = _post_grad_u(L, dmu, dSu)
+    dKprior = -0.5 * L['Dout'] * L['Kuu']
+    dAh = dm.T @ kfu
+    dBh = np.einsum('nd,na,nb->dab', dv, kfu, kfu)
+    dK = (dAh.T @ L['mh'] + 2 * np.einsum('dab,dac->bc', K[None] @ L['Sh'], dBh) - dBh.sum(0)
+          + dKc + dKp + dKprior)
+    Minner = -K @ dK @ K
+    dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, Minner)
+    return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1c + e1p, 'eta2': e2c + e2p}
+
+
+# --------------------------------------------------------------------------
+# likelihood / emission (lik_layers.py)
+# --------------------------------------------------------------------------
+
+def gauss_logZ(m, v, y, sn, alpha):
+    """``Gauss_Layer.compute_log_Z`` (2-D case) lik_layers.py:119-133."""
+    sn2 = np.exp(2.0 * _scalar(sn))
+    vt = v + sn2 / alpha
+    r = y - m
+    logZ = np.sum(-0.5 * (np.log(2 * np.pi * vt) + r ** 2 / vt))
+    logZ += y.shape[0] * y.shape[1] * (0.5 * np.log(2 * np.pi * sn2 / alpha)
+                                       - 0.5 * alpha * np.log(2 * np.pi * sn2))
+    return logZ, r / vt, -0.5 / vt + 0.5 * r ** 2 / vt ** 2
+
+
+def gauss_dsn(dv, nb, D, sn, alpha, scale):
+    """``Gauss_Layer.backprop_grads`` lik_layers.py:154-181 (2-D case)."""
+    sn2 = np.exp(2.0 * _scalar(sn))
+    return scale * (dv.sum() * 2 * sn2 / alpha + nb * D * (1 - alpha))
+
+
+def emission_tilted(C, Rlog, y, mx, vx, alpha, scale):
+    """``Gauss_Emis.compute_emission_tilted`` lik_layers.py:573-627.
+
+    C [Dy,Dx], Rlog = log std (R = exp(2 Rlog)), y [Nb,Dy], mx, vx [Nb,Dx].
+    Returns (scale*logZ, {'mx','vx'}, {'C','R'}).
+    """
+    R = np.exp(2 * np.asarray(Rlog, dtype=float))
+    Nb, Dy = y.shape
+    CVC = np.einsum('da,na,ba->ndb', C, vx, C)
+    Vy = CVC + np.diag(R / alpha)[None]
+    Yd = y - mx @ C.T
+    VinvY = np.linalg.solve(Vy, Yd[..., None])[..., 0]
+    quad = -0.5 * np.sum(Yd * VinvY)
+    ICVCR = np.eye(Dy)[None] + alpha * CVC / R
+    logZ = (-Nb * Dy * 0.5 * alpha * np.log(2 * np.pi) - 0.5 * Nb * alpha * np.sum(np.log(R))
+            - 0.5 * np.sum(np.linalg.slogdet(ICVCR)[1]) + quad)
+    Vinv = np.linalg.inv(Vy)
+    dR = (-0.5 * np.sum(np.diagonal(Vinv, axis1=1, axis2=2), axis=0)
+          + 0.5 * np.sum(VinvY ** 2, axis=0)) / alpha
+    dR = (dR + 0.5 * Nb * (1 - alpha) / R) * 2 * R
+    dSig = -0.5 * Vinv + 0.5 * np.einsum('na,nb->nab', VinvY, VinvY)
+    dC = VinvY.T @ mx + 2 * np.einsum('nc,bc,nab->ac', vx, C, dSig)
+    dmx = VinvY @ C
+    dvx = np.einsum('nab,ad,bd->nd', dSig, C, C)
+    return logZ * scale, {'mx': dmx * scale, 'vx': dvx * scale}, {'C': dC * scale, 'R': dR * scale}
+
+
+# --------------------------------------------------------------------------
+# models (aep_models.py)
+# --------------------------------------------------------------------------
+
+def _layer_dims(p, suffix):
+    eta2 = np.asarray(p['eta2' + suffix])
+    return eta2.shape[1], eta2.shape[0]
+
+
+def _finish(energy, grads, N, fixed=(), divide=True):
+    for k in fixed:
+        grads[k] = np.zeros_like(grads[k])
+    if divide:
+        energy = energy / N
+        grads = {k: g / N for k, g in grads.items()}
+    return energy, grads
+
+
+def sgpr_objective(x, y, p, alpha, idx=None, nat_param=True, fixed=()):
+    """``SGPR.objective_function`` aep_models.py:610-667 (Gaussian likelihood)."""
+    N = y.shape[0]
+    xb, yb = (x, y) if idx is None else (x[idx], y[idx])
+    Mz, Dout = _layer_dims(p, '')
+    scale = -N / yb.shape[0] / alpha
+    L = layer_cavity(layer_unpack(p, '', Mz, Dout, nat_param), N, alpha)
+    m, v, kfu = fwd_det(L, xb)
+    logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
+    g = bwd_det(L, N, alpha, scale * dm, scale * dv, kfu, xb)
+    g['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
+    return _finish(scale * logZ + layer_phi(L, N, alpha), g, N, fixed)
+
+
+def sdgpr_objective(x, y, p, alpha, idx=None, fixed=()):
+    """``SDGPR.objective_function`` aep_models.py:895-988 (moment matching)."""
+    N = y.shape[0]
+    xb, yb = (x, y) if idx is None else (x[idx], y[idx])
+    nl = 0
+    while ('eta2_%d' % nl) in p:
+        nl += 1
+    scale = -N / yb.shape[0] / alpha
+    layers = []
+    for i in range(nl):
+        Mz, Dout = _layer_dims(p, '_%d' % i)
+        layers.append(layer_cavity(layer_unpack(p, '_%d' % i, Mz, Dout), N, alpha))
+    ms, vs, aux = [], [], []
+    for i, L in enumerate(layers):
+        if i == 0:
+            m, v, kfu = fwd_det(L, xb)
+            aux.append(kfu)
+        else:
+            m, v, p1, p2 = fwd_mm(L, ms[-1], vs[-1])
+            aux.append((p1, p2))
+        ms.append(m)
+        vs.append(v)
+    logZ, dm, dv = gauss_logZ(ms[-1], vs[-1], yb, p['sn'], alpha)
+    dmi, dvi = scale * dm, scale * dv
+    grads = {}
+    for i in range(nl - 1, -1, -1):
+        L = layers[i]
+        if i == 0:
+            gh = bwd_det(L, N, alpha, dmi, dvi, aux[0], xb)
+        else:
+            gh, gi = bwd_mm(L, N, alpha, ms[i], dmi, dvi, aux[i][0], aux[i][1], ms[i - 1], vs[i - 1])
+            dmi, dvi = gi['mx'], gi['vx']
+        for k, val in gh.items():
+            grads['%s_%d' % (k, i)] = val
+    grads['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
+    energy = scale * logZ + sum(layer_phi(L, N, alpha) for L in layers)
+    return _finish(energy, grads, N, fixed)
+
+
+def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
+                     nat_param=True, fixed=()):
+    """``SGPLVM.objective_function`` aep_models.py:694-815 (MM; energy not divided by N)."""
+    N, Dy = y.shape
+    Mz, Dout = _layer_dims(p, '')
+    Q = np.asarray(p['x1']).shape[1]
+    if idx is None:
+        idx = np.arange(N)
+    yb = y[idx]
+    nb = yb.shape[0]
+    scale = -N / nb / alpha
+    L = layer_cavity(layer_unpack(p, '', Mz, Dout, nat_param), N, alpha)
+    f1 = np.asarray(p['x1'], dtype=float)
+    f2 = np.exp(2 * np.asarray(p['x2'], dtype=float))          # base_models.py:903-911
+    px1, px2 = prior_mean / prior_var, 1.0 / prior_var
+    if nat_param:
+        post1, post2 = px1 + f1, px2 + f2
+        c1 = px1 + (1.0 - alpha) * f1[idx]                       # aep_models.py:840-861
+        c2 = px2 + (1.0 - alpha) * f2[idx]
+    else:
+        post1, post2 = f1 / f2, 1.0 / f2
+        t1, t2 = f1[idx] / f2[idx], 1.0 / f2[idx]
+        c1 = px1 + (t1 - px1) * (1 - alpha)
+        c2 = px2 + (t2 - px2) * (1 - alpha)
+    mcav, vcav = c1 / c2, 1.0 / c2
+    mpost, vpost = post1[idx] / post2[idx], 1.0 / post2[idx]
+    m, v, p1, p2 = fwd_mm(L, mcav, vcav)
+    logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
+    gh, gi = bwd_mm(L, N, alpha, m, scale * dm, scale * dv, p1, p2, mcav, vcav)
+    grads = dict(gh)
+    grads['sn'] = gauss_dsn(dv, nb, Dy, p['sn'], alpha, scale)
+
+    def phi_x(mx, vx):                                           # aep_models.py:863-867
+        return np.sum(0.5 * (mx ** 2 / vx + np.log(vx))), mx / vx, 0.5 * (-mx ** 2 / vx ** 2 + 1 / vx)
+
+    phi_prior = phi_x(prior_mean, prior_var)[0] * N * Q
+    phi_cav, dmc, dvc = phi_x(mcav, vcav)
+    phi_post, dmp, dvp = phi_x(mpost, vpost)
+    sc_cav = -N / nb / alpha
+    sc_post = -N / nb * (1.0 - 1.0 / alpha)
+    xc = phi_prior + sc_cav * phi_cav + sc_post * phi_post
+    dmc = sc_cav * dmc + gi['mx']
+    dvc = sc_cav * dvc + gi['vx']
+    dmp, dvp = sc_post * dmp, sc_post * dvp
+    # compute_cav_grad_x aep_models.py:817-838
+    t1, t2 = mcav / vcav, 1.0 / vcav
+    dt1 = (1.0 - alpha) * dmc / t2
+    dt2 = (1.0 - alpha) * (-dmc * t1 / t2 ** 2 - dvc / t2 ** 2)
+    if nat_param:
+        dt2 = dt2 * 2 * f2[idx]
+    else:
+        mp_, vp_ = f1[idx], f2[idx]
+        dm_ = dt1 / vp_
+        dv_ = -dt1 * mp_ / vp_ ** 2 - dt2 / vp_ ** 2
+        dt1, dt2 = dm_, dv_ * 2 * f2[idx]
+    g1 = np.zeros_like(f1)
+    g2 = np.zeros_like(f1)
+    g1[idx], g2[idx] = dt1, dt2
+    # compute_posterior_grad_x base_models.py:913-929
+    h1 = np.zeros_like(f1)
+    h2 = np.zeros_like(f1)
+    if nat_param:
+        h1[idx] = dmp / post2[idx]
+        h2[idx] = (-dmp * post1[idx] / post2[idx] ** 2 - dvp / post2[idx] ** 2) * 2 * f2[idx]
+    else:
+        h1[idx] = dmp
+        h2[idx] = dvp * 2 * f2[idx]
+    grads['x1'] = g1 + h1
+    grads['x2'] = g2 + h2
+    energy = scale * logZ + xc + layer_phi(L, N, alpha)
+    return _finish(energy, grads, N, fixed, divide=False)
+
+
+def sgpssm_objective(y, p, alpha, start=None, mb_size=None, prior_mean=0.0, prior_var=1.0,
+                     fixed=()):
+    """``SGPSSM.objective_function`` aep_models.py:1024-1206, linear-Gaussian emission,
+    moment matching, no control inputs.  ``start`` is the window start when minibatching
+    (the reference draws it with ``np.random.randint``, aep_models.py:1051)."""
+    N, Dy = y.shape
+    Mz, Dx = _layer_dims(p, '_dynamic')
+    if mb_size is None or mb_size >= N:
+        emi = np.arange(0, N)
+        dyn = np.arange(0, N - 1)
+    else:
+        emi = np.arange(start, start + mb_size)
+        dyn = np.arange(start, start + mb_size - 1)
+    yb = y[emi]
+    s_dyn = -(N - 1) / dyn.shape[0] / alpha
+    s_emi = -N / emi.shape[0] / alpha
+    L = layer_cavity(layer_unpack(p, '_dynamic', Mz, Dx), N - 1, alpha)
+    f1 = np.asarray(p['x_factor_1'], dtype=float)
+    f2 = np.exp(2 * np.asarray(p['x_factor_2'], dtype=float))
+    px1, px2 = prior_mean / prior_var, 1.0 / prior_var
+    # base_models.py:1715-1725 posterior of x
+    post1, post2 = 3 * f1, 3 * f2
+    post1[[0, -1]] = 2 * f1[[0, -1]]
+    post2[[0, -1]] = 2 * f2[[0, -1]]
+    post1[0] += px1
+    post2[0] += px2
+    # aep_models.py:1376-1387 cavity of x
+    cav1 = post1 - alpha * f1
+    cav2 = post2 - alpha * f2
+    cm, cv = cav1 / (cav2 + 1e-16), 1.0 / (cav2 + 1e-16)
+    mt, vt = cm[dyn + 1], cv[dyn + 1]
+    mtm1, vtm1 = cm[dyn], cv[dyn]
+    mup, vup = cm[emi], cv[emi]
+    mprop, vprop, p1, p2 = fwd_mm(L, mtm1, vtm1)
+    # compute_transition_tilted aep_models.py:1317-1374 (2-D case)
+    sn = _scalar(p['sn'])
+    sn2 = np.exp(2 * sn)
+    vsum = vt + vprop + sn2 / alpha
+    md = mt - mprop
+    logZd = (-0.5 * md ** 2 / vsum - 0.5 * np.log(1 + alpha * (vt + vprop) / sn2)
+             - 0.5 * alpha * np.log(2 * np.pi * sn2))
+    logZ_dyn = s_dyn * np.sum(logZd)
+    dvt = s_dyn * (-0.5 / vsum + 0.5 * md ** 2 / vsum ** 2)
+    dvprop = dvt
+    dmt = s_dyn * (-md / vsum)
+    dmprop = -dmt
+    dsn = dvt.sum() * 2 * sn2 / alpha + s_dyn * mprop.shape[0] * Dx * (1 - alpha)
+    gh, gi = bwd_mm(L, N - 1, alpha, mprop, dmprop, dvprop, p1, p2, mtm1, vtm1)
+    logZ_emi, ge_in, ge_hyp = emission_tilted(np.asarray(p['C_emission'], dtype=float),
+                                              p['R_emission'], y[emi], mup, vup, alpha, s_emi)
+    grads = {'sn': dsn}
+    for k, val in gh.items():
+        grads[k + '_dynamic'] = val
+    for k, val in ge_hyp.items():
+        grads[k + '_emission'] = val
+    # gradients w.r.t. the x factors: aep_models.py:1208-1315
+    sp = -(1.0 - 1.0 / alpha) * np.ones((N, 1))
+    sp[0:N - 1] += 1.0 / alpha
+    sp[1:N] += 1.0 / alpha
+    gp1 = sp * (post1 / post2)
+    gp2 = sp * (-0.5 * post1 ** 2 / post2 ** 2 - 0.5 / post2)
+    post_g1 = 3.0 * gp1
+    post_g2 = 6.0 * gp2 * f2
+    post_g1[[0, -1]] = 2.0 * gp1[[0, -1]]
+    post_g2[[0, -1]] = 4.0 * gp2[[0, -1]] * f2[[0, -1]]
+    scx = (3.0 - alpha) * np.ones((N, 1))
+    scx[0] = scx[-1] = 2.0 - alpha
+    sc = -1.0 / alpha * np.ones((N, 1))
+    sc[0:N - 1] += -1.0 / alpha
+    sc[1:N] += -1.0 / alpha
+    cav_g1 = sc * (cav1 / cav2) * scx
+    cav_g2 = sc * (-0.5 * cav1 ** 2 / cav2 ** 2 - 0.5 / cav2) * scx * 2 * f2
+    z1 = np.zeros_like(cav1)
+    z2 = np.zeros_like(cav1)
+
+    def acc(ix, dmc, dvc):
+        z1[ix] += dmc / cav2[ix]
+        z2[ix] += -dmc * cav1[ix] / cav2[ix] ** 2 - dvc / cav2[ix] ** 2
+
+    acc(emi, ge_in['mx'][:, :Dx], ge_in['vx'][:, :Dx])
+    acc(np.arange(emi[0] + 1, emi[-1] + 1), dmt, dvt)
+    acc(np.arange(emi[0], emi[-1]), gi['mx'][:, :Dx], gi['vx'][:, :Dx])
+    lz_g1 = z1 * scx
+    lz_g2 = z2 * scx * 2 * f2
+    grads['x_factor_1'] = post_g1 + cav_g1 + lz_g1
+    grads['x_factor_2'] = post_g2 + cav_g2 + lz_g2
+    # energy terms aep_models.py:1389-1437
+    phi_prior_x = 0.5 * Dx * ((px1 / px2) ** 2 * px2 + np.log(1.0 / px2))
+    phi_post_x = np.sum(sp * 0.5 * (post1 ** 2 / post2 - np.log(post2)))
+    phi_cav_x = np.sum(sc * 0.5 * (cav1 ** 2 / cav2 - np.log(cav2)))
+    energy = logZ_dyn + logZ_emi + phi_prior_x + phi_post_x + phi_cav_x + layer_phi(L, N - 1, alpha)
+    return _finish(energy, grads, N, fixed)
+
+
+# --------------------------------------------------------------------------
+# prediction (base_models.py)
+# --------------------------------------------------------------------------
+
+def sgpr_predict(p, xs, nat_param=True):
+    """``Base_SGPR.predict_f/predict_y`` base_models.py:985-1034 -> (mf, vf, my, vy)."""
+    Mz, Dout = _layer_dims(p, '')
+    L = layer_unpack(p, '', Mz, Dout, nat_param)
+    mf, vf, _ = fwd_det(L, xs, cav=False)
+    return mf, vf, mf, vf + np.exp(2.0 * _scalar(p['sn']))
+
+
+def sdgpr_predict(p, xs):
+    """``Base_SDGPR.predict_f_mm/predict_y`` base_models.py:1140-1158, 1264-1275."""
+    i = 0
+    mf = vf = None
+    while ('eta2_%d' % i) in p:
+        Mz, Dout = _layer_dims(p, '_%d' % i)
+        L = layer_unpack(p, '_%d' % i, Mz, Dout)
+        if i == 0:
+            mf, vf, _ = fwd_det(L, xs, cav=False)
+        else:
+            mf, vf, _, _ = fwd_mm(L, mf, vf, cav=False)
+        i += 1
+    return mf, vf, mf, vf + np.exp(2.0 * _scalar(p['sn']))
+
+
+# --------------------------------------------------------------------------
+# utils.py
+# --------------------------------------------------------------------------
+
+def flatten(params):
+    """``flatten_dict`` utils.py:68-81 (sorted keys)."""
+    keys = sorted(params.keys())
+    vec = np.concatenate([np.ravel(np.asarray(params[k], dtype=float)) for k in keys])
+    return vec, keys

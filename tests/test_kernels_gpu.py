@@ -1,0 +1,192 @@
+"""GPU parity of the libgpk kernels against the float64 oracle (small sizes)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import geepee_np as O
+from tests._helpers import load, assert_close
+
+pytestmark = pytest.mark.gpu
+
+DF64_TOL = 1e-10   # double-float (~48-bit) arithmetic against float64
+FP32_TOL = 1e-5    # FP32 psi statistics (spec tolerance)
+
+
+def dev(a, dtype=torch.float64):
+    return torch.as_tensor(np.asarray(a, dtype=np.float64), device='cuda').to(dtype).contiguous()
+
+
+def test_kernel_matrix_golden():
+    from geepee_gb300 import kernels as K
+    g = load('kernels_small.npz')
+    assert_close(K.compute_kernel(g['k_lls'], g['k_lsf'], g['k_x'], g['k_z']), g['k_out'], DF64_TOL)
+
+
+def test_psi_stats_golden():
+    from geepee_gb300 import kernels as K
+    g = load('kernels_small.npz')
+    p1, p2 = K.compute_psi_weave(g['p_lls2'], g['p_lsf2'], g['p_mu'], g['p_S'], g['p_Z'])
+    assert_close(p1, g['p_psi1_weave'], DF64_TOL, 'psi1')
+    assert_close(p2, g['p_psi2_weave'], DF64_TOL, 'psi2')
+
+
+@pytest.mark.parametrize('tag', ['n', 's'])
+def test_psi_derivatives_golden(tag):
+    from geepee_gb300 import kernels as K
+    g = load('kernels_small.npz')
+    ell = np.exp(0.5 * g['p_lls2'])
+    sf2 = float(np.exp(g['p_lsf2'][0]))
+    dpsi2 = g['d_dpsi2_n'] if tag == 'n' else g['d_dpsi2_s']
+    r = K.compute_psi_derivatives(g['d_dpsi1'], g['p_psi1'], dpsi2, g['p_psi2'], ell, sf2,
+                                  g['p_mu'], g['p_S'], g['p_Z'])
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dmu', 'dS'), r):
+        assert_close(val, g['d_%s_%s' % (tag, name)], 1e-9, name)
+
+
+def test_kfu_derivatives_and_trace_golden():
+    from geepee_gb300 import kernels as K
+    g = load('kernels_small.npz')
+    ell = np.exp(0.5 * g['p_lls2'])
+    sf2 = float(np.exp(g['p_lsf2'][0]))
+    r = K.compute_kfu_derivatives(g['f_dkfu'], g['f_kfu'], ell, sf2, g['p_mu'], g['p_Z'], grad_x=True)
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dx'), r):
+        assert_close(val, g['f_' + name], 1e-9, name)
+    t = K.d_trace_MKzz_dhypers(g['p_lls2'], g['p_lsf2'], g['p_Z'], g['t_M'], g['t_Kzz'])
+    for name, val in zip(('lsf', 'lls', 'z'), t):
+        assert_close(val, g['t_' + name], 1e-9, name)
+
+
+@pytest.mark.parametrize('M,Q,Dout,N', [(24, 5, 2, 200), (1, 1, 1, 3), (33, 3, 1, 17), (100, 2, 1, 300),
+                                        (128, 8, 3, 40)])
+def test_psi_fused_fwd_bwd_vs_oracle(M, Q, Dout, N):
+    from geepee_gb300 import gpk, workloads as W
+    wl = W.psi_workload(seed=M + Q, N=N, Q=Q, M=M, Dout=Dout)
+    lls2, lsf2 = 2 * wl['ls'], 2 * wl['sf']
+    p1, p2 = O.psi_stats(lls2, lsf2, wl['mu'], wl['S'], wl['Z'])
+    A, B = wl['Ahat'], wl['Bhat']
+    sf2 = float(np.exp(lsf2[0]))
+    m_ref = p1 @ A.T
+    v_ref = sf2 + np.einsum('dab,nab->nd', B, p2) - m_ref ** 2
+    mu, S, Z = dev(wl['mu']), dev(wl['S']), dev(wl['Z'])
+    l2, s2, At, Bt = dev(lls2), dev(lsf2), dev(A), dev(B)
+    m = torch.empty((N, Dout), dtype=torch.float64, device='cuda')
+    v = torch.empty_like(m)
+    psi1 = torch.empty((N, M), dtype=torch.float64, device='cuda')
+    ssum = torch.zeros((M, M), dtype=torch.float64, device='cuda')
+    gpk.psi_fwd(mu, S, Z, l2, s2, At, Bt, psi1=psi1, psi2_sum=ssum, m_out=m, v_out=v)
+    assert_close(psi1.cpu().numpy(), p1, DF64_TOL, 'psi1')
+    assert_close(ssum.cpu().numpy(), p2.sum(0), DF64_TOL, 'psi2 sum')
+    assert_close(m.cpu().numpy(), m_ref, DF64_TOL, 'm')
+    assert_close(v.cpu().numpy(), v_ref, DF64_TOL, 'v')
+    # backward
+    dm, dv = wl['dm'], wl['dv']
+    dm_all = dm - 2 * dv * m_ref
+    r = O.psi_derivatives(dm_all @ A, p1, np.einsum('nd,dab->nab', dv, B), p2, np.exp(wl['ls']), sf2,
+                          wl['mu'], wl['S'], wl['Z'])
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    out = dict(dsf2=z(1), dl=z(Q), dZ=z(M, Q), dA=z(Dout, M), dB=z(Dout, M, M),
+               dmu=z(N, Q), dS=z(N, Q))
+    gpk.psi_bwd(mu, S, Z, l2, s2, At, Bt, dev(m_ref), dev(dm), dev(dv), out['dsf2'], out['dl'], out['dZ'],
+                out['dA'], out['dB'], out['dmu'], out['dS'])
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dmu', 'dS'), r):
+        assert_close(out[name].cpu().numpy(), val, 1e-9, name)
+    assert_close(out['dA'].cpu().numpy(), dm_all.T @ p1, 1e-9, 'dA')
+    assert_close(out['dB'].cpu().numpy(), np.einsum('nd,nab->dab', dv, p2), 1e-9, 'dB')
+
+
+def test_psi_fp32_within_tolerance():
+    from geepee_gb300 import gpk, workloads as W
+    g = load('psi_reduced.npz')
+    wl = W.psi_workload(seed=5, N=200, Q=5, M=24, Dout=2)
+    f = lambda a: dev(a, torch.float32)
+    N, M = 200, 24
+    psi1 = torch.empty((N, M), dtype=torch.float32, device='cuda')
+    ssum = torch.zeros((M, M), dtype=torch.float64, device='cuda')
+    v = torch.empty((N, 2), dtype=torch.float32, device='cuda')
+    m = torch.empty_like(v)
+    gpk.psi_fwd(f(wl['mu']), f(wl['S']), f(wl['Z']), dev(2 * wl['ls']), dev(2 * wl['sf']), f(wl['Ahat']),
+                f(wl['Bhat']), psi1=psi1, psi2_sum=ssum, m_out=m, v_out=v)
+    assert_close(psi1.double().cpu().numpy(), g['psi1'], FP32_TOL, 'psi1 fp32')
+    assert_close(ssum.cpu().numpy(), g['psi2_sum'], FP32_TOL, 'psi2 sum fp32')
+
+
+@pytest.mark.parametrize('M', [1, 7, 64, 100, 128])
+def test_chol_inv_logdet(M):
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(M)
+    Z = rng.randn(M, 2)
+    K = O.ard_kernel(np.zeros(2), 0.0, Z, Z) + 1e-5 * np.eye(M)
+    A = np.stack([K, K + np.diag(rng.rand(M))])
+    At = dev(A)
+    inv = torch.empty_like(At)
+    L = torch.empty_like(At)
+    ld = torch.empty(2, dtype=torch.float64, device='cuda')
+    info = torch.empty(2, dtype=torch.int32, device='cuda')
+    gpk.chol_inv(At, inv, L, ld, info)
+    assert info.cpu().numpy().tolist() == [0, 0]
+    for b in range(2):
+        ref_inv = np.linalg.inv(A[b])
+        cond = np.linalg.cond(A[b])
+        assert_close(inv[b].cpu().numpy(), ref_inv, max(1e-12, 1e-13 * cond), 'inv')
+        assert abs(ld[b].item() - np.linalg.slogdet(A[b])[1]) <= 1e-9 * max(1, abs(np.linalg.slogdet(A[b])[1]))
+        assert_close(L[b].cpu().numpy(), np.linalg.cholesky(A[b]), 1e-12, 'L')
+
+
+def test_chol_reports_non_pd():
+    from geepee_gb300 import gpk
+    A = dev(np.array([[[1.0, 2.0], [2.0, 1.0]]]))
+    info = torch.empty(1, dtype=torch.int32, device='cuda')
+    gpk.chol_inv(A, torch.empty_like(A), None, None, info)
+    assert info.item() == 2
+
+
+@pytest.mark.parametrize('m,n,k,tA,tB', [(100, 100, 100, False, False), (37, 5, 64, True, False),
+                                         (3, 130, 17, False, True), (64, 64, 1, True, True)])
+def test_gemm(m, n, k, tA, tB):
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(m + n + k)
+    A = rng.randn(k, m) if tA else rng.randn(m, k)
+    B = rng.randn(n, k) if tB else rng.randn(k, n)
+    C0 = rng.randn(m, n)
+    ref = 0.5 * (A.T if tA else A) @ (B.T if tB else B) - 2.0 * C0
+    C = dev(C0)
+    gpk.gemm(dev(A), dev(B), C, alpha=0.5, beta=-2.0, tA=tA, tB=tB)
+    assert_close(C.cpu().numpy(), ref, 1e-12)
+
+
+def test_det_layer_fwd_bwd_vs_oracle():
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(3)
+    N, M, D, Dout = 301, 30, 8, 2
+    x, Z = rng.randn(N, D), rng.randn(M, D)
+    ls, sf = rng.uniform(-0.3, 0.5, D), np.array([0.2])
+    A = rng.randn(Dout, M)
+    B = rng.randn(Dout, M, M)
+    kfu = O.ard_kernel(2 * ls, 2 * sf, x, Z)
+    m_ref = kfu @ A.T
+    v_ref = np.exp(2 * sf) + np.einsum('dab,na,nb->nd', B, kfu, kfu)
+    xt, Zt, At, Bt = dev(x), dev(Z), dev(A), dev(B)
+    l2, s2 = dev(2 * ls), dev(2 * sf)
+    kt = torch.empty((N, M), dtype=torch.float64, device='cuda')
+    Bk = torch.empty((N, Dout, M), dtype=torch.float64, device='cuda')
+    m = torch.empty((N, Dout), dtype=torch.float64, device='cuda')
+    v = torch.empty_like(m)
+    gpk.det_fwd(xt, Zt, l2, s2, At, Bt, kt, Bk, m, v)
+    assert_close(kt.cpu().numpy(), kfu, DF64_TOL, 'kfu')
+    assert_close(m.cpu().numpy(), m_ref, DF64_TOL, 'm')
+    assert_close(v.cpu().numpy(), v_ref, DF64_TOL, 'v')
+    dm, dv = rng.randn(N, Dout), rng.randn(N, Dout)
+    dkfu = dm @ A + 2 * np.einsum('nd,dab,na->nb', dv, B, kfu)
+    r = O.kfu_derivatives(dkfu, kfu, np.exp(ls), float(np.exp(2 * sf[0])), x, Z)
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    dsf2, dl, dZ, dA = z(1), z(D), z(M, D), z(Dout, M)
+    gpk.det_bwd(xt, Zt, l2, s2, At, kt, Bk, dev(dm), dev(dv), dsf2, dl, dZ, dA)
+    for name, got, val in (('dsf2', dsf2, r[0]), ('dl', dl, r[1]), ('dZ', dZ, r[2])):
+        assert_close(got.cpu().numpy(), val, 1e-9, name)
+    assert_close(dA.cpu().numpy(), dm.T @ kfu, 1e-10, 'dA')
+    C = z(Dout, M, M)
+    gpk.gram(kt, kt, dev(dv), C)
+    assert_close(C.cpu().numpy(), np.einsum('nd,na,nb->dab', dv, kfu, kfu), 1e-10, 'gram')
+    c = z(Dout, M)
+    gpk.wsum(kt, dev(dm), c)
+    assert_close(c.cpu().numpy(), dm.T @ kfu, 1e-10, 'wsum')

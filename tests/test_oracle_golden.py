@@ -1,0 +1,133 @@
+"""Pin the CPU oracle against fixtures produced by the reference's own code."""
+import numpy as np
+import pytest
+
+from oracle import geepee_np as O
+from tests._helpers import load, sub, assert_close, assert_dict_close, noise_floor, assert_grads_close, assert_truth_close
+
+TOL = 1e-10   # float64 vs float64, different operation order
+
+
+def test_kernel_matrix():
+    g = load('kernels_small.npz')
+    assert_close(O.ard_kernel(g['k_lls'], g['k_lsf'], g['k_x'], g['k_z']), g['k_out'], TOL)
+
+
+def test_psi_stats_match_reference_and_weave_loop():
+    g = load('kernels_small.npz')
+    p1, p2 = O.psi_stats(g['p_lls2'], g['p_lsf2'], g['p_mu'], g['p_S'], g['p_Z'])
+    assert_close(p1, g['p_psi1'], TOL)
+    assert_close(p2, g['p_psi2'], TOL)
+    # the reference's own native (weave) loop, compiled from kernels.py:201-234
+    assert_close(p1, g['p_psi1_weave'], TOL)
+    assert_close(p2, g['p_psi2_weave'], TOL)
+
+
+@pytest.mark.parametrize('tag', ['n', 's'])
+def test_psi_derivatives(tag):
+    g = load('kernels_small.npz')
+    p1, p2 = g['p_psi1'], g['p_psi2']
+    ell = np.exp(0.5 * g['p_lls2'])
+    sf2 = float(np.exp(g['p_lsf2'][0]))
+    dpsi2 = g['d_dpsi2_n'] if tag == 'n' else g['d_dpsi2_s']
+    r = O.psi_derivatives(g['d_dpsi1'], p1, dpsi2, p2, ell, sf2, g['p_mu'], g['p_S'], g['p_Z'])
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dmu', 'dS'), r):
+        assert_close(val, g['d_%s_%s' % (tag, name)], TOL, name)
+
+
+def test_kfu_derivatives_and_trace():
+    g = load('kernels_small.npz')
+    ell = np.exp(0.5 * g['p_lls2'])
+    sf2 = float(np.exp(g['p_lsf2'][0]))
+    r = O.kfu_derivatives(g['f_dkfu'], g['f_kfu'], ell, sf2, g['p_mu'], g['p_Z'], grad_x=True)
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dx'), r):
+        assert_close(val, g['f_' + name], TOL, name)
+    t = O.trace_kzz_grads(g['p_lls2'], g['p_lsf2'], g['p_Z'], g['t_M'], g['t_Kzz'])
+    for name, val in zip(('lsf', 'lls', 'z'), t):
+        assert_close(val, g['t_' + name], TOL, name)
+
+
+def test_psi_workload_reduced():
+    from geepee_gb300 import workloads as W
+    g = load('psi_reduced.npz')
+    wl = W.psi_workload(seed=5, N=200, Q=5, M=24, Dout=2)
+    p1, p2 = O.psi_stats(2 * wl['ls'], 2 * wl['sf'], wl['mu'], wl['S'], wl['Z'])
+    assert_close(p1, g['psi1'], TOL)
+    assert_close(p2.sum(0), g['psi2_sum'], TOL)
+    dpsi2 = np.einsum('nd,dab->nab', wl['dv'], wl['Bhat'])
+    r = O.psi_derivatives(wl['dm'] @ wl['Ahat'], p1, dpsi2, p2, np.exp(wl['ls']),
+                          float(np.exp(2 * wl['sf'][0])), wl['mu'], wl['S'], wl['Z'])
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dmu', 'dS'), r):
+        assert_close(val, g[name], TOL, name)
+
+
+def test_sgpr_c1():
+    from geepee_gb300 import workloads as W
+    g = load('sgpr_c1.npz')
+    x, y, params, xs = W.sgpr_1d(seed=0)
+    e, gr = O.sgpr_objective(x, y, params, 0.5)
+    assert abs(e - g["energy"]) <= 1e-8 * abs(g["energy"])
+    assert_truth_close(gr, sub(g, 'g_'), sub(g, 't_'), 1e-8, what='sgpr')
+    e, gr = O.sgpr_objective(x, y, params, 0.5, idx=g['mb_idx'])
+    assert abs(e - g["energy_mb"]) <= 1e-8 * abs(g["energy_mb"])
+    fl = noise_floor(lambda p: O.sgpr_objective(x, y, p, 0.5, idx=g['mb_idx']), params)
+    assert_grads_close(gr, sub(g, 'gmb_'), fl, 1e-8, 100, 'sgpr mb')
+    mf, vf, my, vy = O.sgpr_predict(params, xs)
+    for k, v in dict(mf=mf, vf=vf, my=my, vy=vy).items():
+        assert_close(v, g[k], 1e-9, k)
+
+
+@pytest.mark.parametrize('nat', [1, 0])
+def test_sgpr_small(nat):
+    g = load('sgpr_small_nat%d.npz' % nat)
+    e, gr = O.sgpr_objective(g['x'], g['y'], sub(g, 'p_'), 0.3, nat_param=bool(nat))
+    assert abs(e - g['energy']) <= 1e-9 * abs(g['energy'])
+    assert_dict_close(gr, sub(g, 'g_'), 1e-7, 'sgpr small')
+
+
+def test_sdgpr_small():
+    g = load('sdgpr_small.npz')
+    p = sub(g, 'p_')
+    e, gr = O.sdgpr_objective(g['x'], g['y'], p, 1.0)
+    assert abs(e - g['energy']) <= 1e-9 * abs(g['energy'])
+    assert_dict_close(gr, sub(g, 'g_'), 1e-7, 'sdgpr small')
+    mf, vf, my, vy = O.sdgpr_predict(p, g['xs'])
+    for k, v in dict(mf=mf, vf=vf, my=my, vy=vy).items():
+        assert_close(v, g[k], 1e-9, k)
+
+
+def test_sdgpr_c3():
+    from geepee_gb300 import workloads as W
+    g = load('sdgpr_c3.npz')
+    x, y = W.dgp_regression(seed=0)
+    p = sub(g, 'p_')
+    e, gr = O.sdgpr_objective(x, y, p, 0.5, idx=g['mb_idx'])
+    assert abs(e - g['energy']) <= 1e-8 * abs(g['energy'])
+    assert abs(e - g['t_energy']) <= 1e-8 * abs(g['t_energy'])
+    assert_truth_close(gr, sub(g, 'g_'), sub(g, 't_'), 1e-8, what='sdgpr c3')
+    mf, vf, my, vy = O.sdgpr_predict(p, x[:int(g['n_test'])])
+    for k, v in dict(mf=mf, vf=vf, my=my, vy=vy).items():
+        assert_close(v, g[k], 1e-8, k)
+
+
+@pytest.mark.parametrize('nat', [1, 0])
+def test_sgplvm_small(nat):
+    g = load('sgplvm_small_nat%d.npz' % nat)
+    p = sub(g, 'p_')
+    e, gr = O.sgplvm_objective(g['y'], p, 0.5, nat_param=bool(nat))
+    assert abs(e - g['energy']) <= 1e-9 * abs(g['energy'])
+    assert_dict_close(gr, sub(g, 'g_'), 1e-7, 'sgplvm')
+    e, gr = O.sgplvm_objective(g['y'], p, 0.5, idx=g['mb_idx'], nat_param=bool(nat))
+    assert abs(e - g['energy_mb']) <= 1e-9 * abs(g['energy_mb'])
+    assert_dict_close(gr, sub(g, 'gmb_'), 1e-7, 'sgplvm mb')
+
+
+def test_sgpssm_small():
+    g = load('sgpssm_small.npz')
+    p = sub(g, 'p_')
+    e, gr = O.sgpssm_objective(g['y'], p, 0.5)
+    assert abs(e - g['energy']) <= 1e-9 * abs(g['energy'])
+    assert_truth_close(gr, sub(g, 'g_'), sub(g, 't_'), 1e-8, what='sgpssm')
+    e, gr = O.sgpssm_objective(g['y'], p, 0.5, start=int(g['mb_start']), mb_size=20)
+    assert abs(e - g['energy_mb']) <= 1e-9 * abs(g['energy_mb'])
+    assert_dict_close(gr, sub(g, 'gmb_'), 1e-6, 'sgpssm mb')
