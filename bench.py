@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark: objective+gradient evaluations/s of the 2-layer deep-GP AEP model
+(N=20000 inputs x~N(0,I_8), hidden width 2, M=100 pseudo-inputs per layer, minibatch 1000,
+alpha=0.5) on one GB300, against the plain FP64 GPU form and the reference's CPU path.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).  Under torchrun each rank runs an independent replica
+(the objective does not shard: replicas only) and the reported value is the sum over
+ranks of evaluations divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRAIN, D_IN, HIDDEN, M_PSEUDO, MB, ALPHA = 20000, 8, 2, 100, 1000, 0.5
+METRIC = 'obj+grad evals/s (DGP N=20k,M=100)'
+WORKLOAD = ('2-layer deep GP regression, AEP alpha=0.5: N=20000, x~N(0,I_8), hidden 2, M=100 per layer, '
+            'minibatch 1000, y=tanh(W2 sin(W1 x))+N(0,0.05^2)')
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=50)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def workload(seed=0):
+    from geepee_gb300 import workloads as W
+    x, y = W.dgp_regression(seed=seed, N=N_TRAIN, D=D_IN, hidden=HIDDEN)
+    return x, y
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix='.csv')
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(gpu_index), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(smax) if smax else None,
+                'samples': len(sm), 'reasons': sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------- CPU baselines
+def reference_module():
+    """The reference's own code (Python 3 shim built by oracle/make_ref.py into oracle/_ref),
+    else None."""
+    ref = os.path.join(ROOT, 'oracle', '_ref')
+    if not os.path.isdir(os.path.join(ref, 'geepee_ref')):
+        return None
+    sys.path.insert(0, ref)
+    try:
+        from geepee_ref import aep_models
+        return aep_models
+    except Exception:
+        return None
+
+
+def cpu_eval_rate(x, y, params, idx_list, seconds):
+    """Time the reference's CPU objective (or the oracle port) on a bounded sample."""
+    aep = reference_module()
+    if aep is not None:
+        mdl = aep.SDGPR(x, y, M_PSEUDO, [HIDDEN], lik='Gaussian')
+        kind = 'reference'
+
+        def one(i):
+            np.random.seed(1000 + i)
+            mdl.objective_function({k: np.copy(v) for k, v in params.items()}, MB, alpha=ALPHA)
+    else:
+        from oracle import geepee_np as O
+        kind = 'port'
+
+        def one(i):
+            O.sdgpr_objective(x, y, params, ALPHA, idx=idx_list[i % len(idx_list)])
+    one(0)
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < seconds and n < 200:
+        one(n + 1)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, kind, n, dt
+
+
+# ----------------------------------------------------------------------------- roofline helpers
+def df64_ops_psi_bwd(N, M, Q, D):
+    """FP32-pipe operations of the df64 psi backward per launch: the reference formula's
+    float64 operations, each weighted by the FP32-instruction cost of its double-float
+    implementation (add 11, mul 7, fma 18, exp 45, log 60, div 40)."""
+    P = M * (M + 1) // 2
+    add, mul, fma, exp_ = 11, 7, 18, 45
+    pair = (2 * add + Q * fma + add + exp_) + D * (add + fma) + D * fma + mul + add
+    row = 2 * (add + Q * fma)                       # row-sum pass, two entries per pair
+    per_a = exp_ + Q * (4 * add + 6 * mul + 3 * fma) + D * 2 * fma
+    return N * (P * (pair + row) + M * per_a)
+
+
+def psi_bwd_bytes(N, M, Q, D):
+    """Algorithmic HBM bytes: read mu, var, m, dm, dv; write dmu, dvar; read Z, A, B once."""
+    return 8 * (N * (2 * Q + 3 * D + 2 * Q) + M * Q + D * M + D * M * M)
+
+
+# ----------------------------------------------------------------------------- our implementation
+def run_ours(args, world, rank, local):
+    import torch
+    from geepee_gb300 import aep_models as A, fp64_form, _lib
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    x, y = workload()
+    np.random.seed(1)
+    mdl = A.SDGPR(x, y, M_PSEUDO, [HIDDEN])
+    params = mdl.init_hypers(y)
+    K, W = args.steps, args.warmup
+    rng = np.random.RandomState(123 + rank)
+    idx_np = np.stack([rng.choice(N_TRAIN, MB, replace=False) for _ in range(W + K)])
+    idx_all = torch.as_tensor(idx_np, dtype=torch.int64, device=dev)
+
+    # ---- kernel launch count per evaluation (our kernels only): count C-ABI calls eagerly
+    calls = {'n': 0}
+    orig_call = _lib.call
+
+    def counting(name, *a):
+        calls['n'] += 1
+        return orig_call(name, *a)
+    _lib.call = counting
+    import geepee_gb300.gpk as G
+    G.call = counting
+    mdl.update_hypers(params)
+    mdl.use_graphs = False
+    mdl._idx_buf = idx_all[0].clone()
+    mdl.device_objective(mdl._idx_buf, ALPHA)
+    torch.cuda.synchronize()
+    launches_per_eval = calls['n']
+    _lib.call = orig_call
+    G.call = orig_call
+    mdl.use_graphs = True
+
+    # ---- device-resident value: graph replay, L2 flushed between timed steps
+    flush = torch.empty(int(256 * 2 ** 20 // 4), dtype=torch.float32, device=dev)
+    mdl.update_hypers(params)
+    step = lambda: mdl.device_objective(mdl._idx_buf, ALPHA)
+    key = ('mb', MB, ALPHA)
+    mdl._run(key, step)
+    for i in range(W):
+        mdl._idx_buf.copy_(idx_all[i])
+        mdl._run(key, step)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = Clocks(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    torch.cuda.synchronize()
+    for i in range(K):
+        flush.fill_(float(i))
+        ev[i][0].record()
+        mdl._idx_buf.copy_(idx_all[W + i])
+        mdl._run(key, step)
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_dev], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * K / t_dev
+
+    # ---- parity of the first timed step against the oracle (energy)
+    mdl._idx_buf.copy_(idx_all[W])
+    mdl._run(key, step)
+    e_gpu = float(mdl.energy.item())
+
+    # ---- end to end through the public API (host params in, host gradients out)
+    e2e_steps = max(5, K // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        np.random.seed(10 + i)
+        mdl.objective_function(params, MB, alpha=ALPHA)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    clocks = clk.stop()
+    e2e = {'value': world * e2e_steps / t_e2e, 'unit': 'evals/s', 'steps': e2e_steps,
+           'h2d_bytes_per_step': mdl.ppack.nbytes() + MB * 8,
+           'd2h_bytes_per_step': mdl.gpack.nbytes(),
+           'path': 'SDGPR.objective_function(params: dict[np.ndarray], mb_size=1000, alpha=0.5) -> (float, dict)'}
+
+    # ---- plain FP64 GPU form on the same parameters / minibatches
+    pt = {k: torch.as_tensor(np.asarray(v, dtype=np.float64), device=dev) for k, v in params.items()}
+    xd = torch.as_tensor(x, device=dev)
+    yd = torch.as_tensor(y, device=dev)
+    n64 = max(1, min(10, K))
+    for i in range(2):
+        fp64_form.sdgpr_objective(pt, xd, yd, idx_all[i], ALPHA, 2)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(n64):
+        fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W + i], ALPHA, 2)
+    e1.record()
+    torch.cuda.synchronize()
+    fp64_rate = n64 / (e0.elapsed_time(e1) / 1e3)
+    e64, _ = fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W], ALPHA, 2)
+
+    # ---- dominant kernel roofline: psi backward of layer 1 on this step's inputs
+    lay1 = mdl.layers[1]
+    lay0 = mdl.layers[0]
+    xb = xd.index_select(0, idx_all[W])
+    m0, v0, _, _ = lay0.fwd_det(xb)
+    m1, v1 = lay1.fwd_mm(m0, v0)
+    from geepee_gb300 import gpk
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device=dev)
+    dm, dv = torch.randn_like(m1), torch.randn_like(m1)
+    bufs = (z(1), z(2), z(M_PSEUDO, 2), z(1, M_PSEUDO), z(1, M_PSEUDO, M_PSEUDO), z(MB, 2), z(MB, 2))
+    run_k = lambda: gpk.psi_bwd(m0, v0, lay1.zu, lay1.lls2, lay1.lsf2, lay1.Ah, lay1.Bh_sto, m1, dm, dv, *bufs)
+    for _ in range(3):
+        run_k()
+    reps = 50
+    ks = torch.cuda.Event(enable_timing=True)
+    ke = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ks.record()
+    for _ in range(reps):
+        run_k()
+    ke.record()
+    torch.cuda.synchronize()
+    t_k = ks.elapsed_time(ke) / 1e3 / reps
+    ops = df64_ops_psi_bwd(MB, M_PSEUDO, HIDDEN, 1)
+    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
+        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
+    sm_mhz = peaks.get('sm_max_mhz', 2070.0)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12
+    achieved = ops / t_k / 1e12
+    roofline = {'kernel': 'psi_bwd_kernel<df64> (layer 2, 1000 points, M=100, Q=2)',
+                'bound': 'fp32-pipe', 'achieved': round(achieved, 3), 'peak': round(fp32_peak, 1),
+                'unit': 'TFLOP/s', 'frac': round(achieved / fp32_peak, 4),
+                'peak_source': 'nominal: %d SMs x 128 FP32 lanes x 2 x %.0f MHz (max SM clock, '
+                               'MEASURED_PEAKS.json); no measured FP32 peak exists' % (n_sm, sm_mhz),
+                'work_per_launch': ops, 'us_per_launch': round(t_k * 1e6, 2),
+                'hbm_algorithmic_gbs': round(psi_bwd_bytes(MB, M_PSEUDO, HIDDEN, 1) / t_k / 1e9, 2),
+                'hbm_peak_gbs': peaks.get('hbm_gbs'), 'traffic': None}
+    out = {'e_gpu': e_gpu, 'e_fp64': float(e64.item()), 'value': value, 'ms': 1e3 * t_dev / K,
+           'e2e': e2e, 'fp64_rate': fp64_rate, 'n64': n64, 'roofline': roofline, 'clocks': clocks,
+           'launches_per_eval': launches_per_eval, 'params': params, 'x': x, 'y': y,
+           'idx0': idx_np[W]}
+    return out
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group('nccl' if args.impl == 'ours' else 'gloo')
+    if args.impl == 'reference':
+        if rank == 0:
+            x, y = workload()
+            np.random.seed(1)
+            from geepee_gb300.aep_models import layer_init_hypers
+            params = {}
+            params.update(layer_init_hypers(N_TRAIN, M_PSEUDO, D_IN, HIDDEN, True, x, '_0'))
+            params.update(layer_init_hypers(N_TRAIN, M_PSEUDO, HIDDEN, 1, True, None, '_1'))
+            params['sn'] = np.log(0.01)
+            rng = np.random.RandomState(7)
+            idx = [rng.choice(N_TRAIN, MB, replace=False) for _ in range(4)]
+            secs = max(5.0, min(args.cpu_seconds * 4, 60.0))
+            rate, kind, n, dt = cpu_eval_rate(x, y, params, idx, secs)
+            line = {'metric': METRIC, 'value': rate, 'unit': 'evals/s', 'n_gpus': args.gpus,
+                    'steps': n, 'warmup': 1, 'ms_per_step': 1e3 / rate, 'higher_is_better': True,
+                    'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+                    'impl': 'reference',
+                    'config': {'workload': WORKLOAD, 'N': N_TRAIN, 'M': M_PSEUDO, 'minibatch': MB,
+                               'alpha': ALPHA},
+                    'cpu_baseline': {'value': rate, 'unit': 'evals/s', 'cores': os.cpu_count(), 'kind': kind,
+                                     'sample': '%d objective+gradient evaluations (%.1f s) of the reference '
+                                               'numpy path on the host cores, BLAS threads = all' % (n, dt)},
+                    'e2e': {'value': rate, 'unit': 'evals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+            print(json.dumps(line))
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+        return
+    r = run_ours(args, world, rank, local)
+    if rank != 0:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+        return
+    # oracle parity of the first timed step, and the CPU baseline (rank 0, N=1 only)
+    from oracle import geepee_np as O
+    e_ref, _ = O.sdgpr_objective(r['x'], r['y'], r['params'], ALPHA, idx=r['idx0'])
+    cpu = None
+    if world == 1:
+        rate, kind, n, dt = cpu_eval_rate(r['x'], r['y'], r['params'], [r['idx0']], args.cpu_seconds)
+        cpu = {'value': rate, 'unit': 'evals/s', 'cores': os.cpu_count(), 'kind': kind,
+               'sample': '%d objective+gradient evaluations (%.1f s) of the same workload' % (n, dt)}
+    line = {'metric': METRIC, 'value': r['value'], 'unit': 'evals/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': r['ms'], 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'df64 (double-float on FP32 pipes; float64 storage)', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'N': N_TRAIN, 'D': D_IN, 'hidden': HIDDEN, 'M': M_PSEUDO,
+                       'minibatch': MB, 'alpha': ALPHA, 'parallelism': 'replicas' if world > 1 else 'single',
+                       'l2': 'flushed (256 MiB write) between timed steps; CUDA-graph replay per step'},
+            'roofline': r['roofline'], 'cpu_baseline': cpu, 'e2e': r['e2e'], 'clocks': r['clocks'],
+            'gpu_launches': r['launches_per_eval'] * args.steps,
+            'fp64_gpu_form': {'value': r['fp64_rate'], 'unit': 'evals/s', 'steps': r['n64'],
+                              'speedup_of_value': r['value'] / r['fp64_rate'],
+                              'speedup_of_e2e': r['e2e']['value'] / r['fp64_rate']},
+            'parity': {'energy_rel_err_vs_oracle': abs(r['e_gpu'] - e_ref) / abs(e_ref),
+                       'fp64_form_energy_rel_err_vs_oracle': abs(r['e_fp64'] - e_ref) / abs(e_ref),
+                       'tolerance': 1e-6}}
+    print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,740 @@
+"""AEP (black-box alpha) sparse-GP models with geepee's Python API, on the GPU.
+
+Drop-in counterparts of geepee/aep_models.py: ``SGPR`` (:589-667), ``SGPLVM``
+(:670-867), ``SDGPR`` (:870-988) and ``SGPSSM`` (:991-1437), with the
+``Base_Model`` / ``Base_*`` behaviour they inherit from geepee/base_models.py
+(parameter dicts, ``init_hypers``/``get_hypers``/``update_hypers``, ``optimise``,
+``set_fixed_params``, ``save_model``/``load_model``, ``predict_f``/``predict_y``).
+
+``objective_function(params, mb_size, alpha, prop_mode)`` takes and returns numpy
+float64 exactly like the reference (minibatches drawn from numpy's global RNG in the
+same way); internally the whole energy+gradient evaluation runs on the device and is
+replayed from a captured CUDA graph.  ``device_objective`` is the device-resident
+fast path (parameters and data already in HBM).
+"""
+from __future__ import annotations
+
+import pickle
+
+import numpy as np
+import torch
+from scipy.optimize import minimize
+
+from .config import PROP_MM, PROP_MC, PROP_LIN, JITTER
+from .layer import DevLayer, gauss_logZ, gauss_dsn, mm, mv, setup_layers
+from .utils import ObjectiveWrapper, flatten_dict, unflatten_dict, adam
+from .pack import Pack
+from . import gpk
+
+F64 = torch.float64
+
+
+def _dev():
+    if not torch.cuda.is_available():
+        raise RuntimeError('geepee_gb300 models need a CUDA device (no CPU fallback)')
+    return torch.device('cuda', torch.cuda.current_device())
+
+
+def _to_dev(a, dev):
+    return torch.as_tensor(np.ascontiguousarray(np.asarray(a, dtype=np.float64)), device=dev)
+
+
+class _Graph:
+    """A captured CUDA graph of one device computation with static inputs/outputs."""
+
+    def __init__(self, fn, warmup=2):
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(warmup):
+                fn()
+        torch.cuda.current_stream().wait_stream(s)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.out = fn()
+
+    def replay(self):
+        self.graph.replay()
+        return self.out
+
+
+# ------------------------------------------------------------------------------------------
+# base behaviour (geepee/base_models.py:15-165)
+# ------------------------------------------------------------------------------------------
+class Base_Model(object):
+    """Shared model plumbing: optimise / fixed params / save / load (base_models.py:15-165)."""
+
+    def __init__(self, y_train):
+        self.y_train = y_train
+        self.N = y_train.shape[0]
+        self.fixed_params = []
+        self.updated = False
+        self.use_graphs = True
+        self._graphs = {}
+        self.dev = _dev()
+
+    def optimise(self, method='L-BFGS-B', tol=None, reinit_hypers=True, callback=None, maxfun=100000,
+                 maxiter=1000, alpha=0.5, mb_size=None, adam_lr=0.001, prop_mode=PROP_MM, disp=True,
+                 return_cost=False, **kargs):
+        """base_models.py:59-134 (L-BFGS-B or Adam over the flattened parameter vector)."""
+        self.updated = False
+        init_params_dict = self.init_hypers(self.y_train) if reinit_hypers else self.get_hypers()
+        init_params_vec, params_args = flatten_dict(init_params_dict)
+        objective_wrapper = ObjectiveWrapper()
+        if mb_size is None:
+            mb_size = self.N
+        costs = []
+        try:
+            if method.lower() == 'adam':
+                results = adam(objective_wrapper, init_params_vec, step_size=adam_lr, maxiter=maxiter,
+                               args=(params_args, self, mb_size, alpha, prop_mode), disp=disp,
+                               callback=callback, return_cost=return_cost)
+                final_params, costs = (results if return_cost else (results, []))
+            else:
+                options = {'maxfun': maxfun, 'maxiter': maxiter, 'disp': disp, 'gtol': 1e-6, 'ftol': 1e-6}
+                results = minimize(fun=objective_wrapper, x0=init_params_vec,
+                                   args=(params_args, self, self.N, alpha, prop_mode), method=method,
+                                   jac=True, tol=tol, callback=callback, options=options)
+                final_params = results.x
+        except KeyboardInterrupt:
+            print('Caught KeyboardInterrupt ...')
+            final_params = objective_wrapper.previous_x
+        final_params = unflatten_dict(final_params, params_args)
+        self.update_hypers(final_params)
+        if return_cost and method.lower() == 'adam':
+            return final_params, costs
+        return final_params
+
+    def set_fixed_params(self, params):
+        """base_models.py:136-147."""
+        if isinstance(params, list):
+            for p in params:
+                if p not in self.fixed_params:
+                    self.fixed_params.append(p)
+        else:
+            self.fixed_params.append(params)
+
+    def save_model(self, fname='/tmp/model.pickle'):
+        with open(fname, 'wb') as f:
+            pickle.dump(self.get_hypers(), f)
+
+    def load_model(self, fname='/tmp/model.pickle'):
+        with open(fname, 'rb') as f:
+            self.update_hypers(pickle.load(f))
+
+    # ---- helpers
+    def _check_info(self, layers):
+        for lay in layers:
+            info = lay.info.cpu().numpy()
+            if np.any(info > 0):
+                raise np.linalg.LinAlgError('matrix is not positive definite (Cholesky info %s)' % info)
+
+    def _run(self, key, fn):
+        if not self.use_graphs:
+            return fn()
+        g = self._graphs.get(key)
+        if g is None:
+            g = self._graphs[key] = _Graph(fn)
+        return g.replay()
+
+
+def _ard_np(lls, lsf, x, z):
+    ell2 = np.exp(np.asarray(lls, dtype=float))
+    sq = (((x[:, None, :] - z[None, :, :]) ** 2) / ell2).sum(-1)
+    return np.exp(np.asarray(lsf, dtype=float)) * np.exp(-0.5 * sq)
+
+
+def layer_init_hypers(N, M, Din, Dout, nat_param=True, x_train=None, key_suffix=''):
+    """Base_SGP_Layer.init_hypers (base_models.py:518-597): identical consumption of numpy's
+    global RNG, so a seeded run produces the reference's initial parameters."""
+    from scipy.cluster.vq import kmeans2
+    from scipy.spatial.distance import cdist
+    if x_train is None:
+        ls = np.log(np.ones((Din,)) + 0.1 * np.random.rand(Din))
+        sf = np.log(np.array([1]))
+        zu = np.tile(np.linspace(-1, 1, M).reshape((M, 1)), (1, Din))
+    else:
+        if N < 10000:
+            centroids, label = kmeans2(x_train, M, minit='points')
+        else:
+            randind = np.random.permutation(N)
+            centroids = x_train[randind[0:M], :]
+        zu = centroids
+        if N < 1000:
+            X1 = np.copy(x_train)
+        else:
+            randind = np.random.permutation(N)
+            X1 = x_train[randind[:1000], :]
+        x_dist = cdist(X1, X1, 'euclidean')
+        triu_ind = np.triu_indices(X1.shape[0])
+        d2imed = np.median(x_dist[triu_ind])
+        ls = np.full((Din,), np.log(d2imed / 2 + 1e-16))
+        sf = np.log(np.array([0.5]))
+    Kuu = _ard_np(2 * ls, 2 * sf, zu, zu) + np.diag(JITTER * np.ones((M,)))
+    Kuuinv = np.linalg.inv(Kuu)
+    iu, di = np.triu_indices(M), np.diag_indices(M)
+    eta1_R = np.zeros((Dout, M * (M + 1) // 2))
+    eta2 = np.zeros((Dout, M))
+    for d in range(Dout):
+        mu = np.linspace(-1, 1, M).reshape((M, 1))
+        alpha = 0.5 * np.random.rand(M)
+        if nat_param:
+            Suinv = np.diag(1 / alpha)
+            theta2 = np.dot(Suinv, mu)
+            theta1 = Suinv
+        else:
+            Suinv = np.diag(1 / alpha) + Kuuinv
+            Su = np.linalg.inv(Suinv)
+            theta1 = Su
+            theta2 = np.dot(Su, mu / alpha.reshape((M, 1)))
+        R = np.linalg.cholesky(theta1).T
+        R[di] = np.log(R[di])
+        eta1_R[d, :] = R[iu]
+        eta2[d, :] = theta2.reshape((M,))
+    return {'sf' + key_suffix: sf, 'ls' + key_suffix: ls, 'zu' + key_suffix: zu,
+            'eta1_R' + key_suffix: eta1_R, 'eta2' + key_suffix: eta2}
+
+
+class _PackedModel(Base_Model):
+    """Parameters, gradients, energy and Cholesky status in two flat buffers (see pack.py)."""
+
+    def _make_packs(self, spec):
+        self.ppack = Pack(spec, self.dev)
+        self.gpack = Pack(spec + [('__energy__', ()), ('__info__', ())], self.dev)
+        self.sn = self.ppack.views['sn']
+        self.g_sn = self.gpack.views['sn']
+        self.energy = self.gpack.views['__energy__']
+        self._shapes = {k: s for k, s in spec}
+
+    def get_hypers(self):
+        return self.ppack.download(self._shapes)
+
+    def update_hypers(self, params):
+        self._shapes = {k: np.shape(params[k]) for k, _ in self.ppack.spec}
+        self.ppack.upload(params)
+        self.updated = False
+
+    def _flag_info(self, layers):
+        """Cholesky status of every layer -> one float slot of the gradient pack (on device)."""
+        worst = torch.stack([lay.info.max() for lay in layers]).max()
+        self.gpack.views['__info__'].copy_(worst.to(F64).reshape(1))
+
+    def _objective_host(self, idx, alpha):
+        if idx is None:
+            self._run(('full', alpha), lambda: self.device_objective(None, alpha))
+        else:
+            key = ('mb', len(idx), alpha)
+            if key not in self._graphs or getattr(self, '_idx_buf', None) is None \
+                    or self._idx_buf.shape[0] != len(idx):
+                self._idx_buf = torch.zeros(len(idx), dtype=torch.int64, device=self.dev)
+                self._graphs.pop(key, None)
+            if getattr(self, '_idx_host', None) is None or self._idx_host.shape[0] != len(idx):
+                self._idx_host = torch.zeros(len(idx), dtype=torch.int64, pin_memory=True)
+            self._idx_host.numpy()[:] = idx
+            self._idx_buf.copy_(self._idx_host, non_blocking=True)
+            self._run(key, lambda: self.device_objective(self._idx_buf, alpha))
+        out = self.gpack.download(self._shapes)
+        energy, info = out.pop('__energy__'), out.pop('__info__')
+        if info > 0:
+            raise np.linalg.LinAlgError('matrix is not positive definite (Cholesky pivot %d)' % int(info))
+        for p in self.fixed_params:
+            out[p] = np.zeros_like(out[p])
+        return energy, out
+
+
+# ------------------------------------------------------------------------------------------
+# SGPR (aep_models.py:589-667)
+# ------------------------------------------------------------------------------------------
+class SGPR(_PackedModel):
+    """Sparse GP regression with AEP; Gaussian likelihood."""
+
+    def __init__(self, x_train, y_train, no_pseudo, lik='Gaussian', nat_param=True):
+        super().__init__(y_train)
+        if lik.lower() != 'gaussian':
+            raise NotImplementedError('likelihood not implemented')
+        self.N, self.Dout = y_train.shape
+        self.Din = x_train.shape[1]
+        self.M = no_pseudo
+        self.x_train = x_train
+        self.nat_param = nat_param
+        self._make_packs(DevLayer.spec(self.Din, self.Dout, self.M) + [('sn', ())])
+        self.layer = DevLayer(self.N, self.Din, self.Dout, self.M, nat_param, self.dev,
+                              self.ppack.views, self.gpack.views)
+        self.sgp_layer = self.layer
+        self.x_dev = _to_dev(x_train, self.dev)
+        self.y_dev = _to_dev(y_train, self.dev)
+
+    def init_hypers(self, y_train=None):
+        """Base_SGPR.init_hypers (base_models.py:1036-1049)."""
+        p = layer_init_hypers(self.N, self.M, self.Din, self.Dout, self.nat_param, self.x_train)
+        p['sn'] = np.log(0.01)
+        return p
+
+    def device_objective(self, idx, alpha):
+        """Energy and gradients for minibatch rows `idx` (device int64, or None for all);
+        everything stays on the device.  Results: self.energy, self.layer.g, self.g_sn."""
+        lay, N = self.layer, self.N
+        xb = self.x_dev if idx is None else self.x_dev.index_select(0, idx)
+        yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
+        nb = yb.shape[0]
+        scale = -N / nb / alpha
+        setup_layers([lay], alpha)
+        m, v, kfu, Bk = lay.fwd_det(xb)
+        logZ, dm, dv = gauss_logZ(m, v, yb, self.sn, alpha)
+        lay.bwd_det(alpha, scale * dm, scale * dv, kfu, Bk, xb)
+        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
+        self.energy.copy_((scale * logZ + lay.phi(alpha)) / N)
+        for g in lay.g.values():
+            g.div_(N)
+        self.g_sn.div_(N)
+        self._flag_info([lay])
+        return self.energy
+
+    def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
+        """aep_models.py:610-667."""
+        N = self.N
+        idx = None if mb_size >= N else np.random.choice(N, mb_size, replace=False)
+        self.update_hypers(params)
+        return self._objective_host(idx, alpha)
+
+    def _prepare_predict(self):
+        if not self.updated:
+            self.layer.setup_posterior()
+            self.layer.setup_predict()
+            self.updated = True
+
+    def predict_f(self, inputs):
+        """base_models.py:985-998."""
+        self._prepare_predict()
+        m, v, _, _ = self.layer.fwd_det(_to_dev(inputs, self.dev), cav=False)
+        return m.cpu().numpy(), v.cpu().numpy()
+
+    def predict_y(self, inputs):
+        """base_models.py:1020-1034 (Gauss_Layer.output_probabilistic adds exp(2 sn))."""
+        mf, vf = self.predict_f(inputs)
+        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+
+
+# ------------------------------------------------------------------------------------------
+# SDGPR (aep_models.py:870-988, base_models.py:1073-1336)
+# ------------------------------------------------------------------------------------------
+class SDGPR(_PackedModel):
+    """Deep GP regression with AEP and moment-matching propagation."""
+
+    def __init__(self, x_train, y_train, no_pseudos, hidden_sizes, lik='Gaussian'):
+        super().__init__(y_train)
+        if lik.lower() != 'gaussian':
+            raise NotImplementedError('likelihood not implemented')
+        self.N, self.Dout = y_train.shape
+        self.Din = x_train.shape[1]
+        self.size = [self.Din] + list(hidden_sizes) + [self.Dout]
+        self.L = len(self.size) - 1
+        self.Ms = list(no_pseudos) if isinstance(no_pseudos, (list, tuple)) else [no_pseudos] * self.L
+        self.x_train = x_train
+        spec = []
+        for i in range(self.L):
+            spec += DevLayer.spec(self.size[i], self.size[i + 1], self.Ms[i], '_%d' % i)
+        self._make_packs(spec + [('sn', ())])
+        self.layers = [DevLayer(self.N, self.size[i], self.size[i + 1], self.Ms[i], True, self.dev,
+                                self.ppack.views, self.gpack.views, '_%d' % i) for i in range(self.L)]
+        self.sgp_layers = self.layers
+        self.x_dev = _to_dev(x_train, self.dev)
+        self.y_dev = _to_dev(y_train, self.dev)
+
+    def init_hypers(self, y_train=None):
+        """Base_SDGPR.init_hypers (base_models.py:1290-1312)."""
+        p = {}
+        for i in range(self.L):
+            p.update(layer_init_hypers(self.N, self.Ms[i], self.size[i], self.size[i + 1], True,
+                                       self.x_train if i == 0 else None, '_%d' % i))
+        p['sn'] = np.log(0.01)
+        return p
+
+    def device_objective(self, idx, alpha):
+        """Device-resident energy+gradient (aep_models.py:895-988); see SGPR.device_objective."""
+        N, L = self.N, self.L
+        xb = self.x_dev if idx is None else self.x_dev.index_select(0, idx)
+        yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
+        nb = yb.shape[0]
+        scale = -N / nb / alpha
+        setup_layers(self.layers, alpha)
+        ms, vs = [], []
+        m, v, kfu, Bk = self.layers[0].fwd_det(xb)
+        ms.append(m)
+        vs.append(v)
+        for i in range(1, L):
+            m, v = self.layers[i].fwd_mm(ms[-1], vs[-1])
+            ms.append(m)
+            vs.append(v)
+        logZ, dm, dv = gauss_logZ(ms[-1], vs[-1], yb, self.sn, alpha)
+        dmi, dvi = scale * dm, scale * dv
+        for i in range(L - 1, -1, -1):
+            lay = self.layers[i]
+            if i == 0:
+                lay.bwd_det(alpha, dmi, dvi, kfu, Bk, xb)
+            else:
+                dmi, dvi = lay.bwd_mm(alpha, ms[i], dmi, dvi, ms[i - 1], vs[i - 1])
+        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
+        energy = scale * logZ
+        for lay in self.layers:
+            energy = energy + lay.phi(alpha)
+        self.energy.copy_(energy / N)
+        for lay in self.layers:
+            for g in lay.g.values():
+                g.div_(N)
+        self.g_sn.div_(N)
+        self._flag_info(self.layers)
+        return self.energy
+
+    def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
+        """aep_models.py:895-988."""
+        N = self.N
+        idx = None if mb_size >= N else np.random.choice(N, mb_size, replace=False)
+        self.update_hypers(params)
+        return self._objective_host(idx, alpha)
+
+    def _prepare_predict(self):
+        if not self.updated:
+            for lay in self.layers:
+                lay.setup_posterior()
+                lay.setup_predict()
+            self.updated = True
+
+    def predict_f_device(self, x):
+        """Posterior moment propagation (base_models.py:1140-1158) on device tensors."""
+        self._prepare_predict()
+        m, v, _, _ = self.layers[0].fwd_det(x, cav=False)
+        for lay in self.layers[1:]:
+            m, v = lay.fwd_mm(m, v, cav=False)
+        return m, v
+
+    def predict_f(self, inputs, prop_mode=PROP_MM, no_samples=200):
+        if prop_mode != PROP_MM:
+            raise NotImplementedError('prop_mode %s not implemented' % prop_mode)
+        m, v = self.predict_f_device(_to_dev(inputs, self.dev))
+        return m.cpu().numpy(), v.cpu().numpy()
+
+    def predict_y(self, inputs):
+        """base_models.py:1264-1275."""
+        mf, vf = self.predict_f(inputs)
+        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+
+
+# ------------------------------------------------------------------------------------------
+# SGPLVM (aep_models.py:670-867, base_models.py:661-929)
+# ------------------------------------------------------------------------------------------
+def _phi_x(mx, vx):
+    """compute_phi_x (aep_models.py:863-867)."""
+    return (0.5 * (mx * mx / vx + torch.log(vx))).sum(), mx / vx, 0.5 * (-mx * mx / (vx * vx) + 1 / vx)
+
+
+class SGPLVM(_PackedModel):
+    """GP latent-variable model with AEP; Gaussian likelihood; energy is NOT divided by N."""
+
+    def __init__(self, y_train, hidden_size, no_pseudo, lik='Gaussian', prior_mean=0, prior_var=1,
+                 nat_param=True):
+        super().__init__(y_train)
+        if lik.lower() != 'gaussian':
+            raise NotImplementedError('likelihood not implemented')
+        self.N, self.Dout = y_train.shape
+        self.Din = hidden_size
+        self.M = no_pseudo
+        self.nat_param = nat_param
+        self.prior_mean, self.prior_var = prior_mean, prior_var
+        self.prior_x1, self.prior_x2 = prior_mean / prior_var, 1.0 / prior_var
+        spec = DevLayer.spec(self.Din, self.Dout, self.M) + [('sn', ()), ('x1', (self.N, self.Din)),
+                                                              ('x2', (self.N, self.Din))]
+        self._make_packs(spec)
+        self.layer = DevLayer(self.N, self.Din, self.Dout, self.M, nat_param, self.dev, self.ppack.views,
+                              self.gpack.views)
+        self.sgp_layer = self.layer
+        self.y_dev = _to_dev(y_train, self.dev)
+
+    def init_hypers(self, y_train=None):
+        """Latent means from PCA (base_models.py:848-862); the GP part is initialised on them with
+        the layer initialiser.  (The reference additionally runs 100 L-BFGS steps of its VFE SGPR,
+        base_models.py:864-876; the VFE family is outside this package.)"""
+        y = self.y_train if y_train is None else y_train
+        from .utils import pca_reduce
+        post_m = pca_reduce(y, self.Din)
+        post_m = (post_m - post_m.mean(0)) / (post_m.std(0) + 1e-5)
+        post_v = 0.1 * np.ones_like(post_m)
+        p = layer_init_hypers(self.N, self.M, self.Din, self.Dout, self.nat_param, post_m)
+        p['sn'] = np.log(0.01)
+        if self.nat_param:
+            post_2 = 1.0 / post_v
+            p['x1'] = post_2 * post_m
+            p['x2'] = np.log(post_2 - 1) / 2
+        else:
+            p['x1'] = post_m
+            p['x2'] = np.log(post_v) / 2
+        return p
+
+    def device_objective(self, idx, alpha):
+        """aep_models.py:694-815 on device tensors; idx: device int64 rows (all rows if None)."""
+        N, lay = self.N, self.layer
+        v = self.ppack.views
+        f1 = v['x1']
+        f2 = torch.exp(2.0 * v['x2'])
+        if idx is None:
+            idx = torch.arange(N, device=self.dev)
+        yb = self.y_dev.index_select(0, idx)
+        nb = yb.shape[0]
+        scale = -N / nb / alpha
+        setup_layers([lay], alpha)
+        px1, px2 = self.prior_x1, self.prior_x2
+        f1b, f2b = f1.index_select(0, idx), f2.index_select(0, idx)
+        if self.nat_param:
+            post1, post2 = px1 + f1, px2 + f2
+            c1 = px1 + (1.0 - alpha) * f1b
+            c2 = px2 + (1.0 - alpha) * f2b
+        else:
+            post1, post2 = f1 / f2, 1.0 / f2
+            t1, t2 = f1b / f2b, 1.0 / f2b
+            c1 = px1 + (t1 - px1) * (1 - alpha)
+            c2 = px2 + (t2 - px2) * (1 - alpha)
+        mcav, vcav = (c1 / c2).contiguous(), (1.0 / c2).contiguous()
+        p1b, p2b = post1.index_select(0, idx), post2.index_select(0, idx)
+        mpost, vpost = p1b / p2b, 1.0 / p2b
+        m, vv = lay.fwd_mm(mcav, vcav)
+        logZ, dm, dv = gauss_logZ(m, vv, yb, self.sn, alpha)
+        dmx, dvx = lay.bwd_mm(alpha, m, scale * dm, scale * dv, mcav, vcav)
+        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
+        phi_prior = float(0.5 * (self.prior_mean ** 2 / self.prior_var + np.log(self.prior_var))) * N * self.Din
+        phi_cav, dmc, dvc = _phi_x(mcav, vcav)
+        phi_post, dmp, dvp = _phi_x(mpost, vpost)
+        sc_cav = -N / nb / alpha
+        sc_post = -N / nb * (1.0 - 1.0 / alpha)
+        xc = phi_prior + sc_cav * phi_cav + sc_post * phi_post
+        dmc = sc_cav * dmc + dmx
+        dvc = sc_cav * dvc + dvx
+        dmp, dvp = sc_post * dmp, sc_post * dvp
+        # compute_cav_grad_x (aep_models.py:817-838)
+        t1, t2 = mcav / vcav, 1.0 / vcav
+        dt1 = (1.0 - alpha) * dmc / t2
+        dt2 = (1.0 - alpha) * (-dmc * t1 / t2 ** 2 - dvc / t2 ** 2)
+        if self.nat_param:
+            dt2 = dt2 * 2 * f2b
+        else:
+            dm_ = dt1 / f2b
+            dv_ = -dt1 * f1b / f2b ** 2 - dt2 / f2b ** 2
+            dt1, dt2 = dm_, dv_ * 2 * f2b
+        # compute_posterior_grad_x (base_models.py:913-929)
+        if self.nat_param:
+            h1 = dmp / p2b
+            h2 = (-dmp * p1b / p2b ** 2 - dvp / p2b ** 2) * 2 * f2b
+        else:
+            h1, h2 = dmp, dvp * 2 * f2b
+        gx1, gx2 = self.gpack.views['x1'], self.gpack.views['x2']
+        gx1.zero_()
+        gx2.zero_()
+        gx1.index_put_((idx,), dt1 + h1, accumulate=True)
+        gx2.index_put_((idx,), dt2 + h2, accumulate=True)
+        self.energy.copy_((scale * logZ + xc + lay.phi(alpha)).reshape(1))
+        self._flag_info([lay])
+        return self.energy
+
+    def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
+        """aep_models.py:694-815 (PROP_MM)."""
+        if prop_mode != PROP_MM:
+            raise NotImplementedError('propagation mode not implemented')
+        N = self.N
+        idx = np.arange(N) if mb_size == N else np.random.choice(N, mb_size, replace=False)
+        self.update_hypers(params)
+        return self._objective_host(idx, alpha)
+
+    def predict_f(self, inputs):
+        """base_models.py:734-747 (deterministic inputs through the posterior)."""
+        if not self.updated:
+            self.layer.setup_posterior()
+            self.layer.setup_predict()
+            self.updated = True
+        m, v, _, _ = self.layer.fwd_det(_to_dev(inputs, self.dev), cav=False)
+        return m.cpu().numpy(), v.cpu().numpy()
+
+    def predict_y(self, inputs):
+        mf, vf = self.predict_f(inputs)
+        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+
+    def get_posterior_x(self, idxs=None):
+        """base_models.py:765-775."""
+        p = self.get_hypers()
+        f1, f2 = np.asarray(p['x1']), np.exp(2 * np.asarray(p['x2']))
+        post1, post2 = (self.prior_x1 + f1, self.prior_x2 + f2) if self.nat_param else (f1 / f2, 1.0 / f2)
+        if idxs is None:
+            idxs = np.arange(self.N)
+        return post1[idxs] / post2[idxs], 1.0 / post2[idxs]
+
+
+# ------------------------------------------------------------------------------------------
+# SGPSSM with linear-Gaussian emission (aep_models.py:991-1437, base_models.py:1339-1752,
+# lik_layers.py:474-627)
+# ------------------------------------------------------------------------------------------
+class SGPSSM(_PackedModel):
+    """GP state-space model with AEP: GP transition (moment matching), linear-Gaussian emission."""
+
+    def __init__(self, y_train, hidden_size, no_pseudo, lik='Gaussian', prior_mean=0, prior_var=1,
+                 x_control=None, gp_emi=False, control_to_emi=True, nat_param=True):
+        super().__init__(y_train)
+        if gp_emi or x_control is not None:
+            raise NotImplementedError('GP emission / control inputs are not implemented on the device path')
+        if lik.lower() != 'gaussian':
+            raise NotImplementedError('likelihood not implemented')
+        self.N, self.Dout = y_train.shape
+        self.Din = hidden_size
+        self.M = no_pseudo
+        self.gp_emi = False
+        self.prior_mean, self.prior_var = prior_mean, prior_var
+        self.x_prior_1, self.x_prior_2 = prior_mean / prior_var, 1.0 / prior_var
+        Dx, Dy, N = self.Din, self.Dout, self.N
+        spec = (DevLayer.spec(Dx, Dx, self.M, '_dynamic') +
+                [('sn', (1,)), ('x_factor_1', (N, Dx)), ('x_factor_2', (N, Dx)),
+                 ('C_emission', (Dy, Dx)), ('R_emission', (Dy,))])
+        self._make_packs(spec)
+        self.dyn_layer = DevLayer(N - 1, Dx, Dx, self.M, True, self.dev, self.ppack.views, self.gpack.views,
+                                  '_dynamic')
+        self.y_dev = _to_dev(y_train, self.dev)
+        w1 = np.full((N, 1), 3.0)
+        w1[0] = w1[-1] = 2.0
+        first = np.zeros((N, 1))
+        first[0] = 1.0
+        # constants built outside graph capture: x-posterior factor counts and the first step
+        self._consts = {'w1': _to_dev(w1, self.dev), 'first': _to_dev(first, self.dev)}
+
+    def init_hypers(self, y_train=None):
+        raise NotImplementedError('SGPSSM.init_hypers needs the VFE SGPR and pylds initialisers '
+                                  '(base_models.py:1597-1683); construct the parameter dict directly')
+
+    def _emission(self, mx, vx, yb, alpha, scale):
+        """Gauss_Emis.compute_emission_tilted (lik_layers.py:573-627) on device tensors."""
+        C = self.ppack.views['C_emission']
+        R = torch.exp(2.0 * self.ppack.views['R_emission'])
+        nb, Dy = yb.shape
+        CVC = torch.einsum('da,na,ba->ndb', C, vx, C)
+        Vy = (CVC + torch.diag(R / alpha)).contiguous()
+        Vinv = torch.empty_like(Vy)
+        ldV = torch.empty(nb, dtype=F64, device=self.dev)
+        gpk.small_spd(Vy, Vinv, ldV, self._emi_info[:nb])
+        Yd = yb - mx @ C.T
+        VinvY = torch.einsum('nab,nb->na', Vinv, Yd)
+        quad = -0.5 * (Yd * VinvY).sum()
+        # log det(I + alpha CVC R^-1) = log det Vy + sum log(alpha / R)
+        logdet_I = ldV + torch.log(alpha / R).sum()
+        logZ = (-nb * Dy * 0.5 * alpha * np.log(2 * np.pi) - 0.5 * nb * alpha * torch.log(R).sum()
+                - 0.5 * logdet_I.sum() + quad)
+        dR = (-0.5 * torch.diagonal(Vinv, dim1=1, dim2=2).sum(0) + 0.5 * (VinvY ** 2).sum(0)) / alpha
+        dR = (dR + 0.5 * nb * (1 - alpha) / R) * 2 * R
+        dSig = -0.5 * Vinv + 0.5 * VinvY[:, :, None] * VinvY[:, None, :]
+        dC = VinvY.T @ mx + 2 * torch.einsum('nc,bc,nab->ac', vx, C, dSig)
+        dmx = VinvY @ C
+        dvx = torch.einsum('nab,ad,bd->nd', dSig, C, C)
+        return logZ * scale, dmx * scale, dvx * scale, dC * scale, dR * scale
+
+    def device_objective(self, emi, alpha):
+        """aep_models.py:1024-1206; emi: device int64 window of time indices (contiguous)."""
+        N, Dx = self.N, self.Din
+        v = self.ppack.views
+        lay = self.dyn_layer
+        f1 = v['x_factor_1']
+        f2 = torch.exp(2.0 * v['x_factor_2'])
+        dyn = emi[:-1]
+        nd, ne = dyn.shape[0], emi.shape[0]
+        s_dyn = -(N - 1) / nd / alpha
+        s_emi = -N / ne / alpha
+        setup_layers([lay], alpha)
+        px1, px2 = self.x_prior_1, self.x_prior_2
+        c = self._consts
+        post1 = c['w1'] * f1 + px1 * c['first']
+        post2 = c['w1'] * f2 + px2 * c['first']
+        cav1 = post1 - alpha * f1
+        cav2 = post2 - alpha * f2
+        cm, cv = cav1 / (cav2 + 1e-16), 1.0 / (cav2 + 1e-16)
+        mt, vt = cm.index_select(0, dyn + 1), cv.index_select(0, dyn + 1)
+        mtm1, vtm1 = cm.index_select(0, dyn).contiguous(), cv.index_select(0, dyn).contiguous()
+        mup, vup = cm.index_select(0, emi), cv.index_select(0, emi)
+        mprop, vprop = lay.fwd_mm(mtm1, vtm1)
+        sn = v['sn']
+        sn2 = torch.exp(2 * sn)
+        vsum = vt + vprop + sn2 / alpha
+        md = mt - mprop
+        logZd = (-0.5 * md ** 2 / vsum - 0.5 * torch.log(1 + alpha * (vt + vprop) / sn2)
+                 - 0.5 * alpha * torch.log(2 * np.pi * sn2))
+        logZ_dyn = s_dyn * logZd.sum()
+        dvt = s_dyn * (-0.5 / vsum + 0.5 * md ** 2 / vsum ** 2)
+        dmt = s_dyn * (-md / vsum)
+        self.g_sn.copy_(dvt.sum() * 2 * sn2 / alpha + s_dyn * nd * Dx * (1 - alpha))
+        gmx, gvx = lay.bwd_mm(alpha, mprop, (-dmt).contiguous(), dvt.contiguous(), mtm1, vtm1)
+        yb = self.y_dev.index_select(0, emi)
+        logZ_emi, emx, evx, dC, dR = self._emission(mup, vup, yb, alpha, s_emi)
+        self.gpack.views['C_emission'].copy_(dC)
+        self.gpack.views['R_emission'].copy_(dR)
+        # gradients w.r.t. the x factors (aep_models.py:1208-1315)
+        # per-time-step weights (aep_models.py:1221-1223, 1277-1279, 1301-1303)
+        nb2 = c['w1'] - 1.0                          # 2 inside, 1 at the ends: neighbouring factors
+        sp = -(1.0 - 1.0 / alpha) + nb2 / alpha
+        gp1 = sp * (post1 / post2)
+        gp2 = sp * (-0.5 * post1 ** 2 / post2 ** 2 - 0.5 / post2)
+        w1 = c['w1']
+        post_g1 = w1 * gp1
+        post_g2 = 2 * w1 * gp2 * f2
+        scx = w1 - alpha
+        sc = -(1.0 + nb2) / alpha
+        cav_g1 = sc * (cav1 / cav2) * scx
+        cav_g2 = sc * (-0.5 * cav1 ** 2 / cav2 ** 2 - 0.5 / cav2) * scx * 2 * f2
+        z1 = torch.zeros_like(cav1)
+        z2 = torch.zeros_like(cav1)
+
+        def acc(ix, dmc, dvc):
+            c1, c2 = cav1.index_select(0, ix), cav2.index_select(0, ix)
+            z1.index_add_(0, ix, dmc / c2)
+            z2.index_add_(0, ix, -dmc * c1 / c2 ** 2 - dvc / c2 ** 2)
+
+        acc(emi, emx, evx)
+        acc(emi[1:], dmt, dvt)
+        acc(emi[:-1], gmx, gvx)
+        self.gpack.views['x_factor_1'].copy_(post_g1 + cav_g1 + z1 * scx)
+        self.gpack.views['x_factor_2'].copy_(post_g2 + cav_g2 + z2 * scx * 2 * f2)
+        phi_prior_x = 0.5 * Dx * ((px1 / px2) ** 2 * px2 + np.log(1.0 / px2))
+        phi_post_x = (sp * 0.5 * (post1 ** 2 / post2 - torch.log(post2))).sum()
+        phi_cav_x = (sc * 0.5 * (cav1 ** 2 / cav2 - torch.log(cav2))).sum()
+        energy = logZ_dyn + logZ_emi + phi_prior_x + phi_post_x + phi_cav_x + lay.phi(alpha)
+        self.energy.copy_(energy.reshape(1) / N)
+        for k, g in self.gpack.views.items():
+            if not k.startswith('__'):
+                g.div_(N)
+        worst = torch.stack([lay.info.max(), self._emi_info.max()]).max()
+        self.gpack.views['__info__'].copy_(worst.to(F64).reshape(1))
+        return self.energy
+
+    def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
+        """aep_models.py:1024-1206 (PROP_MM; a contiguous window when mb_size < N)."""
+        if prop_mode != PROP_MM:
+            raise NotImplementedError('propgation mode not implemented')
+        N = self.N
+        if mb_size >= N:
+            emi = np.arange(0, N)
+        else:
+            start = np.random.randint(0, N - mb_size)
+            emi = np.arange(start, start + mb_size)
+        if not hasattr(self, '_emi_info') or self._emi_info.shape[0] < len(emi):
+            self._emi_info = torch.zeros(N, dtype=torch.int32, device=self.dev)
+        self.update_hypers(params)
+        return self._objective_host(emi, alpha)
+
+    def predict_f(self, inputs):
+        """base_models.py:1441-1451 (deterministic inputs through the transition posterior)."""
+        if not self.updated:
+            self.dyn_layer.setup_posterior()
+            self.dyn_layer.setup_predict()
+            self.updated = True
+        m, v, _, _ = self.dyn_layer.fwd_det(_to_dev(inputs, self.dev), cav=False)
+        return m.cpu().numpy(), v.cpu().numpy()
+
+    def predict_y(self, inputs):
+        """base_models.py:1544-1560 with Gauss_Emis.output_probabilistic (lik_layers.py:558-571)."""
+        mf, vf = self.predict_f(inputs)
+        p = self.get_hypers()
+        C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
+        my = mf @ C.T
+        vy = np.einsum('ab,nb,ab->na', C, vf, C) + R
+        return my, vy

@@ -92,28 +92,43 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
   }
   if (tid == 0) s_info = 0;
   __syncthreads();
-  // right-looking Cholesky on the lower triangle
+  // right-looking Cholesky on the lower triangle.  The square root and reciprocal of each
+  // pivot are computed once, by the thread that finalises that diagonal entry in the
+  // previous step's trailing update, and published through shared memory.
+  if (tid == 0) {
+    T piv = S[0];
+    if (!(Num<T>::approx(piv) > 0.f)) {
+      s_info = 1;
+    } else {
+      T d = sqrt_(piv);
+      dg[0] = d;
+      di[0] = recip(d);
+    }
+  }
+  __syncthreads();
   for (int kk = 0; kk < M; ++kk) {
-    T piv = S[kk * ld + kk];
-    if (!(Num<T>::approx(piv) > 0.f)) {   // uniform: every thread read the same value
-      if (tid == 0) s_info = kk + 1;
-      break;
-    }
-    T d = sqrt_(piv);
-    T inv = recip(d);
-    if (tid == 0) {
-      dg[kk] = d;
-      di[kk] = inv;
-    }
+    if (s_info) break;   // uniform: written before the last barrier
+    const T inv = di[kk];
     for (int i = kk + 1 + tid; i < M; i += blockDim.x) S[i * ld + kk] = mul(S[i * ld + kk], inv);
     __syncthreads();
     for (int i = kk + 1 + ty; i < M; i += 32) {
       T lik = S[i * ld + kk];
-      for (int j = kk + 1 + tx; j <= i; j += 32) S[i * ld + j] = sub(S[i * ld + j], mul(lik, S[j * ld + kk]));
+      for (int j = kk + 1 + tx; j <= i; j += 32) {
+        T v = sub(S[i * ld + j], mul(lik, S[j * ld + kk]));
+        S[i * ld + j] = v;
+        if (i == kk + 1 && j == kk + 1) {
+          if (!(Num<T>::approx(v) > 0.f)) {
+            s_info = kk + 2;
+          } else {
+            T d = sqrt_(v);
+            dg[kk + 1] = d;
+            di[kk + 1] = recip(d);
+          }
+        }
+      }
     }
     __syncthreads();
   }
-  __syncthreads();
   int bad = s_info;
   if (info && tid == 0) info[b] = bad;
   if (bad) return;
@@ -137,13 +152,13 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
     }
   }
   if (!Ainv) return;
-  // in-place inverse of the unit-scaled lower factor, columns right to left:
+  // in-place inverse of the lower factor, columns right to left:
   //   X_jj = 1/L_jj,  X_ij = -X_jj sum_{k=j+1..i} X_ik L_kj   (i > j)
+  // column j's L entries are staged in tmp one step ahead, so each column costs two barriers.
+  for (int k = M - 1 + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + (M - 1)];
+  __syncthreads();
   for (int j = M - 1; j >= 0; --j) {
-    for (int k = j + 1 + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + j];
-    __syncthreads();
-    // 8 threads per row
-    int i = j + 1 + (tid >> 3), sl = tid & 7;
+    int i = j + 1 + (tid >> 3), sl = tid & 7;   // 8 threads per row
     T s = Num<T>::zero();
     if (i < M)
       for (int k = j + 1 + sl; k <= i; k += 8) s = fma_(S[i * ld + k], tmp[k], s);
@@ -152,6 +167,8 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
     __syncthreads();
     if (i < M && sl == 0) S[i * ld + j] = neg(mul(di[j], s));
     if (tid == 0) S[j * ld + j] = di[j];
+    if (j > 0)
+      for (int k = j + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + (j - 1)];
     __syncthreads();
   }
   // Ainv = X^T X  (X lower): Ainv_ij = sum_{k >= max(i,j)} X_ki X_kj
@@ -238,6 +255,63 @@ __global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const type
   }
 }
 
+
+// Many tiny SPD matrices (n <= 8), one thread each: inverse and log-determinant by an
+// in-register Cholesky.  The per-time-step Dy x Dy emission covariances of the GP
+// state-space model (geepee/lik_layers.py:596-610 solve / slogdet / inv).
+template <typename T>
+__global__ void __launch_bounds__(128) small_spd_kernel(int B, int n, const typename Num<T>::store_t* A,
+                                                        typename Num<T>::store_t* Ainv, double* logdet, int* info) {
+  __shared__ float2 tab[256];
+  load_exp_table(tab);
+  __syncthreads();
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const typename Num<T>::store_t* a = A + (size_t)b * n * n;
+  T L[8][8];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) L[i][j] = Num<T>::ld(a[i * n + j]);
+  int bad = 0;
+  T ld = Num<T>::zero();
+  for (int k = 0; k < n && !bad; ++k) {
+    T s = L[k][k];
+    for (int j = 0; j < k; ++j) s = sub(s, mul(L[k][j], L[k][j]));
+    if (!(Num<T>::approx(s) > 0.f)) { bad = k + 1; break; }
+    T d = sqrt_(s);
+    L[k][k] = d;
+    ld = add(ld, log_tab(d, tab));
+    T inv = recip(d);
+    for (int i = k + 1; i < n; ++i) {
+      T t = L[i][k];
+      for (int j = 0; j < k; ++j) t = sub(t, mul(L[i][j], L[k][j]));
+      L[i][k] = mul(t, inv);
+    }
+  }
+  if (info) info[b] = bad;
+  if (bad) return;
+  if (logdet) logdet[b] = (double)Num<T>::st(scale2(ld, 1));
+  if (!Ainv) return;
+  // X = L^-1 (lower), then Ainv = X^T X
+  T X[8][8];
+  for (int j = 0; j < n; ++j) {
+    X[j][j] = recip(L[j][j]);
+    for (int i = j + 1; i < n; ++i) {
+      T t = Num<T>::zero();
+      for (int k = j; k < i; ++k) t = fma_(L[i][k], X[k][j], t);
+      X[i][j] = neg(mul(t, recip(L[i][i])));
+    }
+  }
+  typename Num<T>::store_t* o = Ainv + (size_t)b * n * n;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) {
+      T t = Num<T>::zero();
+      for (int k = i; k < n; ++k) t = fma_(X[k][i], X[k][j], t);
+      typename Num<T>::store_t v = Num<T>::st(t);
+      o[i * n + j] = v;
+      o[j * n + i] = v;
+    }
+}
+
 template <typename T>
 int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
                 const void* B, int ldb, long sB, double beta, void* C, int ldc, long sC, cudaStream_t st) {
@@ -307,4 +381,20 @@ extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void*
   else
     return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);
   return gpk::check_launch("trace_kzz");
+}
+
+extern "C" int gpk_small_spd(int prec, int batch, int n, const void* A, void* Ainv, double* logdet, int* info,
+                             void* stream) {
+  GPK_REQUIRE(batch >= 0 && n >= 1 && n <= 8, "small_spd: n=%d outside [1,8]", n);
+  GPK_REQUIRE(A, "small_spd: null input");
+  if (batch == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  int grid = gpk::ceil_div(batch, 128);
+  if (prec == GPK_DF64)
+    small_spd_kernel<df64><<<grid, 128, 0, st>>>(batch, n, (const double*)A, (double*)Ainv, logdet, info);
+  else if (prec == GPK_FP32)
+    small_spd_kernel<float><<<grid, 128, 0, st>>>(batch, n, (const float*)A, (float*)Ainv, logdet, info);
+  else
+    return gpk::fail(GPK_EINVAL, "small_spd: unknown precision %d", prec);
+  return gpk::check_launch("small_spd");
 }

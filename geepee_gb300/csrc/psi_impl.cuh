@@ -45,6 +45,7 @@ struct PsiArgs {
   const S* dm;
   const S* dv;
   const S* dpsi1;    // optional [N,M]: replaces dm_all A
+  int bs_smem;       // symmetrised B staged in shared memory (set by the launcher)
   long b_stride;     // != 0: B is per point (B + n*b_stride), dv treated as 1
   double* dsf2;
   double* dl;
@@ -82,13 +83,14 @@ struct Smem {
   T* h;          // [M*Q]
   T* ps1;        // [M]
   T* G;          // [P]
-  T* red;        // [32 * 64]
+  T* Bs;         // [Dout*P] symmetrised B (B_ab + B_ba off the diagonal), or nullptr
+  T* red;        // [32 * 24]
   T* L;          // [P]   (backward only)
   T* rows;       // [M*(1+Q)] row statistics (backward only)
 };
 
 template <typename T>
-__device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd) {
+__device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd, int nbs) {
   Smem<T> s;
   s.tab = reinterpret_cast<float2*>(base);
   T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
@@ -107,7 +109,8 @@ __device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd) {
   s.h = t; t += M * Q;
   s.ps1 = t; t += M;
   s.G = t; t += P;
-  s.red = t; t += 32 * 64;
+  s.Bs = nbs ? t : nullptr; t += nbs;
+  s.red = t; t += 32 * 24;
   if (bwd) {
     s.L = t; t += P;
     s.rows = t; t += M * (1 + QMAX);
@@ -118,24 +121,24 @@ __device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd) {
   return s;
 }
 
-__host__ __device__ inline size_t smem_bytes(int M, int Q, int P, bool bwd, size_t tsz) {
-  size_t n = (size_t)M * Q + 5 * QMAX + 4 + 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + M + P + 32 * 64;
+__host__ __device__ inline size_t smem_bytes(int M, int Q, int P, bool bwd, size_t tsz, int nbs) {
+  size_t n = (size_t)M * Q + 5 * QMAX + 4 + 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + M + P + nbs + 32 * 24;
   if (bwd) n += P + (size_t)M * (1 + QMAX);
   return 256 * 8 + n * tsz;
 }
 
-// CTA-wide sum of K values per thread (K <= 64); result valid in thread 0.
+// CTA-wide sum of K values per thread (K <= 24); result valid in warp 0.
 template <typename T>
 __device__ __forceinline__ void block_sum(T* vals, int K, T* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = 0; i < K; ++i) {
     T s = warp_sum(vals[i]);
-    if (lane == 0) red[warp * 64 + i] = s;
+    if (lane == 0) red[warp * 24 + i] = s;
   }
   __syncthreads();
   if (warp == 0) {
     for (int i = 0; i < K; ++i) {
-      T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
+      T s = lane < nw ? red[lane * 24 + i] : Num<T>::zero();
       vals[i] = warp_sum(s);
     }
   }
@@ -171,6 +174,14 @@ __device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
       g = fma_(mul(d, d), s.inv4l[q], g);
     }
     s.G[p] = neg(g);
+    if (s.Bs) {
+      for (int d = 0; d < a.Dout; ++d) {
+        const S* Bd = a.B + (size_t)d * M * M;
+        T w = Num<T>::ld(Bd[ia * M + ib]);
+        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+        s.Bs[d * P + p] = w;
+      }
+    }
   }
 }
 
@@ -238,10 +249,16 @@ __device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a
     a.psi2[((size_t)n * M + ib) * M + ia] = v;
   }
   if (contract) {
+    const int P = M * (M + 1) / 2;
     for (int d = 0; d < a.Dout; ++d) {
-      const S* Bd = a.B + (size_t)d * M * M;
-      T w = Num<T>::ld(Bd[ia * M + ib]);
-      if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+      T w;
+      if (s.Bs) {
+        w = s.Bs[d * P + p];
+      } else {
+        const S* Bd = a.B + (size_t)d * M * M;
+        w = Num<T>::ld(Bd[ia * M + ib]);
+        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+      }
       vals[DMAX + d] = fma_(w, ps, vals[DMAX + d]);
     }
   }
@@ -256,9 +273,9 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
-  Smem<T> s = carve<T>(smem_raw, M, Q, P, false);
-  cta_setup<T, S>(a, s, P);
   const bool contract = (a.A != nullptr) && (a.B != nullptr) && (a.m_out != nullptr || a.v_out != nullptr);
+  Smem<T> s = carve<T>(smem_raw, M, Q, P, false, a.bs_smem ? a.Dout * P : 0);
+  cta_setup<T, S>(a, s, P);
   T acc[PPT > 0 ? PPT : 1];
 #pragma unroll
   for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) acc[k] = Num<T>::zero();
@@ -332,7 +349,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
-  Smem<T> s = carve<T>(smem_raw, M, Q, P, true);
+  Smem<T> s = carve<T>(smem_raw, M, Q, P, true, a.bs_smem ? a.Dout * P : 0);
   cta_setup<T, S>(a, s, P);
   const int lane = threadIdx.x & 31;
 
@@ -414,9 +431,14 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
         for (int d = 0; d < DB; ++d) {
           if (d < D) {
-            const S* Bd = a.B + (size_t)d * M * M + (size_t)n * a.b_stride;
-            T bb = Num<T>::ld(Bd[ia * M + ib]);
-            if (ia != ib) bb = add(bb, Num<T>::ld(Bd[ib * M + ia]));
+            T bb;
+            if (s.Bs) {
+              bb = s.Bs[d * P + p];
+            } else {
+              const S* Bd = a.B + (size_t)d * M * M + (size_t)n * a.b_stride;
+              bb = Num<T>::ld(Bd[ia * M + ib]);
+              if (ia != ib) bb = add(bb, Num<T>::ld(Bd[ib * M + ia]));
+            }
             w = fma_(dvr[d], bb, w);
             accB[k][d] = fma_(dvr[d], ps, accB[k][d]);
           }
@@ -564,9 +586,12 @@ int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cud
 }
 
 template <typename T>
-int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a, cudaStream_t st) {
+int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
+  PsiArgs<typename Num<T>::store_t> a = a_in;
   const int P = a.M * (a.M + 1) / 2;
-  size_t sm = smem_bytes(a.M, a.Q, P, false, sizeof(T));
+  const bool contract = a.A && a.B && (a.m_out || a.v_out);
+  a.bs_smem = contract && smem_bytes(a.M, a.Q, P, false, sizeof(T), a.Dout * P) <= 200 * 1024;
+  size_t sm = smem_bytes(a.M, a.Q, P, false, sizeof(T), a.bs_smem ? a.Dout * P : 0);
   if (sm > 227 * 1024) return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: M=%d needs %zu B of shared memory", a.M, sm);
   const bool sum = a.psi2_sum != nullptr;
   if (sum && P > PPT_MAX * NT)
@@ -597,11 +622,14 @@ int bwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t 
 }
 
 template <typename T>
-int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a, cudaStream_t st) {
+int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
+  PsiArgs<typename Num<T>::store_t> a = a_in;
   const int P = a.M * (a.M + 1) / 2;
-  size_t sm = smem_bytes(a.M, a.Q, P, true, sizeof(T));
-  if (a.M > 128 || sm > 227 * 1024)
-    return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d unsupported (M <= 128)", a.M);
+  a.bs_smem = a.b_stride == 0 && smem_bytes(a.M, a.Q, P, true, sizeof(T), a.Dout * P) <= 200 * 1024;
+  size_t sm = smem_bytes(a.M, a.Q, P, true, sizeof(T), a.bs_smem ? a.Dout * P : 0);
+  if (P > PPT_MAX * NT || sm > 227 * 1024)
+    return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d unsupported (M(M+1)/2 <= %d, i.e. M <= 127)", a.M,
+                     PPT_MAX * NT);
   int grid = gpk::sm_count();
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;

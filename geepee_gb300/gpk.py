@@ -109,3 +109,10 @@ def trace_kzz(Mm, Z, lls2, lsf2, g_sf, g_ls, g_z, s_sf=1.0, s_ls=1.0):
     M, Q = Z.shape
     call('gpk_trace_kzz', prec_of(Z.dtype), M, Q, ptr(Mm), ptr(Z), ptr(lls2), ptr(lsf2), float(s_sf),
          float(s_ls), ptr(g_sf), ptr(g_ls), ptr(g_z), stream())
+
+
+def small_spd(A, Ainv=None, logdet=None, info=None):
+    """Inverse / log-determinant of many tiny SPD matrices A [B, n, n] (n <= 8)."""
+    n = A.shape[-1]
+    call('gpk_small_spd', prec_of(A.dtype), A.numel() // (n * n), n, ptr(A), ptr(Ainv), ptr(logdet),
+         ptr(info), stream())

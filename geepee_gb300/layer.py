@@ -1,0 +1,355 @@
+"""Device-resident AEP sparse-GP layer (the SGP_Layer of geepee, aep_models.py:26-586).
+
+State lives in float64 CUDA tensors; every matrix product goes through libgpk's
+double-float GEMM, factorisations through its batched SPD Cholesky/inverse, and the
+data-sized work through the fused kernel-matrix / psi-statistics kernels.  Small
+elementwise glue uses torch float64 ops.  Nothing here synchronises with the host,
+so a whole objective+gradient evaluation can be captured in one CUDA graph.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from . import gpk
+from .config import JITTER
+
+F64 = torch.float64
+
+
+def mm(A, B, tA=False, tB=False, alpha=1.0, C=None, beta=0.0):
+    return gpk.gemm(A.contiguous(), B.contiguous(), C, alpha=alpha, beta=beta, tA=tA, tB=tB)
+
+
+def mv(A, v):
+    """Batched matrix-vector: A [D,M,M] (or [M,M]) times v [D,M] -> [D,M]."""
+    return mm(A, v.unsqueeze(-1)).squeeze(-1)
+
+
+def outer(a, b):
+    return a.unsqueeze(-1) * b.unsqueeze(-2)
+
+
+class DevLayer:
+    """One sparse-GP layer: M pseudo-inputs in Din dims, Dout outputs, N training points."""
+
+    @staticmethod
+    def spec(Din, Dout, M, suffix=''):
+        """(key, shape) of the layer's parameters, reference key names."""
+        return [('ls' + suffix, (Din,)), ('sf' + suffix, (1,)), ('zu' + suffix, (M, Din)),
+                ('eta1_R' + suffix, (Dout, M * (M + 1) // 2)), ('eta2' + suffix, (Dout, M))]
+
+    def __init__(self, N, Din, Dout, M, nat_param=True, device=None, params=None, grads=None, suffix=''):
+        """params / grads: optional dicts of preallocated views (keys with `suffix`)."""
+        self.N, self.Din, self.Dout, self.M = N, Din, Dout, M
+        self.nat = nat_param
+        self.dev = device if device is not None else torch.device('cuda', torch.cuda.current_device())
+        z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
+        P = M * (M + 1) // 2
+        if params is None:
+            params = {k: z(*s) for k, s in self.spec(Din, Dout, M, suffix)}
+        if grads is None:
+            grads = {k: z(*s) for k, s in self.spec(Din, Dout, M, suffix)}
+        # parameters (reference keys: ls, sf, zu, eta1_R, eta2) and gradients, as views
+        self.ls, self.sf, self.zu = params['ls' + suffix], params['sf' + suffix], params['zu' + suffix]
+        self.eta1, self.eta2 = params['eta1_R' + suffix], params['eta2' + suffix]
+        self.g = {k: grads[k + suffix] for k in ('ls', 'sf', 'zu', 'eta1_R', 'eta2')}
+        del P
+        iu = torch.triu_indices(M, M)
+        self.iu_flat = (iu[0] * M + iu[1]).to(self.dev)
+        self.diag_flat = (torch.arange(M) * (M + 1)).to(self.dev)
+        # which packed entries sit on the diagonal
+        self.pk_diag = (iu[0] == iu[1]).to(self.dev)
+        # Cholesky status words: [Kuu, Su^-1 (Dout), Suhat^-1 (Dout)]
+        self.info = torch.zeros(1 + 2 * Dout, dtype=torch.int32, device=self.dev)
+
+    # ---------------------------------------------------------------- parameters
+    def param_tensors(self):
+        return {'ls': self.ls, 'sf': self.sf, 'zu': self.zu, 'eta1_R': self.eta1, 'eta2': self.eta2}
+
+    # ---------------------------------------------------------------- q(u) and Kuu
+    def prep_kuu(self):
+        """eta -> (R, theta_1, theta_2) and the jittered Kuu (base_models.py:630-658,454-463)."""
+        M, D = self.M, self.Dout
+        self.lls2 = 2.0 * self.ls
+        self.lsf2 = 2.0 * self.sf
+        R = torch.zeros((D, M * M), dtype=F64, device=self.dev)
+        R[:, self.iu_flat] = self.eta1
+        R[:, self.diag_flat] = torch.exp(R[:, self.diag_flat])
+        self.R = R.view(D, M, M)
+        self.th1 = mm(self.R, self.R, tA=True)
+        self.th2 = self.eta2
+        self.Kuu = gpk.kern(self.zu, self.zu, self.lls2, self.lsf2, jitter=JITTER)
+        return self.Kuu
+
+    def set_kuu_factors(self, Kinv, logdetK):
+        self.Kinv, self.logdetK = Kinv, logdetK
+
+    def prep_s(self, alpha):
+        """The SPD matrices whose inverses the posterior and the cavity need:
+        Su^-1 = Kuu^-1 + theta_1 and Suhat^-1 = Kuu^-1 + beta theta_1 (natural parameters)."""
+        beta = (self.N - alpha) / self.N
+        self.beta = beta
+        K = self.Kinv.unsqueeze(0)
+        self.Suinv = K + self.th1
+        self.Shinv = K + beta * self.th1
+        return torch.cat([self.Suinv, self.Shinv], 0)
+
+    def set_s_factors(self, inv, logdet):
+        D = self.Dout
+        self.Su, self.Sh = inv[:D], inv[D:]
+        self.logdetSu = -logdet[:D]
+        self.ldShinv = logdet[D:]
+        self.mu = mv(self.Su, self.th2)
+        self.Spmm = self.Su + outer(self.mu, self.mu)
+        self.mh = mv(self.Sh, self.beta * self.th2)
+        self._cavity_tail()
+
+    def setup_posterior(self):
+        """update_hypers + compute_kuu + update_posterior (base_models.py:630-658,454-488)."""
+        D = self.Dout
+        self.prep_kuu()
+        self.Kinv = torch.empty_like(self.Kuu)
+        self.logdetK = torch.empty(1, dtype=F64, device=self.dev)
+        gpk.chol_inv(self.Kuu, self.Kinv, None, self.logdetK, self.info[0:1])
+        if self.nat:
+            self.Suinv = self.Kinv.unsqueeze(0) + self.th1
+            self.Su = torch.empty_like(self.Suinv)
+            self.ldSuinv = torch.empty(D, dtype=F64, device=self.dev)
+            gpk.chol_inv(self.Suinv, self.Su, None, self.ldSuinv, self.info[1:1 + D])
+            self.logdetSu = -self.ldSuinv
+            self.mu = mv(self.Su, self.th2)
+        else:
+            self.Su = self.th1
+            self.Suinv = torch.empty_like(self.Su)
+            self.logdetSu = torch.empty(D, dtype=F64, device=self.dev)
+            gpk.chol_inv(self.Su, self.Suinv, None, self.logdetSu, self.info[1:1 + D])
+            self.mu = self.th2
+        self.Spmm = self.Su + outer(self.mu, self.mu)
+
+    def setup_cavity(self, alpha):
+        """SGP_Layer.compute_cavity (aep_models.py:513-546)."""
+        beta = (self.N - alpha) / self.N
+        self.beta = beta
+        K = self.Kinv
+        if self.nat:
+            self.Shinv = K.unsqueeze(0) + beta * self.th1
+            f2 = beta * self.th2
+        else:
+            self.Shinv = K.unsqueeze(0) + beta * (self.Suinv - K.unsqueeze(0))
+            f2 = beta * mv(self.Suinv, self.mu)
+        self.Sh = torch.empty_like(self.Shinv)
+        self.ldShinv = torch.empty(self.Dout, dtype=F64, device=self.dev)
+        gpk.chol_inv(self.Shinv, self.Sh, None, self.ldShinv, self.info[1 + self.Dout:1 + 2 * self.Dout])
+        self.mh = mv(self.Sh, f2)
+        self._cavity_tail()
+
+    def _cavity_tail(self):
+        K = self.Kinv
+        self.Smm_h = self.Sh + outer(self.mh, self.mh)
+        self.Ah = mv(K, self.mh)
+        KS = mm(K, self.Smm_h)
+        self.Bh_sto = mm(KS, K, C=-K.unsqueeze(0).expand_as(KS).contiguous(), beta=1.0)
+        KS2 = mm(K, self.Sh)
+        self.Bh_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
+
+    def setup_predict(self):
+        """Posterior A, B_det, B_sto used by predict (base_models.py:480-488)."""
+        K = self.Kinv
+        self.A = mv(K, self.mu)
+        KS = mm(K, self.Spmm)
+        self.B_sto = mm(KS, K, C=-K.unsqueeze(0).expand_as(KS).contiguous(), beta=1.0)
+        KS2 = mm(K, self.Su)
+        self.B_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
+
+    # ---------------------------------------------------------------- log-partitions
+    def phi(self, alpha):
+        """compute_phi (aep_models.py:62-114): prior + (N/a - 1) posterior - (N/a) cavity."""
+        N = self.N
+        phi_prior = self.Dout * 0.5 * self.logdetK
+        q_post = (self.mu * mv(self.Suinv, self.mu)).sum()
+        q_cav = (self.mh * mv(self.Shinv, self.mh)).sum()
+        phi_post = 0.5 * self.logdetSu.sum() + 0.5 * q_post
+        phi_cav = -0.5 * self.ldShinv.sum() + 0.5 * q_cav
+        return phi_prior + (N / alpha - 1.0) * phi_post - (N / alpha) * phi_cav
+
+    # ---------------------------------------------------------------- forward
+    def fwd_det(self, x, cav=True):
+        n = x.shape[0]
+        A, B = (self.Ah, self.Bh_det) if cav else (self.A, self.B_det)
+        kfu = torch.empty((n, self.M), dtype=F64, device=self.dev)
+        Bk = torch.empty((n, self.Dout, self.M), dtype=F64, device=self.dev)
+        m = torch.empty((n, self.Dout), dtype=F64, device=self.dev)
+        v = torch.empty_like(m)
+        gpk.det_fwd(x, self.zu, self.lls2, self.lsf2, A, B, kfu, Bk, m, v)
+        return m, v, kfu, Bk
+
+    def fwd_mm(self, mx, vx, cav=True):
+        n = mx.shape[0]
+        A, B = (self.Ah, self.Bh_sto) if cav else (self.A, self.B_sto)
+        m = torch.empty((n, self.Dout), dtype=F64, device=self.dev)
+        v = torch.empty_like(m)
+        gpk.psi_fwd(mx, vx, self.zu, self.lls2, self.lsf2, A, B, m_out=m, v_out=v)
+        return m, v
+
+    # ---------------------------------------------------------------- backward pieces
+    def _pack_eta1(self, dth1):
+        """d theta_1 -> d eta1_R (aep_models.py:274-287)."""
+        dR = mm(self.R, dth1 + dth1.transpose(1, 2))
+        flat = dR.reshape(self.Dout, -1)
+        out = flat[:, self.iu_flat]
+        rd = self.R.reshape(self.Dout, -1)[:, self.iu_flat]
+        return torch.where(self.pk_diag, out * rd, out)
+
+    def _finish_hyp(self, Minner):
+        gpk.trace_kzz(Minner.contiguous(), self.zu, self.lls2, self.lsf2, self.g['sf'], self.g['ls'],
+                      self.g['zu'], s_sf=2.0, s_ls=2.0)
+
+    def _kernel_grads(self, dsf2, dl, dv_sum):
+        ell = torch.exp(self.ls)
+        sf2 = torch.exp(2.0 * self.sf)
+        self.g['ls'].copy_(dl * ell)
+        self.g['sf'].copy_(2.0 * sf2 * (dsf2 + dv_sum))
+
+    def bwd_mm(self, alpha, m, dm, dv, mx, vx):
+        """backprop_grads_lvm_mm (aep_models.py:201-304); returns (dmx, dvx)."""
+        N, M, D, Q = self.N, self.M, self.Dout, self.Din
+        s_post, s_cav = N / alpha - 1.0, -N / alpha
+        beta = self.beta
+        z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
+        dsf2, dl, dZ, dAh, dBh = z(1), z(Q), self.g['zu'], z(D, M), z(D, M, M)
+        dZ.zero_()
+        n = mx.shape[0]
+        dmx = torch.empty((n, Q), dtype=F64, device=self.dev)
+        dvx = torch.empty_like(dmx)
+        gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, dsf2, dl, dZ,
+                    dAh, dBh, dmx, dvx)
+        self._kernel_grads(dsf2, dl, dv.sum())
+        K = self.Kinv
+        dvcav = mm(mm(K, dBh), K)
+        dmcav = 2.0 * mv(dvcav, self.mh) + mm(dAh, K, tB=True)
+        dvcav = dvcav + beta * outer(dmcav, self.th2)
+        dvcavinv = -mm(mm(self.Sh, dvcav), self.Sh)
+        dth1 = beta * dvcavinv
+        dth2 = beta * mv(self.Sh, dmcav)
+        KS = mm(K, self.Smm_h)
+        dK = (dvcavinv.sum(0) + mm(dAh, self.mh, tA=True)
+              + 2.0 * mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True) - dBh.sum(0))
+        Minner = s_post * self.Spmm.sum(0) + s_cav * self.Smm_h.sum(0) - 2.0 * dK
+        dth1 = -0.5 * s_post * self.Spmm - 0.5 * s_cav * beta * self.Smm_h + dth1
+        dth2 = s_post * self.mu + s_cav * beta * self.mh + dth2
+        Mall = 0.5 * (D * K + mm(mm(K, Minner), K))
+        self._finish_hyp(Mall)
+        self.g['eta1_R'].copy_(self._pack_eta1(dth1))
+        self.g['eta2'].copy_(dth2)
+        return dmx, dvx
+
+    def _cav_grad_u(self, dmu, dSu):
+        """compute_cav_grad_u (aep_models.py:548-586)."""
+        beta = self.beta
+        if self.nat:
+            dSu = dSu + outer(dmu, beta * self.th2)
+            dSinv = -mm(mm(self.Sh, dSu), self.Sh)
+            return self._pack_eta1(beta * dSinv), beta * mv(self.Sh, dmu), dSinv.sum(0)
+        f2 = mv(self.Suinv, self.mu)
+        dSh = dSu + outer(dmu, beta * f2)
+        dSinv1 = beta * -mm(mm(self.Sh, dSh), self.Sh)
+        Shdmu = mv(self.Sh, dmu)
+        dSinv = dSinv1 + beta * outer(Shdmu, self.mu)
+        dth1 = -mm(mm(self.Suinv, dSinv), self.Suinv)
+        return self._pack_eta1(dth1), beta * mv(self.Suinv, Shdmu), (1 - beta) / beta * dSinv1.sum(0)
+
+    def _post_grad_u(self, dmu, dSu):
+        """compute_posterior_grad_u (base_models.py:490-516)."""
+        if self.nat:
+            dSu = dSu + outer(dmu, self.th2)
+            dSinv = -mm(mm(self.Su, dSu), self.Su)
+            return self._pack_eta1(dSinv), mv(self.Su, dmu), dSinv.sum(0)
+        return self._pack_eta1(dSu), dmu, torch.zeros_like(self.Kinv)
+
+    def bwd_det(self, alpha, dm, dv, kfu, Bk, x):
+        """backprop_grads_reg (aep_models.py:412-511)."""
+        N, M, D, Q = self.N, self.M, self.Dout, self.Din
+        s_post, s_cav = N / alpha - 1.0, -N / alpha
+        z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
+        K = self.Kinv
+        dsf2, dl, dAh = z(1), z(Q), z(D, M)
+        dZ = self.g['zu']
+        dZ.zero_()
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh)
+        self._kernel_grads(dsf2, dl, dv.sum())
+        kK = mm(kfu, K)
+        dmucav = z(D, M)
+        gpk.wsum(kK, dm, dmucav)
+        dSucav = z(D, M, M)
+        gpk.gram(kK, kK, dv, dSucav)
+        Sinv_mh = mv(self.Shinv, self.mh)
+        dmucav = dmucav + s_cav * Sinv_mh
+        dSucav = dSucav + s_cav * (0.5 * self.Shinv - 0.5 * outer(Sinv_mh, Sinv_mh))
+        e1c, e2c, dKc = self._cav_grad_u(dmucav, dSucav)
+        Sinv_mu = mv(self.Suinv, self.mu)
+        dmu = s_post * Sinv_mu
+        dSu = s_post * (0.5 * self.Suinv - 0.5 * outer(Sinv_mu, Sinv_mu))
+        e1p, e2p, dKp = self._post_grad_u(dmu, dSu)
+        dBh = z(D, M, M)
+        gpk.gram(kfu, kfu, dv, dBh)
+        KS = mm(K, self.Sh)
+        dK = (mm(dAh, self.mh, tA=True) + 2.0 * mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True)
+              - dBh.sum(0) + dKc + dKp - 0.5 * D * self.Kuu)
+        Minner = -mm(mm(K, dK), K)
+        self._finish_hyp(Minner)
+        self.g['eta1_R'].copy_(e1c + e1p)
+        self.g['eta2'].copy_(e2c + e2p)
+
+
+def gauss_logZ(m, v, y, sn, alpha):
+    """Gauss_Layer.compute_log_Z (lik_layers.py:119-133) on the device.
+    Returns (logZ, dlogZ/dm, dlogZ/dv) as device tensors."""
+    sn2 = torch.exp(2.0 * sn)
+    vt = v + sn2 / alpha
+    r = y - m
+    nb, D = y.shape
+    logZ = (-0.5 * (torch.log(2 * math.pi * vt) + r * r / vt)).sum()
+    logZ = logZ + nb * D * (0.5 * torch.log(2 * math.pi * sn2 / alpha) - 0.5 * alpha * torch.log(2 * math.pi * sn2))
+    return logZ.reshape(1), r / vt, -0.5 / vt + 0.5 * r * r / (vt * vt)
+
+
+def gauss_dsn(dv, nb, D, sn, alpha, scale):
+    """Gauss_Layer.backprop_grads (lik_layers.py:154-181)."""
+    sn2 = torch.exp(2.0 * sn)
+    return scale * (dv.sum() * 2 * sn2 / alpha + nb * D * (1 - alpha))
+
+
+def setup_layers(layers, alpha):
+    """Posterior + cavity of several layers with batched factorisations: one SPD launch for
+    every layer's Kuu (grouped by M), then one for every Su^-1 and Suhat^-1 (natural-parameter
+    layers; others fall back to the per-layer path)."""
+    nat = [l for l in layers if l.nat]
+    for l in layers:
+        if not l.nat:
+            l.setup_posterior()
+            l.setup_cavity(alpha)
+    by_m = {}
+    for l in nat:
+        by_m.setdefault(l.M, []).append(l)
+    for M, group in by_m.items():
+        K = torch.stack([l.prep_kuu() for l in group])
+        Kinv = torch.empty_like(K)
+        ld = torch.empty(len(group), dtype=F64, device=K.device)
+        info = torch.zeros(len(group), dtype=torch.int32, device=K.device)
+        gpk.chol_inv(K, Kinv, None, ld, info)
+        for i, l in enumerate(group):
+            l.set_kuu_factors(Kinv[i], ld[i:i + 1])
+            l.info[0:1].copy_(info[i:i + 1])
+        S = torch.cat([l.prep_s(alpha) for l in group], 0)
+        Sinv = torch.empty_like(S)
+        lds = torch.empty(S.shape[0], dtype=F64, device=S.device)
+        infos = torch.zeros(S.shape[0], dtype=torch.int32, device=S.device)
+        gpk.chol_inv(S, Sinv, None, lds, infos)
+        o = 0
+        for l in group:
+            n = 2 * l.Dout
+            l.info[1:1 + n].copy_(infos[o:o + n])
+            l.set_s_factors(Sinv[o:o + n], lds[o:o + n])
+            o += n

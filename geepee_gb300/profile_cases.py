@@ -1,0 +1,103 @@
+"""Small, self-contained kernel cases for profiling (ncu) and micro-timing.
+
+  python -m geepee_gb300.profile_cases <case> [--reps R] [--time]
+
+Cases run one kernel of the deep-GP objective on its real input shapes:
+  psi_bwd_dgp   psi backward, 1000 points, M=100, Q=2 (layer 2 of the 2-layer DGP), df64
+  psi_fwd_dgp   psi forward, same shapes, df64
+  psi_fwd_c2    psi forward with sum_n psi2, N=10000, Q=5, M=100, df64
+  psi_fwd_c2_f32  the same in FP32
+  psi_bwd_c2    psi backward, N=10000, Q=5, M=100, df64
+  chol_m100     SPD Cholesky + inverse + logdet of one 100x100 Kuu, df64
+  objective_dgp one full objective+gradient evaluation (eager, every kernel)
+With --time, prints the mean device time per launch (CUDA events).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+
+import numpy as np
+import torch
+
+from . import gpk, workloads as W
+
+
+def _d(a, dtype=torch.float64):
+    return torch.as_tensor(np.asarray(a, dtype=np.float64), device='cuda').to(dtype).contiguous()
+
+
+def _psi_case(N, Q, M, D, dtype, seed=0):
+    wl = W.psi_workload(seed=seed, N=N, Q=Q, M=M, Dout=D)
+    t = {k: _d(wl[k], dtype) for k in ('mu', 'S', 'Z', 'Ahat', 'Bhat', 'dm', 'dv')}
+    t['lls2'] = _d(2 * wl['ls'])
+    t['lsf2'] = _d(2 * wl['sf'])
+    return t
+
+
+def case(name):
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    if name in ('psi_bwd_dgp', 'psi_bwd_c2'):
+        N, Q, M = (1000, 2, 100) if name == 'psi_bwd_dgp' else (10000, 5, 100)
+        t = _psi_case(N, Q, M, 1, torch.float64)
+        m = torch.empty((N, 1), dtype=torch.float64, device='cuda')
+        gpk.psi_fwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'], m_out=m,
+                    v_out=torch.empty_like(m))
+        bufs = (z(1), z(Q), z(M, Q), z(1, M), z(1, M, M), z(N, Q), z(N, Q))
+        return lambda: gpk.psi_bwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'], m,
+                                   t['dm'], t['dv'], *bufs)
+    if name in ('psi_fwd_dgp', 'psi_fwd_c2', 'psi_fwd_c2_f32'):
+        N, Q, M = (1000, 2, 100) if name == 'psi_fwd_dgp' else (10000, 5, 100)
+        dtype = torch.float32 if name.endswith('f32') else torch.float64
+        t = _psi_case(N, Q, M, 1, dtype)
+        m = torch.empty((N, 1), dtype=dtype, device='cuda')
+        v = torch.empty_like(m)
+        s = z(M, M) if name != 'psi_fwd_dgp' else None
+        return lambda: gpk.psi_fwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'],
+                                   psi2_sum=s, m_out=m, v_out=v)
+    if name == 'chol_m100':
+        rng = np.random.RandomState(0)
+        Zr = rng.randn(100, 2)
+        K = np.exp(-0.5 * ((Zr[:, None] - Zr[None]) ** 2).sum(-1)) + 1e-5 * np.eye(100)
+        A = _d(K[None])
+        inv, ld, info = torch.empty_like(A), z(1), torch.zeros(1, dtype=torch.int32, device='cuda')
+        return lambda: gpk.chol_inv(A, inv, None, ld, info)
+    if name == 'objective_dgp':
+        from . import aep_models as A
+        x, y = W.dgp_regression(seed=0)
+        np.random.seed(1)
+        mdl = A.SDGPR(x, y, 100, [2])
+        mdl.update_hypers(mdl.init_hypers(y))
+        mdl.use_graphs = False
+        idx = torch.as_tensor(np.random.RandomState(2).choice(x.shape[0], 1000, replace=False),
+                              device='cuda')
+        return lambda: mdl.device_objective(idx, 0.5)
+    raise SystemExit(f'unknown case {name}')
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument('case')
+    ap.add_argument('--reps', type=int, default=3)
+    ap.add_argument('--time', action='store_true')
+    a = ap.parse_args(argv)
+    fn = case(a.case)
+    fn()
+    torch.cuda.synchronize()
+    if a.time:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        print(f'{a.case}: {e0.elapsed_time(e1) / a.reps * 1e3:.1f} us per call ({a.reps} reps)')
+    else:
+        for _ in range(a.reps):
+            fn()
+        torch.cuda.synchronize()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -144,6 +144,13 @@ int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const d
                   const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
                   void* stream);
 
+/* Batched inverse and log-determinant of many tiny SPD matrices A[b] (n x n, n <= 8), one
+ * thread per matrix; info[b] as in gpk_chol_inv.  Replaces the per-time-step
+ * np.linalg.solve / inv / slogdet of Gauss_Emis.compute_emission_tilted,
+ * geepee/lik_layers.py:596-610. */
+int gpk_small_spd(int prec, int batch, int n, const void* A, void* Ainv, double* logdet, int* info,
+                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

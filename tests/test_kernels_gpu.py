@@ -57,7 +57,7 @@ def test_kfu_derivatives_and_trace_golden():
 
 
 @pytest.mark.parametrize('M,Q,Dout,N', [(24, 5, 2, 200), (1, 1, 1, 3), (33, 3, 1, 17), (100, 2, 1, 300),
-                                        (128, 8, 3, 40)])
+                                        (127, 8, 3, 40)])
 def test_psi_fused_fwd_bwd_vs_oracle(M, Q, Dout, N):
     from geepee_gb300 import gpk, workloads as W
     wl = W.psi_workload(seed=M + Q, N=N, Q=Q, M=M, Dout=Dout)
@@ -129,7 +129,7 @@ def test_chol_inv_logdet(M):
         cond = np.linalg.cond(A[b])
         assert_close(inv[b].cpu().numpy(), ref_inv, max(1e-12, 1e-13 * cond), 'inv')
         assert abs(ld[b].item() - np.linalg.slogdet(A[b])[1]) <= 1e-9 * max(1, abs(np.linalg.slogdet(A[b])[1]))
-        assert_close(L[b].cpu().numpy(), np.linalg.cholesky(A[b]), 1e-12, 'L')
+        assert_close(L[b].cpu().numpy(), np.linalg.cholesky(A[b]), max(1e-12, 1e-14 * cond), 'L')
 
 
 def test_chol_reports_non_pd():
@@ -190,3 +190,18 @@ def test_det_layer_fwd_bwd_vs_oracle():
     c = z(Dout, M)
     gpk.wsum(kt, dev(dm), c)
     assert_close(c.cpu().numpy(), dm.T @ kfu, 1e-10, 'wsum')
+
+
+def test_psi_size_limits_are_reported():
+    """Sizes beyond the register-resident pair tables are refused, not silently truncated."""
+    from geepee_gb300 import gpk
+    from geepee_gb300._lib import GpkError
+    N, M, Q = 4, 128, 2
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    mu, S, Z = z(N, Q), z(N, Q) + 0.1, torch.randn(M, Q, dtype=torch.float64, device='cuda')
+    l2, s2 = z(Q), z(1)
+    with pytest.raises(GpkError):
+        gpk.psi_fwd(mu, S, Z, l2, s2, psi2_sum=z(M, M))
+    with pytest.raises(GpkError):
+        gpk.psi_bwd(mu, S, Z, l2, s2, z(1, M), z(1, M, M), z(N, 1), z(N, 1), z(N, 1), z(1), z(Q), z(M, Q),
+                    z(1, M), z(1, M, M), z(N, Q), z(N, Q))
