@@ -248,18 +248,22 @@ def run_ours(args, world, rank, local):
     xd = torch.as_tensor(x, device=dev)
     yd = torch.as_tensor(y, device=dev)
     n64 = max(1, min(10, K))
-    for i in range(2):
-        fp64_form.sdgpr_objective(pt, xd, yd, idx_all[i], ALPHA, 2)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for i in range(n64):
-        fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W + i], ALPHA, 2)
-    e1.record()
-    torch.cuda.synchronize()
-    fp64_rate = n64 / (e0.elapsed_time(e1) / 1e3)
-    e64, _ = fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W], ALPHA, 2)
+    fp64_rate, e64 = None, None
+    try:
+        for i in range(2):
+            fp64_form.sdgpr_objective(pt, xd, yd, idx_all[i], ALPHA, 2)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(n64):
+            fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W + i], ALPHA, 2)
+        e1.record()
+        torch.cuda.synchronize()
+        fp64_rate = n64 / (e0.elapsed_time(e1) / 1e3)
+        e64 = float(fp64_form.sdgpr_objective(pt, xd, yd, idx_all[W], ALPHA, 2)[0].item())
+    except RuntimeError as exc:      # e.g. torch's linalg library not loadable under a profiler
+        print('fp64 form skipped: %s' % exc, file=sys.stderr)
 
     # ---- dominant kernel roofline: psi backward of layer 1 on this step's inputs
     lay1 = mdl.layers[1]
@@ -299,7 +303,7 @@ def run_ours(args, world, rank, local):
                 'work_per_launch': ops, 'us_per_launch': round(t_k * 1e6, 2),
                 'hbm_algorithmic_gbs': round(psi_bwd_bytes(MB, M_PSEUDO, HIDDEN, 1) / t_k / 1e9, 2),
                 'hbm_peak_gbs': peaks.get('hbm_gbs'), 'traffic': None}
-    out = {'e_gpu': e_gpu, 'e_fp64': float(e64.item()), 'value': value, 'ms': 1e3 * t_dev / K,
+    out = {'e_gpu': e_gpu, 'e_fp64': e64, 'value': value, 'ms': 1e3 * t_dev / K,
            'e2e': e2e, 'fp64_rate': fp64_rate, 'n64': n64, 'roofline': roofline, 'clocks': clocks,
            'launches_per_eval': launches_per_eval, 'params': params, 'x': x, 'y': y,
            'idx0': idx_np[W]}
@@ -364,11 +368,13 @@ def main():
                        'l2': 'flushed (256 MiB write) between timed steps; CUDA-graph replay per step'},
             'roofline': r['roofline'], 'cpu_baseline': cpu, 'e2e': r['e2e'], 'clocks': r['clocks'],
             'gpu_launches': r['launches_per_eval'] * args.steps,
-            'fp64_gpu_form': {'value': r['fp64_rate'], 'unit': 'evals/s', 'steps': r['n64'],
-                              'speedup_of_value': r['value'] / r['fp64_rate'],
-                              'speedup_of_e2e': r['e2e']['value'] / r['fp64_rate']},
+            'fp64_gpu_form': None if r['fp64_rate'] is None else {
+                'value': r['fp64_rate'], 'unit': 'evals/s', 'steps': r['n64'],
+                'speedup_of_value': r['value'] / r['fp64_rate'],
+                'speedup_of_e2e': r['e2e']['value'] / r['fp64_rate']},
             'parity': {'energy_rel_err_vs_oracle': abs(r['e_gpu'] - e_ref) / abs(e_ref),
-                       'fp64_form_energy_rel_err_vs_oracle': abs(r['e_fp64'] - e_ref) / abs(e_ref),
+                       'fp64_form_energy_rel_err_vs_oracle': None if r['e_fp64'] is None else
+                       abs(r['e_fp64'] - e_ref) / abs(e_ref),
                        'tolerance': 1e-6}}
     print(json.dumps(line))
     if world > 1:

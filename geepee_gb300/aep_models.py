@@ -321,6 +321,11 @@ class SGPR(_PackedModel):
 class SDGPR(_PackedModel):
     """Deep GP regression with AEP and moment-matching propagation."""
 
+    def _side_streams(self):
+        if not hasattr(self, '_sides'):
+            self._sides = [torch.cuda.Stream(device=self.dev) for _ in range(2)]
+        return self._sides
+
     def __init__(self, x_train, y_train, no_pseudos, hidden_sizes, lik='Gaussian'):
         super().__init__(y_train)
         if lik.lower() != 'gaussian':
@@ -368,12 +373,22 @@ class SDGPR(_PackedModel):
             vs.append(v)
         logZ, dm, dv = gauss_logZ(ms[-1], vs[-1], yb, self.sn, alpha)
         dmi, dvi = scale * dm, scale * dv
+        # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
+        # while the backward continues into layer i-1 (a parallel branch of the captured graph)
+        main = torch.cuda.current_stream()
+        side = self._side_streams()
         for i in range(L - 1, -1, -1):
             lay = self.layers[i]
             if i == 0:
                 lay.bwd_det(alpha, dmi, dvi, kfu, Bk, xb)
             else:
-                dmi, dvi = lay.bwd_mm(alpha, ms[i], dmi, dvi, ms[i - 1], vs[i - 1])
+                dmi, dvi = lay.bwd_mm_data(alpha, ms[i], dmi, dvi, ms[i - 1], vs[i - 1])
+                st = side[i % len(side)]
+                st.wait_stream(main)
+                with torch.cuda.stream(st):
+                    lay.bwd_mm_algebra(alpha)
+        for st in side:
+            main.wait_stream(st)
         self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
         energy = scale * logZ
         for lay in self.layers:

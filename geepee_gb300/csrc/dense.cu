@@ -6,83 +6,103 @@
 
 namespace {
 
-constexpr int TB = 32;   // GEMM tile
 constexpr int TK = 16;   // GEMM k-chunk
 
-template <typename T>
+// C tile TBM x TBM per CTA (256 threads, R x R outputs each with R = TBM/16).  The k extent is
+// staged through shared memory in chunks of up to KC: all global loads of a chunk are issued
+// together (one latency per chunk instead of one per 16-wide slice), then R*R*KC double-float
+// multiply-adds per thread run from shared memory.
+constexpr int KC = 128;
+template <typename T, int TBM>
 __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, int tA, int tB, double alpha,
                                                    const typename Num<T>::store_t* A, int lda, long sA,
                                                    const typename Num<T>::store_t* B, int ldb, long sB,
                                                    double beta, typename Num<T>::store_t* C, int ldc, long sC) {
   typedef typename Num<T>::store_t S;
-  __shared__ T As[TK][TB + 1];
-  __shared__ T Bs[TK][TB + 1];
+  constexpr int R = TBM / 16;
+  extern __shared__ __align__(16) char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);      // [KC][TBM]
+  T* Bs = As + KC * TBM;                        // [KC][TBM]
   const int bz = blockIdx.z;
   A += bz * sA;
   B += bz * sB;
   C += bz * sC;
-  const int i0 = blockIdx.y * TB, j0 = blockIdx.x * TB;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 2 x 2 outputs each
-  T acc[2][2];
+  const int i0 = blockIdx.y * TBM, j0 = blockIdx.x * TBM;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[R][R];
 #pragma unroll
-  for (int r = 0; r < 2; ++r)
+  for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int c = 0; c < 2; ++c) acc[r][c] = Num<T>::zero();
-  for (int k0 = 0; k0 < k; k0 += TK) {
-    for (int e = threadIdx.x; e < TK * TB; e += 256) {
-      int kk = e / TB, ii = e % TB;
+    for (int c = 0; c < R; ++c) acc[r][c] = Num<T>::zero();
+  for (int k0 = 0; k0 < k; k0 += KC) {
+    const int kc = min(KC, k - k0);
+    // A tile: element (ii, kk) of op(A); consecutive threads take consecutive memory
+    for (int e = threadIdx.x; e < kc * TBM; e += 256) {
+      int kk, ii;
+      if (tA) { kk = e / TBM; ii = e % TBM; } else { ii = e / kc; kk = e % kc; }
       int gi = i0 + ii, gk = k0 + kk;
       T av = Num<T>::zero();
-      if (gi < m && gk < k) av = Num<T>::ld(tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk]);
-      As[kk][ii] = av;
-      int gj = j0 + ii;
+      if (gi < m) av = Num<T>::ld(tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk]);
+      As[kk * TBM + ii] = av;
+    }
+    for (int e = threadIdx.x; e < kc * TBM; e += 256) {
+      int kk, jj;
+      if (tB) { jj = e / kc; kk = e % kc; } else { kk = e / TBM; jj = e % TBM; }
+      int gj = j0 + jj, gk = k0 + kk;
       T bv = Num<T>::zero();
-      if (gj < n && gk < k) bv = Num<T>::ld(tB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj]);
-      Bs[kk][ii] = bv;
+      if (gj < n) bv = Num<T>::ld(tB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj]);
+      Bs[kk * TBM + jj] = bv;
     }
     __syncthreads();
 #pragma unroll 4
-    for (int kk = 0; kk < TK; ++kk) {
-      T a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
-      T b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
-      acc[0][0] = fma_(a0, b0, acc[0][0]);
-      acc[0][1] = fma_(a0, b1, acc[0][1]);
-      acc[1][0] = fma_(a1, b0, acc[1][0]);
-      acc[1][1] = fma_(a1, b1, acc[1][1]);
+    for (int kk = 0; kk < kc; ++kk) {
+      T av[R], bv[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        av[r] = As[kk * TBM + ty * R + r];
+        bv[r] = Bs[kk * TBM + tx * R + r];
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc[r][c] = fma_(av[r], bv[c], acc[r][c]);
     }
     __syncthreads();
   }
+  const bool unit = alpha == 1.0;
   const T al = Num<T>::ld(static_cast<S>(alpha));
   const T be = Num<T>::ld(static_cast<S>(beta));
 #pragma unroll
-  for (int r = 0; r < 2; ++r)
+  for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      int gi = i0 + ty * 2 + r, gj = j0 + tx * 2 + c;
+    for (int c = 0; c < R; ++c) {
+      int gi = i0 + ty * R + r, gj = j0 + tx * R + c;
       if (gi < m && gj < n) {
-        T v = mul(al, acc[r][c]);
+        T v = unit ? acc[r][c] : mul(al, acc[r][c]);
         if (beta != 0.0) v = fma_(be, Num<T>::ld(C[(size_t)gi * ldc + gj]), v);
         C[(size_t)gi * ldc + gj] = Num<T>::st(v);
       }
     }
 }
 
-// ---- SPD Cholesky + inverse, one 1024-thread CTA per matrix, matrix in shared memory ----
-template <typename T>
+// GMEM = false: the matrix lives in shared memory (M <= 128).  GMEM = true: it lives in the
+// caller's workspace (work, M*M elements per matrix, L2-resident), any M.
+template <typename T, bool GMEM>
 __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Num<T>::store_t* A, long sA,
                                                         typename Num<T>::store_t* Ainv, long sI,
                                                         typename Num<T>::store_t* Lout, long sL, double* logdet,
-                                                        int* info) {
+                                                        int* info, typename Num<T>::store_t* work) {
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
-  const int ld = M + 1;
-  T* S = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][M+1]
-  T* dg = S + M * ld;                                              // [M] diagonal of L
+  const int b = blockIdx.x;
+  const int ld = GMEM ? M : M + 1;
+  T* base = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));
+  T* S = GMEM ? reinterpret_cast<T*>(work) + (size_t)b * M * M : base;   // [M][ld]
+  T* dg = GMEM ? base : base + M * ld;                             // [M] diagonal of L
   T* di = dg + M;                                                  // [M] 1/diag
   T* tmp = di + M;                                                 // [M]
   T* red = tmp + M;                                                // [32]
   __shared__ int s_info;
-  const int b = blockIdx.x;
   A += b * sA;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   load_exp_table(tab);
@@ -141,7 +161,8 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
     }
   }
   if (logdet) {
-    T l = tid < M ? log_tab(dg[tid], tab) : Num<T>::zero();
+    T l = Num<T>::zero();
+    for (int i = tid; i < M; i += blockDim.x) l = add(l, log_tab(dg[i], tab));
     l = warp_sum(l);
     if (tx == 0) red[ty] = l;
     __syncthreads();
@@ -158,14 +179,18 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
   for (int k = M - 1 + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + (M - 1)];
   __syncthreads();
   for (int j = M - 1; j >= 0; --j) {
-    int i = j + 1 + (tid >> 3), sl = tid & 7;   // 8 threads per row
-    T s = Num<T>::zero();
-    if (i < M)
-      for (int k = j + 1 + sl; k <= i; k += 8) s = fma_(S[i * ld + k], tmp[k], s);
+    // 8 threads per row, 128 rows per pass.  Row i reads only columns > j of S and the staged
+    // column tmp, so writing X_ij into column j right away cannot race with other rows.
+    for (int r0 = j + 1; r0 < M; r0 += 128) {
+      int i = r0 + (tid >> 3), sl = tid & 7;
+      T s = Num<T>::zero();
+      if (i < M)
+        for (int k = j + 1 + sl; k <= i; k += 8) s = fma_(S[i * ld + k], tmp[k], s);
 #pragma unroll
-    for (int m = 1; m < 8; m <<= 1) s = add(s, shfl_xor(s, m));
+      for (int m = 1; m < 8; m <<= 1) s = add(s, shfl_xor(s, m));
+      if (i < M && sl == 0) S[i * ld + j] = neg(mul(di[j], s));
+    }
     __syncthreads();
-    if (i < M && sl == 0) S[i * ld + j] = neg(mul(di[j], s));
     if (tid == 0) S[j * ld + j] = di[j];
     if (j > 0)
       for (int k = j + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + (j - 1)];
@@ -195,6 +220,7 @@ __global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const type
                                                         const typename Num<T>::store_t* Z, const double* lls2,
                                                         const double* lsf2, double s_sf, double s_ls,
                                                         double* g_sf, double* g_ls, double* g_z) {
+  // one warp per pseudo-input a (lanes over b), 8 rows per CTA
   typedef typename Num<T>::store_t S;
   __shared__ float2 tab[256];
   __shared__ T il[8], lsf;
@@ -202,59 +228,69 @@ __global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const type
   load_exp_table(tab);
   __syncthreads();
   if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
-  if (threadIdx.x == 0) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
+  if (threadIdx.x == 32) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
   __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int a = blockIdx.x * 8 + warp;
   T gs = Num<T>::zero();
-  T gl[8];
+  T gl[8], gz[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) gl[q] = Num<T>::zero();
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
-    T gz[8];
+  for (int q = 0; q < 8; ++q) gl[q] = gz[q] = Num<T>::zero();
+  if (a < M) {
+    T za[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) gz[q] = Num<T>::zero();
-    for (int b = 0; b < M; ++b) {
+    for (int q = 0; q < 8; ++q) za[q] = q < Q ? Num<T>::ld(Z[a * Q + q]) : Num<T>::zero();
+    for (int b = lane; b < M; b += 32) {
       T r = Num<T>::zero();
-      for (int q = 0; q < Q; ++q) {
-        T d = sub(Num<T>::ld(Z[a * Q + q]), Num<T>::ld(Z[b * Q + q]));
-        r = fma_(mul(d, d), il[q], r);
+      T d[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        d[q] = q < Q ? sub(Num<T>::ld(Z[b * Q + q]), za[q]) : Num<T>::zero();   // z_b - z_a
+        if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
       }
       T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
       T mab = Num<T>::ld(Mm[(size_t)a * M + b]);
       T w = mul(mab, k);
       T ws = mul(add(mab, Num<T>::ld(Mm[(size_t)b * M + a])), k);
       gs = add(gs, w);
-      for (int q = 0; q < Q; ++q) {
-        T d = sub(Num<T>::ld(Z[b * Q + q]), Num<T>::ld(Z[a * Q + q]));
-        T dil = mul(d, il[q]);
-        gl[q] = fma_(mul(w, d), dil, gl[q]);
-        gz[q] = fma_(ws, dil, gz[q]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (q < Q) {
+          T dil = mul(d[q], il[q]);
+          gl[q] = fma_(mul(w, d[q]), dil, gl[q]);
+          gz[q] = fma_(ws, dil, gz[q]);
+        }
       }
     }
-    for (int q = 0; q < Q; ++q) atomicAdd(&g_z[a * Q + q], (double)Num<T>::st(gz[q]));
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q < Q) {
+        T v = warp_sum(gz[q]);
+        if (lane == 0) atomicAdd(&g_z[a * Q + q], (double)Num<T>::st(v));
+      }
+    }
   }
   // reduce gs and gl over the CTA
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T v[9];
   v[0] = gs;
 #pragma unroll
   for (int q = 0; q < 8; ++q) v[1 + q] = gl[q];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    T s = warp_sum(v[i]);
-    if (lane == 0) red[warp][i] = s;
+    T t = warp_sum(v[i]);
+    if (lane == 0) red[warp][i] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int i = 0; i < 9; ++i) {
-      T s = red[0][i];
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = add(s, red[w][i]);
-      v[i] = s;
+      T t = red[0][i];
+      for (int w = 1; w < 8; ++w) t = add(t, red[w][i]);
+      v[i] = t;
     }
     atomicAdd(g_sf, s_sf * (double)Num<T>::st(v[0]));
     for (int q = 0; q < Q; ++q) atomicAdd(&g_ls[q], s_ls * 0.5 * (double)Num<T>::st(v[1 + q]));
   }
 }
-
 
 // Many tiny SPD matrices (n <= 8), one thread each: inverse and log-determinant by an
 // in-register Cholesky.  The per-time-step Dy x Dy emission covariances of the GP
@@ -316,9 +352,21 @@ template <typename T>
 int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
                 const void* B, int ldb, long sB, double beta, void* C, int ldc, long sC, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
-  dim3 grid(gpk::ceil_div(n, TB), gpk::ceil_div(m, TB), batch);
-  gemm_kernel<T><<<grid, 256, 0, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB, beta,
-                                       (S*)C, ldc, sC);
+  // 32x32 tiles when they already fill the GPU, else 16x16 tiles for more CTAs
+  long tiles32 = (long)gpk::ceil_div(n, 32) * gpk::ceil_div(m, 32) * batch;
+  if (tiles32 >= 2L * gpk::sm_count()) {
+    dim3 grid(gpk::ceil_div(n, 32), gpk::ceil_div(m, 32), batch);
+    size_t sm = 2 * KC * 32 * sizeof(T);
+    auto kfn = gemm_kernel<T, 32>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    kfn<<<grid, 256, sm, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB, beta, (S*)C,
+                               ldc, sC);
+  } else {
+    dim3 grid(gpk::ceil_div(n, 16), gpk::ceil_div(m, 16), batch);
+    size_t sm = 2 * KC * 16 * sizeof(T);
+    gemm_kernel<T, 16><<<grid, 256, sm, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB,
+                                              beta, (S*)C, ldc, sC);
+  }
   return gpk::check_launch("gemm");
 }
 
@@ -342,27 +390,39 @@ extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, in
   return gpk::fail(GPK_EINVAL, "gemm: unknown precision %d", prec);
 }
 
-extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
-                            void* stream) {
-  GPK_REQUIRE(batch >= 0 && M >= 1 && M <= 128, "chol_inv: M=%d outside [1,128]", M);
+template <typename T, bool GMEM>
+int chol_launch(int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info, void* work,
+                cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  long s = (long)M * M;
+  size_t sm = 256 * 8 + ((GMEM ? 0 : (size_t)M * (M + 1)) + 3 * M + 32) * sizeof(T);
+  auto k = chol_inv_kernel<T, GMEM>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<batch, 1024, sm, st>>>(M, (const S*)A, s, (S*)Ainv, s, (S*)L, s, logdet, info, (S*)work);
+  return gpk::check_launch("chol_inv");
+}
+
+extern "C" int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet,
+                               int* info, void* work, void* stream) {
+  GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "chol_inv: M=%d outside [1,4096]", M);
   GPK_REQUIRE(A, "chol_inv: null input");
+  GPK_REQUIRE(M <= 128 || work, "chol_inv: M=%d > 128 needs a workspace of batch*M*M elements", M);
   if (batch == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  long s = (long)M * M;
-  if (prec == GPK_DF64) {
-    size_t sm = 256 * 8 + ((size_t)M * (M + 1) + 3 * M + 32) * sizeof(df64);
-    auto k = chol_inv_kernel<df64>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<batch, 1024, sm, st>>>(M, (const double*)A, s, (double*)Ainv, s, (double*)L, s, logdet, info);
-  } else if (prec == GPK_FP32) {
-    size_t sm = 256 * 8 + ((size_t)M * (M + 1) + 3 * M + 32) * sizeof(float);
-    auto k = chol_inv_kernel<float>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<batch, 1024, sm, st>>>(M, (const float*)A, s, (float*)Ainv, s, (float*)L, s, logdet, info);
-  } else {
-    return gpk::fail(GPK_EINVAL, "chol_inv: unknown precision %d", prec);
-  }
-  return gpk::check_launch("chol_inv");
+  const bool gm = M > 128;
+  if (prec == GPK_DF64)
+    return gm ? chol_launch<df64, true>(batch, M, A, Ainv, L, logdet, info, work, st)
+              : chol_launch<df64, false>(batch, M, A, Ainv, L, logdet, info, work, st);
+  if (prec == GPK_FP32)
+    return gm ? chol_launch<float, true>(batch, M, A, Ainv, L, logdet, info, work, st)
+              : chol_launch<float, false>(batch, M, A, Ainv, L, logdet, info, work, st);
+  return gpk::fail(GPK_EINVAL, "chol_inv: unknown precision %d", prec);
+}
+
+extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
+                            void* stream) {
+  GPK_REQUIRE(M <= 128, "chol_inv: M=%d > 128 needs gpk_chol_inv_ws", M);
+  return gpk_chol_inv_ws(prec, batch, M, A, Ainv, L, logdet, info, nullptr, stream);
 }
 
 extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
@@ -371,12 +431,12 @@ extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void*
   GPK_REQUIRE(M >= 1 && Q >= 1 && Q <= 8, "trace_kzz: bad sizes M=%d Q=%d", M, Q);
   GPK_REQUIRE(Mm && Z && lls2 && lsf2 && g_sf && g_ls && g_z, "trace_kzz: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
-  int grid = gpk::ceil_div(M, 128);
+  int grid = gpk::ceil_div(M, 8);
   if (prec == GPK_DF64)
-    trace_kzz_kernel<df64><<<grid, 128, 0, st>>>(M, Q, (const double*)Mm, (const double*)Z, lls2, lsf2, s_sf, s_ls,
+    trace_kzz_kernel<df64><<<grid, 256, 0, st>>>(M, Q, (const double*)Mm, (const double*)Z, lls2, lsf2, s_sf, s_ls,
                                                  g_sf, g_ls, g_z);
   else if (prec == GPK_FP32)
-    trace_kzz_kernel<float><<<grid, 128, 0, st>>>(M, Q, (const float*)Mm, (const float*)Z, lls2, lsf2, s_sf, s_ls,
+    trace_kzz_kernel<float><<<grid, 256, 0, st>>>(M, Q, (const float*)Mm, (const float*)Z, lls2, lsf2, s_sf, s_ls,
                                                   g_sf, g_ls, g_z);
   else
     return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);

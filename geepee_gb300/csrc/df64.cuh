@@ -20,10 +20,60 @@ struct df64 {
 
 __host__ __device__ __forceinline__ df64 make_df(float h, float l = 0.f) { df64 r; r.hi = h; r.lo = l; return r; }
 
-__device__ __forceinline__ df64 df_from_double(double x) {
+// float64 -> (hi, lo): hi = x rounded to float, lo = (x - hi) rounded to float.  Done with
+// integer operations on the bit pattern (round-to-nearest-even of the 53-bit significand to
+// 24 bits, then the signed remainder normalised to 24 bits): the FP64 pipe, which the plain
+// conversion would use, issues ~64x slower than the integer pipes on this part.  Exponents
+// outside 2^-74 .. 2^127 (and zeros, subnormals, inf, nan) take the FP64 path.
+__device__ __forceinline__ df64 df_from_double_fp64(double x) {
   float h = __double2float_rn(x);
   float l = __double2float_rn(x - (double)h);
   return make_df(h, l);
+}
+__device__ __forceinline__ df64 df_from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 949 || e > 1150) return df_from_double_fp64(x);
+  const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  unsigned top = (unsigned)(mant >> 29);
+  int rem = (int)(mant & 0x1FFFFFFFull);
+  if (rem > 0x10000000 || (rem == 0x10000000 && (top & 1u))) {
+    top += 1u;
+    rem -= 0x20000000;
+  }
+  int fe = e - 1023 + 127;
+  if (top == 0x1000000u) {
+    top >>= 1;
+    fe += 1;
+  }
+  const unsigned sign = (unsigned)(b >> 63);
+  const float hi = __uint_as_float((sign << 31) | ((unsigned)fe << 23) | (top & 0x7fffffu));
+  float lo = 0.f;
+  if (rem != 0) {
+    unsigned rs = 0u;
+    unsigned r = (unsigned)rem;
+    if (rem < 0) {
+      rs = 1u;
+      r = (unsigned)(-rem);
+    }
+    const int nb = 32 - __clz(r);
+    int sh = nb - 24;
+    unsigned m;
+    if (sh > 0) {
+      m = r >> sh;
+      const unsigned rem2 = r & ((1u << sh) - 1u), half = 1u << (sh - 1);
+      if (rem2 > half || (rem2 == half && (m & 1u))) ++m;
+      if (m == 0x1000000u) {
+        m >>= 1;
+        ++sh;
+      }
+    } else {
+      m = r << (-sh);
+    }
+    const int le = e - 1075 + sh + 23 + 127;
+    lo = __uint_as_float(((sign ^ rs) << 31) | ((unsigned)le << 23) | (m & 0x7fffffu));
+  }
+  return make_df(hi, lo);
 }
 __device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
 

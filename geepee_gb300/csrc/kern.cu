@@ -63,14 +63,17 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
                                                       typename Num<T>::store_t* kfu,
                                                       typename Num<T>::store_t* Bk,
                                                       typename Num<T>::store_t* m_out,
-                                                      typename Num<T>::store_t* v_out) {
+                                                      typename Num<T>::store_t* v_out, int bstage) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
   T* kr = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [RR][M]
-  T* red = kr + RR * M;                                                              // [32][64]
+  T* red = kr + RR * M;                                                              // [33][64]
+  T* Bsm = red + 33 * 64;                                        // [Dout][M][M] when staged
   load_exp_table(tab);
+  if (bstage)
+    for (int i = threadIdx.x; i < Dout * M * M; i += blockDim.x) Bsm[i] = Num<T>::ld(B[i]);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
   __syncthreads();
@@ -99,10 +102,19 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
         T acc[RR];
 #pragma unroll
         for (int r = 0; r < RR; ++r) acc[r] = Num<T>::zero();
-        for (int a = 0; a < M; ++a) {
-          T bab = Num<T>::ld(Bd[(size_t)a * M + b]);
+        if (bstage) {
+          const T* Bt = Bsm + (size_t)d * M * M;
+          for (int a = 0; a < M; ++a) {
+            T bab = Bt[(size_t)a * M + b];
 #pragma unroll
-          for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
+            for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
+          }
+        } else {
+          for (int a = 0; a < M; ++a) {
+            T bab = Num<T>::ld(Bd[(size_t)a * M + b]);
+#pragma unroll
+            for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
+          }
         }
         T ad = Num<T>::ld(A[(size_t)d * M + b]);
 #pragma unroll
@@ -379,17 +391,21 @@ extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* 
   if (grid > cap) grid = cap;
   if (prec == GPK_DF64) {
     size_t sm = det_fwd_smem(M, sizeof(df64));
+    int bstage = sm + (size_t)Dout * M * M * sizeof(df64) <= 200 * 1024;
+    if (bstage) sm += (size_t)Dout * M * M * sizeof(df64);
     auto k = det_fwd_kernel<df64>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
                              (const double*)A, (const double*)B, (double*)kfu, (double*)Bk, (double*)m_out,
-                             (double*)v_out);
+                             (double*)v_out, bstage);
   } else if (prec == GPK_FP32) {
     size_t sm = det_fwd_smem(M, sizeof(float));
+    int bstage = sm + (size_t)Dout * M * M * sizeof(float) <= 200 * 1024;
+    if (bstage) sm += (size_t)Dout * M * M * sizeof(float);
     auto k = det_fwd_kernel<float>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
-                             (const float*)B, (float*)kfu, (float*)Bk, (float*)m_out, (float*)v_out);
+                             (const float*)B, (float*)kfu, (float*)Bk, (float*)m_out, (float*)v_out, bstage);
   } else {
     return gpk::fail(GPK_EINVAL, "det_fwd: unknown precision %d", prec);
   }

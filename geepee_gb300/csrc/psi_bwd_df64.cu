@@ -1,0 +1,5 @@
+// df64 instantiation of the psi backward kernels (one translation unit per kernel family
+// and precision, so the build compiles them in parallel).
+#include "psi_impl.cuh"
+
+int psi_bwd_df64(const psi_impl::PsiArgs<double>& a, cudaStream_t st) { return psi_impl::launch_bwd<df64>(a, st); }

@@ -1,0 +1,5 @@
+// f32 instantiation of the psi backward kernels (one translation unit per kernel family
+// and precision, so the build compiles them in parallel).
+#include "psi_impl.cuh"
+
+int psi_bwd_f32(const psi_impl::PsiArgs<float>& a, cudaStream_t st) { return psi_impl::launch_bwd<float>(a, st); }

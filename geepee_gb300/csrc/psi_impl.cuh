@@ -5,17 +5,21 @@
 // n; for each point its threads first build per-point tables in shared memory
 // (per-dimension constants, per-pseudo-input terms u_a, h_aq), then sweep the
 // M(M+1)/2 unordered pairs (a <= b) of pseudo-inputs.  Each thread owns a fixed set of
-// pairs (p = tid + k*blockDim) across all of its points, so sums over n of per-pair
+// pairs (p = tid + k*NT) across all of its points, so sums over n of per-pair
 // quantities (sum_n psi2, dB = sum_n dv psi2) stay in registers until one atomic
 // flush per CTA.  psi2 per point is never materialised in HBM (unless requested).
 //
 // log psi2[n,a,b] = u_a + u_b + G_ab - sum_q h_aq z_bq   with
-//   G_ab = -sum_q (z_aq - z_bq)^2 / (4 l_q)                      (per call)
+//   G_ab = -sum_q (z_aq - z_bq)^2 / (4 l_q)                      (per call, shared memory)
 //   u_a  = k_n/2 + sum_q c_q z_aq (mu_q - z_aq/4),  h_aq = c_q z_aq / 2   (per point)
 //   k_n  = 2 log sf2 + 1/2 sum_q log(l_q / (l_q + 2 S_q)) - sum_q c_q mu_q^2,
 //   c_q  = 1 / (l_q + 2 S_q)
 // which is the reference's exponent (geepee/kernels.py:219-225) regrouped so that the
 // inner loop costs Q multiply-adds plus one exp.
+//
+// Template parameters: T compute type (df64 or float); PPT pairs per thread held in
+// registers (0: plain strided sweep); QC a compile-time cap on Q and DB on Dout, so
+// every per-dimension / per-output array is fully unrolled into registers.
 #pragma once
 #include "common.cuh"
 
@@ -25,6 +29,7 @@ constexpr int QMAX = 8;
 constexpr int DMAX = 4;
 constexpr int NT = 512;        // threads per CTA
 constexpr int PPT_MAX = 16;    // pairs per thread for register-resident per-pair sums
+constexpr int RED = 24;        // reduction slots per warp
 
 template <typename S>
 struct PsiArgs {
@@ -69,24 +74,25 @@ template <typename T>
 struct Smem {
   float2* tab;   // [256]
   T* z;          // [M*Q]
-  T* ell2;       // [Q]
-  T* lnl;        // [Q]   log ell2
-  T* inv4l;      // [Q]   1/(4 ell2)
-  T* misc;       // [4]   log sf2, sf2, ...
-  T* pmu;        // [Q]   per point
-  T* pis1;       // [Q]   1/(l+S)
-  T* pc;         // [Q]   1/(l+2S)
-  T* pld1;       // [Q]   1/2 log(l/(l+S))
-  T* pld2;       // [Q]   1/2 log(l/(l+2S))
+  T* ell2;       // [QMAX]
+  T* lnl;        // [QMAX] log ell2
+  T* inv4l;      // [QMAX] 1/(4 ell2)
+  T* il;         // [QMAX] 1/ell2
+  T* misc;       // [4]    log sf2, sf2
+  T* pmu;        // [QMAX] per point
+  T* pis1;       // [QMAX] 1/(l+S)
+  T* pc;         // [QMAX] 1/(l+2S)
+  T* pld1;       // [QMAX] 1/2 log(l/(l+S))
+  T* pld2;       // [QMAX] 1/2 log(l/(l+2S))
   T* pd;         // [2*DMAX] per-point dm_all, dv
   T* u;          // [M]
   T* h;          // [M*Q]
-  T* ps1;        // [M]
   T* G;          // [P]
   T* Bs;         // [Dout*P] symmetrised B (B_ab + B_ba off the diagonal), or nullptr
-  T* red;        // [32 * 24]
+  T* red;        // [32 * RED]
   T* L;          // [P]   (backward only)
-  T* rows;       // [M*(1+Q)] row statistics (backward only)
+  T* rows;       // [M*(1+QMAX)] row statistics (backward only)
+  T* dz;         // [M*Q]  dZ accumulator over the CTA's points (backward only)
 };
 
 template <typename T>
@@ -98,6 +104,7 @@ __device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd, int nbs) {
   s.ell2 = t; t += QMAX;
   s.lnl = t; t += QMAX;
   s.inv4l = t; t += QMAX;
+  s.il = t; t += QMAX;
   s.misc = t; t += 4;
   s.pmu = t; t += QMAX;
   s.pis1 = t; t += QMAX;
@@ -107,45 +114,48 @@ __device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd, int nbs) {
   s.pd = t; t += 2 * DMAX;
   s.u = t; t += M;
   s.h = t; t += M * Q;
-  s.ps1 = t; t += M;
   s.G = t; t += P;
   s.Bs = nbs ? t : nullptr; t += nbs;
-  s.red = t; t += 32 * 24;
+  s.red = t; t += 32 * RED;
   if (bwd) {
     s.L = t; t += P;
     s.rows = t; t += M * (1 + QMAX);
+    s.dz = t; t += M * Q;
   } else {
     s.L = nullptr;
     s.rows = nullptr;
+    s.dz = nullptr;
   }
   return s;
 }
 
 __host__ __device__ inline size_t smem_bytes(int M, int Q, int P, bool bwd, size_t tsz, int nbs) {
-  size_t n = (size_t)M * Q + 5 * QMAX + 4 + 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + M + P + nbs + 32 * 24;
-  if (bwd) n += P + (size_t)M * (1 + QMAX);
+  size_t n = (size_t)M * Q + 10 * QMAX + 4 + 2 * DMAX + M + (size_t)M * Q + P + nbs + 32 * RED;
+  if (bwd) n += P + (size_t)M * (1 + QMAX) + (size_t)M * Q;
   return 256 * 8 + n * tsz;
 }
 
-// CTA-wide sum of K values per thread (K <= 24); result valid in warp 0.
-template <typename T>
-__device__ __forceinline__ void block_sum(T* vals, int K, T* red) {
+// CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.
+template <typename T, int K>
+__device__ __forceinline__ void block_sum(T* vals, T* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
   for (int i = 0; i < K; ++i) {
     T s = warp_sum(vals[i]);
-    if (lane == 0) red[warp * 24 + i] = s;
+    if (lane == 0) red[warp * RED + i] = s;
   }
   __syncthreads();
   if (warp == 0) {
+#pragma unroll
     for (int i = 0; i < K; ++i) {
-      T s = lane < nw ? red[lane * 24 + i] : Num<T>::zero();
+      T s = lane < nw ? red[lane * RED + i] : Num<T>::zero();
       vals[i] = warp_sum(s);
     }
   }
 }
 
-// common per-CTA setup: exp table, Z, lengthscales, signal variance, G table
-template <typename T, typename S>
+// common per-CTA setup: exp table, Z, lengthscales, signal variance, G and B tables
+template <typename T, typename S, int QC>
 __device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
   const int M = a.M, Q = a.Q;
   load_exp_table(s.tab);
@@ -157,6 +167,7 @@ __device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
     T l2 = exp_tab(lnl, s.tab);
     s.lnl[q] = lnl;
     s.ell2[q] = l2;
+    s.il[q] = recip(l2);
     s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
   }
   if (threadIdx.x == 32) {
@@ -169,9 +180,12 @@ __device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
     int ia, ib;
     pair_of(p, ia, ib);
     T g = Num<T>::zero();
-    for (int q = 0; q < Q; ++q) {
-      T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
-      g = fma_(mul(d, d), s.inv4l[q], g);
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      if (q < Q) {
+        T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
+        g = fma_(mul(d, d), s.inv4l[q], g);
+      }
     }
     s.G[p] = neg(g);
     if (s.Bs) {
@@ -203,46 +217,50 @@ __device__ __forceinline__ void point_dims(const PsiArgs<S>& a, Smem<T>& s, int 
 }
 
 // per-pseudo-input terms for point n: psi1_a, u_a, h_aq (threads over a)
-template <typename T>
-__device__ __forceinline__ T point_rows(Smem<T>& s, int M, int Q, int ia) {
+template <typename T, int QC>
+__device__ __forceinline__ T point_rows(Smem<T>& s, int Q, int ia) {
   const T lsf = s.misc[0];
   T e1 = lsf;
   T kap = add(lsf, lsf);
-  for (int q = 0; q < Q; ++q) {
-    T d = sub(s.pmu[q], s.z[ia * Q + q]);
-    e1 = add(e1, sub(s.pld1[q], scale2(mul(mul(d, d), s.pis1[q]), -1)));
-    kap = add(kap, sub(s.pld2[q], mul(mul(s.pmu[q], s.pmu[q]), s.pc[q])));
+#pragma unroll
+  for (int q = 0; q < QC; ++q) {
+    if (q < Q) {
+      T d = sub(s.pmu[q], s.z[ia * Q + q]);
+      e1 = add(e1, sub(s.pld1[q], scale2(mul(mul(d, d), s.pis1[q]), -1)));
+      kap = add(kap, sub(s.pld2[q], mul(mul(s.pmu[q], s.pmu[q]), s.pc[q])));
+    }
   }
   T u = scale2(kap, -1);
-  for (int q = 0; q < Q; ++q) {
-    T zq = s.z[ia * Q + q];
-    T czq = mul(s.pc[q], zq);
-    u = add(u, mul(czq, sub(s.pmu[q], scale2(zq, -2))));
-    s.h[ia * Q + q] = scale2(czq, -1);
+#pragma unroll
+  for (int q = 0; q < QC; ++q) {
+    if (q < Q) {
+      T zq = s.z[ia * Q + q];
+      T czq = mul(s.pc[q], zq);
+      u = add(u, mul(czq, sub(s.pmu[q], scale2(zq, -2))));
+      s.h[ia * Q + q] = scale2(czq, -1);
+    }
   }
   s.u[ia] = u;
-  T p1 = exp_tab(e1, s.tab);
-  s.ps1[ia] = p1;
-  return p1;
+  return exp_tab(e1, s.tab);
 }
 
-template <typename T>
+template <typename T, int QC>
 __device__ __forceinline__ T pair_psi2(const Smem<T>& s, int Q, int p, int ia, int ib) {
   T x = add(add(s.u[ia], s.u[ib]), s.G[p]);
   T cr = Num<T>::zero();
-  for (int q = 0; q < Q; ++q) cr = fma_(s.h[ia * Q + q], s.z[ib * Q + q], cr);
+#pragma unroll
+  for (int q = 0; q < QC; ++q)
+    if (q < Q) cr = fma_(s.h[ia * Q + q], s.z[ib * Q + q], cr);
   return exp_tab(sub(x, cr), s.tab);
 }
 
 // ---------------------------------------------------------------------------------
-template <typename T>
+template <typename T, int QC>
 __device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a, const Smem<T>& s, int n,
-                                      int p, bool contract, T* vals) {
+                                      int p, int ia, int ib, bool contract, T* vals) {
   typedef typename Num<T>::store_t S;
   const int M = a.M;
-  int ia, ib;
-  pair_of(p, ia, ib);
-  T ps = pair_psi2(s, a.Q, p, ia, ib);
+  T ps = pair_psi2<T, QC>(s, a.Q, p, ia, ib);
   if (a.psi2) {
     S v = Num<T>::st(ps);
     a.psi2[((size_t)n * M + ia) * M + ib] = v;
@@ -250,16 +268,19 @@ __device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a
   }
   if (contract) {
     const int P = M * (M + 1) / 2;
-    for (int d = 0; d < a.Dout; ++d) {
-      T w;
-      if (s.Bs) {
-        w = s.Bs[d * P + p];
-      } else {
-        const S* Bd = a.B + (size_t)d * M * M;
-        w = Num<T>::ld(Bd[ia * M + ib]);
-        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+#pragma unroll
+    for (int d = 0; d < DMAX; ++d) {
+      if (d < a.Dout) {
+        T w;
+        if (s.Bs) {
+          w = s.Bs[d * P + p];
+        } else {
+          const S* Bd = a.B + (size_t)d * M * M;
+          w = Num<T>::ld(Bd[ia * M + ib]);
+          if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+        }
+        vals[DMAX + d] = fma_(w, ps, vals[DMAX + d]);
       }
-      vals[DMAX + d] = fma_(w, ps, vals[DMAX + d]);
     }
   }
   return ps;
@@ -267,7 +288,7 @@ __device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a
 
 // PPT > 0: each thread owns pairs tid + k*NT (k < PPT) and keeps sum_n psi2 in registers.
 // PPT == 0: plain strided sweep over any number of pairs (no psi2_sum).
-template <typename T, int PPT>
+template <typename T, int PPT, int QC>
 __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
@@ -275,10 +296,17 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
   const int P = M * (M + 1) / 2;
   const bool contract = (a.A != nullptr) && (a.B != nullptr) && (a.m_out != nullptr || a.v_out != nullptr);
   Smem<T> s = carve<T>(smem_raw, M, Q, P, false, a.bs_smem ? a.Dout * P : 0);
-  cta_setup<T, S>(a, s, P);
-  T acc[PPT > 0 ? PPT : 1];
+  cta_setup<T, S, QC>(a, s, P);
+  constexpr int KP = PPT > 0 ? PPT : 1;
+  T acc[KP];
+  int pab[KP];
 #pragma unroll
-  for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) acc[k] = Num<T>::zero();
+  for (int k = 0; k < KP; ++k) {
+    acc[k] = Num<T>::zero();
+    int p = threadIdx.x + k * NT, ia = 0, ib = 0;
+    if (PPT > 0 && p < P) pair_of(p, ia, ib);
+    pab[k] = (ia << 16) | ib;
+  }
   __syncthreads();
 
   for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
@@ -288,29 +316,39 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
     for (int i = 0; i < 2 * DMAX; ++i) vals[i] = Num<T>::zero();
     for (int ia = threadIdx.x; ia < M; ia += blockDim.x) {
-      T p1 = point_rows(s, M, Q, ia);
+      T p1 = point_rows<T, QC>(s, Q, ia);
       if (a.psi1) a.psi1[(size_t)n * M + ia] = Num<T>::st(p1);
-      if (contract)
-        for (int d = 0; d < D; ++d) vals[d] = fma_(p1, Num<T>::ld(a.A[d * M + ia]), vals[d]);
+      if (contract) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+          if (d < D) vals[d] = fma_(p1, Num<T>::ld(a.A[d * M + ia]), vals[d]);
+      }
     }
     __syncthreads();
     if (PPT > 0) {
 #pragma unroll
-      for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) {
+      for (int k = 0; k < KP; ++k) {
         int p = threadIdx.x + k * NT;
-        if (p < P) acc[k] = add(acc[k], fwd_pair<T>(a, s, n, p, contract, vals));
+        if (p < P) acc[k] = add(acc[k], fwd_pair<T, QC>(a, s, n, p, pab[k] >> 16, pab[k] & 0xffff, contract, vals));
       }
     } else {
-      for (int p = threadIdx.x; p < P; p += NT) fwd_pair<T>(a, s, n, p, contract, vals);
+      for (int p = threadIdx.x; p < P; p += NT) {
+        int ia, ib;
+        pair_of(p, ia, ib);
+        fwd_pair<T, QC>(a, s, n, p, ia, ib, contract, vals);
+      }
     }
     if (contract) {
-      block_sum(vals, 2 * DMAX, s.red);
+      block_sum<T, 2 * DMAX>(vals, s.red);
       if (threadIdx.x == 0) {
-        for (int d = 0; d < D; ++d) {
-          T mm = vals[d];
-          T vv = sub(add(s.misc[1], vals[DMAX + d]), mul(mm, mm));
-          if (a.m_out) a.m_out[(size_t)n * D + d] = Num<T>::st(mm);
-          if (a.v_out) a.v_out[(size_t)n * D + d] = Num<T>::st(vv);
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d) {
+          if (d < D) {
+            T mm = vals[d];
+            T vv = sub(add(s.misc[1], vals[DMAX + d]), mul(mm, mm));
+            if (a.m_out) a.m_out[(size_t)n * D + d] = Num<T>::st(mm);
+            if (a.v_out) a.v_out[(size_t)n * D + d] = Num<T>::st(vv);
+          }
         }
       }
     }
@@ -318,11 +356,10 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
   }
   if (PPT > 0 && a.psi2_sum) {
 #pragma unroll
-    for (int k = 0; k < (PPT > 0 ? PPT : 1); ++k) {
+    for (int k = 0; k < KP; ++k) {
       int p = threadIdx.x + k * NT;
       if (p < P) {
-        int ia, ib;
-        pair_of(p, ia, ib);
+        int ia = pab[k] >> 16, ib = pab[k] & 0xffff;
         double v = (double)Num<T>::st(acc[k]);
         atomicAdd(&a.psi2_sum[ia * M + ib], v);
         if (ia != ib) atomicAdd(&a.psi2_sum[ib * M + ia], v);
@@ -343,32 +380,35 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
 //   dl_q  += 2 ell (Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 (mu^2 Rt - 2 mu St + Z2R/2 + ZS/2))
 // with Z2R = sum_a z_a^2 R_a, ZS = sum_a z_a S_a; these restate psi2compDer
 // (geepee/kernels.py:402-444) without its N x M x M temporaries.
-template <typename T, int PPT, int DB>
+template <typename T, int PPT, int DB, int QC>
 __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
   Smem<T> s = carve<T>(smem_raw, M, Q, P, true, a.bs_smem ? a.Dout * P : 0);
-  cta_setup<T, S>(a, s, P);
-  const int lane = threadIdx.x & 31;
+  cta_setup<T, S, QC>(a, s, P);
 
   T accB[PPT][DB];
+  int pab[PPT];
 #pragma unroll
-  for (int k = 0; k < PPT; ++k)
+  for (int k = 0; k < PPT; ++k) {
 #pragma unroll
     for (int d = 0; d < DB; ++d) accB[k][d] = Num<T>::zero();
+    int p = threadIdx.x + k * NT, ia = 0, ib = 0;
+    if (p < P) pair_of(p, ia, ib);
+    pab[k] = (ia << 16) | ib;
+  }
   // per-thread accumulators over points
   T g_sf = Num<T>::zero();                 // sum L1 + 2 sum L (for dsf2 * sf2)
-  T g_l[QMAX];                             // dl (before the ell factor)
-  T g_z[2][QMAX];                          // dZ of the rows this thread owns (row phase, M <= 128)
-  T g_zp[QMAX];                            // dZ psi1 part (pseudo-input a = tid)
+  T g_l[QC];                               // dl (before the ell factor)
   T g_A[DB];
 #pragma unroll
-  for (int q = 0; q < QMAX; ++q) g_l[q] = g_z[0][q] = g_z[1][q] = g_zp[q] = Num<T>::zero();
+  for (int q = 0; q < QC; ++q) g_l[q] = Num<T>::zero();
 #pragma unroll
   for (int d = 0; d < DB; ++d) g_A[d] = Num<T>::zero();
-  // rows owned in the row phase: 8 threads per row, rows a = tid/8 + k*(NT/8), k < 2
+  // dZ accumulates in shared memory: each row has a single owner in each phase
+  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) s.dz[i] = Num<T>::zero();
   __syncthreads();
 
   for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
@@ -384,35 +424,39 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
       s.pd[DMAX + d] = dvv;
     }
     __syncthreads();
-    // ---- psi1 terms, one pseudo-input per thread
-    T pv[2 * QMAX];     // per-point dmu, dS partials (psi1 part)
+    // ---- psi1 terms, one pseudo-input per thread (M <= NT)
+    T pv[2 * QC];     // per-point dmu, dS partials (psi1 part)
 #pragma unroll
-    for (int i = 0; i < 2 * QMAX; ++i) pv[i] = Num<T>::zero();
-    for (int ia = threadIdx.x; ia < M; ia += blockDim.x) {
-      T p1 = point_rows(s, M, Q, ia);
+    for (int i = 0; i < 2 * QC; ++i) pv[i] = Num<T>::zero();
+    const int ia0 = threadIdx.x;
+    if (ia0 < M) {
+      T p1 = point_rows<T, QC>(s, Q, ia0);
       T dp1 = Num<T>::zero();
       if (a.dpsi1) {
-        dp1 = Num<T>::ld(a.dpsi1[(size_t)n * M + ia]);
+        dp1 = Num<T>::ld(a.dpsi1[(size_t)n * M + ia0]);
       } else {
 #pragma unroll
         for (int d = 0; d < DB; ++d) {
           if (d < D) {
-            dp1 = fma_(s.pd[d], Num<T>::ld(a.A[d * M + ia]), dp1);
+            dp1 = fma_(s.pd[d], Num<T>::ld(a.A[d * M + ia0]), dp1);
             g_A[d] = fma_(s.pd[d], p1, g_A[d]);
           }
         }
       }
       T L1 = mul(dp1, p1);
       g_sf = add(g_sf, L1);
-      for (int q = 0; q < Q; ++q) {
-        T dd = sub(s.pmu[q], s.z[ia * Q + q]);
-        T ds = mul(dd, s.pis1[q]);                       // (mu - z)/s1
-        T ds2 = mul(ds, ds);
-        pv[q] = sub(pv[q], mul(L1, ds));                 // dmu
-        pv[QMAX + q] = add(pv[QMAX + q], scale2(mul(L1, sub(ds2, s.pis1[q])), -1));  // dS
-        g_zp[q] = add(g_zp[q], mul(L1, ds));             // dZ (psi1)
-        // dl/ell: 1/l - 1/s1 + d^2/s1^2
-        g_l[q] = add(g_l[q], mul(L1, add(sub(recip(s.ell2[q]), s.pis1[q]), ds2)));
+#pragma unroll
+      for (int q = 0; q < QC; ++q) {
+        if (q < Q) {
+          T dd = sub(s.pmu[q], s.z[ia0 * Q + q]);
+          T ds = mul(dd, s.pis1[q]);                       // (mu - z)/s1
+          T ds2 = mul(ds, ds);
+          T L1ds = mul(L1, ds);
+          pv[q] = neg(L1ds);                               // dmu
+          pv[QC + q] = scale2(mul(L1, sub(ds2, s.pis1[q])), -1);   // dS
+          s.dz[ia0 * Q + q] = add(s.dz[ia0 * Q + q], L1ds);   // dZ (psi1)
+          g_l[q] = add(g_l[q], mul(L1, add(sub(s.il[q], s.pis1[q]), ds2)));   // 1/l - 1/s1 + d^2/s1^2
+        }
       }
     }
     __syncthreads();
@@ -422,11 +466,10 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
     for (int d = 0; d < DB; ++d) dvr[d] = d < D ? s.pd[DMAX + d] : Num<T>::zero();
 #pragma unroll
     for (int k = 0; k < PPT; ++k) {
-      int p = threadIdx.x + k * blockDim.x;
+      int p = threadIdx.x + k * NT;
       if (p < P) {
-        int ia, ib;
-        pair_of(p, ia, ib);
-        T ps = pair_psi2(s, Q, p, ia, ib);
+        int ia = pab[k] >> 16, ib = pab[k] & 0xffff;
+        T ps = pair_psi2<T, QC>(s, Q, p, ia, ib);
         T w = Num<T>::zero();
 #pragma unroll
         for (int d = 0; d < DB; ++d) {
@@ -455,80 +498,90 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
       int ia = rk * (NT / 8) + (threadIdx.x >> 3);
       int sl = threadIdx.x & 7;
       T R = Num<T>::zero();
-      T Sq[QMAX];
+      T Sq[QC];
 #pragma unroll
-      for (int q = 0; q < QMAX; ++q) Sq[q] = Num<T>::zero();
+      for (int q = 0; q < QC; ++q) Sq[q] = Num<T>::zero();
       if (ia < M) {
+        const int rowbase = ia * (ia + 1) / 2;
         for (int ib = sl; ib < M; ib += 8) {
-          int p = ia >= ib ? ia * (ia + 1) / 2 + ib : ib * (ib + 1) / 2 + ia;
+          int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
           T l = s.L[p];
           R = add(R, l);
-          for (int q = 0; q < Q; ++q) Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
+#pragma unroll
+          for (int q = 0; q < QC; ++q)
+            if (q < Q) Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
         }
       }
 #pragma unroll
       for (int m = 1; m < 8; m <<= 1) {
         R = add(R, shfl_xor(R, m));
-        for (int q = 0; q < Q; ++q) Sq[q] = add(Sq[q], shfl_xor(Sq[q], m));
+#pragma unroll
+        for (int q = 0; q < QC; ++q) Sq[q] = add(Sq[q], shfl_xor(Sq[q], m));
       }
       if (ia < M && sl == 0) {
         T* row = s.rows + ia * (1 + QMAX);
         row[0] = R;
-        for (int q = 0; q < Q; ++q) {
-          row[1 + q] = Sq[q];
-          T zq = s.z[ia * Q + q];
-          T il = recip(s.ell2[q]);
-          T cq = s.pc[q];
-          // R(-z/l + 2 c mu - c z) + S (1/l - c)
-          T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, s.pmu[q]), 1)), mul(cq, zq));
-          g_z[rk][q] = add(g_z[rk][q], add(mul(R, t), mul(Sq[q], sub(il, cq))));
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          if (q < Q) {
+            row[1 + q] = Sq[q];
+            T zq = s.z[ia * Q + q];
+            T il = s.il[q];
+            T cq = s.pc[q];
+            // R(-z/l + 2 c mu - c z) + S (1/l - c)
+            T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, s.pmu[q]), 1)), mul(cq, zq));
+            s.dz[ia * Q + q] = add(s.dz[ia * Q + q], add(mul(R, t), mul(Sq[q], sub(il, cq))));
+          }
         }
       }
     }
-    (void)lane;
     __syncthreads();
     // ---- per-point totals (warp 0), combined with the psi1 partials
-    // pv partials live in threads < M; reduce them with the row statistics
-    T vals[2 * QMAX];
-#pragma unroll
-    for (int i = 0; i < 2 * QMAX; ++i) vals[i] = pv[i];
-    block_sum(vals, 2 * QMAX, s.red);   // thread 0 holds psi1 part of dmu, dS
+    block_sum<T, 2 * QC>(pv, s.red);   // warp 0 holds the psi1 part of dmu, dS
     if (threadIdx.x < 32) {
       T Rt = Num<T>::zero();
-      T St[QMAX], Z2R[QMAX], ZS[QMAX];
+      T St[QC], Z2R[QC], ZS[QC];
 #pragma unroll
-      for (int q = 0; q < QMAX; ++q) St[q] = Z2R[q] = ZS[q] = Num<T>::zero();
+      for (int q = 0; q < QC; ++q) St[q] = Z2R[q] = ZS[q] = Num<T>::zero();
       for (int ia = threadIdx.x; ia < M; ia += 32) {
         const T* row = s.rows + ia * (1 + QMAX);
         Rt = add(Rt, row[0]);
-        for (int q = 0; q < Q; ++q) {
-          T zq = s.z[ia * Q + q];
-          St[q] = add(St[q], row[1 + q]);
-          Z2R[q] = fma_(mul(zq, zq), row[0], Z2R[q]);
-          ZS[q] = fma_(zq, row[1 + q], ZS[q]);
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          if (q < Q) {
+            T zq = s.z[ia * Q + q];
+            St[q] = add(St[q], row[1 + q]);
+            Z2R[q] = fma_(mul(zq, zq), row[0], Z2R[q]);
+            ZS[q] = fma_(zq, row[1 + q], ZS[q]);
+          }
         }
       }
       Rt = warp_sum(Rt);
-      for (int q = 0; q < Q; ++q) {
+#pragma unroll
+      for (int q = 0; q < QC; ++q) {
         St[q] = warp_sum(St[q]);
         Z2R[q] = warp_sum(Z2R[q]);
         ZS[q] = warp_sum(ZS[q]);
       }
-      if (threadIdx.x == 0) {
-        g_sf = add(g_sf, scale2(Rt, 1));
-        for (int q = 0; q < Q; ++q) {
-          T mu = s.pmu[q], cq = s.pc[q], il = recip(s.ell2[q]);
-          T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St[q]), 1)), scale2(add(Z2R[q], ZS[q]), -1));
-          T dmu = add(vals[q], mul(scale2(cq, 1), sub(St[q], mul(mu, Rt))));
-          T dS = add(vals[QMAX + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
-          // (dl / 2 ell) accumulates: Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 e2
-          T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R[q], ZS[q]), mul(il, il)), -1)),
-                    mul(mul(cq, cq), e2));
-          g_l[q] = add(g_l[q], scale2(t, 1));
-          a.dmu[(size_t)n * Q + q] = Num<T>::st(dmu);
-          a.dvar[(size_t)n * Q + q] = Num<T>::st(dS);
+      if (threadIdx.x < Q) {
+        // lane q finalises dimension q (registers are indexed at compile time)
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          if (q == (int)threadIdx.x) {
+            T mu = s.pmu[q], cq = s.pc[q], il = s.il[q];
+            T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St[q]), 1)), scale2(add(Z2R[q], ZS[q]), -1));
+            T dmu = add(pv[q], mul(scale2(cq, 1), sub(St[q], mul(mu, Rt))));
+            T dS = add(pv[QC + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
+            // (dl / 2 ell) accumulates: Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 e2
+            T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R[q], ZS[q]), mul(il, il)), -1)),
+                      mul(mul(cq, cq), e2));
+            g_l[q] = add(g_l[q], scale2(t, 1));
+            a.dmu[(size_t)n * Q + q] = Num<T>::st(dmu);
+            a.dvar[(size_t)n * Q + q] = Num<T>::st(dS);
+          }
         }
       }
+      if (threadIdx.x == 0) g_sf = add(g_sf, scale2(Rt, 1));
     }
     __syncthreads();
   }
@@ -536,12 +589,11 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     int p = threadIdx.x + k * NT;
-    if (p < P) {
-      int ia, ib;
-      pair_of(p, ia, ib);
+    if (p < P && a.dB) {
+      int ia = pab[k] >> 16, ib = pab[k] & 0xffff;
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
-        if (d < D && a.dB) {
+        if (d < D) {
           double v = (double)Num<T>::st(accB[k][d]);
           atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
           if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
@@ -552,37 +604,41 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   if (threadIdx.x < M) {
 #pragma unroll
     for (int d = 0; d < DB; ++d)
-      if (d < D && a.dA) atomicAdd(&a.dA[d * M + threadIdx.x], (double)Num<T>::st(g_A[d]));
-    for (int q = 0; q < Q; ++q) atomicAdd(&a.dZ[threadIdx.x * Q + q], (double)Num<T>::st(g_zp[q]));
+      if (d < D && a.dA && !a.dpsi1) atomicAdd(&a.dA[d * M + threadIdx.x], (double)Num<T>::st(g_A[d]));
   }
-#pragma unroll
-  for (int rk = 0; rk < 2; ++rk) {
-    int ia = rk * (NT / 8) + (threadIdx.x >> 3);
-    if (ia < M && (threadIdx.x & 7) == 0)
-      for (int q = 0; q < Q; ++q) atomicAdd(&a.dZ[ia * Q + q], (double)Num<T>::st(g_z[rk][q]));
-  }
+  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) atomicAdd(&a.dZ[i], (double)Num<T>::st(s.dz[i]));
   // dsf2 and dl need the ell / sf2 factors: (sum L1 + 2 sum L) / sf2 and ell * g_l
-  T vals[1 + QMAX];
+  T vals[1 + QC];
   vals[0] = g_sf;
 #pragma unroll
-  for (int q = 0; q < QMAX; ++q) vals[1 + q] = g_l[q];
+  for (int q = 0; q < QC; ++q) vals[1 + q] = g_l[q];
   __syncthreads();
-  block_sum(vals, 1 + QMAX, s.red);
+  block_sum<T, 1 + QC>(vals, s.red);
   if (threadIdx.x == 0) {
     atomicAdd(a.dsf2, (double)Num<T>::st(div(vals[0], s.misc[1])));
-    for (int q = 0; q < Q; ++q) {
-      T ell = sqrt_(s.ell2[q]);
-      atomicAdd(&a.dl[q], (double)Num<T>::st(mul(vals[1 + q], ell)));
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      if (q < Q) {
+        T ell = sqrt_(s.ell2[q]);
+        atomicAdd(&a.dl[q], (double)Num<T>::st(mul(vals[1 + q], ell)));
+      }
     }
   }
 }
 
-template <typename T, int PPT>
+template <typename T, int PPT, int QC>
 int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
-  auto k = psi_fwd_kernel<T, PPT>;
+  auto k = psi_fwd_kernel<T, PPT, QC>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<grid, NT, sm, st>>>(a);
   return gpk::check_launch("psi_fwd");
+}
+
+template <typename T, int QC>
+int fwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, bool sum, int P, int grid, size_t sm, cudaStream_t st) {
+  if (!sum) return run_fwd<T, 0, QC>(a, grid, sm, st);
+  if (P <= 4 * NT) return run_fwd<T, 4, QC>(a, grid, sm, st);
+  return run_fwd<T, 16, QC>(a, grid, sm, st);
 }
 
 template <typename T>
@@ -602,23 +658,29 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   int grid = gpk::sm_count() * per_sm;
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;
-  if (!sum) return run_fwd<T, 0>(a, grid, sm, st);
-  if (P <= 4 * NT) return run_fwd<T, 4>(a, grid, sm, st);
-  return run_fwd<T, 16>(a, grid, sm, st);
+  if (a.Q <= 2) return fwd_ppt<T, 2>(a, sum, P, grid, sm, st);
+  return fwd_ppt<T, QMAX>(a, sum, P, grid, sm, st);
 }
 
-template <typename T, int PPT, int DB>
+template <typename T, int PPT, int DB, int QC>
 int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
-  auto k = psi_bwd_kernel<T, PPT, DB>;
+  auto k = psi_bwd_kernel<T, PPT, DB, QC>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<grid, NT, sm, st>>>(a);
   return gpk::check_launch("psi_bwd");
 }
 
-template <typename T, int DB>
+template <typename T, int DB, int QC>
 int bwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t sm, cudaStream_t st) {
-  if (P <= 4 * NT) return run_bwd<T, 4, DB>(a, grid, sm, st);
-  return run_bwd<T, 16, DB>(a, grid, sm, st);
+  if (P <= 4 * NT) return run_bwd<T, 4, DB, QC>(a, grid, sm, st);
+  return run_bwd<T, 16, DB, QC>(a, grid, sm, st);
+}
+
+template <typename T, int QC>
+int bwd_db(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t sm, cudaStream_t st) {
+  if (a.Dout == 1) return bwd_ppt<T, 1, QC>(a, P, grid, sm, st);
+  if (a.Dout == 2) return bwd_ppt<T, 2, QC>(a, P, grid, sm, st);
+  return bwd_ppt<T, 4, QC>(a, P, grid, sm, st);
 }
 
 template <typename T>
@@ -633,9 +695,8 @@ int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   int grid = gpk::sm_count();
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;
-  if (a.Dout == 1) return bwd_ppt<T, 1>(a, P, grid, sm, st);
-  if (a.Dout == 2) return bwd_ppt<T, 2>(a, P, grid, sm, st);
-  return bwd_ppt<T, 4>(a, P, grid, sm, st);
+  if (a.Q <= 2) return bwd_db<T, 2>(a, P, grid, sm, st);
+  return bwd_db<T, QMAX>(a, P, grid, sm, st);
 }
 
 }  // namespace psi_impl

@@ -97,12 +97,15 @@ def gemm(A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False):
     return C
 
 
-def chol_inv(A, Ainv=None, L=None, logdet=None, info=None):
-    """Batched SPD inverse / Cholesky / log-determinant of A [..., M, M] (M <= 128)."""
+def chol_inv(A, Ainv=None, L=None, logdet=None, info=None, work=None):
+    """Batched SPD inverse / Cholesky / log-determinant of A [..., M, M].  M > 128 runs in a
+    device workspace (allocated here when not given)."""
     M = A.shape[-1]
     batch = A.numel() // (M * M)
-    call('gpk_chol_inv', prec_of(A.dtype), batch, M, ptr(A), ptr(Ainv), ptr(L), ptr(logdet), ptr(info),
-         stream())
+    if M > 128 and work is None:
+        work = torch.empty_like(A)
+    call('gpk_chol_inv_ws', prec_of(A.dtype), batch, M, ptr(A), ptr(Ainv), ptr(L), ptr(logdet), ptr(info),
+         ptr(work), stream())
 
 
 def trace_kzz(Mm, Z, lls2, lsf2, g_sf, g_ls, g_z, s_sf=1.0, s_ls=1.0):

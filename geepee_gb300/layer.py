@@ -146,22 +146,24 @@ class DevLayer:
         self._cavity_tail()
 
     def _cavity_tail(self):
+        """Ahat, Bhat_det = K^-1 Suhat K^-1 - K^-1 and Bhat_sto = K^-1 (Suhat + mh mh^T) K^-1 - K^-1
+        (aep_models.py:536-546); Bhat_sto is formed as Bhat_det + Ahat Ahat^T, the same matrix
+        with two fewer M^3 products."""
         K = self.Kinv
         self.Smm_h = self.Sh + outer(self.mh, self.mh)
         self.Ah = mv(K, self.mh)
-        KS = mm(K, self.Smm_h)
-        self.Bh_sto = mm(KS, K, C=-K.unsqueeze(0).expand_as(KS).contiguous(), beta=1.0)
         KS2 = mm(K, self.Sh)
         self.Bh_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
+        self.Bh_sto = self.Bh_det + outer(self.Ah, self.Ah)
 
     def setup_predict(self):
-        """Posterior A, B_det, B_sto used by predict (base_models.py:480-488)."""
+        """Posterior A, B_det, B_sto used by predict (base_models.py:480-488);
+        B_sto = B_det + A A^T."""
         K = self.Kinv
         self.A = mv(K, self.mu)
-        KS = mm(K, self.Spmm)
-        self.B_sto = mm(KS, K, C=-K.unsqueeze(0).expand_as(KS).contiguous(), beta=1.0)
         KS2 = mm(K, self.Su)
         self.B_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
+        self.B_sto = self.B_det + outer(self.A, self.A)
 
     # ---------------------------------------------------------------- log-partitions
     def phi(self, alpha):
@@ -214,18 +216,31 @@ class DevLayer:
 
     def bwd_mm(self, alpha, m, dm, dv, mx, vx):
         """backprop_grads_lvm_mm (aep_models.py:201-304); returns (dmx, dvx)."""
-        N, M, D, Q = self.N, self.M, self.Dout, self.Din
-        s_post, s_cav = N / alpha - 1.0, -N / alpha
-        beta = self.beta
+        dmx, dvx = self.bwd_mm_data(alpha, m, dm, dv, mx, vx)
+        self.bwd_mm_algebra(alpha)
+        return dmx, dvx
+
+    def bwd_mm_data(self, alpha, m, dm, dv, mx, vx):
+        """The data-sized part of the backward: psi-statistic gradients (recomputing psi2),
+        dAhat, dBhat and the gradient w.r.t. the input moments (dmx, dvx)."""
+        M, D, Q = self.M, self.Dout, self.Din
         z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
-        dsf2, dl, dZ, dAh, dBh = z(1), z(Q), self.g['zu'], z(D, M), z(D, M, M)
+        dsf2, dl, dZ, self._dAh, self._dBh = z(1), z(Q), self.g['zu'], z(D, M), z(D, M, M)
         dZ.zero_()
         n = mx.shape[0]
         dmx = torch.empty((n, Q), dtype=F64, device=self.dev)
         dvx = torch.empty_like(dmx)
         gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, dsf2, dl, dZ,
-                    dAh, dBh, dmx, dvx)
+                    self._dAh, self._dBh, dmx, dvx)
         self._kernel_grads(dsf2, dl, dv.sum())
+        return dmx, dvx
+
+    def bwd_mm_algebra(self, alpha):
+        """The M x M part of backprop_grads_lvm_mm: cavity, natural-parameter and Kuu gradients."""
+        N, M, D = self.N, self.M, self.Dout
+        s_post, s_cav = N / alpha - 1.0, -N / alpha
+        beta = self.beta
+        dAh, dBh = self._dAh, self._dBh
         K = self.Kinv
         dvcav = mm(mm(K, dBh), K)
         dmcav = 2.0 * mv(dvcav, self.mh) + mm(dAh, K, tB=True)

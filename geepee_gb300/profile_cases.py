@@ -9,6 +9,9 @@ Cases run one kernel of the deep-GP objective on its real input shapes:
   psi_fwd_c2_f32  the same in FP32
   psi_bwd_c2    psi backward, N=10000, Q=5, M=100, df64
   chol_m100     SPD Cholesky + inverse + logdet of one 100x100 Kuu, df64
+  gemm_m100     one 100x100x100 df64 GEMM (the M x M algebra)
+  det_fwd_dgp   deterministic layer forward, 1000 rows, D=8, M=100, Dout=2, df64
+  trace_m100    gradient of tr(M Kzz), M=100, Q=2, df64
   objective_dgp one full objective+gradient evaluation (eager, every kernel)
 With --time, prints the mean device time per launch (CUDA events).
 """
@@ -62,6 +65,25 @@ def case(name):
         A = _d(K[None])
         inv, ld, info = torch.empty_like(A), z(1), torch.zeros(1, dtype=torch.int32, device='cuda')
         return lambda: gpk.chol_inv(A, inv, None, ld, info)
+    if name == 'gemm_m100':
+        rng = np.random.RandomState(0)
+        A, B = _d(rng.randn(100, 100)), _d(rng.randn(100, 100))
+        C = torch.empty_like(A)
+        return lambda: gpk.gemm(A, B, C)
+    if name == 'det_fwd_dgp':
+        rng = np.random.RandomState(0)
+        x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))
+        A, B = _d(rng.randn(2, 100)), _d(rng.randn(2, 100, 100))
+        l2, s2 = _d(np.zeros(8)), _d(np.zeros(1))
+        kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
+        m, v = z(1000, 2), z(1000, 2)
+        return lambda: gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, m, v)
+    if name == 'trace_m100':
+        rng = np.random.RandomState(0)
+        Mm, Z = _d(rng.randn(100, 100)), _d(rng.randn(100, 2))
+        l2, s2 = _d(np.zeros(2)), _d(np.zeros(1))
+        g1, g2, g3 = z(1), z(2), z(100, 2)
+        return lambda: gpk.trace_kzz(Mm, Z, l2, s2, g1, g2, g3)
     if name == 'objective_dgp':
         from . import aep_models as A
         x, y = W.dgp_regression(seed=0)

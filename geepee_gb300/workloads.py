@@ -104,3 +104,37 @@ def kink_ssm(seed: int = 0, T: int = 5000, Dx: int = 2, Dy: int = 4, M: int = 50
               'zu_dynamic': x[rng.permutation(T - 1)[:M]]}
     params.update(natural_q_init(rng, M, Dx, '_dynamic'))
     return y, params
+
+
+def serving_models(seed: int = 0, n_models: int = 32, Ms=(50, 100, 200), D: int = 8, hidden: int = 2,
+                   n_fit: int = 2000):
+    """Parameters of `n_models` 2-layer deep GPs (input D, hidden width, 1 output) with M drawn in
+    turn from Ms, initialised the way the reference initialises SDGPR (pseudo-inputs on data,
+    median-distance lengthscales, natural q(u) parameters) on per-model synthetic data."""
+    from .aep_models import layer_init_hypers
+    out = []
+    rs = np.random.get_state()
+    for i in range(n_models):
+        M = Ms[i % len(Ms)]
+        x, y = dgp_regression(seed=seed * 1000 + i, N=n_fit, D=D, hidden=hidden)
+        np.random.seed(seed * 1000 + i)
+        p = {}
+        p.update(layer_init_hypers(n_fit, M, D, hidden, True, x, '_0'))
+        p.update(layer_init_hypers(n_fit, M, hidden, 1, True, None, '_1'))
+        p['sn'] = np.log(0.05)
+        out.append((p, [D, hidden, 1], [M, M]))
+    np.random.set_state(rs)
+    return out
+
+
+def serving_trace(seed: int = 0, rate: float = 2000.0, seconds: float = 2.0, n_models: int = 32,
+                  max_rows: int = 4096, D: int = 8):
+    """Poisson request arrivals at `rate` per second; each request picks a model uniformly and a
+    query batch size log-uniform in [1, max_rows]; inputs ~ N(0, I_D)."""
+    rng = np.random.RandomState(seed)
+    n = rng.poisson(rate * seconds)
+    t = np.sort(rng.uniform(0.0, seconds, n))
+    model = rng.randint(0, n_models, n)
+    rows = np.exp(rng.uniform(0.0, np.log(max_rows), n)).astype(int).clip(1, max_rows)
+    xs = [rng.randn(int(b), D) for b in rows]
+    return t, model, rows, xs

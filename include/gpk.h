@@ -137,6 +137,12 @@ int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, d
 int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
                  void* stream);
 
+/* As gpk_chol_inv for any M <= 4096: the factorisation runs in the caller's device workspace
+ * `work` (batch*M*M elements of the buffer precision) instead of shared memory; required for
+ * M > 128 (e.g. the M = 200 models of the serving mix). */
+int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
+                    void* work, void* stream);
+
 /* Gradient of tr(Mm Kzz), Kzz = K(Z, Z) without jitter, w.r.t. log sf^2, log ell^2 and Z,
  * added with scales: g_sf += s_sf * d/dlog sf^2, g_ls += s_ls * d/dlog ell^2, g_z += d/dZ.
  * Replaces geepee/kernels.py:447-475 d_trace_MKzz_dhypers. */

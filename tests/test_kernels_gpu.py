@@ -110,7 +110,7 @@ def test_psi_fp32_within_tolerance():
     assert_close(ssum.cpu().numpy(), g['psi2_sum'], FP32_TOL, 'psi2 sum fp32')
 
 
-@pytest.mark.parametrize('M', [1, 7, 64, 100, 128])
+@pytest.mark.parametrize('M', [1, 7, 64, 100, 128, 129, 200])
 def test_chol_inv_logdet(M):
     from geepee_gb300 import gpk
     rng = np.random.RandomState(M)
@@ -205,3 +205,15 @@ def test_psi_size_limits_are_reported():
     with pytest.raises(GpkError):
         gpk.psi_bwd(mu, S, Z, l2, s2, z(1, M), z(1, M, M), z(N, 1), z(N, 1), z(N, 1), z(1), z(Q), z(M, Q),
                     z(1, M), z(1, M, M), z(N, Q), z(N, Q))
+
+
+def test_double_split_is_exact():
+    """The integer-pipe float64 -> (hi, lo) split must equal the FP64-pipe split bit for bit:
+    checked through gpk_gemm with an identity operand (C = A I reproduces A's df64 rounding)."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(0)
+    A = rng.randn(64, 64) * 10 ** rng.uniform(-20, 20, (64, 64))
+    C = gpk.gemm(dev(A), dev(np.eye(64)))
+    hi = A.astype(np.float32).astype(np.float64)
+    lo = (A - hi).astype(np.float32).astype(np.float64)
+    assert np.array_equal(C.cpu().numpy(), hi + lo)
