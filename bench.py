@@ -37,6 +37,8 @@ def parse():
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--serving-seconds', type=float, default=2.0,
+                    help='length of the Poisson serving trace (0 disables the serving measurement)')
     return ap.parse_args()
 
 
@@ -310,6 +312,75 @@ def run_ours(args, world, rank, local):
     return out
 
 
+def run_serving(seconds, local):
+    """Serving mix: 32 resident 2-layer deep GPs (input 8, hidden 2, M in {50,100,200}), Poisson
+    arrivals at 2000 requests/s, query batch log-uniform in [1,4096]; predict_y (df64 arithmetic,
+    float64 factors).  The trace is replayed once untimed (graph capture) and then timed."""
+    import threading
+    import torch
+    from geepee_gb300 import serving, workloads as W, fp64_form
+    dev = torch.device('cuda', local)
+    models = W.serving_models(seed=0, n_models=32, Ms=(50, 100, 200))
+    res = [serving.ResidentDGP(p, sizes, Ms, dev) for p, sizes, Ms in models]
+    t_arr, mids, rows, xs = W.serving_trace(seed=1, rate=2000.0, seconds=seconds, n_models=32)
+
+    def play(srv):
+        reqs = [None] * len(t_arr)
+        t0 = time.perf_counter() + 0.01
+
+        def feeder():
+            for i in range(len(t_arr)):
+                tt = t0 + t_arr[i]
+                while True:
+                    d = tt - time.perf_counter()
+                    if d <= 0:
+                        break
+                    time.sleep(min(d, 0.0002) if d > 0.0003 else 0)
+                reqs[i] = srv.submit(int(mids[i]), xs[i], t_arrive=tt)
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        for r in reqs:
+            r.future.result(timeout=120)
+        t_end = max(r.t_done for r in reqs)
+        lat = np.array([r.t_done - r.t_arrive for r in reqs]) * 1e3
+        return lat, t_end - t0
+
+    srv = serving.Server(res, n_streams=4, max_rows=4096, budget_rows=1 << 16, device=dev)
+    srv.start()
+    play(srv)                      # untimed: captures every (model, bucket, stream) graph used
+    lat, span = play(srv)
+    srv.stop()
+    out = {'requests': int(len(t_arr)), 'rate_req_per_s': 2000.0, 'trace_s': seconds,
+           'p50_ms': float(np.percentile(lat, 50)), 'p99_ms': float(np.percentile(lat, 99)),
+           'max_ms': float(lat.max()), 'queries_per_s': float(rows.sum() / span),
+           'requests_per_s': float(len(t_arr) / span), 'graphs': len(srv.slots),
+           'models': '32 x 2-layer DGP, M in {50,100,200}, batch log-uniform [1,4096]'}
+    # per-request plain FP64 launch (no batching), on a sample of the same requests
+    fp = [fp64_form.PredictFP64(p, 2, dev) for p, _, _ in models]
+    sample = list(range(0, len(t_arr), max(1, len(t_arr) // 150)))
+    svc = []
+    try:
+        for i in sample[:5]:
+            fp[int(mids[i])].predict_y(torch.as_tensor(xs[i], device=dev))
+        torch.cuda.synchronize()
+        for i in sample:
+            t0 = time.perf_counter()
+            m, v = fp[int(mids[i])].predict_y(torch.as_tensor(xs[i], device=dev))
+            m.cpu(), v.cpu()
+            svc.append(time.perf_counter() - t0)
+        svc = np.array(svc) * 1e3
+        out['fp64_per_request'] = {'service_p50_ms': float(np.percentile(svc, 50)),
+                                   'service_p99_ms': float(np.percentile(svc, 99)),
+                                   'service_mean_ms': float(svc.mean()),
+                                   'max_req_per_s': float(1e3 / svc.mean()), 'sampled': len(svc),
+                                   'note': 'service time alone (no queueing); at 2000 req/s the '
+                                           'offered load is %.1fx its capacity' % (2000.0 * svc.mean() / 1e3)}
+    except RuntimeError as exc:
+        out['fp64_per_request'] = {'error': str(exc)[:200]}
+    return out
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -359,6 +430,12 @@ def main():
         rate, kind, n, dt = cpu_eval_rate(r['x'], r['y'], r['params'], [r['idx0']], args.cpu_seconds)
         cpu = {'value': rate, 'unit': 'evals/s', 'cores': os.cpu_count(), 'kind': kind,
                'sample': '%d objective+gradient evaluations (%.1f s) of the same workload' % (n, dt)}
+    serving_out = None
+    if args.serving_seconds > 0:
+        try:
+            serving_out = run_serving(args.serving_seconds, local)
+        except Exception as exc:            # reported, never silently dropped
+            serving_out = {'error': '%s: %s' % (type(exc).__name__, str(exc)[:300])}
     line = {'metric': METRIC, 'value': r['value'], 'unit': 'evals/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': r['ms'], 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None,
@@ -372,6 +449,7 @@ def main():
                 'value': r['fp64_rate'], 'unit': 'evals/s', 'steps': r['n64'],
                 'speedup_of_value': r['value'] / r['fp64_rate'],
                 'speedup_of_e2e': r['e2e']['value'] / r['fp64_rate']},
+            'serving': serving_out,
             'parity': {'energy_rel_err_vs_oracle': abs(r['e_gpu'] - e_ref) / abs(e_ref),
                        'fp64_form_energy_rel_err_vs_oracle': None if r['e_fp64'] is None else
                        abs(r['e_fp64'] - e_ref) / abs(e_ref),

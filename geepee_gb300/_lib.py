@@ -40,6 +40,7 @@ _SIGS = {
                  ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp],
     'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_chol_inv_ws': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_chol_linv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_small_spd': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
 }

@@ -377,6 +377,7 @@ class SDGPR(_PackedModel):
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
         main = torch.cuda.current_stream()
         side = self._side_streams()
+        forked = []
         for i in range(L - 1, -1, -1):
             lay = self.layers[i]
             if i == 0:
@@ -387,7 +388,8 @@ class SDGPR(_PackedModel):
                 st.wait_stream(main)
                 with torch.cuda.stream(st):
                     lay.bwd_mm_algebra(alpha)
-        for st in side:
+                forked.append(st)
+        for st in forked:          # join only the branches forked here (graph-capture rule)
             main.wait_stream(st)
         self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
         energy = scale * logZ

@@ -91,7 +91,8 @@ template <typename T, bool GMEM>
 __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Num<T>::store_t* A, long sA,
                                                         typename Num<T>::store_t* Ainv, long sI,
                                                         typename Num<T>::store_t* Lout, long sL, double* logdet,
-                                                        int* info, typename Num<T>::store_t* work) {
+                                                        int* info, typename Num<T>::store_t* work,
+                                                        typename Num<T>::store_t* Xout) {
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   const int b = blockIdx.x;
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
       if (tx == 0) logdet[b] = (double)Num<T>::st(scale2(s, 1));
     }
   }
-  if (!Ainv) return;
+  if (!Ainv && !Xout) return;
   // in-place inverse of the lower factor, columns right to left:
   //   X_jj = 1/L_jj,  X_ij = -X_jj sum_{k=j+1..i} X_ik L_kj   (i > j)
   // column j's L entries are staged in tmp one step ahead, so each column costs two barriers.
@@ -195,6 +196,16 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
     if (j > 0)
       for (int k = j + tid; k < M; k += blockDim.x) tmp[k] = S[k * ld + (j - 1)];
     __syncthreads();
+  }
+  if (Xout) {
+    // hand X = L^-1 (zeros above the diagonal) to the caller; the product X^T X is left to a
+    // many-CTA GEMM instead of this single CTA
+    Xout += (size_t)b * M * M;
+    for (int e = tid; e < M * M; e += blockDim.x) {
+      int i = e / M, j = e % M;
+      Xout[e] = Num<T>::st(i >= j ? S[i * ld + j] : Num<T>::zero());
+    }
+    return;
   }
   // Ainv = X^T X  (X lower): Ainv_ij = sum_{k >= max(i,j)} X_ki X_kj
   Ainv += b * sI;
@@ -392,13 +403,13 @@ extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, in
 
 template <typename T, bool GMEM>
 int chol_launch(int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info, void* work,
-                cudaStream_t st) {
+                void* Xout, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
   long s = (long)M * M;
   size_t sm = 256 * 8 + ((GMEM ? 0 : (size_t)M * (M + 1)) + 3 * M + 32) * sizeof(T);
   auto k = chol_inv_kernel<T, GMEM>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<batch, 1024, sm, st>>>(M, (const S*)A, s, (S*)Ainv, s, (S*)L, s, logdet, info, (S*)work);
+  k<<<batch, 1024, sm, st>>>(M, (const S*)A, s, (S*)Ainv, s, (S*)L, s, logdet, info, (S*)work, (S*)Xout);
   return gpk::check_launch("chol_inv");
 }
 
@@ -411,12 +422,29 @@ extern "C" int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* 
   cudaStream_t st = gpk::as_stream(stream);
   const bool gm = M > 128;
   if (prec == GPK_DF64)
-    return gm ? chol_launch<df64, true>(batch, M, A, Ainv, L, logdet, info, work, st)
-              : chol_launch<df64, false>(batch, M, A, Ainv, L, logdet, info, work, st);
+    return gm ? chol_launch<df64, true>(batch, M, A, Ainv, L, logdet, info, work, nullptr, st)
+              : chol_launch<df64, false>(batch, M, A, Ainv, L, logdet, info, work, nullptr, st);
   if (prec == GPK_FP32)
-    return gm ? chol_launch<float, true>(batch, M, A, Ainv, L, logdet, info, work, st)
-              : chol_launch<float, false>(batch, M, A, Ainv, L, logdet, info, work, st);
+    return gm ? chol_launch<float, true>(batch, M, A, Ainv, L, logdet, info, work, nullptr, st)
+              : chol_launch<float, false>(batch, M, A, Ainv, L, logdet, info, work, nullptr, st);
   return gpk::fail(GPK_EINVAL, "chol_inv: unknown precision %d", prec);
+}
+
+extern "C" int gpk_chol_linv(int prec, int batch, int M, const void* A, void* Linv, double* logdet, int* info,
+                             void* work, void* stream) {
+  GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "chol_linv: M=%d outside [1,4096]", M);
+  GPK_REQUIRE(A && Linv, "chol_linv: null pointer");
+  GPK_REQUIRE(M <= 128 || work, "chol_linv: M=%d > 128 needs a workspace of batch*M*M elements", M);
+  if (batch == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  const bool gm = M > 128;
+  if (prec == GPK_DF64)
+    return gm ? chol_launch<df64, true>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st)
+              : chol_launch<df64, false>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st);
+  if (prec == GPK_FP32)
+    return gm ? chol_launch<float, true>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st)
+              : chol_launch<float, false>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st);
+  return gpk::fail(GPK_EINVAL, "chol_linv: unknown precision %d", prec);
 }
 
 extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
 import torch
 
 from .config import JITTER
@@ -108,3 +109,45 @@ def sdgpr_objective(p, x, y, idx, alpha, n_layers):
     keys = sorted(leaves)
     grads = torch.autograd.grad(e, [leaves[k] for k in keys])
     return e.detach(), dict(zip(keys, grads))
+
+
+class PredictFP64:
+    """Per-request plain-FP64 predict_y of a 2-layer deep GP: the posterior A, B_det, B_sto are
+    computed once with torch.linalg; each request evaluates Kfu / psi1 / the materialised psi2
+    (base_models.py:265-307, 1264-1275) in torch float64."""
+
+    def __init__(self, params, n_layers, device):
+        p = {k: torch.as_tensor(np.asarray(v, dtype=np.float64), device=device) for k, v in params.items()}
+        self.layers = []
+        for i in range(n_layers):
+            sfx = '_%d' % i
+            ls, sf, Z = p['ls' + sfx], p['sf' + sfx], p['zu' + sfx]
+            eta1, eta2 = p['eta1_R' + sfx], p['eta2' + sfx]
+            D, M = eta2.shape
+            iu = torch.triu_indices(M, M, device=device)
+            R = torch.zeros((D, M, M), dtype=F64, device=device)
+            R[:, iu[0], iu[1]] = eta1
+            d = torch.diagonal(R, dim1=1, dim2=2)
+            R = R - torch.diag_embed(d) + torch.diag_embed(torch.exp(d))
+            Kuu = _ard(2 * ls, 2 * sf, Z, Z) + JITTER * torch.eye(M, dtype=F64, device=device)
+            Kinv = torch.linalg.inv(Kuu)
+            Su = torch.linalg.inv(Kinv + R.transpose(1, 2) @ R)
+            mu = (Su @ eta2[..., None])[..., 0]
+            A = (Kinv @ mu[..., None])[..., 0]
+            B_det = -Kinv + Kinv @ Su @ Kinv
+            B_sto = -Kinv + Kinv @ (Su + mu[:, :, None] * mu[:, None, :]) @ Kinv
+            self.layers.append((ls, sf, Z, A, B_det, B_sto))
+        self.sn2 = torch.exp(2.0 * p['sn'])
+
+    def predict_y(self, x):
+        for i, (ls, sf, Z, A, B_det, B_sto) in enumerate(self.layers):
+            if i == 0:
+                kfu = _ard(2 * ls, 2 * sf, x, Z)
+                m = kfu @ A.T
+                v = torch.exp(2 * sf) + torch.einsum('dab,na,nb->nd', B_det, kfu, kfu)
+            else:
+                psi1, psi2 = _psi(2 * ls, 2 * sf, m, v, Z)
+                m2 = psi1 @ A.T
+                v = torch.exp(2 * sf) + torch.einsum('dab,nab->nd', B_sto, psi2) - m2 ** 2
+                m = m2
+        return m, v + self.sn2

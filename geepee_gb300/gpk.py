@@ -99,11 +99,19 @@ def gemm(A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False):
 
 def chol_inv(A, Ainv=None, L=None, logdet=None, info=None, work=None):
     """Batched SPD inverse / Cholesky / log-determinant of A [..., M, M].  M > 128 runs in a
-    device workspace (allocated here when not given)."""
+    device workspace (allocated here when not given).  When only the inverse (and logdet) is
+    wanted, the factorisation returns L^-1 and the inverse is formed as L^-T L^-1 by the GEMM."""
     M = A.shape[-1]
     batch = A.numel() // (M * M)
     if M > 128 and work is None:
         work = torch.empty_like(A)
+    if Ainv is not None and L is None:
+        X = torch.empty_like(A)
+        call('gpk_chol_linv', prec_of(A.dtype), batch, M, ptr(A), ptr(X), ptr(logdet), ptr(info), ptr(work),
+             stream())
+        X3 = X.reshape(batch, M, M)
+        gemm(X3, X3, Ainv.view(batch, M, M), tA=True)
+        return
     call('gpk_chol_inv_ws', prec_of(A.dtype), batch, M, ptr(A), ptr(Ainv), ptr(L), ptr(logdet), ptr(info),
          ptr(work), stream())
 

@@ -258,7 +258,6 @@ class DevLayer:
         self._finish_hyp(Mall)
         self.g['eta1_R'].copy_(self._pack_eta1(dth1))
         self.g['eta2'].copy_(dth2)
-        return dmx, dvx
 
     def _cav_grad_u(self, dmu, dSu):
         """compute_cav_grad_u (aep_models.py:548-586)."""

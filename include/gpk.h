@@ -143,6 +143,12 @@ int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L,
 int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
                     void* work, void* stream);
 
+/* The inverse Cholesky factor: Linv[b] = L[b]^-1 (lower triangular, zeros above the diagonal),
+ * logdet and info as in gpk_chol_inv.  A^-1 = Linv^T Linv is then one batched gpk_gemm, which
+ * spreads that third of the work over many CTAs.  `work` as in gpk_chol_inv_ws (M > 128). */
+int gpk_chol_linv(int prec, int batch, int M, const void* A, void* Linv, double* logdet, int* info, void* work,
+                  void* stream);
+
 /* Gradient of tr(Mm Kzz), Kzz = K(Z, Z) without jitter, w.r.t. log sf^2, log ell^2 and Z,
  * added with scales: g_sf += s_sf * d/dlog sf^2, g_ls += s_ls * d/dlog ell^2, g_z += d/dZ.
  * Replaces geepee/kernels.py:447-475 d_trace_MKzz_dhypers. */
