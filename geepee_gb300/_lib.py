@@ -38,11 +38,20 @@ _SIGS = {
     'gpk_wsum': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
     'gpk_gemm': [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_dbl, _vp, _c_int,
                  ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp],
+    'gpk_gemm_ex': [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_dbl, _vp, _c_int,
+                    ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp, _c_int,
+                    ctypes.c_long, _vp],
     'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_chol_inv_ws': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
-    'gpk_chol_linv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_spd_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_small_spd': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
+    'gpk_lincomb': [_vp, _vp],
+    'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp],
+    'gpk_nat_prep': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_triu_pack': [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp],
+    'gpk_hyp_grads': [_c_int, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
+    'gpk_aep_phi': [_c_int, _c_int, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _vp, _vp],
 }
 
 _lib = None

@@ -214,10 +214,27 @@ class _PackedModel(Base_Model):
         self.ppack.upload(params)
         self.updated = False
 
-    def _flag_info(self, layers):
-        """Cholesky status of every layer -> one float slot of the gradient pack (on device)."""
-        worst = torch.stack([lay.info.max() for lay in layers]).max()
-        self.gpack.views['__info__'].copy_(worst.to(F64).reshape(1))
+    def _flag_info(self, statuses):
+        """Cholesky status words (int32 device tensors from setup_layers) -> their maximum in
+        one float slot of the gradient pack (on device)."""
+        worst = statuses[0].max() if len(statuses) == 1 else torch.cat([t.reshape(-1) for t in statuses]).max()
+        self.gpack.views['__info__'].copy_(worst.reshape(1))
+
+    def _layer_grad_span(self):
+        """Length of the leading part of the gradient pack that holds layer gradients (every key
+        before 'sn')."""
+        keys = [k for k, _ in self.gpack.spec]
+        return int(self.gpack.offsets[keys.index('sn')])
+
+    def _energy_terms(self, layers, alpha, N):
+        """energy += sum of the layers' weighted log-partitions / N (fused for natural-parameter
+        layers); then the layer gradients are divided by N in one pass."""
+        for lay in layers:
+            if lay.nat:
+                lay.phi(alpha, out=self.energy, w=1.0 / N)
+            else:
+                self.energy.add_(lay.phi(alpha).reshape(1) / N)
+        self.gpack.dev[:self._layer_grad_span()].div_(N)
 
     def _objective_host(self, idx, alpha):
         if idx is None:
@@ -278,16 +295,13 @@ class SGPR(_PackedModel):
         yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
         nb = yb.shape[0]
         scale = -N / nb / alpha
-        setup_layers([lay], alpha)
+        st = setup_layers([lay], alpha)
         m, v, kfu, Bk = lay.fwd_det(xb)
-        logZ, dm, dv = gauss_logZ(m, v, yb, self.sn, alpha)
-        lay.bwd_det(alpha, scale * dm, scale * dv, kfu, Bk, xb)
-        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
-        self.energy.copy_((scale * logZ + lay.phi(alpha)) / N)
-        for g in lay.g.values():
-            g.div_(N)
-        self.g_sn.div_(N)
-        self._flag_info([lay])
+        dm, dv = torch.empty_like(m), torch.empty_like(v)
+        gpk.gauss_lik(m, v, yb, self.sn, alpha, scale, 1.0 / N, dm, dv, self.energy, self.g_sn)
+        lay.bwd_det(alpha, dm, dv, kfu, Bk, xb)
+        self._energy_terms([lay], alpha, N)
+        self._flag_info(st)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
@@ -362,7 +376,7 @@ class SDGPR(_PackedModel):
         yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
         nb = yb.shape[0]
         scale = -N / nb / alpha
-        setup_layers(self.layers, alpha)
+        st = setup_layers(self.layers, alpha)
         ms, vs = [], []
         m, v, kfu, Bk = self.layers[0].fwd_det(xb)
         ms.append(m)
@@ -371,8 +385,8 @@ class SDGPR(_PackedModel):
             m, v = self.layers[i].fwd_mm(ms[-1], vs[-1])
             ms.append(m)
             vs.append(v)
-        logZ, dm, dv = gauss_logZ(ms[-1], vs[-1], yb, self.sn, alpha)
-        dmi, dvi = scale * dm, scale * dv
+        dmi, dvi = torch.empty_like(ms[-1]), torch.empty_like(vs[-1])
+        gpk.gauss_lik(ms[-1], vs[-1], yb, self.sn, alpha, scale, 1.0 / N, dmi, dvi, self.energy, self.g_sn)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
         main = torch.cuda.current_stream()
@@ -384,23 +398,15 @@ class SDGPR(_PackedModel):
                 lay.bwd_det(alpha, dmi, dvi, kfu, Bk, xb)
             else:
                 dmi, dvi = lay.bwd_mm_data(alpha, ms[i], dmi, dvi, ms[i - 1], vs[i - 1])
-                st = side[i % len(side)]
-                st.wait_stream(main)
-                with torch.cuda.stream(st):
+                st_side = side[i % len(side)]
+                st_side.wait_stream(main)
+                with torch.cuda.stream(st_side):
                     lay.bwd_mm_algebra(alpha)
-                forked.append(st)
-        for st in forked:          # join only the branches forked here (graph-capture rule)
-            main.wait_stream(st)
-        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
-        energy = scale * logZ
-        for lay in self.layers:
-            energy = energy + lay.phi(alpha)
-        self.energy.copy_(energy / N)
-        for lay in self.layers:
-            for g in lay.g.values():
-                g.div_(N)
-        self.g_sn.div_(N)
-        self._flag_info(self.layers)
+                forked.append(st_side)
+        for st_side in forked:     # join only the branches forked here (graph-capture rule)
+            main.wait_stream(st_side)
+        self._energy_terms(self.layers, alpha, N)
+        self._flag_info(st)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
@@ -498,7 +504,7 @@ class SGPLVM(_PackedModel):
         yb = self.y_dev.index_select(0, idx)
         nb = yb.shape[0]
         scale = -N / nb / alpha
-        setup_layers([lay], alpha)
+        st = setup_layers([lay], alpha)
         px1, px2 = self.prior_x1, self.prior_x2
         f1b, f2b = f1.index_select(0, idx), f2.index_select(0, idx)
         if self.nat_param:
@@ -548,7 +554,7 @@ class SGPLVM(_PackedModel):
         gx1.index_put_((idx,), dt1 + h1, accumulate=True)
         gx2.index_put_((idx,), dt2 + h2, accumulate=True)
         self.energy.copy_((scale * logZ + xc + lay.phi(alpha)).reshape(1))
-        self._flag_info([lay])
+        self._flag_info(st)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
@@ -658,7 +664,7 @@ class SGPSSM(_PackedModel):
         nd, ne = dyn.shape[0], emi.shape[0]
         s_dyn = -(N - 1) / nd / alpha
         s_emi = -N / ne / alpha
-        setup_layers([lay], alpha)
+        st = setup_layers([lay], alpha)
         px1, px2 = self.x_prior_1, self.x_prior_2
         c = self._consts
         post1 = c['w1'] * f1 + px1 * c['first']
@@ -719,8 +725,7 @@ class SGPSSM(_PackedModel):
         for k, g in self.gpack.views.items():
             if not k.startswith('__'):
                 g.div_(N)
-        worst = torch.stack([lay.info.max(), self._emi_info.max()]).max()
-        self.gpack.views['__info__'].copy_(worst.to(F64).reshape(1))
+        self._flag_info(st + [self._emi_info])
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):

@@ -1,0 +1,244 @@
+// Fused float64 elementwise pieces of the M x M AEP algebra: the q(u) parameter unpacking,
+// linear combinations with broadcast, transposes and rank-one terms, the packing of
+// d eta1_R, the kernel-hyperparameter chain rule and the natural-parameter log-partition.
+// These replace the chains of small tensor operations between the factorisations and the
+// products; the arithmetic is plain float64 (the sizes are M^2 per output, so the FP64 pipe
+// is not the limit), so every value equals the unfused expression's up to the order of the
+// additions.
+#include "common.cuh"
+
+namespace {
+
+__global__ void lincomb_kernel(gpk_lincomb_t d) {
+  const long per = (long)d.rows * d.cols;
+  const long total = d.sum_batch ? per : per * d.batch;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long b0 = d.sum_batch ? 0 : e / per;
+    const long r = e - b0 * per;
+    const int i = (int)(r / d.cols), j = (int)(r - (long)i * d.cols);
+    const long rt = (long)j * d.cols + i;   // transposed element (square only)
+    const int bb = d.sum_batch ? 0 : (int)b0, be = d.sum_batch ? d.batch : (int)b0 + 1;
+    double acc = 0.0;
+    for (int t = 0; t < d.nterm; ++t) {
+      const bool once = d.sum_batch && d.sX[t] == 0;   // a batch-broadcast term enters a batch sum once
+      for (int b = once ? 0 : bb; b < (once ? 1 : be); ++b)
+        acc += d.cX[t] * d.X[t][b * d.sX[t] + (d.tX[t] ? rt : r)];
+    }
+    for (int t = 0; t < d.nrank; ++t) {
+      const bool once = d.sum_batch && d.su[t] == 0 && d.sv[t] == 0;
+      for (int b = once ? 0 : bb; b < (once ? 1 : be); ++b)
+        acc += d.cr[t] * d.u[t][b * d.su[t] + i] * d.v[t][b * d.sv[t] + j];
+    }
+    d.out[e] = acc;
+  }
+}
+
+// R[d] (M x M): upper triangle from the packed eta1_R[d] (row-major triu order), exp() on the
+// diagonal, zeros below; lls2 = 2 ls, lsf2 = 2 sf.
+__global__ void nat_prep_kernel(int D, int M, int Q, const double* eta1, const double* ls, const double* sf,
+                                double* R, double* lls2, double* lsf2) {
+  const long total = (long)D * M * M;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int d = (int)(e / ((long)M * M));
+    const int r = (int)(e - (long)d * M * M);
+    const int a = r / M, b = r - a * M;
+    double v = 0.0;
+    if (a <= b) {
+      const long p = (long)a * M - (long)a * (a - 1) / 2 + (b - a);
+      v = eta1[(long)d * M * (M + 1) / 2 + p];
+      if (a == b) v = exp(v);
+    }
+    R[e] = v;
+  }
+  if (blockIdx.x == 0) {
+    for (int q = threadIdx.x; q < Q; q += blockDim.x) lls2[q] = 2.0 * ls[q];
+    if (threadIdx.x == 0) lsf2[0] = 2.0 * sf[0];
+  }
+}
+
+// out[d, p] (+)= dR[d, a, b] * (a == b ? R[d, a, a] : 1) for the upper-triangle entry p = (a, b)
+__global__ void triu_pack_kernel(int D, int M, const double* dR, const double* R, double* out, int accumulate) {
+  const long total = (long)D * M * M;
+  const long P = (long)M * (M + 1) / 2;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int d = (int)(e / ((long)M * M));
+    const int r = (int)(e - (long)d * M * M);
+    const int a = r / M, b = r - a * M;
+    if (a > b) continue;
+    const long p = (long)a * M - (long)a * (a - 1) / 2 + (b - a);
+    double v = dR[e];
+    if (a == b) v *= R[e];
+    double* o = out + (long)d * P + p;
+    *o = accumulate ? *o + v : v;
+  }
+}
+
+// g_ls[q] = dl[q] exp(ls[q]);  g_sf = 2 exp(2 sf) (dsf2 + sum(dv))   (one CTA)
+__global__ void hyp_grads_kernel(int Q, const double* ls, const double* sf, const double* dl, const double* dsf2,
+                                 const double* dv, int ndv, double* g_ls, double* g_sf) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ndv; i += blockDim.x) s += dv[i];
+  for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    if (threadIdx.x == 0) g_sf[0] = 2.0 * exp(2.0 * sf[0]) * (dsf2[0] + s);
+  }
+  for (int q = threadIdx.x; q < Q; q += blockDim.x) g_ls[q] = dl[q] * exp(ls[q]);
+}
+
+// Natural-parameter log-partition of one layer, added into *out with weight w:
+//   phi = D/2 logdet Kuu + (N/a - 1)(-1/2 sum logdet Su^-1 + 1/2 mu.th2)
+//         - (N/a)(-1/2 sum logdet Suhat^-1 + 1/2 beta muhat.th2)
+// (mu.Su^-1 mu = mu.th2 and muhat.Suhat^-1 muhat = beta muhat.th2 because mu = Su th2 and
+// muhat = Suhat beta th2.)
+__global__ void aep_phi_kernel(int D, int M, double N, double alpha, const double* logdetK,
+                               const double* ldSuinv, const double* ldShinv, const double* mu, const double* mh,
+                               const double* th2, double w, double* out) {
+  __shared__ double red[2][32];
+  double qp = 0.0, qc = 0.0;
+  for (int i = threadIdx.x; i < D * M; i += blockDim.x) {
+    qp += mu[i] * th2[i];
+    qc += mh[i] * th2[i];
+  }
+  for (int m = 16; m > 0; m >>= 1) {
+    qp += __shfl_xor_sync(0xffffffffu, qp, m);
+    qc += __shfl_xor_sync(0xffffffffu, qc, m);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = qp;
+    red[1][threadIdx.x >> 5] = qc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    qp = qc = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      qp += red[0][k];
+      qc += red[1][k];
+    }
+    double lsu = 0.0, lsh = 0.0;
+    for (int d = 0; d < D; ++d) {
+      lsu -= ldSuinv[d];
+      lsh += ldShinv[d];
+    }
+    const double beta = (N - alpha) / N;
+    const double phi = D * 0.5 * logdetK[0] + (N / alpha - 1.0) * (0.5 * lsu + 0.5 * qp) -
+                       (N / alpha) * (-0.5 * lsh + 0.5 * beta * qc);
+    out[0] += w * phi;
+  }
+}
+
+// Gaussian likelihood of one minibatch (lik_layers.py:119-181), one CTA:
+//   vt = v + sn2/a, r = y - m;  logZ = sum(-1/2 (log(2 pi vt) + r^2/vt))
+//                                     + n D (1/2 log(2 pi sn2/a) - a/2 log(2 pi sn2))
+//   dm = scale r/vt,  dv = scale (-1/2/vt + 1/2 r^2/vt^2)
+//   energy = scale logZ / N,  g_sn = scale (sum(dv/scale) 2 sn2/a + n D (1 - a)) / N
+__global__ void gauss_lik_kernel(int n, int D, const double* m, const double* v, const double* y,
+                                 const double* sn, double alpha, double scale, double invN, double* dm,
+                                 double* dv, double* energy, double* g_sn) {
+  __shared__ double red[2][32];
+  const double sn2 = exp(2.0 * sn[0]);
+  const double two_pi = 6.283185307179586;
+  double sl = 0.0, sd = 0.0;
+  for (int i = threadIdx.x; i < n * D; i += blockDim.x) {
+    const double vt = v[i] + sn2 / alpha;
+    const double r = y[i] - m[i];
+    sl += -0.5 * (log(two_pi * vt) + r * r / vt);
+    const double g = -0.5 / vt + 0.5 * r * r / (vt * vt);
+    sd += g;
+    dm[i] = scale * (r / vt);
+    dv[i] = scale * g;
+  }
+  for (int k = 16; k > 0; k >>= 1) {
+    sl += __shfl_xor_sync(0xffffffffu, sl, k);
+    sd += __shfl_xor_sync(0xffffffffu, sd, k);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = sl;
+    red[1][threadIdx.x >> 5] = sd;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sl = sd = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      sl += red[0][k];
+      sd += red[1][k];
+    }
+    const double nD = (double)n * D;
+    const double logZ = sl + nD * (0.5 * log(two_pi * sn2 / alpha) - 0.5 * alpha * log(two_pi * sn2));
+    energy[0] = scale * logZ * invN;
+    g_sn[0] = scale * (sd * 2.0 * sn2 / alpha + nD * (1.0 - alpha)) * invN;
+  }
+}
+
+int grid_for(long n) {
+  long g = (n + 255) / 256;
+  long cap = 4L * gpk::sm_count();
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+}  // namespace
+
+extern "C" int gpk_lincomb(const gpk_lincomb_t* d, void* stream) {
+  GPK_REQUIRE(d && d->out, "lincomb: null descriptor or output");
+  GPK_REQUIRE(d->batch >= 1 && d->rows >= 0 && d->cols >= 0, "lincomb: bad shape");
+  GPK_REQUIRE(d->nterm >= 0 && d->nterm <= GPK_LC_TERMS && d->nrank >= 0 && d->nrank <= GPK_LC_RANK,
+              "lincomb: %d dense / %d rank-one terms (max %d / %d)", d->nterm, d->nrank, GPK_LC_TERMS, GPK_LC_RANK);
+  for (int t = 0; t < d->nterm; ++t) {
+    GPK_REQUIRE(d->X[t], "lincomb: null dense term %d", t);
+    GPK_REQUIRE(!d->tX[t] || d->rows == d->cols, "lincomb: transposed term %d needs a square shape", t);
+  }
+  for (int t = 0; t < d->nrank; ++t) GPK_REQUIRE(d->u[t] && d->v[t], "lincomb: null rank-one term %d", t);
+  const long n = (long)d->rows * d->cols * (d->sum_batch ? 1 : d->batch);
+  if (n == 0) return GPK_OK;
+  lincomb_kernel<<<grid_for(n), 256, 0, gpk::as_stream(stream)>>>(*d);
+  return gpk::check_launch("lincomb");
+}
+
+extern "C" int gpk_nat_prep(int D, int M, int Q, const double* eta1, const double* ls, const double* sf, double* R,
+                            double* lls2, double* lsf2, void* stream) {
+  GPK_REQUIRE(D >= 1 && M >= 1 && Q >= 1, "nat_prep: bad sizes");
+  GPK_REQUIRE(eta1 && ls && sf && R && lls2 && lsf2, "nat_prep: null pointer");
+  nat_prep_kernel<<<grid_for((long)D * M * M), 256, 0, gpk::as_stream(stream)>>>(D, M, Q, eta1, ls, sf, R, lls2,
+                                                                                   lsf2);
+  return gpk::check_launch("nat_prep");
+}
+
+extern "C" int gpk_triu_pack(int D, int M, const double* dR, const double* R, double* out, int accumulate,
+                             void* stream) {
+  GPK_REQUIRE(D >= 1 && M >= 1, "triu_pack: bad sizes");
+  GPK_REQUIRE(dR && R && out, "triu_pack: null pointer");
+  triu_pack_kernel<<<grid_for((long)D * M * M), 256, 0, gpk::as_stream(stream)>>>(D, M, dR, R, out, accumulate);
+  return gpk::check_launch("triu_pack");
+}
+
+extern "C" int gpk_hyp_grads(int Q, const double* ls, const double* sf, const double* dl, const double* dsf2,
+                             const double* dv, int ndv, double* g_ls, double* g_sf, void* stream) {
+  GPK_REQUIRE(Q >= 1 && ndv >= 0, "hyp_grads: bad sizes");
+  GPK_REQUIRE(ls && sf && dl && dsf2 && g_ls && g_sf && (dv || ndv == 0), "hyp_grads: null pointer");
+  hyp_grads_kernel<<<1, 256, 0, gpk::as_stream(stream)>>>(Q, ls, sf, dl, dsf2, dv, ndv, g_ls, g_sf);
+  return gpk::check_launch("hyp_grads");
+}
+
+extern "C" int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, const double* ldSuinv,
+                           const double* ldShinv, const double* mu, const double* mh, const double* th2, double w,
+                           double* out, void* stream) {
+  GPK_REQUIRE(D >= 1 && M >= 1 && N > 0 && alpha > 0, "aep_phi: bad sizes");
+  GPK_REQUIRE(logdetK && ldSuinv && ldShinv && mu && mh && th2 && out, "aep_phi: null pointer");
+  aep_phi_kernel<<<1, 256, 0, gpk::as_stream(stream)>>>(D, M, N, alpha, logdetK, ldSuinv, ldShinv, mu, mh, th2, w,
+                                                        out);
+  return gpk::check_launch("aep_phi");
+}
+
+extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn,
+                             double alpha, double scale, double invN, double* dm, double* dv, double* energy,
+                             double* g_sn, void* stream) {
+  GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0, "gauss_lik: bad sizes");
+  GPK_REQUIRE(m && v && y && sn && dm && dv && energy && g_sn, "gauss_lik: null pointer");
+  gauss_lik_kernel<<<1, 1024, 0, gpk::as_stream(stream)>>>(n, D, m, v, y, sn, alpha, scale, invN, dm, dv, energy,
+                                                           g_sn);
+  return gpk::check_launch("gauss_lik");
+}

@@ -6,20 +6,38 @@
 
 namespace {
 
-constexpr int TK = 16;   // GEMM k-chunk
+// An 8-byte element that holds a double-float as its raw (hi, lo) float pair (P2 operands).
+template <typename T>
+__device__ __forceinline__ T pair_bits(typename Num<T>::store_t v);
+template <>
+__device__ __forceinline__ df64 pair_bits<df64>(double v) {
+  return make_df(__int_as_float(__double2loint(v)), __int_as_float(__double2hiint(v)));
+}
+template <>
+__device__ __forceinline__ float pair_bits<float>(float v) { return v; }
 
-// C tile TBM x TBM per CTA (256 threads, R x R outputs each with R = TBM/16).  The k extent is
-// staged through shared memory in chunks of up to KC: all global loads of a chunk are issued
-// together (one latency per chunk instead of one per 16-wide slice), then R*R*KC double-float
-// multiply-adds per thread run from shared memory.
+// C tile TBM x TBM per CTA, NG*KS threads: KS groups of NG = (TBM/R)^2 threads each take every
+// KS-th k of a chunk (R x R outputs per thread, R = 2 for 32-wide tiles, else 1; 8-wide tiles
+// put small products on more SMs), so a thread's chain of dependent
+// double-float multiply-adds is k/KS long; the KS partial sums are added through shared
+// memory at the end.  The k extent is staged through shared memory in chunks of up to KC,
+// and every global load a thread makes for a chunk is issued before any is converted, so a
+// chunk costs one memory latency rather than one per element.
 constexpr int KC = 128;
-template <typename T, int TBM>
-__global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, int tA, int tB, double alpha,
-                                                   const typename Num<T>::store_t* A, int lda, long sA,
-                                                   const typename Num<T>::store_t* B, int ldb, long sB,
-                                                   double beta, typename Num<T>::store_t* C, int ldc, long sC) {
+// The epilogue is C = alpha acc + beta E, where E may be C itself or another (possibly
+// batch-broadcast, sE = 0) matrix.
+template <int TBM>
+struct GemmShape {
+  static constexpr int R = TBM >= 32 ? 2 : 1, TPD = TBM / R, NG = TPD * TPD;
+};
+template <typename T, int TBM, int KS, bool P2>
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_kernel(
+    int m, int n, int k, int tA, int tB, double alpha, const typename Num<T>::store_t* A, int lda, long sA,
+    const typename Num<T>::store_t* B, int ldb, long sB, double beta, const typename Num<T>::store_t* E, int lde,
+    long sE, typename Num<T>::store_t* C, int ldc, long sC) {
   typedef typename Num<T>::store_t S;
-  constexpr int R = TBM / 16;
+  constexpr int R = GemmShape<TBM>::R, TPD = GemmShape<TBM>::TPD, NG = GemmShape<TBM>::NG;
+  constexpr int NT = NG * KS, NPT = KC * TBM / NT;
   extern __shared__ __align__(16) char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);      // [KC][TBM]
   T* Bs = As + KC * TBM;                        // [KC][TBM]
@@ -27,35 +45,49 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, int tA, 
   A += bz * sA;
   B += bz * sB;
   C += bz * sC;
+  if (E) E += bz * sE;
   const int i0 = blockIdx.y * TBM, j0 = blockIdx.x * TBM;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int g = threadIdx.x / NG, t = threadIdx.x % NG;
+  const int tx = t % TPD, ty = t / TPD;
   T acc[R][R];
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
     for (int c = 0; c < R; ++c) acc[r][c] = Num<T>::zero();
   for (int k0 = 0; k0 < k; k0 += KC) {
-    const int kc = min(KC, k - k0);
-    // A tile: element (ii, kk) of op(A); consecutive threads take consecutive memory
-    for (int e = threadIdx.x; e < kc * TBM; e += 256) {
-      int kk, ii;
-      if (tA) { kk = e / TBM; ii = e % TBM; } else { ii = e / kc; kk = e % kc; }
-      int gi = i0 + ii, gk = k0 + kk;
-      T av = Num<T>::zero();
-      if (gi < m) av = Num<T>::ld(tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk]);
-      As[kk * TBM + ii] = av;
+    const int kc = min(KC, k - k0), ne = kc * TBM;
+    // element e of a tile: (ii, kk) of op(A) / (kk, jj) of op(B); consecutive threads take
+    // consecutive memory
+    S ra[NPT], rb[NPT];
+    int oa[NPT], ob[NPT];
+#pragma unroll
+    for (int u = 0; u < NPT; ++u) {
+      const int e = threadIdx.x + u * NT;
+      ra[u] = rb[u] = S(0);
+      oa[u] = ob[u] = -1;
+      if (e < ne) {
+        int kk, ii;
+        if (tA) { kk = e / TBM; ii = e - kk * TBM; } else { ii = e / kc; kk = e - ii * kc; }
+        const int gi = i0 + ii, gk = k0 + kk;
+        oa[u] = kk * TBM + ii;
+        if (gi < m) ra[u] = tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
+        int jj;
+        if (tB) { jj = e / kc; kk = e - jj * kc; } else { kk = e / TBM; jj = e - kk * TBM; }
+        const int gj = j0 + jj, gk2 = k0 + kk;
+        ob[u] = kk * TBM + jj;
+        if (gj < n) rb[u] = tB ? B[(size_t)gj * ldb + gk2] : B[(size_t)gk2 * ldb + gj];
+      }
     }
-    for (int e = threadIdx.x; e < kc * TBM; e += 256) {
-      int kk, jj;
-      if (tB) { jj = e / kc; kk = e % kc; } else { kk = e / TBM; jj = e % TBM; }
-      int gj = j0 + jj, gk = k0 + kk;
-      T bv = Num<T>::zero();
-      if (gj < n) bv = Num<T>::ld(tB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj]);
-      Bs[kk * TBM + jj] = bv;
+#pragma unroll
+    for (int u = 0; u < NPT; ++u) {
+      if (oa[u] >= 0) {
+        As[oa[u]] = P2 ? pair_bits<T>(ra[u]) : Num<T>::ld(ra[u]);
+        Bs[ob[u]] = P2 ? pair_bits<T>(rb[u]) : Num<T>::ld(rb[u]);
+      }
     }
     __syncthreads();
 #pragma unroll 4
-    for (int kk = 0; kk < kc; ++kk) {
+    for (int kk = g; kk < kc; kk += KS) {
       T av[R], bv[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -69,20 +101,235 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, int tA, 
     }
     __syncthreads();
   }
-  const bool unit = alpha == 1.0;
-  const T al = Num<T>::ld(static_cast<S>(alpha));
-  const T be = Num<T>::ld(static_cast<S>(beta));
+  if (KS > 1) {
+    // the tiles are no longer read (barrier at the end of the last chunk): reuse them
+    T* red = As;   // [KS-1][NG][R*R]
+    if (g > 0) {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) red[((g - 1) * NG + t) * R * R + r * R + c] = acc[r][c];
+    }
+    __syncthreads();
+    if (g > 0) return;
+#pragma unroll
+    for (int q = 0; q < KS - 1; ++q)
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc[r][c] = add(acc[r][c], red[(q * NG + t) * R * R + r * R + c]);
+  }
+  // epilogue in the storage type (float64 for df64): the product is rounded once to it, and
+  // alpha / beta E enter with that type's arithmetic, as separate BLAS-style operations would
+  const S al = static_cast<S>(alpha), be = static_cast<S>(beta);
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
     for (int c = 0; c < R; ++c) {
       int gi = i0 + ty * R + r, gj = j0 + tx * R + c;
       if (gi < m && gj < n) {
-        T v = unit ? acc[r][c] : mul(al, acc[r][c]);
-        if (beta != 0.0) v = fma_(be, Num<T>::ld(C[(size_t)gi * ldc + gj]), v);
-        C[(size_t)gi * ldc + gj] = Num<T>::st(v);
+        S v = Num<T>::st(acc[r][c]);
+        if (alpha != 1.0) v = al * v;
+        if (beta != 0.0) v = v + be * E[(size_t)gi * lde + gj];
+        C[(size_t)gi * ldc + gj] = v;
       }
     }
+}
+
+// ---- the SPD inverse fast path: factor (one CTA) -> L^-1 (many CTAs) -> L^-T L^-1 (GEMM) ----
+
+// Calls f(std::integral_constant<int, i>) for a warp-uniform runtime i < N, so that register
+// arrays are indexed with compile-time constants (no local memory, no select chains).
+template <int N, typename F>
+__device__ __forceinline__ void with_static(int i, F&& f) {
+  if constexpr (N > 0) {
+    if (i == N - 1) f(std::integral_constant<int, N - 1>{});
+    else with_static<N - 1>(i, f);
+  }
+}
+
+// Right-looking Cholesky of one M x M SPD matrix per CTA (M <= min(32*RS, NW*CS)).  Element
+// (i, j) of the lower triangle lives in a register of lane i % 32 of warp j % NW (slot
+// [i/32][j/NW]), so a trailing update touches no shared memory except the column of L it
+// reads.  One barrier per column: while the other warps apply column k, the warp owning column
+// k+1 updates that column first, takes its pivot and publishes column k+1 of L (one-column
+// look-ahead).  Outputs: Lw (column-major L as raw (hi, lo) pairs, 1/L_kk on the diagonal -
+// the input of trinv_kernel), logdet = 2 sum log L_kk, info[b] = k+1 for a non-positive pivot.
+template <typename T, int RS, int CS, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typename Num<T>::store_t* A, long sA,
+                                                                T* Lw, double* logdet, int* info) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  const int LD = M | 1;
+  T* Ls = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][LD], column k at Ls + k*LD
+  T* dg = Ls + (size_t)M * LD;                                       // [M] L_kk
+  T* red = dg + M;                                                   // [NW]
+  __shared__ int s_info;
+  const int b = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NTH = NW * 32;
+  A += b * sA;
+  {
+    // stage A (row-major, storage type) in the Ls area with asynchronous copies
+    S* raw = reinterpret_cast<S*>(Ls);
+    for (int e = threadIdx.x; e < M * M; e += NTH) {
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(raw + e);
+      if (sizeof(S) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(A + e));
+      else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(A + e));
+    }
+    asm volatile("cp.async.wait_all;\n" ::);
+  }
+  load_exp_table(tab);
+  if (threadIdx.x == 0) s_info = 0;
+  __syncthreads();
+  T a[RS][CS];
+  {
+    const S* raw = reinterpret_cast<const S*>(Ls);
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr)
+#pragma unroll
+      for (int cc = 0; cc < CS; ++cc) {
+        const int i = lane + 32 * rr, j = w + NW * cc;
+        a[rr][cc] = (i < M && j <= i) ? Num<T>::ld(raw[i * M + j]) : Num<T>::zero();
+      }
+  }
+  __syncthreads();   // the staging area becomes L
+
+  // column k of L from the registers of warp k % NW (warp-uniform caller)
+  auto finalize = [&](int k) {
+    T col[RS];
+    with_static<CS>(k / NW, [&](auto CK) {
+#pragma unroll
+      for (int rr = 0; rr < RS; ++rr) col[rr] = a[rr][CK.value];
+    });
+    T pv = col[0];
+    with_static<RS>(k >> 5, [&](auto RK) { pv = col[RK.value]; });
+    const T p = shfl_idx(pv, k & 31);
+    if (!(Num<T>::approx(p) > 0.f)) {
+      if (lane == 0) s_info = k + 1;
+      return;
+    }
+    const T d = sqrt_(p), r = recip(d);
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+      const int i = lane + 32 * rr;
+      if (i > k && i < M) Ls[k * LD + i] = mul(col[rr], r);
+    }
+    if (lane == 0) {
+      Ls[k * LD + k] = r;   // 1 / L_kk
+      dg[k] = d;
+    }
+  };
+
+  if (w == 0) finalize(0);
+  __syncthreads();
+  for (int k = 0; k + 1 < M; ++k) {
+    if (s_info) break;   // uniform: written before the last barrier
+    T li[RS];
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+      const int i = lane + 32 * rr;
+      li[rr] = (i > k && i < M) ? neg(Ls[k * LD + i]) : Num<T>::zero();
+    }
+    const int k1 = k + 1, c1 = k1 / NW;
+    const bool owner = w == k1 % NW;
+    if (owner) {
+      const T ljk = Ls[k * LD + k1];
+      const int r1 = k1 >> 5;
+      with_static<CS>(c1, [&](auto C1) {
+#pragma unroll
+        for (int rr = 0; rr < RS; ++rr)
+          if (rr >= r1) a[rr][C1.value] = fma_(li[rr], ljk, a[rr][C1.value]);
+      });
+      finalize(k1);
+    }
+#pragma unroll
+    for (int cc = 0; cc < CS; ++cc) {
+      const int j = w + NW * cc;
+      if (j <= k || j >= M || (owner && cc == c1)) continue;   // warp-uniform
+      const T ljk = Ls[k * LD + j];
+      const int rj = j >> 5;
+#pragma unroll
+      for (int rr = 0; rr < RS; ++rr)
+        if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+    }
+    __syncthreads();
+  }
+  const int bad = s_info;
+  if (info && threadIdx.x == 0) info[b] = bad;
+  if (bad) return;
+  // column-major L with 1/L_kk on the diagonal (rows >= k of column k; the rest unused)
+  T* Lb = Lw + (size_t)b * M * M;
+  for (int e = threadIdx.x; e < M * M; e += NTH) {
+    const int k = e / M, i = e - k * M;
+    if (i >= k) Lb[e] = Ls[k * LD + i];
+  }
+  if (logdet) {
+    T l = Num<T>::zero();
+    for (int i = threadIdx.x; i < M; i += NTH) l = add(l, log_tab(dg[i], tab));
+    l = warp_sum(l);
+    if (lane == 0) red[w] = l;
+    __syncthreads();
+    if (w == 0) {
+      T s = warp_sum(lane < NW ? red[lane] : Num<T>::zero());
+      if (lane == 0) logdet[b] = (double)Num<T>::st(scale2(s, 1));
+    }
+  }
+}
+
+// X = L^-1 by columns: warp j solves L x = e_j by right-looking forward substitution
+//   x_k = t_k / L_kk,  t_i -= L_ik x_k (i > k),  t = e_j at start,
+// with row k held by lane k % 32 and broadcast by shuffle; columns are independent, so the
+// CTAs of a launch (TW columns each) run side by side.  Input: Lw from spd_factor_kernel
+// (column-major, 1/L_kk on the diagonal); output Xt[b][j*M + i] = X_ij (i.e. X^T row-major,
+// zeros for i < j).  info[b] != 0 (a failed factorisation) leaves Xt untouched.
+constexpr int TW = 4;
+template <typename T, int RS>
+__global__ void __launch_bounds__(TW * 32) trinv_kernel(int M, const T* Lw, T* Xt, const int* info) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const int b = blockIdx.y;
+  if (info && info[b]) return;
+  const int j0 = blockIdx.x * TW;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // columns k >= j0 of L (rows >= k) into shared memory: Ls[(k - j0) * M + i]
+  T* Ls = reinterpret_cast<T*>(smem_raw);
+  const T* Lb = Lw + (size_t)b * M * M + (size_t)j0 * M;
+  const int n = (M - j0) * M;
+  for (int e = threadIdx.x; e < n; e += TW * 32) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(Ls + e);
+    if (sizeof(T) == 8)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(Lb + e));
+    else
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(Lb + e));
+  }
+  asm volatile("cp.async.wait_all;\n" ::);
+  __syncthreads();
+  const int j = j0 + w;
+  if (j >= M) return;
+  T t[RS];
+#pragma unroll
+  for (int rr = 0; rr < RS; ++rr) t[rr] = (lane + 32 * rr == j) ? Num<T>::c(1.f) : Num<T>::zero();
+  for (int k = j; k < M; ++k) {
+    const T* col = Ls + (size_t)(k - j0) * M;
+    const int rk = k >> 5;
+    T tk = t[0];
+    with_static<RS>(rk, [&](auto RK) { tk = t[RK.value]; });
+    const T xk = mul(shfl_idx(tk, k & 31), col[k]);
+    if (lane == (k & 31)) with_static<RS>(rk, [&](auto RK) { t[RK.value] = xk; });
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+      const int i = lane + 32 * rr;
+      if (rr >= rk && i > k && i < M) t[rr] = fma_(neg(col[i]), xk, t[rr]);
+    }
+  }
+  T* Xb = Xt + (size_t)b * M * M + (size_t)j * M;
+#pragma unroll
+  for (int rr = 0; rr < RS; ++rr) {
+    const int i = lane + 32 * rr;
+    if (i < M) Xb[i] = i >= j ? t[rr] : Num<T>::zero();
+  }
 }
 
 // GMEM = false: the matrix lives in shared memory (M <= 128).  GMEM = true: it lives in the
@@ -359,25 +606,34 @@ __global__ void __launch_bounds__(128) small_spd_kernel(int B, int n, const type
     }
 }
 
-template <typename T>
-int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
-                const void* B, int ldb, long sB, double beta, void* C, int ldc, long sC, cudaStream_t st) {
+template <typename T, int TBM, int KS, bool P2>
+void gemm_go(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
+             const void* B, int ldb, long sB, double beta, const void* E, int lde, long sE, void* C, int ldc, long sC,
+             cudaStream_t st) {
   typedef typename Num<T>::store_t S;
-  // 32x32 tiles when they already fill the GPU, else 16x16 tiles for more CTAs
-  long tiles32 = (long)gpk::ceil_div(n, 32) * gpk::ceil_div(m, 32) * batch;
-  if (tiles32 >= 2L * gpk::sm_count()) {
-    dim3 grid(gpk::ceil_div(n, 32), gpk::ceil_div(m, 32), batch);
-    size_t sm = 2 * KC * 32 * sizeof(T);
-    auto kfn = gemm_kernel<T, 32>;
-    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    kfn<<<grid, 256, sm, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB, beta, (S*)C,
-                               ldc, sC);
-  } else {
-    dim3 grid(gpk::ceil_div(n, 16), gpk::ceil_div(m, 16), batch);
-    size_t sm = 2 * KC * 16 * sizeof(T);
-    gemm_kernel<T, 16><<<grid, 256, sm, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB,
-                                              beta, (S*)C, ldc, sC);
-  }
+  dim3 grid(gpk::ceil_div(n, TBM), gpk::ceil_div(m, TBM), batch);
+  const size_t sm = 2 * KC * TBM * sizeof(T);
+  auto kfn = gemm_kernel<T, TBM, KS, P2>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  kfn<<<grid, GemmShape<TBM>::NG * KS, sm, st>>>(m, n, k, tA, tB, alpha, (const S*)A, lda, sA, (const S*)B, ldb, sB,
+                                                 beta, (const S*)E, lde, sE, (S*)C, ldc, sC);
+}
+
+// Tile choice: 32x32 tiles when they already fill the GPU twice over, 16x16 when those fill
+// it once, else 8x8 tiles so that a small product still spreads over most SMs.  P2: A and B
+// hold raw double-float pairs (8 bytes per element) instead of float64.
+template <typename T, bool P2 = false>
+int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
+                const void* B, int ldb, long sB, double beta, const void* E, int lde, long sE, void* C, int ldc,
+                long sC, cudaStream_t st) {
+  const long t32 = (long)gpk::ceil_div(n, 32) * gpk::ceil_div(m, 32) * batch;
+  const long t16 = (long)gpk::ceil_div(n, 16) * gpk::ceil_div(m, 16) * batch;
+  if (t32 >= 2L * gpk::sm_count())
+    gemm_go<T, 32, 2, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
+  else if (t16 >= gpk::sm_count())
+    gemm_go<T, 16, 4, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
+  else
+    gemm_go<T, 8, 4, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
   return gpk::check_launch("gemm");
 }
 
@@ -388,17 +644,79 @@ extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, in
                         void* C, int ldc, long strideC, void* stream) {
   GPK_REQUIRE(batch >= 0 && m >= 0 && n >= 0 && k >= 0, "gemm: negative size");
   GPK_REQUIRE(batch <= 65535, "gemm: batch %d > 65535", batch);
-  GPK_REQUIRE(A && B && C, "gemm: null pointer");
+  GPK_REQUIRE(C && (k == 0 || (A && B)), "gemm: null pointer");
   GPK_REQUIRE(lda >= (transA ? m : k) && ldb >= (transB ? k : n) && ldc >= n, "gemm: bad leading dimension");
   if (batch == 0 || m == 0 || n == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
   if (prec == GPK_DF64)
     return gemm_launch<df64>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc,
-                             strideC, st);
+                             strideC, C, ldc, strideC, st);
   if (prec == GPK_FP32)
     return gemm_launch<float>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc,
-                              strideC, st);
+                              strideC, C, ldc, strideC, st);
   return gpk::fail(GPK_EINVAL, "gemm: unknown precision %d", prec);
+}
+
+extern "C" int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
+                           const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
+                           const void* E, int lde, long strideE, void* C, int ldc, long strideC, void* stream) {
+  GPK_REQUIRE(batch >= 0 && m >= 0 && n >= 0 && k >= 0, "gemm_ex: negative size");
+  GPK_REQUIRE(batch <= 65535, "gemm_ex: batch %d > 65535", batch);
+  GPK_REQUIRE(C && (k == 0 || (A && B)) && (beta == 0.0 || E), "gemm_ex: null pointer");
+  GPK_REQUIRE(lda >= (transA ? m : k) && ldb >= (transB ? k : n) && ldc >= n && (beta == 0.0 || lde >= n),
+              "gemm_ex: bad leading dimension");
+  if (batch == 0 || m == 0 || n == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64)
+    return gemm_launch<df64>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, E, lde,
+                             strideE, C, ldc, strideC, st);
+  if (prec == GPK_FP32)
+    return gemm_launch<float>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, E, lde,
+                              strideE, C, ldc, strideC, st);
+  return gpk::fail(GPK_EINVAL, "gemm_ex: unknown precision %d", prec);
+}
+
+template <typename T, int RS, int CS, int NW>
+int spd_factor_launch(int batch, int M, const void* A, T* Lw, double* logdet, int* info, cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  const size_t sm = 256 * sizeof(float2) + ((size_t)M * (M | 1) + M + NW) * sizeof(T);
+  auto k = spd_factor_kernel<T, RS, CS, NW>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<batch, NW * 32, sm, st>>>(M, (const S*)A, (long)M * M, Lw, logdet, info);
+  return gpk::check_launch("spd_factor");
+}
+
+template <typename T, int RS>
+int trinv_launch(int batch, int M, const T* Lw, T* Xt, const int* info, cudaStream_t st) {
+  const size_t sm = (size_t)M * M * sizeof(T);
+  auto k = trinv_kernel<T, RS>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<dim3(gpk::ceil_div(M, TW), batch), TW * 32, sm, st>>>(M, Lw, Xt, info);
+  return gpk::check_launch("trinv");
+}
+
+// M <= 128: A^-1 = L^-T L^-1 through the factor, the column-parallel L^-1 and one GEMM.
+// work: 2*batch*M*M elements of T (L, then X^T).  info is required (it gates trinv).
+template <typename T>
+int spd_inv_small(int batch, int M, const void* A, void* Ainv, double* logdet, int* info, void* work,
+                  cudaStream_t st) {
+  T* Lw = reinterpret_cast<T*>(work);
+  T* Xt = Lw + (size_t)batch * M * M;
+  int rc;
+  if (M <= 32) rc = spd_factor_launch<T, 1, 2, 16>(batch, M, A, Lw, logdet, info, st);
+  else if (M <= 64) rc = spd_factor_launch<T, 2, 4, 16>(batch, M, A, Lw, logdet, info, st);
+  else if (M <= 96) rc = spd_factor_launch<T, 3, 6, 16>(batch, M, A, Lw, logdet, info, st);
+  else if (M <= 112) rc = spd_factor_launch<T, 4, 7, 16>(batch, M, A, Lw, logdet, info, st);
+  else rc = spd_factor_launch<T, 4, 8, 16>(batch, M, A, Lw, logdet, info, st);
+  if (rc) return rc;
+  if (M <= 32) rc = trinv_launch<T, 1>(batch, M, Lw, Xt, info, st);
+  else if (M <= 64) rc = trinv_launch<T, 2>(batch, M, Lw, Xt, info, st);
+  else if (M <= 96) rc = trinv_launch<T, 3>(batch, M, Lw, Xt, info, st);
+  else rc = trinv_launch<T, 4>(batch, M, Lw, Xt, info, st);
+  if (rc) return rc;
+  const long s = (long)M * M;
+  // A^-1 = X^T X = Xt Xt^T
+  return gemm_launch<T, true>(batch, M, M, M, 0, 1, 1.0, Xt, M, s, Xt, M, s, 0.0, nullptr, M, 0, Ainv, M, s, st);
 }
 
 template <typename T, bool GMEM>
@@ -430,27 +748,25 @@ extern "C" int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* 
   return gpk::fail(GPK_EINVAL, "chol_inv: unknown precision %d", prec);
 }
 
-extern "C" int gpk_chol_linv(int prec, int batch, int M, const void* A, void* Linv, double* logdet, int* info,
-                             void* work, void* stream) {
-  GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "chol_linv: M=%d outside [1,4096]", M);
-  GPK_REQUIRE(A && Linv, "chol_linv: null pointer");
-  GPK_REQUIRE(M <= 128 || work, "chol_linv: M=%d > 128 needs a workspace of batch*M*M elements", M);
-  if (batch == 0) return GPK_OK;
-  cudaStream_t st = gpk::as_stream(stream);
-  const bool gm = M > 128;
-  if (prec == GPK_DF64)
-    return gm ? chol_launch<df64, true>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st)
-              : chol_launch<df64, false>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st);
-  if (prec == GPK_FP32)
-    return gm ? chol_launch<float, true>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st)
-              : chol_launch<float, false>(batch, M, A, nullptr, nullptr, logdet, info, work, Linv, st);
-  return gpk::fail(GPK_EINVAL, "chol_linv: unknown precision %d", prec);
-}
-
 extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
                             void* stream) {
   GPK_REQUIRE(M <= 128, "chol_inv: M=%d > 128 needs gpk_chol_inv_ws", M);
   return gpk_chol_inv_ws(prec, batch, M, A, Ainv, L, logdet, info, nullptr, stream);
+}
+
+extern "C" int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
+                           void* work, void* stream) {
+  GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "spd_inv: M=%d outside [1,4096]", M);
+  GPK_REQUIRE(A && Ainv && info && work, "spd_inv: null pointer");
+  if (batch == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec != GPK_DF64 && prec != GPK_FP32) return gpk::fail(GPK_EINVAL, "spd_inv: unknown precision %d", prec);
+  if (M > 128)
+    return prec == GPK_DF64
+               ? chol_launch<df64, true>(batch, M, A, Ainv, nullptr, logdet, info, work, nullptr, st)
+               : chol_launch<float, true>(batch, M, A, Ainv, nullptr, logdet, info, work, nullptr, st);
+  return prec == GPK_DF64 ? spd_inv_small<df64>(batch, M, A, Ainv, logdet, info, work, st)
+                          : spd_inv_small<float>(batch, M, A, Ainv, logdet, info, work, st);
 }
 
 extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,

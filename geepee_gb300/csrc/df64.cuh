@@ -188,6 +188,10 @@ __device__ __forceinline__ df64 shfl_xor(df64 a, int m) {
   return make_df(__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m));
 }
 __device__ __forceinline__ float shfl_xor(float a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+__device__ __forceinline__ df64 shfl_idx(df64 a, int src) {
+  return make_df(__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src));
+}
+__device__ __forceinline__ float shfl_idx(float a, int src) { return __shfl_sync(0xffffffffu, a, src); }
 __device__ __forceinline__ df64 warp_sum(df64 a) {
 #pragma unroll
   for (int m = 16; m > 0; m >>= 1) a = add(a, shfl_xor(a, m));

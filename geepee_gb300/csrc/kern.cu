@@ -6,7 +6,6 @@ namespace {
 
 constexpr int DMAXK = 64;   // max input dimension
 constexpr int DO_MAX = 4;   // max output dimension of a layer
-constexpr int RR = 4;       // rows per CTA pass in the layer kernels
 
 template <typename T>
 struct Hyp {
@@ -54,6 +53,17 @@ __global__ void __launch_bounds__(256) kern_matrix_kernel(int N, int M, int D, c
 // Deterministic-input layer forward for rows n:
 //   k_n = K(x_n, Z);  m_nd = k_n . A_d;  Bk_ndb = sum_a B_d[a,b] k_na;  v_nd = sf2 + k_n . Bk_nd
 // (geepee/aep_models.py:142-158, base_models.py:265-284).
+//
+// A CTA takes tiles of FT rows.  The rows' kernel values go to shared memory; then, for each
+// output d and block of 128 columns b, every thread owns one column and FT/2 rows of Bk and
+// runs their sums over a from shared memory, while B_d streams through shared memory in
+// chunks of FKA rows.  The next chunk's global loads are issued before the current chunk is
+// used (register double buffer), so the stream costs one memory latency per tile, not one
+// per chunk.  m and v are reduced over the columns by warp shuffles.
+constexpr int FT = 8;      // rows per tile
+constexpr int FKA = 32;    // rows of B_d per staged chunk
+constexpr int FCB = 128;   // columns per block
+constexpr int FNL = FKA * FCB / 256;   // staged elements per thread per chunk
 template <typename T>
 __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int Dout,
                                                       const typename Num<T>::store_t* x, int ldx,
@@ -63,97 +73,120 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
                                                       typename Num<T>::store_t* kfu,
                                                       typename Num<T>::store_t* Bk,
                                                       typename Num<T>::store_t* m_out,
-                                                      typename Num<T>::store_t* v_out, int bstage) {
+                                                      typename Num<T>::store_t* v_out, int zstage) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
-  T* kr = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [RR][M]
-  T* red = kr + RR * M;                                                              // [33][64]
-  T* Bsm = red + 33 * 64;                                        // [Dout][M][M] when staged
+  T* kr = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [FT][M]
+  T* Bc = kr + FT * M;                       // [FKA][FCB]
+  T* red = Bc + FKA * FCB;                   // [8 warps][DO_MAX][FT/2][2]
+  T* xs = red + 8 * DO_MAX * FT;             // [FT][D]
+  T* zs = xs + FT * D;                       // [M][D] when staged
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int col = tid & (FCB - 1), rh = tid >> 7;   // column in the block, row half
   load_exp_table(tab);
-  if (bstage)
-    for (int i = threadIdx.x; i < Dout * M * M; i += blockDim.x) Bsm[i] = Num<T>::ld(B[i]);
+  if (zstage)
+    for (int i = tid; i < M * D; i += 256) zs[i] = Num<T>::ld(z[i]);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
-  __syncthreads();
-  for (int n0 = blockIdx.x * RR; n0 < N; n0 += gridDim.x * RR) {
-    for (int i = threadIdx.x; i < RR * M; i += blockDim.x) {
-      int r = i / M, mm = i % M, n = n0 + r;
+  const int nca = (M + FKA - 1) / FKA, ncb = (M + FCB - 1) / FCB, nq = Dout * ncb * nca;
+  const size_t MM = (size_t)M * M;
+  auto issue = [&](int q, S* raw) {
+    const int d = q / (ncb * nca), cb0 = ((q / nca) % ncb) * FCB, a0 = (q % nca) * FKA;
+    const S* Bd = B + (size_t)d * MM;
+#pragma unroll
+    for (int u = 0; u < FNL; ++u) {
+      const int e = tid + u * 256, aa = e / FCB, cc = e % FCB;
+      const int a = a0 + aa, b = cb0 + cc;
+      raw[u] = (a < M && b < M) ? Bd[(size_t)a * M + b] : S(0);
+    }
+  };
+  for (int n0 = blockIdx.x * FT; n0 < N; n0 += gridDim.x * FT) {
+    S raw[FNL];
+    issue(0, raw);   // the first chunk's loads overlap the kernel values below
+    for (int i = tid; i < FT * D; i += 256) {
+      const int r = i / D, q = i - r * D, n = n0 + r;
+      xs[i] = n < N ? Num<T>::ld(x[(size_t)n * ldx + q]) : Num<T>::zero();
+    }
+    __syncthreads();
+    for (int i = tid; i < FT * M; i += 256) {
+      const int r = i / M, mm = i - r * M, n = n0 + r;
       T k = Num<T>::zero();
       if (n < N) {
         T rr = Num<T>::zero();
-        for (int d = 0; d < D; ++d) {
-          T df = sub(Num<T>::ld(x[(size_t)n * ldx + d]), Num<T>::ld(z[(size_t)mm * D + d]));
-          rr = fma_(mul(df, df), h->inv_l2[d], rr);
+        for (int q = 0; q < D; ++q) {
+          const T zq = zstage ? zs[mm * D + q] : Num<T>::ld(z[(size_t)mm * D + q]);
+          const T df = sub(xs[r * D + q], zq);
+          rr = fma_(mul(df, df), h->inv_l2[q], rr);
         }
         k = exp_tab(sub(h->lsf, scale2(rr, -1)), tab);
         if (kfu) kfu[(size_t)n * M + mm] = Num<T>::st(k);
       }
       kr[i] = k;
     }
-    __syncthreads();
-    T vals[2 * DO_MAX * RR];
+    T acc[FT / 2], pm[FT / 2], pv[FT / 2];
+    for (int q = 0; q < nq; ++q) {
+      const int d = q / (ncb * nca), cbi = (q / nca) % ncb, ai = q % nca;
+      const int a0 = ai * FKA, b = cbi * FCB + col;
+      __syncthreads();   // the previous chunk is consumed (and kr is complete)
 #pragma unroll
-    for (int i = 0; i < 2 * DO_MAX * RR; ++i) vals[i] = Num<T>::zero();
-    for (int b = threadIdx.x; b < M; b += blockDim.x) {
-      for (int d = 0; d < Dout; ++d) {
-        const S* Bd = B + (size_t)d * M * M;
-        T acc[RR];
+      for (int u = 0; u < FNL; ++u) Bc[tid + u * 256] = Num<T>::ld(raw[u]);
+      __syncthreads();
+      if (q + 1 < nq) issue(q + 1, raw);
+      if (cbi == 0 && ai == 0) {
 #pragma unroll
-        for (int r = 0; r < RR; ++r) acc[r] = Num<T>::zero();
-        if (bstage) {
-          const T* Bt = Bsm + (size_t)d * M * M;
-          for (int a = 0; a < M; ++a) {
-            T bab = Bt[(size_t)a * M + b];
+        for (int r = 0; r < FT / 2; ++r) pm[r] = pv[r] = Num<T>::zero();
+      }
+      if (ai == 0) {
 #pragma unroll
-            for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
-          }
-        } else {
-          for (int a = 0; a < M; ++a) {
-            T bab = Num<T>::ld(Bd[(size_t)a * M + b]);
+        for (int r = 0; r < FT / 2; ++r) acc[r] = Num<T>::zero();
+      }
+      const int ka = min(FKA, M - a0);
+      const T* kt = kr + (rh * (FT / 2)) * M + a0;
+#pragma unroll 4
+      for (int aa = 0; aa < ka; ++aa) {
+        const T bab = Bc[aa * FCB + col];
 #pragma unroll
-            for (int r = 0; r < RR; ++r) acc[r] = fma_(bab, kr[r * M + a], acc[r]);
-          }
-        }
-        T ad = Num<T>::ld(A[(size_t)d * M + b]);
+        for (int r = 0; r < FT / 2; ++r) acc[r] = fma_(bab, kt[r * M + aa], acc[r]);
+      }
+      if (ai == nca - 1 && b < M) {
+        const T ad = Num<T>::ld(A[(size_t)d * M + b]);
 #pragma unroll
-        for (int r = 0; r < RR; ++r) {
-          int n = n0 + r;
+        for (int r = 0; r < FT / 2; ++r) {
+          const int rl = rh * (FT / 2) + r, n = n0 + rl;
           if (n < N && Bk) Bk[((size_t)n * Dout + d) * M + b] = Num<T>::st(acc[r]);
-          T kb = kr[r * M + b];
-          vals[(r * DO_MAX + d) * 2] = fma_(kb, ad, vals[(r * DO_MAX + d) * 2]);
-          vals[(r * DO_MAX + d) * 2 + 1] = fma_(kb, acc[r], vals[(r * DO_MAX + d) * 2 + 1]);
+          const T kb = kr[rl * M + b];
+          pm[r] = fma_(kb, ad, pm[r]);
+          pv[r] = fma_(kb, acc[r], pv[r]);
+        }
+      }
+      if (ai == nca - 1 && cbi == ncb - 1) {
+#pragma unroll
+        for (int r = 0; r < FT / 2; ++r) {
+          const T sm = warp_sum(pm[r]), sv = warp_sum(pv[r]);
+          if (lane == 0) {
+            red[((warp * DO_MAX + d) * (FT / 2) + r) * 2] = sm;
+            red[((warp * DO_MAX + d) * (FT / 2) + r) * 2 + 1] = sv;
+          }
         }
       }
     }
-    // CTA reduction of RR*Dout*(m, v) values
-    {
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-      const int K = 2 * DO_MAX * RR;
-      for (int i = 0; i < K; ++i) {
-        T s = warp_sum(vals[i]);
-        if (lane == 0) red[warp * 64 + i] = s;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        for (int i = 0; i < K; ++i) {
-          T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
-          s = warp_sum(s);
-          if (lane == 0) red[32 * 64 + i] = s;
+    __syncthreads();
+    for (int i = tid; i < FT * Dout; i += 256) {
+      const int rl = i / Dout, d = i - rl * Dout, n = n0 + rl;
+      const int hh = rl / (FT / 2), r = rl - hh * (FT / 2);
+      if (n < N) {
+        T mm = Num<T>::zero(), vv = Num<T>::zero();
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {   // the four warps of row half hh
+          const int ww = hh * 4 + w;
+          mm = add(mm, red[((ww * DO_MAX + d) * (FT / 2) + r) * 2]);
+          vv = add(vv, red[((ww * DO_MAX + d) * (FT / 2) + r) * 2 + 1]);
         }
+        if (m_out) m_out[(size_t)n * Dout + d] = Num<T>::st(mm);
+        if (v_out) v_out[(size_t)n * Dout + d] = Num<T>::st(add(h->sf2, vv));
       }
-      __syncthreads();
-      for (int i = threadIdx.x; i < RR * Dout; i += blockDim.x) {
-        int r = i / Dout, d = i % Dout, n = n0 + r;
-        if (n < N) {
-          T mm = red[32 * 64 + (r * DO_MAX + d) * 2];
-          T vv = add(h->sf2, red[32 * 64 + (r * DO_MAX + d) * 2 + 1]);
-          if (m_out) m_out[(size_t)n * Dout + d] = Num<T>::st(mm);
-          if (v_out) v_out[(size_t)n * Dout + d] = Num<T>::st(vv);
-        }
-      }
-      __syncthreads();
     }
   }
 }
@@ -180,6 +213,7 @@ __global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int D
   Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
   T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));  // [D]
   T* red = xs + DMAXK;                                                                // [32][64]
+  typedef typename Num<T>::store_t S;
   load_exp_table(tab);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
@@ -193,22 +227,60 @@ __global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int D
   for (int q = 0; q < 16; ++q) gl[q] = gz[q] = Num<T>::zero();
 #pragma unroll
   for (int d = 0; d < DO_MAX; ++d) ga[d] = Num<T>::zero();
+  T ab[DO_MAX];   // A[d, b], the same for every row
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d)
+    ab[d] = (!dkfu && b < M && d < Dout) ? Num<T>::ld(A[(size_t)d * M + b]) : Num<T>::zero();
+  // the next row's inputs are loaded into registers while the current row is processed
+  S pk = S(0), pg = S(0), pdm[DO_MAX], pdv[DO_MAX], pbk[DO_MAX], px[DMAXK / 32];
+  auto fetch = [&](int n) {
+    if (b < M) {
+      pk = kfu[(size_t)n * M + b];
+      if (dkfu) pg = dkfu[(size_t)n * M + b];
+    }
+#pragma unroll
+    for (int d = 0; d < DO_MAX; ++d) {
+      const bool on = !dkfu && b < M && d < Dout;
+      pdm[d] = on ? dm[(size_t)n * Dout + d] : S(0);
+      pdv[d] = on ? dv[(size_t)n * Dout + d] : S(0);
+      pbk[d] = on ? Bk[((size_t)n * Dout + d) * M + b] : S(0);
+    }
+#pragma unroll
+    for (int t = 0; t < DMAXK / 32; ++t) {
+      const int q = threadIdx.x + 32 * t;
+      px[t] = (threadIdx.x < 32 && q < D) ? x[(size_t)n * ldx + q] : S(0);
+    }
+  };
+  if (blockIdx.x < N) fetch(blockIdx.x);
   for (int n = blockIdx.x; n < N; n += gridDim.x) {
-    for (int d = threadIdx.x; d < D; d += blockDim.x) xs[d] = Num<T>::ld(x[(size_t)n * ldx + d]);
+    const T k = Num<T>::ld(pk);
+    T g = Num<T>::ld(pg);
+    T dmd[DO_MAX], dvd[DO_MAX], bk[DO_MAX];
+#pragma unroll
+    for (int d = 0; d < DO_MAX; ++d) {
+      dmd[d] = Num<T>::ld(pdm[d]);
+      dvd[d] = Num<T>::ld(pdv[d]);
+      bk[d] = Num<T>::ld(pbk[d]);
+    }
+    if (threadIdx.x < 32) {
+#pragma unroll
+      for (int t = 0; t < DMAXK / 32; ++t) {
+        const int q = threadIdx.x + 32 * t;
+        if (q < D) xs[q] = Num<T>::ld(px[t]);
+      }
+    }
     __syncthreads();
+    if (n + (int)gridDim.x < N) fetch(n + gridDim.x);
     T L = Num<T>::zero();
     if (b < M) {
-      T k = Num<T>::ld(kfu[(size_t)n * M + b]);
-      T g = Num<T>::zero();
-      if (dkfu) {
-        g = Num<T>::ld(dkfu[(size_t)n * M + b]);
-      } else {
-        for (int d = 0; d < Dout; ++d) {
-          T dmd = Num<T>::ld(dm[(size_t)n * Dout + d]);
-          T dvd = Num<T>::ld(dv[(size_t)n * Dout + d]);
-          g = fma_(dmd, Num<T>::ld(A[(size_t)d * M + b]), g);
-          g = fma_(scale2(dvd, 1), Num<T>::ld(Bk[((size_t)n * Dout + d) * M + b]), g);
-          if (d < DO_MAX) ga[d] = fma_(dmd, k, ga[d]);
+      if (!dkfu) {
+#pragma unroll
+        for (int d = 0; d < DO_MAX; ++d) {
+          if (d < Dout) {
+            g = fma_(dmd[d], ab[d], g);
+            g = fma_(scale2(dvd[d], 1), bk[d], g);
+            ga[d] = fma_(dmd[d], k, ga[d]);
+          }
         }
       }
       L = mul(g, k);
@@ -273,13 +345,16 @@ __global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int D
 }
 
 // Weighted Gram reduction:  C[d] += sum_n w[n,d] u_n v_n^T  (u, v: [N,M] rows; C: [Dout,M,M] f64)
-// 32x32 output tile per CTA, n split across gridDim.z.  (The dBhat / dSucav einsums of
+// 32x32 output tile per CTA, n split across gridDim.z.  Rows are staged GB at a time, with
+// all of a stage's global loads in flight together.  (The dBhat / dSucav einsums of
 // geepee/aep_models.py:463-464, 490-493.)
+constexpr int GB = 32;
 template <typename T>
 __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
                                                    const typename Num<T>::store_t* v,
-                                                   const typename Num<T>::store_t* w, double* C, int nchunk) {
-  __shared__ T su[32], sv[32], sw[DO_MAX];
+                                                   const typename Num<T>::store_t* w, double* C) {
+  typedef typename Num<T>::store_t S;
+  __shared__ T su[GB][32], sv[GB][32], sw[GB][DO_MAX];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of threads, 4 outputs each
   const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
   T acc[DO_MAX][4];
@@ -287,30 +362,42 @@ __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const
   for (int d = 0; d < DO_MAX; ++d)
 #pragma unroll
     for (int r = 0; r < 4; ++r) acc[d][r] = Num<T>::zero();
-  int nbeg = (int)((long)N * blockIdx.z / gridDim.z), nend = (int)((long)N * (blockIdx.z + 1) / gridDim.z);
-  for (int n = nbeg; n < nend; ++n) {
-    if (threadIdx.x < 32) {
-      int i = i0 + threadIdx.x;
-      su[threadIdx.x] = i < M ? Num<T>::ld(u[(size_t)n * M + i]) : Num<T>::zero();
-    } else if (threadIdx.x < 64) {
-      int j = j0 + threadIdx.x - 32;
-      sv[threadIdx.x - 32] = j < M ? Num<T>::ld(v[(size_t)n * M + j]) : Num<T>::zero();
-    } else if (threadIdx.x < 64 + Dout) {
-      sw[threadIdx.x - 64] = Num<T>::ld(w[(size_t)n * Dout + threadIdx.x - 64]);
+  const int nbeg = (int)((long)N * blockIdx.z / gridDim.z), nend = (int)((long)N * (blockIdx.z + 1) / gridDim.z);
+  for (int n0 = nbeg; n0 < nend; n0 += GB) {
+    // stage rows n0 .. n0+GB-1: element e = tid + 256 p of the u and v tiles (row e/32, col e%32)
+    S ru[4], rv[4], rw = S(0);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const int e = threadIdx.x + 256 * p, rl = e >> 5, c = e & 31, n = n0 + rl;
+      ru[p] = (n < nend && i0 + c < M) ? u[(size_t)n * M + i0 + c] : S(0);
+      rv[p] = (n < nend && j0 + c < M) ? v[(size_t)n * M + j0 + c] : S(0);
     }
+    {
+      const int rl = threadIdx.x / DO_MAX, d = threadIdx.x % DO_MAX, n = n0 + rl;
+      if (rl < GB && d < Dout && n < nend) rw = w[(size_t)n * Dout + d];
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const int e = threadIdx.x + 256 * p;
+      su[e >> 5][e & 31] = Num<T>::ld(ru[p]);
+      sv[e >> 5][e & 31] = Num<T>::ld(rv[p]);
+    }
+    if (threadIdx.x < GB * DO_MAX) sw[threadIdx.x / DO_MAX][threadIdx.x % DO_MAX] = Num<T>::ld(rw);
     __syncthreads();
-    T vj = sv[tx];
+    const int nr = min(GB, nend - n0);
+    for (int rl = 0; rl < nr; ++rl) {
+      const T vj = sv[rl][tx];
 #pragma unroll
-    for (int d = 0; d < DO_MAX; ++d) {
-      if (d < Dout) {
-        T wv = mul(sw[d], vj);
+      for (int d = 0; d < DO_MAX; ++d) {
+        if (d < Dout) {
+          const T wv = mul(sw[rl][d], vj);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) acc[d][r] = fma_(su[ty * 4 + r], wv, acc[d][r]);
+          for (int r = 0; r < 4; ++r) acc[d][r] = fma_(su[rl][ty * 4 + r], wv, acc[d][r]);
+        }
       }
     }
     __syncthreads();
   }
-  (void)nchunk;
 #pragma unroll
   for (int d = 0; d < DO_MAX; ++d) {
     if (d < Dout) {
@@ -323,20 +410,37 @@ __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const
   }
 }
 
-// c[d] += sum_n w[n,d] u_n   (u: [N,M]; c: [Dout,M] f64)
+// c[d] += sum_n w[n,d] u_n  (u: [N,M]; c: [Dout,M] f64).  32 columns per CTA, rows split over
+// 8 warps and gridDim.y; each thread keeps WU rows' loads in flight at a time.
+constexpr int WU = 4;
 template <typename T>
 __global__ void __launch_bounds__(256) wsum_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
                                                    const typename Num<T>::store_t* w, double* c) {
+  typedef typename Num<T>::store_t S;
   const int j = blockIdx.x * 32 + (threadIdx.x & 31);
   const int part = threadIdx.x >> 5;  // 8 n-partitions per CTA
   __shared__ T red[8][32][DO_MAX];
   T acc[DO_MAX];
 #pragma unroll
   for (int d = 0; d < DO_MAX; ++d) acc[d] = Num<T>::zero();
+  const int stride = gridDim.y * 8;
   if (j < M) {
-    for (int n = blockIdx.y * 8 + part; n < N; n += gridDim.y * 8) {
-      T uv = Num<T>::ld(u[(size_t)n * M + j]);
-      for (int d = 0; d < Dout && d < DO_MAX; ++d) acc[d] = fma_(Num<T>::ld(w[(size_t)n * Dout + d]), uv, acc[d]);
+    for (int n0 = blockIdx.y * 8 + part; n0 < N; n0 += stride * WU) {
+      S ru[WU], rw[WU][DO_MAX];
+#pragma unroll
+      for (int t = 0; t < WU; ++t) {
+        const int n = n0 + t * stride;
+        ru[t] = n < N ? u[(size_t)n * M + j] : S(0);
+#pragma unroll
+        for (int d = 0; d < DO_MAX; ++d) rw[t][d] = (n < N && d < Dout) ? w[(size_t)n * Dout + d] : S(0);
+      }
+#pragma unroll
+      for (int t = 0; t < WU; ++t) {
+        const T uv = Num<T>::ld(ru[t]);
+#pragma unroll
+        for (int d = 0; d < DO_MAX; ++d)
+          if (d < Dout) acc[d] = fma_(Num<T>::ld(rw[t][d]), uv, acc[d]);
+      }
     }
   }
 #pragma unroll
@@ -351,7 +455,9 @@ __global__ void __launch_bounds__(256) wsum_kernel(int N, int M, int Dout, const
   }
 }
 
-size_t det_fwd_smem(int M, size_t tsz) { return 256 * 8 + sizeof(Hyp<df64>) + (RR * M + 33 * 64) * tsz; }
+size_t det_fwd_smem(int M, int D, bool zstage, size_t tsz) {
+  return 256 * 8 + sizeof(Hyp<df64>) + ((size_t)FT * M + FKA * FCB + 8 * DO_MAX * FT + FT * D + (zstage ? (size_t)M * D : 0)) * tsz;
+}
 size_t det_bwd_smem(size_t tsz) { return 256 * 8 + sizeof(Hyp<df64>) + (DMAXK + 32 * 64) * tsz; }
 
 template <typename T>
@@ -386,26 +492,23 @@ extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* 
   GPK_REQUIRE(x && Z && lls2 && lsf2 && A && B, "det_fwd: null input");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  int grid = gpk::ceil_div(N, RR);
-  int cap = gpk::sm_count() * 4;
+  int grid = gpk::ceil_div(N, FT);
+  int cap = gpk::sm_count() * 2;
   if (grid > cap) grid = cap;
+  const int zstage = (size_t)M * D * sizeof(df64) <= 32 * 1024;
   if (prec == GPK_DF64) {
-    size_t sm = det_fwd_smem(M, sizeof(df64));
-    int bstage = sm + (size_t)Dout * M * M * sizeof(df64) <= 200 * 1024;
-    if (bstage) sm += (size_t)Dout * M * M * sizeof(df64);
+    size_t sm = det_fwd_smem(M, D, zstage, sizeof(df64));
     auto k = det_fwd_kernel<df64>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
                              (const double*)A, (const double*)B, (double*)kfu, (double*)Bk, (double*)m_out,
-                             (double*)v_out, bstage);
+                             (double*)v_out, zstage);
   } else if (prec == GPK_FP32) {
-    size_t sm = det_fwd_smem(M, sizeof(float));
-    int bstage = sm + (size_t)Dout * M * M * sizeof(float) <= 200 * 1024;
-    if (bstage) sm += (size_t)Dout * M * M * sizeof(float);
+    size_t sm = det_fwd_smem(M, D, zstage, sizeof(float));
     auto k = det_fwd_kernel<float>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, 256, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
-                             (const float*)B, (float*)kfu, (float*)Bk, (float*)m_out, (float*)v_out, bstage);
+                             (const float*)B, (float*)kfu, (float*)Bk, (float*)m_out, (float*)v_out, zstage);
   } else {
     return gpk::fail(GPK_EINVAL, "det_fwd: unknown precision %d", prec);
   }
@@ -423,7 +526,7 @@ extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* 
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
   int threads = M <= 128 ? 128 : 256;
-  int grid = N < gpk::sm_count() * 2 ? N : gpk::sm_count() * 2;
+  int grid = N < gpk::sm_count() ? N : gpk::sm_count();
   size_t smd = det_bwd_smem(sizeof(df64)), smf = det_bwd_smem(sizeof(float));
   if (prec == GPK_DF64) {
     det_bwd_kernel<df64><<<grid, threads, smd, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2,
@@ -453,9 +556,9 @@ extern "C" int gpk_gram(int prec, int N, int M, int Dout, const void* u, const v
   if (chunks < 1) chunks = 1;
   dim3 grid(gpk::ceil_div(M, 32), gpk::ceil_div(M, 32), chunks);
   if (prec == GPK_DF64)
-    gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C, chunks);
+    gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C);
   else if (prec == GPK_FP32)
-    gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C, chunks);
+    gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C);
   else
     return gpk::fail(GPK_EINVAL, "gram: unknown precision %d", prec);
   return gpk::check_launch("gram");
@@ -466,8 +569,8 @@ extern "C" int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const v
   GPK_REQUIRE(u && w && c, "wsum: null pointer");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  int gy = gpk::ceil_div(N, 256);
-  if (gy > 64) gy = 64;
+  int gy = gpk::ceil_div(N, 8 * WU);
+  if (gy > 128) gy = 128;
   dim3 grid(gpk::ceil_div(M, 32), gy);
   if (prec == GPK_DF64)
     wsum_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)w, c);

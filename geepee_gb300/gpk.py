@@ -7,9 +7,23 @@ inside the library, and is safe to capture in a CUDA graph.  Accumulating output
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from ._lib import call, ptr, stream, prec_of
+
+_NT, _NR = 6, 3   # GPK_LC_TERMS, GPK_LC_RANK
+
+
+class _LC(ctypes.Structure):
+    """gpk_lincomb_t (include/gpk.h)."""
+    _fields_ = [('batch', ctypes.c_int), ('rows', ctypes.c_int), ('cols', ctypes.c_int),
+                ('sum_batch', ctypes.c_int), ('nterm', ctypes.c_int), ('nrank', ctypes.c_int),
+                ('X', ctypes.c_void_p * _NT), ('sX', ctypes.c_long * _NT), ('cX', ctypes.c_double * _NT),
+                ('tX', ctypes.c_int * _NT),
+                ('u', ctypes.c_void_p * _NR), ('su', ctypes.c_long * _NR), ('v', ctypes.c_void_p * _NR),
+                ('sv', ctypes.c_long * _NR), ('cr', ctypes.c_double * _NR), ('out', ctypes.c_void_p)]
 
 
 def _f64(shape, like):
@@ -75,8 +89,9 @@ def wsum(u, w, c):
     call('gpk_wsum', prec_of(u.dtype), N, M, w.shape[1], ptr(u), ptr(w), ptr(c), stream())
 
 
-def gemm(A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False):
-    """C = alpha op(A) op(B) + beta C for 2-D or batched 3-D operands (batch 1 broadcasts)."""
+def gemm(A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False, E=None):
+    """C = alpha op(A) op(B) + beta E for 2-D or batched 3-D operands (batch 1 broadcasts);
+    E defaults to C itself (the BLAS beta C)."""
     a3 = A if A.dim() == 3 else A.unsqueeze(0)
     b3 = B if B.dim() == 3 else B.unsqueeze(0)
     batch = max(a3.shape[0], b3.shape[0])
@@ -89,29 +104,38 @@ def gemm(A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False):
     out3 = A.dim() == 3 or B.dim() == 3
     if C is None:
         C = torch.empty((batch, m, n) if out3 else (m, n), dtype=A.dtype, device=A.device)
-        beta = 0.0
+        if E is None:
+            beta = 0.0
     sA = 0 if a3.shape[0] == 1 else a3.shape[1] * a3.shape[2]
     sB = 0 if b3.shape[0] == 1 else b3.shape[1] * b3.shape[2]
-    call('gpk_gemm', prec_of(A.dtype), batch, m, n, k, int(tA), int(tB), float(alpha),
-         ptr(a3), a3.shape[2], sA, ptr(b3), b3.shape[2], sB, float(beta), ptr(C), n, m * n, stream())
+    if E is None:
+        call('gpk_gemm', prec_of(A.dtype), batch, m, n, k, int(tA), int(tB), float(alpha),
+             ptr(a3), a3.shape[2], sA, ptr(b3), b3.shape[2], sB, float(beta), ptr(C), n, m * n, stream())
+    else:
+        sE = 0 if E.dim() == 2 or E.shape[0] == 1 else m * n
+        call('gpk_gemm_ex', prec_of(A.dtype), batch, m, n, k, int(tA), int(tB), float(alpha),
+             ptr(a3), a3.shape[2], sA, ptr(b3), b3.shape[2], sB, float(beta), ptr(E), n, sE, ptr(C), n, m * n,
+             stream())
     return C
 
 
 def chol_inv(A, Ainv=None, L=None, logdet=None, info=None, work=None):
-    """Batched SPD inverse / Cholesky / log-determinant of A [..., M, M].  M > 128 runs in a
-    device workspace (allocated here when not given).  When only the inverse (and logdet) is
-    wanted, the factorisation returns L^-1 and the inverse is formed as L^-T L^-1 by the GEMM."""
+    """Batched SPD inverse / Cholesky / log-determinant of A [..., M, M].  When only the inverse
+    (and logdet) is wanted this is gpk_spd_inv (factor, column-parallel L^-1, GEMM); with L
+    requested everything comes from one factorisation kernel (gpk_chol_inv_ws).  Device
+    workspaces are allocated here when not given."""
     M = A.shape[-1]
     batch = A.numel() // (M * M)
+    if Ainv is not None and L is None:
+        if work is None:
+            work = torch.empty((2 * batch, M, M), dtype=A.dtype, device=A.device)
+        if info is None:
+            info = torch.empty(batch, dtype=torch.int32, device=A.device)
+        call('gpk_spd_inv', prec_of(A.dtype), batch, M, ptr(A), ptr(Ainv), ptr(logdet), ptr(info), ptr(work),
+             stream())
+        return
     if M > 128 and work is None:
         work = torch.empty_like(A)
-    if Ainv is not None and L is None:
-        X = torch.empty_like(A)
-        call('gpk_chol_linv', prec_of(A.dtype), batch, M, ptr(A), ptr(X), ptr(logdet), ptr(info), ptr(work),
-             stream())
-        X3 = X.reshape(batch, M, M)
-        gemm(X3, X3, Ainv.view(batch, M, M), tA=True)
-        return
     call('gpk_chol_inv_ws', prec_of(A.dtype), batch, M, ptr(A), ptr(Ainv), ptr(L), ptr(logdet), ptr(info),
          ptr(work), stream())
 
@@ -127,3 +151,69 @@ def small_spd(A, Ainv=None, logdet=None, info=None):
     n = A.shape[-1]
     call('gpk_small_spd', prec_of(A.dtype), A.numel() // (n * n), n, ptr(A), ptr(Ainv), ptr(logdet),
          ptr(info), stream())
+
+
+def lincomb(out, terms=(), ranks=(), sum_batch=False, batch=None):
+    """Fused float64 linear combination (gpk_lincomb):
+        out[b] = sum_t c_t X_t[b] (X_t^T when transposed) + sum_r c_r u_r[b] v_r[b]^T
+    terms: (c, X) or (c, X, transpose) with X [B, rows, cols] or [rows, cols] (broadcast);
+    ranks: (c, u, v) with u [B, rows] / [rows], v [B, cols] / [cols];
+    out: [B, rows, cols], or [rows, cols] for B = 1 or when sum_batch sums over b."""
+    rows, cols = out.shape[-2], out.shape[-1]
+    if batch is None:
+        batch = 1
+        for t in terms:
+            if t[1].dim() == 3:
+                batch = max(batch, t[1].shape[0])
+        for _, u, v in ranks:
+            for w in (u, v):
+                if w.dim() == 2:
+                    batch = max(batch, w.shape[0])
+    d = _LC()
+    d.batch, d.rows, d.cols, d.sum_batch = batch, rows, cols, int(bool(sum_batch))
+    d.nterm, d.nrank = len(terms), len(ranks)
+    if d.nterm > _NT or d.nrank > _NR:
+        raise ValueError('lincomb: too many terms')
+    keep = [out]
+    for i, t in enumerate(terms):
+        c, X = t[0], t[1]
+        tr = len(t) > 2 and t[2]
+        X = X.contiguous()
+        keep.append(X)
+        d.X[i], d.cX[i], d.tX[i] = ptr(X), float(c), int(bool(tr))
+        d.sX[i] = rows * cols if (X.dim() == 3 and X.shape[0] > 1) else 0
+    for i, (c, u, v) in enumerate(ranks):
+        u, v = u.contiguous(), v.contiguous()
+        keep += [u, v]
+        d.u[i], d.v[i], d.cr[i] = ptr(u), ptr(v), float(c)
+        d.su[i] = rows if (u.dim() == 2 and u.shape[0] > 1) else 0
+        d.sv[i] = cols if (v.dim() == 2 and v.shape[0] > 1) else 0
+    d.out = ptr(out)
+    call('gpk_lincomb', ctypes.addressof(d), stream())
+    return out
+
+
+def nat_prep(eta1, ls, sf, R, lls2, lsf2):
+    D, M = R.shape[0], R.shape[1]
+    call('gpk_nat_prep', D, M, ls.numel(), ptr(eta1), ptr(ls), ptr(sf), ptr(R), ptr(lls2), ptr(lsf2), stream())
+
+
+def triu_pack(dR, R, out, accumulate=False):
+    D, M = dR.shape[0], dR.shape[1]
+    call('gpk_triu_pack', D, M, ptr(dR), ptr(R), ptr(out), int(bool(accumulate)), stream())
+
+
+def hyp_grads(ls, sf, dl, dsf2, dv, g_ls, g_sf):
+    call('gpk_hyp_grads', ls.numel(), ptr(ls), ptr(sf), ptr(dl), ptr(dsf2), ptr(dv), dv.numel(), ptr(g_ls),
+         ptr(g_sf), stream())
+
+
+def aep_phi(D, M, N, alpha, logdetK, ldSuinv, ldShinv, mu, mh, th2, w, out):
+    call('gpk_aep_phi', D, M, float(N), float(alpha), ptr(logdetK), ptr(ldSuinv), ptr(ldShinv), ptr(mu), ptr(mh),
+         ptr(th2), float(w), ptr(out), stream())
+
+
+def gauss_lik(m, v, y, sn, alpha, scale, invN, dm, dv, energy, g_sn):
+    n, D = y.shape
+    call('gpk_gauss_lik', n, D, ptr(m), ptr(v), ptr(y), ptr(sn), float(alpha), float(scale), float(invN), ptr(dm),
+         ptr(dv), ptr(energy), ptr(g_sn), stream())

@@ -2,9 +2,11 @@
 
 State lives in float64 CUDA tensors; every matrix product goes through libgpk's
 double-float GEMM, factorisations through its batched SPD Cholesky/inverse, and the
-data-sized work through the fused kernel-matrix / psi-statistics kernels.  Small
-elementwise glue uses torch float64 ops.  Nothing here synchronises with the host,
-so a whole objective+gradient evaluation can be captured in one CUDA graph.
+data-sized work through the fused kernel-matrix / psi-statistics kernels, and the
+elementwise glue of the natural-parameter algebra (sums with broadcast, transposes,
+rank-one terms, the eta1_R packing) through libgpk's fused float64 kernels, so one
+evaluation is a few dozen launches.  Nothing here synchronises with the host, so a whole
+objective+gradient evaluation can be captured in one CUDA graph.
 """
 from __future__ import annotations
 
@@ -18,8 +20,8 @@ from .config import JITTER
 F64 = torch.float64
 
 
-def mm(A, B, tA=False, tB=False, alpha=1.0, C=None, beta=0.0):
-    return gpk.gemm(A.contiguous(), B.contiguous(), C, alpha=alpha, beta=beta, tA=tA, tB=tB)
+def mm(A, B, tA=False, tB=False, alpha=1.0, C=None, beta=0.0, E=None):
+    return gpk.gemm(A.contiguous(), B.contiguous(), C, alpha=alpha, beta=beta, tA=tA, tB=tB, E=E)
 
 
 def mv(A, v):
@@ -63,47 +65,63 @@ class DevLayer:
         self.pk_diag = (iu[0] == iu[1]).to(self.dev)
         # Cholesky status words: [Kuu, Su^-1 (Dout), Suhat^-1 (Dout)]
         self.info = torch.zeros(1 + 2 * Dout, dtype=torch.int32, device=self.dev)
+        # fixed-address buffers (CUDA-graph friendly): R, log hyperparameters, and the
+        # accumulators the data kernels add into (zeroed by one fill per evaluation)
+        self.R_buf = torch.zeros((Dout, M, M), dtype=F64, device=self.dev)
+        self.lls2 = torch.zeros(Din, dtype=F64, device=self.dev)
+        self.lsf2 = torch.zeros(1, dtype=F64, device=self.dev)
+        sizes = [1, Din, Dout * M, Dout * M * M]
+        self._acc = torch.zeros(sum(sizes), dtype=F64, device=self.dev)
+        o = 0
+        views = []
+        for n in sizes:
+            views.append(self._acc[o:o + n])
+            o += n
+        self._dsf2, self._dl = views[0], views[1]
+        self._dAh, self._dBh = views[2].view(Dout, M), views[3].view(Dout, M, M)
 
     # ---------------------------------------------------------------- parameters
     def param_tensors(self):
         return {'ls': self.ls, 'sf': self.sf, 'zu': self.zu, 'eta1_R': self.eta1, 'eta2': self.eta2}
 
     # ---------------------------------------------------------------- q(u) and Kuu
-    def prep_kuu(self):
-        """eta -> (R, theta_1, theta_2) and the jittered Kuu (base_models.py:630-658,454-463)."""
-        M, D = self.M, self.Dout
-        self.lls2 = 2.0 * self.ls
-        self.lsf2 = 2.0 * self.sf
-        R = torch.zeros((D, M * M), dtype=F64, device=self.dev)
-        R[:, self.iu_flat] = self.eta1
-        R[:, self.diag_flat] = torch.exp(R[:, self.diag_flat])
-        self.R = R.view(D, M, M)
+    def prep_kuu(self, out=None):
+        """eta -> (R, theta_1, theta_2) and the jittered Kuu (base_models.py:630-658,454-463);
+        Kuu is written into `out` when given."""
+        gpk.nat_prep(self.eta1, self.ls, self.sf, self.R_buf, self.lls2, self.lsf2)
+        self.R = self.R_buf
         self.th1 = mm(self.R, self.R, tA=True)
         self.th2 = self.eta2
-        self.Kuu = gpk.kern(self.zu, self.zu, self.lls2, self.lsf2, jitter=JITTER)
+        self.Kuu = gpk.kern(self.zu, self.zu, self.lls2, self.lsf2, jitter=JITTER, out=out)
         return self.Kuu
 
     def set_kuu_factors(self, Kinv, logdetK):
         self.Kinv, self.logdetK = Kinv, logdetK
 
-    def prep_s(self, alpha):
+    def prep_s(self, alpha, out=None):
         """The SPD matrices whose inverses the posterior and the cavity need:
-        Su^-1 = Kuu^-1 + theta_1 and Suhat^-1 = Kuu^-1 + beta theta_1 (natural parameters)."""
+        Su^-1 = Kuu^-1 + theta_1 and Suhat^-1 = Kuu^-1 + beta theta_1 (natural parameters),
+        stacked [2 Dout, M, M] (into `out` when given)."""
         beta = (self.N - alpha) / self.N
         self.beta = beta
-        K = self.Kinv.unsqueeze(0)
-        self.Suinv = K + self.th1
-        self.Shinv = K + beta * self.th1
-        return torch.cat([self.Suinv, self.Shinv], 0)
+        D, M = self.Dout, self.M
+        if out is None:
+            out = torch.empty((2 * D, M, M), dtype=F64, device=self.dev)
+        gpk.lincomb(out[:D], [(1.0, self.Kinv), (1.0, self.th1)])
+        gpk.lincomb(out[D:], [(1.0, self.Kinv), (beta, self.th1)])
+        self.Suinv, self.Shinv = out[:D], out[D:]
+        return out
 
     def set_s_factors(self, inv, logdet):
         D = self.Dout
         self.Su, self.Sh = inv[:D], inv[D:]
-        self.logdetSu = -logdet[:D]
+        self.ldSuinv = logdet[:D]
         self.ldShinv = logdet[D:]
-        self.mu = mv(self.Su, self.th2)
-        self.Spmm = self.Su + outer(self.mu, self.mu)
-        self.mh = mv(self.Sh, self.beta * self.th2)
+        self.logdetSu = None   # -ldSuinv, formed only where a non-fused path needs it
+        th2 = self.th2.unsqueeze(-1)
+        self.mu = mm(self.Su, th2).squeeze(-1)
+        self.mh = mm(self.Sh, th2, alpha=self.beta).squeeze(-1)
+        self.Spmm = gpk.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
         self._cavity_tail()
 
     def setup_posterior(self):
@@ -150,11 +168,11 @@ class DevLayer:
         (aep_models.py:536-546); Bhat_sto is formed as Bhat_det + Ahat Ahat^T, the same matrix
         with two fewer M^3 products."""
         K = self.Kinv
-        self.Smm_h = self.Sh + outer(self.mh, self.mh)
-        self.Ah = mv(K, self.mh)
+        self.Smm_h = gpk.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
+        self.Ah = mm(K, self.mh.unsqueeze(-1)).squeeze(-1)
         KS2 = mm(K, self.Sh)
-        self.Bh_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
-        self.Bh_sto = self.Bh_det + outer(self.Ah, self.Ah)
+        self.Bh_det = mm(KS2, K, beta=-1.0, E=K)
+        self.Bh_sto = gpk.lincomb(torch.empty_like(self.Bh_det), [(1.0, self.Bh_det)], [(1.0, self.Ah, self.Ah)])
 
     def setup_predict(self):
         """Posterior A, B_det, B_sto used by predict (base_models.py:480-488);
@@ -162,17 +180,24 @@ class DevLayer:
         K = self.Kinv
         self.A = mv(K, self.mu)
         KS2 = mm(K, self.Su)
-        self.B_det = mm(KS2, K, C=-K.unsqueeze(0).expand_as(KS2).contiguous(), beta=1.0)
+        self.B_det = mm(KS2, K, beta=-1.0, E=K)
         self.B_sto = self.B_det + outer(self.A, self.A)
 
     # ---------------------------------------------------------------- log-partitions
-    def phi(self, alpha):
-        """compute_phi (aep_models.py:62-114): prior + (N/a - 1) posterior - (N/a) cavity."""
+    def phi(self, alpha, out=None, w=1.0):
+        """compute_phi (aep_models.py:62-114): prior + (N/a - 1) posterior - (N/a) cavity.
+        Natural-parameter layers with `out` given: out += w * phi in one fused kernel
+        (mu.Su^-1 mu = mu.theta_2 there); otherwise returns phi as a device scalar."""
         N = self.N
+        if self.nat and out is not None:
+            gpk.aep_phi(self.Dout, self.M, N, alpha, self.logdetK, self.ldSuinv, self.ldShinv, self.mu, self.mh,
+                        self.th2, w, out)
+            return None
+        lsu = self.logdetSu if self.logdetSu is not None else -self.ldSuinv
         phi_prior = self.Dout * 0.5 * self.logdetK
         q_post = (self.mu * mv(self.Suinv, self.mu)).sum()
         q_cav = (self.mh * mv(self.Shinv, self.mh)).sum()
-        phi_post = 0.5 * self.logdetSu.sum() + 0.5 * q_post
+        phi_post = 0.5 * lsu.sum() + 0.5 * q_post
         phi_cav = -0.5 * self.ldShinv.sum() + 0.5 * q_cav
         return phi_prior + (N / alpha - 1.0) * phi_post - (N / alpha) * phi_cav
 
@@ -196,23 +221,25 @@ class DevLayer:
         return m, v
 
     # ---------------------------------------------------------------- backward pieces
-    def _pack_eta1(self, dth1):
-        """d theta_1 -> d eta1_R (aep_models.py:274-287)."""
-        dR = mm(self.R, dth1 + dth1.transpose(1, 2))
-        flat = dR.reshape(self.Dout, -1)
-        out = flat[:, self.iu_flat]
-        rd = self.R.reshape(self.Dout, -1)[:, self.iu_flat]
-        return torch.where(self.pk_diag, out * rd, out)
+    def _pack_eta1(self, dth1, out=None, accumulate=False):
+        """d theta_1 -> d eta1_R (aep_models.py:274-287): dR = R (dth1 + dth1^T), then the
+        upper-triangle entries, the diagonal ones times R_aa (exp parameterisation).  Written
+        into `out` (e.g. the gradient slot) when given."""
+        D, M = self.Dout, self.M
+        sym = gpk.lincomb(torch.empty_like(dth1), [(1.0, dth1), (1.0, dth1, True)])
+        dR = mm(self.R, sym)
+        if out is None:
+            out = torch.empty((D, M * (M + 1) // 2), dtype=F64, device=self.dev)
+        gpk.triu_pack(dR, self.R, out, accumulate)
+        return out
 
     def _finish_hyp(self, Minner):
         gpk.trace_kzz(Minner.contiguous(), self.zu, self.lls2, self.lsf2, self.g['sf'], self.g['ls'],
                       self.g['zu'], s_sf=2.0, s_ls=2.0)
 
-    def _kernel_grads(self, dsf2, dl, dv_sum):
-        ell = torch.exp(self.ls)
-        sf2 = torch.exp(2.0 * self.sf)
-        self.g['ls'].copy_(dl * ell)
-        self.g['sf'].copy_(2.0 * sf2 * (dsf2 + dv_sum))
+    def _kernel_grads(self, dsf2, dl, dv):
+        """g_ls = dl * ell, g_sf = 2 sf2 (dsf2 + sum dv) (aep_models.py:226-231, 445-450)."""
+        gpk.hyp_grads(self.ls, self.sf, dl, dsf2, dv, self.g['ls'], self.g['sf'])
 
     def bwd_mm(self, alpha, m, dm, dv, mx, vx):
         """backprop_grads_lvm_mm (aep_models.py:201-304); returns (dmx, dvx)."""
@@ -223,41 +250,46 @@ class DevLayer:
     def bwd_mm_data(self, alpha, m, dm, dv, mx, vx):
         """The data-sized part of the backward: psi-statistic gradients (recomputing psi2),
         dAhat, dBhat and the gradient w.r.t. the input moments (dmx, dvx)."""
-        M, D, Q = self.M, self.Dout, self.Din
-        z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
-        dsf2, dl, dZ, self._dAh, self._dBh = z(1), z(Q), self.g['zu'], z(D, M), z(D, M, M)
+        Q = self.Din
+        self._acc.zero_()
+        dZ = self.g['zu']
         dZ.zero_()
         n = mx.shape[0]
         dmx = torch.empty((n, Q), dtype=F64, device=self.dev)
         dvx = torch.empty_like(dmx)
-        gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, dsf2, dl, dZ,
-                    self._dAh, self._dBh, dmx, dvx)
-        self._kernel_grads(dsf2, dl, dv.sum())
+        gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, self._dsf2, self._dl,
+                    dZ, self._dAh, self._dBh, dmx, dvx)
+        self._kernel_grads(self._dsf2, self._dl, dv)
         return dmx, dvx
 
     def bwd_mm_algebra(self, alpha):
-        """The M x M part of backprop_grads_lvm_mm: cavity, natural-parameter and Kuu gradients."""
+        """The M x M part of backprop_grads_lvm_mm (aep_models.py:250-304): cavity,
+        natural-parameter and Kuu gradients."""
         N, M, D = self.N, self.M, self.Dout
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
         dAh, dBh = self._dAh, self._dBh
         K = self.Kinv
         dvcav = mm(mm(K, dBh), K)
-        dmcav = 2.0 * mv(dvcav, self.mh) + mm(dAh, K, tB=True)
-        dvcav = dvcav + beta * outer(dmcav, self.th2)
-        dvcavinv = -mm(mm(self.Sh, dvcav), self.Sh)
-        dth1 = beta * dvcavinv
-        dth2 = beta * mv(self.Sh, dmcav)
+        t = mm(dvcav, self.mh.unsqueeze(-1), alpha=2.0).squeeze(-1)
+        dmcav = mm(dAh, K, tB=True, beta=1.0, E=t)                       # 2 dvcav mh + dAh K^T
+        gpk.lincomb(dvcav, [(1.0, dvcav)], [(beta, dmcav, self.th2)])    # + beta dmcav th2^T
+        dvcavinv = mm(mm(self.Sh, dvcav), self.Sh, alpha=-1.0)
+        dth2 = mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta).squeeze(-1)
         KS = mm(K, self.Smm_h)
-        dK = (dvcavinv.sum(0) + mm(dAh, self.mh, tA=True)
-              + 2.0 * mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True) - dBh.sum(0))
-        Minner = s_post * self.Spmm.sum(0) + s_cav * self.Smm_h.sum(0) - 2.0 * dK
-        dth1 = -0.5 * s_post * self.Spmm - 0.5 * s_cav * beta * self.Smm_h + dth1
-        dth2 = s_post * self.mu + s_cav * beta * self.mh + dth2
-        Mall = 0.5 * (D * K + mm(mm(K, Minner), K))
+        T1 = mm(dAh, self.mh, tA=True)
+        T2 = mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
+        # dK = sum_d dvcavinv + dAh^T mh + 2 sum_d KS^T dBh - sum_d dBh;
+        # Minner = s_post sum Spmm + s_cav sum Smm_h - 2 dK
+        Minner = gpk.lincomb(torch.empty_like(K), [(s_post, self.Spmm), (s_cav, self.Smm_h), (-2.0, dvcavinv),
+                                                   (2.0, dBh), (-2.0, T2)], sum_batch=True, batch=D)
+        dth1 = gpk.lincomb(torch.empty_like(dvcavinv), [(-0.5 * s_post, self.Spmm), (-0.5 * s_cav * beta, self.Smm_h),
+                                                        (beta, dvcavinv)])
+        # Mall = 1/2 (D K + K Minner K)
+        Mall = mm(mm(K, Minner), K, alpha=0.5, beta=0.5 * D, E=K)
         self._finish_hyp(Mall)
-        self.g['eta1_R'].copy_(self._pack_eta1(dth1))
-        self.g['eta2'].copy_(dth2)
+        self._pack_eta1(dth1, out=self.g['eta1_R'])
+        gpk.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2)])
 
     def _cav_grad_u(self, dmu, dSu):
         """compute_cav_grad_u (aep_models.py:548-586)."""
@@ -284,6 +316,8 @@ class DevLayer:
 
     def bwd_det(self, alpha, dm, dv, kfu, Bk, x):
         """backprop_grads_reg (aep_models.py:412-511)."""
+        if self.nat:
+            return self._bwd_det_nat(alpha, dm, dv, kfu, Bk, x)
         N, M, D, Q = self.N, self.M, self.Dout, self.Din
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
@@ -292,12 +326,13 @@ class DevLayer:
         dZ = self.g['zu']
         dZ.zero_()
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh)
-        self._kernel_grads(dsf2, dl, dv.sum())
-        kK = mm(kfu, K)
-        dmucav = z(D, M)
-        gpk.wsum(kK, dm, dmucav)
-        dSucav = z(D, M, M)
-        gpk.gram(kK, kK, dv, dSucav)
+        self._kernel_grads(dsf2, dl, dv)
+        # sum_n dm_nd (kfu_n K^-1) = dAhat_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T =
+        # K^-1 dBhat_d K^-1: the M x M forms of the reference's kfu Kuuinv contractions
+        dBh = z(D, M, M)
+        gpk.gram(kfu, kfu, dv, dBh)
+        dmucav = mm(dAh, K)
+        dSucav = mm(mm(K, dBh), K)
         Sinv_mh = mv(self.Shinv, self.mh)
         dmucav = dmucav + s_cav * Sinv_mh
         dSucav = dSucav + s_cav * (0.5 * self.Shinv - 0.5 * outer(Sinv_mh, Sinv_mh))
@@ -306,8 +341,6 @@ class DevLayer:
         dmu = s_post * Sinv_mu
         dSu = s_post * (0.5 * self.Suinv - 0.5 * outer(Sinv_mu, Sinv_mu))
         e1p, e2p, dKp = self._post_grad_u(dmu, dSu)
-        dBh = z(D, M, M)
-        gpk.gram(kfu, kfu, dv, dBh)
         KS = mm(K, self.Sh)
         dK = (mm(dAh, self.mh, tA=True) + 2.0 * mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True)
               - dBh.sum(0) + dKc + dKp - 0.5 * D * self.Kuu)
@@ -315,6 +348,49 @@ class DevLayer:
         self._finish_hyp(Minner)
         self.g['eta1_R'].copy_(e1c + e1p)
         self.g['eta2'].copy_(e2c + e2p)
+
+    def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x):
+        """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
+        compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so
+        that the eta1_R terms of the cavity and the posterior are packed once."""
+        N, M, D = self.N, self.M, self.Dout
+        s_post, s_cav = N / alpha - 1.0, -N / alpha
+        beta = self.beta
+        K = self.Kinv
+        self._acc.zero_()
+        dZ = self.g['zu']
+        dZ.zero_()
+        dAh, dBh = self._dAh, self._dBh
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh)
+        self._kernel_grads(self._dsf2, self._dl, dv)
+        gpk.gram(kfu, kfu, dv, dBh)
+        # cavity: dmucav = dAhat K^-1 + s_cav Suhat^-1 muhat (sum_n dm (kfu K^-1) = dAhat K^-1);
+        # dSucav = K^-1 dBhat K^-1 + s_cav (Suhat^-1/2 - s s^T/2), plus the mean's beta dmucav th2^T
+        Sinv_mh = mm(self.Shinv, self.mh.unsqueeze(-1)).squeeze(-1)
+        dmucav = mm(dAh, K, beta=s_cav, E=Sinv_mh)
+        X = mm(mm(K, dBh), K)
+        gpk.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
+                    [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
+        dSinv_c = mm(mm(self.Sh, X), self.Sh, alpha=-1.0)
+        # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
+        Sinv_mu = mm(self.Suinv, self.mu.unsqueeze(-1)).squeeze(-1)
+        Y = gpk.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
+                        [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
+        dSinv_p = mm(mm(self.Su, Y), self.Su, alpha=-1.0)
+        # d eta1_R = pack(beta dSinv_c + dSinv_p); d eta2 = beta Suhat dmucav + Su dmu
+        dth1 = gpk.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (1.0, dSinv_p)])
+        self._pack_eta1(dth1, out=self.g['eta1_R'])
+        e2p = mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
+        mm(self.Sh, dmucav.unsqueeze(-1), alpha=beta, beta=1.0, E=e2p, C=self.g['eta2'].view(D, M, 1))
+        # Kuu^-1 gradient: dAhat^T muhat + 2 sum_d (K^-1 Suhat)^T dBhat - sum_d dBhat
+        #                  + sum_d dSinv_c + sum_d dSinv_p - D/2 Kuu
+        KS = mm(K, self.Sh)
+        T1 = mm(dAh, self.mh, tA=True)
+        T2 = mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
+        dK = gpk.lincomb(torch.empty_like(K), [(1.0, T2), (-1.0, dBh), (1.0, dSinv_c), (1.0, dSinv_p),
+                                               (-0.5 * D, self.Kuu)], sum_batch=True, batch=D)
+        Minner = mm(mm(K, dK), K, alpha=-1.0)
+        self._finish_hyp(Minner)
 
 
 def gauss_logZ(m, v, y, sn, alpha):
@@ -336,34 +412,44 @@ def gauss_dsn(dv, nb, D, sn, alpha, scale):
 
 
 def setup_layers(layers, alpha):
-    """Posterior + cavity of several layers with batched factorisations: one SPD launch for
+    """Posterior + cavity of several layers with batched factorisations: one SPD inverse for
     every layer's Kuu (grouped by M), then one for every Su^-1 and Suhat^-1 (natural-parameter
-    layers; others fall back to the per-layer path)."""
+    layers; others take the per-layer path).  Returns the int32 Cholesky status words of the
+    factorisations (0 = fine), for one reduction at the end of the evaluation."""
     nat = [l for l in layers if l.nat]
+    statuses = []
     for l in layers:
         if not l.nat:
             l.setup_posterior()
             l.setup_cavity(alpha)
+            statuses.append(l.info)
     by_m = {}
     for l in nat:
         by_m.setdefault(l.M, []).append(l)
     for M, group in by_m.items():
-        K = torch.stack([l.prep_kuu() for l in group])
+        G = len(group)
+        dev = group[0].dev
+        nS = sum(2 * l.Dout for l in group)
+        info = torch.empty(G + nS, dtype=torch.int32, device=dev)
+        K = torch.empty((G, M, M), dtype=F64, device=dev)
+        for i, l in enumerate(group):
+            l.prep_kuu(out=K[i])
         Kinv = torch.empty_like(K)
-        ld = torch.empty(len(group), dtype=F64, device=K.device)
-        info = torch.zeros(len(group), dtype=torch.int32, device=K.device)
-        gpk.chol_inv(K, Kinv, None, ld, info)
+        ld = torch.empty(G, dtype=F64, device=dev)
+        gpk.chol_inv(K, Kinv, None, ld, info[:G])
+        S = torch.empty((nS, M, M), dtype=F64, device=dev)
+        o = 0
         for i, l in enumerate(group):
             l.set_kuu_factors(Kinv[i], ld[i:i + 1])
-            l.info[0:1].copy_(info[i:i + 1])
-        S = torch.cat([l.prep_s(alpha) for l in group], 0)
+            l.prep_s(alpha, out=S[o:o + 2 * l.Dout])
+            o += 2 * l.Dout
         Sinv = torch.empty_like(S)
-        lds = torch.empty(S.shape[0], dtype=F64, device=S.device)
-        infos = torch.zeros(S.shape[0], dtype=torch.int32, device=S.device)
-        gpk.chol_inv(S, Sinv, None, lds, infos)
+        lds = torch.empty(nS, dtype=F64, device=dev)
+        gpk.chol_inv(S, Sinv, None, lds, info[G:])
         o = 0
         for l in group:
             n = 2 * l.Dout
-            l.info[1:1 + n].copy_(infos[o:o + n])
             l.set_s_factors(Sinv[o:o + n], lds[o:o + n])
             o += n
+        statuses.append(info)
+    return statuses

@@ -124,10 +124,18 @@ int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const void* w, dou
 /* Batched GEMM  C[b] = alpha op(A[b]) op(B[b]) + beta C[b]  (row-major; op = transpose when
  * transA/transB != 0; batch strides in elements, 0 broadcasts).  In the df64 precision the
  * products of the M x M AEP algebra (np.einsum chains such as 'ab,dbc,ce->dae',
- * geepee/aep_models.py:252,258, base_models.py:480-488) run on the FP32 pipes. */
+ * geepee/aep_models.py:252,258, base_models.py:480-488) run on the FP32 pipes.  With k == 0,
+ * C = beta C and A, B may be null. */
 int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
              const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
              void* C, int ldc, long strideC, void* stream);
+
+/* gpk_gemm with a separate addend:  C[b] = alpha op(A[b]) op(B[b]) + beta E[b]  (E may alias C;
+ * strideE = 0 broadcasts one E to every batch entry).  Folds the "- Kuuinv" / "+ scale * X"
+ * terms of the AEP algebra (geepee/aep_models.py:536-546) into the product's epilogue. */
+int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
+                const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
+                const void* E, int lde, long strideE, void* C, int ldc, long strideC, void* stream);
 
 /* Batched SPD factorisation of A[b] (M x M, M <= 128): writes (each optional) the inverse
  * Ainv, the lower Cholesky factor L, logdet = log det A, and info[b] = 0 or the 1-based
@@ -143,11 +151,76 @@ int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L,
 int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
                     void* work, void* stream);
 
-/* The inverse Cholesky factor: Linv[b] = L[b]^-1 (lower triangular, zeros above the diagonal),
- * logdet and info as in gpk_chol_inv.  A^-1 = Linv^T Linv is then one batched gpk_gemm, which
- * spreads that third of the work over many CTAs.  `work` as in gpk_chol_inv_ws (M > 128). */
-int gpk_chol_linv(int prec, int batch, int M, const void* A, void* Linv, double* logdet, int* info, void* work,
-                  void* stream);
+/* SPD inverse and log-determinant, the fast path for the AEP algebra: Ainv[b] = A[b]^-1,
+ * logdet and info as in gpk_chol_inv (info is required).  For M <= 128 three launches: a
+ * one-CTA register-tiled Cholesky writes L into `work`, a many-CTA column-parallel forward
+ * substitution writes L^-1 after it, and the GEMM forms L^-T L^-1; for larger M the
+ * factorisation runs in `work`.  `work`: 2*batch*M*M elements of the buffer precision.
+ * Replaces np.linalg.inv + slogdet of Kuu, Su^-1, Suhat^-1 (geepee/base_models.py:464, 471,
+ * aep_models.py:68,78,91,525). */
+int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info, void* work,
+                void* stream);
+
+/* ---- fused float64 pieces of the M x M AEP algebra (no counterpart kernels in the reference:
+ * each replaces a chain of numpy expressions; the arithmetic stays float64) ---- */
+
+#define GPK_LC_TERMS 6
+#define GPK_LC_RANK 3
+
+/* out[b,i,j] = sum_t cX[t] X[t][b*sX[t] + (tX[t] ? j*cols+i : i*cols+j)]
+ *            + sum_r cr[r] u[r][b*su[r] + i] v[r][b*sv[r] + j]
+ * for b < batch, i < rows, j < cols (row-major).  A stride of 0 broadcasts a term over the
+ * batch; tX transposes a (square) term.  With sum_batch != 0 the result is summed over b into
+ * one rows x cols output (broadcast terms then enter once).  `out` may alias a term only
+ * elementwise (same index, no transpose, no batch sum).  E.g. Su^-1 = Kuu^-1 + theta_1,
+ * Bhat_sto = Bhat_det + Ahat Ahat^T, sum_d(...) of geepee/aep_models.py:226-304, 536-546. */
+typedef struct {
+  int batch, rows, cols, sum_batch;
+  int nterm, nrank;
+  const double* X[GPK_LC_TERMS];
+  long sX[GPK_LC_TERMS];
+  double cX[GPK_LC_TERMS];
+  int tX[GPK_LC_TERMS];
+  const double* u[GPK_LC_RANK];
+  long su[GPK_LC_RANK];
+  const double* v[GPK_LC_RANK];
+  long sv[GPK_LC_RANK];
+  double cr[GPK_LC_RANK];
+  double* out;
+} gpk_lincomb_t;
+int gpk_lincomb(const gpk_lincomb_t* desc, void* stream);
+
+/* q(u) unpacking for a natural-parameter layer: R[d] = upper triangle of the packed
+ * eta1_R[d] (row-major np.triu_indices order) with exp() on the diagonal, zeros below;
+ * lls2 = 2 ls, lsf2 = 2 sf.  (geepee/base_models.py:630-658 update_hypers.) */
+int gpk_nat_prep(int D, int M, int Q, const double* eta1, const double* ls, const double* sf, double* R,
+                 double* lls2, double* lsf2, void* stream);
+
+/* d eta1_R from dR = R (dtheta_1 + dtheta_1^T): out[d,p] (+)= dR[d,a,b] * (a == b ? R[d,a,a] : 1)
+ * for the upper-triangle entry p = (a, b) (geepee/aep_models.py:274-287). */
+int gpk_triu_pack(int D, int M, const double* dR, const double* R, double* out, int accumulate, void* stream);
+
+/* Kernel hyperparameter gradients: g_ls[q] = dl[q] exp(ls[q]), g_sf = 2 exp(2 sf) (dsf2 + sum dv)
+ * (geepee/aep_models.py:226-231, 445-450). */
+int gpk_hyp_grads(int Q, const double* ls, const double* sf, const double* dl, const double* dsf2,
+                  const double* dv, int ndv, double* g_ls, double* g_sf, void* stream);
+
+/* *out += w * phi, the natural-parameter layer's weighted log-partition
+ * phi = D/2 logdet Kuu + (N/a - 1)(-1/2 sum_d logdet Su^-1 + 1/2 mu.th2)
+ *       - (N/a)(-1/2 sum_d logdet Suhat^-1 + 1/2 beta muhat.th2),  beta = (N - a)/N
+ * (geepee/aep_models.py:62-114; mu.Su^-1 mu = mu.th2 since mu = Su th2). */
+int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, const double* ldSuinv,
+                const double* ldShinv, const double* mu, const double* mh, const double* th2, double w,
+                double* out, void* stream);
+
+/* Gaussian likelihood of a minibatch of n x D outputs (Gauss_Layer.compute_log_Z and
+ * backprop_grads, geepee/lik_layers.py:119-181), with vt = v + exp(2 sn)/alpha, r = y - m:
+ *   dm = scale r/vt,  dv = scale (-1/(2 vt) + r^2/(2 vt^2))         (written, [n, D])
+ *   *energy = scale * logZ * invN,  *g_sn = scale (sum(dv)/scale * 2 sn2/alpha + n D (1-alpha)) * invN
+ * (both overwritten); logZ includes the alpha-power normaliser n D (log(2 pi sn2/alpha)/2
+ * - alpha log(2 pi sn2)/2). */
+int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn, double alpha,
+                  double scale, double invN, double* dm, double* dv, double* energy, double* g_sn, void* stream);
 
 /* Gradient of tr(Mm Kzz), Kzz = K(Z, Z) without jitter, w.r.t. log sf^2, log ell^2 and Z,
  * added with scales: g_sf += s_sf * d/dlog sf^2, g_ls += s_ls * d/dlog ell^2, g_z += d/dZ.

@@ -110,8 +110,11 @@ def test_psi_fp32_within_tolerance():
     assert_close(ssum.cpu().numpy(), g['psi2_sum'], FP32_TOL, 'psi2 sum fp32')
 
 
-@pytest.mark.parametrize('M', [1, 7, 64, 100, 128, 129, 200])
-def test_chol_inv_logdet(M):
+@pytest.mark.parametrize('with_L', [True, False])
+@pytest.mark.parametrize('M', [1, 7, 32, 33, 64, 65, 96, 100, 128, 129, 200])
+def test_chol_inv_logdet(M, with_L):
+    """with_L: factor, inverse and log-determinant in one kernel; without: the kernel returns
+    L^-1 and the GEMM forms L^-T L^-1."""
     from geepee_gb300 import gpk
     rng = np.random.RandomState(M)
     Z = rng.randn(M, 2)
@@ -119,7 +122,7 @@ def test_chol_inv_logdet(M):
     A = np.stack([K, K + np.diag(rng.rand(M))])
     At = dev(A)
     inv = torch.empty_like(At)
-    L = torch.empty_like(At)
+    L = torch.empty_like(At) if with_L else None
     ld = torch.empty(2, dtype=torch.float64, device='cuda')
     info = torch.empty(2, dtype=torch.int32, device='cuda')
     gpk.chol_inv(At, inv, L, ld, info)
@@ -129,7 +132,8 @@ def test_chol_inv_logdet(M):
         cond = np.linalg.cond(A[b])
         assert_close(inv[b].cpu().numpy(), ref_inv, max(1e-12, 1e-13 * cond), 'inv')
         assert abs(ld[b].item() - np.linalg.slogdet(A[b])[1]) <= 1e-9 * max(1, abs(np.linalg.slogdet(A[b])[1]))
-        assert_close(L[b].cpu().numpy(), np.linalg.cholesky(A[b]), max(1e-12, 1e-14 * cond), 'L')
+        if with_L:
+            assert_close(L[b].cpu().numpy(), np.linalg.cholesky(A[b]), max(1e-12, 1e-14 * cond), 'L')
 
 
 def test_chol_reports_non_pd():
@@ -140,8 +144,25 @@ def test_chol_reports_non_pd():
     assert info.item() == 2
 
 
+@pytest.mark.parametrize('M,bad', [(100, 40), (50, 0), (128, 127)])
+def test_chol_reports_non_pd_pivot(M, bad):
+    """info = (index of the first non-positive pivot) + 1, as LAPACK potrf reports it."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(M)
+    G = rng.randn(M, M)
+    A = G @ G.T + M * np.eye(M)
+    A[bad, bad] = -1.0
+    info = torch.empty(2, dtype=torch.int32, device='cuda')
+    At = dev(np.stack([A, G @ G.T + M * np.eye(M)]))
+    for L in (None, torch.empty_like(At)):
+        gpk.chol_inv(At, torch.empty_like(At), L, None, info)
+        assert info.cpu().numpy().tolist() == [bad + 1, 0]
+
+
 @pytest.mark.parametrize('m,n,k,tA,tB', [(100, 100, 100, False, False), (37, 5, 64, True, False),
-                                         (3, 130, 17, False, True), (64, 64, 1, True, True)])
+                                         (3, 130, 17, False, True), (64, 64, 1, True, True),
+                                         (100, 100, 1000, True, False), (600, 600, 300, False, True),
+                                         (200, 200, 50, False, False), (5, 7, 0, False, False)])
 def test_gemm(m, n, k, tA, tB):
     from geepee_gb300 import gpk
     rng = np.random.RandomState(m + n + k)
@@ -154,10 +175,24 @@ def test_gemm(m, n, k, tA, tB):
     assert_close(C.cpu().numpy(), ref, 1e-12)
 
 
-def test_det_layer_fwd_bwd_vs_oracle():
+def test_gemm_batched_addend():
+    """C[b] = alpha A[b] B + beta E with E broadcast over the batch (gpk_gemm_ex)."""
     from geepee_gb300 import gpk
-    rng = np.random.RandomState(3)
-    N, M, D, Dout = 301, 30, 8, 2
+    rng = np.random.RandomState(11)
+    A, B, E = rng.randn(3, 100, 90), rng.randn(90, 100), rng.randn(100, 100)
+    C = gpk.gemm(dev(A), dev(B), alpha=-1.5, beta=0.25, E=dev(E))
+    assert_close(C.cpu().numpy(), -1.5 * A @ B + 0.25 * E, 1e-12)
+    E3 = rng.randn(3, 100, 100)
+    C = gpk.gemm(dev(A), dev(B), alpha=1.0, beta=-1.0, E=dev(E3))
+    assert_close(C.cpu().numpy(), A @ B - E3, 1e-12)
+
+
+@pytest.mark.parametrize('N,M,D,Dout', [(301, 30, 8, 2), (1000, 100, 8, 2), (37, 200, 3, 1), (5, 129, 2, 4),
+                                        (1, 1, 1, 1)])
+def test_det_layer_fwd_bwd_vs_oracle(N, M, D, Dout):
+    """Row tiles of 8 with ragged ends, several 32-row chunks and 128-column blocks of B."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(3 + N + M)
     x, Z = rng.randn(N, D), rng.randn(M, D)
     ls, sf = rng.uniform(-0.3, 0.5, D), np.array([0.2])
     A = rng.randn(Dout, M)
