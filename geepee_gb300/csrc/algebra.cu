@@ -136,21 +136,33 @@ __global__ void aep_phi_kernel(int D, int M, double N, double alpha, const doubl
 //                                     + n D (1/2 log(2 pi sn2/a) - a/2 log(2 pi sn2))
 //   dm = scale r/vt,  dv = scale (-1/2/vt + 1/2 r^2/vt^2)
 //   energy = scale logZ / N,  g_sn = scale (sum(dv/scale) 2 sn2/a + n D (1 - a)) / N
-__global__ void gauss_lik_kernel(int n, int D, const double* m, const double* v, const double* y,
-                                 const double* sn, double alpha, double scale, double invN, double* dm,
-                                 double* dv, double* energy, double* g_sn) {
+// dm and dv (the upstream gradients of the whole backward) are float64 with one division per
+// element; the logarithm, which only enters the energy, is the double-float one on the FP32
+// pipes (a float64 logarithm per element on one SM's FP64 units costs tens of microseconds).
+__global__ void __launch_bounds__(1024) gauss_lik_kernel(int n, int D, const double* m, const double* v,
+                                                         const double* y, const double* sn, double alpha,
+                                                         double scale, double invN, double* dm, double* dv,
+                                                         double* energy, double* g_sn) {
+  __shared__ float2 tab[256];
   __shared__ double red[2][32];
-  const double sn2 = exp(2.0 * sn[0]);
+  load_exp_table(tab);
+  __syncthreads();
   const double two_pi = 6.283185307179586;
+  const double sn2 = exp(2.0 * sn[0]);
+  const double sn2a = sn2 / alpha;
   double sl = 0.0, sd = 0.0;
   for (int i = threadIdx.x; i < n * D; i += blockDim.x) {
-    const double vt = v[i] + sn2 / alpha;
+    const double vt = v[i] + sn2a;
     const double r = y[i] - m[i];
-    sl += -0.5 * (log(two_pi * vt) + r * r / vt);
-    const double g = -0.5 / vt + 0.5 * r * r / (vt * vt);
-    sd += g;
-    dm[i] = scale * (r / vt);
-    dv[i] = scale * g;
+    const double ivt = 1.0 / vt;
+    const double dmv = r * ivt;
+    const double r2v = r * dmv;                       // r^2 / vt
+    const double dvv = 0.5 * (r2v - 1.0) * ivt;       // -1/(2 vt) + r^2/(2 vt^2)
+    const double lg = df_to_double(log_tab(df_from_double(two_pi * vt), tab));
+    sl -= 0.5 * (lg + r2v);
+    sd += dvv;
+    dm[i] = scale * dmv;
+    dv[i] = scale * dvv;
   }
   for (int k = 16; k > 0; k >>= 1) {
     sl += __shfl_xor_sync(0xffffffffu, sl, k);

@@ -148,6 +148,15 @@ __device__ __forceinline__ void with_static(int i, F&& f) {
   }
 }
 
+// f(std::integral_constant<int, I>) for I = 0 .. N-1 in order
+template <int I, int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>{});
+    static_for<I + 1, N>(f);
+  }
+}
+
 // Right-looking Cholesky of one M x M SPD matrix per CTA (M <= min(32*RS, NW*CS)).  Element
 // (i, j) of the lower triangle lives in a register of lane i % 32 of warp j % NW (slot
 // [i/32][j/NW]), so a trailing update touches no shared memory except the column of L it
@@ -197,16 +206,10 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   }
   __syncthreads();   // the staging area becomes L
 
-  // column k of L from the registers of warp k % NW (warp-uniform caller)
-  auto finalize = [&](int k) {
-    T col[RS];
-    with_static<CS>(k / NW, [&](auto CK) {
-#pragma unroll
-      for (int rr = 0; rr < RS; ++rr) col[rr] = a[rr][CK.value];
-    });
-    T pv = col[0];
-    with_static<RS>(k >> 5, [&](auto RK) { pv = col[RK.value]; });
-    const T p = shfl_idx(pv, k & 31);
+  // column k of L from the registers of warp k % NW; CK = k / NW and RK = k / 32 are
+  // compile-time slot indices (warp-uniform caller)
+  auto finalize = [&](int k, auto CK, auto RK) {
+    const T p = shfl_idx(a[RK.value][CK.value], k & 31);
     if (!(Num<T>::approx(p) > 0.f)) {
       if (lane == 0) s_info = k + 1;
       return;
@@ -215,7 +218,7 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
 #pragma unroll
     for (int rr = 0; rr < RS; ++rr) {
       const int i = lane + 32 * rr;
-      if (i > k && i < M) Ls[k * LD + i] = mul(col[rr], r);
+      if (i > k && i < M) Ls[k * LD + i] = mul(a[rr][CK.value], r);
     }
     if (lane == 0) {
       Ls[k * LD + k] = r;   // 1 / L_kk
@@ -223,40 +226,52 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     }
   };
 
-  if (w == 0) finalize(0);
+  if (w == 0) finalize(0, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
   __syncthreads();
-  for (int k = 0; k + 1 < M; ++k) {
-    if (s_info) break;   // uniform: written before the last barrier
-    T li[RS];
+  // step k applies column k to the columns > k; the column k1 = k + 1 that its owner warp
+  // finalises after updating it is written k1 = 32 KB + NW H + kk (KB, H compile-time), so
+  // the owner's slots are compile-time indices too
+  static_assert(32 % NW == 0, "NW must divide 32");
+  bool stop = false;
+  static_for<0, RS>([&](auto KB) {
+    static_for<0, 32 / NW>([&](auto H) {
+      constexpr int kb = KB.value;
+      constexpr int C1 = (32 * kb + NW * H.value) / NW;   // slot of column k1 in its owner warp
+      const int base = 32 * kb + NW * H.value;             // k1 = base + kk
+      for (int kk = 0; kk < NW && !stop; ++kk) {
+        const int k1 = base + kk, k = k1 - 1;
+        if (k1 == 0) continue;
+        if (k1 >= M || s_info) {   // uniform: s_info is written before the last barrier
+          stop = true;
+          break;
+        }
+        T li[RS];
 #pragma unroll
-    for (int rr = 0; rr < RS; ++rr) {
-      const int i = lane + 32 * rr;
-      li[rr] = (i > k && i < M) ? neg(Ls[k * LD + i]) : Num<T>::zero();
-    }
-    const int k1 = k + 1, c1 = k1 / NW;
-    const bool owner = w == k1 % NW;
-    if (owner) {
-      const T ljk = Ls[k * LD + k1];
-      const int r1 = k1 >> 5;
-      with_static<CS>(c1, [&](auto C1) {
+        for (int rr = 0; rr < RS; ++rr) {
+          const int i = lane + 32 * rr;
+          li[rr] = (i > k && i < M) ? neg(Ls[k * LD + i]) : Num<T>::zero();
+        }
+        const bool owner = w == kk;
+        if (owner) {
+          const T ljk = Ls[k * LD + k1];
 #pragma unroll
-        for (int rr = 0; rr < RS; ++rr)
-          if (rr >= r1) a[rr][C1.value] = fma_(li[rr], ljk, a[rr][C1.value]);
-      });
-      finalize(k1);
-    }
+          for (int rr = kb; rr < RS; ++rr) a[rr][C1] = fma_(li[rr], ljk, a[rr][C1]);
+          finalize(k1, std::integral_constant<int, C1>{}, KB);
+        }
 #pragma unroll
-    for (int cc = 0; cc < CS; ++cc) {
-      const int j = w + NW * cc;
-      if (j <= k || j >= M || (owner && cc == c1)) continue;   // warp-uniform
-      const T ljk = Ls[k * LD + j];
-      const int rj = j >> 5;
+        for (int cc = 0; cc < CS; ++cc) {
+          const int j = w + NW * cc;
+          if (j <= k || j >= M || (owner && cc == C1)) continue;   // warp-uniform
+          const T ljk = Ls[k * LD + j];
+          const int rj = j >> 5;
 #pragma unroll
-      for (int rr = 0; rr < RS; ++rr)
-        if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
-    }
-    __syncthreads();
-  }
+          for (int rr = 0; rr < RS; ++rr)
+            if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+        }
+        __syncthreads();
+      }
+    });
+  });
   const int bad = s_info;
   if (info && threadIdx.x == 0) info[b] = bad;
   if (bad) return;
@@ -311,17 +326,24 @@ __global__ void __launch_bounds__(TW * 32) trinv_kernel(int M, const T* Lw, T* X
   T t[RS];
 #pragma unroll
   for (int rr = 0; rr < RS; ++rr) t[rr] = (lane + 32 * rr == j) ? Num<T>::c(1.f) : Num<T>::zero();
-  for (int k = j; k < M; ++k) {
-    const T* col = Ls + (size_t)(k - j0) * M;
-    const int rk = k >> 5;
-    T tk = t[0];
-    with_static<RS>(rk, [&](auto RK) { tk = t[RK.value]; });
-    const T xk = mul(shfl_idx(tk, k & 31), col[k]);
-    if (lane == (k & 31)) with_static<RS>(rk, [&](auto RK) { t[RK.value] = xk; });
+  // k = 32 kb + kk: the slot kb of the pivot row is a compile-time index (no selects or
+  // branches on the loop-carried path), the pivot lane is kk
+  const int kb0 = j >> 5;
 #pragma unroll
-    for (int rr = 0; rr < RS; ++rr) {
-      const int i = lane + 32 * rr;
-      if (rr >= rk && i > k && i < M) t[rr] = fma_(neg(col[i]), xk, t[rr]);
+  for (int kb = 0; kb < RS; ++kb) {
+    if (kb < kb0) continue;   // warp-uniform
+    const int kend = min(32, M - 32 * kb);
+    for (int kk = (kb == kb0 ? (j & 31) : 0); kk < kend; ++kk) {
+      const int k = 32 * kb + kk;
+      const T* col = Ls + (size_t)(k - j0) * M;
+      const T xk = mul(shfl_idx(t[kb], kk), col[k]);
+      t[kb] = lane == kk ? xk : t[kb];
+#pragma unroll
+      for (int rr = kb; rr < RS; ++rr) {
+        const int i = lane + 32 * rr;
+        const T lik = col[min(i, M - 1)];
+        t[rr] = fma_(neg(i > k && i < M ? lik : Num<T>::zero()), xk, t[rr]);
+      }
     }
   }
   T* Xb = Xt + (size_t)b * M * M + (size_t)j * M;

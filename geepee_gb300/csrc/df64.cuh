@@ -23,8 +23,8 @@ __host__ __device__ __forceinline__ df64 make_df(float h, float l = 0.f) { df64 
 // float64 -> (hi, lo): hi = x rounded to float, lo = (x - hi) rounded to float.  Done with
 // integer operations on the bit pattern (round-to-nearest-even of the 53-bit significand to
 // 24 bits, then the signed remainder normalised to 24 bits): the FP64 pipe, which the plain
-// conversion would use, issues ~64x slower than the integer pipes on this part.  Exponents
-// outside 2^-74 .. 2^127 (and zeros, subnormals, inf, nan) take the FP64 path.
+// conversion would use, issues ~64x slower than the integer pipes on this part.  Zeros are
+// taken directly; exponents outside 2^-74 .. 2^127 (subnormals, inf, nan) take the FP64 path.
 __device__ __forceinline__ df64 df_from_double_fp64(double x) {
   float h = __double2float_rn(x);
   float l = __double2float_rn(x - (double)h);
@@ -33,6 +33,7 @@ __device__ __forceinline__ df64 df_from_double_fp64(double x) {
 __device__ __forceinline__ df64 df_from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
+  if ((b << 1) == 0ull) return make_df(__int_as_float((int)(b >> 32)), 0.f);   // +-0
   if (e < 949 || e > 1150) return df_from_double_fp64(x);
   const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
   unsigned top = (unsigned)(mant >> 29);
@@ -123,7 +124,16 @@ __device__ __forceinline__ df64 mul(df64 a, float b) {
 }
 // a*b + c
 __device__ __forceinline__ df64 fma_(df64 a, df64 b, df64 c) { return add(mul(a, b), c); }
-__device__ __forceinline__ df64 scale2(df64 a, int e) { return make_df(ldexpf(a.hi, e), ldexpf(a.lo, e)); }
+// 2^e as a float for e in [-126, 127] (built from the exponent field: no conversion unit)
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+// a * 2^e, exact while the results stay normal: one multiply for |e| <= 126 (constant e folds
+// to it), two for |e| <= 252 (the range exp_tab needs)
+__device__ __forceinline__ float scale2f(float a, int e) {
+  if (e >= -126 && e <= 127) return a * pow2f(e);
+  const int e1 = e >> 1;
+  return a * pow2f(e1) * pow2f(e - e1);
+}
+__device__ __forceinline__ df64 scale2(df64 a, int e) { return make_df(scale2f(a.hi, e), scale2f(a.lo, e)); }
 
 __device__ __forceinline__ df64 div(df64 a, df64 b) {
   float q1 = __fdiv_rn(a.hi, b.hi);
@@ -159,8 +169,11 @@ __device__ __forceinline__ df64 exp_tab(df64 x, const Tab& tab) {
   if (x.hi < -103.0f) return make_df(0.f);
   if (x.hi > 88.0f) return make_df(__int_as_float(0x7f800000), 0.f);
   const float inv = 369.32993f;  // 256 / ln 2
-  float kf = rintf(x.hi * inv);
-  int k = (int)kf;
+  // k = round(x / (ln2/256)) by the 1.5*2^23 magic addition (|x * inv| < 2^22 here): the
+  // rounding and the integer both come from one FP32 add, with no conversion instruction
+  const float kb = __fadd_rn(x.hi * inv, 12582912.f);
+  const float kf = __fsub_rn(kb, 12582912.f);
+  const int k = __float_as_int(kb) - 0x4B400000;
   df64 r = sub(x, mul(ln2_over_256(), kf));
   // exp(r) - 1 = r + r^2/2 + r^3/6 + r^4/24  (|r| < 1.4e-3; next term < 4e-17)
   df64 r2 = mul(r, r);
@@ -212,7 +225,7 @@ __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float recip(float b) { return __fdiv_rn(1.f, b); }
 __device__ __forceinline__ float sqrt_(float a) { return sqrtf(fmaxf(a, 0.f)); }
-__device__ __forceinline__ float scale2(float a, int e) { return ldexpf(a, e); }
+__device__ __forceinline__ float scale2(float a, int e) { return scale2f(a, e); }
 template <typename Tab> __device__ __forceinline__ float exp_tab(float x, const Tab&) { return expf(x); }
 template <typename Tab> __device__ __forceinline__ float log_tab(float x, const Tab&) { return logf(x); }
 

@@ -199,49 +199,74 @@ __device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
   }
 }
 
-// per-point constants for dimension q (threads q < Q)
+// Per-point tables of one data point n: per-dimension constants (pmu, pis1 = 1/(l+S),
+// pc = 1/(l+2S), pld1/pld2 = 1/2 log(l/(l+S)), 1/2 log(l/(l+2S))) and per-pseudo-input terms
+// (u_a, h_aq).  The backward keeps one point's tables, the forward NPB points' side by side.
+template <typename T>
+struct PointSlot {
+  T* pmu;
+  T* pis1;
+  T* pc;
+  T* pld1;
+  T* pld2;
+  T* u;   // [M]
+  T* h;   // [M*Q]
+};
+
+// per-point constants for dimension q of point n
+template <typename T, typename S>
+__device__ __forceinline__ void dims_of(const PsiArgs<S>& a, const T* ell2, const T* lnl, const float2* tab,
+                                        const PointSlot<T>& ps, int n, int q) {
+  T mu = Num<T>::ld(a.mu[(size_t)n * a.Q + q]);
+  T var = Num<T>::ld(a.var[(size_t)n * a.Q + q]);
+  T s1 = add(ell2[q], var);
+  T s2 = add(ell2[q], add(var, var));
+  ps.pmu[q] = mu;
+  ps.pis1[q] = recip(s1);
+  ps.pc[q] = recip(s2);
+  ps.pld1[q] = scale2(sub(lnl[q], log_tab(s1, tab)), -1);
+  ps.pld2[q] = scale2(sub(lnl[q], log_tab(s2, tab)), -1);
+}
+
 template <typename T, typename S>
 __device__ __forceinline__ void point_dims(const PsiArgs<S>& a, Smem<T>& s, int n) {
   if (threadIdx.x < a.Q) {
-    int q = threadIdx.x;
-    T mu = Num<T>::ld(a.mu[(size_t)n * a.Q + q]);
-    T var = Num<T>::ld(a.var[(size_t)n * a.Q + q]);
-    T s1 = add(s.ell2[q], var);
-    T s2 = add(s.ell2[q], add(var, var));
-    s.pmu[q] = mu;
-    s.pis1[q] = recip(s1);
-    s.pc[q] = recip(s2);
-    s.pld1[q] = scale2(sub(s.lnl[q], log_tab(s1, s.tab)), -1);
-    s.pld2[q] = scale2(sub(s.lnl[q], log_tab(s2, s.tab)), -1);
+    PointSlot<T> ps{s.pmu, s.pis1, s.pc, s.pld1, s.pld2, s.u, s.h};
+    dims_of<T, S>(a, s.ell2, s.lnl, s.tab, ps, n, threadIdx.x);
   }
 }
 
-// per-pseudo-input terms for point n: psi1_a, u_a, h_aq (threads over a)
+// per-pseudo-input terms of one point: psi1_a (returned), u_a and h_aq (written to the slot)
 template <typename T, int QC>
-__device__ __forceinline__ T point_rows(Smem<T>& s, int Q, int ia) {
-  const T lsf = s.misc[0];
+__device__ __forceinline__ T rows_of(const T* z, T lsf, const float2* tab, const PointSlot<T>& ps, int Q, int ia) {
   T e1 = lsf;
   T kap = add(lsf, lsf);
 #pragma unroll
   for (int q = 0; q < QC; ++q) {
     if (q < Q) {
-      T d = sub(s.pmu[q], s.z[ia * Q + q]);
-      e1 = add(e1, sub(s.pld1[q], scale2(mul(mul(d, d), s.pis1[q]), -1)));
-      kap = add(kap, sub(s.pld2[q], mul(mul(s.pmu[q], s.pmu[q]), s.pc[q])));
+      T d = sub(ps.pmu[q], z[ia * Q + q]);
+      e1 = add(e1, sub(ps.pld1[q], scale2(mul(mul(d, d), ps.pis1[q]), -1)));
+      kap = add(kap, sub(ps.pld2[q], mul(mul(ps.pmu[q], ps.pmu[q]), ps.pc[q])));
     }
   }
   T u = scale2(kap, -1);
 #pragma unroll
   for (int q = 0; q < QC; ++q) {
     if (q < Q) {
-      T zq = s.z[ia * Q + q];
-      T czq = mul(s.pc[q], zq);
-      u = add(u, mul(czq, sub(s.pmu[q], scale2(zq, -2))));
-      s.h[ia * Q + q] = scale2(czq, -1);
+      T zq = z[ia * Q + q];
+      T czq = mul(ps.pc[q], zq);
+      u = add(u, mul(czq, sub(ps.pmu[q], scale2(zq, -2))));
+      ps.h[ia * Q + q] = scale2(czq, -1);
     }
   }
-  s.u[ia] = u;
-  return exp_tab(e1, s.tab);
+  ps.u[ia] = u;
+  return exp_tab(e1, tab);
+}
+
+template <typename T, int QC>
+__device__ __forceinline__ T point_rows(Smem<T>& s, int Q, int ia) {
+  PointSlot<T> ps{s.pmu, s.pis1, s.pc, s.pld1, s.pld2, s.u, s.h};
+  return rows_of<T, QC>(s.z, s.misc[0], s.tab, ps, Q, ia);
 }
 
 template <typename T, int QC>
@@ -255,48 +280,113 @@ __device__ __forceinline__ T pair_psi2(const Smem<T>& s, int Q, int p, int ia, i
 }
 
 // ---------------------------------------------------------------------------------
-template <typename T, int QC>
-__device__ __forceinline__ T fwd_pair(const PsiArgs<typename Num<T>::store_t>& a, const Smem<T>& s, int n,
-                                      int p, int ia, int ib, bool contract, T* vals) {
-  typedef typename Num<T>::store_t S;
-  const int M = a.M;
-  T ps = pair_psi2<T, QC>(s, a.Q, p, ia, ib);
-  if (a.psi2) {
-    S v = Num<T>::st(ps);
-    a.psi2[((size_t)n * M + ia) * M + ib] = v;
-    a.psi2[((size_t)n * M + ib) * M + ia] = v;
-  }
-  if (contract) {
-    const int P = M * (M + 1) / 2;
-#pragma unroll
-    for (int d = 0; d < DMAX; ++d) {
-      if (d < a.Dout) {
-        T w;
-        if (s.Bs) {
-          w = s.Bs[d * P + p];
-        } else {
-          const S* Bd = a.B + (size_t)d * M * M;
-          w = Num<T>::ld(Bd[ia * M + ib]);
-          if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
-        }
-        vals[DMAX + d] = fma_(w, ps, vals[DMAX + d]);
-      }
-    }
-  }
-  return ps;
+// Forward, NPB points per pass.  Per pass: the NPB points' per-dimension constants (threads
+// over (point, q)), then their per-pseudo-input terms (threads over (point, a)), then the pair
+// sweep, in which each thread loads a pair's point-independent data once (G_ab, z_b, the
+// symmetrised B weights) and evaluates psi2 for all NPB points - NPB independent exp chains
+// per pair - and finally one CTA reduction for the NPB points' m and v.  PPT > 0 keeps
+// sum_n psi2 of each thread's pairs in registers (pairs tid + k*NT); PPT == 0 sweeps any number
+// of pairs.  The pass count, barriers and reductions per point are 1/NPB of a per-point sweep.
+template <typename T>
+struct FSmem {
+  float2* tab;
+  T* z;      // [M*Q]
+  T* ell2;   // [QMAX]
+  T* lnl;    // [QMAX]
+  T* inv4l;  // [QMAX]
+  T* misc;   // [4] log sf2, sf2
+  T* pd;     // [NPB][5][QMAX] per-point constants
+  T* u;      // [NPB][M]
+  T* h;      // [NPB][M*Q]
+  T* p1;     // [NPB][M]
+  T* As;     // [Dout][M]
+  T* G;      // [P]
+  T* Bs;     // [Dout*P] or nullptr
+  T* red;    // [32*RED]
+};
+
+__host__ __device__ inline size_t fwd_smem_bytes(int M, int Q, int P, int D, int npb, size_t tsz, int nbs) {
+  size_t n = (size_t)M * Q + 3 * QMAX + 4 + (size_t)npb * 5 * QMAX + (size_t)npb * M * (2 + Q) + (size_t)D * M + P +
+             nbs + 32 * RED;
+  return 256 * 8 + n * tsz;
 }
 
-// PPT > 0: each thread owns pairs tid + k*NT (k < PPT) and keeps sum_n psi2 in registers.
-// PPT == 0: plain strided sweep over any number of pairs (no psi2_sum).
-template <typename T, int PPT, int QC>
+template <typename T>
+__device__ FSmem<T> fcarve(char* base, int M, int Q, int P, int D, int npb, int nbs) {
+  FSmem<T> s;
+  s.tab = reinterpret_cast<float2*>(base);
+  T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
+  s.z = t; t += M * Q;
+  s.ell2 = t; t += QMAX;
+  s.lnl = t; t += QMAX;
+  s.inv4l = t; t += QMAX;
+  s.misc = t; t += 4;
+  s.pd = t; t += npb * 5 * QMAX;
+  s.u = t; t += npb * M;
+  s.h = t; t += npb * M * Q;
+  s.p1 = t; t += npb * M;
+  s.As = t; t += D * M;
+  s.G = t; t += P;
+  s.Bs = nbs ? t : nullptr; t += nbs;
+  s.red = t;
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ PointSlot<T> fslot(const FSmem<T>& s, int pt, int M, int Q) {
+  T* pd = s.pd + pt * 5 * QMAX;
+  return PointSlot<T>{pd, pd + QMAX, pd + 2 * QMAX, pd + 3 * QMAX, pd + 4 * QMAX, s.u + pt * M, s.h + pt * M * Q};
+}
+
+template <typename T, int NPB, int PPT, int QC, int DB>
 __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
   const bool contract = (a.A != nullptr) && (a.B != nullptr) && (a.m_out != nullptr || a.v_out != nullptr);
-  Smem<T> s = carve<T>(smem_raw, M, Q, P, false, a.bs_smem ? a.Dout * P : 0);
-  cta_setup<T, S, QC>(a, s, P);
+  FSmem<T> s = fcarve<T>(smem_raw, M, Q, P, contract ? D : 0, NPB, a.bs_smem ? D * P : 0);
+  // ---- per-CTA tables: exp table, Z, lengthscales, sf2, A, G_ab and the symmetrised B
+  load_exp_table(s.tab);
+  for (int i = threadIdx.x; i < M * Q; i += NT) s.z[i] = Num<T>::ld(a.Z[i]);
+  if (contract)
+    for (int i = threadIdx.x; i < D * M; i += NT) s.As[i] = Num<T>::ld(a.A[i]);
+  __syncthreads();
+  if (threadIdx.x < Q) {
+    const int q = threadIdx.x;
+    T lnl = Num<T>::ld(static_cast<S>(a.lls2[q]));
+    T l2 = exp_tab(lnl, s.tab);
+    s.lnl[q] = lnl;
+    s.ell2[q] = l2;
+    s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
+  }
+  if (threadIdx.x == 32) {
+    T lsf = Num<T>::ld(static_cast<S>(a.lsf2[0]));
+    s.misc[0] = lsf;
+    s.misc[1] = exp_tab(lsf, s.tab);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < P; p += NT) {
+    int ia, ib;
+    pair_of(p, ia, ib);
+    T g = Num<T>::zero();
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      if (q < Q) {
+        T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
+        g = fma_(mul(d, d), s.inv4l[q], g);
+      }
+    }
+    s.G[p] = neg(g);
+    if (s.Bs) {
+      for (int d = 0; d < D; ++d) {
+        const S* Bd = a.B + (size_t)d * M * M;
+        T w = Num<T>::ld(Bd[ia * M + ib]);
+        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+        s.Bs[d * P + p] = w;
+      }
+    }
+  }
   constexpr int KP = PPT > 0 ? PPT : 1;
   T acc[KP];
   int pab[KP];
@@ -309,47 +399,120 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
   }
   __syncthreads();
 
-  for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
-    point_dims<T, S>(a, s, n);
-    __syncthreads();
-    T vals[2 * DMAX];
-#pragma unroll
-    for (int i = 0; i < 2 * DMAX; ++i) vals[i] = Num<T>::zero();
-    for (int ia = threadIdx.x; ia < M; ia += blockDim.x) {
-      T p1 = point_rows<T, QC>(s, Q, ia);
-      if (a.psi1) a.psi1[(size_t)n * M + ia] = Num<T>::st(p1);
-      if (contract) {
-#pragma unroll
-        for (int d = 0; d < DMAX; ++d)
-          if (d < D) vals[d] = fma_(p1, Num<T>::ld(a.A[d * M + ia]), vals[d]);
-      }
+  const T lsf = s.misc[0];
+  // each CTA takes a contiguous range of points, NPB at a time
+  const int nbeg = (int)((long)a.N * blockIdx.x / gridDim.x);
+  const int nend = (int)((long)a.N * (blockIdx.x + 1) / gridDim.x);
+  for (int n0 = nbeg; n0 < nend; n0 += NPB) {
+    const int npts = min(NPB, nend - n0);
+    // ---- per-dimension constants of the NPB points
+    for (int t = threadIdx.x; t < npts * Q; t += NT) {
+      const int pt = t / Q, q = t - pt * Q;
+      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, fslot(s, pt, M, Q), n0 + pt, q);
     }
     __syncthreads();
+    // ---- per-pseudo-input terms (and psi1)
+    for (int t = threadIdx.x; t < npts * M; t += NT) {
+      const int pt = t / M, ia = t - pt * M;
+      const T v1 = rows_of<T, QC>(s.z, lsf, s.tab, fslot(s, pt, M, Q), Q, ia);
+      s.p1[pt * M + ia] = v1;
+      if (a.psi1) a.psi1[(size_t)(n0 + pt) * M + ia] = Num<T>::st(v1);
+    }
+    __syncthreads();
+    // ---- pairs
+    T vacc[NPB][DB];
+#pragma unroll
+    for (int pt = 0; pt < NPB; ++pt)
+#pragma unroll
+      for (int d = 0; d < DB; ++d) vacc[pt][d] = Num<T>::zero();
+    auto do_pair = [&](int p, int ia, int ib, T& sum) {
+      const T gab = s.G[p];
+      T zb[QC];
+#pragma unroll
+      for (int q = 0; q < QC; ++q) zb[q] = q < Q ? s.z[ib * Q + q] : Num<T>::zero();
+      T w[DB];
+      if (contract) {
+#pragma unroll
+        for (int d = 0; d < DB; ++d) {
+          w[d] = Num<T>::zero();
+          if (d < D) {
+            if (s.Bs) {
+              w[d] = s.Bs[d * P + p];
+            } else {
+              const S* Bd = a.B + (size_t)d * M * M;
+              w[d] = Num<T>::ld(Bd[ia * M + ib]);
+              if (ia != ib) w[d] = add(w[d], Num<T>::ld(Bd[ib * M + ia]));
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt) {
+        if (pt < npts) {
+          const T* hu = s.u + pt * M;
+          const T* hh = s.h + pt * M * Q + ia * Q;
+          T x = add(add(hu[ia], hu[ib]), gab);
+          T cr = Num<T>::zero();
+#pragma unroll
+          for (int q = 0; q < QC; ++q)
+            if (q < Q) cr = fma_(hh[q], zb[q], cr);
+          const T ps = exp_tab(sub(x, cr), s.tab);
+          if (a.psi2) {
+            const S v = Num<T>::st(ps);
+            const size_t o = (size_t)(n0 + pt) * M;
+            a.psi2[(o + ia) * M + ib] = v;
+            a.psi2[(o + ib) * M + ia] = v;
+          }
+          if (PPT > 0) sum = add(sum, ps);
+          if (contract) {
+#pragma unroll
+            for (int d = 0; d < DB; ++d)
+              if (d < D) vacc[pt][d] = fma_(w[d], ps, vacc[pt][d]);
+          }
+        }
+      }
+    };
     if (PPT > 0) {
 #pragma unroll
       for (int k = 0; k < KP; ++k) {
-        int p = threadIdx.x + k * NT;
-        if (p < P) acc[k] = add(acc[k], fwd_pair<T, QC>(a, s, n, p, pab[k] >> 16, pab[k] & 0xffff, contract, vals));
+        const int p = threadIdx.x + k * NT;
+        if (p < P) do_pair(p, pab[k] >> 16, pab[k] & 0xffff, acc[k]);
       }
     } else {
+      T dummy = Num<T>::zero();
       for (int p = threadIdx.x; p < P; p += NT) {
         int ia, ib;
         pair_of(p, ia, ib);
-        fwd_pair<T, QC>(a, s, n, p, ia, ib, contract, vals);
+        do_pair(p, ia, ib, dummy);
       }
     }
     if (contract) {
-      block_sum<T, 2 * DMAX>(vals, s.red);
+      // m = psi1 . A_d per point, then one CTA reduction of (m, v) for the NPB points
+      T vals[2 * NPB * DB];
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt)
+#pragma unroll
+        for (int d = 0; d < DB; ++d) {
+          T mm = Num<T>::zero();
+          if (pt < npts && d < D)
+            for (int ia = threadIdx.x; ia < M; ia += NT) mm = fma_(s.p1[pt * M + ia], s.As[d * M + ia], mm);
+          vals[(pt * DB + d) * 2] = mm;
+          vals[(pt * DB + d) * 2 + 1] = vacc[pt][d];
+        }
+      block_sum<T, 2 * NPB * DB>(vals, s.red);
       if (threadIdx.x == 0) {
 #pragma unroll
-        for (int d = 0; d < DMAX; ++d) {
-          if (d < D) {
-            T mm = vals[d];
-            T vv = sub(add(s.misc[1], vals[DMAX + d]), mul(mm, mm));
-            if (a.m_out) a.m_out[(size_t)n * D + d] = Num<T>::st(mm);
-            if (a.v_out) a.v_out[(size_t)n * D + d] = Num<T>::st(vv);
+        for (int pt = 0; pt < NPB; ++pt)
+#pragma unroll
+          for (int d = 0; d < DB; ++d) {
+            if (pt < npts && d < D) {
+              const int n = n0 + pt;
+              const T mm = vals[(pt * DB + d) * 2];
+              const T vv = sub(add(s.misc[1], vals[(pt * DB + d) * 2 + 1]), mul(mm, mm));
+              if (a.m_out) a.m_out[(size_t)n * D + d] = Num<T>::st(mm);
+              if (a.v_out) a.v_out[(size_t)n * D + d] = Num<T>::st(vv);
+            }
           }
-        }
       }
     }
     __syncthreads();
@@ -626,19 +789,32 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   }
 }
 
-template <typename T, int PPT, int QC>
-int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
-  auto k = psi_fwd_kernel<T, PPT, QC>;
+template <typename T, int NPB, int PPT, int QC, int DB>
+int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int per_sm, size_t sm, cudaStream_t st) {
+  auto k = psi_fwd_kernel<T, NPB, PPT, QC, DB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int resident = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k, NT, sm);
+  if (resident < 1) resident = 1;
+  if (resident > per_sm) resident = per_sm;
+  int grid = gpk::sm_count() * resident;
+  if (grid > a.N) grid = a.N;
+  if (grid < 1) return GPK_OK;
   k<<<grid, NT, sm, st>>>(a);
   return gpk::check_launch("psi_fwd");
 }
 
+// points per pass: 4 for Dout <= 2, 2 for Dout <= 4 (so 2*NPB*Dout sums fit one reduction)
 template <typename T, int QC>
-int fwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, bool sum, int P, int grid, size_t sm, cudaStream_t st) {
-  if (!sum) return run_fwd<T, 0, QC>(a, grid, sm, st);
-  if (P <= 4 * NT) return run_fwd<T, 4, QC>(a, grid, sm, st);
-  return run_fwd<T, 16, QC>(a, grid, sm, st);
+int fwd_variant(const PsiArgs<typename Num<T>::store_t>& a, bool sum, bool contract, int P, int per_sm, size_t sm,
+                cudaStream_t st) {
+  if (sum) {
+    if (P <= 4 * NT) return run_fwd<T, 2, 4, QC, 4>(a, per_sm, sm, st);
+    return run_fwd<T, 2, 16, QC, 4>(a, per_sm, sm, st);
+  }
+  if (!contract || a.Dout == 1) return run_fwd<T, 4, 0, QC, 1>(a, per_sm, sm, st);
+  if (a.Dout == 2) return run_fwd<T, 4, 0, QC, 2>(a, per_sm, sm, st);
+  return run_fwd<T, 2, 0, QC, 4>(a, per_sm, sm, st);
 }
 
 template <typename T>
@@ -646,20 +822,19 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   PsiArgs<typename Num<T>::store_t> a = a_in;
   const int P = a.M * (a.M + 1) / 2;
   const bool contract = a.A && a.B && (a.m_out || a.v_out);
-  a.bs_smem = contract && smem_bytes(a.M, a.Q, P, false, sizeof(T), a.Dout * P) <= 200 * 1024;
-  size_t sm = smem_bytes(a.M, a.Q, P, false, sizeof(T), a.bs_smem ? a.Dout * P : 0);
-  if (sm > 227 * 1024) return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: M=%d needs %zu B of shared memory", a.M, sm);
   const bool sum = a.psi2_sum != nullptr;
+  const int npb = (sum || (contract && a.Dout > 2)) ? 2 : 4;
+  const int D = contract ? a.Dout : 0;
+  a.bs_smem = contract && fwd_smem_bytes(a.M, a.Q, P, D, npb, sizeof(T), a.Dout * P) <= 200 * 1024;
+  size_t sm = fwd_smem_bytes(a.M, a.Q, P, D, npb, sizeof(T), a.bs_smem ? a.Dout * P : 0);
+  if (sm > 227 * 1024) return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: M=%d needs %zu B of shared memory", a.M, sm);
   if (sum && P > PPT_MAX * NT)
     return gpk::fail(GPK_EUNSUPPORTED, "psi_fwd: psi2_sum needs M(M+1)/2 <= %d (M=%d)", PPT_MAX * NT, a.M);
   int per_sm = (int)((227 * 1024) / (sm + 1024));
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 2) per_sm = 2;
-  int grid = gpk::sm_count() * per_sm;
-  if (grid > a.N) grid = a.N;
-  if (grid < 1) return GPK_OK;
-  if (a.Q <= 2) return fwd_ppt<T, 2>(a, sum, P, grid, sm, st);
-  return fwd_ppt<T, QMAX>(a, sum, P, grid, sm, st);
+  if (a.Q <= 2) return fwd_variant<T, 2>(a, sum, contract, P, per_sm, sm, st);
+  return fwd_variant<T, QMAX>(a, sum, contract, P, per_sm, sm, st);
 }
 
 template <typename T, int PPT, int DB, int QC>
