@@ -44,6 +44,7 @@ _SIGS = {
     'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_chol_inv_ws': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_spd_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_spd_inv_static': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     'gpk_small_spd': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     'gpk_lincomb': [_vp, _vp],

@@ -2,6 +2,8 @@
 //   gpk_gemm      batched C = alpha op(A) op(B) + beta C
 //   gpk_chol_inv  batched SPD Cholesky + inverse + log-determinant (M <= 128, one CTA each)
 //   gpk_trace_kzz gradient of tr(M Kzz) w.r.t. log sf^2, log ell^2 and Z
+#include <mutex>
+
 #include "common.cuh"
 
 namespace {
@@ -787,6 +789,55 @@ extern "C" int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv
     return prec == GPK_DF64
                ? chol_launch<df64, true>(batch, M, A, Ainv, nullptr, logdet, info, work, nullptr, st)
                : chol_launch<float, true>(batch, M, A, Ainv, nullptr, logdet, info, work, nullptr, st);
+  return prec == GPK_DF64 ? spd_inv_small<df64>(batch, M, A, Ainv, logdet, info, work, st)
+                          : spd_inv_small<float>(batch, M, A, Ainv, logdet, info, work, st);
+}
+
+// ---- gpk_spd_inv_static: gpk_spd_inv with its workspace in a file-scope device array ----
+// Limit: M <= 128 and batch * M * M <= SPD_STATIC_ELEMS (e.g. 8 matrices of 128 x 128).
+// Nothing in the array needs to start at zero (every element a call reads was written
+// earlier in the same call).  There is one array per device: calls that overlap on the
+// device (different streams or host threads) race on it.
+constexpr long SPD_STATIC_ELEMS = 8L * 128 * 128;
+static __device__ __align__(256) unsigned char g_spd_scratch[2 * SPD_STATIC_ELEMS * 8];
+
+namespace {
+constexpr int SPD_MAX_DEVICES = 64;
+void* g_spd_scratch_addr[SPD_MAX_DEVICES];
+std::mutex g_spd_scratch_mu;
+
+// device address of g_spd_scratch on the current device, looked up once per device
+int spd_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return gpk::fail(GPK_ECUDA, "spd_inv_static: cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= SPD_MAX_DEVICES)
+    return gpk::fail(GPK_EUNSUPPORTED, "spd_inv_static: device %d >= %d", dev, SPD_MAX_DEVICES);
+  std::lock_guard<std::mutex> lock(g_spd_scratch_mu);
+  if (!g_spd_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_spd_scratch);
+    if (e != cudaSuccess || !p)
+      return gpk::fail(GPK_ECUDA, "spd_inv_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_spd_scratch_addr[dev] = p;
+  }
+  *out = g_spd_scratch_addr[dev];
+  return GPK_OK;
+}
+}  // namespace
+
+extern "C" int gpk_spd_inv_static(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
+                                  void* stream) {
+  GPK_REQUIRE(batch >= 0 && M >= 1 && M <= 128, "spd_inv_static: M=%d outside [1,128]", M);
+  GPK_REQUIRE((long)batch * M * M <= SPD_STATIC_ELEMS, "spd_inv_static: batch*M*M = %ld > %ld",
+              (long)batch * M * M, SPD_STATIC_ELEMS);
+  GPK_REQUIRE(A && Ainv && info, "spd_inv_static: null pointer");
+  if (prec != GPK_DF64 && prec != GPK_FP32) return gpk::fail(GPK_EINVAL, "spd_inv_static: unknown precision %d", prec);
+  if (batch == 0) return GPK_OK;
+  void* work = nullptr;
+  const int rc = spd_scratch(&work);
+  if (rc) return rc;
+  cudaStream_t st = gpk::as_stream(stream);
   return prec == GPK_DF64 ? spd_inv_small<df64>(batch, M, A, Ainv, logdet, info, work, st)
                           : spd_inv_small<float>(batch, M, A, Ainv, logdet, info, work, st);
 }

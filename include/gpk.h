@@ -161,6 +161,15 @@ int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void*
 int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info, void* work,
                 void* stream);
 
+/* gpk_spd_inv without a workspace argument and without allocating: the workspace is a
+ * file-scope device array of the library (2 MiB), so the limit is M <= 128 and
+ * batch*M*M <= 131072 (e.g. 8 matrices of 128 x 128); larger inputs are rejected with
+ * GPK_EINVAL.  No counterpart in the reference (an interface of this library only).  The
+ * array is one per device and needs no zeroing; calls that overlap on a device (other
+ * streams or host threads) race on it. */
+int gpk_spd_inv_static(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
+                       void* stream);
+
 /* ---- fused float64 pieces of the M x M AEP algebra (no counterpart kernels in the reference:
  * each replaces a chain of numpy expressions; the arithmetic stays float64) ---- */
 
