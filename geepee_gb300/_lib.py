@@ -41,6 +41,7 @@ _SIGS = {
     'gpk_gemm_ex': [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_dbl, _vp, _c_int,
                     ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp, _c_int,
                     ctypes.c_long, _vp],
+    'gpk_gemm_group': [_c_int, _c_int, _vp, _vp],
     'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_chol_inv_ws': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_spd_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],

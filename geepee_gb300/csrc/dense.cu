@@ -33,22 +33,22 @@ struct GemmShape {
   static constexpr int R = TBM >= 32 ? 2 : 1, TPD = TBM / R, NG = TPD * TPD;
 };
 template <typename T, int TBM, int KS, bool P2>
-__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_kernel(
-    int m, int n, int k, int tA, int tB, double alpha, const typename Num<T>::store_t* A, int lda, long sA,
-    const typename Num<T>::store_t* B, int ldb, long sB, double beta, const typename Num<T>::store_t* E, int lde,
-    long sE, typename Num<T>::store_t* C, int ldc, long sC) {
+__device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, int k, int tA, int tB, double alpha,
+                                          const typename Num<T>::store_t* A, int lda, long sA,
+                                          const typename Num<T>::store_t* B, int ldb, long sB, double beta,
+                                          const typename Num<T>::store_t* E, int lde, long sE,
+                                          typename Num<T>::store_t* C, int ldc, long sC) {
   typedef typename Num<T>::store_t S;
   constexpr int R = GemmShape<TBM>::R, TPD = GemmShape<TBM>::TPD, NG = GemmShape<TBM>::NG;
   constexpr int NT = NG * KS, NPT = KC * TBM / NT;
   extern __shared__ __align__(16) char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);      // [KC][TBM]
   T* Bs = As + KC * TBM;                        // [KC][TBM]
-  const int bz = blockIdx.z;
   A += bz * sA;
   B += bz * sB;
   C += bz * sC;
   if (E) E += bz * sE;
-  const int i0 = blockIdx.y * TBM, j0 = blockIdx.x * TBM;
+  const int i0 = by * TBM, j0 = bx * TBM;
   const int g = threadIdx.x / NG, t = threadIdx.x % NG;
   const int tx = t % TPD, ty = t / TPD;
   T acc[R][R];
@@ -136,6 +136,42 @@ __global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_kernel(
         C[(size_t)gi * ldc + gj] = v;
       }
     }
+}
+
+template <typename T, int TBM, int KS, bool P2>
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_kernel(
+    int m, int n, int k, int tA, int tB, double alpha, const typename Num<T>::store_t* A, int lda, long sA,
+    const typename Num<T>::store_t* B, int ldb, long sB, double beta, const typename Num<T>::store_t* E, int lde,
+    long sE, typename Num<T>::store_t* C, int ldc, long sC) {
+  gemm_tile<T, TBM, KS, P2>(blockIdx.x, blockIdx.y, blockIdx.z, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta,
+                            E, lde, sE, C, ldc, sC);
+}
+
+// Several independent products in one launch: problem p owns the flat tile range
+// [first[p], first[p+1]); a CTA finds its problem and runs that tile.
+struct GemmGroupArgs {
+  int count;
+  int first[GPK_GEMM_GROUP + 1];
+  int tiles_n[GPK_GEMM_GROUP], tiles_m[GPK_GEMM_GROUP];
+  gpk_gemm_t pr[GPK_GEMM_GROUP];
+};
+
+template <typename T, int TBM, int KS>
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_group_kernel(GemmGroupArgs g) {
+  typedef typename Num<T>::store_t S;
+  const int t = blockIdx.x;
+  int p = 0;
+#pragma unroll
+  for (int q = 1; q < GPK_GEMM_GROUP; ++q)
+    if (q < g.count && t >= g.first[q]) p = q;
+  const gpk_gemm_t& pr = g.pr[p];
+  const int r = t - g.first[p];
+  const int per = g.tiles_n[p] * g.tiles_m[p];
+  const int bz = r / per, rem = r - bz * per;
+  const int by = rem / g.tiles_n[p], bx = rem - by * g.tiles_n[p];
+  gemm_tile<T, TBM, KS, false>(bx, by, bz, pr.m, pr.n, pr.k, pr.transA, pr.transB, pr.alpha, (const S*)pr.A, pr.lda,
+                               pr.strideA, (const S*)pr.B, pr.ldb, pr.strideB, pr.beta, (const S*)pr.E, pr.lde,
+                               pr.strideE, (S*)pr.C, pr.ldc, pr.strideC);
 }
 
 // ---- the SPD inverse fast path: factor (one CTA) -> L^-1 (many CTAs) -> L^-T L^-1 (GEMM) ----
@@ -661,6 +697,41 @@ int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, co
   return gpk::check_launch("gemm");
 }
 
+template <typename T, int TBM, int KS>
+int gemm_group_go(const GemmGroupArgs& g, cudaStream_t st) {
+  const size_t sm = 2 * KC * TBM * sizeof(T);
+  auto kfn = gemm_group_kernel<T, TBM, KS>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  kfn<<<g.first[g.count], GemmShape<TBM>::NG * KS, sm, st>>>(g);
+  return gpk::check_launch("gemm_group");
+}
+
+template <typename T>
+int gemm_group_launch(int count, const gpk_gemm_t* pr, cudaStream_t st) {
+  // the tile size is chosen for the whole group, as gemm_launch chooses it for one product
+  long t32 = 0, t16 = 0;
+  for (int p = 0; p < count; ++p) {
+    t32 += (long)gpk::ceil_div(pr[p].n, 32) * gpk::ceil_div(pr[p].m, 32) * pr[p].batch;
+    t16 += (long)gpk::ceil_div(pr[p].n, 16) * gpk::ceil_div(pr[p].m, 16) * pr[p].batch;
+  }
+  const int tbm = t32 >= 2L * gpk::sm_count() ? 32 : (t16 >= gpk::sm_count() ? 16 : 8);
+  GemmGroupArgs g{};
+  g.count = count;
+  g.first[0] = 0;
+  for (int p = 0; p < count; ++p) {
+    g.pr[p] = pr[p];
+    g.tiles_n[p] = gpk::ceil_div(pr[p].n, tbm);
+    g.tiles_m[p] = gpk::ceil_div(pr[p].m, tbm);
+    const long tiles = (long)g.tiles_n[p] * g.tiles_m[p] * pr[p].batch;
+    if (g.first[p] + tiles > 0x7fffffffL) return gpk::fail(GPK_EUNSUPPORTED, "gemm_group: too many tiles");
+    g.first[p + 1] = g.first[p] + (int)tiles;
+  }
+  if (g.first[count] == 0) return GPK_OK;
+  if (tbm == 32) return gemm_group_go<T, 32, 2>(g, st);
+  if (tbm == 16) return gemm_group_go<T, 16, 4>(g, st);
+  return gemm_group_go<T, 8, 4>(g, st);
+}
+
 }  // namespace
 
 extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
@@ -698,6 +769,24 @@ extern "C" int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA,
     return gemm_launch<float>(batch, m, n, k, transA, transB, alpha, A, lda, strideA, B, ldb, strideB, beta, E, lde,
                               strideE, C, ldc, strideC, st);
   return gpk::fail(GPK_EINVAL, "gemm_ex: unknown precision %d", prec);
+}
+
+extern "C" int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, void* stream) {
+  GPK_REQUIRE(count >= 0 && count <= GPK_GEMM_GROUP, "gemm_group: count %d outside [0,%d]", count, GPK_GEMM_GROUP);
+  GPK_REQUIRE(count == 0 || problems, "gemm_group: null problem list");
+  for (int p = 0; p < count; ++p) {
+    const gpk_gemm_t& q = problems[p];
+    GPK_REQUIRE(q.batch >= 0 && q.m >= 0 && q.n >= 0 && q.k >= 0 && q.batch <= 65535, "gemm_group[%d]: bad size", p);
+    GPK_REQUIRE(q.C && (q.k == 0 || (q.A && q.B)) && (q.beta == 0.0 || q.E), "gemm_group[%d]: null pointer", p);
+    GPK_REQUIRE(q.lda >= (q.transA ? q.m : q.k) && q.ldb >= (q.transB ? q.k : q.n) && q.ldc >= q.n &&
+                    (q.beta == 0.0 || q.lde >= q.n),
+                "gemm_group[%d]: bad leading dimension", p);
+  }
+  if (count == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64) return gemm_group_launch<df64>(count, problems, st);
+  if (prec == GPK_FP32) return gemm_group_launch<float>(count, problems, st);
+  return gpk::fail(GPK_EINVAL, "gemm_group: unknown precision %d", prec);
 }
 
 template <typename T, int RS, int CS, int NW>

@@ -25,7 +25,9 @@ __host__ __device__ __forceinline__ df64 make_df(float h, float l = 0.f) { df64 
 // 24 bits, then the signed remainder normalised to 24 bits): the FP64 pipe, which the plain
 // conversion would use, issues ~64x slower than the integer pipes on this part.  Zeros are
 // taken directly; exponents outside 2^-74 .. 2^127 (subnormals, inf, nan) take the FP64 path.
-__device__ __forceinline__ df64 df_from_double_fp64(double x) {
+// Kept out of line: inlined, the compiler if-converts the rare branch that calls it and runs
+// its FP64 instructions for every conversion.
+static __device__ __noinline__ df64 df_from_double_fp64(double x) {
   float h = __double2float_rn(x);
   float l = __double2float_rn(x - (double)h);
   return make_df(h, l);

@@ -1,12 +1,12 @@
 // Psi statistics of the ARD kernel under Gaussian inputs, fused with the
 // moment-matching contractions of a sparse-GP layer, and their backward pass.
 //
-// Work decomposition (both kernels): a CTA walks a strided sequence of data points
-// n; for each point its threads first build per-point tables in shared memory
-// (per-dimension constants, per-pseudo-input terms u_a, h_aq), then sweep the
-// M(M+1)/2 unordered pairs (a <= b) of pseudo-inputs.  Each thread owns a fixed set of
-// pairs (p = tid + k*NT) across all of its points, so sums over n of per-pair
-// quantities (sum_n psi2, dB = sum_n dv psi2) stay in registers until one atomic
+// Work decomposition (both kernels): a CTA takes a contiguous range of data points, NPB
+// points per pass; per pass its threads first build the points' tables in shared memory
+// (per-dimension constants, per-pseudo-input terms u_a, h_aq), then sweep the M(M+1)/2
+// unordered pairs (a <= b) of pseudo-inputs, each pair for all NPB points.  Each thread
+// owns a fixed set of pairs (p = tid + k*NT) across all of its points, so sums over n of
+// per-pair quantities (sum_n psi2, dB = sum_n dv psi2) stay in registers until one atomic
 // flush per CTA.  psi2 per point is never materialised in HBM (unless requested).
 //
 // log psi2[n,a,b] = u_a + u_b + G_ab - sum_q h_aq z_bq   with
@@ -29,7 +29,7 @@ constexpr int QMAX = 8;
 constexpr int DMAX = 4;
 constexpr int NT = 512;        // threads per CTA
 constexpr int PPT_MAX = 16;    // pairs per thread for register-resident per-pair sums
-constexpr int RED = 24;        // reduction slots per warp
+constexpr int RED = 48;        // reduction slots per warp
 
 template <typename S>
 struct PsiArgs {
@@ -51,6 +51,7 @@ struct PsiArgs {
   const S* dv;
   const S* dpsi1;    // optional [N,M]: replaces dm_all A
   int bs_smem;       // symmetrised B staged in shared memory (set by the launcher)
+  int accb_smem;     // backward: dBhat accumulates in shared memory (else atomically in dB)
   long b_stride;     // != 0: B is per point (B + n*b_stride), dv treated as 1
   double* dsf2;
   double* dl;
@@ -70,71 +71,6 @@ __device__ __forceinline__ void pair_of(int p, int& a, int& b) {
   b = p - r * (r + 1) / 2;
 }
 
-template <typename T>
-struct Smem {
-  float2* tab;   // [256]
-  T* z;          // [M*Q]
-  T* ell2;       // [QMAX]
-  T* lnl;        // [QMAX] log ell2
-  T* inv4l;      // [QMAX] 1/(4 ell2)
-  T* il;         // [QMAX] 1/ell2
-  T* misc;       // [4]    log sf2, sf2
-  T* pmu;        // [QMAX] per point
-  T* pis1;       // [QMAX] 1/(l+S)
-  T* pc;         // [QMAX] 1/(l+2S)
-  T* pld1;       // [QMAX] 1/2 log(l/(l+S))
-  T* pld2;       // [QMAX] 1/2 log(l/(l+2S))
-  T* pd;         // [2*DMAX] per-point dm_all, dv
-  T* u;          // [M]
-  T* h;          // [M*Q]
-  T* G;          // [P]
-  T* Bs;         // [Dout*P] symmetrised B (B_ab + B_ba off the diagonal), or nullptr
-  T* red;        // [32 * RED]
-  T* L;          // [P]   (backward only)
-  T* rows;       // [M*(1+QMAX)] row statistics (backward only)
-  T* dz;         // [M*Q]  dZ accumulator over the CTA's points (backward only)
-};
-
-template <typename T>
-__device__ Smem<T> carve(char* base, int M, int Q, int P, bool bwd, int nbs) {
-  Smem<T> s;
-  s.tab = reinterpret_cast<float2*>(base);
-  T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
-  s.z = t; t += M * Q;
-  s.ell2 = t; t += QMAX;
-  s.lnl = t; t += QMAX;
-  s.inv4l = t; t += QMAX;
-  s.il = t; t += QMAX;
-  s.misc = t; t += 4;
-  s.pmu = t; t += QMAX;
-  s.pis1 = t; t += QMAX;
-  s.pc = t; t += QMAX;
-  s.pld1 = t; t += QMAX;
-  s.pld2 = t; t += QMAX;
-  s.pd = t; t += 2 * DMAX;
-  s.u = t; t += M;
-  s.h = t; t += M * Q;
-  s.G = t; t += P;
-  s.Bs = nbs ? t : nullptr; t += nbs;
-  s.red = t; t += 32 * RED;
-  if (bwd) {
-    s.L = t; t += P;
-    s.rows = t; t += M * (1 + QMAX);
-    s.dz = t; t += M * Q;
-  } else {
-    s.L = nullptr;
-    s.rows = nullptr;
-    s.dz = nullptr;
-  }
-  return s;
-}
-
-__host__ __device__ inline size_t smem_bytes(int M, int Q, int P, bool bwd, size_t tsz, int nbs) {
-  size_t n = (size_t)M * Q + 10 * QMAX + 4 + 2 * DMAX + M + (size_t)M * Q + P + nbs + 32 * RED;
-  if (bwd) n += P + (size_t)M * (1 + QMAX) + (size_t)M * Q;
-  return 256 * 8 + n * tsz;
-}
-
 // CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.
 template <typename T, int K>
 __device__ __forceinline__ void block_sum(T* vals, T* red) {
@@ -150,51 +86,6 @@ __device__ __forceinline__ void block_sum(T* vals, T* red) {
     for (int i = 0; i < K; ++i) {
       T s = lane < nw ? red[lane * RED + i] : Num<T>::zero();
       vals[i] = warp_sum(s);
-    }
-  }
-}
-
-// common per-CTA setup: exp table, Z, lengthscales, signal variance, G and B tables
-template <typename T, typename S, int QC>
-__device__ void cta_setup(const PsiArgs<S>& a, Smem<T>& s, int P) {
-  const int M = a.M, Q = a.Q;
-  load_exp_table(s.tab);
-  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) s.z[i] = Num<T>::ld(a.Z[i]);
-  __syncthreads();
-  if (threadIdx.x < Q) {
-    int q = threadIdx.x;
-    T lnl = Num<T>::ld(static_cast<S>(a.lls2[q]));
-    T l2 = exp_tab(lnl, s.tab);
-    s.lnl[q] = lnl;
-    s.ell2[q] = l2;
-    s.il[q] = recip(l2);
-    s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
-  }
-  if (threadIdx.x == 32) {
-    T lsf = Num<T>::ld(static_cast<S>(a.lsf2[0]));
-    s.misc[0] = lsf;
-    s.misc[1] = exp_tab(lsf, s.tab);
-  }
-  __syncthreads();
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    int ia, ib;
-    pair_of(p, ia, ib);
-    T g = Num<T>::zero();
-#pragma unroll
-    for (int q = 0; q < QC; ++q) {
-      if (q < Q) {
-        T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
-        g = fma_(mul(d, d), s.inv4l[q], g);
-      }
-    }
-    s.G[p] = neg(g);
-    if (s.Bs) {
-      for (int d = 0; d < a.Dout; ++d) {
-        const S* Bd = a.B + (size_t)d * M * M;
-        T w = Num<T>::ld(Bd[ia * M + ib]);
-        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
-        s.Bs[d * P + p] = w;
-      }
     }
   }
 }
@@ -228,14 +119,6 @@ __device__ __forceinline__ void dims_of(const PsiArgs<S>& a, const T* ell2, cons
   ps.pld2[q] = scale2(sub(lnl[q], log_tab(s2, tab)), -1);
 }
 
-template <typename T, typename S>
-__device__ __forceinline__ void point_dims(const PsiArgs<S>& a, Smem<T>& s, int n) {
-  if (threadIdx.x < a.Q) {
-    PointSlot<T> ps{s.pmu, s.pis1, s.pc, s.pld1, s.pld2, s.u, s.h};
-    dims_of<T, S>(a, s.ell2, s.lnl, s.tab, ps, n, threadIdx.x);
-  }
-}
-
 // per-pseudo-input terms of one point: psi1_a (returned), u_a and h_aq (written to the slot)
 template <typename T, int QC>
 __device__ __forceinline__ T rows_of(const T* z, T lsf, const float2* tab, const PointSlot<T>& ps, int Q, int ia) {
@@ -261,22 +144,6 @@ __device__ __forceinline__ T rows_of(const T* z, T lsf, const float2* tab, const
   }
   ps.u[ia] = u;
   return exp_tab(e1, tab);
-}
-
-template <typename T, int QC>
-__device__ __forceinline__ T point_rows(Smem<T>& s, int Q, int ia) {
-  PointSlot<T> ps{s.pmu, s.pis1, s.pc, s.pld1, s.pld2, s.u, s.h};
-  return rows_of<T, QC>(s.z, s.misc[0], s.tab, ps, Q, ia);
-}
-
-template <typename T, int QC>
-__device__ __forceinline__ T pair_psi2(const Smem<T>& s, int Q, int p, int ia, int ib) {
-  T x = add(add(s.u[ia], s.u[ib]), s.G[p]);
-  T cr = Num<T>::zero();
-#pragma unroll
-  for (int q = 0; q < QC; ++q)
-    if (q < Q) cr = fma_(s.h[ia * Q + q], s.z[ib * Q + q], cr);
-  return exp_tab(sub(x, cr), s.tab);
 }
 
 // ---------------------------------------------------------------------------------
@@ -532,35 +399,129 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
 }
 
 // ---------------------------------------------------------------------------------
-// Backward.  Per point: psi1 terms per pseudo-input; per pair L = W psi2 with
-// W = sum_d dv_d (B_d[a,b] + B_d[b,a]) (the symmetrised upstream gradient, as
-// psi2compDer does, geepee/kernels.py:415-418) staged in shared memory; then per row
-// a the full-square sums R_a = sum_b L~_ab, S_aq = sum_b L~_ab z_bq (L~ the symmetric
-// half-weight matrix).  Every psi2 gradient is an affine function of R and S:
+// Backward, NPB points per pass.  Per point: psi1 terms per pseudo-input; per pair
+// L = W psi2 with W = sum_d dv_d (B_d[a,b] + B_d[b,a]) (the symmetrised upstream gradient, as
+// psi2compDer does, geepee/kernels.py:415-418) staged in shared memory; then per row a the
+// full-square sums R_a = sum_b L~_ab, S_aq = sum_b L~_ab z_bq (L~ the symmetric half-weight
+// matrix).  Every psi2 gradient is an affine function of R and S:
 //   dZ_aq += R_a(-z_aq/l + 2 c mu - c z_aq) + S_aq (1/l - c)
 //   dmu_q  = -2c (mu Rt - St)                    (Rt = sum_a R_a, St = sum_a S_a)
 //   dS_q   = -c Rt + 2c^2 (mu^2 Rt - 2 mu St + Z2R/2 + ZS/2)
 //   dl_q  += 2 ell (Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 (mu^2 Rt - 2 mu St + Z2R/2 + ZS/2))
 // with Z2R = sum_a z_a^2 R_a, ZS = sum_a z_a S_a; these restate psi2compDer
-// (geepee/kernels.py:402-444) without its N x M x M temporaries.
-template <typename T, int PPT, int DB, int QC>
+// (geepee/kernels.py:402-444) without its N x M x M temporaries.  A pass evaluates each of a
+// thread's pairs for all NPB points (the pair's G_ab, z_b and B weights loaded once), and the
+// per-point phases and barriers are shared by the NPB points.
+template <typename T>
+struct BSmem {
+  float2* tab;
+  T* z;      // [M*Q]
+  T* ell2;   // [QMAX]
+  T* lnl;    // [QMAX]
+  T* inv4l;  // [QMAX]
+  T* il;     // [QMAX]
+  T* misc;   // [4] log sf2, sf2
+  T* pd;     // [NPB][5][QMAX] per-point constants
+  T* pg;     // [NPB][2*DMAX] dm_all, dv per point
+  T* u;      // [NPB][M]
+  T* h;      // [NPB][M*Q]
+  T* G;      // [P]
+  T* Bs;     // [Dout*P] or nullptr
+  T* L;      // [NPB][P]
+  T* rows;   // [NPB][M][1+QMAX]
+  T* dz;     // [M*Q]
+  T* accB;   // [Dout*P] sum over the CTA's points of dv psi2 (dBhat)
+  T* red;    // [32*RED]
+};
+
+__host__ __device__ inline size_t bwd_smem_bytes(int M, int Q, int P, int nacc, int npb, size_t tsz, int nbs) {
+  size_t n = (size_t)M * Q + 4 * QMAX + 4 + (size_t)npb * (5 * QMAX + 2 * DMAX) + (size_t)npb * M * (1 + Q) + P +
+             nbs + (size_t)npb * P + (size_t)npb * M * (1 + QMAX) + (size_t)M * Q + nacc + 32 * RED;
+  return 256 * 8 + n * tsz;
+}
+
+template <typename T>
+__device__ BSmem<T> bcarve(char* base, int M, int Q, int P, int nacc, int npb, int nbs) {
+  BSmem<T> s;
+  s.tab = reinterpret_cast<float2*>(base);
+  T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
+  s.z = t; t += M * Q;
+  s.ell2 = t; t += QMAX;
+  s.lnl = t; t += QMAX;
+  s.inv4l = t; t += QMAX;
+  s.il = t; t += QMAX;
+  s.misc = t; t += 4;
+  s.pd = t; t += npb * 5 * QMAX;
+  s.pg = t; t += npb * 2 * DMAX;
+  s.u = t; t += npb * M;
+  s.h = t; t += npb * M * Q;
+  s.G = t; t += P;
+  s.Bs = nbs ? t : nullptr; t += nbs;
+  s.L = t; t += npb * P;
+  s.rows = t; t += npb * M * (1 + QMAX);
+  s.dz = t; t += M * Q;
+  s.accB = nacc ? t : nullptr; t += nacc;
+  s.red = t;
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ PointSlot<T> bslot(const BSmem<T>& s, int pt, int M, int Q) {
+  T* pd = s.pd + pt * 5 * QMAX;
+  return PointSlot<T>{pd, pd + QMAX, pd + 2 * QMAX, pd + 3 * QMAX, pd + 4 * QMAX, s.u + pt * M, s.h + pt * M * Q};
+}
+
+template <typename T, int NPB, int DB, int QC>
 __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
-  Smem<T> s = carve<T>(smem_raw, M, Q, P, true, a.bs_smem ? a.Dout * P : 0);
-  cta_setup<T, S, QC>(a, s, P);
-
-  T accB[PPT][DB];
-  int pab[PPT];
+  BSmem<T> s = bcarve<T>(smem_raw, M, Q, P, a.accb_smem ? D * P : 0, NPB, a.bs_smem ? D * P : 0);
+  // ---- per-CTA tables: exp table, Z, lengthscales, sf2, G_ab and the symmetrised B
+  load_exp_table(s.tab);
+  for (int i = threadIdx.x; i < M * Q; i += NT) {
+    s.z[i] = Num<T>::ld(a.Z[i]);
+    s.dz[i] = Num<T>::zero();
+  }
+  if (s.accB)
+    for (int i = threadIdx.x; i < D * P; i += NT) s.accB[i] = Num<T>::zero();
+  __syncthreads();
+  if (threadIdx.x < Q) {
+    const int q = threadIdx.x;
+    T lnl = Num<T>::ld(static_cast<S>(a.lls2[q]));
+    T l2 = exp_tab(lnl, s.tab);
+    s.lnl[q] = lnl;
+    s.ell2[q] = l2;
+    s.il[q] = recip(l2);
+    s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
+  }
+  if (threadIdx.x == 32) {
+    T lsf = Num<T>::ld(static_cast<S>(a.lsf2[0]));
+    s.misc[0] = lsf;
+    s.misc[1] = exp_tab(lsf, s.tab);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < P; p += NT) {
+    int ia, ib;
+    pair_of(p, ia, ib);
+    T g = Num<T>::zero();
 #pragma unroll
-  for (int k = 0; k < PPT; ++k) {
-#pragma unroll
-    for (int d = 0; d < DB; ++d) accB[k][d] = Num<T>::zero();
-    int p = threadIdx.x + k * NT, ia = 0, ib = 0;
-    if (p < P) pair_of(p, ia, ib);
-    pab[k] = (ia << 16) | ib;
+    for (int q = 0; q < QC; ++q) {
+      if (q < Q) {
+        T d = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
+        g = fma_(mul(d, d), s.inv4l[q], g);
+      }
+    }
+    s.G[p] = neg(g);
+    if (s.Bs) {
+      for (int d = 0; d < D; ++d) {
+        const S* Bd = a.B + (size_t)d * M * M;
+        T w = Num<T>::ld(Bd[ia * M + ib]);
+        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
+        s.Bs[d * P + p] = w;
+      }
+    }
   }
   // per-thread accumulators over points
   T g_sf = Num<T>::zero();                 // sum L1 + 2 sum L (for dsf2 * sf2)
@@ -570,105 +531,162 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   for (int q = 0; q < QC; ++q) g_l[q] = Num<T>::zero();
 #pragma unroll
   for (int d = 0; d < DB; ++d) g_A[d] = Num<T>::zero();
-  // dZ accumulates in shared memory: each row has a single owner in each phase
-  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) s.dz[i] = Num<T>::zero();
+  const T lsf = s.misc[0];
   __syncthreads();
 
-  for (int n = blockIdx.x; n < a.N; n += gridDim.x) {
-    point_dims<T, S>(a, s, n);
-    if (threadIdx.x >= 32 && threadIdx.x < 32 + D) {
-      int d = threadIdx.x - 32;
+  // each CTA takes a contiguous range of points, NPB at a time
+  const int nbeg = (int)((long)a.N * blockIdx.x / gridDim.x);
+  const int nend = (int)((long)a.N * (blockIdx.x + 1) / gridDim.x);
+  const int ia0 = threadIdx.x;   // the pseudo-input of this thread in the per-row phases (M <= NT)
+  for (int n0 = nbeg; n0 < nend; n0 += NPB) {
+    const int npts = min(NPB, nend - n0);
+    // ---- per-point constants and upstream gradients
+    for (int t = threadIdx.x; t < npts * Q; t += NT) {
+      const int pt = t / Q, q = t - pt * Q;
+      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, bslot(s, pt, M, Q), n0 + pt, q);
+    }
+    if (threadIdx.x >= 256 && threadIdx.x < 256 + npts * D) {
+      const int t = threadIdx.x - 256, pt = t / D, d = t - pt * D, n = n0 + pt;
       T dvv = a.b_stride ? Num<T>::c(1.f) : Num<T>::ld(a.dv[(size_t)n * D + d]);
       if (!a.dpsi1) {
         T mm = Num<T>::ld(a.m[(size_t)n * D + d]);
         T dmv = Num<T>::ld(a.dm[(size_t)n * D + d]);
-        s.pd[d] = sub(dmv, mul(scale2(dvv, 1), mm));     // dm_all
+        s.pg[pt * 2 * DMAX + d] = sub(dmv, mul(scale2(dvv, 1), mm));     // dm_all
       }
-      s.pd[DMAX + d] = dvv;
+      s.pg[pt * 2 * DMAX + DMAX + d] = dvv;
     }
     __syncthreads();
-    // ---- psi1 terms, one pseudo-input per thread (M <= NT)
-    T pv[2 * QC];     // per-point dmu, dS partials (psi1 part)
+    // ---- psi1 terms, one pseudo-input per thread for all the pass's points
+    // vals[pt]: dmu, dS (psi1 part, 2Q) then Rt, St (Q), Z2R (Q), ZS (Q) - reduced together
+    constexpr int KV = 5 * QC + 1;
+    T vals[NPB * KV];
 #pragma unroll
-    for (int i = 0; i < 2 * QC; ++i) pv[i] = Num<T>::zero();
-    const int ia0 = threadIdx.x;
+    for (int i = 0; i < NPB * KV; ++i) vals[i] = Num<T>::zero();
     if (ia0 < M) {
-      T p1 = point_rows<T, QC>(s, Q, ia0);
-      T dp1 = Num<T>::zero();
-      if (a.dpsi1) {
-        dp1 = Num<T>::ld(a.dpsi1[(size_t)n * M + ia0]);
-      } else {
 #pragma unroll
-        for (int d = 0; d < DB; ++d) {
-          if (d < D) {
-            dp1 = fma_(s.pd[d], Num<T>::ld(a.A[d * M + ia0]), dp1);
-            g_A[d] = fma_(s.pd[d], p1, g_A[d]);
-          }
-        }
-      }
-      T L1 = mul(dp1, p1);
-      g_sf = add(g_sf, L1);
+      for (int pt = 0; pt < NPB; ++pt) {
+        if (pt < npts) {
+          const int n = n0 + pt;
+          const PointSlot<T> ps = bslot(s, pt, M, Q);
+          const T* pg = s.pg + pt * 2 * DMAX;
+          T p1 = rows_of<T, QC>(s.z, lsf, s.tab, ps, Q, ia0);
+          T dp1 = Num<T>::zero();
+          if (a.dpsi1) {
+            dp1 = Num<T>::ld(a.dpsi1[(size_t)n * M + ia0]);
+          } else {
 #pragma unroll
-      for (int q = 0; q < QC; ++q) {
-        if (q < Q) {
-          T dd = sub(s.pmu[q], s.z[ia0 * Q + q]);
-          T ds = mul(dd, s.pis1[q]);                       // (mu - z)/s1
-          T ds2 = mul(ds, ds);
-          T L1ds = mul(L1, ds);
-          pv[q] = neg(L1ds);                               // dmu
-          pv[QC + q] = scale2(mul(L1, sub(ds2, s.pis1[q])), -1);   // dS
-          s.dz[ia0 * Q + q] = add(s.dz[ia0 * Q + q], L1ds);   // dZ (psi1)
-          g_l[q] = add(g_l[q], mul(L1, add(sub(s.il[q], s.pis1[q]), ds2)));   // 1/l - 1/s1 + d^2/s1^2
-        }
-      }
-    }
-    __syncthreads();
-    // ---- pairs: L = W psi2 -> shared memory; dB accumulation
-    T dvr[DB];
-#pragma unroll
-    for (int d = 0; d < DB; ++d) dvr[d] = d < D ? s.pd[DMAX + d] : Num<T>::zero();
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-      int p = threadIdx.x + k * NT;
-      if (p < P) {
-        int ia = pab[k] >> 16, ib = pab[k] & 0xffff;
-        T ps = pair_psi2<T, QC>(s, Q, p, ia, ib);
-        T w = Num<T>::zero();
-#pragma unroll
-        for (int d = 0; d < DB; ++d) {
-          if (d < D) {
-            T bb;
-            if (s.Bs) {
-              bb = s.Bs[d * P + p];
-            } else {
-              const S* Bd = a.B + (size_t)d * M * M + (size_t)n * a.b_stride;
-              bb = Num<T>::ld(Bd[ia * M + ib]);
-              if (ia != ib) bb = add(bb, Num<T>::ld(Bd[ib * M + ia]));
+            for (int d = 0; d < DB; ++d) {
+              if (d < D) {
+                dp1 = fma_(pg[d], Num<T>::ld(a.A[d * M + ia0]), dp1);
+                g_A[d] = fma_(pg[d], p1, g_A[d]);
+              }
             }
-            w = fma_(dvr[d], bb, w);
-            accB[k][d] = fma_(dvr[d], ps, accB[k][d]);
+          }
+          T L1 = mul(dp1, p1);
+          g_sf = add(g_sf, L1);
+#pragma unroll
+          for (int q = 0; q < QC; ++q) {
+            if (q < Q) {
+              T dd = sub(ps.pmu[q], s.z[ia0 * Q + q]);
+              T ds = mul(dd, ps.pis1[q]);                       // (mu - z)/s1
+              T ds2 = mul(ds, ds);
+              T L1ds = mul(L1, ds);
+              vals[pt * KV + q] = neg(L1ds);                    // dmu
+              vals[pt * KV + QC + q] = scale2(mul(L1, sub(ds2, ps.pis1[q])), -1);   // dS
+              s.dz[ia0 * Q + q] = add(s.dz[ia0 * Q + q], L1ds);  // dZ (psi1)
+              g_l[q] = add(g_l[q], mul(L1, add(sub(s.il[q], ps.pis1[q]), ds2)));   // 1/l - 1/s1 + d^2/s1^2
+            }
           }
         }
-        // L~ (half weight off the diagonal: the symmetric matrix entry)
-        T l = mul(w, ps);
-        s.L[p] = ia == ib ? l : scale2(l, -1);
       }
     }
     __syncthreads();
-    // ---- row sums, 8 threads per row
+    // ---- pairs: L = W psi2 -> shared memory; dBhat accumulates in shared memory (each
+    // pair has one owner thread)
+    T dvr[NPB][DB];
 #pragma unroll
-    for (int rk = 0; rk < 2; ++rk) {
-      int ia = rk * (NT / 8) + (threadIdx.x >> 3);
-      int sl = threadIdx.x & 7;
+    for (int pt = 0; pt < NPB; ++pt)
+#pragma unroll
+      for (int d = 0; d < DB; ++d)
+        dvr[pt][d] = (pt < npts && d < D) ? s.pg[pt * 2 * DMAX + DMAX + d] : Num<T>::zero();
+    for (int p = threadIdx.x; p < P; p += NT) {
+      int ia, ib;
+      pair_of(p, ia, ib);
+      const T gab = s.G[p];
+      T zb[QC];
+#pragma unroll
+      for (int q = 0; q < QC; ++q) zb[q] = q < Q ? s.z[ib * Q + q] : Num<T>::zero();
+      T bb[DB], ab[DB];
+#pragma unroll
+      for (int d = 0; d < DB; ++d) {
+        bb[d] = ab[d] = Num<T>::zero();
+        if (d < D) {
+          if (s.Bs) {
+            bb[d] = s.Bs[d * P + p];
+          } else {
+            const S* Bd = a.B + (size_t)d * M * M + (size_t)n0 * a.b_stride;
+            bb[d] = Num<T>::ld(Bd[ia * M + ib]);
+            if (ia != ib) bb[d] = add(bb[d], Num<T>::ld(Bd[ib * M + ia]));
+          }
+        }
+      }
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt) {
+        if (pt < npts) {
+          if (a.b_stride && pt > 0) {   // per-point B (Dout == 1): reload for this point
+            const S* Bd = a.B + (size_t)(n0 + pt) * a.b_stride;
+            bb[0] = Num<T>::ld(Bd[ia * M + ib]);
+            if (ia != ib) bb[0] = add(bb[0], Num<T>::ld(Bd[ib * M + ia]));
+          }
+          const T* hu = s.u + pt * M;
+          const T* hh = s.h + pt * M * Q + ia * Q;
+          T x = add(add(hu[ia], hu[ib]), gab);
+          T cr = Num<T>::zero();
+#pragma unroll
+          for (int q = 0; q < QC; ++q)
+            if (q < Q) cr = fma_(hh[q], zb[q], cr);
+          const T ps = exp_tab(sub(x, cr), s.tab);
+          T w = Num<T>::zero();
+#pragma unroll
+          for (int d = 0; d < DB; ++d) {
+            if (d < D) {
+              w = fma_(dvr[pt][d], bb[d], w);
+              ab[d] = fma_(dvr[pt][d], ps, ab[d]);
+            }
+          }
+          // L~ (half weight off the diagonal: the symmetric matrix entry)
+          const T l = mul(w, ps);
+          s.L[pt * P + p] = ia == ib ? l : scale2(l, -1);
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < DB; ++d) {
+        if (d < D) {
+          if (s.accB) {
+            s.accB[d * P + p] = add(s.accB[d * P + p], ab[d]);
+          } else if (a.dB) {   // no room for the accumulators: straight into dB
+            const double v = (double)Num<T>::st(ab[d]);
+            atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
+            if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- row sums, 8 threads per (point, row)
+    for (int rid0 = 0; rid0 < npts * M; rid0 += NT / 8) {
+      const int rid = rid0 + (threadIdx.x >> 3), sl = threadIdx.x & 7;
+      const int pt = rid / M, ia = rid - pt * M;
       T R = Num<T>::zero();
       T Sq[QC];
 #pragma unroll
       for (int q = 0; q < QC; ++q) Sq[q] = Num<T>::zero();
-      if (ia < M) {
+      if (rid < npts * M) {
+        const T* Lp = s.L + pt * P;
         const int rowbase = ia * (ia + 1) / 2;
         for (int ib = sl; ib < M; ib += 8) {
-          int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
-          T l = s.L[p];
+          const int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
+          const T l = Lp[p];
           R = add(R, l);
 #pragma unroll
           for (int q = 0; q < QC; ++q)
@@ -681,86 +699,83 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
         for (int q = 0; q < QC; ++q) Sq[q] = add(Sq[q], shfl_xor(Sq[q], m));
       }
-      if (ia < M && sl == 0) {
-        T* row = s.rows + ia * (1 + QMAX);
+      if (rid < npts * M && sl == 0) {
+        T* row = s.rows + (pt * M + ia) * (1 + QMAX);
         row[0] = R;
 #pragma unroll
-        for (int q = 0; q < QC; ++q) {
-          if (q < Q) {
-            row[1 + q] = Sq[q];
-            T zq = s.z[ia * Q + q];
-            T il = s.il[q];
-            T cq = s.pc[q];
-            // R(-z/l + 2 c mu - c z) + S (1/l - c)
-            T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, s.pmu[q]), 1)), mul(cq, zq));
-            s.dz[ia * Q + q] = add(s.dz[ia * Q + q], add(mul(R, t), mul(Sq[q], sub(il, cq))));
+        for (int q = 0; q < QC; ++q)
+          if (q < Q) row[1 + q] = Sq[q];
+      }
+    }
+    __syncthreads();
+    // ---- dZ from the row sums, and this row's share of the per-point totals
+    if (ia0 < M) {
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt) {
+        if (pt < npts) {
+          const PointSlot<T> ps = bslot(s, pt, M, Q);
+          const T* row = s.rows + (pt * M + ia0) * (1 + QMAX);
+          const T R = row[0];
+          vals[pt * KV + 2 * QC] = R;
+#pragma unroll
+          for (int q = 0; q < QC; ++q) {
+            if (q < Q) {
+              T zq = s.z[ia0 * Q + q];
+              T il = s.il[q];
+              T cq = ps.pc[q];
+              const T Sa = row[1 + q];
+              // R(-z/l + 2 c mu - c z) + S (1/l - c)
+              T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, ps.pmu[q]), 1)), mul(cq, zq));
+              s.dz[ia0 * Q + q] = add(s.dz[ia0 * Q + q], add(mul(R, t), mul(Sa, sub(il, cq))));
+              vals[pt * KV + 2 * QC + 1 + q] = Sa;                          // St
+              vals[pt * KV + 3 * QC + 1 + q] = mul(mul(zq, zq), R);         // Z2R
+              vals[pt * KV + 4 * QC + 1 + q] = mul(zq, Sa);                 // ZS
+            }
           }
         }
       }
     }
-    __syncthreads();
-    // ---- per-point totals (warp 0), combined with the psi1 partials
-    block_sum<T, 2 * QC>(pv, s.red);   // warp 0 holds the psi1 part of dmu, dS
+    // ---- per-point totals: one CTA reduction, then lane q of warp 0 finalises dimension q
+    block_sum<T, NPB * KV>(vals, s.red);
     if (threadIdx.x < 32) {
-      T Rt = Num<T>::zero();
-      T St[QC], Z2R[QC], ZS[QC];
 #pragma unroll
-      for (int q = 0; q < QC; ++q) St[q] = Z2R[q] = ZS[q] = Num<T>::zero();
-      for (int ia = threadIdx.x; ia < M; ia += 32) {
-        const T* row = s.rows + ia * (1 + QMAX);
-        Rt = add(Rt, row[0]);
+      for (int pt = 0; pt < NPB; ++pt) {
+        if (pt < npts) {
+          const int n = n0 + pt;
+          const PointSlot<T> ps = bslot(s, pt, M, Q);
+          const T Rt = vals[pt * KV + 2 * QC];
 #pragma unroll
-        for (int q = 0; q < QC; ++q) {
-          if (q < Q) {
-            T zq = s.z[ia * Q + q];
-            St[q] = add(St[q], row[1 + q]);
-            Z2R[q] = fma_(mul(zq, zq), row[0], Z2R[q]);
-            ZS[q] = fma_(zq, row[1 + q], ZS[q]);
+          for (int q = 0; q < QC; ++q) {
+            if (q < Q && q == (int)threadIdx.x) {
+              const T St = vals[pt * KV + 2 * QC + 1 + q], Z2R = vals[pt * KV + 3 * QC + 1 + q];
+              const T ZS = vals[pt * KV + 4 * QC + 1 + q];
+              T mu = ps.pmu[q], cq = ps.pc[q], il = s.il[q];
+              T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St), 1)), scale2(add(Z2R, ZS), -1));
+              T dmu = add(vals[pt * KV + q], mul(scale2(cq, 1), sub(St, mul(mu, Rt))));
+              T dS = add(vals[pt * KV + QC + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
+              // (dl / 2 ell) accumulates: Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 e2
+              T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R, ZS), mul(il, il)), -1)),
+                        mul(mul(cq, cq), e2));
+              g_l[q] = add(g_l[q], scale2(t, 1));
+              a.dmu[(size_t)n * Q + q] = Num<T>::st(dmu);
+              a.dvar[(size_t)n * Q + q] = Num<T>::st(dS);
+            }
           }
+          if (threadIdx.x == 0) g_sf = add(g_sf, scale2(Rt, 1));
         }
       }
-      Rt = warp_sum(Rt);
-#pragma unroll
-      for (int q = 0; q < QC; ++q) {
-        St[q] = warp_sum(St[q]);
-        Z2R[q] = warp_sum(Z2R[q]);
-        ZS[q] = warp_sum(ZS[q]);
-      }
-      if (threadIdx.x < Q) {
-        // lane q finalises dimension q (registers are indexed at compile time)
-#pragma unroll
-        for (int q = 0; q < QC; ++q) {
-          if (q == (int)threadIdx.x) {
-            T mu = s.pmu[q], cq = s.pc[q], il = s.il[q];
-            T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St[q]), 1)), scale2(add(Z2R[q], ZS[q]), -1));
-            T dmu = add(pv[q], mul(scale2(cq, 1), sub(St[q], mul(mu, Rt))));
-            T dS = add(pv[QC + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
-            // (dl / 2 ell) accumulates: Rt (1/(2l) - c/2) + (Z2R - ZS)/(2 l^2) + c^2 e2
-            T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R[q], ZS[q]), mul(il, il)), -1)),
-                      mul(mul(cq, cq), e2));
-            g_l[q] = add(g_l[q], scale2(t, 1));
-            a.dmu[(size_t)n * Q + q] = Num<T>::st(dmu);
-            a.dvar[(size_t)n * Q + q] = Num<T>::st(dS);
-          }
-        }
-      }
-      if (threadIdx.x == 0) g_sf = add(g_sf, scale2(Rt, 1));
     }
     __syncthreads();
   }
   // ---- flush CTA accumulators
-#pragma unroll
-  for (int k = 0; k < PPT; ++k) {
-    int p = threadIdx.x + k * NT;
-    if (p < P && a.dB) {
-      int ia = pab[k] >> 16, ib = pab[k] & 0xffff;
-#pragma unroll
-      for (int d = 0; d < DB; ++d) {
-        if (d < D) {
-          double v = (double)Num<T>::st(accB[k][d]);
-          atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
-          if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
-        }
+  if (a.dB && s.accB) {
+    for (int p = threadIdx.x; p < P; p += NT) {
+      int ia, ib;
+      pair_of(p, ia, ib);
+      for (int d = 0; d < D; ++d) {
+        const double v = (double)Num<T>::st(s.accB[d * P + p]);
+        atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
+        if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
       }
     }
   }
@@ -771,19 +786,19 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   }
   for (int i = threadIdx.x; i < M * Q; i += blockDim.x) atomicAdd(&a.dZ[i], (double)Num<T>::st(s.dz[i]));
   // dsf2 and dl need the ell / sf2 factors: (sum L1 + 2 sum L) / sf2 and ell * g_l
-  T vals[1 + QC];
-  vals[0] = g_sf;
+  T fin[1 + QC];
+  fin[0] = g_sf;
 #pragma unroll
-  for (int q = 0; q < QC; ++q) vals[1 + q] = g_l[q];
+  for (int q = 0; q < QC; ++q) fin[1 + q] = g_l[q];
   __syncthreads();
-  block_sum<T, 1 + QC>(vals, s.red);
+  block_sum<T, 1 + QC>(fin, s.red);
   if (threadIdx.x == 0) {
-    atomicAdd(a.dsf2, (double)Num<T>::st(div(vals[0], s.misc[1])));
+    atomicAdd(a.dsf2, (double)Num<T>::st(div(fin[0], s.misc[1])));
 #pragma unroll
     for (int q = 0; q < QC; ++q) {
       if (q < Q) {
         T ell = sqrt_(s.ell2[q]);
-        atomicAdd(&a.dl[q], (double)Num<T>::st(mul(vals[1 + q], ell)));
+        atomicAdd(&a.dl[q], (double)Num<T>::st(mul(fin[1 + q], ell)));
       }
     }
   }
@@ -837,41 +852,50 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   return fwd_variant<T, QMAX>(a, sum, contract, P, per_sm, sm, st);
 }
 
-template <typename T, int PPT, int DB, int QC>
-int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, int grid, size_t sm, cudaStream_t st) {
-  auto k = psi_bwd_kernel<T, PPT, DB, QC>;
+template <typename T, int NPB, int DB, int QC>
+int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t st) {
+  auto k = psi_bwd_kernel<T, NPB, DB, QC>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int grid = gpk::sm_count();
+  if (grid > a.N) grid = a.N;
+  if (grid < 1) return GPK_OK;
   k<<<grid, NT, sm, st>>>(a);
   return gpk::check_launch("psi_bwd");
 }
 
-template <typename T, int DB, int QC>
-int bwd_ppt(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t sm, cudaStream_t st) {
-  if (P <= 4 * NT) return run_bwd<T, 4, DB, QC>(a, grid, sm, st);
-  return run_bwd<T, 16, DB, QC>(a, grid, sm, st);
+template <typename T, int NPB, int QC>
+int bwd_db(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t st) {
+  if (a.Dout == 1) return run_bwd<T, NPB, 1, QC>(a, sm, st);
+  if (a.Dout == 2) return run_bwd<T, NPB, 2, QC>(a, sm, st);
+  return run_bwd<T, NPB, 4, QC>(a, sm, st);
 }
 
-template <typename T, int QC>
-int bwd_db(const PsiArgs<typename Num<T>::store_t>& a, int P, int grid, size_t sm, cudaStream_t st) {
-  if (a.Dout == 1) return bwd_ppt<T, 1, QC>(a, P, grid, sm, st);
-  if (a.Dout == 2) return bwd_ppt<T, 2, QC>(a, P, grid, sm, st);
-  return bwd_ppt<T, 4, QC>(a, P, grid, sm, st);
-}
-
+// points per pass: BWD_NPB when their tables fit in shared memory and the per-point sums
+// (NPB (5 Q + 1) values) fit one reduction; else one
+constexpr int BWD_NPB = 1;
 template <typename T>
 int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   PsiArgs<typename Num<T>::store_t> a = a_in;
   const int P = a.M * (a.M + 1) / 2;
-  a.bs_smem = a.b_stride == 0 && smem_bytes(a.M, a.Q, P, true, sizeof(T), a.Dout * P) <= 200 * 1024;
-  size_t sm = smem_bytes(a.M, a.Q, P, true, sizeof(T), a.bs_smem ? a.Dout * P : 0);
-  if (P > PPT_MAX * NT || sm > 227 * 1024)
-    return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d unsupported (M(M+1)/2 <= %d, i.e. M <= 127)", a.M,
-                     PPT_MAX * NT);
-  int grid = gpk::sm_count();
-  if (grid > a.N) grid = a.N;
-  if (grid < 1) return GPK_OK;
-  if (a.Q <= 2) return bwd_db<T, 2>(a, P, grid, sm, st);
-  return bwd_db<T, QMAX>(a, P, grid, sm, st);
+  if (a.M > NT) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d > %d", a.M, NT);
+  if (5 * (a.Q <= 2 ? 2 : QMAX) + 1 > RED) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: Q=%d too large", a.Q);
+  const size_t cap = 227 * 1024;
+  const int nbs = a.b_stride == 0 ? a.Dout * P : 0, nacc = a.Dout * P;
+  for (int npb = (a.Q <= 2 ? BWD_NPB : 1); npb >= 1; --npb) {
+    // preference: B and the dBhat accumulators both in shared memory, then without B, then
+    // without either (dBhat then accumulates with atomics in global memory)
+    const int opts[3][2] = {{nbs, nacc}, {0, nacc}, {0, 0}};
+    for (int o = 0; o < 3; ++o) {
+      const size_t sm = bwd_smem_bytes(a.M, a.Q, P, opts[o][1], npb, sizeof(T), opts[o][0]);
+      if (sm > cap) continue;
+      a.bs_smem = opts[o][0] > 0;
+      a.accb_smem = opts[o][1] > 0;
+      if (npb == 2) return bwd_db<T, 2, 2>(a, sm, st);
+      if (a.Q <= 2) return bwd_db<T, 1, 2>(a, sm, st);
+      return bwd_db<T, 1, QMAX>(a, sm, st);
+    }
+  }
+  return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d needs too much shared memory", a.M);
 }
 
 }  // namespace psi_impl

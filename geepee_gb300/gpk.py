@@ -153,6 +153,72 @@ def small_spd(A, Ainv=None, logdet=None, info=None):
          ptr(info), stream())
 
 
+class _GemmT(ctypes.Structure):
+    """gpk_gemm_t (include/gpk.h)."""
+    _fields_ = [('batch', ctypes.c_int), ('m', ctypes.c_int), ('n', ctypes.c_int), ('k', ctypes.c_int),
+                ('transA', ctypes.c_int), ('transB', ctypes.c_int), ('alpha', ctypes.c_double),
+                ('beta', ctypes.c_double), ('A', ctypes.c_void_p), ('lda', ctypes.c_int), ('strideA', ctypes.c_long),
+                ('B', ctypes.c_void_p), ('ldb', ctypes.c_int), ('strideB', ctypes.c_long), ('E', ctypes.c_void_p),
+                ('lde', ctypes.c_int), ('strideE', ctypes.c_long), ('C', ctypes.c_void_p), ('ldc', ctypes.c_int),
+                ('strideC', ctypes.c_long)]
+
+
+_GROUP = 8   # GPK_GEMM_GROUP
+
+
+class GemmGroup:
+    """Collects independent products (same arguments as gemm) and launches them together
+    (gpk_gemm_group) when the `with` block ends; outputs are allocated at collection time."""
+
+    def __init__(self):
+        self.items = []
+        self.keep = []
+
+    def __enter__(self):
+        return self
+
+    def mm(self, A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False, E=None):
+        A, B = A.contiguous(), B.contiguous()
+        a3 = A if A.dim() == 3 else A.unsqueeze(0)
+        b3 = B if B.dim() == 3 else B.unsqueeze(0)
+        batch = max(a3.shape[0], b3.shape[0])
+        m = a3.shape[2] if tA else a3.shape[1]
+        k = a3.shape[1] if tA else a3.shape[2]
+        n = b3.shape[1] if tB else b3.shape[2]
+        if (b3.shape[2] if tB else b3.shape[1]) != k:
+            raise ValueError('gemm: inner dimensions differ')
+        out3 = A.dim() == 3 or B.dim() == 3
+        if C is None:
+            C = torch.empty((batch, m, n) if out3 else (m, n), dtype=A.dtype, device=A.device)
+            if E is None:
+                beta = 0.0
+        g = _GemmT()
+        g.batch, g.m, g.n, g.k, g.transA, g.transB = batch, m, n, k, int(tA), int(tB)
+        g.alpha, g.beta = float(alpha), float(beta)
+        g.A, g.lda, g.strideA = ptr(a3), a3.shape[2], 0 if a3.shape[0] == 1 else a3.shape[1] * a3.shape[2]
+        g.B, g.ldb, g.strideB = ptr(b3), b3.shape[2], 0 if b3.shape[0] == 1 else b3.shape[1] * b3.shape[2]
+        Ee = C if E is None else E
+        g.E, g.lde = ptr(Ee), n
+        g.strideE = m * n if E is None else (0 if E.dim() == 2 or E.shape[0] == 1 else m * n)
+        g.C, g.ldc, g.strideC = ptr(C), n, m * n
+        self.items.append((prec_of(A.dtype), g))
+        self.keep += [A, B, C, Ee]
+        return C
+
+    def __exit__(self, *exc):
+        if exc[0] is None:
+            self.run()
+        return False
+
+    def run(self):
+        items, self.items = self.items, []
+        for i in range(0, len(items), _GROUP):
+            chunk = items[i:i + _GROUP]
+            arr = (_GemmT * len(chunk))(*[g for _, g in chunk])
+            call('gpk_gemm_group', chunk[0][0], len(chunk), ctypes.addressof(arr), stream())
+        self.keep = []
+
+
 def lincomb(out, terms=(), ranks=(), sum_batch=False, batch=None):
     """Fused float64 linear combination (gpk_lincomb):
         out[b] = sum_t c_t X_t[b] (X_t^T when transposed) + sum_r c_r u_r[b] v_r[b]^T

@@ -88,10 +88,19 @@ class DevLayer:
     def prep_kuu(self, out=None):
         """eta -> (R, theta_1, theta_2) and the jittered Kuu (base_models.py:630-658,454-463);
         Kuu is written into `out` when given."""
+        self.prep_r()
+        self.prep_th1()
+        return self.prep_k(out)
+
+    def prep_r(self):
         gpk.nat_prep(self.eta1, self.ls, self.sf, self.R_buf, self.lls2, self.lsf2)
         self.R = self.R_buf
-        self.th1 = mm(self.R, self.R, tA=True)
         self.th2 = self.eta2
+
+    def prep_th1(self, g=None):
+        self.th1 = (g.mm if g is not None else mm)(self.R, self.R, tA=True)
+
+    def prep_k(self, out=None):
         self.Kuu = gpk.kern(self.zu, self.zu, self.lls2, self.lsf2, jitter=JITTER, out=out)
         return self.Kuu
 
@@ -113,16 +122,42 @@ class DevLayer:
         return out
 
     def set_s_factors(self, inv, logdet):
+        """Posterior and cavity moments from the inverted Su^-1, Suhat^-1, then the cavity
+        tail; the products of each stage are launched together."""
+        with gpk.GemmGroup() as g:
+            self._s_stage1(inv, logdet, g)
+        with gpk.GemmGroup() as g:
+            self._s_stage2(g)
+        with gpk.GemmGroup() as g:
+            self._s_stage3(g)
+        self._s_stage4()
+
+    # the four stages of set_s_factors (setup_layers interleaves them across layers)
+    def _s_stage1(self, inv, logdet, g):
         D = self.Dout
         self.Su, self.Sh = inv[:D], inv[D:]
         self.ldSuinv = logdet[:D]
         self.ldShinv = logdet[D:]
         self.logdetSu = None   # -ldSuinv, formed only where a non-fused path needs it
         th2 = self.th2.unsqueeze(-1)
-        self.mu = mm(self.Su, th2).squeeze(-1)
-        self.mh = mm(self.Sh, th2, alpha=self.beta).squeeze(-1)
+        self._mu3 = g.mm(self.Su, th2)                     # mu = Su theta_2
+        self._mh3 = g.mm(self.Sh, th2, alpha=self.beta)    # muhat = Suhat beta theta_2
+
+    def _s_stage2(self, g):
+        self.mu, self.mh = self._mu3.squeeze(-1), self._mh3.squeeze(-1)
         self.Spmm = gpk.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
-        self._cavity_tail()
+        self.Smm_h = gpk.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
+        self._Ah3 = g.mm(self.Kinv, self._mh3)             # Ahat = K^-1 muhat
+        self._KS2 = g.mm(self.Kinv, self.Sh)
+
+    def _s_stage3(self, g):
+        self.Ah = self._Ah3.squeeze(-1)
+        # Bhat_det = K^-1 Suhat K^-1 - K^-1 (aep_models.py:536-546)
+        self.Bh_det = g.mm(self._KS2, self.Kinv, beta=-1.0, E=self.Kinv)
+
+    def _s_stage4(self):
+        # Bhat_sto = K^-1 (Suhat + mh mh^T) K^-1 - K^-1 = Bhat_det + Ahat Ahat^T
+        self.Bh_sto = gpk.lincomb(torch.empty_like(self.Bh_det), [(1.0, self.Bh_det)], [(1.0, self.Ah, self.Ah)])
 
     def setup_posterior(self):
         """update_hypers + compute_kuu + update_posterior (base_models.py:630-658,454-488)."""
@@ -264,32 +299,43 @@ class DevLayer:
 
     def bwd_mm_algebra(self, alpha):
         """The M x M part of backprop_grads_lvm_mm (aep_models.py:250-304): cavity,
-        natural-parameter and Kuu gradients."""
+        natural-parameter and Kuu gradients.  Products of one dependency level are launched
+        together; 2 dvcav muhat is formed as 2 (K^-1 dBhat) Ahat (K^-1 muhat = Ahat)."""
         N, M, D = self.N, self.M, self.Dout
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
         dAh, dBh = self._dAh, self._dBh
         K = self.Kinv
-        dvcav = mm(mm(K, dBh), K)
-        t = mm(dvcav, self.mh.unsqueeze(-1), alpha=2.0).squeeze(-1)
-        dmcav = mm(dAh, K, tB=True, beta=1.0, E=t)                       # 2 dvcav mh + dAh K^T
-        gpk.lincomb(dvcav, [(1.0, dvcav)], [(beta, dmcav, self.th2)])    # + beta dmcav th2^T
-        dvcavinv = mm(mm(self.Sh, dvcav), self.Sh, alpha=-1.0)
-        dth2 = mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta).squeeze(-1)
-        KS = mm(K, self.Smm_h)
-        T1 = mm(dAh, self.mh, tA=True)
-        T2 = mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
+        with gpk.GemmGroup() as g:
+            KdB = g.mm(K, dBh)
+            KS = g.mm(K, self.Smm_h)
+            T1 = g.mm(dAh, self.mh, tA=True)
+            U = g.mm(dAh, K, tB=True)
+        with gpk.GemmGroup() as g:
+            dvcav = g.mm(KdB, K)                                             # K^-1 dBhat K^-1
+            t = g.mm(KdB, self.Ah.unsqueeze(-1), alpha=2.0)                  # 2 dvcav muhat
+            T2 = g.mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
+        dmcav = gpk.lincomb(torch.empty_like(U), [(1.0, U), (1.0, t.reshape(D, M))])
+        gpk.lincomb(dvcav, [(1.0, dvcav)], [(beta, dmcav, self.th2)])        # + beta dmcav th2^T
+        with gpk.GemmGroup() as g:
+            SD = g.mm(self.Sh, dvcav)
+            dth2 = g.mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta)
+        dvcavinv = mm(SD, self.Sh, alpha=-1.0)
         # dK = sum_d dvcavinv + dAh^T mh + 2 sum_d KS^T dBh - sum_d dBh;
         # Minner = s_post sum Spmm + s_cav sum Smm_h - 2 dK
         Minner = gpk.lincomb(torch.empty_like(K), [(s_post, self.Spmm), (s_cav, self.Smm_h), (-2.0, dvcavinv),
                                                    (2.0, dBh), (-2.0, T2)], sum_batch=True, batch=D)
         dth1 = gpk.lincomb(torch.empty_like(dvcavinv), [(-0.5 * s_post, self.Spmm), (-0.5 * s_cav * beta, self.Smm_h),
                                                         (beta, dvcavinv)])
+        sym = gpk.lincomb(torch.empty_like(dth1), [(1.0, dth1), (1.0, dth1, True)])
+        with gpk.GemmGroup() as g:
+            KM = g.mm(K, Minner)
+            dR = g.mm(self.R, sym)
         # Mall = 1/2 (D K + K Minner K)
-        Mall = mm(mm(K, Minner), K, alpha=0.5, beta=0.5 * D, E=K)
+        Mall = mm(KM, K, alpha=0.5, beta=0.5 * D, E=K)
         self._finish_hyp(Mall)
-        self._pack_eta1(dth1, out=self.g['eta1_R'])
-        gpk.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2)])
+        gpk.triu_pack(dR, self.R, self.g['eta1_R'])
+        gpk.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2.reshape(D, M))])
 
     def _cav_grad_u(self, dmu, dSu):
         """compute_cav_grad_u (aep_models.py:548-586)."""
@@ -352,7 +398,8 @@ class DevLayer:
     def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x):
         """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
         compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so
-        that the eta1_R terms of the cavity and the posterior are packed once."""
+        that the eta1_R terms of the cavity and the posterior are packed once.  Products of
+        one dependency level are launched together."""
         N, M, D = self.N, self.M, self.Dout
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
@@ -364,33 +411,47 @@ class DevLayer:
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh)
         self._kernel_grads(self._dsf2, self._dl, dv)
         gpk.gram(kfu, kfu, dv, dBh)
+        with gpk.GemmGroup() as g:
+            Sinv_mh = g.mm(self.Shinv, self.mh.unsqueeze(-1))
+            Sinv_mu = g.mm(self.Suinv, self.mu.unsqueeze(-1))
+            KdB = g.mm(K, dBh)
+            KS = g.mm(K, self.Sh)
+            T1 = g.mm(dAh, self.mh, tA=True)
+            U = g.mm(dAh, K)
+        Sinv_mh, Sinv_mu = Sinv_mh.reshape(D, M), Sinv_mu.reshape(D, M)
         # cavity: dmucav = dAhat K^-1 + s_cav Suhat^-1 muhat (sum_n dm (kfu K^-1) = dAhat K^-1);
         # dSucav = K^-1 dBhat K^-1 + s_cav (Suhat^-1/2 - s s^T/2), plus the mean's beta dmucav th2^T
-        Sinv_mh = mm(self.Shinv, self.mh.unsqueeze(-1)).squeeze(-1)
-        dmucav = mm(dAh, K, beta=s_cav, E=Sinv_mh)
-        X = mm(mm(K, dBh), K)
+        dmucav = gpk.lincomb(torch.empty_like(U), [(1.0, U), (s_cav, Sinv_mh)])
+        with gpk.GemmGroup() as g:
+            X = g.mm(KdB, K)
+            T2 = g.mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
+            e2p = g.mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
         gpk.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
                     [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
-        dSinv_c = mm(mm(self.Sh, X), self.Sh, alpha=-1.0)
         # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
-        Sinv_mu = mm(self.Suinv, self.mu.unsqueeze(-1)).squeeze(-1)
         Y = gpk.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
                         [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
-        dSinv_p = mm(mm(self.Su, Y), self.Su, alpha=-1.0)
-        # d eta1_R = pack(beta dSinv_c + dSinv_p); d eta2 = beta Suhat dmucav + Su dmu
+        with gpk.GemmGroup() as g:
+            SX = g.mm(self.Sh, X)
+            SY = g.mm(self.Su, Y)
+            # d eta2 = beta Suhat dmucav + Su dmu
+            g.mm(self.Sh, dmucav.unsqueeze(-1), alpha=beta, beta=1.0, E=e2p, C=self.g['eta2'].view(D, M, 1))
+        with gpk.GemmGroup() as g:
+            dSinv_c = g.mm(SX, self.Sh, alpha=-1.0)
+            dSinv_p = g.mm(SY, self.Su, alpha=-1.0)
+        # d eta1_R = pack(beta dSinv_c + dSinv_p)
         dth1 = gpk.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (1.0, dSinv_p)])
-        self._pack_eta1(dth1, out=self.g['eta1_R'])
-        e2p = mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
-        mm(self.Sh, dmucav.unsqueeze(-1), alpha=beta, beta=1.0, E=e2p, C=self.g['eta2'].view(D, M, 1))
+        sym = gpk.lincomb(torch.empty_like(dth1), [(1.0, dth1), (1.0, dth1, True)])
         # Kuu^-1 gradient: dAhat^T muhat + 2 sum_d (K^-1 Suhat)^T dBhat - sum_d dBhat
         #                  + sum_d dSinv_c + sum_d dSinv_p - D/2 Kuu
-        KS = mm(K, self.Sh)
-        T1 = mm(dAh, self.mh, tA=True)
-        T2 = mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
         dK = gpk.lincomb(torch.empty_like(K), [(1.0, T2), (-1.0, dBh), (1.0, dSinv_c), (1.0, dSinv_p),
                                                (-0.5 * D, self.Kuu)], sum_batch=True, batch=D)
-        Minner = mm(mm(K, dK), K, alpha=-1.0)
+        with gpk.GemmGroup() as g:
+            dR = g.mm(self.R, sym)
+            KdK = g.mm(K, dK)
+        Minner = mm(KdK, K, alpha=-1.0)
         self._finish_hyp(Minner)
+        gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 
 
 def gauss_logZ(m, v, y, sn, alpha):
@@ -432,8 +493,13 @@ def setup_layers(layers, alpha):
         nS = sum(2 * l.Dout for l in group)
         info = torch.empty(G + nS, dtype=torch.int32, device=dev)
         K = torch.empty((G, M, M), dtype=F64, device=dev)
+        for l in group:
+            l.prep_r()
+        with gpk.GemmGroup() as g:
+            for l in group:
+                l.prep_th1(g)
         for i, l in enumerate(group):
-            l.prep_kuu(out=K[i])
+            l.prep_k(out=K[i])
         Kinv = torch.empty_like(K)
         ld = torch.empty(G, dtype=F64, device=dev)
         gpk.chol_inv(K, Kinv, None, ld, info[:G])
@@ -446,10 +512,19 @@ def setup_layers(layers, alpha):
         Sinv = torch.empty_like(S)
         lds = torch.empty(nS, dtype=F64, device=dev)
         gpk.chol_inv(S, Sinv, None, lds, info[G:])
-        o = 0
+        with gpk.GemmGroup() as g:
+            o = 0
+            for l in group:
+                n = 2 * l.Dout
+                l._s_stage1(Sinv[o:o + n], lds[o:o + n], g)
+                o += n
+        with gpk.GemmGroup() as g:
+            for l in group:
+                l._s_stage2(g)
+        with gpk.GemmGroup() as g:
+            for l in group:
+                l._s_stage3(g)
         for l in group:
-            n = 2 * l.Dout
-            l.set_s_factors(Sinv[o:o + n], lds[o:o + n])
-            o += n
+            l._s_stage4()
         statuses.append(info)
     return statuses

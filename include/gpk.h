@@ -137,6 +137,30 @@ int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB
                 const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
                 const void* E, int lde, long strideE, void* C, int ldc, long strideC, void* stream);
 
+/* One product of a gpk_gemm_group: the arguments of gpk_gemm_ex. */
+typedef struct {
+  int batch, m, n, k, transA, transB;
+  double alpha, beta;
+  const void* A;
+  int lda;
+  long strideA;
+  const void* B;
+  int ldb;
+  long strideB;
+  const void* E;
+  int lde;
+  long strideE;
+  void* C;
+  int ldc;
+  long strideC;
+} gpk_gemm_t;
+#define GPK_GEMM_GROUP 8
+
+/* Up to GPK_GEMM_GROUP independent gpk_gemm_ex products in one launch (the products of one
+ * dependency level of the AEP algebra, e.g. mu = Su theta_2 and muhat = beta Suhat theta_2 of
+ * every layer).  The outputs must not overlap each other or the inputs. */
+int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, void* stream);
+
 /* Batched SPD factorisation of A[b] (M x M, M <= 128): writes (each optional) the inverse
  * Ainv, the lower Cholesky factor L, logdet = log det A, and info[b] = 0 or the 1-based
  * pivot where A[b] stopped being positive definite (LAPACK potrf convention).

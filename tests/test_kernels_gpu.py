@@ -228,7 +228,8 @@ def test_det_layer_fwd_bwd_vs_oracle(N, M, D, Dout):
 
 
 def test_psi_size_limits_are_reported():
-    """Sizes beyond the register-resident pair tables are refused, not silently truncated."""
+    """Sizes beyond the register-resident pair tables (forward sum_n psi2) or beyond shared
+    memory (backward) are refused, not silently truncated."""
     from geepee_gb300 import gpk
     from geepee_gb300._lib import GpkError
     N, M, Q = 4, 128, 2
@@ -237,6 +238,8 @@ def test_psi_size_limits_are_reported():
     l2, s2 = z(Q), z(1)
     with pytest.raises(GpkError):
         gpk.psi_fwd(mu, S, Z, l2, s2, psi2_sum=z(M, M))
+    M = 200
+    Z = torch.randn(M, Q, dtype=torch.float64, device='cuda')
     with pytest.raises(GpkError):
         gpk.psi_bwd(mu, S, Z, l2, s2, z(1, M), z(1, M, M), z(N, 1), z(N, 1), z(N, 1), z(1), z(Q), z(M, Q),
                     z(1, M), z(1, M, M), z(N, Q), z(N, Q))
@@ -252,3 +255,26 @@ def test_double_split_is_exact():
     hi = A.astype(np.float32).astype(np.float64)
     lo = (A - hi).astype(np.float32).astype(np.float64)
     assert np.array_equal(C.cpu().numpy(), hi + lo)
+
+
+def test_gemm_group_matches_single_products():
+    """gpk_gemm_group: several independent products (different shapes, transposes,
+    batch broadcasting and addends) in one launch equal the one-at-a-time products."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(12)
+    K, S = dev(rng.randn(100, 100)), dev(rng.randn(3, 100, 100))
+    v, E = dev(rng.randn(3, 100, 1)), dev(rng.randn(100, 100))
+    a, b = dev(rng.randn(2, 100)), dev(rng.randn(2, 100))
+    with gpk.GemmGroup() as g:
+        c1 = g.mm(K, S)
+        c2 = g.mm(S, v, alpha=0.5)
+        c3 = g.mm(a, b, tA=True)
+        c4 = g.mm(S, K, beta=-1.0, E=E)
+        c5 = g.mm(S.reshape(300, 100), S.reshape(300, 100), tA=True, alpha=2.0, beta=1.0, E=E)
+    Kn, Sn, vn, En = (t.cpu().numpy() for t in (K, S, v, E))
+    an, bn = a.cpu().numpy(), b.cpu().numpy()
+    assert_close(c1.cpu().numpy(), Kn @ Sn, 1e-12)
+    assert_close(c2.cpu().numpy(), 0.5 * Sn @ vn, 1e-12)
+    assert_close(c3.cpu().numpy(), an.T @ bn, 1e-12)
+    assert_close(c4.cpu().numpy(), Sn @ Kn - En, 1e-12)
+    assert_close(c5.cpu().numpy(), 2.0 * Sn.reshape(300, 100).T @ Sn.reshape(300, 100) + En, 1e-12)
