@@ -131,58 +131,74 @@ __global__ void aep_phi_kernel(int D, int M, double N, double alpha, const doubl
   }
 }
 
-// Gaussian likelihood of one minibatch (lik_layers.py:119-181), one CTA:
+// Gaussian likelihood of one minibatch (lik_layers.py:119-181):
 //   vt = v + sn2/a, r = y - m;  logZ = sum(-1/2 (log(2 pi vt) + r^2/vt))
 //                                     + n D (1/2 log(2 pi sn2/a) - a/2 log(2 pi sn2))
 //   dm = scale r/vt,  dv = scale (-1/2/vt + 1/2 r^2/vt^2)
 //   energy = scale logZ / N,  g_sn = scale (sum(dv/scale) 2 sn2/a + n D (1 - a)) / N
-// dm and dv (the upstream gradients of the whole backward) are float64 with one division per
-// element; the logarithm, which only enters the energy, is the double-float one on the FP32
-// pipes (a float64 logarithm per element on one SM's FP64 units costs tens of microseconds).
-__global__ void __launch_bounds__(1024) gauss_lik_kernel(int n, int D, const double* m, const double* v,
-                                                         const double* y, const double* sn, double alpha,
-                                                         double scale, double invN, double* dm, double* dv,
-                                                         double* energy, double* g_sn) {
+// Two launches.  gauss_grad_kernel writes dm and dv (the upstream gradients of the whole
+// backward) in float64, one division per element, spread over many CTAs (GB300's float64
+// units are narrow, so per-element float64 work on one SM is slow).  gauss_sum_kernel (one
+// CTA) forms the two sums and the scalars in double-float on the FP32 pipes.
+__global__ void __launch_bounds__(128) gauss_grad_kernel(int nD, const double* m, const double* v, const double* y,
+                                                         const double* sn, double alpha, double scale, double* dm,
+                                                         double* dv) {
+  __shared__ double s_sn2a;
+  if (threadIdx.x == 0) s_sn2a = exp(2.0 * sn[0]) / alpha;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nD) return;
+  const double vt = v[i] + s_sn2a;
+  const double r = y[i] - m[i];
+  const double ivt = 1.0 / vt;
+  const double dmv = r * ivt;
+  dm[i] = scale * dmv;
+  dv[i] = scale * (0.5 * (r * dmv - 1.0) * ivt);   // -1/(2 vt) + r^2/(2 vt^2)
+}
+
+__global__ void __launch_bounds__(1024) gauss_sum_kernel(int n, int D, const double* m, const double* v,
+                                                         const double* y, const double* sn, const double* dv,
+                                                         double alpha, double scale, double invN, double* energy,
+                                                         double* g_sn) {
   __shared__ float2 tab[256];
-  __shared__ double red[2][32];
+  __shared__ df64 red[2][32];
   load_exp_table(tab);
   __syncthreads();
-  const double two_pi = 6.283185307179586;
-  const double sn2 = exp(2.0 * sn[0]);
-  const double sn2a = sn2 / alpha;
-  double sl = 0.0, sd = 0.0;
+  const df64 two_pi = df_from_double(6.283185307179586);
+  const df64 sn2 = exp_tab(scale2(df_from_double(sn[0]), 1), tab);
+  const df64 sn2a = div(sn2, df_from_double(alpha));
+  const df64 inv_scale = recip(df_from_double(scale));
+  df64 sl = make_df(0.f), sd = make_df(0.f);
   for (int i = threadIdx.x; i < n * D; i += blockDim.x) {
-    const double vt = v[i] + sn2a;
-    const double r = y[i] - m[i];
-    const double ivt = 1.0 / vt;
-    const double dmv = r * ivt;
-    const double r2v = r * dmv;                       // r^2 / vt
-    const double dvv = 0.5 * (r2v - 1.0) * ivt;       // -1/(2 vt) + r^2/(2 vt^2)
-    const double lg = df_to_double(log_tab(df_from_double(two_pi * vt), tab));
-    sl -= 0.5 * (lg + r2v);
-    sd += dvv;
-    dm[i] = scale * dmv;
-    dv[i] = scale * dvv;
+    const df64 vt = add(df_from_double(v[i]), sn2a);
+    const df64 r = sub(df_from_double(y[i]), df_from_double(m[i]));
+    sl = add(sl, add(log_tab(mul(two_pi, vt), tab), div(mul(r, r), vt)));
+    sd = add(sd, df_from_double(dv[i]));
   }
-  for (int k = 16; k > 0; k >>= 1) {
-    sl += __shfl_xor_sync(0xffffffffu, sl, k);
-    sd += __shfl_xor_sync(0xffffffffu, sd, k);
-  }
+  sl = warp_sum(sl);
+  sd = warp_sum(sd);
   if ((threadIdx.x & 31) == 0) {
     red[0][threadIdx.x >> 5] = sl;
     red[1][threadIdx.x >> 5] = sd;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    sl = sd = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      sl += red[0][k];
-      sd += red[1][k];
+  if (threadIdx.x < 32) {
+    sl = threadIdx.x < (blockDim.x >> 5) ? red[0][threadIdx.x] : make_df(0.f);
+    sd = threadIdx.x < (blockDim.x >> 5) ? red[1][threadIdx.x] : make_df(0.f);
+    sl = warp_sum(sl);
+    sd = warp_sum(sd);
+    if (threadIdx.x == 0) {
+      const df64 a_ = df_from_double(alpha);
+      const df64 nD = df_from_double((double)n * D);
+      const df64 l1 = log_tab(mul(two_pi, sn2a), tab), l2 = log_tab(mul(two_pi, sn2), tab);
+      // logZ = -sl/2 + nD (l1/2 - a l2/2)
+      const df64 logZ = add(scale2(neg(sl), -1), mul(nD, scale2(sub(l1, mul(a_, l2)), -1)));
+      const double sc = scale * invN;
+      energy[0] = sc * df_to_double(logZ);
+      // sum(dv) / scale * 2 sn2 / a + nD (1 - a)
+      const df64 t = add(mul(mul(sd, inv_scale), scale2(sn2a, 1)), mul(nD, sub(make_df(1.f), a_)));
+      g_sn[0] = sc * df_to_double(t);
     }
-    const double nD = (double)n * D;
-    const double logZ = sl + nD * (0.5 * log(two_pi * sn2 / alpha) - 0.5 * alpha * log(two_pi * sn2));
-    energy[0] = scale * logZ * invN;
-    g_sn[0] = scale * (sd * 2.0 * sn2 / alpha + nD * (1.0 - alpha)) * invN;
   }
 }
 
@@ -248,9 +264,11 @@ extern "C" int gpk_aep_phi(int D, int M, double N, double alpha, const double* l
 extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn,
                              double alpha, double scale, double invN, double* dm, double* dv, double* energy,
                              double* g_sn, void* stream) {
-  GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0, "gauss_lik: bad sizes");
+  GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0 && scale != 0.0, "gauss_lik: bad sizes");
   GPK_REQUIRE(m && v && y && sn && dm && dv && energy && g_sn, "gauss_lik: null pointer");
-  gauss_lik_kernel<<<1, 1024, 0, gpk::as_stream(stream)>>>(n, D, m, v, y, sn, alpha, scale, invN, dm, dv, energy,
-                                                           g_sn);
+  cudaStream_t st = gpk::as_stream(stream);
+  const int nD = n * D;
+  if (nD > 0) gauss_grad_kernel<<<(nD + 127) / 128, 128, 0, st>>>(nD, m, v, y, sn, alpha, scale, dm, dv);
+  gauss_sum_kernel<<<1, 1024, 0, st>>>(n, D, m, v, y, sn, dv, alpha, scale, invN, energy, g_sn);
   return gpk::check_launch("gauss_lik");
 }

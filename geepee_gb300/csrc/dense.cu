@@ -269,8 +269,9 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   // step k applies column k to the columns > k; the column k1 = k + 1 that its owner warp
   // finalises after updating it is written k1 = 32 KB + NW H + kk (KB, H compile-time), so
   // the owner's slots are compile-time indices too
-  static_assert(32 % NW == 0, "NW must divide 32");
+  static_assert(32 % NW == 0 && NW > 1, "NW must divide 32");
   bool stop = false;
+  int pend = -1;   // a column this warp still has to apply to its other columns
   static_for<0, RS>([&](auto KB) {
     static_for<0, 32 / NW>([&](auto H) {
       constexpr int kb = KB.value;
@@ -291,20 +292,43 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
         }
         const bool owner = w == kk;
         if (owner) {
+          // the critical path: column k1 only; the owner's other columns take column k at
+          // the next step (deferred), so the pivot is published as early as possible
           const T ljk = Ls[k * LD + k1];
 #pragma unroll
           for (int rr = kb; rr < RS; ++rr) a[rr][C1] = fma_(li[rr], ljk, a[rr][C1]);
           finalize(k1, std::integral_constant<int, C1>{}, KB);
-        }
+          pend = k;
+        } else {
+          if (pend >= 0) {   // this warp's deferred column (it owned the previous step)
+            T lp[RS];
 #pragma unroll
-        for (int cc = 0; cc < CS; ++cc) {
-          const int j = w + NW * cc;
-          if (j <= k || j >= M || (owner && cc == C1)) continue;   // warp-uniform
-          const T ljk = Ls[k * LD + j];
-          const int rj = j >> 5;
+            for (int rr = 0; rr < RS; ++rr) {
+              const int i = lane + 32 * rr;
+              lp[rr] = (i > pend && i < M) ? neg(Ls[pend * LD + i]) : Num<T>::zero();
+            }
 #pragma unroll
-          for (int rr = 0; rr < RS; ++rr)
-            if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+            for (int cc = 0; cc < CS; ++cc) {
+              const int j = w + NW * cc;
+              if (j <= pend + 1 || j >= M) continue;   // warp-uniform; column pend+1 had it
+              const T ljk = Ls[pend * LD + j];
+              const int rj = j >> 5;
+#pragma unroll
+              for (int rr = 0; rr < RS; ++rr)
+                if (rr >= rj) a[rr][cc] = fma_(lp[rr], ljk, a[rr][cc]);
+            }
+            pend = -1;
+          }
+#pragma unroll
+          for (int cc = 0; cc < CS; ++cc) {
+            const int j = w + NW * cc;
+            if (j <= k || j >= M) continue;   // warp-uniform
+            const T ljk = Ls[k * LD + j];
+            const int rj = j >> 5;
+#pragma unroll
+            for (int rr = 0; rr < RS; ++rr)
+              if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+          }
         }
         __syncthreads();
       }
