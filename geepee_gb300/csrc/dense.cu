@@ -557,55 +557,74 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
 //   d/dlog sf2 = sum_ab Mm_ab K_ab;  d/dlog l_q = 1/2 sum_ab Mm_ab K_ab (z_aq-z_bq)^2 / l_q
 //   d/dz_aq = sum_b (Mm_ab + Mm_ba) K_ab (z_bq - z_aq) / l_q
 // (geepee/kernels.py:447-475).  Results are ADDED, scaled: g_sf += s_sf * ., g_ls += s_ls * ., g_z += .
-template <typename T>
-__global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
-                                                        const typename Num<T>::store_t* Z, const double* lls2,
-                                                        const double* lsf2, double s_sf, double s_ls,
-                                                        double* g_sf, double* g_ls, double* g_z) {
-  // one warp per pseudo-input a (lanes over b), 8 rows per CTA
+constexpr int TKW = 4;    // rows (warps) per trace_kzz CTA
+constexpr int TKB = 8;    // b-values per lane kept in flight (M <= 32 * TKB without a second round)
+template <typename T, int QC>
+__global__ void __launch_bounds__(TKW * 32) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
+                                                             const typename Num<T>::store_t* Z, const double* lls2,
+                                                             const double* lsf2, double s_sf, double s_ls,
+                                                             double* g_sf, double* g_ls, double* g_z) {
+  // one warp per pseudo-input a (lanes over b); Z staged in shared memory; the row's Mm_ab and
+  // Mm_ba loads of a round are issued together before they are used
   typedef typename Num<T>::store_t S;
-  __shared__ float2 tab[256];
-  __shared__ T il[8], lsf;
-  __shared__ T red[8][9];
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  T* zs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M*Q]
+  __shared__ T il[QC], lsf;
+  __shared__ T red[TKW][1 + QC];
   load_exp_table(tab);
+  for (int i = threadIdx.x; i < M * Q; i += TKW * 32) zs[i] = Num<T>::ld(Z[i]);
   __syncthreads();
   if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
   if (threadIdx.x == 32) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int a = blockIdx.x * 8 + warp;
+  const int a = blockIdx.x * TKW + warp;
   T gs = Num<T>::zero();
-  T gl[8], gz[8];
+  T gl[QC], gz[QC];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) gl[q] = gz[q] = Num<T>::zero();
+  for (int q = 0; q < QC; ++q) gl[q] = gz[q] = Num<T>::zero();
   if (a < M) {
-    T za[8];
+    T za[QC];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) za[q] = q < Q ? Num<T>::ld(Z[a * Q + q]) : Num<T>::zero();
-    for (int b = lane; b < M; b += 32) {
-      T r = Num<T>::zero();
-      T d[8];
+    for (int q = 0; q < QC; ++q) za[q] = q < Q ? zs[a * Q + q] : Num<T>::zero();
+    for (int b0 = 0; b0 < M; b0 += 32 * TKB) {
+      S mab[TKB], mba[TKB];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        d[q] = q < Q ? sub(Num<T>::ld(Z[b * Q + q]), za[q]) : Num<T>::zero();   // z_b - z_a
-        if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
+      for (int u = 0; u < TKB; ++u) {
+        const int b = b0 + lane + 32 * u;
+        mab[u] = b < M ? Mm[(size_t)a * M + b] : S(0);
+        mba[u] = b < M ? Mm[(size_t)b * M + a] : S(0);
       }
-      T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
-      T mab = Num<T>::ld(Mm[(size_t)a * M + b]);
-      T w = mul(mab, k);
-      T ws = mul(add(mab, Num<T>::ld(Mm[(size_t)b * M + a])), k);
-      gs = add(gs, w);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < Q) {
-          T dil = mul(d[q], il[q]);
-          gl[q] = fma_(mul(w, d[q]), dil, gl[q]);
-          gz[q] = fma_(ws, dil, gz[q]);
+      for (int u = 0; u < TKB; ++u) {
+        const int b = b0 + lane + 32 * u;
+        if (b < M) {
+          T r = Num<T>::zero();
+          T d[QC];
+#pragma unroll
+          for (int q = 0; q < QC; ++q) {
+            d[q] = q < Q ? sub(zs[b * Q + q], za[q]) : Num<T>::zero();   // z_b - z_a
+            if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
+          }
+          const T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
+          const T m1 = Num<T>::ld(mab[u]);
+          const T w = mul(m1, k);
+          const T ws = mul(add(m1, Num<T>::ld(mba[u])), k);
+          gs = add(gs, w);
+#pragma unroll
+          for (int q = 0; q < QC; ++q) {
+            if (q < Q) {
+              const T dil = mul(d[q], il[q]);
+              gl[q] = fma_(mul(w, d[q]), dil, gl[q]);
+              gz[q] = fma_(ws, dil, gz[q]);
+            }
+          }
         }
       }
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < QC; ++q) {
       if (q < Q) {
         T v = warp_sum(gz[q]);
         if (lane == 0) atomicAdd(&g_z[a * Q + q], (double)Num<T>::st(v));
@@ -613,24 +632,27 @@ __global__ void __launch_bounds__(256) trace_kzz_kernel(int M, int Q, const type
     }
   }
   // reduce gs and gl over the CTA
-  T v[9];
+  T v[1 + QC];
   v[0] = gs;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) v[1 + q] = gl[q];
+  for (int q = 0; q < QC; ++q) v[1 + q] = gl[q];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) {
+  for (int i = 0; i < 1 + QC; ++i) {
     T t = warp_sum(v[i]);
     if (lane == 0) red[warp][i] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 9; ++i) {
+#pragma unroll
+    for (int i = 0; i < 1 + QC; ++i) {
       T t = red[0][i];
-      for (int w = 1; w < 8; ++w) t = add(t, red[w][i]);
+      for (int w = 1; w < TKW; ++w) t = add(t, red[w][i]);
       v[i] = t;
     }
     atomicAdd(g_sf, s_sf * (double)Num<T>::st(v[0]));
-    for (int q = 0; q < Q; ++q) atomicAdd(&g_ls[q], s_ls * 0.5 * (double)Num<T>::st(v[1 + q]));
+#pragma unroll
+    for (int q = 0; q < QC; ++q)
+      if (q < Q) atomicAdd(&g_ls[q], s_ls * 0.5 * (double)Num<T>::st(v[1 + q]));
   }
 }
 
@@ -955,22 +977,32 @@ extern "C" int gpk_spd_inv_static(int prec, int batch, int M, const void* A, voi
                           : spd_inv_small<float>(batch, M, A, Ainv, logdet, info, work, st);
 }
 
+template <typename T, int QC>
+int trace_launch(int M, int Q, const void* Mm, const void* Z, const double* lls2, const double* lsf2, double s_sf,
+                 double s_ls, double* g_sf, double* g_ls, double* g_z, cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  const size_t sm = 256 * sizeof(float2) + (size_t)M * Q * sizeof(T);
+  auto k = trace_kzz_kernel<T, QC>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<gpk::ceil_div(M, TKW), TKW * 32, sm, st>>>(M, Q, (const S*)Mm, (const S*)Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls,
+                                                 g_z);
+  return gpk::check_launch("trace_kzz");
+}
+
 extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
                              const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
                              void* stream) {
   GPK_REQUIRE(M >= 1 && Q >= 1 && Q <= 8, "trace_kzz: bad sizes M=%d Q=%d", M, Q);
+  GPK_REQUIRE((size_t)M * Q * 8 <= 200 * 1024, "trace_kzz: M*Q=%d too large", M * Q);
   GPK_REQUIRE(Mm && Z && lls2 && lsf2 && g_sf && g_ls && g_z, "trace_kzz: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
-  int grid = gpk::ceil_div(M, 8);
   if (prec == GPK_DF64)
-    trace_kzz_kernel<df64><<<grid, 256, 0, st>>>(M, Q, (const double*)Mm, (const double*)Z, lls2, lsf2, s_sf, s_ls,
-                                                 g_sf, g_ls, g_z);
-  else if (prec == GPK_FP32)
-    trace_kzz_kernel<float><<<grid, 256, 0, st>>>(M, Q, (const float*)Mm, (const float*)Z, lls2, lsf2, s_sf, s_ls,
-                                                  g_sf, g_ls, g_z);
-  else
-    return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);
-  return gpk::check_launch("trace_kzz");
+    return Q <= 2 ? trace_launch<df64, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st)
+                  : trace_launch<df64, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st);
+  if (prec == GPK_FP32)
+    return Q <= 2 ? trace_launch<float, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st)
+                  : trace_launch<float, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st);
+  return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);
 }
 
 extern "C" int gpk_small_spd(int prec, int batch, int n, const void* A, void* Ainv, double* logdet, int* info,

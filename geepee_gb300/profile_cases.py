@@ -11,6 +11,8 @@ Cases run one kernel of the deep-GP objective on its real input shapes:
   chol_m100     SPD Cholesky + inverse + logdet of one 100x100 Kuu, df64
   gemm_m100     one 100x100x100 df64 GEMM (the M x M algebra)
   det_fwd_dgp   deterministic layer forward, 1000 rows, D=8, M=100, Dout=2, df64
+  det_bwd_dgp   its backward (kfu derivatives, dAhat), df64
+  gram_dgp      dBhat = sum_n dv_n kfu_n kfu_n^T for the same rows, df64
   trace_m100    gradient of tr(M Kzz), M=100, Q=2, df64
   objective_dgp one full objective+gradient evaluation (eager, every kernel)
 With --time, prints the mean device time per launch (CUDA events).
@@ -78,6 +80,19 @@ def case(name):
         kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
         m, v = z(1000, 2), z(1000, 2)
         return lambda: gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, m, v)
+    if name in ('det_bwd_dgp', 'gram_dgp'):
+        rng = np.random.RandomState(0)
+        x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))
+        A, B = _d(rng.randn(2, 100)), _d(rng.randn(2, 100, 100))
+        l2, s2 = _d(np.zeros(8)), _d(np.zeros(1))
+        kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
+        gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, z(1000, 2), z(1000, 2))
+        dm, dv = _d(rng.randn(1000, 2)), _d(rng.randn(1000, 2))
+        if name == 'gram_dgp':
+            C = z(2, 100, 100)
+            return lambda: gpk.gram(kfu, kfu, dv, C)
+        bufs = (z(1), z(8), z(100, 8), z(2, 100))
+        return lambda: gpk.det_bwd(x, Z, l2, s2, A, kfu, Bk, dm, dv, *bufs)
     if name == 'trace_m100':
         rng = np.random.RandomState(0)
         Mm, Z = _d(rng.randn(100, 100)), _d(rng.randn(100, 2))

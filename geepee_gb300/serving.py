@@ -9,9 +9,10 @@ The server:
   * admits requests into a queue from any thread (``submit`` returns a Future);
   * a scheduler thread repeatedly takes everything queued, merges the requests of the same
     model into one batch (up to ``max_rows``), pads it to a power-of-two bucket and runs it
-    on one of ``n_streams`` CUDA streams as a captured CUDA graph (one graph per model, bucket
-    and stream slot, captured on first use): pinned H2D of the rows, the fused layer kernels,
-    D2H of the moments;
+    on one of ``n_streams`` CUDA streams as a captured CUDA graph: pinned H2D of the rows, the
+    fused layer kernels, D2H of the moments.  Graphs are kept per (model, bucket) in a small
+    pool of instances with their own buffers; any free instance runs on any free stream, and
+    ``warm`` captures them all before serving, so no capture ever happens on the serving path;
   * admission is by memory: at most ``budget_rows`` query rows are in flight; a request that
     arrives while others run is admitted as soon as a stream slot and budget free up, so work
     overlaps on the device;
@@ -73,7 +74,8 @@ class ResidentDGP:
 
 
 class _Slot:
-    """A captured predict graph with static, pinned-backed buffers for one bucket size."""
+    """A captured predict graph with static, pinned-backed buffers for one bucket size.  It is
+    captured on `stream` and replayed on whichever stream the scheduler picks."""
 
     def __init__(self, model, rows, din, dout, device, stream):
         self.rows = rows
@@ -104,13 +106,16 @@ class Request:
 
 
 class Server:
-    def __init__(self, models, n_streams=4, max_rows=4096, budget_rows=1 << 15, device=None):
+    def __init__(self, models, n_streams=4, max_rows=4096, budget_rows=1 << 15, device=None, instances=None):
         self.dev = device if device is not None else torch.device('cuda', torch.cuda.current_device())
         self.models = models
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(n_streams)]
+        self.capture_stream = torch.cuda.Stream(device=self.dev)
         self.max_rows = max_rows
         self.budget_rows = budget_rows
-        self.slots = {}                # (model, bucket, stream index) -> _Slot
+        # one instance per stream: a (model, bucket) can then run on every stream at once
+        self.instances = instances if instances is not None else n_streams
+        self.slots = {}                # (model, bucket) -> [_Slot, ...]
         self.queue = collections.deque()
         self.lock = threading.Lock()
         self.wake = threading.Event()
@@ -138,22 +143,30 @@ class Server:
         if self.thread is not None:
             self.thread.join()
 
+    def buckets(self):
+        return [1 << i for i in range(int(math.log2(self.max_rows)) + 1)]
+
     def warm(self, buckets=None):
-        """Capture every (model, bucket, stream) graph up front."""
-        buckets = buckets or [1 << i for i in range(int(math.log2(self.max_rows)) + 1)]
+        """Capture every (model, bucket) graph instance up front."""
         for mid in range(len(self.models)):
-            for b in buckets:
-                for si in range(len(self.streams)):
-                    self._slot(mid, b, si)
+            for b in (buckets or self.buckets()):
+                pool = self.slots.setdefault((mid, b), [])
+                while len(pool) < self.instances:
+                    pool.append(self._new_slot(mid, b))
         torch.cuda.synchronize()
 
     # ---------------------------------------------------------------- internals
-    def _slot(self, mid, bucket, si):
-        key = (mid, bucket, si)
-        s = self.slots.get(key)
-        if s is None:
-            m = self.models[mid]
-            s = self.slots[key] = _Slot(m, bucket, m.sizes[0], m.sizes[-1], self.dev, self.streams[si])
+    def _new_slot(self, mid, bucket):
+        m = self.models[mid]
+        return _Slot(m, bucket, m.sizes[0], m.sizes[-1], self.dev, self.capture_stream)
+
+    def _free_slot(self, mid, bucket):
+        pool = self.slots.setdefault((mid, bucket), [])
+        for s in pool:
+            if not s.busy:
+                return s
+        s = self._new_slot(mid, bucket)   # only when warm() did not cover this case
+        pool.append(s)
         return s
 
     def _free_stream(self):
@@ -186,7 +199,7 @@ class Server:
         rows = sum(r.x.shape[0] for r in reqs)
         si = self._free_stream()
         bucket = 1 << max(0, math.ceil(math.log2(rows)))
-        slot = self._slot(mid, bucket, si)
+        slot = self._free_slot(mid, bucket)
         stream = self.streams[si]
         hin = slot.h_in.numpy()
         o = 0
