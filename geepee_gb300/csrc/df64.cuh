@@ -24,7 +24,8 @@ __host__ __device__ __forceinline__ df64 make_df(float h, float l = 0.f) { df64 
 // integer operations on the bit pattern (round-to-nearest-even of the 53-bit significand to
 // 24 bits, then the signed remainder normalised to 24 bits): the FP64 pipe, which the plain
 // conversion would use, issues ~64x slower than the integer pipes on this part.  Zeros are
-// taken directly; exponents outside 2^-74 .. 2^127 (subnormals, inf, nan) take the FP64 path.
+// taken directly (lo may come out subnormal); values whose hi would not be a normal float
+// (|x| < 2^-126 or >= 2^128, inf, nan) take the FP64 path.
 // Kept out of line: inlined, the compiler if-converts the rare branch that calls it and runs
 // its FP64 instructions for every conversion.
 static __device__ __noinline__ df64 df_from_double_fp64(double x) {
@@ -36,7 +37,7 @@ __device__ __forceinline__ df64 df_from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
   if ((b << 1) == 0ull) return make_df(__int_as_float((int)(b >> 32)), 0.f);   // +-0
-  if (e < 949 || e > 1150) return df_from_double_fp64(x);
+  if (e < 897 || e > 1150) return df_from_double_fp64(x);   // hi would be subnormal / inf / nan
   const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
   unsigned top = (unsigned)(mant >> 29);
   int rem = (int)(mant & 0x1FFFFFFFull);
@@ -61,20 +62,37 @@ __device__ __forceinline__ df64 df_from_double(double x) {
     }
     const int nb = 32 - __clz(r);
     int sh = nb - 24;
-    unsigned m;
-    if (sh > 0) {
-      m = r >> sh;
-      const unsigned rem2 = r & ((1u << sh) - 1u), half = 1u << (sh - 1);
-      if (rem2 > half || (rem2 == half && (m & 1u))) ++m;
-      if (m == 0x1000000u) {
-        m >>= 1;
-        ++sh;
+    const unsigned ls = (sign ^ rs) << 31;
+    const int le0 = e - 1075 + sh + 23 + 127;   // lo's exponent field before rounding
+    if (le0 >= 1) {
+      unsigned m;
+      if (sh > 0) {
+        m = r >> sh;
+        const unsigned rem2 = r & ((1u << sh) - 1u), half = 1u << (sh - 1);
+        if (rem2 > half || (rem2 == half && (m & 1u))) ++m;
+        if (m == 0x1000000u) {
+          m >>= 1;
+          ++sh;
+        }
+      } else {
+        m = r << (-sh);
       }
+      const int le = e - 1075 + sh + 23 + 127;
+      lo = __uint_as_float(ls | ((unsigned)le << 23) | (m & 0x7fffffu));
     } else {
-      m = r << (-sh);
+      // subnormal lo: round the remainder once, straight to the subnormal's precision (a
+      // carry into bit 23 gives the smallest normal, which the bit pattern encodes as is)
+      const int t = sh + 1 - le0;
+      unsigned q = 0u;
+      if (t <= 0) {
+        q = r << (-t);
+      } else if (t < 32) {
+        q = r >> t;
+        const unsigned rr = r & ((1u << t) - 1u), hf = 1u << (t - 1);
+        if (rr > hf || (rr == hf && (q & 1u))) ++q;
+      }
+      lo = __uint_as_float(ls | q);
     }
-    const int le = e - 1075 + sh + 23 + 127;
-    lo = __uint_as_float(((sign ^ rs) << 31) | ((unsigned)le << 23) | (m & 0x7fffffu));
   }
   return make_df(hi, lo);
 }

@@ -196,8 +196,12 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
 //   dkfu_nb = sum_d dm_nd A_db + 2 sum_d dv_nd Bk_ndb,   L_nb = dkfu_nb kfu_nb
 //   dsf2 += sum L / sf2;  dl_q += sum L (x-z)^2 / l^{3/2};  dZ_bq += sum_n L (x_nq - z_bq)/l_q
 //   dA_db += sum_n dm_nd kfu_nb;   dx_nq = -sum_b L_nb (x_nq - z_bq)/l_q   (optional)
-template <typename T>
-__global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int Dout,
+// Threads are (b, row group): threadIdx.x is the pseudo-input b, threadIdx.y one of RG row
+// groups; a CTA takes a contiguous range of rows, RG at a time.  Per-b sums (dZ, dA) are
+// reduced over the row groups in shared memory and flushed with one atomic per CTA; dsf2 and
+// dl by one CTA reduction.
+template <typename T, int DC>
+__global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int Dout,
                                                       const typename Num<T>::store_t* x, int ldx,
                                                       const typename Num<T>::store_t* z, const double* lls2,
                                                       const double* lsf2, const typename Num<T>::store_t* A,
@@ -208,137 +212,147 @@ __global__ void __launch_bounds__(256) det_bwd_kernel(int N, int M, int D, int D
                                                       const typename Num<T>::store_t* dkfu, double* dsf2,
                                                       double* dl, double* dZ, double* dA,
                                                       typename Num<T>::store_t* dx) {
+  typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
-  T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));  // [D]
-  T* red = xs + DMAXK;                                                                // [32][64]
-  typedef typename Num<T>::store_t S;
+  const int RG = blockDim.y, XW = blockDim.x >> 5;
+  T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [RG][DC]
+  T* gv = xs + RG * DC;                      // [RG][2*DO_MAX]  dm_d, dv_d of the group's row
+  T* red = gv + RG * 2 * DO_MAX;             // [RG][XW][DC] (dx) / [RG][blockDim.x][DC+DO_MAX]
+  const int b = threadIdx.x, rg = threadIdx.y, lane = threadIdx.x & 31, xw = threadIdx.x >> 5;
+  const int tid = rg * blockDim.x + b, nth = blockDim.x * blockDim.y;
   load_exp_table(tab);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
-  __syncthreads();
-  const int b = threadIdx.x;  // one pseudo-input per thread (M <= blockDim)
-  T gsf = Num<T>::zero();
-  T gl[16];
-  T gz[16];
-  T ga[DO_MAX];
+  T zb[DC], gz[DC], gl[DC];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) gl[q] = gz[q] = Num<T>::zero();
+  for (int q = 0; q < DC; ++q) {
+    zb[q] = (b < M && q < D) ? Num<T>::ld(z[(size_t)b * D + q]) : Num<T>::zero();
+    gz[q] = gl[q] = Num<T>::zero();
+  }
+  T ab[DO_MAX], ga[DO_MAX];
 #pragma unroll
-  for (int d = 0; d < DO_MAX; ++d) ga[d] = Num<T>::zero();
-  T ab[DO_MAX];   // A[d, b], the same for every row
-#pragma unroll
-  for (int d = 0; d < DO_MAX; ++d)
+  for (int d = 0; d < DO_MAX; ++d) {
     ab[d] = (!dkfu && b < M && d < Dout) ? Num<T>::ld(A[(size_t)d * M + b]) : Num<T>::zero();
-  // the next row's inputs are loaded into registers while the current row is processed
-  S pk = S(0), pg = S(0), pdm[DO_MAX], pdv[DO_MAX], pbk[DO_MAX], px[DMAXK / 32];
-  auto fetch = [&](int n) {
-    if (b < M) {
-      pk = kfu[(size_t)n * M + b];
-      if (dkfu) pg = dkfu[(size_t)n * M + b];
-    }
-#pragma unroll
-    for (int d = 0; d < DO_MAX; ++d) {
-      const bool on = !dkfu && b < M && d < Dout;
-      pdm[d] = on ? dm[(size_t)n * Dout + d] : S(0);
-      pdv[d] = on ? dv[(size_t)n * Dout + d] : S(0);
-      pbk[d] = on ? Bk[((size_t)n * Dout + d) * M + b] : S(0);
-    }
-#pragma unroll
-    for (int t = 0; t < DMAXK / 32; ++t) {
-      const int q = threadIdx.x + 32 * t;
-      px[t] = (threadIdx.x < 32 && q < D) ? x[(size_t)n * ldx + q] : S(0);
-    }
-  };
-  if (blockIdx.x < N) fetch(blockIdx.x);
-  for (int n = blockIdx.x; n < N; n += gridDim.x) {
-    const T k = Num<T>::ld(pk);
-    T g = Num<T>::ld(pg);
-    T dmd[DO_MAX], dvd[DO_MAX], bk[DO_MAX];
-#pragma unroll
-    for (int d = 0; d < DO_MAX; ++d) {
-      dmd[d] = Num<T>::ld(pdm[d]);
-      dvd[d] = Num<T>::ld(pdv[d]);
-      bk[d] = Num<T>::ld(pbk[d]);
-    }
-    if (threadIdx.x < 32) {
-#pragma unroll
-      for (int t = 0; t < DMAXK / 32; ++t) {
-        const int q = threadIdx.x + 32 * t;
-        if (q < D) xs[q] = Num<T>::ld(px[t]);
+    ga[d] = Num<T>::zero();
+  }
+  T gsf = Num<T>::zero();
+  const int nbeg = (int)((long)N * blockIdx.x / gridDim.x), nend = (int)((long)N * (blockIdx.x + 1) / gridDim.x);
+  __syncthreads();
+  for (int n0 = nbeg; n0 < nend; n0 += RG) {
+    const int n = n0 + rg;
+    const bool row = n < nend;
+    if (row) {
+      if (b < D) xs[rg * DC + b] = Num<T>::ld(x[(size_t)n * ldx + b]);
+      if (!dkfu && b >= D && b < D + 2 * Dout) {   // D + 2 Dout <= 16 + 8 <= blockDim.x
+        const int t = b - D, d = t >> 1;
+        gv[rg * 2 * DO_MAX + t] = Num<T>::ld((t & 1) ? dv[(size_t)n * Dout + d] : dm[(size_t)n * Dout + d]);
       }
     }
     __syncthreads();
-    if (n + (int)gridDim.x < N) fetch(n + gridDim.x);
     T L = Num<T>::zero();
-    if (b < M) {
-      if (!dkfu) {
+    if (row && b < M) {
+      const T k = Num<T>::ld(kfu[(size_t)n * M + b]);
+      T g = Num<T>::zero();
+      if (dkfu) {
+        g = Num<T>::ld(dkfu[(size_t)n * M + b]);
+      } else {
 #pragma unroll
         for (int d = 0; d < DO_MAX; ++d) {
           if (d < Dout) {
-            g = fma_(dmd[d], ab[d], g);
-            g = fma_(scale2(dvd[d], 1), bk[d], g);
-            ga[d] = fma_(dmd[d], k, ga[d]);
+            const T dmd = gv[rg * 2 * DO_MAX + 2 * d], dvd = gv[rg * 2 * DO_MAX + 2 * d + 1];
+            g = fma_(dmd, ab[d], g);
+            g = fma_(scale2(dvd, 1), Num<T>::ld(Bk[((size_t)n * Dout + d) * M + b]), g);
+            ga[d] = fma_(dmd, k, ga[d]);
           }
         }
       }
       L = mul(g, k);
       gsf = add(gsf, L);
-      for (int q = 0; q < D && q < 16; ++q) {
-        T df = sub(xs[q], Num<T>::ld(z[(size_t)b * D + q]));
-        T t = mul(L, df);
-        gz[q] = fma_(t, h->inv_l2[q], gz[q]);
-        gl[q] = fma_(t, df, gl[q]);
+#pragma unroll
+      for (int q = 0; q < DC; ++q) {
+        if (q < D) {
+          const T df = sub(xs[rg * DC + q], zb[q]);
+          const T t = mul(L, df);
+          gz[q] = fma_(t, h->inv_l2[q], gz[q]);
+          gl[q] = fma_(t, df, gl[q]);
+        }
       }
     }
     if (dx) {
-      // dx_nq = -sum_b L (x - z)/l : CTA reduction per dimension
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-      for (int q = 0; q < D; ++q) {
-        T t = Num<T>::zero();
-        if (b < M) t = mul(L, mul(sub(xs[q], Num<T>::ld(z[(size_t)b * D + q])), h->inv_l2[q]));
-        t = warp_sum(t);
-        if (lane == 0) red[warp * 64 + (q & 63)] = t;
+      // dx_nq = -sum_b L (x_nq - z_bq) / l_q: warp sums over b, then over the group's warps
+#pragma unroll
+      for (int q = 0; q < DC; ++q) {
+        if (q < D) {
+          T t = (row && b < M) ? mul(L, mul(sub(xs[rg * DC + q], zb[q]), h->inv_l2[q])) : Num<T>::zero();
+          t = warp_sum(t);
+          if (lane == 0) red[(rg * XW + xw) * DC + q] = t;
+        }
       }
       __syncthreads();
-      if (warp == 0) {
-        for (int q = 0; q < D; ++q) {
-          T s = lane < nw ? red[lane * 64 + q] : Num<T>::zero();
-          s = warp_sum(s);
-          if (lane == 0) dx[(size_t)n * D + q] = Num<T>::st(neg(s));
-        }
+      if (row && b < D) {
+        T sacc = Num<T>::zero();
+        for (int w = 0; w < XW; ++w) sacc = add(sacc, red[(rg * XW + w) * DC + b]);
+        dx[(size_t)n * D + b] = Num<T>::st(neg(sacc));
       }
     }
     __syncthreads();
   }
-  if (b < M) {
-    for (int q = 0; q < D && q < 16; ++q) atomicAdd(&dZ[(size_t)b * D + q], (double)Num<T>::st(gz[q]));
-    if (dA && !dkfu)
-      for (int d = 0; d < Dout && d < DO_MAX; ++d) atomicAdd(&dA[(size_t)d * M + b], (double)Num<T>::st(ga[d]));
-  }
-  // dsf2 and dl: CTA reductions
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  T vals[17];
-  vals[0] = gsf;
+  // per-b sums over the row groups -> one atomic per CTA and (b, q) / (d, b)
+  T* pb = red;   // [RG][blockDim.x][DC + DO_MAX]
+  const int W = DC + DO_MAX;
 #pragma unroll
-  for (int q = 0; q < 16; ++q) vals[1 + q] = gl[q];
-  for (int i = 0; i < 17; ++i) {
-    T s = warp_sum(vals[i]);
-    if (lane == 0) red[warp * 64 + i] = s;
+  for (int q = 0; q < DC; ++q) pb[(rg * blockDim.x + b) * W + q] = gz[q];
+#pragma unroll
+  for (int d = 0; d < DO_MAX; ++d) pb[(rg * blockDim.x + b) * W + DC + d] = ga[d];
+  __syncthreads();
+  if (rg == 0 && b < M) {
+#pragma unroll
+    for (int q = 0; q < DC; ++q) {
+      if (q < D) {
+        T sacc = pb[b * W + q];
+        for (int r = 1; r < RG; ++r) sacc = add(sacc, pb[(r * blockDim.x + b) * W + q]);
+        atomicAdd(&dZ[(size_t)b * D + q], (double)Num<T>::st(sacc));
+      }
+    }
+    if (dA && !dkfu) {
+#pragma unroll
+      for (int d = 0; d < DO_MAX; ++d) {
+        if (d < Dout) {
+          T sacc = pb[b * W + DC + d];
+          for (int r = 1; r < RG; ++r) sacc = add(sacc, pb[(r * blockDim.x + b) * W + DC + d]);
+          atomicAdd(&dA[(size_t)d * M + b], (double)Num<T>::st(sacc));
+        }
+      }
+    }
   }
   __syncthreads();
-  if (warp == 0) {
-    for (int i = 0; i < 17; ++i) {
-      T s = lane < nw ? red[lane * 64 + i] : Num<T>::zero();
-      vals[i] = warp_sum(s);
-    }
-    if (lane == 0) {
+  // dsf2 and dl: CTA reduction (warp sums, then warp 0 of the CTA)
+  T vals[1 + DC];
+  vals[0] = gsf;
+#pragma unroll
+  for (int q = 0; q < DC; ++q) vals[1 + q] = gl[q];
+  const int wid = tid >> 5, nw = nth >> 5;
+  T* rw = red;   // [nw][1 + DC]
+#pragma unroll
+  for (int i = 0; i < 1 + DC; ++i) {
+    const T t = warp_sum(vals[i]);
+    if ((tid & 31) == 0) rw[wid * (1 + DC) + i] = t;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int i = 0; i < 1 + DC; ++i) vals[i] = warp_sum((tid & 31) < nw ? rw[(tid & 31) * (1 + DC) + i] : Num<T>::zero());
+    if (tid == 0) {
       atomicAdd(dsf2, (double)Num<T>::st(div(vals[0], h->sf2)));
-      for (int q = 0; q < D && q < 16; ++q) {
-        // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
-        T il = h->inv_l2[q];
-        atomicAdd(&dl[q], (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il)))));
+#pragma unroll
+      for (int q = 0; q < DC; ++q) {
+        if (q < D) {
+          // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
+          const T il = h->inv_l2[q];
+          atomicAdd(&dl[q], (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il)))));
+        }
       }
     }
   }
@@ -458,7 +472,10 @@ __global__ void __launch_bounds__(256) wsum_kernel(int N, int M, int Dout, const
 size_t det_fwd_smem(int M, int D, bool zstage, size_t tsz) {
   return 256 * 8 + sizeof(Hyp<df64>) + ((size_t)FT * M + FKA * FCB + 8 * DO_MAX * FT + FT * D + (zstage ? (size_t)M * D : 0)) * tsz;
 }
-size_t det_bwd_smem(size_t tsz) { return 256 * 8 + sizeof(Hyp<df64>) + (DMAXK + 32 * 64) * tsz; }
+size_t det_bwd_smem(int bx, int rg, int dc, size_t tsz) {
+  const size_t red = (size_t)rg * bx * (dc + DO_MAX);   // the largest of the three uses of the area
+  return 256 * 8 + sizeof(Hyp<df64>) + ((size_t)rg * dc + (size_t)rg * 2 * DO_MAX + red) * tsz;
+}
 
 template <typename T>
 int kern_launch(int N, int M, int D, const void* x, int ldx, const void* z, int ldz, const double* lls2,
@@ -525,19 +542,26 @@ extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* 
   GPK_REQUIRE(dkfu || (A && Bk && dm && dv), "det_bwd: need dkfu or (A, Bk, dm, dv)");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  int threads = M <= 128 ? 128 : 256;
-  int grid = N < gpk::sm_count() ? N : gpk::sm_count();
-  size_t smd = det_bwd_smem(sizeof(df64)), smf = det_bwd_smem(sizeof(float));
+  // threads: b (a multiple of 32 >= M) x row groups, 512 at most; CTAs of ~16 rows
+  const int bx = 32 * gpk::ceil_div(M, 32), rg = bx <= 128 ? 4 : 2;
+  int grid = gpk::ceil_div(N, 4 * rg);
+  if (grid > gpk::sm_count()) grid = gpk::sm_count();
+  const dim3 threads(bx, rg);
+  const int dc = D <= 8 ? 8 : 16;
   if (prec == GPK_DF64) {
-    det_bwd_kernel<df64><<<grid, threads, smd, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2,
-                                                     lsf2, (const double*)A, (const double*)kfu,
-                                                     (const double*)Bk, (const double*)dm, (const double*)dv, (const double*)dkfu, dsf2,
-                                                     dl, dZ, dA, (double*)dx);
+    const size_t sm = det_bwd_smem(bx, rg, dc, sizeof(df64));
+    auto k = dc == 8 ? det_bwd_kernel<df64, 8> : det_bwd_kernel<df64, 16>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
+                                 (const double*)A, (const double*)kfu, (const double*)Bk, (const double*)dm,
+                                 (const double*)dv, (const double*)dkfu, dsf2, dl, dZ, dA, (double*)dx);
   } else if (prec == GPK_FP32) {
-    det_bwd_kernel<float><<<grid, threads, smf, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2,
-                                                      lsf2, (const float*)A, (const float*)kfu, (const float*)Bk,
-                                                      (const float*)dm, (const float*)dv, (const float*)dkfu, dsf2, dl, dZ, dA,
-                                                      (float*)dx);
+    const size_t sm = det_bwd_smem(bx, rg, dc, sizeof(float));
+    auto k = dc == 8 ? det_bwd_kernel<float, 8> : det_bwd_kernel<float, 16>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
+                                 (const float*)kfu, (const float*)Bk, (const float*)dm, (const float*)dv,
+                                 (const float*)dkfu, dsf2, dl, dZ, dA, (float*)dx);
   } else {
     return gpk::fail(GPK_EINVAL, "det_bwd: unknown precision %d", prec);
   }

@@ -250,7 +250,9 @@ def test_double_split_is_exact():
     checked through gpk_gemm with an identity operand (C = A I reproduces A's df64 rounding)."""
     from geepee_gb300 import gpk
     rng = np.random.RandomState(0)
-    A = rng.randn(64, 64) * 10 ** rng.uniform(-20, 20, (64, 64))
+    # magnitudes down to 1e-37: lo subnormal (and, below 2^-126, the float64 fallback)
+    A = rng.randn(64, 64) * 10 ** rng.uniform(-37, 20, (64, 64))
+    A[0, :8] = [0.0, -0.0, 1e-40, -3e-39, 2.0 ** -126, 2.0 ** -100, 1.0 + 2.0 ** -40, -(2.0 ** 127)]
     C = gpk.gemm(dev(A), dev(np.eye(64)))
     hi = A.astype(np.float32).astype(np.float64)
     lo = (A - hi).astype(np.float32).astype(np.float64)
