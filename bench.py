@@ -429,17 +429,17 @@ def main():
     # oracle parity of the first timed step, and the CPU baseline (rank 0, N=1 only)
     from oracle import geepee_np as O
     e_ref, _ = O.sdgpr_objective(r['x'], r['y'], r['params'], ALPHA, idx=r['idx0'])
-    cpu = None
-    if world == 1:
-        rate, kind, n, dt = cpu_eval_rate(r['x'], r['y'], r['params'], [r['idx0']], args.cpu_seconds)
-        cpu = {'value': rate, 'unit': 'evals/s', 'cores': os.cpu_count(), 'kind': kind,
-               'sample': '%d objective+gradient evaluations (%.1f s) of the same workload' % (n, dt)}
     serving_out = None
     if args.serving_seconds > 0:
         try:
             serving_out = run_serving(args.serving_seconds, local)
         except Exception as exc:            # reported, never silently dropped
             serving_out = {'error': '%s: %s' % (type(exc).__name__, str(exc)[:300])}
+    cpu = None
+    if world == 1:
+        rate, kind, n, dt = cpu_eval_rate(r['x'], r['y'], r['params'], [r['idx0']], args.cpu_seconds)
+        cpu = {'value': rate, 'unit': 'evals/s', 'cores': os.cpu_count(), 'kind': kind,
+               'sample': '%d objective+gradient evaluations (%.1f s) of the same workload' % (n, dt)}
     line = {'metric': METRIC, 'value': r['value'], 'unit': 'evals/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': r['ms'], 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None,

@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import collections
 import concurrent.futures as cf
+import gc
 import math
 import threading
 import time
@@ -134,6 +135,11 @@ class Server:
         return r
 
     def start(self):
+        # objects alive now (models, graphs, the caller's state) leave the collector's
+        # scans: a full collection over a large host process otherwise stalls the
+        # dispatch loop for tens of milliseconds while it holds the interpreter lock
+        gc.collect()
+        gc.freeze()
         self.thread = threading.Thread(target=self._loop, daemon=True)
         self.thread.start()
 
@@ -142,6 +148,7 @@ class Server:
         self.wake.set()
         if self.thread is not None:
             self.thread.join()
+        gc.unfreeze()
 
     def buckets(self):
         return [1 << i for i in range(int(math.log2(self.max_rows)) + 1)]
