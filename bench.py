@@ -304,7 +304,10 @@ def run_ours(args, world, rank, local):
                                'MEASURED_PEAKS.json); no measured FP32 peak exists' % (n_sm, sm_mhz),
                 'work_per_launch': ops, 'us_per_launch': round(t_k * 1e6, 2),
                 'hbm_algorithmic_gbs': round(psi_bwd_bytes(MB, M_PSEUDO, HIDDEN, 1) / t_k / 1e9, 2),
-                'hbm_peak_gbs': peaks.get('hbm_gbs'), 'traffic': None}
+                'hbm_peak_gbs': peaks.get('hbm_gbs'),
+                # dram__bytes (read + write) of this launch in one ncu capture of the same case
+                # (profiles/psi_bwd_psi_bwd_dgp.md): the inputs and outputs stay in L2
+                'traffic': 350464, 'traffic_unit': 'bytes per launch'}
     out = {'e_gpu': e_gpu, 'e_fp64': e64, 'value': value, 'ms': 1e3 * t_dev / K,
            'e2e': e2e, 'fp64_rate': fp64_rate, 'n64': n64, 'roofline': roofline, 'clocks': clocks,
            'launches_per_eval': launches_per_eval, 'params': params, 'x': x, 'y': y,
