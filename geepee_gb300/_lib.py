@@ -42,6 +42,7 @@ _SIGS = {
                     ctypes.c_long, _vp, _c_int, ctypes.c_long, _c_dbl, _vp, _c_int, ctypes.c_long, _vp, _c_int,
                     ctypes.c_long, _vp],
     'gpk_gemm_group': [_c_int, _c_int, _vp, _vp],
+    'gpk_level': [_c_int, _c_int, _vp, _c_int, _vp, _vp],
     'gpk_chol_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_chol_inv_ws': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_spd_inv': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -50,6 +51,8 @@ _SIGS = {
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     'gpk_lincomb': [_vp, _vp],
     'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp],
+    'gpk_gather_rows': [_c_int, ctypes.c_longlong, _vp, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp],
+    'gpk_finish': [_c_int, _vp, _c_dbl, _c_int, _vp, _vp, _vp],
     'gpk_nat_prep': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_triu_pack': [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp],
     'gpk_hyp_grads': [_c_int, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],

@@ -226,15 +226,21 @@ class _PackedModel(Base_Model):
         keys = [k for k, _ in self.gpack.spec]
         return int(self.gpack.offsets[keys.index('sn')])
 
-    def _energy_terms(self, layers, alpha, N):
+    def _energy_terms(self, layers, alpha, N, statuses):
         """energy += sum of the layers' weighted log-partitions / N (fused for natural-parameter
-        layers); then the layer gradients are divided by N in one pass."""
+        layers); then one launch divides the layer gradients by N and, for a single status
+        buffer, records the worst Cholesky status."""
         for lay in layers:
             if lay.nat:
                 lay.phi(alpha, out=self.energy, w=1.0 / N)
             else:
                 self.energy.add_(lay.phi(alpha).reshape(1) / N)
-        self.gpack.dev[:self._layer_grad_span()].div_(N)
+        g = self.gpack.dev[:self._layer_grad_span()]
+        if len(statuses) == 1:
+            gpk.finish(g, N, statuses[0].reshape(-1), self.gpack.views['__info__'])
+        else:
+            gpk.finish(g, N)
+            self._flag_info(statuses)
 
     def _objective_host(self, idx, alpha):
         if idx is None:
@@ -291,8 +297,7 @@ class SGPR(_PackedModel):
         """Energy and gradients for minibatch rows `idx` (device int64, or None for all);
         everything stays on the device.  Results: self.energy, self.layer.g, self.g_sn."""
         lay, N = self.layer, self.N
-        xb = self.x_dev if idx is None else self.x_dev.index_select(0, idx)
-        yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
+        xb, yb = (self.x_dev, self.y_dev) if idx is None else gpk.gather_rows(idx, self.x_dev, self.y_dev)
         nb = yb.shape[0]
         scale = -N / nb / alpha
         st = setup_layers([lay], alpha)
@@ -300,8 +305,7 @@ class SGPR(_PackedModel):
         dm, dv = torch.empty_like(m), torch.empty_like(v)
         gpk.gauss_lik(m, v, yb, self.sn, alpha, scale, 1.0 / N, dm, dv, self.energy, self.g_sn)
         lay.bwd_det(alpha, dm, dv, kfu, Bk, xb)
-        self._energy_terms([lay], alpha, N)
-        self._flag_info(st)
+        self._energy_terms([lay], alpha, N, st)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
@@ -372,8 +376,7 @@ class SDGPR(_PackedModel):
     def device_objective(self, idx, alpha):
         """Device-resident energy+gradient (aep_models.py:895-988); see SGPR.device_objective."""
         N, L = self.N, self.L
-        xb = self.x_dev if idx is None else self.x_dev.index_select(0, idx)
-        yb = self.y_dev if idx is None else self.y_dev.index_select(0, idx)
+        xb, yb = (self.x_dev, self.y_dev) if idx is None else gpk.gather_rows(idx, self.x_dev, self.y_dev)
         nb = yb.shape[0]
         scale = -N / nb / alpha
         st = setup_layers(self.layers, alpha)
@@ -405,8 +408,7 @@ class SDGPR(_PackedModel):
                 forked.append(st_side)
         for st_side in forked:     # join only the branches forked here (graph-capture rule)
             main.wait_stream(st_side)
-        self._energy_terms(self.layers, alpha, N)
-        self._flag_info(st)
+        self._energy_terms(self.layers, alpha, N, st)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):

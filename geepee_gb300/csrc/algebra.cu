@@ -10,27 +10,7 @@
 namespace {
 
 __global__ void lincomb_kernel(gpk_lincomb_t d) {
-  const long per = (long)d.rows * d.cols;
-  const long total = d.sum_batch ? per : per * d.batch;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const long b0 = d.sum_batch ? 0 : e / per;
-    const long r = e - b0 * per;
-    const int i = (int)(r / d.cols), j = (int)(r - (long)i * d.cols);
-    const long rt = (long)j * d.cols + i;   // transposed element (square only)
-    const int bb = d.sum_batch ? 0 : (int)b0, be = d.sum_batch ? d.batch : (int)b0 + 1;
-    double acc = 0.0;
-    for (int t = 0; t < d.nterm; ++t) {
-      const bool once = d.sum_batch && d.sX[t] == 0;   // a batch-broadcast term enters a batch sum once
-      for (int b = once ? 0 : bb; b < (once ? 1 : be); ++b)
-        acc += d.cX[t] * d.X[t][b * d.sX[t] + (d.tX[t] ? rt : r)];
-    }
-    for (int t = 0; t < d.nrank; ++t) {
-      const bool once = d.sum_batch && d.su[t] == 0 && d.sv[t] == 0;
-      for (int b = once ? 0 : bb; b < (once ? 1 : be); ++b)
-        acc += d.cr[t] * d.u[t][b * d.su[t] + i] * d.v[t][b * d.sv[t] + j];
-    }
-    d.out[e] = acc;
-  }
+  lincomb_run(d, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
 }
 
 // R[d] (M x M): upper triangle from the packed eta1_R[d] (row-major triu order), exp() on the
@@ -211,16 +191,8 @@ int grid_for(long n) {
 }  // namespace
 
 extern "C" int gpk_lincomb(const gpk_lincomb_t* d, void* stream) {
-  GPK_REQUIRE(d && d->out, "lincomb: null descriptor or output");
-  GPK_REQUIRE(d->batch >= 1 && d->rows >= 0 && d->cols >= 0, "lincomb: bad shape");
-  GPK_REQUIRE(d->nterm >= 0 && d->nterm <= GPK_LC_TERMS && d->nrank >= 0 && d->nrank <= GPK_LC_RANK,
-              "lincomb: %d dense / %d rank-one terms (max %d / %d)", d->nterm, d->nrank, GPK_LC_TERMS, GPK_LC_RANK);
-  for (int t = 0; t < d->nterm; ++t) {
-    GPK_REQUIRE(d->X[t], "lincomb: null dense term %d", t);
-    GPK_REQUIRE(!d->tX[t] || d->rows == d->cols, "lincomb: transposed term %d needs a square shape", t);
-  }
-  for (int t = 0; t < d->nrank; ++t) GPK_REQUIRE(d->u[t] && d->v[t], "lincomb: null rank-one term %d", t);
-  const long n = (long)d->rows * d->cols * (d->sum_batch ? 1 : d->batch);
+  long n = 0;
+  if (const int rc = lincomb_check(d, &n)) return rc;
   if (n == 0) return GPK_OK;
   lincomb_kernel<<<grid_for(n), 256, 0, gpk::as_stream(stream)>>>(*d);
   return gpk::check_launch("lincomb");
@@ -271,4 +243,63 @@ extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, con
   if (nD > 0) gauss_grad_kernel<<<(nD + 127) / 128, 128, 0, st>>>(nD, m, v, y, sn, alpha, scale, dm, dv);
   gauss_sum_kernel<<<1, 1024, 0, st>>>(n, D, m, v, y, sn, dv, alpha, scale, invN, energy, g_sn);
   return gpk::check_launch("gauss_lik");
+}
+
+namespace {
+
+// d0[i,:] = s0[idx[i],:] (c0 columns) and d1[i,:] = s1[idx[i],:] (c1 columns) in one pass over
+// the n x (c0 + c1) outputs; an index outside [0, rows) gives a NaN row.
+__global__ void __launch_bounds__(256) gather_rows_kernel(int n, long long rows, const long long* idx, int c0,
+                                                          const double* s0, double* d0, int c1, const double* s1,
+                                                          double* d1) {
+  const int c = c0 + c1;
+  const long long total = (long long)n * c;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < total; e += (long long)gridDim.x * 256) {
+    const int i = (int)(e / c), j = (int)(e - (long long)i * c);
+    const long long r = idx[i];
+    const bool ok = r >= 0 && r < rows;
+    if (j < c0) d0[(size_t)i * c0 + j] = ok ? s0[(size_t)r * c0 + j] : __longlong_as_double(0x7ff8000000000000LL);
+    else d1[(size_t)i * c1 + (j - c0)] = ok ? s1[(size_t)r * c1 + (j - c0)] : __longlong_as_double(0x7ff8000000000000LL);
+  }
+}
+
+// g[0:span] /= divisor over all CTAs; CTA 0 also writes *worst = max(info[0:ninfo]).
+__global__ void __launch_bounds__(256) finish_kernel(int span, double* g, double divisor, int ninfo, const int* info,
+                                                     double* worst) {
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < span; i += gridDim.x * 256) g[i] /= divisor;
+  if (blockIdx.x != 0 || !worst) return;
+  __shared__ int wmax[8];
+  int v = 0;
+  for (int i = threadIdx.x; i < ninfo; i += 256) v = max(v, info[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) v = max(v, wmax[w]);
+    *worst = (double)v;
+  }
+}
+
+}  // namespace
+
+extern "C" int gpk_gather_rows(int n, long long rows, const long long* idx, int c0, const double* s0, double* d0,
+                               int c1, const double* s1, double* d1, void* stream) {
+  GPK_REQUIRE(n >= 0 && rows >= 0 && c0 >= 1 && c1 >= 0, "gather_rows: bad sizes n=%d c0=%d c1=%d", n, c0, c1);
+  GPK_REQUIRE(idx && s0 && d0 && (c1 == 0 || (s1 && d1)), "gather_rows: null pointer");
+  if (n == 0) return GPK_OK;
+  const long long total = (long long)n * (c0 + c1);
+  const int grid = (int)std::min<long long>((total + 255) / 256, (long long)gpk::sm_count() * 8);
+  gather_rows_kernel<<<grid, 256, 0, gpk::as_stream(stream)>>>(n, rows, idx, c0, s0, d0, c1, s1, d1);
+  return gpk::check_launch("gather_rows");
+}
+
+extern "C" int gpk_finish(int span, double* g, double divisor, int ninfo, const int* info, double* worst,
+                          void* stream) {
+  GPK_REQUIRE(span >= 0 && ninfo >= 0 && divisor != 0.0, "finish: bad sizes span=%d ninfo=%d", span, ninfo);
+  GPK_REQUIRE((span == 0 || g) && (ninfo == 0 || (info && worst)), "finish: null pointer");
+  const int grid = std::max(1, std::min((span + 255) / 256, gpk::sm_count()));
+  finish_kernel<<<grid, 256, 0, gpk::as_stream(stream)>>>(span, g, divisor, ninfo, ninfo ? info : nullptr,
+                                                          ninfo ? worst : nullptr);
+  return gpk::check_launch("finish");
 }

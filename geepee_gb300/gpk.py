@@ -166,13 +166,24 @@ class _GemmT(ctypes.Structure):
 _GROUP = 8   # GPK_GEMM_GROUP
 
 
+_LC_GROUP = 4   # GPK_LC_GROUP
+
+
 class GemmGroup:
-    """Collects independent products (same arguments as gemm) and launches them together
-    (gpk_gemm_group) when the `with` block ends; outputs are allocated at collection time."""
+    """Collects independent products (same arguments as gemm) and linear combinations (same
+    arguments as lincomb) and launches them together (gpk_level) when the `with` block ends;
+    outputs are allocated at collection time.  Members must not read each other's outputs."""
 
     def __init__(self):
         self.items = []
+        self.lcs = []
         self.keep = []
+
+    def lincomb(self, out, terms=(), ranks=(), sum_batch=False, batch=None):
+        d, keep = _lc_desc(out, terms, ranks, sum_batch, batch)
+        self.lcs.append(d)
+        self.keep += keep
+        return out
 
     def __enter__(self):
         return self
@@ -212,10 +223,16 @@ class GemmGroup:
 
     def run(self):
         items, self.items = self.items, []
-        for i in range(0, len(items), _GROUP):
-            chunk = items[i:i + _GROUP]
-            arr = (_GemmT * len(chunk))(*[g for _, g in chunk])
-            call('gpk_gemm_group', chunk[0][0], len(chunk), ctypes.addressof(arr), stream())
+        lcs, self.lcs = self.lcs, []
+        prec = items[0][0] if items else 0
+        i = j = 0
+        while i < len(items) or j < len(lcs):
+            chunk, lc = items[i:i + _GROUP], lcs[j:j + _LC_GROUP]
+            garr = (_GemmT * max(1, len(chunk)))(*[g for _, g in chunk])
+            larr = (_LC * max(1, len(lc)))(*lc)
+            call('gpk_level', prec, len(chunk), ctypes.addressof(garr), len(lc), ctypes.addressof(larr), stream())
+            i += len(chunk)
+            j += len(lc)
         self.keep = []
 
 
@@ -225,6 +242,13 @@ def lincomb(out, terms=(), ranks=(), sum_batch=False, batch=None):
     terms: (c, X) or (c, X, transpose) with X [B, rows, cols] or [rows, cols] (broadcast);
     ranks: (c, u, v) with u [B, rows] / [rows], v [B, cols] / [cols];
     out: [B, rows, cols], or [rows, cols] for B = 1 or when sum_batch sums over b."""
+    d, keep = _lc_desc(out, terms, ranks, sum_batch, batch)
+    call('gpk_lincomb', ctypes.addressof(d), stream())
+    return out
+
+
+def _lc_desc(out, terms, ranks, sum_batch, batch):
+    """The gpk_lincomb_t of a lincomb call and the tensors it points into."""
     rows, cols = out.shape[-2], out.shape[-1]
     if batch is None:
         batch = 1
@@ -255,8 +279,7 @@ def lincomb(out, terms=(), ranks=(), sum_batch=False, batch=None):
         d.su[i] = rows if (u.dim() == 2 and u.shape[0] > 1) else 0
         d.sv[i] = cols if (v.dim() == 2 and v.shape[0] > 1) else 0
     d.out = ptr(out)
-    call('gpk_lincomb', ctypes.addressof(d), stream())
-    return out
+    return d, keep
 
 
 def nat_prep(eta1, ls, sf, R, lls2, lsf2):
@@ -283,3 +306,27 @@ def gauss_lik(m, v, y, sn, alpha, scale, invN, dm, dv, energy, g_sn):
     n, D = y.shape
     call('gpk_gauss_lik', n, D, ptr(m), ptr(v), ptr(y), ptr(sn), float(alpha), float(scale), float(invN), ptr(dm),
          ptr(dv), ptr(energy), ptr(g_sn), stream())
+
+
+def gather_rows(idx, x, y=None):
+    """(x[idx], y[idx]) of row-major float64 device matrices in one launch (y optional)."""
+    n = idx.shape[0]
+    assert idx.dtype == torch.int64 and x.dtype == torch.float64 and x.is_contiguous()
+    xb = torch.empty((n, x.shape[1]), dtype=x.dtype, device=x.device)
+    if y is None:
+        call('gpk_gather_rows', n, x.shape[0], ptr(idx), x.shape[1], ptr(x), ptr(xb), 0, None, None, stream())
+        return xb, None
+    assert y.shape[0] == x.shape[0] and y.dtype == torch.float64 and y.is_contiguous()
+    yb = torch.empty((n, y.shape[1]), dtype=y.dtype, device=y.device)
+    call('gpk_gather_rows', n, x.shape[0], ptr(idx), x.shape[1], ptr(x), ptr(xb), y.shape[1], ptr(y), ptr(yb),
+         stream())
+    return xb, yb
+
+
+def finish(g, divisor, info=None, worst=None):
+    """g /= divisor in place (a contiguous float64 span); worst[0] = max(info) when info is given."""
+    assert g.dtype == torch.float64 and g.is_contiguous()
+    if info is not None:
+        assert info.dtype == torch.int32 and info.is_contiguous() and worst.dtype == torch.float64
+    call('gpk_finish', g.numel(), ptr(g), float(divisor), 0 if info is None else info.numel(),
+         None if info is None else ptr(info), None if info is None else ptr(worst), stream())

@@ -107,17 +107,18 @@ class DevLayer:
     def set_kuu_factors(self, Kinv, logdetK):
         self.Kinv, self.logdetK = Kinv, logdetK
 
-    def prep_s(self, alpha, out=None):
+    def prep_s(self, alpha, out=None, g=None):
         """The SPD matrices whose inverses the posterior and the cavity need:
         Su^-1 = Kuu^-1 + theta_1 and Suhat^-1 = Kuu^-1 + beta theta_1 (natural parameters),
-        stacked [2 Dout, M, M] (into `out` when given)."""
+        stacked [2 Dout, M, M] (into `out` when given; launched with group `g` when given)."""
         beta = (self.N - alpha) / self.N
         self.beta = beta
         D, M = self.Dout, self.M
         if out is None:
             out = torch.empty((2 * D, M, M), dtype=F64, device=self.dev)
-        gpk.lincomb(out[:D], [(1.0, self.Kinv), (1.0, self.th1)])
-        gpk.lincomb(out[D:], [(1.0, self.Kinv), (beta, self.th1)])
+        lc = g.lincomb if g is not None else gpk.lincomb
+        lc(out[:D], [(1.0, self.Kinv), (1.0, self.th1)])
+        lc(out[D:], [(1.0, self.Kinv), (beta, self.th1)])
         self.Suinv, self.Shinv = out[:D], out[D:]
         return out
 
@@ -145,8 +146,8 @@ class DevLayer:
 
     def _s_stage2(self, g):
         self.mu, self.mh = self._mu3.squeeze(-1), self._mh3.squeeze(-1)
-        self.Spmm = gpk.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
-        self.Smm_h = gpk.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
+        self.Spmm = g.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
+        self.Smm_h = g.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
         self._Ah3 = g.mm(self.Kinv, self._mh3)             # Ahat = K^-1 muhat
         self._KS2 = g.mm(self.Kinv, self.Sh)
 
@@ -155,9 +156,10 @@ class DevLayer:
         # Bhat_det = K^-1 Suhat K^-1 - K^-1 (aep_models.py:536-546)
         self.Bh_det = g.mm(self._KS2, self.Kinv, beta=-1.0, E=self.Kinv)
 
-    def _s_stage4(self):
+    def _s_stage4(self, g=None):
         # Bhat_sto = K^-1 (Suhat + mh mh^T) K^-1 - K^-1 = Bhat_det + Ahat Ahat^T
-        self.Bh_sto = gpk.lincomb(torch.empty_like(self.Bh_det), [(1.0, self.Bh_det)], [(1.0, self.Ah, self.Ah)])
+        lc = g.lincomb if g is not None else gpk.lincomb
+        self.Bh_sto = lc(torch.empty_like(self.Bh_det), [(1.0, self.Bh_det)], [(1.0, self.Ah, self.Ah)])
 
     def setup_posterior(self):
         """update_hypers + compute_kuu + update_posterior (base_models.py:630-658,454-488)."""
@@ -315,27 +317,33 @@ class DevLayer:
             dvcav = g.mm(KdB, K)                                             # K^-1 dBhat K^-1
             t = g.mm(KdB, self.Ah.unsqueeze(-1), alpha=2.0)                  # 2 dvcav muhat
             T2 = g.mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
-        dmcav = gpk.lincomb(torch.empty_like(U), [(1.0, U), (1.0, t.reshape(D, M))])
-        gpk.lincomb(dvcav, [(1.0, dvcav)], [(beta, dmcav, self.th2)])        # + beta dmcav th2^T
+        # dmcav = U + t, and dvcav += beta dmcav th2^T as beta (U + t) th2^T (one level)
+        t2 = t.reshape(D, M)
+        with gpk.GemmGroup() as g:
+            dmcav = g.lincomb(torch.empty_like(U), [(1.0, U), (1.0, t2)])
+            g.lincomb(dvcav, [(1.0, dvcav)], [(beta, U, self.th2), (beta, t2, self.th2)])
         with gpk.GemmGroup() as g:
             SD = g.mm(self.Sh, dvcav)
             dth2 = g.mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta)
         dvcavinv = mm(SD, self.Sh, alpha=-1.0)
         # dK = sum_d dvcavinv + dAh^T mh + 2 sum_d KS^T dBh - sum_d dBh;
-        # Minner = s_post sum Spmm + s_cav sum Smm_h - 2 dK
-        Minner = gpk.lincomb(torch.empty_like(K), [(s_post, self.Spmm), (s_cav, self.Smm_h), (-2.0, dvcavinv),
-                                                   (2.0, dBh), (-2.0, T2)], sum_batch=True, batch=D)
-        dth1 = gpk.lincomb(torch.empty_like(dvcavinv), [(-0.5 * s_post, self.Spmm), (-0.5 * s_cav * beta, self.Smm_h),
-                                                        (beta, dvcavinv)])
-        sym = gpk.lincomb(torch.empty_like(dth1), [(1.0, dth1), (1.0, dth1, True)])
+        # Minner = s_post sum Spmm + s_cav sum Smm_h - 2 dK;
+        # sym = dth1 + dth1^T, dth1 = -s_post/2 Spmm - s_cav beta/2 Smm_h + beta dvcavinv
+        a1, a2 = -0.5 * s_post, -0.5 * s_cav * beta
+        with gpk.GemmGroup() as g:
+            Minner = g.lincomb(torch.empty_like(K), [(s_post, self.Spmm), (s_cav, self.Smm_h), (-2.0, dvcavinv),
+                                                     (2.0, dBh), (-2.0, T2)], sum_batch=True, batch=D)
+            sym = g.lincomb(torch.empty_like(dvcavinv), [(a1, self.Spmm), (a1, self.Spmm, True), (a2, self.Smm_h),
+                                                         (a2, self.Smm_h, True), (beta, dvcavinv),
+                                                         (beta, dvcavinv, True)])
         with gpk.GemmGroup() as g:
             KM = g.mm(K, Minner)
             dR = g.mm(self.R, sym)
+            g.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2.reshape(D, M))])
         # Mall = 1/2 (D K + K Minner K)
         Mall = mm(KM, K, alpha=0.5, beta=0.5 * D, E=K)
         self._finish_hyp(Mall)
         gpk.triu_pack(dR, self.R, self.g['eta1_R'])
-        gpk.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2.reshape(D, M))])
 
     def _cav_grad_u(self, dmu, dSu):
         """compute_cav_grad_u (aep_models.py:548-586)."""
@@ -421,16 +429,16 @@ class DevLayer:
         Sinv_mh, Sinv_mu = Sinv_mh.reshape(D, M), Sinv_mu.reshape(D, M)
         # cavity: dmucav = dAhat K^-1 + s_cav Suhat^-1 muhat (sum_n dm (kfu K^-1) = dAhat K^-1);
         # dSucav = K^-1 dBhat K^-1 + s_cav (Suhat^-1/2 - s s^T/2), plus the mean's beta dmucav th2^T
-        dmucav = gpk.lincomb(torch.empty_like(U), [(1.0, U), (s_cav, Sinv_mh)])
+        # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
         with gpk.GemmGroup() as g:
             X = g.mm(KdB, K)
             T2 = g.mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
             e2p = g.mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
+            dmucav = g.lincomb(torch.empty_like(U), [(1.0, U), (s_cav, Sinv_mh)])
+            Y = g.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
+                          [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
         gpk.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
                     [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
-        # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
-        Y = gpk.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
-                        [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
         with gpk.GemmGroup() as g:
             SX = g.mm(self.Sh, X)
             SY = g.mm(self.Su, Y)
@@ -439,13 +447,14 @@ class DevLayer:
         with gpk.GemmGroup() as g:
             dSinv_c = g.mm(SX, self.Sh, alpha=-1.0)
             dSinv_p = g.mm(SY, self.Su, alpha=-1.0)
-        # d eta1_R = pack(beta dSinv_c + dSinv_p)
-        dth1 = gpk.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (1.0, dSinv_p)])
-        sym = gpk.lincomb(torch.empty_like(dth1), [(1.0, dth1), (1.0, dth1, True)])
+        # d eta1_R = pack(dth1 + dth1^T), dth1 = beta dSinv_c + dSinv_p;
         # Kuu^-1 gradient: dAhat^T muhat + 2 sum_d (K^-1 Suhat)^T dBhat - sum_d dBhat
         #                  + sum_d dSinv_c + sum_d dSinv_p - D/2 Kuu
-        dK = gpk.lincomb(torch.empty_like(K), [(1.0, T2), (-1.0, dBh), (1.0, dSinv_c), (1.0, dSinv_p),
-                                               (-0.5 * D, self.Kuu)], sum_batch=True, batch=D)
+        with gpk.GemmGroup() as g:
+            sym = g.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (beta, dSinv_c, True), (1.0, dSinv_p),
+                                                        (1.0, dSinv_p, True)])
+            dK = g.lincomb(torch.empty_like(K), [(1.0, T2), (-1.0, dBh), (1.0, dSinv_c), (1.0, dSinv_p),
+                                                 (-0.5 * D, self.Kuu)], sum_batch=True, batch=D)
         with gpk.GemmGroup() as g:
             dR = g.mm(self.R, sym)
             KdK = g.mm(K, dK)
@@ -505,10 +514,11 @@ def setup_layers(layers, alpha):
         gpk.chol_inv(K, Kinv, None, ld, info[:G])
         S = torch.empty((nS, M, M), dtype=F64, device=dev)
         o = 0
-        for i, l in enumerate(group):
-            l.set_kuu_factors(Kinv[i], ld[i:i + 1])
-            l.prep_s(alpha, out=S[o:o + 2 * l.Dout])
-            o += 2 * l.Dout
+        with gpk.GemmGroup() as g:
+            for i, l in enumerate(group):
+                l.set_kuu_factors(Kinv[i], ld[i:i + 1])
+                l.prep_s(alpha, out=S[o:o + 2 * l.Dout], g=g)
+                o += 2 * l.Dout
         Sinv = torch.empty_like(S)
         lds = torch.empty(nS, dtype=F64, device=dev)
         gpk.chol_inv(S, Sinv, None, lds, info[G:])
@@ -524,7 +534,8 @@ def setup_layers(layers, alpha):
         with gpk.GemmGroup() as g:
             for l in group:
                 l._s_stage3(g)
-        for l in group:
-            l._s_stage4()
+        with gpk.GemmGroup() as g:
+            for l in group:
+                l._s_stage4(g)
         statuses.append(info)
     return statuses

@@ -223,6 +223,14 @@ typedef struct {
 } gpk_lincomb_t;
 int gpk_lincomb(const gpk_lincomb_t* desc, void* stream);
 
+/* One dependency level of the AEP algebra in one launch: up to GPK_GEMM_GROUP products (as
+ * gpk_gemm_group) and up to GPK_LC_GROUP linear combinations (as gpk_lincomb), all independent
+ * of each other (no output read or written by another member).  E.g. the posterior moments
+ * Su + mu mu^T and Suhat + muhat muhat^T with the products K^-1 muhat and K^-1 Suhat
+ * (geepee/aep_models.py:536-546).  gpk_gemm_group is this call without linear combinations. */
+#define GPK_LC_GROUP 4
+int gpk_level(int prec, int ngemm, const gpk_gemm_t* gemms, int nlc, const gpk_lincomb_t* lincombs, void* stream);
+
 /* q(u) unpacking for a natural-parameter layer: R[d] = upper triangle of the packed
  * eta1_R[d] (row-major np.triu_indices order) with exp() on the diagonal, zeros below;
  * lls2 = 2 ls, lsf2 = 2 sf.  (geepee/base_models.py:630-658 update_hypers.) */
@@ -254,6 +262,18 @@ int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, con
  * - alpha log(2 pi sn2)/2). */
 int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn, double alpha,
                   double scale, double invN, double* dm, double* dv, double* energy, double* g_sn, void* stream);
+
+/* Minibatch rows of two row-major float64 arrays in one launch, x[idx] and y[idx] of
+ * geepee/aep_models.py:912-916 (rows = the arrays' row count): d0[i,:] = s0[idx[i],:] with c0
+ * columns and d1[i,:] = s1[idx[i],:] with c1 columns (c1 = 0: none).  An index outside
+ * [0, rows) gives a NaN row. */
+int gpk_gather_rows(int n, long long rows, const long long* idx, int c0, const double* s0, double* d0, int c1,
+                    const double* s1, double* d1, void* stream);
+
+/* The end of an objective evaluation: g[0:span] /= divisor (grad_all[key] /= N,
+ * geepee/aep_models.py:663-665, 984-986) and *worst = max(info[0:ninfo]) as a double (0, or a
+ * failing Cholesky pivot of the evaluation's factorisations). */
+int gpk_finish(int span, double* g, double divisor, int ninfo, const int* info, double* worst, void* stream);
 
 /* Gradient of tr(Mm Kzz), Kzz = K(Z, Z) without jitter, w.r.t. log sf^2, log ell^2 and Z,
  * added with scales: g_sf += s_sf * d/dlog sf^2, g_ls += s_ls * d/dlog ell^2, g_z += d/dZ.
