@@ -57,9 +57,10 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
 #pragma unroll
     for (int c = 0; c < R; ++c) acc[r][c] = Num<T>::zero();
   for (int k0 = 0; k0 < k; k0 += KC) {
-    const int kc = min(KC, k - k0), ne = kc * TBM;
-    // element e of a tile: (ii, kk) of op(A) / (kk, jj) of op(B); consecutive threads take
-    // consecutive memory
+    const int kc = min(KC, k - k0);
+    // element e < TBM * KC of a tile: (ii, kk) of op(A) / (kk, jj) of op(B), with the
+    // compile-time extents TBM and KC as divisors; consecutive threads take consecutive
+    // memory, and elements with kk >= kc are skipped
     S ra[NPT], rb[NPT];
     int oa[NPT], ob[NPT];
 #pragma unroll
@@ -67,25 +68,27 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
       const int e = threadIdx.x + u * NT;
       ra[u] = rb[u] = S(0);
       oa[u] = ob[u] = -1;
-      if (e < ne) {
-        int kk, ii;
-        if (tA) { kk = e / TBM; ii = e - kk * TBM; } else { ii = e / kc; kk = e - ii * kc; }
-        const int gi = i0 + ii, gk = k0 + kk;
-        oa[u] = kk * TBM + ii;
-        if (gi < m) ra[u] = tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
-        int jj;
-        if (tB) { jj = e / kc; kk = e - jj * kc; } else { kk = e / TBM; jj = e - kk * TBM; }
-        const int gj = j0 + jj, gk2 = k0 + kk;
-        ob[u] = kk * TBM + jj;
-        if (gj < n) rb[u] = tB ? B[(size_t)gj * ldb + gk2] : B[(size_t)gk2 * ldb + gj];
+      {
+        const int kk = tA ? e / TBM : e % KC, ii = tA ? e % TBM : e / KC;
+        if (kk < kc) {
+          const int gi = i0 + ii, gk = k0 + kk;
+          oa[u] = kk * TBM + ii;
+          if (gi < m) ra[u] = tA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
+        }
+      }
+      {
+        const int kk = tB ? e % KC : e / TBM, jj = tB ? e / KC : e % TBM;
+        if (kk < kc) {
+          const int gj = j0 + jj, gk = k0 + kk;
+          ob[u] = kk * TBM + jj;
+          if (gj < n) rb[u] = tB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
+        }
       }
     }
 #pragma unroll
     for (int u = 0; u < NPT; ++u) {
-      if (oa[u] >= 0) {
-        As[oa[u]] = P2 ? pair_bits<T>(ra[u]) : Num<T>::ld(ra[u]);
-        Bs[ob[u]] = P2 ? pair_bits<T>(rb[u]) : Num<T>::ld(rb[u]);
-      }
+      if (oa[u] >= 0) As[oa[u]] = P2 ? pair_bits<T>(ra[u]) : Num<T>::ld(ra[u]);
+      if (ob[u] >= 0) Bs[ob[u]] = P2 ? pair_bits<T>(rb[u]) : Num<T>::ld(rb[u]);
     }
     __syncthreads();
 #pragma unroll 4
@@ -214,13 +217,40 @@ __device__ __forceinline__ void static_for(F&& f) {
   }
 }
 
+// mbarriers in shared memory (CTA scope): init with an arrival count; arrive (release);
+// wait for phase 0 to complete (acquire), bounded: false after ~2^31 SM cycles
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  const long long t0 = clock64();
+  while (clock64() - t0 < (1LL << 31)) {   // about one second at the SM clock
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Right-looking Cholesky of one M x M SPD matrix per CTA (M <= min(32*RS, NW*CS)).  Element
 // (i, j) of the lower triangle lives in a register of lane i % 32 of warp j % NW (slot
 // [i/32][j/NW]), so a trailing update touches no shared memory except the column of L it
-// reads.  One barrier per column: while the other warps apply column k, the warp owning column
-// k+1 updates that column first, takes its pivot and publishes column k+1 of L (one-column
-// look-ahead).  Outputs: Lw (column-major L as raw (hi, lo) pairs, 1/L_kk on the diagonal -
-// the input of trinv_kernel), logdet = 2 sum log L_kk, info[b] = k+1 for a non-positive pivot.
+// reads.  Column k of L is published by its owner warp through an mbarrier of its own (32
+// arrivals); a warp waits only for the column it applies next, so there is no CTA barrier in
+// the loop.  The warp owning column k+1 applies column k to it first, takes its pivot and
+// publishes it before updating its other columns.  Outputs: Lw (column-major L as raw (hi, lo)
+// pairs, 1/L_kk on the diagonal - the input of trinv_kernel), logdet = sum log L_kk^2,
+// info[b] = k+1 for a non-positive pivot (M+1 if a bounded wait ran out, never expected).
 template <typename T, int RS, int CS, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typename Num<T>::store_t* A, long sA,
                                                                 T* Lw, double* logdet, int* info) {
@@ -231,7 +261,8 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   T* Ls = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][LD], column k at Ls + k*LD
   T* dg = Ls + (size_t)M * LD;                                       // [M] L_kk
   T* red = dg + M;                                                   // [NW]
-  __shared__ int s_info;
+  __shared__ int s_info, s_err;
+  __shared__ __align__(8) unsigned long long s_bar[32 * RS];   // column k published (32 arrivals)
   const int b = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int NTH = NW * 32;
   A += b * sA;
@@ -248,7 +279,8 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     asm volatile("cp.async.wait_all;\n" ::);
   }
   load_exp_table(tab);
-  if (threadIdx.x == 0) s_info = 0;
+  if (threadIdx.x == 0) s_info = s_err = 0;
+  for (int k = threadIdx.x; k < M; k += NTH) mbar_init(&s_bar[k], 32);
   __syncthreads();
   T a[RS][CS];
   {
@@ -269,6 +301,10 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     const T p = shfl_idx(a[RK.value][CK.value], k & 31);
     if (!(Num<T>::approx(p) > 0.f)) {
       if (lane == 0) s_info = k + 1;
+      __syncwarp();
+      // complete every remaining column's barrier: warps already waiting further on wake,
+      // see s_info and stop (no later column is published after a failure)
+      for (int c = k; c < M; ++c) mbar_arrive(&s_bar[c]);
       return;
     }
     const T r = rsqrt_(p);   // 1 / L_kk
@@ -281,16 +317,19 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
       Ls[k * LD + k] = r;
       dg[k] = p;   // L_kk^2
     }
+    __syncwarp();
+    mbar_arrive(&s_bar[k]);   // every lane arrives: each releases its own stores of column k
   };
 
   if (w == 0) finalize(0, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
-  __syncthreads();
   // step k applies column k to the columns > k; the column k1 = k + 1 that its owner warp
   // finalises after updating it is written k1 = 32 KB + NW H + kk (KB, H compile-time), so
-  // the owner's slots are compile-time indices too
+  // the owner's slots are compile-time indices too.  No CTA barrier: a warp waits only for the
+  // column it applies (its mbarrier), so warps drift apart and the owner of column k1 publishes
+  // it as soon as column k has reached it.
   static_assert(32 % NW == 0 && NW > 1, "NW must divide 32");
-  bool stop = false;
-  int pend = -1;   // a column this warp still has to apply to its other columns
+  const int last = w + NW * ((M - 1 - w) / NW);   // this warp's last column (w < M)
+  bool stop = w >= M;
   static_for<0, RS>([&](auto KB) {
     static_for<0, 32 / NW>([&](auto H) {
       constexpr int kb = KB.value;
@@ -299,7 +338,16 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
       for (int kk = 0; kk < NW && !stop; ++kk) {
         const int k1 = base + kk, k = k1 - 1;
         if (k1 == 0) continue;
-        if (k1 >= M || s_info) {   // uniform: s_info is written before the last barrier
+        if (k1 >= M || k >= last) {   // no column of this warp is right of column k
+          stop = true;
+          break;
+        }
+        if (!mbar_wait(&s_bar[k])) {   // bounded; never expected to run out
+          if (lane == 0) s_err = 1;
+          stop = true;
+          break;
+        }
+        if (s_info) {   // a pivot failed (written before its column's arrival)
           stop = true;
           break;
         }
@@ -311,49 +359,28 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
           li[rr] = Num<T>::zero();
           if (32 * rr + 31 > k && i > k && i < M) li[rr] = neg(Ls[k * LD + i]);
         }
-        const bool owner = w == kk;
-        if (owner) {
-          // the critical path: column k1 only; the owner's other columns take column k at
-          // the next step (deferred), so the pivot is published as early as possible
+        if (w == kk) {   // owner of column k1: that column first, publish, then the others
           const T ljk = Ls[k * LD + k1];
 #pragma unroll
           for (int rr = kb; rr < RS; ++rr) a[rr][C1] = fma_(li[rr], ljk, a[rr][C1]);
           finalize(k1, std::integral_constant<int, C1>{}, KB);
-          pend = k;
-        } else {
-          if (pend >= 0) {   // this warp's deferred column (it owned the previous step)
-            T lp[RS];
-#pragma unroll
-            for (int rr = 0; rr < RS; ++rr) {
-              const int i = lane + 32 * rr;
-              lp[rr] = Num<T>::zero();
-              if (32 * rr + 31 > pend && i > pend && i < M) lp[rr] = neg(Ls[pend * LD + i]);
-            }
-#pragma unroll
-            for (int cc = 0; cc < CS; ++cc) {
-              const int j = w + NW * cc;
-              if (j <= pend + 1 || j >= M) continue;   // warp-uniform; column pend+1 had it
-              const T ljk = Ls[pend * LD + j];
-#pragma unroll
-              for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(lp[rr], ljk, a[rr][cc]);
-            }
-            pend = -1;
-          }
-#pragma unroll
-          for (int cc = 0; cc < CS; ++cc) {
-            const int j = w + NW * cc;
-            if (j <= k || j >= M) continue;   // warp-uniform
-            const T ljk = Ls[k * LD + j];
-            // floor(j / 32) = floor(NW cc / 32) as NW divides 32 and w < NW: rows above the
-            // diagonal slot are skipped at compile time
-#pragma unroll
-            for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
-          }
         }
-        __syncthreads();
+#pragma unroll
+        for (int cc = 0; cc < CS; ++cc) {
+          const int j = w + NW * cc;
+          if (j <= k || j >= M || (w == kk && cc == C1)) continue;   // warp-uniform
+          const T ljk = Ls[k * LD + j];
+          // floor(j / 32) = floor(NW cc / 32) as NW divides 32 and w < NW: rows above the
+          // diagonal slot are skipped at compile time
+#pragma unroll
+          for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+        }
       }
     });
   });
+  __syncthreads();
+  if (threadIdx.x == 0 && s_err && !s_info) s_info = M + 1;   // a wait ran out: reported as a failure
+  __syncthreads();
   const int bad = s_info;
   if (info && threadIdx.x == 0) info[b] = bad;
   if (bad) return;

@@ -111,20 +111,22 @@ def test_graph_replay_matches_eager_and_tracks_params():
     assert abs(e2 - ref[0]) <= 1e-8 * abs(ref[0])
 
 
-def test_sdgpr_finite_differences():
-    """Central finite differences (eps = 1e-6) of the GPU energy on 50 random parameter
-    coordinates (the reference's check_grad, tests/test_utils.py:49-128, with its
-    tolerance: rel diff < 1e-4, or |numerical| < 1e-4 and rel diff <= 1.1)."""
+def _fd_check(eps, noise_ulps):
+    """Central finite differences of the GPU energy on 50 random parameter coordinates with the
+    reference's rule (check_grad, tests/test_utils.py:40-128): rel diff < 1e-4, or |numerical| <
+    1e-4 and rel diff <= 1.1.  A central difference resolves the energy only to about
+    |E| u / eps, u the energy's relative precision; `noise_ulps` * 2^-48 * |E| / eps is allowed
+    on top of the rule (0 for the strict form)."""
     from geepee_gb300 import aep_models as A
     g = load('sdgpr_small.npz')
     p = {k: np.array(v, dtype=float) for k, v in sub(g, 'p_').items()}
     mdl = A.SDGPR(g['x'], g['y'], 5, [3, 2])
     e0, gr = mdl.objective_function(p, 10, alpha=1.0)
+    res = noise_ulps * 2.0 ** -48 * abs(e0) / eps
     rng = np.random.RandomState(0)
     keys = sorted(p)
     sizes = [np.size(p[k]) for k in keys]
     flat = rng.choice(sum(sizes), 50, replace=False)
-    eps = 1e-6
     bad = []
     for f in flat:
         ki = int(np.searchsorted(np.cumsum(sizes), f, side='right'))
@@ -141,10 +143,22 @@ def test_sdgpr_finite_differences():
         num = (mdl.objective_function(pp, 10, alpha=1.0)[0] - mdl.objective_function(pm, 10, alpha=1.0)[0]) / (2 * eps)
         ana = float(np.ravel(gr[k])[j]) if np.ndim(gr[k]) else float(gr[k])
         diff = (ana - num) / num if num != 0 else np.inf
-        ok = abs(diff) < 1e-4 or (abs(num) < 1e-4 and abs(diff) <= 1.1)
+        ok = abs(diff) < 1e-4 or (abs(num) < 1e-4 and abs(diff) <= 1.1) or abs(ana - num) <= res
         if not ok:
             bad.append((k, j, ana, num, diff))
     assert not bad, bad
+
+
+def test_sdgpr_finite_differences_reference_eps():
+    """The reference's own step, eps = 1e-5, and its rule unchanged."""
+    _fd_check(1e-5, 0)
+
+
+def test_sdgpr_finite_differences_eps_1e6():
+    """eps = 1e-6: the double-float energy (relative precision ~2^-46, against float64's 2^-52)
+    limits the difference's resolution to ~|E| 2^-46 / eps; 8 units of 2^-48 |E| / eps are allowed
+    on top of the reference's rule (1.5e-7 absolute for this model's E = 5.2)."""
+    _fd_check(1e-6, 8)
 
 
 @pytest.mark.parametrize('nat', [1, 0])
