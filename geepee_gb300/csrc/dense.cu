@@ -748,6 +748,17 @@ __global__ void __launch_bounds__(128) small_spd_kernel(int B, int n, const type
     }
 }
 
+// Tile edge for a set of products with t8 8-wide / t16 16-wide tiles: 8 (256-thread CTAs,
+// about four resident per SM) while the tiles fill at most two such waves, then 16 (one
+// 1024-thread CTA per SM) up to two waves, then 32.  Small products are latency-bound: more,
+// smaller CTAs start together and finish sooner.
+inline int gemm_tile_edge(long t8, long t16) {
+  const long sms = gpk::sm_count();
+  if (t8 <= 8 * sms) return 8;
+  if (t16 <= 2 * sms) return 16;
+  return 32;
+}
+
 template <typename T, int TBM, int KS, bool P2>
 void gemm_go(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
              const void* B, int ldb, long sB, double beta, const void* E, int lde, long sE, void* C, int ldc, long sC,
@@ -768,11 +779,11 @@ template <typename T, bool P2 = false>
 int gemm_launch(int batch, int m, int n, int k, int tA, int tB, double alpha, const void* A, int lda, long sA,
                 const void* B, int ldb, long sB, double beta, const void* E, int lde, long sE, void* C, int ldc,
                 long sC, cudaStream_t st) {
-  const long t32 = (long)gpk::ceil_div(n, 32) * gpk::ceil_div(m, 32) * batch;
-  const long t16 = (long)gpk::ceil_div(n, 16) * gpk::ceil_div(m, 16) * batch;
-  if (t32 >= 2L * gpk::sm_count())
+  const int tbm = gemm_tile_edge((long)gpk::ceil_div(n, 8) * gpk::ceil_div(m, 8) * batch,
+                                 (long)gpk::ceil_div(n, 16) * gpk::ceil_div(m, 16) * batch);
+  if (tbm == 32)
     gemm_go<T, 32, 2, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
-  else if (t16 >= gpk::sm_count())
+  else if (tbm == 16)
     gemm_go<T, 16, 4, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
   else
     gemm_go<T, 8, 4, P2>(batch, m, n, k, tA, tB, alpha, A, lda, sA, B, ldb, sB, beta, E, lde, sE, C, ldc, sC, st);
@@ -802,12 +813,12 @@ int gemm_group_go(const GemmGroupArgs& g, LincombGroupArgs& l, cudaStream_t st) 
 template <typename T>
 int gemm_group_launch(int count, const gpk_gemm_t* pr, int nlc, const gpk_lincomb_t* lcs, cudaStream_t st) {
   // the tile size is chosen for the whole group, as gemm_launch chooses it for one product
-  long t32 = 0, t16 = 0;
+  long t8 = 0, t16 = 0;
   for (int p = 0; p < count; ++p) {
-    t32 += (long)gpk::ceil_div(pr[p].n, 32) * gpk::ceil_div(pr[p].m, 32) * pr[p].batch;
+    t8 += (long)gpk::ceil_div(pr[p].n, 8) * gpk::ceil_div(pr[p].m, 8) * pr[p].batch;
     t16 += (long)gpk::ceil_div(pr[p].n, 16) * gpk::ceil_div(pr[p].m, 16) * pr[p].batch;
   }
-  const int tbm = t32 >= 2L * gpk::sm_count() ? 32 : (t16 >= gpk::sm_count() ? 16 : 8);
+  const int tbm = gemm_tile_edge(t8, t16);
   GemmGroupArgs g{};
   g.count = count;
   g.first[0] = 0;

@@ -71,14 +71,18 @@ __device__ __forceinline__ void pair_of(int p, int& a, int& b) {
   b = p - r * (r + 1) / 2;
 }
 
-// CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.
+// CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.  Only the
+// first `nact` warps hold non-zero values (the others skip the shuffles; default: all).
 template <typename T, int K>
-__device__ __forceinline__ void block_sum(T* vals, T* red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ __forceinline__ void block_sum(T* vals, T* red, int nact = 0) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = nact > 0 ? nact : (int)(blockDim.x >> 5);
+  if (warp < nw) {
 #pragma unroll
-  for (int i = 0; i < K; ++i) {
-    T s = warp_sum(vals[i]);
-    if (lane == 0) red[warp * RED + i] = s;
+    for (int i = 0; i < K; ++i) {
+      T s = warp_sum(vals[i]);
+      if (lane == 0) red[warp * RED + i] = s;
+    }
   }
   __syncthreads();
   if (warp == 0) {
@@ -736,7 +740,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
       }
     }
     // ---- per-point totals: one CTA reduction, then lane q of warp 0 finalises dimension q
-    block_sum<T, NPB * KV>(vals, s.red);
+    block_sum<T, NPB * KV>(vals, s.red, (M + 31) >> 5);   // vals live in the row threads ia0 < M
     if (threadIdx.x < 32) {
 #pragma unroll
       for (int pt = 0; pt < NPB; ++pt) {
