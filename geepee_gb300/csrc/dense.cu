@@ -142,7 +142,7 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
 }
 
 template <typename T, int TBM, int KS, bool P2>
-__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_kernel(
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS, TBM == 8 ? 6 : 1) gemm_kernel(
     int m, int n, int k, int tA, int tB, double alpha, const typename Num<T>::store_t* A, int lda, long sA,
     const typename Num<T>::store_t* B, int ldb, long sB, double beta, const typename Num<T>::store_t* E, int lde,
     long sE, typename Num<T>::store_t* C, int ldc, long sC) {
@@ -168,7 +168,7 @@ struct LincombGroupArgs {
 };
 
 template <typename T, int TBM, int KS>
-__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS) gemm_group_kernel(GemmGroupArgs g, LincombGroupArgs l) {
+__global__ void __launch_bounds__(GemmShape<TBM>::NG * KS, TBM == 8 ? 6 : 1) gemm_group_kernel(GemmGroupArgs g, LincombGroupArgs l) {
   typedef typename Num<T>::store_t S;
   const int ng = g.first[g.count];
   if ((int)blockIdx.x >= ng) {   // a linear-combination CTA (uniform over the CTA)
