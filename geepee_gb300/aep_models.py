@@ -379,7 +379,7 @@ class SDGPR(_PackedModel):
         xb, yb = (self.x_dev, self.y_dev) if idx is None else gpk.gather_rows(idx, self.x_dev, self.y_dev)
         nb = yb.shape[0]
         scale = -N / nb / alpha
-        st = setup_layers(self.layers, alpha)
+        st = setup_layers(self.layers, alpha, streams=self._side_streams())
         ms, vs = [], []
         m, v, kfu, Bk = self.layers[0].fwd_det(xb)
         ms.append(m)

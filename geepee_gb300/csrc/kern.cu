@@ -546,9 +546,10 @@ extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* 
   GPK_REQUIRE(dkfu || (A && Bk && dm && dv), "det_bwd: need dkfu or (A, Bk, dm, dv)");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  // threads: b (a multiple of 32 >= M) x row groups, 512 at most; CTAs of ~16 rows
+  // threads: b (a multiple of 32 >= M) x row groups, 512 at most; CTAs of two passes of the row
+  // groups (8 rows at rg = 4): 125 CTAs for 1000 rows
   const int bx = 32 * gpk::ceil_div(M, 32), rg = bx <= 128 ? 4 : 2;
-  int grid = gpk::ceil_div(N, 4 * rg);
+  int grid = gpk::ceil_div(N, 2 * rg);
   if (grid > gpk::sm_count()) grid = gpk::sm_count();
   const dim3 threads(bx, rg);
   const int dc = D <= 8 ? 8 : 16;

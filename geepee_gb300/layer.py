@@ -481,10 +481,12 @@ def gauss_dsn(dv, nb, D, sn, alpha, scale):
     return scale * (dv.sum() * 2 * sn2 / alpha + nb * D * (1 - alpha))
 
 
-def setup_layers(layers, alpha):
+def setup_layers(layers, alpha, streams=None):
     """Posterior + cavity of several layers with batched factorisations: one SPD inverse for
     every layer's Kuu (grouped by M), then one for every Su^-1 and Suhat^-1 (natural-parameter
-    layers; others take the per-layer path).  Returns the int32 Cholesky status words of the
+    layers; others take the per-layer path).  With side `streams`, each layer's parameter
+    unpacking and Kuu run on its own stream, and theta_1 = R^T R alongside the Kuu inverse
+    (parallel branches of a captured graph).  Returns the int32 Cholesky status words of the
     factorisations (0 = fine), for one reduction at the end of the evaluation."""
     nat = [l for l in layers if l.nat]
     statuses = []
@@ -502,16 +504,37 @@ def setup_layers(layers, alpha):
         nS = sum(2 * l.Dout for l in group)
         info = torch.empty(G + nS, dtype=torch.int32, device=dev)
         K = torch.empty((G, M, M), dtype=F64, device=dev)
-        for l in group:
-            l.prep_r()
-        with gpk.GemmGroup() as g:
+        side = streams if streams and G > 1 else None
+        main = torch.cuda.current_stream()
+        if side:
+            forked = []
+            for i, l in enumerate(group):
+                s_i = side[i % len(side)]
+                s_i.wait_stream(main)
+                with torch.cuda.stream(s_i):
+                    l.prep_r()
+                    l.prep_k(out=K[i])
+                forked.append(s_i)
+            for s_i in forked:   # join only the branches forked here (graph-capture rule)
+                main.wait_stream(s_i)
+            s_th = side[0]
+            s_th.wait_stream(main)
+            with torch.cuda.stream(s_th), gpk.GemmGroup() as g:
+                for l in group:
+                    l.prep_th1(g)
+        else:
             for l in group:
-                l.prep_th1(g)
-        for i, l in enumerate(group):
-            l.prep_k(out=K[i])
+                l.prep_r()
+            with gpk.GemmGroup() as g:
+                for l in group:
+                    l.prep_th1(g)
+            for i, l in enumerate(group):
+                l.prep_k(out=K[i])
         Kinv = torch.empty_like(K)
         ld = torch.empty(G, dtype=F64, device=dev)
         gpk.chol_inv(K, Kinv, None, ld, info[:G])
+        if side:
+            main.wait_stream(s_th)   # theta_1 for Su^-1 and Suhat^-1
         S = torch.empty((nS, M, M), dtype=F64, device=dev)
         o = 0
         with gpk.GemmGroup() as g:
