@@ -343,7 +343,38 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
         }
       }
     };
-    if (PPT > 0) {
+    // the common configuration (a full pass of points, m and v only, Q == QC, Dout == DB, B in
+    // shared memory): the same sums without branches, so the NPB points' exps interleave
+    auto do_pair_fast = [&](int p, int ia, int ib) {
+      const T gab = s.G[p];
+      T w[DB];
+#pragma unroll
+      for (int d = 0; d < DB; ++d) w[d] = s.Bs[d * P + p];
+      T arg[NPB];
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt) {
+        const T* hu = s.u + pt * M;
+        const T* hh = s.h + pt * M * QC + ia * QC;
+        T cr = Num<T>::zero();
+#pragma unroll
+        for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib * QC + q], cr);
+        arg[pt] = sub(add(add(hu[ia], hu[ib]), gab), cr);
+      }
+#pragma unroll
+      for (int pt = 0; pt < NPB; ++pt) {
+        const T ps = exp_tab(arg[pt], s.tab);
+#pragma unroll
+        for (int d = 0; d < DB; ++d) vacc[pt][d] = fma_(w[d], ps, vacc[pt][d]);
+      }
+    };
+    const bool fast = PPT == 0 && npts == NPB && contract && !a.psi2 && Q == QC && D == DB && s.Bs;
+    if (fast) {
+      for (int p = threadIdx.x; p < P; p += NT) {
+        int ia, ib;
+        pair_of(p, ia, ib);
+        do_pair_fast(p, ia, ib);
+      }
+    } else if (PPT > 0) {
 #pragma unroll
       for (int k = 0; k < KP; ++k) {
         const int p = threadIdx.x + k * NT;
@@ -613,6 +644,50 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
       for (int d = 0; d < DB; ++d)
         dvr[pt][d] = (pt < npts && d < D) ? s.pg[pt * 2 * DMAX + DMAX + d] : Num<T>::zero();
+    if (NPB == 1 && Q == QC && D == DB && s.Bs && s.accB && !a.b_stride) {
+      // the common configuration, branch-free: two pairs (p, p + NT) per iteration, each step
+      // written for both, so that their dependent double-float chains interleave
+      const T* hu = s.u;
+      for (int p0 = threadIdx.x; p0 < P; p0 += 2 * NT) {
+        int pp[2], ia[2], ib[2];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          ok[u] = p0 + u * NT < P;
+          pp[u] = ok[u] ? p0 + u * NT : p0;
+          pair_of(pp[u], ia[u], ib[u]);
+        }
+        T arg[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const T* hh = s.h + ia[u] * QC;
+          T cr = Num<T>::zero();
+#pragma unroll
+          for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
+          arg[u] = sub(add(add(hu[ia[u]], hu[ib[u]]), s.G[pp[u]]), cr);
+        }
+        T ps[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) ps[u] = exp_tab(arg[u], s.tab);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          T w = Num<T>::zero();
+          T ab[DB];
+#pragma unroll
+          for (int d = 0; d < DB; ++d) {
+            w = fma_(dvr[0][d], s.Bs[d * P + pp[u]], w);
+            ab[d] = mul(dvr[0][d], ps[u]);
+          }
+          // L~ (half weight off the diagonal: the symmetric matrix entry)
+          const T l = mul(w, ps[u]);
+          if (ok[u]) {
+            s.L[pp[u]] = ia[u] == ib[u] ? l : scale2(l, -1);
+#pragma unroll
+            for (int d = 0; d < DB; ++d) s.accB[d * P + pp[u]] = add(s.accB[d * P + pp[u]], ab[d]);
+          }
+        }
+      }
+    } else
     for (int p = threadIdx.x; p < P; p += NT) {
       int ia, ib;
       pair_of(p, ia, ib);
@@ -688,14 +763,30 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
       if (rid < npts * M) {
         const T* Lp = s.L + pt * P;
         const int rowbase = ia * (ia + 1) / 2;
-        for (int ib = sl; ib < M; ib += 8) {
+        // two interleaved partial sums (b = sl + 16 j and sl + 8 + 16 j) halve the chains
+        T R1 = Num<T>::zero(), S1[QC];
+#pragma unroll
+        for (int q = 0; q < QC; ++q) S1[q] = Num<T>::zero();
+        for (int ib = sl; ib < M; ib += 16) {
+          const int jb = ib + 8;
           const int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
           const T l = Lp[p];
           R = add(R, l);
 #pragma unroll
           for (int q = 0; q < QC; ++q)
             if (q < Q) Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
+          if (jb < M) {
+            const int p1 = ia >= jb ? rowbase + jb : jb * (jb + 1) / 2 + ia;
+            const T l1 = Lp[p1];
+            R1 = add(R1, l1);
+#pragma unroll
+            for (int q = 0; q < QC; ++q)
+              if (q < Q) S1[q] = fma_(l1, s.z[jb * Q + q], S1[q]);
+          }
         }
+        R = add(R, R1);
+#pragma unroll
+        for (int q = 0; q < QC; ++q) Sq[q] = add(Sq[q], S1[q]);
       }
 #pragma unroll
       for (int m = 1; m < 8; m <<= 1) {
