@@ -379,7 +379,14 @@ class SDGPR(_PackedModel):
         xb, yb = (self.x_dev, self.y_dev) if idx is None else gpk.gather_rows(idx, self.x_dev, self.y_dev)
         nb = yb.shape[0]
         scale = -N / nb / alpha
-        st = setup_layers(self.layers, alpha, streams=self._side_streams())
+        side = self._side_streams()
+        st = setup_layers(self.layers, alpha, streams=side)
+        # the backward's accumulators are zeroed on a side stream while the forward runs
+        main = torch.cuda.current_stream()
+        side[0].wait_stream(main)
+        with torch.cuda.stream(side[0]):
+            for lay in self.layers:
+                lay.zero_accumulators()
         ms, vs = [], []
         m, v, kfu, Bk = self.layers[0].fwd_det(xb)
         ms.append(m)
@@ -392,8 +399,10 @@ class SDGPR(_PackedModel):
         gpk.gauss_lik(ms[-1], vs[-1], yb, self.sn, alpha, scale, 1.0 / N, dmi, dvi, self.energy, self.g_sn)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
-        main = torch.cuda.current_stream()
-        side = self._side_streams()
+        main.wait_stream(side[0])   # the zeroed accumulators
+        for lay in self.layers:
+            lay.prezeroed = True
+        self.layers[0].side = side[0]
         forked = []
         for i in range(L - 1, -1, -1):
             lay = self.layers[i]
@@ -408,6 +417,9 @@ class SDGPR(_PackedModel):
                 forked.append(st_side)
         for st_side in forked:     # join only the branches forked here (graph-capture rule)
             main.wait_stream(st_side)
+        for lay in self.layers:
+            lay.prezeroed = False
+        self.layers[0].side = None
         self._energy_terms(self.layers, alpha, N, st)
         return self.energy
 

@@ -368,11 +368,24 @@ constexpr int GB = 32;
 template <typename T>
 __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
                                                    const typename Num<T>::store_t* v,
-                                                   const typename Num<T>::store_t* w, double* C) {
+                                                   const typename Num<T>::store_t* w, double* C, int sym) {
   typedef typename Num<T>::store_t S;
   __shared__ T su[GB][32], sv[GB][32], sw[GB][DO_MAX];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of threads, 4 outputs each
-  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  // sym (u == v, C symmetric): blockIdx.x enumerates the tiles bi <= bj only, and an
+  // off-diagonal tile is added at both (i, j) and (j, i)
+  int bi = blockIdx.y, bj = blockIdx.x;
+  if (sym) {
+    const int nt = (M + 31) >> 5;
+    bi = 0;
+    bj = blockIdx.x;
+    while (bj >= nt - bi) {
+      bj -= nt - bi;
+      ++bi;
+    }
+    bj += bi;
+  }
+  const int i0 = bi * 32, j0 = bj * 32;
   T acc[DO_MAX][4];
 #pragma unroll
   for (int d = 0; d < DO_MAX; ++d)
@@ -420,7 +433,11 @@ __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         int i = i0 + ty * 4 + r, j = j0 + tx;
-        if (i < M && j < M) atomicAdd(&C[((size_t)d * M + i) * M + j], (double)Num<T>::st(acc[d][r]));
+        if (i < M && j < M) {
+          const double val = (double)Num<T>::st(acc[d][r]);
+          atomicAdd(&C[((size_t)d * M + i) * M + j], val);
+          if (sym && bi != bj) atomicAdd(&C[((size_t)d * M + j) * M + i], val);
+        }
       }
     }
   }
@@ -579,15 +596,19 @@ extern "C" int gpk_gram(int prec, int N, int M, int Dout, const void* u, const v
   GPK_REQUIRE(u && v && w && C, "gram: null pointer");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  int tiles = gpk::ceil_div(M, 32) * gpk::ceil_div(M, 32);
+  const int nt = gpk::ceil_div(M, 32);
+  const int sym = u == v;   // C symmetric: the upper tiles only
+  const int tiles = sym ? nt * (nt + 1) / 2 : nt * nt;
   int chunks = gpk::ceil_div(gpk::sm_count() * 2, tiles);
   if (chunks > gpk::ceil_div(N, 16)) chunks = gpk::ceil_div(N, 16);
   if (chunks < 1) chunks = 1;
-  dim3 grid(gpk::ceil_div(M, 32), gpk::ceil_div(M, 32), chunks);
+  const dim3 grid(sym ? tiles : nt, sym ? 1 : nt, chunks);
   if (prec == GPK_DF64)
-    gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C);
+    gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C,
+                                            sym);
   else if (prec == GPK_FP32)
-    gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C);
+    gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C,
+                                             sym);
   else
     return gpk::fail(GPK_EINVAL, "gram: unknown precision %d", prec);
   return gpk::check_launch("gram");

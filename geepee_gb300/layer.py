@@ -78,6 +78,10 @@ class DevLayer:
             views.append(self._acc[o:o + n])
             o += n
         self._dsf2, self._dl = views[0], views[1]
+        # set by a model for one evaluation: the accumulators were zeroed ahead (on a side
+        # stream), and `side` is a stream for the hyperparameter chain rule of the det layer
+        self.prezeroed = False
+        self.side = None
         self._dAh, self._dBh = views[2].view(Dout, M), views[3].view(Dout, M, M)
 
     # ---------------------------------------------------------------- parameters
@@ -274,6 +278,12 @@ class DevLayer:
         gpk.trace_kzz(Minner.contiguous(), self.zu, self.lls2, self.lsf2, self.g['sf'], self.g['ls'],
                       self.g['zu'], s_sf=2.0, s_ls=2.0)
 
+    def zero_accumulators(self):
+        """Zero what the data-sized backward kernels add into: the kernel-hyperparameter and
+        dA-hat / dB-hat accumulators and the zu gradient."""
+        self._acc.zero_()
+        self.g['zu'].zero_()
+
     def _kernel_grads(self, dsf2, dl, dv):
         """g_ls = dl * ell, g_sf = 2 sf2 (dsf2 + sum dv) (aep_models.py:226-231, 445-450)."""
         gpk.hyp_grads(self.ls, self.sf, dl, dsf2, dv, self.g['ls'], self.g['sf'])
@@ -288,15 +298,15 @@ class DevLayer:
         """The data-sized part of the backward: psi-statistic gradients (recomputing psi2),
         dAhat, dBhat and the gradient w.r.t. the input moments (dmx, dvx)."""
         Q = self.Din
-        self._acc.zero_()
+        if not self.prezeroed:
+            self.zero_accumulators()
         dZ = self.g['zu']
-        dZ.zero_()
         n = mx.shape[0]
         dmx = torch.empty((n, Q), dtype=F64, device=self.dev)
         dvx = torch.empty_like(dmx)
         gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, self._dsf2, self._dl,
                     dZ, self._dAh, self._dBh, dmx, dvx)
-        self._kernel_grads(self._dsf2, self._dl, dv)
+        self._dv = dv   # for the hyperparameter chain rule, with the algebra
         return dmx, dvx
 
     def bwd_mm_algebra(self, alpha):
@@ -308,6 +318,7 @@ class DevLayer:
         beta = self.beta
         dAh, dBh = self._dAh, self._dBh
         K = self.Kinv
+        self._kernel_grads(self._dsf2, self._dl, self._dv)
         with gpk.GemmGroup() as g:
             KdB = g.mm(K, dBh)
             KS = g.mm(K, self.Smm_h)
@@ -412,12 +423,18 @@ class DevLayer:
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
         K = self.Kinv
-        self._acc.zero_()
+        if not self.prezeroed:
+            self.zero_accumulators()
         dZ = self.g['zu']
-        dZ.zero_()
         dAh, dBh = self._dAh, self._dBh
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh)
-        self._kernel_grads(self._dsf2, self._dl, dv)
+        main = torch.cuda.current_stream()
+        if self.side is not None:   # the chain rule beside the algebra; joined before trace_kzz
+            self.side.wait_stream(main)
+            with torch.cuda.stream(self.side):
+                self._kernel_grads(self._dsf2, self._dl, dv)
+        else:
+            self._kernel_grads(self._dsf2, self._dl, dv)
         gpk.gram(kfu, kfu, dv, dBh)
         with gpk.GemmGroup() as g:
             Sinv_mh = g.mm(self.Shinv, self.mh.unsqueeze(-1))
@@ -459,6 +476,8 @@ class DevLayer:
             dR = g.mm(self.R, sym)
             KdK = g.mm(K, dK)
         Minner = mm(KdK, K, alpha=-1.0)
+        if self.side is not None:
+            main.wait_stream(self.side)
         self._finish_hyp(Minner)
         gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 

@@ -113,7 +113,8 @@ int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx,
 
 /* Weighted Gram reduction over rows:  C[d] += sum_n w[n,d] u_n v_n^T  (u, v [N,M], w [N,Dout],
  * C [Dout,M,M] float64).  The einsum('nd,na,nb->dab') / einsum('na,nd,nb->dab') reductions of
- * geepee/aep_models.py:464,493. */
+ * geepee/aep_models.py:464,493.  When u and v are the same buffer, C is symmetric: the tiles
+ * above the diagonal are formed once and added at both positions. */
 int gpk_gram(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
              void* stream);
 

@@ -220,8 +220,12 @@ def test_det_layer_fwd_bwd_vs_oracle(N, M, D, Dout):
         assert_close(got.cpu().numpy(), val, 1e-9, name)
     assert_close(dA.cpu().numpy(), dm.T @ kfu, 1e-10, 'dA')
     C = z(Dout, M, M)
-    gpk.gram(kt, kt, dev(dv), C)
+    gpk.gram(kt, kt, dev(dv), C)   # one buffer: the symmetric path
     assert_close(C.cpu().numpy(), np.einsum('nd,na,nb->dab', dv, kfu, kfu), 1e-10, 'gram')
+    u2 = rng.randn(N, M)
+    C2 = z(Dout, M, M)
+    gpk.gram(dev(u2), kt, dev(dv), C2)
+    assert_close(C2.cpu().numpy(), np.einsum('nd,na,nb->dab', dv, u2, kfu), 1e-10, 'gram u != v')
     c = z(Dout, M)
     gpk.wsum(kt, dev(dm), c)
     assert_close(c.cpu().numpy(), dm.T @ kfu, 1e-10, 'wsum')
