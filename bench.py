@@ -309,7 +309,7 @@ def run_ours(args, world, rank, local):
                 'hbm_peak_gbs': peaks.get('hbm_gbs'),
                 # dram__bytes (read + write) of this launch in one ncu capture of the same case
                 # (profiles/psi_bwd_psi_bwd_dgp.md): the inputs and outputs stay in L2
-                'traffic': 350464, 'traffic_unit': 'bytes per launch'}
+                'traffic': 361472, 'traffic_unit': 'bytes per launch'}
     out = {'e_gpu': e_gpu, 'e_fp64': e64, 'value': value, 'ms': 1e3 * t_dev / K,
            'e2e': e2e, 'fp64_rate': fp64_rate, 'n64': n64, 'roofline': roofline, 'clocks': clocks,
            'launches_per_eval': launches_per_eval, 'params': params, 'x': x, 'y': y,
