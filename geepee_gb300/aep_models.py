@@ -774,3 +774,44 @@ class SGPSSM(_PackedModel):
         my = mf @ C.T
         vy = np.einsum('ab,nb,ab->na', C, vf, C) + R
         return my, vy
+
+    def get_posterior_x(self, idxs=None):
+        """Base_SGPSSM.get_posterior_x (base_models.py:1562-1572) with update_hypers' natural-
+        parameter x posterior (base_models.py:1715-1725): (mean, variance) [T, Dx]."""
+        p = self.get_hypers()
+        f1 = np.asarray(p['x_factor_1'], dtype=float)
+        f2 = np.exp(2 * np.asarray(p['x_factor_2'], dtype=float))
+        post1, post2 = 3 * f1, 3 * f2
+        post1[[0, -1]] = 2 * f1[[0, -1]]
+        post2[[0, -1]] = 2 * f2[[0, -1]]
+        post1[0] += self.x_prior_1
+        post2[0] += self.x_prior_2
+        if idxs is None:
+            idxs = np.arange(self.N)
+        return post1[idxs] / post2[idxs], 1.0 / post2[idxs]
+
+    def predict_forward(self, T, x_control=None, prop_mode=PROP_MM, no_samples=200):
+        """Base_SGPSSM.predict_forward / predict_forward_mm (base_models.py:1453-1502): from the
+        posterior of the last latent state, T steps of moment propagation through the transition
+        GP's posterior - one launch for the whole sequence (gpk_psi_rollout: one CTA, each step
+        reading the previous step's moments) - then the linear-Gaussian emission
+        (lik_layers.py:558-571).  Returns mx, vx [T, Dx] and my, vy_noiseless, vy [T, Dy] (the
+        emission covariances' diagonals, as the reference returns them)."""
+        if prop_mode != PROP_MM:
+            raise NotImplementedError('propagation mode %s not implemented on the device path' % prop_mode)
+        if x_control is not None:
+            raise NotImplementedError('control inputs are not implemented on the device path')
+        lay = self.dyn_layer
+        if not self.updated:
+            lay.setup_posterior()
+            lay.setup_predict()
+            self.updated = True
+        pm, pv = self.get_posterior_x()
+        m0, v0 = _to_dev(pm[-1], self.dev), _to_dev(pv[-1], self.dev)
+        mx, vx = gpk.psi_rollout(m0, v0, lay.zu, lay.lls2, lay.lsf2, lay.A, lay.B_sto, T)
+        mxh, vxh = mx.cpu().numpy(), vx.cpu().numpy()
+        p = self.get_hypers()
+        C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
+        my = mxh @ C.T
+        vyn = np.einsum('ab,nb,ab->na', C, vxh, C)
+        return mxh, vxh, my, vyn, vyn + R

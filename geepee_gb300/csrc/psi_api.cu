@@ -43,6 +43,28 @@ extern "C" int gpk_psi_fwd(int prec, int N, int M, int Q, int Dout, const void* 
   return gpk::fail(GPK_EINVAL, "psi_fwd: unknown precision %d", prec);
 }
 
+extern "C" int gpk_psi_rollout(int prec, int T, int M, int Q, const void* mu0, const void* var0, const void* Z,
+                               const double* lls2, const double* lsf2, const void* A, const void* B, void* m_out,
+                               void* v_out, void* stream) {
+  GPK_REQUIRE(T >= 0 && M >= 1 && Q >= 1 && Q <= DMAX && Q <= QMAX, "psi_rollout: bad sizes T=%d M=%d Q=%d", T, M, Q);
+  GPK_REQUIRE(mu0 && var0 && Z && lls2 && lsf2 && A && B && m_out && v_out, "psi_rollout: null pointer");
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64) {
+    auto a = make_args<double>(T, M, Q, Q, mu0, var0, Z, lls2, lsf2, A, B);
+    a.m_out = (double*)m_out;
+    a.v_out = (double*)v_out;
+    a.chain = 1;
+    return psi_fwd_df64(a, st);
+  } else if (prec == GPK_FP32) {
+    auto a = make_args<float>(T, M, Q, Q, mu0, var0, Z, lls2, lsf2, A, B);
+    a.m_out = (float*)m_out;
+    a.v_out = (float*)v_out;
+    a.chain = 1;
+    return psi_fwd_f32(a, st);
+  }
+  return gpk::fail(GPK_EINVAL, "psi_rollout: unknown precision %d", prec);
+}
+
 extern "C" int gpk_psi_bwd_ex(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
                               const void* Z, const double* lls2, const double* lsf2, const void* A,
                               const void* B, const void* m, const void* dm, const void* dv, const void* dpsi1,

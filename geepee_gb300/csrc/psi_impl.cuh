@@ -50,6 +50,7 @@ struct PsiArgs {
   const S* dm;
   const S* dv;
   const S* dpsi1;    // optional [N,M]: replaces dm_all A
+  int chain;         // forward rollout: point n > 0 takes point n-1's (m, v) as its (mu, var)
   int bs_smem;       // symmetrised B staged in shared memory (set by the launcher)
   int accb_smem;     // backward: dBhat accumulates in shared memory (else atomically in dB)
   long b_stride;     // != 0: B is per point (B + n*b_stride), dv treated as 1
@@ -112,8 +113,11 @@ struct PointSlot {
 template <typename T, typename S>
 __device__ __forceinline__ void dims_of(const PsiArgs<S>& a, const T* ell2, const T* lnl, const float2* tab,
                                         const PointSlot<T>& ps, int n, int q) {
-  T mu = Num<T>::ld(a.mu[(size_t)n * a.Q + q]);
-  T var = Num<T>::ld(a.var[(size_t)n * a.Q + q]);
+  // a rollout reads the previous point's outputs (written before the pass's last barrier)
+  const S* pmu = a.chain ? (n > 0 ? a.m_out + (size_t)(n - 1) * a.Q : a.mu) : a.mu + (size_t)n * a.Q;
+  const S* pvar = a.chain ? (n > 0 ? a.v_out + (size_t)(n - 1) * a.Q : a.var) : a.var + (size_t)n * a.Q;
+  T mu = Num<T>::ld(pmu[q]);
+  T var = Num<T>::ld(pvar[q]);
   T s1 = add(ell2[q], var);
   T s2 = add(ell2[q], add(var, var));
   ps.pmu[q] = mu;
@@ -907,7 +911,7 @@ int run_fwd(const PsiArgs<typename Num<T>::store_t>& a, int per_sm, size_t sm, c
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k, NT, sm);
   if (resident < 1) resident = 1;
   if (resident > per_sm) resident = per_sm;
-  int grid = gpk::sm_count() * resident;
+  int grid = a.chain ? 1 : gpk::sm_count() * resident;   // a rollout is one CTA's sequence
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;
   k<<<grid, NT, sm, st>>>(a);
@@ -922,6 +926,11 @@ int fwd_variant(const PsiArgs<typename Num<T>::store_t>& a, bool sum, bool contr
     if (P <= 4 * NT) return run_fwd<T, 2, 4, QC, 4>(a, per_sm, sm, st);
     return run_fwd<T, 2, 16, QC, 4>(a, per_sm, sm, st);
   }
+  if (a.chain) {   // one point per pass: each point needs the previous one's moments
+    if (a.Dout == 1) return run_fwd<T, 1, 0, QC, 1>(a, per_sm, sm, st);
+    if (a.Dout == 2) return run_fwd<T, 1, 0, QC, 2>(a, per_sm, sm, st);
+    return run_fwd<T, 1, 0, QC, 4>(a, per_sm, sm, st);
+  }
   if (!contract || a.Dout == 1) return run_fwd<T, 4, 0, QC, 1>(a, per_sm, sm, st);
   if (a.Dout == 2) return run_fwd<T, 4, 0, QC, 2>(a, per_sm, sm, st);
   return run_fwd<T, 2, 0, QC, 4>(a, per_sm, sm, st);
@@ -933,7 +942,7 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   const int P = a.M * (a.M + 1) / 2;
   const bool contract = a.A && a.B && (a.m_out || a.v_out);
   const bool sum = a.psi2_sum != nullptr;
-  const int npb = (sum || (contract && a.Dout > 2)) ? 2 : 4;
+  const int npb = a.chain ? 1 : ((sum || (contract && a.Dout > 2)) ? 2 : 4);
   const int D = contract ? a.Dout : 0;
   a.bs_smem = contract && fwd_smem_bytes(a.M, a.Q, P, D, npb, sizeof(T), a.Dout * P) <= 200 * 1024;
   size_t sm = fwd_smem_bytes(a.M, a.Q, P, D, npb, sizeof(T), a.bs_smem ? a.Dout * P : 0);

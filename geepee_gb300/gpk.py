@@ -330,3 +330,13 @@ def finish(g, divisor, info=None, worst=None):
         assert info.dtype == torch.int32 and info.is_contiguous() and worst.dtype == torch.float64
     call('gpk_finish', g.numel(), ptr(g), float(divisor), 0 if info is None else info.numel(),
          None if info is None else ptr(info), None if info is None else ptr(worst), stream())
+
+
+def psi_rollout(mu0, var0, Z, lls2, lsf2, A, B, T):
+    """T-step moment rollout through a Q -> Q GP layer (gpk_psi_rollout): returns m, v [T, Q]."""
+    Q = Z.shape[1]
+    m = torch.empty((T, Q), dtype=Z.dtype, device=Z.device)
+    v = torch.empty_like(m)
+    call('gpk_psi_rollout', prec_of(Z.dtype), T, Z.shape[0], Q, ptr(mu0), ptr(var0), ptr(Z), ptr(lls2), ptr(lsf2),
+         ptr(A), ptr(B), ptr(m), ptr(v), stream())
+    return m, v

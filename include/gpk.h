@@ -111,6 +111,15 @@ int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx,
                 const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
                 double* dA, void* dx, void* stream);
 
+/* Moment-propagation rollout through a GP layer's posterior (Q inputs -> Q outputs): T steps,
+ * step t taking step t-1's output moments as its input means and variances (step 0: mu0,
+ * var0 [Q]); m_out, v_out [T, Q] receive m_t = psi1 A^T and v_t = sf2 + sum_ab B psi2 - m_t^2.
+ * One CTA runs the whole sequence (one launch).  The transition rollout of the GP state-space
+ * model's predict_forward_mm, geepee/base_models.py:1463-1502. */
+int gpk_psi_rollout(int prec, int T, int M, int Q, const void* mu0, const void* var0, const void* Z,
+                    const double* lls2, const double* lsf2, const void* A, const void* B, void* m_out, void* v_out,
+                    void* stream);
+
 /* Weighted Gram reduction over rows:  C[d] += sum_n w[n,d] u_n v_n^T  (u, v [N,M], w [N,Dout],
  * C [Dout,M,M] float64).  The einsum('nd,na,nb->dab') / einsum('na,nd,nb->dab') reductions of
  * geepee/aep_models.py:464,493.  When u and v are the same buffer, C is symmetric: the tiles

@@ -670,6 +670,40 @@ def sdgpr_predict(p, xs):
     return mf, vf, mf, vf + np.exp(2.0 * _scalar(p['sn']))
 
 
+def sgpssm_posterior_x(p, prior_mean=0.0, prior_var=1.0):
+    """``Base_SGPSSM.get_posterior_x`` base_models.py:1562-1572 with the natural-parameter
+    x posterior of ``update_hypers`` base_models.py:1715-1725 -> (mx, vx) [T, Dx]."""
+    f1 = np.asarray(p['x_factor_1'], dtype=float)
+    f2 = np.exp(2 * np.asarray(p['x_factor_2'], dtype=float))
+    post1, post2 = 3 * f1, 3 * f2
+    post1[[0, -1]] = 2 * f1[[0, -1]]
+    post2[[0, -1]] = 2 * f2[[0, -1]]
+    post1[0] += prior_mean / prior_var
+    post2[0] += 1.0 / prior_var
+    return post1 / post2, 1.0 / post2
+
+
+def sgpssm_predict_forward(p, T, prior_mean=0.0, prior_var=1.0):
+    """``Base_SGPSSM.predict_forward_mm`` base_models.py:1463-1502 (no control inputs, linear-
+    Gaussian emission ``Gauss_Emis.output_probabilistic`` lik_layers.py:558-571): from the
+    posterior of the last latent state, T steps of moment propagation through the transition
+    GP's posterior.  Returns mx, vx [T, Dx], my, vy_noiseless, vy [T, Dy] (diagonals)."""
+    Mz, Dx = _layer_dims(p, '_dynamic')
+    L = layer_unpack(p, '_dynamic', Mz, Dx)
+    pm, pv = sgpssm_posterior_x(p, prior_mean, prior_var)
+    C = np.asarray(p['C_emission'], dtype=float)
+    R = np.exp(2 * np.asarray(p['R_emission'], dtype=float))
+    mtm1, vtm1 = pm[[-1]], pv[[-1]]
+    mx, vx = np.zeros((T, Dx)), np.zeros((T, Dx))
+    for t in range(T):
+        mt, vt, _, _ = fwd_mm(L, mtm1, vtm1, cav=False)
+        mx[t], vx[t] = mt[0], vt[0]
+        mtm1, vtm1 = mt, vt
+    my = mx @ C.T
+    vyn = np.einsum('ab,nb,ab->na', C, vx, C)
+    return mx, vx, my, vyn, vyn + R
+
+
 # --------------------------------------------------------------------------
 # utils.py
 # --------------------------------------------------------------------------

@@ -181,6 +181,22 @@ def test_sgplvm_small(nat):
         assert_close(gr[k], ref[k], 1e-5, 'sgplvm mb ' + k)
 
 
+def test_sgpssm_forecast():
+    """predict_forward (moment matching) against the reference's own rollout
+    (tests/golden/make_forecast.py): 15 steps from the last latent state's posterior."""
+    from geepee_gb300 import aep_models as A
+    g = load('sgpssm_forecast.npz')
+    mdl = A.SGPSSM(g['y'], 2, 8, gp_emi=False)
+    mdl.update_hypers(sub(g, 'p_'))
+    pm, pv = mdl.get_posterior_x()
+    assert_close(pm, g['post_m'], 1e-13, 'posterior x mean')
+    out = mdl.predict_forward(int(g['T']))
+    for name, got in zip(('mx', 'vx', 'my', 'vy_noiseless', 'vy'), out):
+        assert_close(got, g[name], P_TOL, name)
+    with pytest.raises(NotImplementedError):
+        mdl.predict_forward(3, prop_mode='MC')
+
+
 def test_sgpssm_small():
     from geepee_gb300 import aep_models as A
     g = load('sgpssm_small.npz')

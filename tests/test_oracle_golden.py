@@ -131,3 +131,16 @@ def test_sgpssm_small():
     e, gr = O.sgpssm_objective(g['y'], p, 0.5, start=int(g['mb_start']), mb_size=20)
     assert abs(e - g['energy_mb']) <= 1e-9 * abs(g['energy_mb'])
     assert_dict_close(gr, sub(g, 'gmb_'), 1e-6, 'sgpssm mb')
+
+
+def test_sgpssm_forecast():
+    """The oracle's T-step moment-matching forecast against the reference's predict_forward
+    (tests/golden/make_forecast.py)."""
+    g = load('sgpssm_forecast.npz')
+    p = sub(g, 'p_')
+    pm, pv = O.sgpssm_posterior_x(p)
+    assert_close(pm, g['post_m'], 1e-13, 'posterior x mean')
+    assert_close(pv, g['post_v'], 1e-13, 'posterior x var')
+    mx, vx, my, vyn, vy = O.sgpssm_predict_forward(p, int(g['T']))
+    for name, got in (('mx', mx), ('vx', vx), ('my', my), ('vy_noiseless', vyn), ('vy', vy)):
+        assert_close(got, g[name], 1e-10, name)
