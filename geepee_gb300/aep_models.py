@@ -20,8 +20,8 @@ import numpy as np
 import torch
 from scipy.optimize import minimize
 
-from .config import PROP_MM, PROP_MC, PROP_LIN, JITTER
-from .layer import DevLayer, gauss_logZ, gauss_dsn, mm, mv, setup_layers
+from .config import PROP_MM, PROP_MC, PROP_LIN, JITTER, MC_NO_SAMPLES
+from .layer import DevLayer, gauss_logZ, gauss_logZ_mc, gauss_dsn, mm, mv, setup_layers
 from .utils import ObjectiveWrapper, flatten_dict, unflatten_dict, adam
 from .pack import Pack
 from . import gpk
@@ -244,9 +244,9 @@ class _PackedModel(Base_Model):
 
     def _objective_host(self, idx, alpha):
         if idx is None:
-            self._run(('full', alpha), lambda: self.device_objective(None, alpha))
+            self._run(('full', alpha, getattr(self, '_mc', False)), lambda: self.device_objective(None, alpha))
         else:
-            key = ('mb', len(idx), alpha)
+            key = ('mb', len(idx), alpha, getattr(self, '_mc', False))
             if key not in self._graphs or getattr(self, '_idx_buf', None) is None \
                     or self._idx_buf.shape[0] != len(idx):
                 self._idx_buf = torch.zeros(len(idx), dtype=torch.int64, device=self.dev)
@@ -446,10 +446,30 @@ class SDGPR(_PackedModel):
         return m, v
 
     def predict_f(self, inputs, prop_mode=PROP_MM, no_samples=200):
-        if prop_mode != PROP_MM:
+        """Base_SDGPR.predict_f (base_models.py:1124-1130): moment matching (predict_f_mm), or
+        predict_f_mc (base_models.py:1160-1184): every layer's posterior on deterministic
+        inputs, the first layer's output sampled no_samples times per input and every later
+        layer's once per sample, the draws taken from numpy's global RNG in the reference's
+        order.  MC returns (samples [no_samples, K, Dout], mf, vf of the last layer)."""
+        if prop_mode == PROP_MM:
+            m, v = self.predict_f_device(_to_dev(inputs, self.dev))
+            return m.cpu().numpy(), v.cpu().numpy()
+        if prop_mode != PROP_MC:
             raise NotImplementedError('prop_mode %s not implemented' % prop_mode)
-        m, v = self.predict_f_device(_to_dev(inputs, self.dev))
-        return m.cpu().numpy(), v.cpu().numpy()
+        self._prepare_predict()
+        K = np.shape(inputs)[0]
+        samples = _to_dev(inputs, self.dev)
+        for i, lay in enumerate(self.layers):
+            mf, vf, _, _ = lay.fwd_det(samples, cav=False)
+            if i == 0:
+                eps = _to_dev(np.random.randn(no_samples, mf.shape[0], mf.shape[1]), self.dev)
+                samples = (torch.sqrt(vf) * eps + mf).reshape(no_samples * mf.shape[0], mf.shape[1])
+            else:
+                eps = _to_dev(np.random.randn(mf.shape[0], mf.shape[1]), self.dev)
+                samples = torch.sqrt(vf) * eps + mf
+            samples = samples.contiguous()
+        samples = samples.reshape(no_samples, K, self.layers[-1].Dout)
+        return samples.cpu().numpy(), mf.cpu().numpy(), vf.cpu().numpy()
 
     def predict_y(self, inputs):
         """base_models.py:1264-1275."""
@@ -533,9 +553,25 @@ class SGPLVM(_PackedModel):
         mcav, vcav = (c1 / c2).contiguous(), (1.0 / c2).contiguous()
         p1b, p2b = post1.index_select(0, idx), post2.index_select(0, idx)
         mpost, vpost = p1b / p2b, 1.0 / p2b
-        m, vv = lay.fwd_mm(mcav, vcav)
-        logZ, dm, dv = gauss_logZ(m, vv, yb, self.sn, alpha)
-        dmx, dvx = lay.bwd_mm(alpha, m, scale * dm, scale * dv, mcav, vcav)
+        if getattr(self, '_mc', False):
+            # Monte Carlo: cavity samples x = eps sqrt(v) + m through the deterministic layer
+            # (aep_models.py:160-180), log-mean-exp likelihood, backprop_grads_lvm_mc with the
+            # input gradient, then backprop_grads_reparam (base_models.py:373-388)
+            eps = self._eps_buf
+            S, Q, Dy = eps.shape[0], self.Din, self.Dout
+            sd = vcav.sqrt()
+            xs = (eps * sd + mcav).reshape(S * nb, Q).contiguous()
+            ms, vs, kfu, Bk = lay.fwd_det(xs)
+            logZ, dm, dv = gauss_logZ_mc(ms.view(S, nb, Dy), vs.view(S, nb, Dy), yb, self.sn, alpha)
+            dxs = torch.empty_like(xs)
+            lay.bwd_det(alpha, (scale * dm).reshape(S * nb, Dy).contiguous(),
+                        (scale * dv).reshape(S * nb, Dy).contiguous(), kfu, Bk, xs, dx=dxs)
+            dxs = dxs.view(S, nb, Q)
+            dmx, dvx = dxs.sum(0), (dxs * eps).sum(0) / (2.0 * sd)
+        else:
+            m, vv = lay.fwd_mm(mcav, vcav)
+            logZ, dm, dv = gauss_logZ(m, vv, yb, self.sn, alpha)
+            dmx, dvx = lay.bwd_mm(alpha, m, scale * dm, scale * dv, mcav, vcav)
         self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
         phi_prior = float(0.5 * (self.prior_mean ** 2 / self.prior_var + np.log(self.prior_var))) * N * self.Din
         phi_cav, dmc, dvc = _phi_x(mcav, vcav)
@@ -572,11 +608,21 @@ class SGPLVM(_PackedModel):
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
-        """aep_models.py:694-815 (PROP_MM)."""
-        if prop_mode != PROP_MM:
+        """aep_models.py:694-815, moment matching or Monte Carlo propagation.  The Monte Carlo
+        samples are drawn from numpy's global RNG after the minibatch, as the reference draws
+        them (np.random.randn(MC_NO_SAMPLES, n, Din), aep_models.py:171), so a seeded run
+        sees the same samples."""
+        if prop_mode not in (PROP_MM, PROP_MC):
             raise NotImplementedError('propagation mode not implemented')
         N = self.N
         idx = np.arange(N) if mb_size == N else np.random.choice(N, mb_size, replace=False)
+        self._mc = prop_mode == PROP_MC
+        if self._mc:
+            eps = np.random.randn(MC_NO_SAMPLES, len(idx), self.Din)
+            if getattr(self, '_eps_buf', None) is None or tuple(self._eps_buf.shape) != eps.shape:
+                self._eps_buf = torch.empty(eps.shape, dtype=torch.float64, device=self.dev)
+                self._graphs = {k: g for k, g in self._graphs.items() if not k[-1]}   # new buffer
+            self._eps_buf.copy_(torch.from_numpy(eps))
         self.update_hypers(params)
         return self._objective_host(idx, alpha)
 

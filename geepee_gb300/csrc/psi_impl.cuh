@@ -112,19 +112,23 @@ struct PointSlot {
 // per-point constants for dimension q of point n
 template <typename T, typename S>
 __device__ __forceinline__ void dims_of(const PsiArgs<S>& a, const T* ell2, const T* lnl, const float2* tab,
-                                        const PointSlot<T>& ps, int n, int q) {
+                                        const PointSlot<T>& ps, int n, int q, int part) {
   // a rollout reads the previous point's outputs (written before the pass's last barrier)
   const S* pmu = a.chain ? (n > 0 ? a.m_out + (size_t)(n - 1) * a.Q : a.mu) : a.mu + (size_t)n * a.Q;
   const S* pvar = a.chain ? (n > 0 ? a.v_out + (size_t)(n - 1) * a.Q : a.var) : a.var + (size_t)n * a.Q;
-  T mu = Num<T>::ld(pmu[q]);
-  T var = Num<T>::ld(pvar[q]);
-  T s1 = add(ell2[q], var);
-  T s2 = add(ell2[q], add(var, var));
-  ps.pmu[q] = mu;
-  ps.pis1[q] = recip(s1);
-  ps.pc[q] = recip(s2);
-  ps.pld1[q] = scale2(sub(lnl[q], log_tab(s1, tab)), -1);
-  ps.pld2[q] = scale2(sub(lnl[q], log_tab(s2, tab)), -1);
+  // the four transcendental pieces of dimension q run on four threads (part 0..3)
+  const T var = Num<T>::ld(pvar[q]);
+  const T s = (part & 1) ? add(ell2[q], add(var, var)) : add(ell2[q], var);   // l+2S : l+S
+  if (part == 0) {
+    ps.pmu[q] = Num<T>::ld(pmu[q]);
+    ps.pis1[q] = recip(s);
+  } else if (part == 1) {
+    ps.pc[q] = recip(s);
+  } else if (part == 2) {
+    ps.pld1[q] = scale2(sub(lnl[q], log_tab(s, tab)), -1);
+  } else {
+    ps.pld2[q] = scale2(sub(lnl[q], log_tab(s, tab)), -1);
+  }
 }
 
 // per-pseudo-input terms of one point: psi1_a (returned), u_a and h_aq (written to the slot)
@@ -281,9 +285,9 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
   for (int n0 = nbeg; n0 < nend; n0 += NPB) {
     const int npts = min(NPB, nend - n0);
     // ---- per-dimension constants of the NPB points
-    for (int t = threadIdx.x; t < npts * Q; t += NT) {
-      const int pt = t / Q, q = t - pt * Q;
-      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, fslot(s, pt, M, Q), n0 + pt, q);
+    for (int t = threadIdx.x; t < 4 * npts * Q; t += NT) {
+      const int part = t & 3, pq = t >> 2, pt = pq / Q, q = pq - pt * Q;
+      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, fslot(s, pt, M, Q), n0 + pt, q, part);
     }
     __syncthreads();
     // ---- per-pseudo-input terms (and psi1)
@@ -580,9 +584,9 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   for (int n0 = nbeg; n0 < nend; n0 += NPB) {
     const int npts = min(NPB, nend - n0);
     // ---- per-point constants and upstream gradients
-    for (int t = threadIdx.x; t < npts * Q; t += NT) {
-      const int pt = t / Q, q = t - pt * Q;
-      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, bslot(s, pt, M, Q), n0 + pt, q);
+    for (int t = threadIdx.x; t < 4 * npts * Q; t += NT) {
+      const int part = t & 3, pq = t >> 2, pt = pq / Q, q = pq - pt * Q;
+      dims_of<T, S>(a, s.ell2, s.lnl, s.tab, bslot(s, pt, M, Q), n0 + pt, q, part);
     }
     if (threadIdx.x >= 256 && threadIdx.x < 256 + npts * D) {
       const int t = threadIdx.x - 256, pt = t / D, d = t - pt * D, n = n0 + pt;

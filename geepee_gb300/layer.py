@@ -379,10 +379,11 @@ class DevLayer:
             return self._pack_eta1(dSinv), mv(self.Su, dmu), dSinv.sum(0)
         return self._pack_eta1(dSu), dmu, torch.zeros_like(self.Kinv)
 
-    def bwd_det(self, alpha, dm, dv, kfu, Bk, x):
-        """backprop_grads_reg (aep_models.py:412-511)."""
+    def bwd_det(self, alpha, dm, dv, kfu, Bk, x, dx=None):
+        """backprop_grads_reg (aep_models.py:412-511); with `dx` [n, Din] the gradient w.r.t. the
+        inputs is written there too (backprop_grads_lvm_mc, aep_models.py:306-410)."""
         if self.nat:
-            return self._bwd_det_nat(alpha, dm, dv, kfu, Bk, x)
+            return self._bwd_det_nat(alpha, dm, dv, kfu, Bk, x, dx)
         N, M, D, Q = self.N, self.M, self.Dout, self.Din
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         z = lambda *s: torch.zeros(s, dtype=F64, device=self.dev)
@@ -390,7 +391,7 @@ class DevLayer:
         dsf2, dl, dAh = z(1), z(Q), z(D, M)
         dZ = self.g['zu']
         dZ.zero_()
-        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh)
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh, dx=dx)
         self._kernel_grads(dsf2, dl, dv)
         # sum_n dm_nd (kfu_n K^-1) = dAhat_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T =
         # K^-1 dBhat_d K^-1: the M x M forms of the reference's kfu Kuuinv contractions
@@ -414,7 +415,7 @@ class DevLayer:
         self.g['eta1_R'].copy_(e1c + e1p)
         self.g['eta2'].copy_(e2c + e2p)
 
-    def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x):
+    def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x, dx=None):
         """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
         compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so
         that the eta1_R terms of the cavity and the posterior are packed once.  Products of
@@ -427,7 +428,8 @@ class DevLayer:
             self.zero_accumulators()
         dZ = self.g['zu']
         dAh, dBh = self._dAh, self._dBh
-        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh)
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh,
+                    dx=dx)
         main = torch.cuda.current_stream()
         if self.side is not None:   # the chain rule beside the algebra; joined before trace_kzz
             self.side.wait_stream(main)
@@ -492,6 +494,23 @@ def gauss_logZ(m, v, y, sn, alpha):
     logZ = (-0.5 * (torch.log(2 * math.pi * vt) + r * r / vt)).sum()
     logZ = logZ + nb * D * (0.5 * torch.log(2 * math.pi * sn2 / alpha) - 0.5 * alpha * torch.log(2 * math.pi * sn2))
     return logZ.reshape(1), r / vt, -0.5 / vt + 0.5 * r * r / (vt * vt)
+
+
+def gauss_logZ_mc(m, v, y, sn, alpha):
+    """Gauss_Layer.compute_log_Z, 3-D case (lik_layers.py:134-150) on the device: per-sample
+    tilted logZ of m, v [S, n, D] against y [n, D], log-mean-exp over the samples; returns
+    (logZ, dlogZ/dm, dlogZ/dv) with the samples' softmax weights in the gradients."""
+    sn2 = torch.exp(2.0 * sn)
+    vt = v + sn2 / alpha
+    r = y.unsqueeze(0) - m
+    lz = -0.5 * (torch.log(2 * math.pi * vt) + r * r / vt)
+    lz = lz + (0.5 * torch.log(2 * math.pi * sn2 / alpha) - 0.5 * alpha * torch.log(2 * math.pi * sn2))
+    lmax = lz.max(0).values
+    e = torch.exp(lz - lmax)
+    se = e.sum(0)
+    logZ = (lmax + torch.log(se) - math.log(m.shape[0])).sum()
+    w = e / se
+    return logZ.reshape(1), w * r / vt, w * (-0.5 / vt + 0.5 * r * r / (vt * vt))
 
 
 def gauss_dsn(dv, nb, D, sn, alpha, scale):

@@ -326,15 +326,21 @@ def bwd_mm(L, N, alpha, m, dm, dv, psi1, psi2, mx, vx):
             {'mx': dmx, 'vx': dvx})
 
 
-def bwd_det(L, N, alpha, dm, dv, kfu, x):
-    """``backprop_grads_reg`` aep_models.py:412-511 (includes the phi gradients)."""
+def bwd_det(L, N, alpha, dm, dv, kfu, x, grad_x=False):
+    """``backprop_grads_reg`` aep_models.py:412-511 (includes the phi gradients).  With grad_x the
+    gradient w.r.t. the inputs is returned too (the ``compute_kfu_derivatives(..., grad_x=True)``
+    of ``backprop_grads_lvm_mc`` aep_models.py:306-410, whose layer gradients are the same
+    function written through the cavity natural parameters)."""
     ell = np.exp(L['ls'])
     sf2 = np.exp(2 * L['sf'])
     s_post, s_cav = N / alpha - 1.0, -N / alpha
     K = L['Kinv']
     kK = kfu @ K
     dkfu = dm @ L['Ah'] + 2 * np.einsum('nd,dab,na->nb', dv, L['Bh_det'], kfu)
-    dsf2, dl, dz = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'])
+    if grad_x:
+        dsf2, dl, dz, dx = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'], grad_x=True)
+    else:
+        dsf2, dl, dz = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'])
     dls = dl * ell
     dsf = 2 * sf2 * (dsf2 + dv.sum())
     dmucav = dm.T @ kK
@@ -354,7 +360,8 @@ def bwd_det(L, N, alpha, dm, dv, kfu, x):
           + dKc + dKp + dKprior)
     Minner = -K @ dK @ K
     dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, Minner)
-    return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1c + e1p, 'eta2': e2c + e2p}
+    g = {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1c + e1p, 'eta2': e2c + e2p}
+    return (g, dx) if grad_x else g
 
 
 # --------------------------------------------------------------------------
@@ -370,6 +377,23 @@ def gauss_logZ(m, v, y, sn, alpha):
     logZ += y.shape[0] * y.shape[1] * (0.5 * np.log(2 * np.pi * sn2 / alpha)
                                        - 0.5 * alpha * np.log(2 * np.pi * sn2))
     return logZ, r / vt, -0.5 / vt + 0.5 * r ** 2 / vt ** 2
+
+
+def gauss_logZ_mc(m, v, y, sn, alpha):
+    """``Gauss_Layer.compute_log_Z``, 3-D case lik_layers.py:134-150: per-sample tilted logZ of
+    m, v [S, n, D] against y [n, D], log-mean-exp over the S samples, and its gradients (the
+    softmax weights of the samples times the per-sample gradients)."""
+    sn2 = np.exp(2.0 * _scalar(sn))
+    vt = v + sn2 / alpha
+    r = y[None] - m
+    lz = -0.5 * (np.log(2 * np.pi * vt) + r ** 2 / vt)
+    lz = lz + (0.5 * np.log(2 * np.pi * sn2 / alpha) - 0.5 * alpha * np.log(2 * np.pi * sn2))
+    lmax = lz.max(0)
+    e = np.exp(lz - lmax)
+    se = e.sum(0)
+    logZ = np.sum(lmax + np.log(se) - np.log(m.shape[0]))
+    w = e / se
+    return logZ, w * r / vt, w * (-0.5 / vt + 0.5 * r ** 2 / vt ** 2)
 
 
 def gauss_dsn(dv, nb, D, sn, alpha, scale):
@@ -476,9 +500,16 @@ def sdgpr_objective(x, y, p, alpha, idx=None, fixed=()):
     return _finish(energy, grads, N, fixed)
 
 
+MC_NO_SAMPLES = 5   # config.py:16
+
+
 def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
-                     nat_param=True, fixed=()):
-    """``SGPLVM.objective_function`` aep_models.py:694-815 (MM; energy not divided by N)."""
+                     nat_param=True, fixed=(), eps=None):
+    """``SGPLVM.objective_function`` aep_models.py:694-815 (energy not divided by N): moment
+    matching, or, with ``eps`` [MC_NO_SAMPLES, n, Q] (standard normal draws), Monte Carlo
+    propagation of the cavity samples x = eps sqrt(v) + m through the deterministic layer
+    (``_forward_prop_random_thru_cav_mc`` aep_models.py:160-180, ``backprop_grads_lvm_mc``
+    :306-410, ``backprop_grads_reparam`` base_models.py:373-388)."""
     N, Dy = y.shape
     Mz, Dout = _layer_dims(p, '')
     Q = np.asarray(p['x1']).shape[1]
@@ -502,9 +533,19 @@ def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
         c2 = px2 + (t2 - px2) * (1 - alpha)
     mcav, vcav = c1 / c2, 1.0 / c2
     mpost, vpost = post1[idx] / post2[idx], 1.0 / post2[idx]
-    m, v, p1, p2 = fwd_mm(L, mcav, vcav)
-    logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
-    gh, gi = bwd_mm(L, N, alpha, m, scale * dm, scale * dv, p1, p2, mcav, vcav)
+    if eps is None:
+        m, v, p1, p2 = fwd_mm(L, mcav, vcav)
+        logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
+        gh, gi = bwd_mm(L, N, alpha, m, scale * dm, scale * dv, p1, p2, mcav, vcav)
+    else:
+        S = eps.shape[0]
+        xs = (eps * np.sqrt(vcav) + mcav).reshape(S * nb, Q)
+        ms, vs, kfu = fwd_det(L, xs, cav=True)
+        logZ, dm, dv = gauss_logZ_mc(ms.reshape(S, nb, Dy), vs.reshape(S, nb, Dy), yb, p['sn'], alpha)
+        gh, dx = bwd_det(L, N, alpha, scale * dm.reshape(S * nb, Dy), scale * dv.reshape(S * nb, Dy), kfu, xs,
+                         grad_x=True)
+        dx = dx.reshape(eps.shape)
+        gi = {'mx': dx.sum(0), 'vx': np.sum(dx * eps, axis=0) / (2 * np.sqrt(vcav))}
     grads = dict(gh)
     grads['sn'] = gauss_dsn(dv, nb, Dy, p['sn'], alpha, scale)
 
@@ -668,6 +709,26 @@ def sdgpr_predict(p, xs):
             mf, vf, _, _ = fwd_mm(L, mf, vf, cav=False)
         i += 1
     return mf, vf, mf, vf + np.exp(2.0 * _scalar(p['sn']))
+
+
+def sdgpr_predict_mc(p, xs, no_samples):
+    """``Base_SDGPR.predict_f_mc`` base_models.py:1160-1184: posterior on deterministic inputs
+    layer by layer, the first layer's output sampled no_samples times per input, every later
+    layer's once per sample, from numpy's global RNG in that order.  Returns (samples
+    [no_samples, K, Dout], mf, vf of the last layer over the no_samples*K rows)."""
+    i = 0
+    samples = np.asarray(xs, dtype=float)
+    while ('eta2_%d' % i) in p:
+        Mz, Dout = _layer_dims(p, '_%d' % i)
+        L = layer_unpack(p, '_%d' % i, Mz, Dout)
+        mf, vf, _ = fwd_det(L, samples, cav=False)
+        if i == 0:
+            eps = np.random.randn(no_samples, mf.shape[0], mf.shape[1])
+            samples = (np.sqrt(vf) * eps + mf).reshape(no_samples * mf.shape[0], mf.shape[1])
+        else:
+            samples = np.sqrt(vf) * np.random.randn(mf.shape[0], mf.shape[1]) + mf
+        i += 1
+    return samples.reshape(no_samples, np.shape(xs)[0], -1), mf, vf
 
 
 def sgpssm_posterior_x(p, prior_mean=0.0, prior_var=1.0):

@@ -181,6 +181,43 @@ def test_sgplvm_small(nat):
         assert_close(gr[k], ref[k], 1e-5, 'sgplvm mb ' + k)
 
 
+def test_sgplvm_monte_carlo():
+    """prop_mode='MC' against the reference's own Monte Carlo objective with the same seeds
+    (tests/golden/make_lvm_mc.py): the samples come from numpy's global RNG in the reference's
+    order, so the device path sees the reference's draws; full batch and a minibatch of 5."""
+    from geepee_gb300 import aep_models as A
+    g = load('sgplvm_mc.npz')
+    p = sub(g, 'p_')
+    mdl = A.SGPLVM(g['y'], 2, 5, nat_param=True)
+    np.random.seed(21)
+    e, gr = mdl.objective_function({k: np.copy(v) for k, v in p.items()}, 12, alpha=0.5, prop_mode='MC')
+    _energy_ok(e, g['energy'])
+    for k in sub(g, 'g_'):
+        assert_close(gr[k], g['g_' + k], 1e-6, 'lvm mc ' + k)
+    np.random.seed(22)
+    e, gr = mdl.objective_function({k: np.copy(v) for k, v in p.items()}, 5, alpha=0.5, prop_mode='MC')
+    _energy_ok(e, g['energy_mb'])
+    for k in sub(g, 'gmb_'):
+        assert_close(gr[k], g['gmb_' + k], 1e-6, 'lvm mc mb ' + k)
+    # the moment-matching graph of the same model is unaffected
+    e_mm, _ = mdl.objective_function({k: np.copy(v) for k, v in p.items()}, 12, alpha=0.5)
+    assert abs(e_mm - e) > 0
+
+
+def test_sdgpr_predict_monte_carlo():
+    """predict_f(prop_mode='MC') against the reference's predict_f_mc with the same seed
+    (tests/golden/make_dgp_mc.py): the draws come from numpy's global RNG in its order."""
+    from geepee_gb300 import aep_models as A
+    g = load('sdgpr_mc.npz')
+    s = load('sdgpr_small.npz')
+    mdl = A.SDGPR(s['x'], s['y'], 5, [3, 2])
+    mdl.update_hypers(sub(s, 'p_'))
+    np.random.seed(int(g['seed']))
+    samples, mf, vf = mdl.predict_f(g['xs'], prop_mode='MC', no_samples=int(g['no_samples']))
+    for name, got in (('samples', samples), ('mf', mf), ('vf', vf)):
+        assert_close(got, g[name], P_TOL, name)
+
+
 def test_sgpssm_forecast():
     """predict_forward (moment matching) against the reference's own rollout
     (tests/golden/make_forecast.py): 15 steps from the last latent state's posterior."""

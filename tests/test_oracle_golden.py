@@ -144,3 +144,27 @@ def test_sgpssm_forecast():
     mx, vx, my, vyn, vy = O.sgpssm_predict_forward(p, int(g['T']))
     for name, got in (('mx', mx), ('vx', vx), ('my', my), ('vy_noiseless', vyn), ('vy', vy)):
         assert_close(got, g[name], 1e-10, name)
+
+
+def test_sgplvm_monte_carlo():
+    """The oracle's Monte Carlo propagation (the reference's own standard-normal draws, stored
+    in the fixture) against the reference's SGPLVM objective with prop_mode='MC'
+    (tests/golden/make_lvm_mc.py): full batch and a minibatch of 5."""
+    g = load('sgplvm_mc.npz')
+    p = sub(g, 'p_')
+    e, gr = O.sgplvm_objective(g['y'], p, 0.5, eps=g['eps'])
+    assert abs(e - g['energy']) <= 1e-12 * abs(g['energy'])
+    assert_dict_close(gr, sub(g, 'g_'), 1e-10, 'lvm mc')
+    e, gr = O.sgplvm_objective(g['y'], p, 0.5, idx=g['mb_idx'], eps=g['eps_mb'])
+    assert abs(e - g['energy_mb']) <= 1e-12 * abs(g['energy_mb'])
+    assert_dict_close(gr, sub(g, 'gmb_'), 1e-10, 'lvm mc mb')
+
+
+def test_sdgpr_predict_monte_carlo():
+    """The oracle's predict_f_mc against the reference's, same seed (tests/golden/make_dgp_mc.py)."""
+    g = load('sdgpr_mc.npz')
+    p = sub(load('sdgpr_small.npz'), 'p_')
+    np.random.seed(int(g['seed']))
+    samples, mf, vf = O.sdgpr_predict_mc(p, g['xs'], int(g['no_samples']))
+    for name, got in (('samples', samples), ('mf', mf), ('vf', vf)):
+        assert_close(got, g[name], 1e-12, name)
