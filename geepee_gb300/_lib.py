@@ -52,6 +52,10 @@ _SIGS = {
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     'gpk_lincomb': [_vp, _vp],
     'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp],
+    'gpk_probit_lik': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _vp, _c_dbl, _c_dbl,
+                       _vp, _vp, _vp, _vp, _vp],
+    'gpk_lik_exp': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp,
+                    _vp, _vp, _vp],
     'gpk_gather_rows': [_c_int, ctypes.c_longlong, _vp, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp],
     'gpk_finish': [_c_int, _vp, _c_dbl, _c_int, _vp, _vp, _vp],
     'gpk_nat_prep': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],

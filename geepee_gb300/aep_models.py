@@ -198,13 +198,43 @@ def layer_init_hypers(N, M, Din, Dout, nat_param=True, x_train=None, key_suffix=
 class _PackedModel(Base_Model):
     """Parameters, gradients, energy and Cholesky status in two flat buffers (see pack.py)."""
 
+    def _lik_spec(self, lik):
+        """The likelihood layer by name (base_models.py:704-707): 'Gaussian' (Gauss_Layer, one
+        hyperparameter sn) or 'Probit' (Probit_Layer, labels in {-1, +1}, none).  Returns
+        its entries of the parameter pack."""
+        name = lik.lower()
+        if name not in ('gaussian', 'probit'):
+            raise NotImplementedError('likelihood %s not implemented' % lik)
+        self.lik = name
+        return [('sn', ())] if name == 'gaussian' else []
+
     def _make_packs(self, spec):
         self.ppack = Pack(spec, self.dev)
         self.gpack = Pack(spec + [('__energy__', ()), ('__info__', ())], self.dev)
-        self.sn = self.ppack.views['sn']
-        self.g_sn = self.gpack.views['sn']
+        self.sn = self.ppack.views.get('sn')
+        self.g_sn = self.gpack.views.get('sn')
         self.energy = self.gpack.views['__energy__']
         self._shapes = {k: s for k, s in spec}
+
+    def _lik_hypers(self):
+        """Lik_Layer.init_hypers: log(0.01) for the Gaussian noise, nothing for the probit."""
+        return {'sn': np.log(0.01)} if self.lik == 'gaussian' else {}
+
+    def _log_Z(self, m, v, yb, alpha, scale, invN, dm, dv, out, mc=False):
+        """The likelihood's compute_log_Z and backprop_grads on device tensors: dm, dv = scale *
+        dlogZ/d(m, v); out[0] = scale * invN * logZ (overwritten); for the Gaussian also the
+        sn gradient (2-D case), for the probit m, v may be [S, n, D] samples (mc=True)."""
+        if self.lik == 'probit':
+            gpk.probit_lik(m, v, yb, alpha, scale, invN, dm, dv, out, mc=mc)
+        else:
+            gpk.gauss_lik(m, v, yb, self.sn, alpha, scale, invN, dm, dv, out, self.g_sn)
+
+    def _output_probabilistic(self, mf, vf):
+        """Gauss_Layer.output_probabilistic (lik_layers.py:238-249); the reference's probit
+        layer leaves it unimplemented (lik_layers.py:459-471) and so does this one."""
+        if self.lik == 'probit':
+            raise NotImplementedError('TODO: return probablity of y=1')
+        return mf, vf + float(np.exp(2.0 * self.sn.item()))
 
     def get_hypers(self):
         return self.ppack.download(self._shapes)
@@ -224,7 +254,8 @@ class _PackedModel(Base_Model):
         """Length of the leading part of the gradient pack that holds layer gradients (every key
         before 'sn')."""
         keys = [k for k, _ in self.gpack.spec]
-        return int(self.gpack.offsets[keys.index('sn')])
+        first = next(k for k in keys if k in ('sn', 'x1', '__energy__'))
+        return int(self.gpack.offsets[keys.index(first)])
 
     def _energy_terms(self, layers, alpha, N, statuses):
         """energy += sum of the layers' weighted log-partitions / N (fused for natural-parameter
@@ -273,14 +304,12 @@ class SGPR(_PackedModel):
 
     def __init__(self, x_train, y_train, no_pseudo, lik='Gaussian', nat_param=True):
         super().__init__(y_train)
-        if lik.lower() != 'gaussian':
-            raise NotImplementedError('likelihood not implemented')
         self.N, self.Dout = y_train.shape
         self.Din = x_train.shape[1]
         self.M = no_pseudo
         self.x_train = x_train
         self.nat_param = nat_param
-        self._make_packs(DevLayer.spec(self.Din, self.Dout, self.M) + [('sn', ())])
+        self._make_packs(DevLayer.spec(self.Din, self.Dout, self.M) + self._lik_spec(lik))
         self.layer = DevLayer(self.N, self.Din, self.Dout, self.M, nat_param, self.dev,
                               self.ppack.views, self.gpack.views)
         self.sgp_layer = self.layer
@@ -290,7 +319,7 @@ class SGPR(_PackedModel):
     def init_hypers(self, y_train=None):
         """Base_SGPR.init_hypers (base_models.py:1036-1049)."""
         p = layer_init_hypers(self.N, self.M, self.Din, self.Dout, self.nat_param, self.x_train)
-        p['sn'] = np.log(0.01)
+        p.update(self._lik_hypers())
         return p
 
     def device_objective(self, idx, alpha):
@@ -303,7 +332,7 @@ class SGPR(_PackedModel):
         st = setup_layers([lay], alpha)
         m, v, kfu, Bk = lay.fwd_det(xb)
         dm, dv = torch.empty_like(m), torch.empty_like(v)
-        gpk.gauss_lik(m, v, yb, self.sn, alpha, scale, 1.0 / N, dm, dv, self.energy, self.g_sn)
+        self._log_Z(m, v, yb, alpha, scale, 1.0 / N, dm, dv, self.energy)
         lay.bwd_det(alpha, dm, dv, kfu, Bk, xb)
         self._energy_terms([lay], alpha, N, st)
         return self.energy
@@ -330,7 +359,7 @@ class SGPR(_PackedModel):
     def predict_y(self, inputs):
         """base_models.py:1020-1034 (Gauss_Layer.output_probabilistic adds exp(2 sn))."""
         mf, vf = self.predict_f(inputs)
-        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+        return self._output_probabilistic(mf, vf)
 
 
 # ------------------------------------------------------------------------------------------
@@ -346,8 +375,6 @@ class SDGPR(_PackedModel):
 
     def __init__(self, x_train, y_train, no_pseudos, hidden_sizes, lik='Gaussian'):
         super().__init__(y_train)
-        if lik.lower() != 'gaussian':
-            raise NotImplementedError('likelihood not implemented')
         self.N, self.Dout = y_train.shape
         self.Din = x_train.shape[1]
         self.size = [self.Din] + list(hidden_sizes) + [self.Dout]
@@ -357,7 +384,7 @@ class SDGPR(_PackedModel):
         spec = []
         for i in range(self.L):
             spec += DevLayer.spec(self.size[i], self.size[i + 1], self.Ms[i], '_%d' % i)
-        self._make_packs(spec + [('sn', ())])
+        self._make_packs(spec + self._lik_spec(lik))
         self.layers = [DevLayer(self.N, self.size[i], self.size[i + 1], self.Ms[i], True, self.dev,
                                 self.ppack.views, self.gpack.views, '_%d' % i) for i in range(self.L)]
         self.sgp_layers = self.layers
@@ -370,7 +397,7 @@ class SDGPR(_PackedModel):
         for i in range(self.L):
             p.update(layer_init_hypers(self.N, self.Ms[i], self.size[i], self.size[i + 1], True,
                                        self.x_train if i == 0 else None, '_%d' % i))
-        p['sn'] = np.log(0.01)
+        p.update(self._lik_hypers())
         return p
 
     def device_objective(self, idx, alpha):
@@ -396,7 +423,7 @@ class SDGPR(_PackedModel):
             ms.append(m)
             vs.append(v)
         dmi, dvi = torch.empty_like(ms[-1]), torch.empty_like(vs[-1])
-        gpk.gauss_lik(ms[-1], vs[-1], yb, self.sn, alpha, scale, 1.0 / N, dmi, dvi, self.energy, self.g_sn)
+        self._log_Z(ms[-1], vs[-1], yb, alpha, scale, 1.0 / N, dmi, dvi, self.energy)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
         main.wait_stream(side[0])   # the zeroed accumulators
@@ -474,7 +501,7 @@ class SDGPR(_PackedModel):
     def predict_y(self, inputs):
         """base_models.py:1264-1275."""
         mf, vf = self.predict_f(inputs)
-        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+        return self._output_probabilistic(mf, vf)
 
 
 # ------------------------------------------------------------------------------------------
@@ -491,16 +518,14 @@ class SGPLVM(_PackedModel):
     def __init__(self, y_train, hidden_size, no_pseudo, lik='Gaussian', prior_mean=0, prior_var=1,
                  nat_param=True):
         super().__init__(y_train)
-        if lik.lower() != 'gaussian':
-            raise NotImplementedError('likelihood not implemented')
         self.N, self.Dout = y_train.shape
         self.Din = hidden_size
         self.M = no_pseudo
         self.nat_param = nat_param
         self.prior_mean, self.prior_var = prior_mean, prior_var
         self.prior_x1, self.prior_x2 = prior_mean / prior_var, 1.0 / prior_var
-        spec = DevLayer.spec(self.Din, self.Dout, self.M) + [('sn', ()), ('x1', (self.N, self.Din)),
-                                                              ('x2', (self.N, self.Din))]
+        spec = DevLayer.spec(self.Din, self.Dout, self.M) + self._lik_spec(lik) + [('x1', (self.N, self.Din)),
+                                                                               ('x2', (self.N, self.Din))]
         self._make_packs(spec)
         self.layer = DevLayer(self.N, self.Din, self.Dout, self.M, nat_param, self.dev, self.ppack.views,
                               self.gpack.views)
@@ -508,23 +533,29 @@ class SGPLVM(_PackedModel):
         self.y_dev = _to_dev(y_train, self.dev)
 
     def init_hypers(self, y_train=None):
-        """Latent means from PCA (base_models.py:848-862); the GP part is initialised on them with
-        the layer initialiser.  (The reference additionally runs 100 L-BFGS steps of its VFE SGPR,
-        base_models.py:864-876; the VFE family is outside this package.)"""
+        """Base_SGPLVM.init_hypers (base_models.py:839-876): latent means from PCA, standardised,
+        variances 0.1; the GP part from 100 L-BFGS-B steps of a Gaussian VFE regression of y on
+        those means with sn, sf, ls and zu held at their initial values."""
         y = self.y_train if y_train is None else y_train
         from .utils import pca_reduce
+        from .vfe_models import SGPR as VFE_SGPR
         post_m = pca_reduce(y, self.Din)
         post_m = (post_m - post_m.mean(0)) / (post_m.std(0) + 1e-5)
         post_v = 0.1 * np.ones_like(post_m)
-        p = layer_init_hypers(self.N, self.M, self.Din, self.Dout, self.nat_param, post_m)
-        p['sn'] = np.log(0.01)
+        x_params = {}
         if self.nat_param:
             post_2 = 1.0 / post_v
-            p['x1'] = post_2 * post_m
-            p['x2'] = np.log(post_2 - 1) / 2
+            x_params['x1'] = post_2 * post_m
+            x_params['x2'] = np.log(post_2 - 1) / 2
         else:
-            p['x1'] = post_m
-            p['x2'] = np.log(post_v) / 2
+            x_params['x1'] = post_m
+            x_params['x2'] = np.log(post_v) / 2
+        reg = VFE_SGPR(post_m, y, self.M, 'Gaussian', self.nat_param)
+        reg.set_fixed_params(['sn', 'sf', 'ls', 'zu'])
+        reg.optimise(method='L-BFGS-B', maxiter=100, disp=False)
+        p = {k: v for k, v in reg.get_hypers().items() if k != 'sn'}
+        p.update(self._lik_hypers())
+        p.update(x_params)
         return p
 
     def device_objective(self, idx, alpha):
@@ -562,17 +593,28 @@ class SGPLVM(_PackedModel):
             sd = vcav.sqrt()
             xs = (eps * sd + mcav).reshape(S * nb, Q).contiguous()
             ms, vs, kfu, Bk = lay.fwd_det(xs)
-            logZ, dm, dv = gauss_logZ_mc(ms.view(S, nb, Dy), vs.view(S, nb, Dy), yb, self.sn, alpha)
+            if self.lik == 'probit':
+                dm, dv, logZ_s = torch.empty_like(ms), torch.empty_like(vs), torch.empty_like(self.energy)
+                self._log_Z(ms.view(S, nb, Dy), vs.view(S, nb, Dy), yb, alpha, scale, 1.0, dm, dv, logZ_s, mc=True)
+            else:
+                logZ, dm, dv0 = gauss_logZ_mc(ms.view(S, nb, Dy), vs.view(S, nb, Dy), yb, self.sn, alpha)
+                logZ_s, dm, dv = scale * logZ, (scale * dm).reshape(S * nb, Dy).contiguous(), \
+                    (scale * dv0).reshape(S * nb, Dy).contiguous()
             dxs = torch.empty_like(xs)
-            lay.bwd_det(alpha, (scale * dm).reshape(S * nb, Dy).contiguous(),
-                        (scale * dv).reshape(S * nb, Dy).contiguous(), kfu, Bk, xs, dx=dxs)
+            lay.bwd_det(alpha, dm, dv, kfu, Bk, xs, dx=dxs)
             dxs = dxs.view(S, nb, Q)
             dmx, dvx = dxs.sum(0), (dxs * eps).sum(0) / (2.0 * sd)
         else:
             m, vv = lay.fwd_mm(mcav, vcav)
-            logZ, dm, dv = gauss_logZ(m, vv, yb, self.sn, alpha)
-            dmx, dvx = lay.bwd_mm(alpha, m, scale * dm, scale * dv, mcav, vcav)
-        self.g_sn.copy_(gauss_dsn(dv, nb, self.Dout, self.sn, alpha, scale))
+            if self.lik == 'probit':
+                dm, dv, logZ_s = torch.empty_like(m), torch.empty_like(vv), torch.empty_like(self.energy)
+                self._log_Z(m, vv, yb, alpha, scale, 1.0, dm, dv, logZ_s)
+            else:
+                logZ, dm, dv0 = gauss_logZ(m, vv, yb, self.sn, alpha)
+                logZ_s, dm, dv = scale * logZ, scale * dm, scale * dv0
+            dmx, dvx = lay.bwd_mm(alpha, m, dm, dv, mcav, vcav)
+        if self.lik == 'gaussian':
+            self.g_sn.copy_(gauss_dsn(dv0, nb, self.Dout, self.sn, alpha, scale))
         phi_prior = float(0.5 * (self.prior_mean ** 2 / self.prior_var + np.log(self.prior_var))) * N * self.Din
         phi_cav, dmc, dvc = _phi_x(mcav, vcav)
         phi_post, dmp, dvp = _phi_x(mpost, vpost)
@@ -603,7 +645,7 @@ class SGPLVM(_PackedModel):
         gx2.zero_()
         gx1.index_put_((idx,), dt1 + h1, accumulate=True)
         gx2.index_put_((idx,), dt2 + h2, accumulate=True)
-        self.energy.copy_((scale * logZ + xc + lay.phi(alpha)).reshape(1))
+        self.energy.copy_((logZ_s + xc + lay.phi(alpha)).reshape(1))
         self._flag_info(st)
         return self.energy
 
@@ -637,7 +679,7 @@ class SGPLVM(_PackedModel):
 
     def predict_y(self, inputs):
         mf, vf = self.predict_f(inputs)
-        return mf, vf + float(np.exp(2.0 * self.sn.item()))
+        return self._output_probabilistic(mf, vf)
 
     def get_posterior_x(self, idxs=None):
         """base_models.py:765-775."""

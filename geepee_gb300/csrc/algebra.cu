@@ -182,6 +182,173 @@ __global__ void __launch_bounds__(1024) gauss_sum_kernel(int n, int D, const dou
   }
 }
 
+// Probit likelihood of binary labels y in {-1, +1} (Probit_Layer.compute_log_Z,
+// geepee/lik_layers.py:303-416).  A group of 16 lanes owns one output element e of the
+// n x D minibatch.  alpha == 1 takes the closed form: lane s computes sample s,
+//   t = y m / sqrt(1 + v),  Z = (1 + erf(t / sqrt 2)) / 2,  logZ = log(Z + eps),
+//   dlogZ/dm = phi(t)/(Z + eps) y / sqrt(1 + v),  dlogZ/dv = -phi(t)/(Z + eps) y m / (2 (1 + v)^1.5).
+// Otherwise Gauss-Hermite quadrature of the alpha power: lane k takes node k of T <= 16 and
+// the group sums over the lanes with shuffles,
+//   ts = x_k sqrt(2 v) + m,  p_k = (1 + erf(y ts / sqrt 2)) / 2 + eps,
+//   Zt = sum_k w_k p_k^alpha / sqrt(pi),  logZ = log Zt,
+//   dZ/dm = sum_k w_k p_k^(alpha-1) exp(-ts^2/2) y alpha / (pi sqrt 2),  dZ/dv = the same with
+//   an extra x_k, over sqrt(2 v);  dlogZ/dm = dZ/dm / Zt + eps (and likewise for v).
+// The 2-D case (mc = 0, S = 1) uses eps = 1e-8 for the quadrature and 1e-16 for the closed
+// form; the sampled 3-D case (mc = 1, m and v [S, n, D]) uses 1e-16 for both and a
+// log-mean-exp over the S <= 16 samples, each sample's gradient weighted by its softmax share
+// (added eps after the weighting, as the reference does).  The reference's float64 numpy
+// expressions are followed operation for operation; erf, exp and log are CUDA's float64
+// functions (p^a is exp(a log p)).  dm, dv are written times `scale`; work[e] = the element's
+// log-partition for the sum kernel.
+__global__ void __launch_bounds__(128) probit_terms_kernel(int S, int nD, int mc, const double* m, const double* v,
+                                                           const double* y, double alpha, int T, const double* gh_x,
+                                                           const double* gh_w, double scale, double* dm, double* dv,
+                                                           double* work) {
+  const int lane = threadIdx.x & 15;
+  const int e = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 4);
+  if (e >= nD) return;   // whole 16-lane groups leave together
+  const unsigned gmask = 0xffffu << (threadIdx.x & 16);
+  const double ye = y[e];
+  const double kSqrt2 = 1.4142135623730951, kSqrtPi = 1.7724538509055159, kPi = 3.141592653589793;
+  double my_lz = -INFINITY, my_dm = 0.0, my_dv = 0.0;
+  if (alpha == 1.0) {
+    const double eps = 1e-16;
+    if (lane < S) {
+      const double mm = m[(long)lane * nD + e], vv = v[(long)lane * nD + e];
+      const double sv = sqrt(1.0 + vv);
+      const double t = ye * mm / sv;
+      const double Z = 0.5 * (1.0 + erf(t / kSqrt2));
+      my_lz = log(Z + eps);
+      const double g = 1.0 / (Z + eps) / sqrt(2.0 * kPi) * exp(-t * t / 2.0);
+      my_dm = g * (ye / sv);
+      my_dv = g * (-0.5 * ye * mm / ((1.0 + vv) * sv));
+    }
+  } else {
+    const double eps = mc ? 1e-16 : 1e-8;
+    const bool node = lane < T;
+    const double xk = node ? gh_x[lane] : 0.0, wk = node ? gh_w[lane] : 0.0;
+    const double c = ye * alpha / kPi / kSqrt2;
+    for (int s = 0; s < S; ++s) {
+      const double mm = m[(long)s * nD + e], vv = v[(long)s * nD + e];
+      const double s2v = sqrt(2.0 * vv);
+      double zt = 0.0, am = 0.0, av = 0.0;
+      if (node) {
+        const double ts = xk * s2v + mm;
+        const double p = 0.5 * (1.0 + erf(ye * ts / kSqrt2)) + eps;
+        const double lp = log(p);
+        const double pa = exp(alpha * lp);
+        const double a = exp((alpha - 1.0) * lp) * exp(-ts * ts / 2.0);
+        zt = pa * wk;
+        am = wk * a;
+        av = wk * (a * xk);
+      }
+#pragma unroll
+      for (int o = 8; o >= 1; o >>= 1) {
+        zt += __shfl_xor_sync(gmask, zt, o);
+        am += __shfl_xor_sync(gmask, am, o);
+        av += __shfl_xor_sync(gmask, av, o);
+      }
+      zt = zt / kSqrtPi;
+      if (lane == s) {
+        my_lz = log(zt);
+        my_dm = am * c / zt;
+        my_dv = av * c / s2v / zt;
+      }
+    }
+  }
+  double lse = my_lz, w = 1.0;
+  if (mc) {
+    double mx = my_lz;
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(gmask, mx, o));
+    const double ex = lane < S ? exp(my_lz - mx) : 0.0;
+    double se = ex;
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) se += __shfl_xor_sync(gmask, se, o);
+    lse = mx + log(se) - log((double)S);
+    w = ex / se;
+  }
+  if (lane < S) {
+    const double add = alpha == 1.0 ? 0.0 : (mc ? 1e-16 : 1e-8);
+    dm[(long)lane * nD + e] = scale * (w * my_dm + add);
+    dv[(long)lane * nD + e] = scale * (w * my_dv + add);
+  }
+  if (lane == 0) work[e] = lse;
+}
+
+// Expected log-likelihood under q(f) = N(m, v), the variational free energy's data term.
+// kind 0, Gaussian (Gauss_Layer.compute_log_lik_exp and backprop_grads_log_lik_exp,
+// geepee/lik_layers.py:183-228), lane 0 of each 16-lane group:
+//   q = y^2 - 2 y m + m^2 + v,  ll = -log(2 pi sn2)/2 - q/(2 sn2),  dm = (y - m)/sn2,
+//   dv = -1/(2 sn2), and the element's sn term -1 + q/sn2 into work[nD + e].
+// kind 1, probit (Probit_Layer.compute_log_lik_exp, lik_layers.py:418-436), lane k = node k:
+//   ts = x_k sqrt(2 v) + m, z = y ts,  ll = sum_k w_k/sqrt(pi) log Phi(z),
+//   dm = sum_k y w_k/sqrt(pi) phi(z)/Phi(z),  dv = sum_k (the same) x_k sqrt(2/v)/2,
+// with Phi(z) = erfc(-z/sqrt 2)/2 and log Phi(z) = log1p(-erfc(z/sqrt 2)/2) for z > 0 (both
+// accurate in the tails, as scipy's norm.cdf / norm.logcdf are).  dm, dv are written times
+// `scale`; work[e] = the element's ll.
+__global__ void __launch_bounds__(128) lik_exp_kernel(int kind, int nD, const double* m, const double* v,
+                                                      const double* y, const double* sn, int T, const double* gh_x,
+                                                      const double* gh_w, double scale, double* dm, double* dv,
+                                                      double* work) {
+  const int lane = threadIdx.x & 15;
+  const int e = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 4);
+  if (e >= nD) return;   // whole 16-lane groups leave together
+  const unsigned gmask = 0xffffu << (threadIdx.x & 16);
+  const double mm = m[e], vv = v[e], ye = y[e];
+  const double kSqrt2 = 1.4142135623730951, kSqrtPi = 1.7724538509055159, kPi = 3.141592653589793;
+  if (kind == 0) {
+    if (lane != 0) return;
+    const double sn2 = exp(2.0 * sn[0]);
+    const double q = ye * ye - 2.0 * ye * mm + mm * mm + vv;
+    work[e] = -0.5 * log(2.0 * kPi * sn2) - 0.5 / sn2 * q;
+    work[nD + e] = -1.0 + q / sn2;
+    dm[e] = scale * (1.0 / sn2 * (ye - mm));
+    dv[e] = scale * (-0.5 / sn2);
+    return;
+  }
+  double ll = 0.0, gm = 0.0, gv = 0.0;
+  if (lane < T) {
+    const double xk = gh_x[lane], wk = gh_w[lane] / kSqrtPi;
+    const double z = (xk * sqrt(2.0 * vv) + mm) * ye;
+    const double cdf = 0.5 * erfc(-z / kSqrt2);
+    const double lcdf = z > 0.0 ? log1p(-0.5 * erfc(z / kSqrt2)) : log(cdf);
+    const double g = ye * wk * (exp(-0.5 * z * z) / sqrt(2.0 * kPi)) / cdf;
+    ll = wk * lcdf;
+    gm = g;
+    gv = g * (0.5 * xk * sqrt(2.0 / vv));
+  }
+#pragma unroll
+  for (int o = 8; o >= 1; o >>= 1) {
+    ll += __shfl_xor_sync(gmask, ll, o);
+    gm += __shfl_xor_sync(gmask, gm, o);
+    gv += __shfl_xor_sync(gmask, gv, o);
+  }
+  if (lane == 0) {
+    work[e] = ll;
+    dm[e] = scale * gm;
+    dv[e] = scale * gv;
+  }
+}
+
+// out[0] = scale * invN * sum(work[0:nD]) in a fixed order (one CTA).
+__global__ void __launch_bounds__(1024) sum_scaled_kernel(int nD, const double* work, double scale, double invN,
+                                                          double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nD; i += blockDim.x) s += work[i];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[0] = scale * invN * s;
+  }
+}
+
 int grid_for(long n) {
   long g = (n + 255) / 256;
   long cap = 4L * gpk::sm_count();
@@ -243,6 +410,39 @@ extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, con
   if (nD > 0) gauss_grad_kernel<<<(nD + 127) / 128, 128, 0, st>>>(nD, m, v, y, sn, alpha, scale, dm, dv);
   gauss_sum_kernel<<<1, 1024, 0, st>>>(n, D, m, v, y, sn, dv, alpha, scale, invN, energy, g_sn);
   return gpk::check_launch("gauss_lik");
+}
+
+extern "C" int gpk_probit_lik(int S, int n, int D, int mc, const double* m, const double* v, const double* y,
+                              double alpha, int T, const double* gh_x, const double* gh_w, double scale,
+                              double invN, double* dm, double* dv, double* work, double* out, void* stream) {
+  GPK_REQUIRE(n >= 0 && D >= 1 && S >= 1 && S <= 16 && (mc || S == 1) && alpha > 0 && scale != 0.0,
+              "probit_lik: bad sizes");
+  GPK_REQUIRE(alpha == 1.0 || (T >= 1 && T <= 16 && gh_x && gh_w), "probit_lik: need 1..16 Gauss-Hermite nodes");
+  const long nD = (long)n * D;
+  GPK_REQUIRE(out && (nD == 0 || (m && v && y && dm && dv && work)), "probit_lik: null pointer");
+  cudaStream_t st = gpk::as_stream(stream);
+  GPK_REQUIRE(nD * S < (1L << 31) / 16, "probit_lik: too many elements");
+  if (nD > 0) probit_terms_kernel<<<(int)((nD * 16 + 127) / 128), 128, 0, st>>>(S, (int)nD, mc, m, v, y, alpha, T,
+                                                                                gh_x, gh_w, scale, dm, dv, work);
+  sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nD, work, scale, invN, out);
+  return gpk::check_launch("probit_lik");
+}
+
+extern "C" int gpk_lik_exp(int kind, int n, int D, const double* m, const double* v, const double* y,
+                           const double* sn, int T, const double* gh_x, const double* gh_w, double scale, double invN,
+                           double* dm, double* dv, double* work, double* out, double* g_sn, void* stream) {
+  GPK_REQUIRE((kind == 0 || kind == 1) && n >= 0 && D >= 1 && scale != 0.0, "lik_exp: bad sizes");
+  GPK_REQUIRE(kind == 0 || (T >= 1 && T <= 16 && gh_x && gh_w), "lik_exp: need 1..16 Gauss-Hermite nodes");
+  const long nD = (long)n * D;
+  GPK_REQUIRE(nD < (1L << 31) / 16, "lik_exp: too many elements");
+  GPK_REQUIRE(out && (kind == 1 || (sn && g_sn)) && (nD == 0 || (m && v && y && dm && dv && work)),
+              "lik_exp: null pointer");
+  cudaStream_t st = gpk::as_stream(stream);
+  if (nD > 0) lik_exp_kernel<<<(int)((nD * 16 + 127) / 128), 128, 0, st>>>(kind, (int)nD, m, v, y, sn, T, gh_x,
+                                                                           gh_w, scale, dm, dv, work);
+  sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nD, work, scale, invN, out);
+  if (kind == 0) sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nD, work + nD, scale, invN, g_sn);
+  return gpk::check_launch("lik_exp");
 }
 
 namespace {

@@ -8,6 +8,7 @@ inside the library, and is safe to capture in a CUDA graph.  Accumulating output
 from __future__ import annotations
 
 import ctypes
+import numpy as np
 
 import torch
 
@@ -306,6 +307,45 @@ def gauss_lik(m, v, y, sn, alpha, scale, invN, dm, dv, energy, g_sn):
     n, D = y.shape
     call('gpk_gauss_lik', n, D, ptr(m), ptr(v), ptr(y), ptr(sn), float(alpha), float(scale), float(invN), ptr(dm),
          ptr(dv), ptr(energy), ptr(g_sn), stream())
+
+
+GH_DEGREE = 10   # Gauss-Hermite nodes of the probit quadrature (config.py:12)
+_gh_cache = {}
+
+
+def gh_nodes(dev, T=GH_DEGREE):
+    """np.polynomial.hermite.hermgauss(T) as one device tensor [2, T] (nodes, weights)."""
+    key = (str(dev), T)
+    if key not in _gh_cache:
+        x, w = np.polynomial.hermite.hermgauss(T)
+        _gh_cache[key] = torch.tensor(np.stack([x, w]), dtype=torch.float64, device=dev)
+    return _gh_cache[key]
+
+
+def probit_lik(m, v, y, alpha, scale, invN, dm, dv, out, work=None, mc=False):
+    """Probit log-partition and its gradients (lik_layers.py:303-416).  m, v: [n, D], or
+    [S, n, D] with mc=True (log-mean-exp over the S samples); y [n, D] in {-1, +1}.  Writes
+    dm, dv (times scale) and out[0] = scale * invN * logZ; returns the per-element scratch."""
+    n, D = y.shape
+    S = m.shape[0] if mc else 1
+    if work is None:
+        work = torch.empty(n * D, dtype=torch.float64, device=m.device)
+    gh = gh_nodes(m.device)
+    call('gpk_probit_lik', S, n, D, int(mc), ptr(m), ptr(v), ptr(y), float(alpha), gh.shape[1], ptr(gh[0]),
+         ptr(gh[1]), float(scale), float(invN), ptr(dm), ptr(dv), ptr(work), ptr(out), stream())
+    return work
+
+
+def lik_exp(kind, m, v, y, scale, invN, dm, dv, out, sn=None, g_sn=None):
+    """E_q[log p(y | f)] for q(f) = N(m, v) [n, D] and its gradients (lik_layers.py:183-228,
+    418-436): kind 'gaussian' (also the sn gradient into g_sn) or 'probit'.  Writes dm, dv
+    (times scale) and out[0] = scale * invN * sum."""
+    n, D = y.shape
+    k = 0 if kind == 'gaussian' else 1
+    work = torch.empty((2 - k) * n * D, dtype=torch.float64, device=m.device)
+    gh = gh_nodes(m.device)
+    call('gpk_lik_exp', k, n, D, ptr(m), ptr(v), ptr(y), ptr(sn), gh.shape[1], ptr(gh[0]), ptr(gh[1]), float(scale),
+         float(invN), ptr(dm), ptr(dv), ptr(work), ptr(out), ptr(g_sn), stream())
 
 
 def gather_rows(idx, x, y=None):

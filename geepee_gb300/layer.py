@@ -415,6 +415,39 @@ class DevLayer:
         self.g['eta1_R'].copy_(e1c + e1p)
         self.g['eta2'].copy_(e2c + e2p)
 
+    # ---------------------------------------------------------------- VFE (vfe_models.py)
+    def kl(self):
+        """SGP_Layer.compute_KL (vfe_models.py:309-326) as a device scalar:
+        1/2 (D logdet Kuu - sum_d logdet Su_d - D M + sum_d tr(Kuu^-1 (Su_d + mu_d mu_d^T)))."""
+        D, M = self.Dout, self.M
+        lsu = self.logdetSu if self.logdetSu is not None else -self.ldSuinv
+        tr = (self.Kinv.unsqueeze(0) * self.Spmm).sum()
+        return 0.5 * (D * self.logdetK - lsu.sum() - D * M + tr)
+
+    def bwd_det_vfe(self, dm, dv, kfu, Bk, x):
+        """VFE SGP_Layer.backprop_grads_reg (vfe_models.py:479-548): deterministic inputs through
+        the posterior predictive (A, B_det), upstream dm, dv already scaled, plus the KL term's
+        gradients.  Written into the layer's gradient slots."""
+        D, M = self.Dout, self.M
+        K = self.Kinv
+        self.zero_accumulators()
+        dA, dB = self._dAh, self._dBh
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.A, kfu, Bk, dm, dv, self._dsf2, self._dl, self.g['zu'],
+                    dA)
+        self._kernel_grads(self._dsf2, self._dl, dv)
+        gpk.gram(kfu, kfu, dv, dB)
+        # sum_n dm_nd (kfu_n K^-1) = dA_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T = K^-1 dB_d K^-1;
+        # the KL adds K^-1 mu_d to dmu and (K^-1 - Su^-1)/2 to dSu
+        dmu = mm(dA, K, beta=1.0, E=mm(self.mu, K))
+        dSu = gpk.lincomb(torch.empty_like(self.Suinv), [(1.0, mm(mm(K, dB), K)), (0.5, K), (-0.5, self.Suinv)])
+        e1, e2, dKu = self._post_grad_u(dmu, dSu)
+        KS = mm(K, self.Su)
+        dK = (mm(dA, self.mu, tA=True) + 2.0 * mm(KS.reshape(D * M, M), dB.reshape(D * M, M), tA=True)
+              - dB.sum(0) + dKu - 0.5 * D * self.Kuu + 0.5 * self.Spmm.sum(0))
+        self._finish_hyp(mm(mm(K, dK), K, alpha=-1.0))
+        self.g['eta1_R'].copy_(e1)
+        self.g['eta2'].copy_(e2)
+
     def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x, dx=None):
         """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
         compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so

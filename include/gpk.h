@@ -273,6 +273,31 @@ int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, con
 int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn, double alpha,
                   double scale, double invN, double* dm, double* dv, double* energy, double* g_sn, void* stream);
 
+/* Probit likelihood of labels y in {-1, +1} (Probit_Layer.compute_log_Z,
+ * geepee/lik_layers.py:303-416; the layer has no hyperparameters, so backprop_grads
+ * returns nothing).  mc = 0, S = 1: the 2-D case, m, v, y [n, D].  mc = 1: the sampled
+ * 3-D case, m, v [S, n, D] (S <= 16) against y [n, D], a log-mean-exp over the samples.
+ * alpha == 1 is the closed form with erf; any other alpha uses T <= 16 Gauss-Hermite nodes
+ * gh_x, gh_w (device float64; np.polynomial.hermite.hermgauss(T), T = 10 in the reference).
+ * Writes dm, dv = scale * (dlogZ/dm, dlogZ/dv) shaped like m, work[0:n*D] (each element's
+ * log-partition; caller scratch) and *out = scale * invN * logZ (overwritten).  With n = 0 only
+ * out is read (it is set to 0). */
+int gpk_probit_lik(int S, int n, int D, int mc, const double* m, const double* v, const double* y, double alpha,
+                   int T, const double* gh_x, const double* gh_w, double scale, double invN, double* dm,
+                   double* dv, double* work, double* out, void* stream);
+
+/* Expected log-likelihood of a minibatch under q(f) = N(m, v), the data term of the
+ * variational free energy, m, v, y [n, D]:
+ *   kind 0, Gaussian (Gauss_Layer.compute_log_lik_exp, backprop_grads_log_lik_exp,
+ *     geepee/lik_layers.py:183-228): *g_sn = scale * invN * sum(-1 + (y^2 - 2ym + m^2 + v)/sn2),
+ *     work [2 n D];
+ *   kind 1, probit (Probit_Layer.compute_log_lik_exp, lik_layers.py:418-436) with T <= 16
+ *     Gauss-Hermite nodes gh_x, gh_w (hermgauss(T)); sn and g_sn unused; work [n D].
+ * Writes dm, dv = scale * d/d(m, v) and *out = scale * invN * sum E[log p(y|f)] (overwritten). */
+int gpk_lik_exp(int kind, int n, int D, const double* m, const double* v, const double* y, const double* sn, int T,
+                const double* gh_x, const double* gh_w, double scale, double invN, double* dm, double* dv,
+                double* work, double* out, double* g_sn, void* stream);
+
 /* Minibatch rows of two row-major float64 arrays in one launch, x[idx] and y[idx] of
  * geepee/aep_models.py:912-916 (rows = the arrays' row count): d0[i,:] = s0[idx[i],:] with c0
  * columns and d1[i,:] = s1[idx[i],:] with c1 columns (c1 = 0: none).  An index outside

@@ -17,6 +17,7 @@ variance), mu/S the Gaussian input means/variances [N,Q], Z the pseudo-inputs
 from __future__ import annotations
 
 import numpy as np
+from scipy import special
 
 JITTER = 1e-5  # geepee/config.py:11
 
@@ -364,6 +365,37 @@ def bwd_det(L, N, alpha, dm, dv, kfu, x, grad_x=False):
     return (g, dx) if grad_x else g
 
 
+def vfe_kl(L):
+    """``SGP_Layer.compute_KL`` vfe_models.py:309-326: KL(q(u) || p(u)) summed over the outputs,
+    1/2 (D logdet Kuu - sum_d logdet Su_d - D M + sum_d tr(Kuu^-1 (Su_d + mu_d mu_d^T)))."""
+    D, M = L['Dout'], L['M']
+    ld_prior = D * np.linalg.slogdet(L['Kuu'])[1]
+    ld_post = np.sum(np.linalg.slogdet(L['Su'])[1])
+    return 0.5 * (ld_prior - ld_post - D * M + np.sum(L['Kinv'][None] * L['Spmm']))
+
+
+def vfe_bwd_det(L, dm, dv, kfu, x):
+    """VFE ``SGP_Layer.backprop_grads_reg`` vfe_models.py:479-548: the expected log-likelihood's
+    gradients through the posterior predictive (dm, dv already scaled) plus the KL term's."""
+    ell = np.exp(L['ls'])
+    sf2 = np.exp(2 * L['sf'])
+    K = L['Kinv']
+    kK = kfu @ K
+    dkfu = dm @ L['A'] + 2 * np.einsum('nd,dab,na->nb', dv, L['B_det'], kfu)
+    dsf2, dl, dz = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'])
+    dls = dl * ell
+    dsf = 2 * sf2 * (dsf2 + dv.sum())
+    dmu = dm.T @ kK + np.einsum('ab,db->da', K, L['mu'])
+    dSu = np.einsum('na,nd,nb->dab', kK, dv, kK) + 0.5 * (K[None] - L['Suinv'])
+    e1, e2, dKu = _post_grad_u(L, dmu, dSu)
+    dA = dm.T @ kfu
+    dB = np.einsum('nd,na,nb->dab', dv, kfu, kfu)
+    dK = (dA.T @ L['mu'] + 2 * np.einsum('dab,dac->bc', K[None] @ L['Su'], dB) - dB.sum(0) + dKu
+          - 0.5 * L['Dout'] * L['Kuu'] + 0.5 * L['Spmm'].sum(0))
+    dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, -K @ dK @ K)
+    return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1, 'eta2': e2}
+
+
 # --------------------------------------------------------------------------
 # likelihood / emission (lik_layers.py)
 # --------------------------------------------------------------------------
@@ -394,6 +426,110 @@ def gauss_logZ_mc(m, v, y, sn, alpha):
     logZ = np.sum(lmax + np.log(se) - np.log(m.shape[0]))
     w = e / se
     return logZ, w * r / vt, w * (-0.5 / vt + 0.5 * r ** 2 / vt ** 2)
+
+
+GH_DEGREE = 10   # config.py:12
+
+
+def _probit_cdf(z):
+    """(1 + erf(z / sqrt 2)) / 2, the form lik_layers.py:321, 345 uses."""
+    return 0.5 * (1 + special.erf(z / np.sqrt(2)))
+
+
+def probit_logZ(m, v, y, alpha):
+    """``Probit_Layer.compute_log_Z``, 2-D case lik_layers.py:318-361, for labels y in {-1, +1}:
+    the closed form with erf when alpha == 1, else Gauss-Hermite quadrature (GH_DEGREE nodes)
+    of the alpha power of the probit, with its 1e-8 guards (on the probabilities and, as the
+    reference does, added to both gradients)."""
+    if alpha == 1.0:
+        s = np.sqrt(1 + v)
+        t = y * m / s
+        Z = _probit_cdf(t)
+        g = 1 / (Z + 1e-16) / np.sqrt(2 * np.pi) * np.exp(-t ** 2 / 2)
+        return np.sum(np.log(Z + 1e-16)), g * (y / s), g * (-0.5 * y * m / (1 + v) ** 1.5)
+    x, w = np.polynomial.hermite.hermgauss(GH_DEGREE)
+    x, w = x[:, None, None], w[:, None, None]
+    ts = x * np.sqrt(2 * v)[None] + m[None]
+    p = _probit_cdf(y * ts) + 1e-8
+    Zt = np.sum(w * p ** alpha, axis=0) / np.sqrt(np.pi)
+    a = p ** (alpha - 1) * np.exp(-ts ** 2 / 2)
+    c = y * alpha / np.pi / np.sqrt(2)
+    return (np.sum(np.log(Zt)), np.sum(w * a, axis=0) * c / Zt + 1e-8,
+            np.sum(w * a * x, axis=0) * c / np.sqrt(2 * v) / Zt + 1e-8)
+
+
+def probit_logZ_mc(m, v, y, alpha):
+    """``Probit_Layer.compute_log_Z``, 3-D case lik_layers.py:363-410: m, v [S, n, D] against
+    y [n, D]; per-sample log-partitions (guards 1e-16), a log-mean-exp over the samples, each
+    sample's gradient weighted by its softmax share (plus 1e-16 in the quadrature form)."""
+    if alpha == 1.0:
+        s = np.sqrt(1 + v)
+        t = y * m / s
+        Z = _probit_cdf(t)
+        lz = np.log(Z + 1e-16)
+        g = 1 / (Z + 1e-16) / np.sqrt(2 * np.pi) * np.exp(-t ** 2 / 2)
+        dm, dv, add = g * (y / s), g * (-0.5 * y * m / (1 + v) ** 1.5), 0.0
+    else:
+        x, w = np.polynomial.hermite.hermgauss(GH_DEGREE)
+        x, w = x[:, None, None, None], w[:, None, None, None]
+        ts = x * np.sqrt(2 * v) + m
+        p = _probit_cdf(y * ts) + 1e-16
+        Zt = np.sum(w * p ** alpha, axis=0) / np.sqrt(np.pi)
+        lz = np.log(Zt)
+        a = p ** (alpha - 1) * np.exp(-ts ** 2 / 2)
+        c = y * alpha / np.pi / np.sqrt(2)
+        dm, dv, add = np.sum(w * a, axis=0) * c / Zt, np.sum(w * a * x, axis=0) * c / np.sqrt(2 * v) / Zt, 1e-16
+    lmax = lz.max(0)
+    e = np.exp(lz - lmax)
+    se = e.sum(0)
+    wgt = e / se
+    return np.sum(lmax + np.log(se) - np.log(m.shape[0])), wgt * dm + add, wgt * dv + add
+
+
+def lik_logZ(lik, m, v, y, p, alpha):
+    """The likelihood layer's compute_log_Z (2-D) by name: 'gaussian' or 'probit'."""
+    return gauss_logZ(m, v, y, p['sn'], alpha) if lik == 'gaussian' else probit_logZ(m, v, y, alpha)
+
+
+def gauss_lik_exp(m, v, y, sn):
+    """``Gauss_Layer.compute_log_lik_exp`` (2-D) lik_layers.py:183-207: E_q[log N(y; f, sn2)]
+    summed, its gradients, and ``backprop_grads_log_lik_exp``'s sn gradient per unit scale
+    (:220-228)."""
+    sn2 = np.exp(2.0 * _scalar(sn))
+    q = y ** 2 - 2 * y * m + m ** 2 + v
+    return (np.sum(-0.5 * np.log(2 * np.pi * sn2) - 0.5 / sn2 * q), (y - m) / sn2,
+            -0.5 / sn2 * np.ones_like(v), np.sum(-1 + q / sn2))
+
+
+def probit_lik_exp(m, v, y):
+    """``Probit_Layer.compute_log_lik_exp`` (2-D) lik_layers.py:418-436: E_q[log Phi(y f)] by
+    GH_DEGREE-node Gauss-Hermite quadrature, and its gradients."""
+    from scipy.stats import norm
+    x, w = np.polynomial.hermite.hermgauss(GH_DEGREE)
+    x, w = x[:, None, None], w[:, None, None] / np.sqrt(np.pi)
+    ts = x * np.sqrt(2 * v)[None] + m[None]
+    z = ts * y
+    g = y * w * norm.pdf(z) / norm.cdf(z)
+    return np.sum(w * norm.logcdf(z)), np.sum(g, axis=0), np.sum(g * (0.5 * x * np.sqrt(2 / v[None])), axis=0)
+
+
+def vfe_sgpr_objective(x, y, p, idx=None, nat_param=True, fixed=(), lik='gaussian'):
+    """VFE ``SGPR.objective_function`` vfe_models.py:572-632: -N/n E_q[log p(y_b | f)] + KL,
+    divided by N, through the posterior (forward_prop_thru_post)."""
+    N = y.shape[0]
+    xb, yb = (x, y) if idx is None else (x[idx], y[idx])
+    Mz, Dout = _layer_dims(p, '')
+    scale = -N / yb.shape[0]
+    L = layer_unpack(p, '', Mz, Dout, nat_param)
+    m, v, kfu = fwd_det(L, xb, cav=False)
+    if lik == 'gaussian':
+        ll, dm, dv, dsn = gauss_lik_exp(m, v, yb, p['sn'])
+    else:
+        ll, dm, dv = probit_lik_exp(m, v, yb)
+    g = vfe_bwd_det(L, scale * dm, scale * dv, kfu, xb)
+    if lik == 'gaussian':
+        g['sn'] = scale * dsn
+    return _finish(scale * ll + vfe_kl(L), g, N, fixed)
 
 
 def gauss_dsn(dv, nb, D, sn, alpha, scale):
@@ -447,21 +583,22 @@ def _finish(energy, grads, N, fixed=(), divide=True):
     return energy, grads
 
 
-def sgpr_objective(x, y, p, alpha, idx=None, nat_param=True, fixed=()):
-    """``SGPR.objective_function`` aep_models.py:610-667 (Gaussian likelihood)."""
+def sgpr_objective(x, y, p, alpha, idx=None, nat_param=True, fixed=(), lik='gaussian'):
+    """``SGPR.objective_function`` aep_models.py:610-667 (Gaussian or probit likelihood)."""
     N = y.shape[0]
     xb, yb = (x, y) if idx is None else (x[idx], y[idx])
     Mz, Dout = _layer_dims(p, '')
     scale = -N / yb.shape[0] / alpha
     L = layer_cavity(layer_unpack(p, '', Mz, Dout, nat_param), N, alpha)
     m, v, kfu = fwd_det(L, xb)
-    logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
+    logZ, dm, dv = lik_logZ(lik, m, v, yb, p, alpha)
     g = bwd_det(L, N, alpha, scale * dm, scale * dv, kfu, xb)
-    g['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
+    if lik == 'gaussian':
+        g['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
     return _finish(scale * logZ + layer_phi(L, N, alpha), g, N, fixed)
 
 
-def sdgpr_objective(x, y, p, alpha, idx=None, fixed=()):
+def sdgpr_objective(x, y, p, alpha, idx=None, fixed=(), lik='gaussian'):
     """``SDGPR.objective_function`` aep_models.py:895-988 (moment matching)."""
     N = y.shape[0]
     xb, yb = (x, y) if idx is None else (x[idx], y[idx])
@@ -483,7 +620,7 @@ def sdgpr_objective(x, y, p, alpha, idx=None, fixed=()):
             aux.append((p1, p2))
         ms.append(m)
         vs.append(v)
-    logZ, dm, dv = gauss_logZ(ms[-1], vs[-1], yb, p['sn'], alpha)
+    logZ, dm, dv = lik_logZ(lik, ms[-1], vs[-1], yb, p, alpha)
     dmi, dvi = scale * dm, scale * dv
     grads = {}
     for i in range(nl - 1, -1, -1):
@@ -495,7 +632,8 @@ def sdgpr_objective(x, y, p, alpha, idx=None, fixed=()):
             dmi, dvi = gi['mx'], gi['vx']
         for k, val in gh.items():
             grads['%s_%d' % (k, i)] = val
-    grads['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
+    if lik == 'gaussian':
+        grads['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
     energy = scale * logZ + sum(layer_phi(L, N, alpha) for L in layers)
     return _finish(energy, grads, N, fixed)
 
@@ -504,7 +642,7 @@ MC_NO_SAMPLES = 5   # config.py:16
 
 
 def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
-                     nat_param=True, fixed=(), eps=None):
+                     nat_param=True, fixed=(), eps=None, lik='gaussian'):
     """``SGPLVM.objective_function`` aep_models.py:694-815 (energy not divided by N): moment
     matching, or, with ``eps`` [MC_NO_SAMPLES, n, Q] (standard normal draws), Monte Carlo
     propagation of the cavity samples x = eps sqrt(v) + m through the deterministic layer
@@ -535,19 +673,22 @@ def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
     mpost, vpost = post1[idx] / post2[idx], 1.0 / post2[idx]
     if eps is None:
         m, v, p1, p2 = fwd_mm(L, mcav, vcav)
-        logZ, dm, dv = gauss_logZ(m, v, yb, p['sn'], alpha)
+        logZ, dm, dv = lik_logZ(lik, m, v, yb, p, alpha)
         gh, gi = bwd_mm(L, N, alpha, m, scale * dm, scale * dv, p1, p2, mcav, vcav)
     else:
         S = eps.shape[0]
         xs = (eps * np.sqrt(vcav) + mcav).reshape(S * nb, Q)
         ms, vs, kfu = fwd_det(L, xs, cav=True)
-        logZ, dm, dv = gauss_logZ_mc(ms.reshape(S, nb, Dy), vs.reshape(S, nb, Dy), yb, p['sn'], alpha)
+        ms, vs = ms.reshape(S, nb, Dy), vs.reshape(S, nb, Dy)
+        logZ, dm, dv = (gauss_logZ_mc(ms, vs, yb, p['sn'], alpha) if lik == 'gaussian'
+                        else probit_logZ_mc(ms, vs, yb, alpha))
         gh, dx = bwd_det(L, N, alpha, scale * dm.reshape(S * nb, Dy), scale * dv.reshape(S * nb, Dy), kfu, xs,
                          grad_x=True)
         dx = dx.reshape(eps.shape)
         gi = {'mx': dx.sum(0), 'vx': np.sum(dx * eps, axis=0) / (2 * np.sqrt(vcav))}
     grads = dict(gh)
-    grads['sn'] = gauss_dsn(dv, nb, Dy, p['sn'], alpha, scale)
+    if lik == 'gaussian':
+        grads['sn'] = gauss_dsn(dv, nb, Dy, p['sn'], alpha, scale)
 
     def phi_x(mx, vx):                                           # aep_models.py:863-867
         return np.sum(0.5 * (mx ** 2 / vx + np.log(vx))), mx / vx, 0.5 * (-mx ** 2 / vx ** 2 + 1 / vx)

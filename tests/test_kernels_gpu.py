@@ -284,3 +284,74 @@ def test_gemm_group_matches_single_products():
     assert_close(c3.cpu().numpy(), an.T @ bn, 1e-12)
     assert_close(c4.cpu().numpy(), Sn @ Kn - En, 1e-12)
     assert_close(c5.cpu().numpy(), 2.0 * Sn.reshape(300, 100).T @ Sn.reshape(300, 100) + En, 1e-12)
+
+
+@pytest.mark.parametrize('alpha', [1.0, 0.5, 0.3])
+@pytest.mark.parametrize('S,n,D', [(1, 37, 3), (1, 1000, 1), (5, 13, 2), (1, 0, 2)])
+def test_probit_lik_vs_oracle(alpha, S, n, D):
+    """gpk_probit_lik against the oracle's Probit_Layer.compute_log_Z (2-D for S = 1, the
+    sampled 3-D log-mean-exp form for S = 5), with ragged sizes, an empty batch and means far
+    in both tails (where Z + eps and the 1e-8 guards dominate).  float64 arithmetic with
+    CUDA's erf/exp/log, in the reference's form (1 + erf(z))/2: for z << 0 that sum cancels, so
+    one ulp of erf near -1 (1.1e-16) is a relative change of 1.1e-16/p in the probability and
+    two erf implementations may differ by that much; the gradients are held to 1e-9, the
+    log-partition to 1e-12."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(n + S)
+    y = (2 * rng.randint(0, 2, size=(n, D)) - 1).astype(float)
+    shape = (S, n, D) if S > 1 else (n, D)
+    m = 2.0 * rng.randn(*shape)
+    if m.size:
+        m.flat[0], m.flat[-1] = 9.0, -9.0
+    v = 0.05 + rng.rand(*shape)
+    mc = S > 1
+    ref = (O.probit_logZ_mc if mc else O.probit_logZ)(m, v, y, alpha)
+    scale, invN = -3.5, 0.01
+    dm, dv = torch.empty(shape, dtype=torch.float64, device='cuda'), torch.empty(shape, dtype=torch.float64,
+                                                                                   device='cuda')
+    out = torch.full((1,), np.nan, dtype=torch.float64, device='cuda')
+    gpk.probit_lik(dev(m), dev(v), dev(y), alpha, scale, invN, dm, dv, out, mc=mc)
+    torch.cuda.synchronize()
+    e = float(out.item())
+    want = scale * invN * ref[0]
+    assert abs(e - want) <= 1e-12 * max(abs(want), 1e-300), (e, want)
+    if m.size:
+        assert_close(dm.cpu().numpy(), scale * ref[1], 1e-9, 'dm')
+        assert_close(dv.cpu().numpy(), scale * ref[2], 1e-9, 'dv')
+
+
+@pytest.mark.parametrize('kind', ['gaussian', 'probit'])
+@pytest.mark.parametrize('n,D', [(37, 3), (1000, 1), (0, 2)])
+def test_lik_exp_vs_oracle(kind, n, D):
+    """gpk_lik_exp (the VFE data term) against the oracle's Gauss_Layer / Probit_Layer
+    compute_log_lik_exp, with ragged sizes, an empty batch and means in both tails."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(n + 7)
+    if kind == 'gaussian':
+        y = rng.randn(n, D)
+    else:
+        y = (2 * rng.randint(0, 2, size=(n, D)) - 1).astype(float)
+    m = 2.0 * rng.randn(n, D)
+    if m.size:
+        m.flat[0], m.flat[-1] = 7.0, -7.0
+    v = 0.05 + rng.rand(n, D)
+    sn = np.array([0.5 * np.log(0.3)])
+    scale, invN = -2.5, 0.02
+    if kind == 'gaussian':
+        ll, rdm, rdv, dsn = O.gauss_lik_exp(m, v, y, sn)
+    else:
+        ll, rdm, rdv = O.probit_lik_exp(m, v, y)
+    dm = torch.empty((n, D), dtype=torch.float64, device='cuda')
+    dv = torch.empty_like(dm)
+    out = torch.full((1,), np.nan, dtype=torch.float64, device='cuda')
+    g_sn = torch.full((1,), np.nan, dtype=torch.float64, device='cuda')
+    gpk.lik_exp(kind, dev(m), dev(v), dev(y), scale, invN, dm, dv, out, sn=dev(sn), g_sn=g_sn)
+    torch.cuda.synchronize()
+    want = scale * invN * ll
+    assert abs(out.item() - want) <= 1e-12 * max(abs(want), 1e-300), (out.item(), want)
+    if kind == 'gaussian':
+        w = scale * invN * dsn
+        assert abs(g_sn.item() - w) <= 1e-12 * max(abs(w), 1e-300), (g_sn.item(), w)
+    if m.size:
+        assert_close(dm.cpu().numpy(), scale * rdm, 1e-11, 'dm')
+        assert_close(dv.cpu().numpy(), scale * rdv, 1e-11, 'dv')

@@ -168,3 +168,51 @@ def test_sdgpr_predict_monte_carlo():
     samples, mf, vf = O.sdgpr_predict_mc(p, g['xs'], int(g['no_samples']))
     for name, got in (('samples', samples), ('mf', mf), ('vf', vf)):
         assert_close(got, g[name], 1e-12, name)
+
+
+@pytest.mark.parametrize('tag,alpha', [('a1', 1.0), ('a05', 0.5)])
+def test_probit_models(tag, alpha):
+    """The oracle's probit likelihood (closed form at alpha = 1, Gauss-Hermite quadrature
+    otherwise) inside the SGPR, SDGPR and SGPLVM objectives against the reference's models
+    with lik='Probit' (tests/golden/make_probit.py); the SGPLVM also with Monte Carlo
+    propagation (the reference's own draws, stored in the fixture)."""
+    g = load('sgpr_probit.npz')
+    e, gr = O.sgpr_objective(g['x'], g['y'], sub(g, 'p_'), alpha, lik='probit')
+    assert abs(e - g['energy_' + tag]) <= 1e-12 * abs(g['energy_' + tag])
+    assert_dict_close(gr, sub(g, 'g%s_' % tag), 1e-10, 'sgpr probit')
+    if alpha != 1.0:
+        e, gr = O.sgpr_objective(g['x'], g['y'], sub(g, 'p_'), alpha, idx=g['mb_idx'], lik='probit')
+        assert abs(e - g['energy_mb']) <= 1e-12 * abs(g['energy_mb'])
+        assert_dict_close(gr, sub(g, 'gmb_'), 1e-10, 'sgpr probit mb')
+    g = load('sdgpr_probit.npz')
+    e, gr = O.sdgpr_objective(g['x'], g['y'], sub(g, 'p_'), alpha, lik='probit')
+    assert abs(e - g['energy_' + tag]) <= 1e-12 * abs(g['energy_' + tag])
+    assert_dict_close(gr, sub(g, 'g%s_' % tag), 1e-10, 'sdgpr probit')
+    g = load('sgplvm_probit.npz')
+    p = sub(g, 'p_')
+    e, gr = O.sgplvm_objective(g['y'], p, alpha, lik='probit')
+    assert abs(e - g['energy_' + tag]) <= 1e-12 * abs(g['energy_' + tag])
+    assert_dict_close(gr, sub(g, 'g%s_' % tag), 1e-10, 'sgplvm probit')
+    e, gr = O.sgplvm_objective(g['y'], p, alpha, eps=g['eps_mc_' + tag], lik='probit')
+    assert abs(e - g['energy_mc_' + tag]) <= 1e-12 * abs(g['energy_mc_' + tag])
+    assert_dict_close(gr, sub(g, 'gmc%s_' % tag), 1e-10, 'sgplvm probit mc')
+
+
+@pytest.mark.parametrize('tag,lik,ykey,nat', [('g1', 'gaussian', 'y', True), ('g0', 'gaussian', 'y', False),
+                                             ('p1', 'probit', 'yc', True)])
+def test_vfe_sgpr(tag, lik, ykey, nat):
+    """The oracle's VFE regression (expected log-likelihood through the posterior predictive plus
+    the KL term) against the reference's vfe_models.SGPR (tests/golden/make_vfe.py): Gaussian
+    with natural and moment parameters, probit; full batch and a minibatch."""
+    g = load('vfe_sgpr.npz')
+    p = sub(g, tag + '_p_')
+    e, gr = O.vfe_sgpr_objective(g['x'], g[ykey], p, nat_param=nat, lik=lik)
+    assert abs(e - g[tag + '_energy']) <= 1e-12 * abs(g[tag + '_energy'])
+    assert_dict_close(gr, sub(g, tag + '_g_'), 1e-10, 'vfe ' + tag)
+    e, gr = O.vfe_sgpr_objective(g['x'], g[ykey], p, idx=g[tag + '_mb_idx'], nat_param=nat, lik=lik)
+    assert abs(e - g[tag + '_energy_mb']) <= 1e-12 * abs(g[tag + '_energy_mb'])
+    assert_dict_close(gr, sub(g, tag + '_gmb_'), 1e-10, 'vfe mb ' + tag)
+    L = O.layer_unpack(p, '', p['zu'].shape[0], p['eta2'].shape[0], nat)
+    mf, vf, _ = O.fwd_det(L, g['xs'], cav=False)
+    assert_close(mf, g[tag + '_mf'], 1e-12, 'mf')
+    assert_close(vf, g[tag + '_vf'], 1e-12, 'vf')
