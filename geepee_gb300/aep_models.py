@@ -505,6 +505,153 @@ class SDGPR(_PackedModel):
 
 
 # ------------------------------------------------------------------------------------------
+# SDGPR_H (aep_models.py:1440-1863)
+# ------------------------------------------------------------------------------------------
+class SDGPR_H(_PackedModel):
+    """Deep GP regression whose hidden layers' outputs h_i are latent variables with Gaussian
+    factors (natural parameters h_factor_1_i, exp(2 h_factor_2_i) per point and dimension): each
+    hidden layer's moment-propagated output is matched to the h_i cavity by a Gaussian
+    transition with noise exp(2 sn_hidden[i]), the last layer's output by the likelihood.
+    Full batch only: the reference's hidden-factor gradients (aep_models.py:1618-1650) combine
+    minibatch and full-size arrays."""
+
+    def __init__(self, x_train, y_train, no_pseudos, hidden_sizes, lik='Gaussian'):
+        super().__init__(y_train)
+        self.N, self.Dout = y_train.shape
+        self.Din = x_train.shape[1]
+        self.size = [self.Din] + list(hidden_sizes) + [self.Dout]
+        self.L = len(self.size) - 1
+        self.Ms = list(no_pseudos) if isinstance(no_pseudos, (list, tuple)) else [no_pseudos] * self.L
+        self.x_train = x_train
+        spec = []
+        for i in range(self.L):
+            spec += DevLayer.spec(self.size[i], self.size[i + 1], self.Ms[i], '_%d' % i)
+        spec += self._lik_spec(lik) + [('sn_hidden', (self.L - 1,))]
+        for i in range(self.L - 1):
+            spec += [('h_factor_1_%d' % i, (self.N, self.size[i + 1])), ('h_factor_2_%d' % i, (self.N, self.size[i + 1]))]
+        self._make_packs(spec)
+        self.layers = [DevLayer(self.N, self.size[i], self.size[i + 1], self.Ms[i], True, self.dev,
+                                self.ppack.views, self.gpack.views, '_%d' % i) for i in range(self.L)]
+        self.sgp_layers = self.layers
+        self.x_dev = _to_dev(x_train, self.dev)
+        self.y_dev = _to_dev(y_train, self.dev)
+
+    def init_hypers(self, y_train=None):
+        """aep_models.py:1788-1820: layer initialisers, sn_hidden = log(0.001), h factors 0 and
+        log(0.01)."""
+        p = {}
+        for i in range(self.L):
+            p.update(layer_init_hypers(self.N, self.Ms[i], self.size[i], self.size[i + 1], True,
+                                       self.x_train if i == 0 else None, '_%d' % i))
+        p.update(self._lik_hypers())
+        p['sn_hidden'] = np.log(0.001) * np.ones(self.L - 1)
+        for i in range(self.L - 1):
+            p['h_factor_1_%d' % i] = np.zeros((self.N, self.size[i + 1]))
+            p['h_factor_2_%d' % i] = np.log(0.01) * np.ones((self.N, self.size[i + 1]))
+        return p
+
+    def device_objective(self, idx, alpha):
+        """aep_models.py:1506-1616 on device tensors (full batch)."""
+        N, L = self.N, self.L
+        xb, yb = self.x_dev, self.y_dev
+        scale = -1.0 / alpha
+        pv, gv = self.ppack.views, self.gpack.views
+        st = setup_layers(self.layers, alpha)
+        h1 = [pv['h_factor_1_%d' % i] for i in range(L - 1)]
+        h2 = [torch.exp(2.0 * pv['h_factor_2_%d' % i]) for i in range(L - 1)]
+        c1 = [h * (2.0 - alpha) for h in h1]
+        c2 = [h * (2.0 - alpha) for h in h2]
+        cm = [(a / b).contiguous() for a, b in zip(c1, c2)]
+        cv = [(1.0 / b).contiguous() for b in c2]
+        sn2 = torch.exp(2.0 * pv['sn_hidden'])
+        g_snh = gv['sn_hidden']
+        dmc, dvc = [], []
+        logZ = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        for i in range(L - 1):
+            lay = self.layers[i]
+            if i == 0:
+                mp, vp, kfu, Bk = lay.fwd_det(xb)
+            else:
+                mp, vp = lay.fwd_mm(cm[i - 1], cv[i - 1])
+            # compute_transition_tilted (aep_models.py:1688-1728)
+            vs = cv[i] + vp + sn2[i] / alpha
+            md = cm[i] - mp
+            lz = -0.5 * md * md / vs - 0.5 * torch.log(2 * np.pi * vs)
+            lz_c = 0.5 * (1 - alpha) * torch.log(2 * np.pi * sn2[i]) - 0.5 * np.log(alpha)
+            logZ = logZ + scale * (lz.sum() + lz_c * md.numel())
+            dvt = -0.5 / vs + 0.5 * md * md / (vs * vs)
+            g_snh[i:i + 1].copy_(scale * (dvt.sum() * 2 * sn2[i] / alpha + md.numel() * (1 - alpha)))
+            dmp, dvp = (scale * md / vs).contiguous(), (scale * dvt).contiguous()
+            if i == 0:
+                lay.bwd_det(alpha, dmp, dvp, kfu, Bk, xb)
+            else:
+                dmx, dvx = lay.bwd_mm(alpha, mp, dmp, dvp, cm[i - 1], cv[i - 1])
+                dmc[i - 1] = dmc[i - 1] + dmx
+                dvc[i - 1] = dvc[i - 1] + dvx
+            dmc.append(-scale * md / vs)
+            dvc.append(scale * dvt)
+        lay = self.layers[-1]
+        mp, vp = lay.fwd_mm(cm[-1], cv[-1])
+        dm, dv, ll_s = torch.empty_like(mp), torch.empty_like(vp), torch.empty_like(self.energy)
+        self._log_Z(mp, vp, yb, alpha, scale, 1.0, dm, dv, ll_s)
+        dmx, dvx = lay.bwd_mm(alpha, mp, dm, dv, cm[-1], cv[-1])
+        dmc[-1] = dmc[-1] + dmx
+        dvc[-1] = dvc[-1] + dvx
+        # compute_grads_hidden and the h log-partitions (aep_models.py:1618-1686)
+        s_post, s_cav = -(1.0 - 1.0 / alpha), -1.0 / alpha
+        phi_h = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        for i in range(L - 1):
+            q1, q2 = 2.0 * h1[i], 2.0 * h2[i]
+            d1 = ((2 - alpha) * (dmc[i] / c2[i]) + s_cav * (2 - alpha) * (c1[i] / c2[i])
+                  + s_post * 2 * (q1 / q2))
+            d2 = ((2 - alpha) * (-dmc[i] * c1[i] / c2[i] ** 2 - dvc[i] / c2[i] ** 2)
+                  + s_cav * (2 - alpha) * (-0.5 * c1[i] ** 2 / c2[i] ** 2 - 0.5 / c2[i])
+                  + s_post * (-q1 ** 2 / q2 ** 2 - 1 / q2))
+            gv['h_factor_1_%d' % i].copy_(d1)
+            gv['h_factor_2_%d' % i].copy_(2 * d2 * h2[i])
+            phi_h = phi_h + s_post * (0.5 * (q1 * q1 / q2 - torch.log(q2))).sum()
+            phi_h = phi_h + s_cav * (0.5 * (c1[i] ** 2 / c2[i] - torch.log(c2[i]))).sum()
+        self.energy.copy_(ll_s + logZ + phi_h)
+        for lay in self.layers:
+            lay.phi(alpha, out=self.energy, w=1.0)
+        keys = [k for k, _ in self.gpack.spec]
+        span = int(self.gpack.offsets[keys.index('__energy__')])
+        # every gradient and the energy divided by N; the worst Cholesky status recorded
+        gpk.finish(self.gpack.dev[:span + 1], N, st[0].reshape(-1) if len(st) == 1 else None,
+                   gv['__info__'] if len(st) == 1 else None)
+        if len(st) != 1:
+            self._flag_info(st)
+        return self.energy
+
+    def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
+        """aep_models.py:1506-1616 (full batch; a smaller mb_size raises, see the class note)."""
+        if mb_size < self.N:
+            raise NotImplementedError('SDGPR_H supports full-batch evaluation only')
+        self.update_hypers(params)
+        return self._objective_host(None, alpha)
+
+    def _prepare_predict(self):
+        if not self.updated:
+            for lay in self.layers:
+                lay.setup_posterior()
+                lay.setup_predict()
+            self.updated = True
+
+    def predict_f(self, inputs):
+        """aep_models.py:1730-1746: moment matching through every layer's posterior."""
+        self._prepare_predict()
+        m, v, _, _ = self.layers[0].fwd_det(_to_dev(inputs, self.dev), cav=False)
+        for lay in self.layers[1:]:
+            m, v = lay.fwd_mm(m, v, cav=False)
+        return m.cpu().numpy(), v.cpu().numpy()
+
+    def predict_y(self, inputs):
+        """aep_models.py:1769-1786."""
+        mf, vf = self.predict_f(inputs)
+        return self._output_probabilistic(mf, vf)
+
+
+# ------------------------------------------------------------------------------------------
 # SGPLVM (aep_models.py:670-867, base_models.py:661-929)
 # ------------------------------------------------------------------------------------------
 def _phi_x(mx, vx):

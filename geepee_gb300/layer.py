@@ -448,6 +448,33 @@ class DevLayer:
         self.g['eta1_R'].copy_(e1)
         self.g['eta2'].copy_(e2)
 
+    def bwd_mm_vfe(self, m, dm, dv, mx, vx):
+        """VFE SGP_Layer.backprop_grads_lvm_mm (vfe_models.py:328-402): Gaussian inputs through
+        the posterior (A, B_sto) with psi2 recomputed, upstream dm, dv already scaled, plus the
+        KL term's gradients.  Returns (dmx, dvx)."""
+        D, M = self.Dout, self.M
+        K = self.Kinv
+        self.zero_accumulators()
+        dA, dB = self._dAh, self._dBh
+        dmx = torch.empty_like(mx)
+        dvx = torch.empty_like(vx)
+        gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.A, self.B_sto, m, dm, dv, self._dsf2, self._dl,
+                    self.g['zu'], dA, dB, dmx, dvx)
+        self._kernel_grads(self._dsf2, self._dl, dv)
+        # dSu = K^-1 dB K^-1 (+ the KL's (K^-1 - Su^-1)/2);  dmu = 2 dSu mu + K^-1 dA + K^-1 mu
+        KdBK = mm(mm(K, dB), K)
+        dmu = mm(dA, K, beta=1.0, E=mm(self.mu, K))
+        dmu = mm(KdBK, self.mu.unsqueeze(-1), alpha=2.0, beta=1.0, E=dmu.unsqueeze(-1)).squeeze(-1)
+        dSu = gpk.lincomb(torch.empty_like(self.Suinv), [(1.0, KdBK), (0.5, K), (-0.5, self.Suinv)])
+        e1, e2, dKu = self._post_grad_u(dmu, dSu)
+        KSpmm = mm(K, self.Spmm)
+        dK = (mm(dA, self.mu, tA=True) + 2.0 * mm(KSpmm.reshape(D * M, M), dB.reshape(D * M, M), tA=True)
+              - dB.sum(0) + dKu - 0.5 * D * self.Kuu + 0.5 * self.Spmm.sum(0))
+        self._finish_hyp(mm(mm(K, dK), K, alpha=-1.0))
+        self.g['eta1_R'].copy_(e1)
+        self.g['eta2'].copy_(e2)
+        return dmx, dvx
+
     def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x, dx=None):
         """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
         compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so

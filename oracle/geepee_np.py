@@ -396,6 +396,31 @@ def vfe_bwd_det(L, dm, dv, kfu, x):
     return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1, 'eta2': e2}
 
 
+def vfe_bwd_mm(L, m, dm, dv, psi1, psi2, mx, vx):
+    """VFE ``SGP_Layer.backprop_grads_lvm_mm`` vfe_models.py:328-402: Gaussian inputs through the
+    posterior (A, B_sto), upstream dm, dv already scaled, plus the KL term's gradients; returns
+    the layer gradients and those w.r.t. the input moments."""
+    ell = np.exp(L['ls'])
+    sf2 = np.exp(2 * L['sf'])
+    K = L['Kinv']
+    dm_all = dm - 2 * dv * m
+    dpsi1 = dm_all @ L['A']
+    dpsi2 = np.einsum('nd,dab->nab', dv, L['B_sto'])
+    dsf2, dl, dz, dmx, dvx = psi_derivatives(dpsi1, psi1, dpsi2, psi2, ell, sf2, mx, vx, L['Z'])
+    dls = dl * ell
+    dsf = 2 * sf2 * (dsf2 + dv.sum())
+    dA = dm_all.T @ psi1
+    dB = np.einsum('nd,nab->dab', dv, psi2)
+    dSu = K[None] @ dB @ K[None]
+    dmu = 2 * np.einsum('dab,db->da', dSu, L['mu']) + dA @ K + L['mu'] @ K
+    dSu = dSu + 0.5 * (K[None] - L['Suinv'])
+    e1, e2, dKu = _post_grad_u(L, dmu, dSu)
+    dK = (dA.T @ L['mu'] + 2 * np.einsum('dab,dac->bc', K[None] @ L['Spmm'], dB) - dB.sum(0) + dKu
+          - 0.5 * L['Dout'] * L['Kuu'] + 0.5 * L['Spmm'].sum(0))
+    dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, -K @ dK @ K)
+    return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1, 'eta2': e2}, {'mx': dmx, 'vx': dvx}
+
+
 # --------------------------------------------------------------------------
 # likelihood / emission (lik_layers.py)
 # --------------------------------------------------------------------------
@@ -532,6 +557,48 @@ def vfe_sgpr_objective(x, y, p, idx=None, nat_param=True, fixed=(), lik='gaussia
     return _finish(scale * ll + vfe_kl(L), g, N, fixed)
 
 
+def vfe_sgplvm_objective(y, p, idx=None, prior_mean=0.0, prior_var=1.0, nat_param=True, fixed=(), lik='gaussian'):
+    """VFE ``SGPLVM.objective_function`` vfe_models.py:749-845 (moment matching): the latent
+    posterior's moments through the GP posterior, -N/n E_q[log p(y_b | f)] + N/n KL(q(x_b) || p(x))
+    + KL(q(u) || p(u)), divided by N; x gradients by ``compute_posterior_grad_x``
+    (base_models.py:913-929)."""
+    N, Dy = y.shape
+    Mz, Dout = _layer_dims(p, '')
+    if idx is None:
+        idx = np.arange(N)
+    yb = y[idx]
+    nb = yb.shape[0]
+    scale = -N / nb
+    L = layer_unpack(p, '', Mz, Dout, nat_param)
+    f1 = np.asarray(p['x1'], dtype=float)
+    f2 = np.exp(2 * np.asarray(p['x2'], dtype=float))
+    px1, px2 = prior_mean / prior_var, 1.0 / prior_var
+    post1, post2 = (px1 + f1, px2 + f2) if nat_param else (f1 / f2, 1.0 / f2)
+    mx, vx = post1[idx] / post2[idx], 1.0 / post2[idx]
+    m, v, p1, p2 = fwd_mm(L, mx, vx, cav=False)
+    if lik == 'gaussian':
+        ll, dm, dv, dsn = gauss_lik_exp(m, v, yb, p['sn'])
+    else:
+        ll, dm, dv = probit_lik_exp(m, v, yb)
+    grads, gi = vfe_bwd_mm(L, m, scale * dm, scale * dv, p1, p2, mx, vx)
+    if lik == 'gaussian':
+        grads['sn'] = scale * dsn
+    kl_x = 0.5 * (np.log(prior_var) - np.log(vx) + (vx + (mx - prior_mean) ** 2) / prior_var - 1)
+    scale_x = N / nb
+    dmx = gi['mx'] + scale_x * (mx - prior_mean) / prior_var
+    dvx = gi['vx'] + scale_x * (-0.5 / vx + 0.5 / prior_var)
+    g1 = np.zeros_like(f1)
+    g2 = np.zeros_like(f1)
+    if nat_param:
+        g1[idx] = dmx / post2[idx]
+        g2[idx] = (-dmx * post1[idx] / post2[idx] ** 2 - dvx / post2[idx] ** 2) * 2 * f2[idx]
+    else:
+        g1[idx] = dmx
+        g2[idx] = dvx * 2 * f2[idx]
+    grads['x1'], grads['x2'] = g1, g2
+    return _finish(scale * ll + scale_x * np.sum(kl_x) + vfe_kl(L), grads, N, fixed)
+
+
 def gauss_dsn(dv, nb, D, sn, alpha, scale):
     """``Gauss_Layer.backprop_grads`` lik_layers.py:154-181 (2-D case)."""
     sn2 = np.exp(2.0 * _scalar(sn))
@@ -635,6 +702,85 @@ def sdgpr_objective(x, y, p, alpha, idx=None, fixed=(), lik='gaussian'):
     if lik == 'gaussian':
         grads['sn'] = gauss_dsn(dv, yb.shape[0], yb.shape[1], p['sn'], alpha, scale)
     energy = scale * logZ + sum(layer_phi(L, N, alpha) for L in layers)
+    return _finish(energy, grads, N, fixed)
+
+
+def sdgprh_objective(x, y, p, alpha, lik='gaussian', fixed=()):
+    """``SDGPR_H.objective_function`` aep_models.py:1506-1616 (full batch): a deep GP whose
+    hidden layers' outputs are latent variables h_i with Gaussian factors (natural parameters
+    h_factor_1_i, exp(2 h_factor_2_i)); each hidden layer's moment-propagated output is matched
+    to its h_i cavity by a Gaussian transition with noise exp(2 sn_hidden[i])
+    (``compute_transition_tilted`` :1688-1728), the last layer's by the likelihood; the h
+    gradients by ``compute_grads_hidden`` (:1618-1650), the h log-partitions by
+    ``compute_phi_posterior_h`` / ``compute_phi_cavity_h`` (:1652-1686)."""
+    N = y.shape[0]
+    nl = 0
+    while ('eta2_%d' % nl) in p:
+        nl += 1
+    scale = -1.0 / alpha
+    layers = []
+    for i in range(nl):
+        Mz, Dout = _layer_dims(p, '_%d' % i)
+        layers.append(layer_cavity(layer_unpack(p, '_%d' % i, Mz, Dout), N, alpha))
+    snh = np.asarray(p['sn_hidden'], dtype=float)
+    hf1 = [np.asarray(p['h_factor_1_%d' % i], dtype=float) for i in range(nl - 1)]
+    hf2 = [np.exp(2 * np.asarray(p['h_factor_2_%d' % i], dtype=float)) for i in range(nl - 1)]
+    c1 = [h * (2.0 - alpha) for h in hf1]
+    c2 = [h * (2.0 - alpha) for h in hf2]
+    cm = [a / b for a, b in zip(c1, c2)]
+    cv = [1.0 / b for b in c2]
+    grads, dmc, dvc, dsn = {}, [], [], np.zeros(nl - 1)
+    logZ = 0.0
+    for i in range(nl - 1):
+        L = layers[i]
+        if i == 0:
+            mp, vp, kfu = fwd_det(L, x)
+        else:
+            mp, vp, p1, p2 = fwd_mm(L, cm[i - 1], cv[i - 1])
+        sn2 = np.exp(2 * snh[i])
+        vs = cv[i] + vp + sn2 / alpha
+        md = cm[i] - mp
+        lz = -0.5 * md ** 2 / vs - 0.5 * np.log(2 * np.pi * vs) \
+            + 0.5 * (1 - alpha) * np.log(2 * np.pi * sn2) - 0.5 * np.log(alpha)
+        dvt = -0.5 / vs + 0.5 * md ** 2 / vs ** 2
+        logZ += scale * np.sum(lz)
+        dsn[i] = scale * (np.sum(dvt) * 2 * sn2 / alpha + mp.shape[0] * mp.shape[1] * (1 - alpha))
+        if i == 0:
+            gh = bwd_det(L, N, alpha, scale * md / vs, scale * dvt, kfu, x)
+        else:
+            gh, gi = bwd_mm(L, N, alpha, mp, scale * md / vs, scale * dvt, p1, p2, cm[i - 1], cv[i - 1])
+            dmc[i - 1] = dmc[i - 1] + gi['mx']
+            dvc[i - 1] = dvc[i - 1] + gi['vx']
+        for k, val in gh.items():
+            grads['%s_%d' % (k, i)] = val
+        dmc.append(-scale * md / vs)
+        dvc.append(scale * dvt)
+    L = layers[-1]
+    mp, vp, p1, p2 = fwd_mm(L, cm[-1], cv[-1])
+    lz, dm, dv = lik_logZ(lik, mp, vp, y, p, alpha)
+    gh, gi = bwd_mm(L, N, alpha, mp, scale * dm, scale * dv, p1, p2, cm[-1], cv[-1])
+    logZ += scale * lz
+    dmc[-1] = dmc[-1] + gi['mx']
+    dvc[-1] = dvc[-1] + gi['vx']
+    for k, val in gh.items():
+        grads['%s_%d' % (k, nl - 1)] = val
+    if lik == 'gaussian':
+        grads['sn'] = gauss_dsn(dv, y.shape[0], y.shape[1], p['sn'], alpha, scale)
+    phi_h = 0.0
+    for i in range(nl - 1):
+        q1, q2 = 2 * hf1[i], 2 * hf2[i]
+        s_post, s_cav = -(1.0 - 1.0 / alpha), -1.0 / alpha
+        d1 = ((2 - alpha) * (dmc[i] / c2[i]) + s_cav * (2 - alpha) * (c1[i] / c2[i])
+              + s_post * 2 * (q1 / q2))
+        d2 = ((2 - alpha) * (-dmc[i] * c1[i] / c2[i] ** 2 - dvc[i] / c2[i] ** 2)
+              + s_cav * (2 - alpha) * (-0.5 * c1[i] ** 2 / c2[i] ** 2 - 0.5 / c2[i])
+              + s_post * (-q1 ** 2 / q2 ** 2 - 1 / q2))
+        grads['h_factor_1_%d' % i] = d1
+        grads['h_factor_2_%d' % i] = 2 * d2 * hf2[i]
+        phi_h += s_post * np.sum(0.5 * (q1 ** 2 / q2 - np.log(q2)))
+        phi_h += s_cav * np.sum(0.5 * (c1[i] ** 2 / c2[i] - np.log(c2[i])))
+    grads['sn_hidden'] = dsn
+    energy = logZ + sum(layer_phi(L, N, alpha) for L in layers) + phi_h
     return _finish(energy, grads, N, fixed)
 
 

@@ -1,7 +1,8 @@
 """Golden fixtures for the VFE sparse GP regression (vfe_models.py:292-719): the reference's own
 ``vfe_models.SGPR`` through the ``oracle/_ref`` shim on small seeded inputs, with the Gaussian
 likelihood (natural and moment parameters) and the probit likelihood, full batch and a
-minibatch, plus its predictions.  Writes ``vfe_sgpr.npz``.
+minibatch, plus its predictions; and ``vfe_models.SGPLVM`` (moment matching) likewise.  Writes
+``vfe_sgpr.npz`` and ``vfe_sgplvm.npz``.
 Usage:  python tests/golden/make_vfe.py [--src DIR]"""
 from __future__ import annotations
 
@@ -56,6 +57,29 @@ def main(argv=None):
             out.update({tag + '_my': my, tag + '_vy': vy})
     np.savez_compressed(os.path.join(HERE, 'vfe_sgpr.npz'), **out)
     print('wrote', os.path.join(HERE, 'vfe_sgpr.npz'))
+
+    # SGPLVM (moment matching): 14 points, 3 outputs, 2 latent dimensions, 6 pseudo-points; the
+    # latent factors from the model's init_hypers, the GP part from the layer's own initialiser
+    # (base_models.py:518-597) so that q(u) is well conditioned in every case
+    rng = np.random.RandomState(54)
+    y = rng.randn(14, 3)
+    yc = (2 * rng.randint(0, 2, size=(14, 3)) - 1).astype(float)
+    out = dict(y=y, yc=yc)
+    for tag, lik, yy, nat in (('g1', 'Gaussian', y, True), ('g0', 'Gaussian', y, False),
+                              ('p1', 'Probit', yc, True)):
+        np.random.seed(55)
+        mdl = vfe.SGPLVM(yy, 2, 6, lik=lik, nat_param=nat)
+        params = mdl.init_hypers(yy)
+        params.update(mdl.sgp_layer.init_hypers())
+        e, g = mdl.objective_function(cp(params), 14)
+        out.update({tag + '_energy': e}, **_pre(params, tag + '_p_'), **_pre(g, tag + '_g_'))
+        np.random.seed(56)
+        idx = np.random.choice(14, 6, replace=False)
+        np.random.seed(56)
+        e, g = mdl.objective_function(cp(params), 6)
+        out.update({tag + '_energy_mb': e, tag + '_mb_idx': idx}, **_pre(g, tag + '_gmb_'))
+    np.savez_compressed(os.path.join(HERE, 'vfe_sgplvm.npz'), **out)
+    print('wrote', os.path.join(HERE, 'vfe_sgplvm.npz'))
 
 
 if __name__ == '__main__':

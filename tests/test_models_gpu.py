@@ -366,3 +366,51 @@ def test_sgplvm_init_hypers_matches_reference(nat):
             assert_close(p[k], ref[k], 1e-6, k)
         e_aep = O.sgplvm_objective(g['y'], p, 0.5, nat_param=False)[0]
         assert abs(e_aep - g['energy']) <= 1e-6 * abs(g['energy']), (e_aep, g['energy'])
+
+
+@pytest.mark.parametrize('tag,lik,ykey,nat', [('g1', 'Gaussian', 'y', True), ('g0', 'Gaussian', 'y', False),
+                                             ('p1', 'Probit', 'yc', True)])
+def test_vfe_sgplvm(tag, lik, ykey, nat):
+    """vfe_models.SGPLVM (moment matching) against the reference's (tests/golden/make_vfe.py):
+    energy rel <= 1e-6, gradients per key within max(1e-6, G_FACTOR x the oracle's one-ulp
+    sensitivity), full batch and a minibatch drawn as the reference draws it."""
+    from tests._helpers import noise_floor, assert_grads_close
+    from geepee_gb300 import vfe_models as V
+    g = load('vfe_sgplvm.npz')
+    p = sub(g, tag + '_p_')
+    y = g[ykey]
+    cp = lambda q: {k: np.copy(v) for k, v in q.items()}
+    mdl = V.SGPLVM(y, 2, 6, lik=lik, nat_param=nat)
+    e, gr = mdl.objective_function(cp(p), 14)
+    _energy_ok(e, g[tag + '_energy'])
+    ol = lik.lower()
+    fl = noise_floor(lambda q: O.vfe_sgplvm_objective(y, q, nat_param=nat, lik=ol), p)
+    assert_grads_close(gr, sub(g, tag + '_g_'), fl, G_TOL, G_FACTOR, 'vfe lvm ' + tag)
+    np.random.seed(56)
+    e, gr = mdl.objective_function(cp(p), 6)
+    _energy_ok(e, g[tag + '_energy_mb'])
+    fl = noise_floor(lambda q: O.vfe_sgplvm_objective(y, q, idx=g[tag + '_mb_idx'], nat_param=nat, lik=ol), p)
+    assert_grads_close(gr, sub(g, tag + '_gmb_'), fl, G_TOL, G_FACTOR, 'vfe lvm mb ' + tag)
+
+
+@pytest.mark.parametrize('tag,lik,ykey', [('g', 'Gaussian', 'y'), ('p', 'Probit', 'yc')])
+@pytest.mark.parametrize('at,alpha', [('a1', 1.0), ('a05', 0.5)])
+def test_sdgprh(tag, lik, ykey, at, alpha):
+    """SDGPR_H (hidden-variable deep GP, full batch) against the reference's
+    (tests/golden/make_dgph.py): energy rel <= 1e-6, gradients per key within max(1e-6,
+    G_FACTOR x the oracle's one-ulp sensitivity), predictions rel <= 1e-6."""
+    from tests._helpers import noise_floor, assert_grads_close
+    from geepee_gb300 import aep_models as A
+    g = load('sdgprh_small.npz')
+    p = sub(g, tag + '_p_')
+    x, y = g['x'], g[ykey]
+    mdl = A.SDGPR_H(x, y, 5, [3, 2], lik=lik)
+    assert set(mdl.init_hypers(y)) == set(p)
+    e, gr = mdl.objective_function({k: np.copy(v) for k, v in p.items()}, 12, alpha=alpha)
+    _energy_ok(e, g['%s_energy_%s' % (tag, at)])
+    fl = noise_floor(lambda q: O.sdgprh_objective(x, y, q, alpha, lik=lik.lower()), p)
+    assert_grads_close(gr, sub(g, '%s_g%s_' % (tag, at)), fl, G_TOL, G_FACTOR, 'sdgprh ' + tag)
+    mdl.update_hypers(p)
+    mf, vf = mdl.predict_f(x[:5])
+    assert_close(mf, g[tag + '_mf'], P_TOL, 'mf')
+    assert_close(vf, g[tag + '_vf'], P_TOL, 'vf')

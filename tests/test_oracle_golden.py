@@ -216,3 +216,31 @@ def test_vfe_sgpr(tag, lik, ykey, nat):
     mf, vf, _ = O.fwd_det(L, g['xs'], cav=False)
     assert_close(mf, g[tag + '_mf'], 1e-12, 'mf')
     assert_close(vf, g[tag + '_vf'], 1e-12, 'vf')
+
+
+@pytest.mark.parametrize('tag,lik,ykey,nat', [('g1', 'gaussian', 'y', True), ('g0', 'gaussian', 'y', False),
+                                             ('p1', 'probit', 'yc', True)])
+def test_vfe_sgplvm(tag, lik, ykey, nat):
+    """The oracle's VFE latent-variable model (moment matching) against the reference's
+    vfe_models.SGPLVM (tests/golden/make_vfe.py): full batch and a minibatch.  The psi-statistic
+    gradients are formed in another order than the reference's, hence 1e-9."""
+    g = load('vfe_sgplvm.npz')
+    p = sub(g, tag + '_p_')
+    e, gr = O.vfe_sgplvm_objective(g[ykey], p, nat_param=nat, lik=lik)
+    assert abs(e - g[tag + '_energy']) <= 1e-12 * abs(g[tag + '_energy'])
+    assert_dict_close(gr, sub(g, tag + '_g_'), 1e-9, 'vfe lvm ' + tag)
+    e, gr = O.vfe_sgplvm_objective(g[ykey], p, idx=g[tag + '_mb_idx'], nat_param=nat, lik=lik)
+    assert abs(e - g[tag + '_energy_mb']) <= 1e-12 * abs(g[tag + '_energy_mb'])
+    assert_dict_close(gr, sub(g, tag + '_gmb_'), 1e-9, 'vfe lvm mb ' + tag)
+
+
+@pytest.mark.parametrize('tag,lik,ykey', [('g', 'gaussian', 'y'), ('p', 'probit', 'yc')])
+@pytest.mark.parametrize('at,alpha', [('a1', 1.0), ('a05', 0.5)])
+def test_sdgprh(tag, lik, ykey, at, alpha):
+    """The oracle's deep GP with hidden-variable factors against the reference's SDGPR_H
+    (tests/golden/make_dgph.py; the reference module's missing likelihood import supplied)."""
+    g = load('sdgprh_small.npz')
+    e, gr = O.sdgprh_objective(g['x'], g[ykey], sub(g, tag + '_p_'), alpha, lik=lik)
+    ref = g['%s_energy_%s' % (tag, at)]
+    assert abs(e - ref) <= 1e-12 * abs(ref)
+    assert_dict_close(gr, sub(g, '%s_g%s_' % (tag, at)), 1e-10, 'sdgprh')
