@@ -1,10 +1,11 @@
 """AEP (black-box alpha) sparse-GP models with geepee's Python API, on the GPU.
 
 Drop-in counterparts of geepee/aep_models.py: ``SGPR`` (:589-667), ``SGPLVM``
-(:670-867), ``SDGPR`` (:870-988) and ``SGPSSM`` (:991-1437), with the
-``Base_Model`` / ``Base_*`` behaviour they inherit from geepee/base_models.py
-(parameter dicts, ``init_hypers``/``get_hypers``/``update_hypers``, ``optimise``,
-``set_fixed_params``, ``save_model``/``load_model``, ``predict_f``/``predict_y``).
+(:670-867), ``SDGPR`` (:870-988), ``SGPSSM`` (:991-1437) and ``SDGPR_H`` (:1440-1863),
+Gaussian or probit likelihood, with the ``Base_Model`` / ``Base_*`` behaviour they inherit
+from geepee/base_models.py (parameter dicts, ``init_hypers``/``get_hypers``/``update_hypers``,
+``optimise``, ``set_fixed_params``, ``save_model``/``load_model``, ``predict_f``/``predict_y``,
+``sample_f``, the deep GP's ``predict_f_with_input_grad``).
 
 ``objective_function(params, mb_size, alpha, prop_mode)`` takes and returns numpy
 float64 exactly like the reference (minibatches drawn from numpy's global RNG in the
@@ -296,6 +297,22 @@ class _PackedModel(Base_Model):
         return energy, out
 
 
+def _sample_layers(layers, inputs, no_samples, dev):
+    """sample_f (base_models.py:1000-1018, 1239-1262): no_samples joint draws through the layers'
+    posteriors; each layer's two standard-normal draws (randn(Dout, M), then randn(n, Dout))
+    come from numpy's global RNG in the reference's order.  Returns [n, Dout, no_samples]."""
+    x0 = _to_dev(inputs, dev)
+    fs = np.zeros((x0.shape[0], layers[-1].Dout, no_samples))
+    for k in range(no_samples):
+        x = x0
+        for lay in layers:
+            eps_u = np.random.randn(lay.Dout, lay.M)
+            eps_f = np.random.randn(x.shape[0], lay.Dout)
+            x = lay.sample(x, _to_dev(eps_u, dev), _to_dev(eps_f, dev))
+        fs[:, :, k] = x.cpu().numpy()
+    return fs
+
+
 # ------------------------------------------------------------------------------------------
 # SGPR (aep_models.py:589-667)
 # ------------------------------------------------------------------------------------------
@@ -360,6 +377,11 @@ class SGPR(_PackedModel):
         """base_models.py:1020-1034 (Gauss_Layer.output_probabilistic adds exp(2 sn))."""
         mf, vf = self.predict_f(inputs)
         return self._output_probabilistic(mf, vf)
+
+    def sample_f(self, inputs, no_samples=1):
+        """base_models.py:1000-1018."""
+        self._prepare_predict()
+        return _sample_layers([self.layer], inputs, no_samples, self.dev)
 
 
 # ------------------------------------------------------------------------------------------
@@ -502,6 +524,42 @@ class SDGPR(_PackedModel):
         """base_models.py:1264-1275."""
         mf, vf = self.predict_f(inputs)
         return self._output_probabilistic(mf, vf)
+
+    def sample_f(self, inputs, no_samples=1):
+        """base_models.py:1239-1262."""
+        self._prepare_predict()
+        return _sample_layers(self.layers, inputs, no_samples, self.dev)
+
+    def predict_f_with_input_grad(self, inputs):
+        """base_models.py:1186-1237: the last layer's posterior moments and the gradients of
+        their sums over the outputs w.r.t. the inputs, back through every layer
+        (backprop_predictive_grads_lvm_mm / _reg, base_models.py:335-426).  The first layer's
+        dv_dx is formed, as the reference forms it (base_models.py:419-422), from the mean's
+        kfu gradient, so it equals dm_dx."""
+        self._prepare_predict()
+        x = _to_dev(inputs, self.dev)
+        m, v, kfu, Bk = self.layers[0].fwd_det(x, cav=False)
+        ms, vs = [m], [v]
+        for lay in self.layers[1:]:
+            m, v = lay.fwd_mm(ms[-1], vs[-1], cav=False)
+            ms.append(m)
+            vs.append(v)
+        dmdm, dvdv = torch.ones_like(ms[-1]), torch.ones_like(ms[-1])
+        dmdv, dvdm = torch.zeros_like(ms[-1]), torch.zeros_like(ms[-1])
+        for i in range(self.L - 1, 0, -1):
+            lay = self.layers[i]
+            a, b = lay.input_grad_mm(ms[i], dmdm, dmdv, ms[i - 1], vs[i - 1])
+            c, d = lay.input_grad_mm(ms[i], dvdm, dvdv, ms[i - 1], vs[i - 1])
+            dmdm, dmdv, dvdm, dvdv = a, b, c, d
+        dm_dx = self.layers[0].input_grad_det(x, kfu, Bk, dmdm, dmdv)
+        dm_dx = dm_dx.cpu().numpy()
+        return ms[-1].cpu().numpy(), vs[-1].cpu().numpy(), dm_dx, dm_dx.copy()
+
+    def predict_y_with_input_grad(self, inputs):
+        """base_models.py:1277-1288."""
+        mf, vf, dm_dx, dv_dx = self.predict_f_with_input_grad(inputs)
+        my, vy = self._output_probabilistic(mf, vf)
+        return my, vy, dm_dx, dv_dx
 
 
 # ------------------------------------------------------------------------------------------
@@ -649,6 +707,11 @@ class SDGPR_H(_PackedModel):
         """aep_models.py:1769-1786."""
         mf, vf = self.predict_f(inputs)
         return self._output_probabilistic(mf, vf)
+
+    def sample_f(self, inputs, no_samples=1):
+        """aep_models.py:1748-1767."""
+        self._prepare_predict()
+        return _sample_layers(self.layers, inputs, no_samples, self.dev)
 
 
 # ------------------------------------------------------------------------------------------

@@ -11,6 +11,7 @@ objective+gradient evaluation can be captured in one CUDA graph.
 from __future__ import annotations
 
 import math
+import numpy as np
 
 import torch
 
@@ -414,6 +415,56 @@ class DevLayer:
         self._finish_hyp(Minner)
         self.g['eta1_R'].copy_(e1c + e1p)
         self.g['eta2'].copy_(e2c + e2p)
+
+    # ---------------------------------------------------------------- predictive extras
+    def _scratch_acc(self):
+        """Zeroed accumulators (dsf2, dl, dZ, dA, dB) for backward calls whose hyperparameter
+        sums are not wanted."""
+        Q, D, M = self.Din, self.Dout, self.M
+        s = torch.zeros(1 + Q + M * Q + D * M + D * M * M, dtype=F64, device=self.dev)
+        o = [0, 1, 1 + Q, 1 + Q + M * Q, 1 + Q + M * Q + D * M, s.numel()]
+        return (s[o[0]:o[1]], s[o[1]:o[2]], s[o[2]:o[3]].view(M, Q), s[o[3]:o[4]].view(D, M),
+                s[o[4]:o[5]].view(D, M, M))
+
+    def input_grad_det(self, x, kfu, Bk, dm, dv):
+        """Gradient of sum(dm * m + dv * v) w.r.t. deterministic inputs x through the posterior
+        (the kfu chain of backprop_predictive_grads_reg, base_models.py:391-426); kfu, Bk from
+        fwd_det(x, cav=False)."""
+        dx = torch.empty_like(x)
+        dsf2, dl, dZ, dA, _ = self._scratch_acc()
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.A, kfu, Bk, dm.contiguous(), dv.contiguous(), dsf2, dl,
+                    dZ, dA, dx=dx)
+        return dx
+
+    def input_grad_mm(self, m, dm, dv, mx, vx):
+        """Gradient of sum(dm * m + dv * v) w.r.t. the Gaussian inputs' moments (mx, vx) through
+        the posterior (backprop_predictive_grads_lvm_mm, base_models.py:335-372), psi2
+        recomputed; m is this layer's output mean."""
+        dmx, dvx = torch.empty_like(mx), torch.empty_like(vx)
+        dsf2, dl, dZ, dA, dB = self._scratch_acc()
+        gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.A, self.B_sto, m, dm.contiguous(), dv.contiguous(),
+                    dsf2, dl, dZ, dA, dB, dmx, dvx)
+        return dmx, dvx
+
+    def sample(self, x, eps_u, eps_f):
+        """Base_SGP_Layer.sample (base_models.py:428-452) with its two standard-normal draws given:
+        u = mu + chol(Su) eps_u [Dout, M], then f = Kfu Kuu^-1 u + chol(Kff + jitter - Kfu Kuu^-1
+        Kuf) eps_f [n, Dout].  Raises LinAlgError when either factorisation fails, as numpy's
+        cholesky does."""
+        n, D, M = x.shape[0], self.Dout, self.M
+        Lu = torch.empty_like(self.Su)
+        info = torch.zeros(D + 1, dtype=torch.int32, device=self.dev)
+        gpk.chol_inv(self.Su.contiguous(), torch.empty_like(self.Su), L=Lu, info=info[:D])
+        u = mm(torch.tril(Lu), eps_u.unsqueeze(-1), beta=1.0, E=self.mu.unsqueeze(-1).contiguous()).squeeze(-1)
+        kff = gpk.kern(x, x, self.lls2, self.lsf2, jitter=JITTER)
+        kfu = gpk.kern(x, self.zu, self.lls2, self.lsf2)
+        qfu = mm(kfu, self.Kinv)
+        vf = mm(qfu, kfu, tB=True, alpha=-1.0, beta=1.0, E=kff)
+        Lf = torch.empty_like(vf)
+        gpk.chol_inv(vf, torch.empty_like(vf), L=Lf, info=info[D:])
+        if int(info.max()) > 0:
+            raise np.linalg.LinAlgError('Matrix is not positive definite')
+        return mm(torch.tril(Lf), eps_f, beta=1.0, E=mm(qfu, u, tB=True))
 
     # ---------------------------------------------------------------- VFE (vfe_models.py)
     def kl(self):

@@ -1018,6 +1018,72 @@ def sdgpr_predict_mc(p, xs, no_samples):
     return samples.reshape(no_samples, np.shape(xs)[0], -1), mf, vf
 
 
+def sdgpr_predict_with_input_grad(p, xs):
+    """``Base_SDGPR.predict_f_with_input_grad`` base_models.py:1186-1230: the posterior moments
+    of the last layer and the gradients of their sums over the outputs w.r.t. the inputs
+    (``backprop_predictive_grads_lvm_mm`` / ``_reg`` :335-426).  The first layer's dv_dx is
+    formed, as the reference forms it (:419-422), from the mean's kfu gradient, so it equals
+    dm_dx."""
+    nl = 0
+    while ('eta2_%d' % nl) in p:
+        nl += 1
+    layers = [layer_unpack(p, '_%d' % i, *_layer_dims(p, '_%d' % i)) for i in range(nl)]
+    ms, vs, aux = [], [], []
+    for i, L in enumerate(layers):
+        if i == 0:
+            m, v, kfu = fwd_det(L, xs, cav=False)
+            aux.append(kfu)
+        else:
+            m, v, p1, p2 = fwd_mm(L, ms[-1], vs[-1], cav=False)
+            aux.append((p1, p2))
+        ms.append(m)
+        vs.append(v)
+    n, Dl = ms[-1].shape
+    dmdm, dmdv, dvdm, dvdv = np.ones((n, Dl)), np.zeros((n, Dl)), np.zeros((n, Dl)), np.ones((n, Dl))
+    for i in range(nl - 1, -1, -1):
+        L = layers[i]
+        ell, sf2 = np.exp(L['ls']), np.exp(2 * L['sf'])
+        if i == 0:
+            kfu = aux[0]
+            dk = dmdm @ L['A'] + 2 * np.einsum('nd,dab,na->nb', dmdv, L['B_det'], kfu)
+            dm_dx = kfu_derivatives(dk, kfu, ell, sf2, xs, L['Z'], grad_x=True)[3]
+            dv_dx = dm_dx.copy()
+        else:
+            p1, p2 = aux[i]
+            out = []
+            for a, b in ((dmdm, dmdv), (dvdm, dvdv)):
+                r = psi_derivatives((a - 2 * b * ms[i]) @ L['A'], p1, np.einsum('nd,dab->nab', b, L['B_sto']), p2,
+                                    ell, sf2, ms[i - 1], vs[i - 1], L['Z'])
+                out += [r[3], r[4]]
+            dmdm, dmdv, dvdm, dvdv = out
+    return ms[-1], vs[-1], dm_dx, dv_dx
+
+
+def layer_sample(L, x):
+    """``Base_SGP_Layer.sample`` base_models.py:428-452: u ~ q(u), then f | u at x with its full
+    covariance; the draws come from numpy's global RNG in the reference's order."""
+    Lu = np.linalg.cholesky(L['Su'])
+    u = L['mu'] + np.einsum('dab,db->da', Lu, np.random.randn(L['Dout'], L['M']))
+    kff = ard_kernel(2 * L['ls'], 2 * L['sf'], x, x) + JITTER * np.eye(x.shape[0])
+    kfu = ard_kernel(2 * L['ls'], 2 * L['sf'], x, L['Z'])
+    qfu = kfu @ L['Kinv']
+    Lf = np.linalg.cholesky(kff - qfu @ kfu.T)
+    return qfu @ u.T + Lf @ np.random.randn(x.shape[0], L['Dout'])
+
+
+def sample_f(p, xs, no_samples, suffixes=('',), nat_param=True):
+    """``sample_f`` of SGPR / SDGPR, base_models.py:1000-1018, 1239-1262: no_samples joint draws
+    through the layers (layer suffixes in order); returns [n, Dout, no_samples]."""
+    layers = [layer_unpack(p, sf, *_layer_dims(p, sf), nat_param) for sf in suffixes]
+    fs = np.zeros((xs.shape[0], layers[-1]['Dout'], no_samples))
+    for k in range(no_samples):
+        x = xs
+        for L in layers:
+            x = layer_sample(L, x)
+        fs[:, :, k] = x
+    return fs
+
+
 def sgpssm_posterior_x(p, prior_mean=0.0, prior_var=1.0):
     """``Base_SGPSSM.get_posterior_x`` base_models.py:1562-1572 with the natural-parameter
     x posterior of ``update_hypers`` base_models.py:1715-1725 -> (mx, vx) [T, Dx]."""

@@ -414,3 +414,27 @@ def test_sdgprh(tag, lik, ykey, at, alpha):
     mf, vf = mdl.predict_f(x[:5])
     assert_close(mf, g[tag + '_mf'], P_TOL, 'mf')
     assert_close(vf, g[tag + '_vf'], P_TOL, 'vf')
+
+
+def test_predictive_input_grad_and_samples():
+    """The deep GP's predict_f_with_input_grad / predict_y_with_input_grad and sample_f of SGPR
+    and SDGPR against the reference's (tests/golden/make_predictive.py), the samples drawn with
+    the same seeds from numpy's global RNG: rel <= 1e-6."""
+    from geepee_gb300 import aep_models as A
+    g = load('predictive.npz')
+    d = load('sdgpr_small.npz')
+    dgp = A.SDGPR(d['x'], d['y'], 5, [3, 2])
+    dgp.update_hypers(sub(d, 'p_'))
+    mf, vf, dm_dx, dv_dx = dgp.predict_f_with_input_grad(d['xs'])
+    for name, got in (('mf', mf), ('vf', vf), ('dm_dx', dm_dx), ('dv_dx', dv_dx)):
+        assert_close(got, g[name], P_TOL, name)
+    my, vy, _, _ = dgp.predict_y_with_input_grad(d['xs'])
+    assert_close(my, g['my'], P_TOL, 'my')
+    assert_close(vy, g['vy'], P_TOL, 'vy')
+    np.random.seed(int(g['seed_dgp']))
+    assert_close(dgp.sample_f(d['xs'][:6], 3), g['fs_dgp'], P_TOL, 'fs dgp')
+    s = load('sgpr_small_nat1.npz')
+    gpr = A.SGPR(s['x'], s['y'], 10)
+    gpr.update_hypers(sub(s, 'p_'))
+    np.random.seed(int(g['seed_gpr']))
+    assert_close(gpr.sample_f(s['x'][:7], 4), g['fs_gpr'], P_TOL, 'fs gpr')

@@ -244,3 +244,18 @@ def test_sdgprh(tag, lik, ykey, at, alpha):
     ref = g['%s_energy_%s' % (tag, at)]
     assert abs(e - ref) <= 1e-12 * abs(ref)
     assert_dict_close(gr, sub(g, '%s_g%s_' % (tag, at)), 1e-10, 'sdgprh')
+
+
+def test_predictive_input_grad_and_samples():
+    """The oracle's predict_f_with_input_grad (deep GP) and sample_f (SGPR, deep GP) against the
+    reference's (tests/golden/make_predictive.py), the samples with the same seeds."""
+    g = load('predictive.npz')
+    d = load('sdgpr_small.npz')
+    r = O.sdgpr_predict_with_input_grad(sub(d, 'p_'), d['xs'])
+    for name, got in zip(('mf', 'vf', 'dm_dx', 'dv_dx'), r):
+        assert_close(got, g[name], 1e-12, name)
+    np.random.seed(int(g['seed_dgp']))
+    assert_close(O.sample_f(sub(d, 'p_'), d['xs'][:6], 3, ('_0', '_1', '_2')), g['fs_dgp'], 1e-10, 'fs dgp')
+    s = load('sgpr_small_nat1.npz')
+    np.random.seed(int(g['seed_gpr']))
+    assert_close(O.sample_f(sub(s, 'p_'), s['x'][:7], 4), g['fs_gpr'], 1e-10, 'fs gpr')
