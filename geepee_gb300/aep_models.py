@@ -1095,10 +1095,12 @@ class SGPSSM(_PackedModel):
         reading the previous step's moments) - then the linear-Gaussian emission
         (lik_layers.py:558-571).  Returns mx, vx [T, Dx] and my, vy_noiseless, vy [T, Dy] (the
         emission covariances' diagonals, as the reference returns them)."""
-        if prop_mode != PROP_MM:
-            raise NotImplementedError('propagation mode %s not implemented on the device path' % prop_mode)
         if x_control is not None:
             raise NotImplementedError('control inputs are not implemented on the device path')
+        if prop_mode == PROP_MC:
+            return self._predict_forward_mc(T, no_samples)
+        if prop_mode != PROP_MM:
+            raise NotImplementedError('unknown prop mode %s' % prop_mode)
         lay = self.dyn_layer
         if not self.updated:
             lay.setup_posterior()
@@ -1113,3 +1115,37 @@ class SGPSSM(_PackedModel):
         my = mxh @ C.T
         vyn = np.einsum('ab,nb,ab->na', C, vxh, C)
         return mxh, vxh, my, vyn, vyn + R
+
+    def _predict_forward_mc(self, T, no_samples):
+        """Base_SGPSSM.predict_forward_mc (base_models.py:1504-1542): no_samples draws of the last
+        latent state, then T steps of sampling from the transition GP's posterior predictive
+        (gpk_det_fwd per step, the whole loop on the device); the draws are taken from numpy's
+        global RNG up front, in the reference's order.  Returns x [T, S, Dx] and the emission's
+        my [T, S, Dy] and noise variances vy [T, S, Dy] (lik_layers.py:558-571 with vf = 0)."""
+        lay = self.dyn_layer
+        if not self.updated:
+            lay.setup_posterior()
+            lay.setup_predict()
+            self.updated = True
+        pm, pv = self.get_posterior_x()
+        Dx = pm.shape[1]
+        eps = _to_dev(np.random.randn((T + 1) * no_samples * Dx).reshape(T + 1, no_samples, Dx), self.dev)
+        xs = (eps[0] * _to_dev(np.sqrt(pv[[-1]]), self.dev) + _to_dev(pm[[-1]], self.dev)).contiguous()
+        x = torch.empty((T, no_samples, Dx), dtype=F64, device=self.dev)
+        for t in range(T):
+            mt, vt, _, _ = lay.fwd_det(xs, cav=False)
+            xs = torch.addcmul(mt, eps[t + 1], vt.sqrt())
+            x[t] = xs
+        p = self.get_hypers()
+        C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
+        xh = x.cpu().numpy()
+        return xh, xh @ C.T, np.broadcast_to(R, (T, no_samples, C.shape[0])).copy()
+
+    def get_posterior_y(self):
+        """Base_SGPSSM.get_posterior_y (base_models.py:1578-1595), linear-Gaussian emission:
+        my, the noiseless and the noisy variances [T, Dy] (diagonals)."""
+        pm, pv = self.get_posterior_x()
+        p = self.get_hypers()
+        C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
+        vf = np.einsum('ab,nb,ab->na', C, pv, C)
+        return pm @ C.T, vf, vf + R

@@ -1118,6 +1118,38 @@ def sgpssm_predict_forward(p, T, prior_mean=0.0, prior_var=1.0):
     return mx, vx, my, vyn, vyn + R
 
 
+def sgpssm_predict_forward_mc(p, T, no_samples, prior_mean=0.0, prior_var=1.0):
+    """``Base_SGPSSM.predict_forward_mc`` base_models.py:1504-1542 (no control inputs,
+    linear-Gaussian emission): no_samples draws of the last latent state, then T steps of
+    sampling from the transition GP's posterior predictive; the emission's mean and noise
+    variance per step.  The draws come from numpy's global RNG in the reference's order."""
+    Mz, Dx = _layer_dims(p, '_dynamic')
+    L = layer_unpack(p, '_dynamic', Mz, Dx)
+    pm, pv = sgpssm_posterior_x(p, prior_mean, prior_var)
+    C = np.asarray(p['C_emission'], dtype=float)
+    R = np.exp(2 * np.asarray(p['R_emission'], dtype=float))
+    x = np.zeros((T, no_samples, Dx))
+    my = np.zeros((T, no_samples, C.shape[0]))
+    vy = np.zeros_like(my)
+    xs = np.random.randn(no_samples, Dx) * np.sqrt(pv[[-1]]) + pm[[-1]]
+    for t in range(T):
+        mt, vt, _ = fwd_det(L, xs, cav=False)
+        xs = np.random.randn(no_samples, Dx) * np.sqrt(vt) + mt
+        x[t], my[t], vy[t] = xs, xs @ C.T, R
+    return x, my, vy
+
+
+def sgpssm_posterior_y(p, prior_mean=0.0, prior_var=1.0):
+    """``Base_SGPSSM.get_posterior_y`` base_models.py:1578-1595 (linear-Gaussian emission):
+    the emission of the latent posterior -> my, the noiseless and the noisy variances [T, Dy]
+    (diagonals)."""
+    pm, pv = sgpssm_posterior_x(p, prior_mean, prior_var)
+    C = np.asarray(p['C_emission'], dtype=float)
+    R = np.exp(2 * np.asarray(p['R_emission'], dtype=float))
+    vf = np.einsum('ab,nb,ab->na', C, pv, C)
+    return pm @ C.T, vf, vf + R
+
+
 # --------------------------------------------------------------------------
 # utils.py
 # --------------------------------------------------------------------------

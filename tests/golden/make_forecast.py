@@ -32,8 +32,12 @@ def main(argv=None):
     T = 15
     mx, vx, my, vyn, vy = mdl.predict_forward(T)
     pm, pv = mdl.get_posterior_x()
+    py_m, py_vf, py_vyn = mdl.get_posterior_y()
+    np.random.seed(81)
+    mc_x, mc_my, mc_vy = mdl.predict_forward(T, prop_mode='MC', no_samples=6)
     out = dict(y=y, T=T, mx=mx, vx=vx, my=my, vy_noiseless=vyn, vy=vy, post_m=pm, post_v=pv,
-               **{'p_' + k: np.asarray(v) for k, v in params.items()})
+               post_y_m=py_m, post_y_vf=py_vf, post_y_vyn=py_vyn, mc_seed=81, mc_samples=6, mc_x=mc_x,
+               mc_my=mc_my, mc_vy=mc_vy, **{'p_' + k: np.asarray(v) for k, v in params.items()})
     np.savez_compressed(os.path.join(HERE, 'sgpssm_forecast.npz'), **out)
     print('wrote', os.path.join(HERE, 'sgpssm_forecast.npz'))
 

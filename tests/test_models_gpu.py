@@ -231,7 +231,7 @@ def test_sgpssm_forecast():
     for name, got in zip(('mx', 'vx', 'my', 'vy_noiseless', 'vy'), out):
         assert_close(got, g[name], P_TOL, name)
     with pytest.raises(NotImplementedError):
-        mdl.predict_forward(3, prop_mode='MC')
+        mdl.predict_forward(3, prop_mode='LIN')
 
 
 def test_sgpssm_small():
@@ -438,3 +438,19 @@ def test_predictive_input_grad_and_samples():
     gpr.update_hypers(sub(s, 'p_'))
     np.random.seed(int(g['seed_gpr']))
     assert_close(gpr.sample_f(s['x'][:7], 4), g['fs_gpr'], P_TOL, 'fs gpr')
+
+
+def test_sgpssm_forecast_mc_and_posterior_y():
+    """predict_forward(prop_mode='MC') with the reference's seed (the transition samples drawn
+    in its order) and get_posterior_y against the reference's (tests/golden/make_forecast.py)."""
+    from geepee_gb300 import aep_models as A
+    g = load('sgpssm_forecast.npz')
+    p = sub(g, 'p_')
+    mdl = A.SGPSSM(g['y'], 2, 8, lik='Gaussian', gp_emi=False)
+    mdl.update_hypers(p)
+    np.random.seed(int(g['mc_seed']))
+    x, my, vy = mdl.predict_forward(int(g['T']), prop_mode='MC', no_samples=int(g['mc_samples']))
+    for name, got in (('mc_x', x), ('mc_my', my), ('mc_vy', vy)):
+        assert_close(got, g[name], P_TOL, name)
+    for name, got in zip(('post_y_m', 'post_y_vf', 'post_y_vyn'), mdl.get_posterior_y()):
+        assert_close(got, g[name], P_TOL, name)

@@ -259,3 +259,16 @@ def test_predictive_input_grad_and_samples():
     s = load('sgpr_small_nat1.npz')
     np.random.seed(int(g['seed_gpr']))
     assert_close(O.sample_f(sub(s, 'p_'), s['x'][:7], 4), g['fs_gpr'], 1e-10, 'fs gpr')
+
+
+def test_sgpssm_forecast_mc_and_posterior_y():
+    """The oracle's sampled forecast (same seed) and the emission of the latent posterior
+    against the reference's (tests/golden/make_forecast.py)."""
+    g = load('sgpssm_forecast.npz')
+    p = sub(g, 'p_')
+    np.random.seed(int(g['mc_seed']))
+    x, my, vy = O.sgpssm_predict_forward_mc(p, int(g['T']), int(g['mc_samples']))
+    for name, got in (('mc_x', x), ('mc_my', my), ('mc_vy', vy)):
+        assert_close(got, g[name], 1e-10, name)
+    for name, got in zip(('post_y_m', 'post_y_vf', 'post_y_vyn'), O.sgpssm_posterior_y(p)):
+        assert_close(got, g[name], 1e-12, name)
