@@ -54,7 +54,7 @@ _SIGS = {
     'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp],
     'gpk_probit_lik': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _vp, _c_dbl, _c_dbl,
                        _vp, _vp, _vp, _vp, _vp],
-    'gpk_lik_exp': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp,
+    'gpk_lik_exp': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp,
                     _vp, _vp, _vp],
     'gpk_gather_rows': [_c_int, ctypes.c_longlong, _vp, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp],
     'gpk_finish': [_c_int, _vp, _c_dbl, _c_int, _vp, _vp, _vp],

@@ -891,6 +891,12 @@ class SGPLVM(_PackedModel):
         mf, vf = self.predict_f(inputs)
         return self._output_probabilistic(mf, vf)
 
+    def impute_missing(self, y, missing_mask, alpha=0.5, no_iters=10, add_noise=False):
+        """Base_SGPLVM.impute_missing (base_models.py:777-837) is unfinished in the reference: it
+        calls SGP_Layer.update_posterior_for_prediction and compute_logZ_and_gradients_imputation,
+        which exist nowhere in it, so it raises there; this raises too."""
+        raise NotImplementedError('impute_missing: unfinished in the reference (no imputation layer methods)')
+
     def get_posterior_x(self, idxs=None):
         """base_models.py:765-775."""
         p = self.get_hypers()

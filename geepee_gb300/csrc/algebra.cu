@@ -285,26 +285,29 @@ __global__ void __launch_bounds__(128) probit_terms_kernel(int S, int nD, int mc
 //   ts = x_k sqrt(2 v) + m, z = y ts,  ll = sum_k w_k/sqrt(pi) log Phi(z),
 //   dm = sum_k y w_k/sqrt(pi) phi(z)/Phi(z),  dv = sum_k (the same) x_k sqrt(2/v)/2,
 // with Phi(z) = erfc(-z/sqrt 2)/2 and log Phi(z) = log1p(-erfc(z/sqrt 2)/2) for z > 0 (both
-// accurate in the tails, as scipy's norm.cdf / norm.logcdf are).  dm, dv are written times
-// `scale`; work[e] = the element's ll.
-__global__ void __launch_bounds__(128) lik_exp_kernel(int kind, int nD, const double* m, const double* v,
+// accurate in the tails, as scipy's norm.cdf / norm.logcdf are).  With S > 1 samples (m, v
+// [S, n, D] against y [n, D], the 3-D forms) every term is an average over the samples, so each
+// element is weighted 1/S.  dm, dv are written times `scale`; work[e] = the element's ll (and,
+// Gaussian, work[nSD + e] its sn term), nSD = S n D elements.
+__global__ void __launch_bounds__(128) lik_exp_kernel(int kind, int nSD, int nD, const double* m, const double* v,
                                                       const double* y, const double* sn, int T, const double* gh_x,
                                                       const double* gh_w, double scale, double* dm, double* dv,
                                                       double* work) {
   const int lane = threadIdx.x & 15;
   const int e = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 4);
-  if (e >= nD) return;   // whole 16-lane groups leave together
+  if (e >= nSD) return;   // whole 16-lane groups leave together
   const unsigned gmask = 0xffffu << (threadIdx.x & 16);
-  const double mm = m[e], vv = v[e], ye = y[e];
+  const double wS = (double)nD / (double)nSD;   // 1/S
+  const double mm = m[e], vv = v[e], ye = y[e % nD];
   const double kSqrt2 = 1.4142135623730951, kSqrtPi = 1.7724538509055159, kPi = 3.141592653589793;
   if (kind == 0) {
     if (lane != 0) return;
     const double sn2 = exp(2.0 * sn[0]);
     const double q = ye * ye - 2.0 * ye * mm + mm * mm + vv;
-    work[e] = -0.5 * log(2.0 * kPi * sn2) - 0.5 / sn2 * q;
-    work[nD + e] = -1.0 + q / sn2;
-    dm[e] = scale * (1.0 / sn2 * (ye - mm));
-    dv[e] = scale * (-0.5 / sn2);
+    work[e] = wS * (-0.5 * log(2.0 * kPi * sn2) - 0.5 / sn2 * q);
+    work[nSD + e] = wS * (-1.0 + q / sn2);
+    dm[e] = scale * (wS * (1.0 / sn2 * (ye - mm)));
+    dv[e] = scale * (wS * (-0.5 / sn2));
     return;
   }
   double ll = 0.0, gm = 0.0, gv = 0.0;
@@ -325,9 +328,9 @@ __global__ void __launch_bounds__(128) lik_exp_kernel(int kind, int nD, const do
     gv += __shfl_xor_sync(gmask, gv, o);
   }
   if (lane == 0) {
-    work[e] = ll;
-    dm[e] = scale * gm;
-    dv[e] = scale * gv;
+    work[e] = wS * ll;
+    dm[e] = scale * (wS * gm);
+    dv[e] = scale * (wS * gv);
   }
 }
 
@@ -428,20 +431,20 @@ extern "C" int gpk_probit_lik(int S, int n, int D, int mc, const double* m, cons
   return gpk::check_launch("probit_lik");
 }
 
-extern "C" int gpk_lik_exp(int kind, int n, int D, const double* m, const double* v, const double* y,
+extern "C" int gpk_lik_exp(int kind, int S, int n, int D, const double* m, const double* v, const double* y,
                            const double* sn, int T, const double* gh_x, const double* gh_w, double scale, double invN,
                            double* dm, double* dv, double* work, double* out, double* g_sn, void* stream) {
-  GPK_REQUIRE((kind == 0 || kind == 1) && n >= 0 && D >= 1 && scale != 0.0, "lik_exp: bad sizes");
+  GPK_REQUIRE((kind == 0 || kind == 1) && S >= 1 && n >= 0 && D >= 1 && scale != 0.0, "lik_exp: bad sizes");
   GPK_REQUIRE(kind == 0 || (T >= 1 && T <= 16 && gh_x && gh_w), "lik_exp: need 1..16 Gauss-Hermite nodes");
-  const long nD = (long)n * D;
-  GPK_REQUIRE(nD < (1L << 31) / 16, "lik_exp: too many elements");
+  const long nD = (long)n * D, nSD = nD * S;
+  GPK_REQUIRE(nSD < (1L << 31) / 16, "lik_exp: too many elements");
   GPK_REQUIRE(out && (kind == 1 || (sn && g_sn)) && (nD == 0 || (m && v && y && dm && dv && work)),
               "lik_exp: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
-  if (nD > 0) lik_exp_kernel<<<(int)((nD * 16 + 127) / 128), 128, 0, st>>>(kind, (int)nD, m, v, y, sn, T, gh_x,
-                                                                           gh_w, scale, dm, dv, work);
-  sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nD, work, scale, invN, out);
-  if (kind == 0) sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nD, work + nD, scale, invN, g_sn);
+  if (nSD > 0) lik_exp_kernel<<<(int)((nSD * 16 + 127) / 128), 128, 0, st>>>(kind, (int)nSD, (int)nD, m, v, y, sn,
+                                                                             T, gh_x, gh_w, scale, dm, dv, work);
+  sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nSD, work, scale, invN, out);
+  if (kind == 0) sum_scaled_kernel<<<1, 1024, 0, st>>>((int)nSD, work + nSD, scale, invN, g_sn);
   return gpk::check_launch("lik_exp");
 }
 

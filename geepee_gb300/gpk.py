@@ -336,15 +336,17 @@ def probit_lik(m, v, y, alpha, scale, invN, dm, dv, out, work=None, mc=False):
     return work
 
 
-def lik_exp(kind, m, v, y, scale, invN, dm, dv, out, sn=None, g_sn=None):
+def lik_exp(kind, m, v, y, scale, invN, dm, dv, out, sn=None, g_sn=None, mc=False):
     """E_q[log p(y | f)] for q(f) = N(m, v) [n, D] and its gradients (lik_layers.py:183-228,
-    418-436): kind 'gaussian' (also the sn gradient into g_sn) or 'probit'.  Writes dm, dv
-    (times scale) and out[0] = scale * invN * sum."""
+    418-436): kind 'gaussian' (also the sn gradient into g_sn) or 'probit'; with mc=True, m and
+    v are [S, n, D] samples and every term is averaged over them.  Writes dm, dv (times scale)
+    and out[0] = scale * invN * sum."""
     n, D = y.shape
+    S = m.shape[0] if mc else 1
     k = 0 if kind == 'gaussian' else 1
-    work = torch.empty((2 - k) * n * D, dtype=torch.float64, device=m.device)
+    work = torch.empty((2 - k) * S * n * D, dtype=torch.float64, device=m.device)
     gh = gh_nodes(m.device)
-    call('gpk_lik_exp', k, n, D, ptr(m), ptr(v), ptr(y), ptr(sn), gh.shape[1], ptr(gh[0]), ptr(gh[1]), float(scale),
+    call('gpk_lik_exp', k, S, n, D, ptr(m), ptr(v), ptr(y), ptr(sn), gh.shape[1], ptr(gh[0]), ptr(gh[1]), float(scale),
          float(invN), ptr(dm), ptr(dv), ptr(work), ptr(out), ptr(g_sn), stream())
 
 

@@ -475,16 +475,17 @@ class DevLayer:
         tr = (self.Kinv.unsqueeze(0) * self.Spmm).sum()
         return 0.5 * (D * self.logdetK - lsu.sum() - D * M + tr)
 
-    def bwd_det_vfe(self, dm, dv, kfu, Bk, x):
+    def bwd_det_vfe(self, dm, dv, kfu, Bk, x, dx=None):
         """VFE SGP_Layer.backprop_grads_reg (vfe_models.py:479-548): deterministic inputs through
         the posterior predictive (A, B_det), upstream dm, dv already scaled, plus the KL term's
-        gradients.  Written into the layer's gradient slots."""
+        gradients.  Written into the layer's gradient slots; with `dx` [n, Din] the inputs'
+        gradient too (backprop_grads_lvm_mc, vfe_models.py:405-477)."""
         D, M = self.Dout, self.M
         K = self.Kinv
         self.zero_accumulators()
         dA, dB = self._dAh, self._dBh
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.A, kfu, Bk, dm, dv, self._dsf2, self._dl, self.g['zu'],
-                    dA)
+                    dA, dx=dx)
         self._kernel_grads(self._dsf2, self._dl, dv)
         gpk.gram(kfu, kfu, dv, dB)
         # sum_n dm_nd (kfu_n K^-1) = dA_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T = K^-1 dB_d K^-1;

@@ -1,6 +1,6 @@
 """Variational free energy (VFE) sparse GP models on the device: the same parameter
 dictionaries, methods and numpy in/out as geepee's ``vfe_models.SGPR`` (vfe_models.py:551-719)
-and ``vfe_models.SGPLVM`` (moment matching, vfe_models.py:722-864).
+and ``vfe_models.SGPLVM`` (moment matching or Monte Carlo, vfe_models.py:722-864).
 
 The objective is -N/n E_q[log p(y_b | f)] + KL(q(u) || p(u)), divided by N, with f the
 posterior predictive at the minibatch inputs.  It reuses the AEP layer's kernels: the posterior
@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from .aep_models import _PackedModel, _to_dev, layer_init_hypers, SGPLVM as _AEP_SGPLVM
-from .config import PROP_MM
+from .config import PROP_MM, PROP_MC, MC_NO_SAMPLES
 from .layer import DevLayer
 from . import gpk
 
@@ -84,8 +84,8 @@ class SGPR(_PackedModel):
 
 
 class SGPLVM(_PackedModel):
-    """GP latent-variable model with the VFE bound (vfe_models.py:722-864), moment matching;
-    energy and gradients divided by N, as the reference's are."""
+    """GP latent-variable model with the VFE bound (vfe_models.py:722-864), moment matching or
+    Monte Carlo; energy and gradients divided by N, as the reference's are."""
 
     def __init__(self, y_train, hidden_size, no_pseudo, lik='Gaussian', prior_mean=0, prior_var=1,
                  nat_param=True):
@@ -109,7 +109,7 @@ class SGPLVM(_PackedModel):
     get_posterior_x = _AEP_SGPLVM.get_posterior_x
 
     def device_objective(self, idx, alpha=None):
-        """vfe_models.py:749-845 (moment matching) on device tensors; idx: device int64 rows."""
+        """vfe_models.py:749-845 on device tensors; idx: device int64 rows."""
         N, lay = self.N, self.layer
         pv = self.ppack.views
         f1 = pv['x1']
@@ -125,10 +125,27 @@ class SGPLVM(_PackedModel):
         post1, post2 = (px1 + f1, px2 + f2) if self.nat_param else (f1 / f2, 1.0 / f2)
         p1b, p2b = post1.index_select(0, idx), post2.index_select(0, idx)
         mx, vx = (p1b / p2b).contiguous(), (1.0 / p2b).contiguous()
-        m, v = lay.fwd_mm(mx, vx, cav=False)
-        dm, dv, ll_s = torch.empty_like(m), torch.empty_like(v), torch.empty_like(self.energy)
-        gpk.lik_exp(self.lik, m, v, yb, scale, 1.0, dm, dv, ll_s, sn=self.sn, g_sn=self.g_sn)
-        dmx, dvx = lay.bwd_mm_vfe(m, dm, dv, mx, vx)
+        if getattr(self, '_mc', False):
+            # Monte Carlo: samples x = eps sqrt(vx) + mx through the deterministic posterior
+            # (base_models.py:309-333), the sample-averaged expected log-likelihood,
+            # backprop_grads_lvm_mc and backprop_grads_reparam (base_models.py:373-388)
+            eps = self._eps_buf
+            S, Q = eps.shape[0], self.Din
+            sd = vx.sqrt()
+            xs = (eps * sd + mx).reshape(S * nb, Q).contiguous()
+            m, v, kfu, Bk = lay.fwd_det(xs, cav=False)
+            dm, dv, ll_s = torch.empty_like(m), torch.empty_like(v), torch.empty_like(self.energy)
+            gpk.lik_exp(self.lik, m.view(S, nb, -1), v.view(S, nb, -1), yb, scale, 1.0, dm, dv, ll_s, sn=self.sn,
+                        g_sn=self.g_sn, mc=True)
+            dxs = torch.empty_like(xs)
+            lay.bwd_det_vfe(dm, dv, kfu, Bk, xs, dx=dxs)
+            dxs = dxs.view(S, nb, Q)
+            dmx, dvx = dxs.sum(0), (dxs * eps).sum(0) / (2.0 * sd)
+        else:
+            m, v = lay.fwd_mm(mx, vx, cav=False)
+            dm, dv, ll_s = torch.empty_like(m), torch.empty_like(v), torch.empty_like(self.energy)
+            gpk.lik_exp(self.lik, m, v, yb, scale, 1.0, dm, dv, ll_s, sn=self.sn, g_sn=self.g_sn)
+            dmx, dvx = lay.bwd_mm_vfe(m, dm, dv, mx, vx)
         # KL(q(x_b) || p(x)) scaled by N/n (compute_KL_x, vfe_models.py:847-864)
         m0, v0 = self.prior_mean, self.prior_var
         kl_x = (0.5 * (np.log(v0) - torch.log(vx) + (vx + (mx - m0) ** 2) / v0 - 1.0)).sum()
@@ -154,11 +171,21 @@ class SGPLVM(_PackedModel):
         return self.energy
 
     def objective_function(self, params, mb_size, alpha='not_used', prop_mode=PROP_MM):
-        """vfe_models.py:749-845; moment matching only (prop_mode='MC' raises)."""
-        if prop_mode != PROP_MM:
+        """vfe_models.py:749-845, moment matching or Monte Carlo.  The Monte Carlo samples are
+        drawn from numpy's global RNG after the minibatch, as the reference draws them
+        (np.random.randn(MC_NO_SAMPLES, n, Din), base_models.py:320), so a seeded run sees the
+        same samples."""
+        if prop_mode not in (PROP_MM, PROP_MC):
             raise NotImplementedError('propagation mode not implemented')
         N = self.N
         idx = np.arange(N) if mb_size == N else np.random.choice(N, mb_size, replace=False)
+        self._mc = prop_mode == PROP_MC
+        if self._mc:
+            eps = np.random.randn(MC_NO_SAMPLES, len(idx), self.Din)
+            if getattr(self, '_eps_buf', None) is None or tuple(self._eps_buf.shape) != eps.shape:
+                self._eps_buf = torch.empty(eps.shape, dtype=torch.float64, device=self.dev)
+                self._graphs = {k: g for k, g in self._graphs.items() if not k[-1]}   # new buffer
+            self._eps_buf.copy_(torch.from_numpy(eps))
         self.update_hypers(params)
         return self._objective_host(idx, 'vfe')
 

@@ -287,14 +287,15 @@ int gpk_probit_lik(int S, int n, int D, int mc, const double* m, const double* v
                    double* dv, double* work, double* out, void* stream);
 
 /* Expected log-likelihood of a minibatch under q(f) = N(m, v), the data term of the
- * variational free energy, m, v, y [n, D]:
+ * variational free energy, m, v, y [n, D]; with S > 1, m and v hold S samples [S, n, D] against
+ * y [n, D] and every term is averaged over them (the 3-D forms of the same functions):
  *   kind 0, Gaussian (Gauss_Layer.compute_log_lik_exp, backprop_grads_log_lik_exp,
  *     geepee/lik_layers.py:183-228): *g_sn = scale * invN * sum(-1 + (y^2 - 2ym + m^2 + v)/sn2),
- *     work [2 n D];
+ *     work [2 S n D];
  *   kind 1, probit (Probit_Layer.compute_log_lik_exp, lik_layers.py:418-436) with T <= 16
- *     Gauss-Hermite nodes gh_x, gh_w (hermgauss(T)); sn and g_sn unused; work [n D].
+ *     Gauss-Hermite nodes gh_x, gh_w (hermgauss(T)); sn and g_sn unused; work [S n D].
  * Writes dm, dv = scale * d/d(m, v) and *out = scale * invN * sum E[log p(y|f)] (overwritten). */
-int gpk_lik_exp(int kind, int n, int D, const double* m, const double* v, const double* y, const double* sn, int T,
+int gpk_lik_exp(int kind, int S, int n, int D, const double* m, const double* v, const double* y, const double* sn, int T,
                 const double* gh_x, const double* gh_w, double scale, double invN, double* dm, double* dv,
                 double* work, double* out, double* g_sn, void* stream);
 

@@ -374,15 +374,18 @@ def vfe_kl(L):
     return 0.5 * (ld_prior - ld_post - D * M + np.sum(L['Kinv'][None] * L['Spmm']))
 
 
-def vfe_bwd_det(L, dm, dv, kfu, x):
+def vfe_bwd_det(L, dm, dv, kfu, x, grad_x=False):
     """VFE ``SGP_Layer.backprop_grads_reg`` vfe_models.py:479-548: the expected log-likelihood's
-    gradients through the posterior predictive (dm, dv already scaled) plus the KL term's."""
+    gradients through the posterior predictive (dm, dv already scaled) plus the KL term's.  With
+    grad_x also the inputs' gradient (``backprop_grads_lvm_mc`` vfe_models.py:405-477, the same
+    function with compute_kfu_derivatives(..., grad_x=True))."""
     ell = np.exp(L['ls'])
     sf2 = np.exp(2 * L['sf'])
     K = L['Kinv']
     kK = kfu @ K
     dkfu = dm @ L['A'] + 2 * np.einsum('nd,dab,na->nb', dv, L['B_det'], kfu)
-    dsf2, dl, dz = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'])
+    r = kfu_derivatives(dkfu, kfu, ell, sf2, x, L['Z'], grad_x=grad_x)
+    dsf2, dl, dz = r[:3]
     dls = dl * ell
     dsf = 2 * sf2 * (dsf2 + dv.sum())
     dmu = dm.T @ kK + np.einsum('ab,db->da', K, L['mu'])
@@ -393,7 +396,8 @@ def vfe_bwd_det(L, dm, dv, kfu, x):
     dK = (dA.T @ L['mu'] + 2 * np.einsum('dab,dac->bc', K[None] @ L['Su'], dB) - dB.sum(0) + dKu
           - 0.5 * L['Dout'] * L['Kuu'] + 0.5 * L['Spmm'].sum(0))
     dsf, dls, dz = _finish_hyp(L, dsf, dls, dz, -K @ dK @ K)
-    return {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1, 'eta2': e2}
+    g = {'sf': dsf, 'ls': dls, 'zu': dz, 'eta1_R': e1, 'eta2': e2}
+    return (g, r[3]) if grad_x else g
 
 
 def vfe_bwd_mm(L, m, dm, dv, psi1, psi2, mx, vx):
@@ -557,11 +561,15 @@ def vfe_sgpr_objective(x, y, p, idx=None, nat_param=True, fixed=(), lik='gaussia
     return _finish(scale * ll + vfe_kl(L), g, N, fixed)
 
 
-def vfe_sgplvm_objective(y, p, idx=None, prior_mean=0.0, prior_var=1.0, nat_param=True, fixed=(), lik='gaussian'):
-    """VFE ``SGPLVM.objective_function`` vfe_models.py:749-845 (moment matching): the latent
-    posterior's moments through the GP posterior, -N/n E_q[log p(y_b | f)] + N/n KL(q(x_b) || p(x))
-    + KL(q(u) || p(u)), divided by N; x gradients by ``compute_posterior_grad_x``
-    (base_models.py:913-929)."""
+def vfe_sgplvm_objective(y, p, idx=None, prior_mean=0.0, prior_var=1.0, nat_param=True, fixed=(), lik='gaussian',
+                         eps=None):
+    """VFE ``SGPLVM.objective_function`` vfe_models.py:749-845: the latent posterior's moments
+    through the GP posterior, -N/n E_q[log p(y_b | f)] + N/n KL(q(x_b) || p(x)) + KL(q(u) || p(u)),
+    divided by N; x gradients by ``compute_posterior_grad_x`` (base_models.py:913-929).  Moment
+    matching, or with ``eps`` [S, n, Q] Monte Carlo: samples x = eps sqrt(vx) + mx through the
+    deterministic posterior (base_models.py:309-333), the 3-D expected log-likelihood (the
+    sample average), ``backprop_grads_lvm_mc`` and ``backprop_grads_reparam``
+    (base_models.py:373-388)."""
     N, Dy = y.shape
     Mz, Dout = _layer_dims(p, '')
     if idx is None:
@@ -575,14 +583,27 @@ def vfe_sgplvm_objective(y, p, idx=None, prior_mean=0.0, prior_var=1.0, nat_para
     px1, px2 = prior_mean / prior_var, 1.0 / prior_var
     post1, post2 = (px1 + f1, px2 + f2) if nat_param else (f1 / f2, 1.0 / f2)
     mx, vx = post1[idx] / post2[idx], 1.0 / post2[idx]
-    m, v, p1, p2 = fwd_mm(L, mx, vx, cav=False)
-    if lik == 'gaussian':
-        ll, dm, dv, dsn = gauss_lik_exp(m, v, yb, p['sn'])
+    if eps is None:
+        m, v, p1, p2 = fwd_mm(L, mx, vx, cav=False)
+        yy, w = yb, 1.0
     else:
-        ll, dm, dv = probit_lik_exp(m, v, yb)
-    grads, gi = vfe_bwd_mm(L, m, scale * dm, scale * dv, p1, p2, mx, vx)
+        S, Q = eps.shape[0], mx.shape[1]
+        xs = (eps * np.sqrt(vx) + mx).reshape(S * nb, Q)
+        m, v, kfu = fwd_det(L, xs, cav=False)
+        yy, w = np.tile(yb, (S, 1)), 1.0 / S
     if lik == 'gaussian':
-        grads['sn'] = scale * dsn
+        ll, dm, dv, dsn = gauss_lik_exp(m, v, yy, p['sn'])
+    else:
+        ll, dm, dv = probit_lik_exp(m, v, yy)
+    ll, dm, dv = w * ll, w * dm, w * dv
+    if eps is None:
+        grads, gi = vfe_bwd_mm(L, m, scale * dm, scale * dv, p1, p2, mx, vx)
+    else:
+        grads, dx = vfe_bwd_det(L, scale * dm, scale * dv, kfu, xs, grad_x=True)
+        dx = dx.reshape(eps.shape)
+        gi = {'mx': dx.sum(0), 'vx': np.sum(dx * eps, axis=0) / (2 * np.sqrt(vx))}
+    if lik == 'gaussian':
+        grads['sn'] = scale * w * dsn
     kl_x = 0.5 * (np.log(prior_var) - np.log(vx) + (vx + (mx - prior_mean) ** 2) / prior_var - 1)
     scale_x = N / nb
     dmx = gi['mx'] + scale_x * (mx - prior_mean) / prior_var

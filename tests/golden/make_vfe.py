@@ -1,7 +1,7 @@
 """Golden fixtures for the VFE sparse GP regression (vfe_models.py:292-719): the reference's own
 ``vfe_models.SGPR`` through the ``oracle/_ref`` shim on small seeded inputs, with the Gaussian
 likelihood (natural and moment parameters) and the probit likelihood, full batch and a
-minibatch, plus its predictions; and ``vfe_models.SGPLVM`` (moment matching) likewise.  Writes
+minibatch, plus its predictions; and ``vfe_models.SGPLVM`` (moment matching and Monte Carlo) likewise.  Writes
 ``vfe_sgpr.npz`` and ``vfe_sgplvm.npz``.
 Usage:  python tests/golden/make_vfe.py [--src DIR]"""
 from __future__ import annotations
@@ -78,6 +78,11 @@ def main(argv=None):
         np.random.seed(56)
         e, g = mdl.objective_function(cp(params), 6)
         out.update({tag + '_energy_mb': e, tag + '_mb_idx': idx}, **_pre(g, tag + '_gmb_'))
+        # Monte Carlo propagation, full batch: the samples are the first draw after seeding
+        np.random.seed(57)
+        e, g = mdl.objective_function(cp(params), 14, prop_mode='MC')
+        np.random.seed(57)
+        out.update({tag + '_energy_mc': e, tag + '_eps_mc': np.random.randn(5, 14, 2)}, **_pre(g, tag + '_gmc_'))
     np.savez_compressed(os.path.join(HERE, 'vfe_sgplvm.npz'), **out)
     print('wrote', os.path.join(HERE, 'vfe_sgplvm.npz'))
 

@@ -371,9 +371,9 @@ def test_sgplvm_init_hypers_matches_reference(nat):
 @pytest.mark.parametrize('tag,lik,ykey,nat', [('g1', 'Gaussian', 'y', True), ('g0', 'Gaussian', 'y', False),
                                              ('p1', 'Probit', 'yc', True)])
 def test_vfe_sgplvm(tag, lik, ykey, nat):
-    """vfe_models.SGPLVM (moment matching) against the reference's (tests/golden/make_vfe.py):
-    energy rel <= 1e-6, gradients per key within max(1e-6, G_FACTOR x the oracle's one-ulp
-    sensitivity), full batch and a minibatch drawn as the reference draws it."""
+    """vfe_models.SGPLVM against the reference's (tests/golden/make_vfe.py): energy rel <= 1e-6,
+    gradients per key within max(1e-6, G_FACTOR x the oracle's one-ulp sensitivity); moment
+    matching, full batch and a minibatch drawn as the reference draws it, and Monte Carlo."""
     from tests._helpers import noise_floor, assert_grads_close
     from geepee_gb300 import vfe_models as V
     g = load('vfe_sgplvm.npz')
@@ -391,6 +391,13 @@ def test_vfe_sgplvm(tag, lik, ykey, nat):
     _energy_ok(e, g[tag + '_energy_mb'])
     fl = noise_floor(lambda q: O.vfe_sgplvm_objective(y, q, idx=g[tag + '_mb_idx'], nat_param=nat, lik=ol), p)
     assert_grads_close(gr, sub(g, tag + '_gmb_'), fl, G_TOL, G_FACTOR, 'vfe lvm mb ' + tag)
+    # Monte Carlo propagation with the reference's draws (the first after seeding)
+    np.random.seed(57)
+    e, gr = mdl.objective_function(cp(p), 14, prop_mode='MC')
+    _energy_ok(e, g[tag + '_energy_mc'])
+    eps = g[tag + '_eps_mc']
+    fl = noise_floor(lambda q: O.vfe_sgplvm_objective(y, q, nat_param=nat, lik=ol, eps=eps), p)
+    assert_grads_close(gr, sub(g, tag + '_gmc_'), fl, G_TOL, G_FACTOR, 'vfe lvm mc ' + tag)
 
 
 @pytest.mark.parametrize('tag,lik,ykey', [('g', 'Gaussian', 'y'), ('p', 'Probit', 'yc')])

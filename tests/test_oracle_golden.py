@@ -232,6 +232,9 @@ def test_vfe_sgplvm(tag, lik, ykey, nat):
     e, gr = O.vfe_sgplvm_objective(g[ykey], p, idx=g[tag + '_mb_idx'], nat_param=nat, lik=lik)
     assert abs(e - g[tag + '_energy_mb']) <= 1e-12 * abs(g[tag + '_energy_mb'])
     assert_dict_close(gr, sub(g, tag + '_gmb_'), 1e-9, 'vfe lvm mb ' + tag)
+    e, gr = O.vfe_sgplvm_objective(g[ykey], p, nat_param=nat, lik=lik, eps=g[tag + '_eps_mc'])
+    assert abs(e - g[tag + '_energy_mc']) <= 1e-12 * abs(g[tag + '_energy_mc'])
+    assert_dict_close(gr, sub(g, tag + '_gmc_'), 1e-9, 'vfe lvm mc ' + tag)
 
 
 @pytest.mark.parametrize('tag,lik,ykey', [('g', 'gaussian', 'y'), ('p', 'probit', 'yc')])
