@@ -27,7 +27,10 @@ namespace psi_impl {
 
 constexpr int QMAX = 8;
 constexpr int DMAX = 4;
-constexpr int NT = 512;        // threads per CTA
+constexpr int NT = 512;        // threads per CTA (forward)
+// threads per CTA of the backward (one CTA per SM): 32 warps when Q <= 2 (64 registers a
+// thread, no spills), 16 when the per-dimension sums of Q <= 8 need more registers
+__host__ __device__ constexpr int nt_bwd(int QC) { return QC <= 2 ? 1024 : 512; }
 constexpr int PPT_MAX = 16;    // pairs per thread for register-resident per-pair sums
 constexpr int RED = 48;        // reduction slots per warp
 
@@ -515,7 +518,8 @@ __device__ __forceinline__ PointSlot<T> bslot(const BSmem<T>& s, int pt, int M, 
 }
 
 template <typename T, int NPB, int DB, int QC>
-__global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
+__global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
+  constexpr int NTB = nt_bwd(QC);
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   const int M = a.M, Q = a.Q, D = a.Dout;
@@ -523,12 +527,12 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   BSmem<T> s = bcarve<T>(smem_raw, M, Q, P, a.accb_smem ? D * P : 0, NPB, a.bs_smem ? D * P : 0);
   // ---- per-CTA tables: exp table, Z, lengthscales, sf2, G_ab and the symmetrised B
   load_exp_table(s.tab);
-  for (int i = threadIdx.x; i < M * Q; i += NT) {
+  for (int i = threadIdx.x; i < M * Q; i += NTB) {
     s.z[i] = Num<T>::ld(a.Z[i]);
     s.dz[i] = Num<T>::zero();
   }
   if (s.accB)
-    for (int i = threadIdx.x; i < D * P; i += NT) s.accB[i] = Num<T>::zero();
+    for (int i = threadIdx.x; i < D * P; i += NTB) s.accB[i] = Num<T>::zero();
   __syncthreads();
   if (threadIdx.x < Q) {
     const int q = threadIdx.x;
@@ -545,7 +549,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
     s.misc[1] = exp_tab(lsf, s.tab);
   }
   __syncthreads();
-  for (int p = threadIdx.x; p < P; p += NT) {
+  for (int p = threadIdx.x; p < P; p += NTB) {
     int ia, ib;
     pair_of(p, ia, ib);
     T g = Num<T>::zero();
@@ -580,11 +584,11 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   // each CTA takes a contiguous range of points, NPB at a time
   const int nbeg = (int)((long)a.N * blockIdx.x / gridDim.x);
   const int nend = (int)((long)a.N * (blockIdx.x + 1) / gridDim.x);
-  const int ia0 = threadIdx.x;   // the pseudo-input of this thread in the per-row phases (M <= NT)
+  const int ia0 = threadIdx.x;   // the pseudo-input of this thread in the per-row phases (M <= NTB)
   for (int n0 = nbeg; n0 < nend; n0 += NPB) {
     const int npts = min(NPB, nend - n0);
     // ---- per-point constants and upstream gradients
-    for (int t = threadIdx.x; t < 4 * npts * Q; t += NT) {
+    for (int t = threadIdx.x; t < 4 * npts * Q; t += NTB) {
       const int part = t & 3, pq = t >> 2, pt = pq / Q, q = pq - pt * Q;
       dims_of<T, S>(a, s.ell2, s.lnl, s.tab, bslot(s, pt, M, Q), n0 + pt, q, part);
     }
@@ -653,16 +657,16 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
       for (int d = 0; d < DB; ++d)
         dvr[pt][d] = (pt < npts && d < D) ? s.pg[pt * 2 * DMAX + DMAX + d] : Num<T>::zero();
     if (NPB == 1 && Q == QC && D == DB && s.Bs && s.accB && !a.b_stride) {
-      // the common configuration, branch-free: two pairs (p, p + NT) per iteration, each step
+      // the common configuration, branch-free: two pairs (p, p + NTB) per iteration, each step
       // written for both, so that their dependent double-float chains interleave
       const T* hu = s.u;
-      for (int p0 = threadIdx.x; p0 < P; p0 += 2 * NT) {
+      for (int p0 = threadIdx.x; p0 < P; p0 += 2 * NTB) {
         int pp[2], ia[2], ib[2];
         bool ok[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          ok[u] = p0 + u * NT < P;
-          pp[u] = ok[u] ? p0 + u * NT : p0;
+          ok[u] = p0 + u * NTB < P;
+          pp[u] = ok[u] ? p0 + u * NTB : p0;
           pair_of(pp[u], ia[u], ib[u]);
         }
         T arg[2];
@@ -696,7 +700,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
         }
       }
     } else
-    for (int p = threadIdx.x; p < P; p += NT) {
+    for (int p = threadIdx.x; p < P; p += NTB) {
       int ia, ib;
       pair_of(p, ia, ib);
       const T gab = s.G[p];
@@ -761,7 +765,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
     }
     __syncthreads();
     // ---- row sums, 8 threads per (point, row)
-    for (int rid0 = 0; rid0 < npts * M; rid0 += NT / 8) {
+    for (int rid0 = 0; rid0 < npts * M; rid0 += NTB / 8) {
       const int rid = rid0 + (threadIdx.x >> 3), sl = threadIdx.x & 7;
       const int pt = rid / M, ia = rid - pt * M;
       T R = Num<T>::zero();
@@ -872,7 +876,7 @@ __global__ void __launch_bounds__(NT) psi_bwd_kernel(PsiArgs<typename Num<T>::st
   }
   // ---- flush CTA accumulators
   if (a.dB && s.accB) {
-    for (int p = threadIdx.x; p < P; p += NT) {
+    for (int p = threadIdx.x; p < P; p += NTB) {
       int ia, ib;
       pair_of(p, ia, ib);
       for (int d = 0; d < D; ++d) {
@@ -967,7 +971,7 @@ int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t 
   int grid = gpk::sm_count();
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;
-  k<<<grid, NT, sm, st>>>(a);
+  k<<<grid, nt_bwd(QC), sm, st>>>(a);
   return gpk::check_launch("psi_bwd");
 }
 
@@ -985,7 +989,7 @@ template <typename T>
 int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   PsiArgs<typename Num<T>::store_t> a = a_in;
   const int P = a.M * (a.M + 1) / 2;
-  if (a.M > NT) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d > %d", a.M, NT);
+  if (a.M > nt_bwd(QMAX)) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d > %d", a.M, nt_bwd(QMAX));
   if (5 * (a.Q <= 2 ? 2 : QMAX) + 1 > RED) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: Q=%d too large", a.Q);
   const size_t cap = 227 * 1024;
   const int nbs = a.b_stride == 0 ? a.Dout * P : 0, nacc = a.Dout * P;
