@@ -21,8 +21,8 @@ import numpy as np
 import torch
 from scipy.optimize import minimize
 
-from .config import PROP_MM, PROP_MC, PROP_LIN, JITTER, MC_NO_SAMPLES
-from .layer import DevLayer, gauss_logZ, gauss_logZ_mc, gauss_dsn, mm, mv, setup_layers
+from .config import PROP_MM, PROP_MC, PROP_LIN, JITTER, MC_NO_SAMPLES  # noqa: F401  (the reference exports them)
+from .layer import DevLayer, gauss_logZ, gauss_logZ_mc, gauss_dsn, setup_layers
 from .utils import ObjectiveWrapper, flatten_dict, unflatten_dict, adam
 from .pack import Pack
 from . import gpk
