@@ -99,14 +99,17 @@ def case(name):
         l2, s2 = _d(np.zeros(2)), _d(np.zeros(1))
         g1, g2, g3 = z(1), z(2), z(100, 2)
         return lambda: gpk.trace_kzz(Mm, Z, l2, s2, g1, g2, g3)
-    if name == 'objective_dgp':
+    if name == 'objective_dgp' or name.startswith('objective_dgp_mb'):
+        # one objective+gradient evaluation of the 2-layer deep GP (N=20000, M=100); the
+        # minibatch is 1000 points, or the size after 'objective_dgp_mb'
         from . import aep_models as A
+        nb = 1000 if name == 'objective_dgp' else int(name[len('objective_dgp_mb'):])
         x, y = W.dgp_regression(seed=0)
         np.random.seed(1)
         mdl = A.SDGPR(x, y, 100, [2])
         mdl.update_hypers(mdl.init_hypers(y))
         mdl.use_graphs = False
-        idx = torch.as_tensor(np.random.RandomState(2).choice(x.shape[0], 1000, replace=False),
+        idx = torch.as_tensor(np.random.RandomState(2).choice(x.shape[0], nb, replace=False),
                               device='cuda')
         return lambda: mdl.device_objective(idx, 0.5)
     raise SystemExit(f'unknown case {name}')
