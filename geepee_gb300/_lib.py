@@ -51,7 +51,7 @@ _SIGS = {
     'gpk_small_spd': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     'gpk_trace_kzz': [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     'gpk_lincomb': [_vp, _vp],
-    'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp],
+    'gpk_gauss_lik': [_c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _c_int, _vp],
     'gpk_probit_lik': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _vp, _c_dbl, _c_dbl,
                        _vp, _vp, _vp, _vp, _vp],
     'gpk_lik_exp': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp, _vp,

@@ -445,7 +445,15 @@ class SDGPR(_PackedModel):
             ms.append(m)
             vs.append(v)
         dmi, dvi = torch.empty_like(ms[-1]), torch.empty_like(vs[-1])
-        self._log_Z(ms[-1], vs[-1], yb, alpha, scale, 1.0 / N, dmi, dvi, self.energy)
+        if self.lik == 'gaussian':
+            # the backward needs only dm, dv: the energy and sn sums run on a side stream
+            gpk.gauss_lik(ms[-1], vs[-1], yb, self.sn, alpha, scale, 1.0 / N, dmi, dvi, self.energy, self.g_sn, part=1)
+            side[1].wait_stream(main)
+            with torch.cuda.stream(side[1]):
+                gpk.gauss_lik(ms[-1], vs[-1], yb, self.sn, alpha, scale, 1.0 / N, dmi, dvi, self.energy, self.g_sn,
+                              part=2)
+        else:
+            self._log_Z(ms[-1], vs[-1], yb, alpha, scale, 1.0 / N, dmi, dvi, self.energy)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
         main.wait_stream(side[0])   # the zeroed accumulators
@@ -466,6 +474,7 @@ class SDGPR(_PackedModel):
                 forked.append(st_side)
         for st_side in forked:     # join only the branches forked here (graph-capture rule)
             main.wait_stream(st_side)
+        main.wait_stream(side[1])   # the likelihood sums (the energy is added to below)
         for lay in self.layers:
             lay.prezeroed = False
         self.layers[0].side = None

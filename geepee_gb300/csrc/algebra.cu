@@ -405,13 +405,13 @@ extern "C" int gpk_aep_phi(int D, int M, double N, double alpha, const double* l
 
 extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn,
                              double alpha, double scale, double invN, double* dm, double* dv, double* energy,
-                             double* g_sn, void* stream) {
-  GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0 && scale != 0.0, "gauss_lik: bad sizes");
+                             double* g_sn, int part, void* stream) {
+  GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0 && scale != 0.0 && part >= 0 && part <= 2, "gauss_lik: bad sizes");
   GPK_REQUIRE(m && v && y && sn && dm && dv && energy && g_sn, "gauss_lik: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
   const int nD = n * D;
-  if (nD > 0) gauss_grad_kernel<<<(nD + 127) / 128, 128, 0, st>>>(nD, m, v, y, sn, alpha, scale, dm, dv);
-  gauss_sum_kernel<<<1, 1024, 0, st>>>(n, D, m, v, y, sn, dv, alpha, scale, invN, energy, g_sn);
+  if (part != 2 && nD > 0) gauss_grad_kernel<<<(nD + 127) / 128, 128, 0, st>>>(nD, m, v, y, sn, alpha, scale, dm, dv);
+  if (part != 1) gauss_sum_kernel<<<1, 1024, 0, st>>>(n, D, m, v, y, sn, dv, alpha, scale, invN, energy, g_sn);
   return gpk::check_launch("gauss_lik");
 }
 

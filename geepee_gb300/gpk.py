@@ -303,10 +303,12 @@ def aep_phi(D, M, N, alpha, logdetK, ldSuinv, ldShinv, mu, mh, th2, w, out):
          ptr(th2), float(w), ptr(out), stream())
 
 
-def gauss_lik(m, v, y, sn, alpha, scale, invN, dm, dv, energy, g_sn):
+def gauss_lik(m, v, y, sn, alpha, scale, invN, dm, dv, energy, g_sn, part=0):
+    """Gaussian likelihood (gpk_gauss_lik): part 0 both launches, 1 the gradients dm, dv only,
+    2 the energy and sn-gradient sums only (after part 1)."""
     n, D = y.shape
     call('gpk_gauss_lik', n, D, ptr(m), ptr(v), ptr(y), ptr(sn), float(alpha), float(scale), float(invN), ptr(dm),
-         ptr(dv), ptr(energy), ptr(g_sn), stream())
+         ptr(dv), ptr(energy), ptr(g_sn), int(part), stream())
 
 
 GH_DEGREE = 10   # Gauss-Hermite nodes of the probit quadrature (config.py:12)

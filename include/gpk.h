@@ -269,9 +269,11 @@ int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, con
  *   dm = scale r/vt,  dv = scale (-1/(2 vt) + r^2/(2 vt^2))         (written, [n, D])
  *   *energy = scale * logZ * invN,  *g_sn = scale (sum(dv)/scale * 2 sn2/alpha + n D (1-alpha)) * invN
  * (both overwritten); logZ includes the alpha-power normaliser n D (log(2 pi sn2/alpha)/2
- * - alpha log(2 pi sn2)/2). */
+ * - alpha log(2 pi sn2)/2).  part 0 does both; part 1 only dm, dv; part 2 only the two sums
+ * (after part 1, e.g. on a second stream while the backward consumes dm, dv). */
 int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn, double alpha,
-                  double scale, double invN, double* dm, double* dv, double* energy, double* g_sn, void* stream);
+                  double scale, double invN, double* dm, double* dv, double* energy, double* g_sn, int part,
+                  void* stream);
 
 /* Probit likelihood of labels y in {-1, +1} (Probit_Layer.compute_log_Z,
  * geepee/lik_layers.py:303-416; the layer has no hyperparameters, so backprop_grads
