@@ -355,3 +355,32 @@ def test_lik_exp_vs_oracle(kind, n, D):
     if m.size:
         assert_close(dm.cpu().numpy(), scale * rdm, 1e-11, 'dm')
         assert_close(dv.cpu().numpy(), scale * rdv, 1e-11, 'dv')
+
+
+def test_gauss_lik_parts_match_whole():
+    """gpk_gauss_lik as two parts (gradients, then the sums on a second stream) gives exactly
+    the single call's outputs."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(5)
+    n, D = 300, 2
+    m, v, y = dev(rng.randn(n, D)), dev(0.1 + rng.rand(n, D)), dev(rng.randn(n, D))
+    sn = dev([0.5 * np.log(0.2)])
+    outs = []
+    for split in (False, True):
+        dm, dv = torch.empty_like(m), torch.empty_like(m)
+        e, g = torch.zeros(1, dtype=torch.float64, device='cuda'), torch.zeros(1, dtype=torch.float64, device='cuda')
+        if split:
+            gpk.gauss_lik(m, v, y, sn, 0.5, -40.0, 0.01, dm, dv, e, g, part=1)
+            s2 = torch.cuda.Stream()
+            s2.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s2):
+                gpk.gauss_lik(m, v, y, sn, 0.5, -40.0, 0.01, dm, dv, e, g, part=2)
+            torch.cuda.current_stream().wait_stream(s2)
+        else:
+            gpk.gauss_lik(m, v, y, sn, 0.5, -40.0, 0.01, dm, dv, e, g)
+        torch.cuda.synchronize()
+        outs.append([t.cpu().numpy() for t in (dm, dv, e, g)])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    ref = O.gauss_logZ(m.cpu().numpy(), v.cpu().numpy(), y.cpu().numpy(), sn.cpu().numpy(), 0.5)
+    assert abs(outs[0][2][0] - (-40.0 * 0.01 * ref[0])) <= 1e-12 * abs(40.0 * 0.01 * ref[0])
