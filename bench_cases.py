@@ -1,6 +1,7 @@
-"""Small, self-contained kernel cases for profiling (ncu) and micro-timing.
+"""Small, self-contained kernel cases of the benchmark's workloads, for ncu captures and
+micro-timing (a harness beside bench.py; not part of the package).
 
-  python -m geepee_gb300.profile_cases <case> [--reps R] [--time]
+  python bench_cases.py <case> [--reps R] [--time]
 
 Cases run one kernel of the deep-GP objective on its real input shapes:
   psi_bwd_dgp   psi backward, 1000 points, M=100, Q=2 (layer 2 of the 2-layer DGP), df64
@@ -20,12 +21,14 @@ With --time, prints the mean device time per launch (CUDA events).
 from __future__ import annotations
 
 import argparse
+import os
 import sys
 
 import numpy as np
 import torch
 
-from . import gpk, workloads as W
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from geepee_gb300 import gpk, workloads as W  # noqa: E402
 
 
 def _d(a, dtype=torch.float64):
@@ -49,8 +52,9 @@ def case(name):
         gpk.psi_fwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'], m_out=m,
                     v_out=torch.empty_like(m))
         bufs = (z(1), z(Q), z(M, Q), z(1, M), z(1, M, M), z(N, Q), z(N, Q))
+        work = z(gpk.work_elems(gpk.OP_PSI_BWD, N, M, Q, 1))
         return lambda: gpk.psi_bwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'], m,
-                                   t['dm'], t['dv'], *bufs)
+                                   t['dm'], t['dv'], *bufs, work=work)
     if name in ('psi_fwd_dgp', 'psi_fwd_c2', 'psi_fwd_c2_f32'):
         N, Q, M = (1000, 2, 100) if name == 'psi_fwd_dgp' else (10000, 5, 100)
         dtype = torch.float32 if name.endswith('f32') else torch.float64
@@ -90,19 +94,22 @@ def case(name):
         dm, dv = _d(rng.randn(1000, 2)), _d(rng.randn(1000, 2))
         if name == 'gram_dgp':
             C = z(2, 100, 100)
-            return lambda: gpk.gram(kfu, kfu, dv, C)
+            work = z(gpk.work_elems(gpk.OP_GRAM, 1000, 100, 8, 2))
+            return lambda: gpk.gram(kfu, kfu, dv, C, work=work)
         bufs = (z(1), z(8), z(100, 8), z(2, 100))
-        return lambda: gpk.det_bwd(x, Z, l2, s2, A, kfu, Bk, dm, dv, *bufs)
+        work = z(gpk.work_elems(gpk.OP_DET_BWD, 1000, 100, 8, 2))
+        return lambda: gpk.det_bwd(x, Z, l2, s2, A, kfu, Bk, dm, dv, *bufs, work=work)
     if name == 'trace_m100':
         rng = np.random.RandomState(0)
         Mm, Z = _d(rng.randn(100, 100)), _d(rng.randn(100, 2))
         l2, s2 = _d(np.zeros(2)), _d(np.zeros(1))
         g1, g2, g3 = z(1), z(2), z(100, 2)
-        return lambda: gpk.trace_kzz(Mm, Z, l2, s2, g1, g2, g3)
+        work = z(gpk.work_elems(gpk.OP_TRACE_KZZ, 1, 100, 2, 1))
+        return lambda: gpk.trace_kzz(Mm, Z, l2, s2, g1, g2, g3, work=work)
     if name == 'objective_dgp' or name.startswith('objective_dgp_mb'):
         # one objective+gradient evaluation of the 2-layer deep GP (N=20000, M=100); the
         # minibatch is 1000 points, or the size after 'objective_dgp_mb'
-        from . import aep_models as A
+        from geepee_gb300 import aep_models as A
         nb = 1000 if name == 'objective_dgp' else int(name[len('objective_dgp_mb'):])
         x, y = W.dgp_regression(seed=0)
         np.random.seed(1)

@@ -62,7 +62,12 @@ _SIGS = {
     'gpk_triu_pack': [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp],
     'gpk_hyp_grads': [_c_int, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
     'gpk_aep_phi': [_c_int, _c_int, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _vp, _vp],
+    'gpk_work_elems': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp],
+    'gpk_cavity_forms': [_c_int, _vp, _vp],
 }
+# the fixed-order variants: the atomic form's arguments, then (work, work_elems) before the stream
+for _n in ('gpk_psi_bwd_ex', 'gpk_det_bwd', 'gpk_gram', 'gpk_trace_kzz'):
+    _SIGS[(_n[:-3] if _n.endswith('_ex') else _n) + '_ws'] = _SIGS[_n][:-1] + [_vp, ctypes.c_long, _vp]
 
 _lib = None
 

@@ -921,29 +921,40 @@ class SGPLVM(_PackedModel):
 # lik_layers.py:474-627)
 # ------------------------------------------------------------------------------------------
 class SGPSSM(_PackedModel):
-    """GP state-space model with AEP: GP transition (moment matching), linear-Gaussian emission."""
+    """GP state-space model with AEP (aep_models.py:990-1437): GP transition (moment matching),
+    and a linear-Gaussian emission or, with gp_emi, a sparse-GP emission layer with a Gaussian
+    likelihood; optional control inputs x_control [N, Dc] enter the transition's inputs (and
+    the emission's, with control_to_emi) with zero variance."""
 
     def __init__(self, y_train, hidden_size, no_pseudo, lik='Gaussian', prior_mean=0, prior_var=1,
                  x_control=None, gp_emi=False, control_to_emi=True, nat_param=True):
         super().__init__(y_train)
-        if gp_emi or x_control is not None:
-            raise NotImplementedError('GP emission / control inputs are not implemented on the device path')
         if lik.lower() != 'gaussian':
             raise NotImplementedError('likelihood not implemented')
         self.N, self.Dout = y_train.shape
         self.Din = hidden_size
         self.M = no_pseudo
-        self.gp_emi = False
+        self.gp_emi = gp_emi
+        self.x_control = None if x_control is None else np.asarray(x_control, dtype=float)
+        self.Dcon_dyn = 0 if x_control is None else self.x_control.shape[1]
+        self.Dcon_emi = self.Dcon_dyn if control_to_emi else 0
         self.prior_mean, self.prior_var = prior_mean, prior_var
         self.x_prior_1, self.x_prior_2 = prior_mean / prior_var, 1.0 / prior_var
         Dx, Dy, N = self.Din, self.Dout, self.N
-        spec = (DevLayer.spec(Dx, Dx, self.M, '_dynamic') +
-                [('sn', (1,)), ('x_factor_1', (N, Dx)), ('x_factor_2', (N, Dx)),
-                 ('C_emission', (Dy, Dx)), ('R_emission', (Dy,))])
+        Dcd, Dce = self.Dcon_dyn, self.Dcon_emi
+        spec = (DevLayer.spec(Dx + Dcd, Dx, self.M, '_dynamic') +
+                [('sn', (1,)), ('x_factor_1', (N, Dx)), ('x_factor_2', (N, Dx))])
+        if gp_emi:
+            spec += DevLayer.spec(Dx + Dce, Dy, self.M, '_emission') + [('sn_emission', (1,))]
+        else:
+            spec += [('C_emission', (Dy, Dx + Dce)), ('R_emission', (Dy,))]
         self._make_packs(spec)
-        self.dyn_layer = DevLayer(N - 1, Dx, Dx, self.M, True, self.dev, self.ppack.views, self.gpack.views,
+        self.dyn_layer = DevLayer(N - 1, Dx + Dcd, Dx, self.M, True, self.dev, self.ppack.views, self.gpack.views,
                                   '_dynamic')
+        self.emi_layer = (DevLayer(N, Dx + Dce, Dy, self.M, True, self.dev, self.ppack.views, self.gpack.views,
+                                   '_emission') if gp_emi else None)
         self.y_dev = _to_dev(y_train, self.dev)
+        self.u_dev = None if x_control is None else _to_dev(self.x_control, self.dev)
         w1 = np.full((N, 1), 3.0)
         w1[0] = w1[-1] = 2.0
         first = np.zeros((N, 1))
@@ -991,7 +1002,7 @@ class SGPSSM(_PackedModel):
         nd, ne = dyn.shape[0], emi.shape[0]
         s_dyn = -(N - 1) / nd / alpha
         s_emi = -N / ne / alpha
-        st = setup_layers([lay], alpha)
+        st = setup_layers([lay] + ([self.emi_layer] if self.gp_emi else []), alpha)
         px1, px2 = self.x_prior_1, self.x_prior_2
         c = self._consts
         post1 = c['w1'] * f1 + px1 * c['first']
@@ -1002,6 +1013,12 @@ class SGPSSM(_PackedModel):
         mt, vt = cm.index_select(0, dyn + 1), cv.index_select(0, dyn + 1)
         mtm1, vtm1 = cm.index_select(0, dyn).contiguous(), cv.index_select(0, dyn).contiguous()
         mup, vup = cm.index_select(0, emi), cv.index_select(0, emi)
+        if self.Dcon_dyn:    # control inputs: known, zero variance (aep_models.py:1069-1082)
+            u = self.u_dev.index_select(0, dyn)
+            mtm1, vtm1 = torch.cat((mtm1, u), 1).contiguous(), torch.cat((vtm1, torch.zeros_like(u)), 1).contiguous()
+        if self.Dcon_emi:
+            u = self.u_dev.index_select(0, emi)
+            mup, vup = torch.cat((mup, u), 1).contiguous(), torch.cat((vup, torch.zeros_like(u)), 1).contiguous()
         mprop, vprop = lay.fwd_mm(mtm1, vtm1)
         sn = v['sn']
         sn2 = torch.exp(2 * sn)
@@ -1014,10 +1031,24 @@ class SGPSSM(_PackedModel):
         dmt = s_dyn * (-md / vsum)
         self.g_sn.copy_(dvt.sum() * 2 * sn2 / alpha + s_dyn * nd * Dx * (1 - alpha))
         gmx, gvx = lay.bwd_mm(alpha, mprop, (-dmt).contiguous(), dvt.contiguous(), mtm1, vtm1)
+        gmx, gvx = gmx[:, :Dx], gvx[:, :Dx]
         yb = self.y_dev.index_select(0, emi)
-        logZ_emi, emx, evx, dC, dR = self._emission(mup, vup, yb, alpha, s_emi)
-        self.gpack.views['C_emission'].copy_(dC)
-        self.gpack.views['R_emission'].copy_(dR)
+        if self.gp_emi:
+            # the emission factors through the emission layer and the Gaussian likelihood
+            # (aep_models.py:1100-1112)
+            el = self.emi_layer
+            sn_e = v['sn_emission']
+            mout, vout = el.fwd_mm(mup, vup)
+            lz, dme, dve = gauss_logZ(mout, vout, yb, sn_e, alpha)
+            logZ_emi = s_emi * lz.sum()
+            emx, evx = el.bwd_mm(alpha, mout, (s_emi * dme).contiguous(), (s_emi * dve).contiguous(), mup, vup)
+            emx, evx = emx[:, :Dx], evx[:, :Dx]
+            self.gpack.views['sn_emission'].copy_(gauss_dsn(dve, ne, self.Dout, sn_e, alpha, s_emi).reshape(1))
+        else:
+            logZ_emi, emx, evx, dC, dR = self._emission(mup, vup, yb, alpha, s_emi)
+            emx, evx = emx[:, :Dx], evx[:, :Dx]
+            self.gpack.views['C_emission'].copy_(dC)
+            self.gpack.views['R_emission'].copy_(dR)
         # gradients w.r.t. the x factors (aep_models.py:1208-1315)
         # per-time-step weights (aep_models.py:1221-1223, 1277-1279, 1301-1303)
         nb2 = c['w1'] - 1.0                          # 2 inside, 1 at the ends: neighbouring factors
@@ -1048,11 +1079,13 @@ class SGPSSM(_PackedModel):
         phi_post_x = (sp * 0.5 * (post1 ** 2 / post2 - torch.log(post2))).sum()
         phi_cav_x = (sc * 0.5 * (cav1 ** 2 / cav2 - torch.log(cav2))).sum()
         energy = logZ_dyn + logZ_emi + phi_prior_x + phi_post_x + phi_cav_x + lay.phi(alpha)
+        if self.gp_emi:
+            energy = energy + self.emi_layer.phi(alpha)
         self.energy.copy_(energy.reshape(1) / N)
         for k, g in self.gpack.views.items():
             if not k.startswith('__'):
                 g.div_(N)
-        self._flag_info(st + [self._emi_info])
+        self._flag_info(st + ([] if self.gp_emi else [self._emi_info]))
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
@@ -1079,9 +1112,32 @@ class SGPSSM(_PackedModel):
         m, v, _, _ = self.dyn_layer.fwd_det(_to_dev(inputs, self.dev), cav=False)
         return m.cpu().numpy(), v.cpu().numpy()
 
+    def _emi_ready(self):
+        if self.gp_emi and not getattr(self, '_emi_updated', False):
+            self.emi_layer.setup_posterior()
+            self.emi_layer.setup_predict()
+            self._emi_updated = True
+
+    def update_hypers(self, params):
+        super().update_hypers(params)
+        self._emi_updated = False
+
+    def _gp_emission(self, mx, vx):
+        """The GP emission's predictive through its posterior (base_models.py:1132-1158 with the
+        Gaussian likelihood's output_probabilistic, lik_layers.py:238-249): (mf, vf, vy) numpy."""
+        self._emi_ready()
+        mf, vf = self.emi_layer.fwd_mm(_to_dev(mx, self.dev), _to_dev(vx, self.dev), cav=False)
+        mf, vf = mf.cpu().numpy(), vf.cpu().numpy()
+        return mf, vf, vf + float(np.exp(2.0 * self.ppack.views['sn_emission'].item()))
+
     def predict_y(self, inputs):
-        """base_models.py:1544-1560 with Gauss_Emis.output_probabilistic (lik_layers.py:558-571)."""
+        """base_models.py:1544-1560: the transition's predictive, then the emission's -
+        Gauss_Emis.output_probabilistic (lik_layers.py:558-571) or the GP emission layer with the
+        Gaussian likelihood."""
         mf, vf = self.predict_f(inputs)
+        if self.gp_emi:
+            my, _, vy = self._gp_emission(mf, vf)
+            return my, vy
         p = self.get_hypers()
         C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
         my = mf @ C.T
@@ -1110,10 +1166,8 @@ class SGPSSM(_PackedModel):
         reading the previous step's moments) - then the linear-Gaussian emission
         (lik_layers.py:558-571).  Returns mx, vx [T, Dx] and my, vy_noiseless, vy [T, Dy] (the
         emission covariances' diagonals, as the reference returns them)."""
-        if x_control is not None:
-            raise NotImplementedError('control inputs are not implemented on the device path')
         if prop_mode == PROP_MC:
-            return self._predict_forward_mc(T, no_samples)
+            return self._predict_forward_mc(T, no_samples, x_control)
         if prop_mode != PROP_MM:
             raise NotImplementedError('unknown prop mode %s' % prop_mode)
         lay = self.dyn_layer
@@ -1123,20 +1177,47 @@ class SGPSSM(_PackedModel):
             self.updated = True
         pm, pv = self.get_posterior_x()
         m0, v0 = _to_dev(pm[-1], self.dev), _to_dev(pv[-1], self.dev)
-        mx, vx = gpk.psi_rollout(m0, v0, lay.zu, lay.lls2, lay.lsf2, lay.A, lay.B_sto, T)
+        if self.Dcon_dyn:
+            # each step's inputs are [x_{t-1}, u_t] (base_models.py:1474-1477): one launch a step
+            u = _to_dev(np.asarray(x_control, dtype=float)[:T], self.dev)
+            mx = torch.empty((T, self.Din), dtype=F64, device=self.dev)
+            vx = torch.empty_like(mx)
+            m, v = m0.reshape(1, -1), v0.reshape(1, -1)
+            for t in range(T):
+                mc = torch.cat((m, u[t:t + 1]), 1).contiguous()
+                vc = torch.cat((v, torch.zeros_like(u[t:t + 1])), 1).contiguous()
+                m, v = lay.fwd_mm(mc, vc, cav=False)
+                mx[t], vx[t] = m[0], v[0]
+        else:
+            mx, vx = gpk.psi_rollout(m0, v0, lay.zu, lay.lls2, lay.lsf2, lay.A, lay.B_sto, T)
         mxh, vxh = mx.cpu().numpy(), vx.cpu().numpy()
+        if self.gp_emi:
+            mc, vc = mxh, vxh
+            if self.Dcon_emi:
+                u = np.asarray(x_control, dtype=float)[:T]
+                mc, vc = np.hstack((mxh, u)), np.hstack((vxh, np.zeros_like(u)))
+            my, vyn, vy = self._gp_emission(mc, vc)
+            return mxh, vxh, my, vyn, vy
+        if self.Dcon_emi:
+            # the reference's linear emission takes x_t alone here while its C has the control
+            # columns too (base_models.py:1484-1485), which numpy rejects; so does this
+            raise ValueError('the linear emission with control inputs has no forecast (C is [Dy, Dx + Dc])')
         p = self.get_hypers()
         C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
         my = mxh @ C.T
         vyn = np.einsum('ab,nb,ab->na', C, vxh, C)
         return mxh, vxh, my, vyn, vyn + R
 
-    def _predict_forward_mc(self, T, no_samples):
+    def _predict_forward_mc(self, T, no_samples, x_control=None):
         """Base_SGPSSM.predict_forward_mc (base_models.py:1504-1542): no_samples draws of the last
         latent state, then T steps of sampling from the transition GP's posterior predictive
         (gpk_det_fwd per step, the whole loop on the device); the draws are taken from numpy's
         global RNG up front, in the reference's order.  Returns x [T, S, Dx] and the emission's
         my [T, S, Dy] and noise variances vy [T, S, Dy] (lik_layers.py:558-571 with vf = 0)."""
+        if self.Dcon_emi:
+            # the reference's sampled forecast misplaces a parenthesis in the emission's control
+            # tiling (base_models.py:1528-1529) and fails there; so does this
+            raise ValueError('the sampled forecast with control inputs to the emission fails in the reference')
         lay = self.dyn_layer
         if not self.updated:
             lay.setup_posterior()
@@ -1147,10 +1228,19 @@ class SGPSSM(_PackedModel):
         eps = _to_dev(np.random.randn((T + 1) * no_samples * Dx).reshape(T + 1, no_samples, Dx), self.dev)
         xs = (eps[0] * _to_dev(np.sqrt(pv[[-1]]), self.dev) + _to_dev(pm[[-1]], self.dev)).contiguous()
         x = torch.empty((T, no_samples, Dx), dtype=F64, device=self.dev)
+        u = None if not self.Dcon_dyn else _to_dev(np.asarray(x_control, dtype=float)[:T], self.dev)
         for t in range(T):
-            mt, vt, _, _ = lay.fwd_det(xs, cav=False)
+            xin = xs if u is None else torch.cat((xs, u[t:t + 1].expand(no_samples, -1)), 1).contiguous()
+            mt, vt, _, _ = lay.fwd_det(xin, cav=False)
             xs = torch.addcmul(mt, eps[t + 1], vt.sqrt())
             x[t] = xs
+        if self.gp_emi:
+            self._emi_ready()
+            xh = x.cpu().numpy()
+            mf, vf, _, _ = self.emi_layer.fwd_det(x.reshape(T * no_samples, Dx).contiguous(), cav=False)
+            sn2 = float(np.exp(2.0 * self.ppack.views['sn_emission'].item()))
+            return (xh, mf.reshape(T, no_samples, -1).cpu().numpy(),
+                    (vf + sn2).reshape(T, no_samples, -1).cpu().numpy())
         p = self.get_hypers()
         C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
         xh = x.cpu().numpy()
@@ -1160,6 +1250,10 @@ class SGPSSM(_PackedModel):
         """Base_SGPSSM.get_posterior_y (base_models.py:1578-1595), linear-Gaussian emission:
         my, the noiseless and the noisy variances [T, Dy] (diagonals)."""
         pm, pv = self.get_posterior_x()
+        if self.Dcon_emi:
+            pm, pv = np.hstack((pm, self.x_control)), np.hstack((pv, np.zeros_like(self.x_control)))
+        if self.gp_emi:
+            return self._gp_emission(pm, pv)
         p = self.get_hypers()
         C, R = np.asarray(p['C_emission']), np.exp(2 * np.asarray(p['R_emission']))
         vf = np.einsum('ab,nb,ab->na', C, pv, C)

@@ -352,6 +352,70 @@ __global__ void __launch_bounds__(1024) sum_scaled_kernel(int nD, const double* 
   }
 }
 
+// max |x| over n float64 values as the integer order of their magnitude bits (positive IEEE
+// doubles order as their bit patterns), on the integer pipe; the CTA's result in all threads
+__device__ long long maxabs_bits(const double* x, long n, long long* red) {
+  long long m = 0;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long b = __double_as_longlong(x[i]) & 0x7fffffffffffffffLL;
+    m = b > m ? b : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = v > m ? v : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  long long r = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = red[w] > r ? red[w] : r;
+  __syncthreads();
+  return r;
+}
+
+struct FormsArgs {
+  int n, chunks;      // items; CTAs per (item, d)
+  gpk_forms_t it[GPK_FORMS_MAX];
+};
+
+// CTA (c, j): flattened (item, d) = c, element chunk j of that output's M x M block.  Every CTA
+// decides the regime itself (two max-abs scans), so no CTA waits for another.
+__global__ void __launch_bounds__(256) cavity_forms_kernel(FormsArgs f) {
+  __shared__ long long red[8];
+  int c = blockIdx.x / f.chunks;
+  const int j = blockIdx.x - c * f.chunks;
+  int k = 0;
+  while (k < f.n && c >= f.it[k].D) c -= f.it[k++].D;
+  if (k >= f.n) return;
+  const gpk_forms_t& g = f.it[k];
+  const int d = c, M = g.M;
+  const long MM = (long)M * M;
+  const double* T = g.T + d * MM;
+  const long long tb = maxabs_bits(T, MM, red), kb = maxabs_bits(g.Kinv, MM, red);
+  const double tmax = __longlong_as_double(tb), kmax = __longlong_as_double(kb);
+  const bool wc = g.beta * tmax <= kmax, wp = tmax <= kmax;
+  const double b = g.beta;
+  const double *t = g.t + (long)d * M, *Tmh = g.Tmh + (long)d * M, *Kmh = g.Kmh + (long)d * M;
+  const double *Tmu = g.Tmu + (long)d * M, *Kmu = g.Kmu + (long)d * M;
+  if (j == 0) {
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+      g.Ah[(long)d * M + i] = wc ? b * t[i] - b * Tmh[i] : Kmh[i];
+      g.A[(long)d * M + i] = wp ? t[i] - Tmu[i] : Kmu[i];
+    }
+    if (threadIdx.x == 0 && g.regime) g.regime[d] = (wc ? 1 : 0) | (wp ? 2 : 0);
+  }
+  const long e0 = MM * j / f.chunks, e1 = MM * (j + 1) / f.chunks;
+  const long o = d * MM;
+  for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int r = (int)(e / M), q = (int)(e - (long)r * M);
+    const double bd = wc ? b * b * g.Qh[o + e] - b * T[e] : g.KShK[o + e] - g.Kinv[e];
+    g.Bd[o + e] = bd;
+    g.Bp[o + e] = wp ? g.Qu[o + e] - T[e] : g.KSuK[o + e] - g.Kinv[e];
+    const double ar = wc ? b * t[r] - b * Tmh[r] : Kmh[r];
+    const double aq = wc ? b * t[q] - b * Tmh[q] : Kmh[q];
+    g.Bsto[o + e] = bd + ar * aq;
+  }
+}
+
 int grid_for(long n) {
   long g = (n + 255) / 256;
   long cap = 4L * gpk::sm_count();
@@ -361,6 +425,7 @@ int grid_for(long n) {
 }  // namespace
 
 extern "C" int gpk_lincomb(const gpk_lincomb_t* d, void* stream) {
+  GPK_NVTX("gpk_lincomb");
   long n = 0;
   if (const int rc = lincomb_check(d, &n)) return rc;
   if (n == 0) return GPK_OK;
@@ -370,6 +435,7 @@ extern "C" int gpk_lincomb(const gpk_lincomb_t* d, void* stream) {
 
 extern "C" int gpk_nat_prep(int D, int M, int Q, const double* eta1, const double* ls, const double* sf, double* R,
                             double* lls2, double* lsf2, void* stream) {
+  GPK_NVTX("gpk_nat_prep");
   GPK_REQUIRE(D >= 1 && M >= 1 && Q >= 1, "nat_prep: bad sizes");
   GPK_REQUIRE(eta1 && ls && sf && R && lls2 && lsf2, "nat_prep: null pointer");
   nat_prep_kernel<<<grid_for((long)D * M * M), 256, 0, gpk::as_stream(stream)>>>(D, M, Q, eta1, ls, sf, R, lls2,
@@ -379,6 +445,7 @@ extern "C" int gpk_nat_prep(int D, int M, int Q, const double* eta1, const doubl
 
 extern "C" int gpk_triu_pack(int D, int M, const double* dR, const double* R, double* out, int accumulate,
                              void* stream) {
+  GPK_NVTX("gpk_triu_pack");
   GPK_REQUIRE(D >= 1 && M >= 1, "triu_pack: bad sizes");
   GPK_REQUIRE(dR && R && out, "triu_pack: null pointer");
   triu_pack_kernel<<<grid_for((long)D * M * M), 256, 0, gpk::as_stream(stream)>>>(D, M, dR, R, out, accumulate);
@@ -387,6 +454,7 @@ extern "C" int gpk_triu_pack(int D, int M, const double* dR, const double* R, do
 
 extern "C" int gpk_hyp_grads(int Q, const double* ls, const double* sf, const double* dl, const double* dsf2,
                              const double* dv, int ndv, double* g_ls, double* g_sf, void* stream) {
+  GPK_NVTX("gpk_hyp_grads");
   GPK_REQUIRE(Q >= 1 && ndv >= 0, "hyp_grads: bad sizes");
   GPK_REQUIRE(ls && sf && dl && dsf2 && g_ls && g_sf && (dv || ndv == 0), "hyp_grads: null pointer");
   hyp_grads_kernel<<<1, 256, 0, gpk::as_stream(stream)>>>(Q, ls, sf, dl, dsf2, dv, ndv, g_ls, g_sf);
@@ -396,6 +464,7 @@ extern "C" int gpk_hyp_grads(int Q, const double* ls, const double* sf, const do
 extern "C" int gpk_aep_phi(int D, int M, double N, double alpha, const double* logdetK, const double* ldSuinv,
                            const double* ldShinv, const double* mu, const double* mh, const double* th2, double w,
                            double* out, void* stream) {
+  GPK_NVTX("gpk_aep_phi");
   GPK_REQUIRE(D >= 1 && M >= 1 && N > 0 && alpha > 0, "aep_phi: bad sizes");
   GPK_REQUIRE(logdetK && ldSuinv && ldShinv && mu && mh && th2 && out, "aep_phi: null pointer");
   aep_phi_kernel<<<1, 256, 0, gpk::as_stream(stream)>>>(D, M, N, alpha, logdetK, ldSuinv, ldShinv, mu, mh, th2, w,
@@ -406,6 +475,7 @@ extern "C" int gpk_aep_phi(int D, int M, double N, double alpha, const double* l
 extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, const double* y, const double* sn,
                              double alpha, double scale, double invN, double* dm, double* dv, double* energy,
                              double* g_sn, int part, void* stream) {
+  GPK_NVTX("gpk_gauss_lik");
   GPK_REQUIRE(n >= 0 && D >= 1 && alpha > 0 && scale != 0.0 && part >= 0 && part <= 2, "gauss_lik: bad sizes");
   GPK_REQUIRE(m && v && y && sn && dm && dv && energy && g_sn, "gauss_lik: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
@@ -418,6 +488,7 @@ extern "C" int gpk_gauss_lik(int n, int D, const double* m, const double* v, con
 extern "C" int gpk_probit_lik(int S, int n, int D, int mc, const double* m, const double* v, const double* y,
                               double alpha, int T, const double* gh_x, const double* gh_w, double scale,
                               double invN, double* dm, double* dv, double* work, double* out, void* stream) {
+  GPK_NVTX("gpk_probit_lik");
   GPK_REQUIRE(n >= 0 && D >= 1 && S >= 1 && S <= 16 && (mc || S == 1) && alpha > 0 && scale != 0.0,
               "probit_lik: bad sizes");
   GPK_REQUIRE(alpha == 1.0 || (T >= 1 && T <= 16 && gh_x && gh_w), "probit_lik: need 1..16 Gauss-Hermite nodes");
@@ -434,6 +505,7 @@ extern "C" int gpk_probit_lik(int S, int n, int D, int mc, const double* m, cons
 extern "C" int gpk_lik_exp(int kind, int S, int n, int D, const double* m, const double* v, const double* y,
                            const double* sn, int T, const double* gh_x, const double* gh_w, double scale, double invN,
                            double* dm, double* dv, double* work, double* out, double* g_sn, void* stream) {
+  GPK_NVTX("gpk_lik_exp");
   GPK_REQUIRE((kind == 0 || kind == 1) && S >= 1 && n >= 0 && D >= 1 && scale != 0.0, "lik_exp: bad sizes");
   GPK_REQUIRE(kind == 0 || (T >= 1 && T <= 16 && gh_x && gh_w), "lik_exp: need 1..16 Gauss-Hermite nodes");
   const long nD = (long)n * D, nSD = nD * S;
@@ -488,6 +560,7 @@ __global__ void __launch_bounds__(256) finish_kernel(int span, double* g, double
 
 extern "C" int gpk_gather_rows(int n, long long rows, const long long* idx, int c0, const double* s0, double* d0,
                                int c1, const double* s1, double* d1, void* stream) {
+  GPK_NVTX("gpk_gather_rows");
   GPK_REQUIRE(n >= 0 && rows >= 0 && c0 >= 1 && c1 >= 0, "gather_rows: bad sizes n=%d c0=%d c1=%d", n, c0, c1);
   GPK_REQUIRE(idx && s0 && d0 && (c1 == 0 || (s1 && d1)), "gather_rows: null pointer");
   if (n == 0) return GPK_OK;
@@ -499,10 +572,37 @@ extern "C" int gpk_gather_rows(int n, long long rows, const long long* idx, int 
 
 extern "C" int gpk_finish(int span, double* g, double divisor, int ninfo, const int* info, double* worst,
                           void* stream) {
+  GPK_NVTX("gpk_finish");
   GPK_REQUIRE(span >= 0 && ninfo >= 0 && divisor != 0.0, "finish: bad sizes span=%d ninfo=%d", span, ninfo);
   GPK_REQUIRE((span == 0 || g) && (ninfo == 0 || (info && worst)), "finish: null pointer");
   const int grid = std::max(1, std::min((span + 255) / 256, gpk::sm_count()));
   finish_kernel<<<grid, 256, 0, gpk::as_stream(stream)>>>(span, g, divisor, ninfo, ninfo ? info : nullptr,
                                                           ninfo ? worst : nullptr);
   return gpk::check_launch("finish");
+}
+
+extern "C" int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream) {
+  GPK_NVTX("gpk_cavity_forms");
+  GPK_REQUIRE(n >= 0 && n <= GPK_FORMS_MAX && (n == 0 || items), "cavity_forms: %d items (max %d)", n, GPK_FORMS_MAX);
+  FormsArgs f{};
+  f.n = n;
+  int total = 0;
+  long MM = 0;
+  for (int i = 0; i < n; ++i) {
+    const gpk_forms_t& g = items[i];
+    GPK_REQUIRE(g.D >= 1 && g.M >= 1, "cavity_forms: item %d: bad sizes D=%d M=%d", i, g.D, g.M);
+    GPK_REQUIRE(g.T && g.Kinv && g.t && g.Qh && g.KShK && g.Qu && g.KSuK && g.Tmh && g.Kmh && g.Tmu && g.Kmu &&
+                    g.Bd && g.Bp && g.Bsto && g.Ah && g.A,
+                "cavity_forms: item %d: null pointer", i);
+    f.it[i] = g;
+    total += g.D;
+    MM = (long)g.M * g.M > MM ? (long)g.M * g.M : MM;
+  }
+  if (total == 0) return GPK_OK;
+  // about two waves of 256-thread CTAs over the largest block
+  long ch = (MM + 2047) / 2048;
+  const long cap = (2L * gpk::sm_count() + total - 1) / total;
+  f.chunks = (int)(ch < 1 ? 1 : (ch > cap ? cap : ch));
+  cavity_forms_kernel<<<total * f.chunks, 256, 0, gpk::as_stream(stream)>>>(f);
+  return gpk::check_launch("cavity_forms");
 }

@@ -4,6 +4,8 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gpk.h"
 #include "df64.cuh"
 
@@ -33,7 +35,58 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
+// Fixed-order accumulation.  A kernel of the deterministic path writes its per-CTA partial sums
+// to a workspace, part[c * stride + j] for CTA c, instead of adding them into the outputs with
+// atomics; reduce_partials then adds sum_c part[c * stride + j] (in the order c = 0, 1, ...,
+// compensated) into segment j's destination.  Each destination element has exactly one writer,
+// so repeated runs on the same inputs give bit-identical sums.
+constexpr int RED_SEGS = 6;
+struct RedSeg {
+  double* dst;   // null: the segment is skipped
+  int len;
+  int kind;      // 0: dst[j] += s;  1: len = D M(M+1)/2 packed pairs (a >= b) of D M x M
+                 //    matrices, added at (a, b) and, off the diagonal, at (b, a)
+  int M;
+};
+struct RedPlan {
+  int nseg;
+  RedSeg seg[RED_SEGS];
+  long stride() const {
+    long s = 0;
+    for (int i = 0; i < nseg; ++i) s += seg[i].len;
+    return s;
+  }
+  void add(double* dst, int len, int kind = 0, int M = 0) { seg[nseg++] = RedSeg{dst, len, kind, M}; }
+};
+// adds the nparts partial blocks of `part` (stride plan.stride()) into the plan's destinations
+int reduce_partials(const double* part, int nparts, const RedPlan& plan, cudaStream_t st);
+
+// An NVTX range named after the C-ABI entry point, open for the call's host-side duration
+// (argument checks and launches); nvtx3 is header-only and costs a pointer test when no tool
+// is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 }  // namespace gpk
+
+#define GPK_NVTX(name) gpk::NvtxRange gpk_nvtx_range_(name)
+
+// workspace (float64 elements) of the fixed-order path of each accumulating entry point
+long psi_bwd_work_elems(int M, int Q, int Dout);
+long det_bwd_work_elems(int N, int M, int D, int Dout);
+long gram_work_elems(int N, int M, int Dout);
+long trace_kzz_work_elems(int M, int Q);
+
+// Pair p of the row-major lower triangle, p = a (a + 1) / 2 + b with 0 <= b <= a.
+__host__ __device__ __forceinline__ void tri_pair(int p, int& a, int& b) {
+  int r = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
+  if ((r + 1) * (r + 2) / 2 <= p) ++r;
+  if (r * (r + 1) / 2 > p) --r;
+  a = r;
+  b = p - r * (r + 1) / 2;
+}
 
 #define GPK_REQUIRE(cond, ...) \
   do {                          \

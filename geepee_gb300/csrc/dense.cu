@@ -2,7 +2,6 @@
 //   gpk_gemm      batched C = alpha op(A) op(B) + beta C
 //   gpk_chol_inv  batched SPD Cholesky + inverse + log-determinant (M <= 128, one CTA each)
 //   gpk_trace_kzz gradient of tr(M Kzz) w.r.t. log sf^2, log ell^2 and Z
-#include <mutex>
 
 #include "common.cuh"
 
@@ -604,91 +603,93 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(int M, const typename Nu
 //   d/dlog sf2 = sum_ab Mm_ab K_ab;  d/dlog l_q = 1/2 sum_ab Mm_ab K_ab (z_aq-z_bq)^2 / l_q
 //   d/dz_aq = sum_b (Mm_ab + Mm_ba) K_ab (z_bq - z_aq) / l_q
 // (geepee/kernels.py:447-475).  Results are ADDED, scaled: g_sf += s_sf * ., g_ls += s_ls * ., g_z += .
-constexpr int TKW = 4;    // warps per trace_kzz CTA
+// One CTA per pseudo-input a, a thread per b (b = threadIdx.x + k blockDim.x); the CTA sums its
+// threads' d/dz_a in a fixed order and adds it into g_z[a] (one writer per element).  The sums
+// over (a, b) of the log sf2 and log l terms leave each CTA as a partial (into
+// part[a * (1 + Q)], fixed-order path) or by atomics.
+constexpr int TK_MAXW = 8;   // warps per CTA
 template <typename T, int QC>
-__global__ void __launch_bounds__(TKW * 32) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
-                                                             const typename Num<T>::store_t* Z, const double* lls2,
-                                                             const double* lsf2, double s_sf, double s_ls,
-                                                             double* g_sf, double* g_ls, double* g_z) {
-  // one warp per (pseudo-input a, block of 32 b), one b per lane; Z staged in shared memory
+__global__ void __launch_bounds__(TK_MAXW * 32) trace_kzz_kernel(int M, int Q, const typename Num<T>::store_t* Mm,
+                                                                 const typename Num<T>::store_t* Z,
+                                                                 const double* lls2, const double* lsf2, double s_sf,
+                                                                 double s_ls, double* g_sf, double* g_ls, double* g_z,
+                                                                 double* part) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   T* zs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M*Q]
   __shared__ T il[QC], lsf;
-  __shared__ T red[TKW][1 + QC];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nb = (M + 31) >> 5, wid = blockIdx.x * TKW + warp;
-  const int a = wid / nb, b = (wid - a * nb) * 32 + lane;
-  // this lane's M_ab and M_ba are loaded before the staging below
+  __shared__ T red[TK_MAXW][1 + 2 * QC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int a = blockIdx.x;
+  // this thread's first M_ab and M_ba are loaded before the staging below
   S mab = S(0), mba = S(0);
-  if (a < M && b < M) {
-    mab = Mm[(size_t)a * M + b];
-    mba = Mm[(size_t)b * M + a];
+  if (threadIdx.x < M) {
+    mab = Mm[(size_t)a * M + threadIdx.x];
+    mba = Mm[(size_t)threadIdx.x * M + a];
   }
   load_exp_table(tab);
-  for (int i = threadIdx.x; i < M * Q; i += TKW * 32) zs[i] = Num<T>::ld(Z[i]);
+  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) zs[i] = Num<T>::ld(Z[i]);
   __syncthreads();
   if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
-  if (threadIdx.x == 32) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));
+  if (threadIdx.x == 31) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));   // Q <= 8: thread 31 is free
   __syncthreads();
-  T gs = Num<T>::zero();
-  T gl[QC], gz[QC];
+  T v[1 + 2 * QC];   // gs, gl[QC], gz[QC]
 #pragma unroll
-  for (int q = 0; q < QC; ++q) gl[q] = gz[q] = Num<T>::zero();
-  if (a < M) {
-    if (b < M) {
-      T r = Num<T>::zero();
-      T d[QC];
-#pragma unroll
-      for (int q = 0; q < QC; ++q) {
-        d[q] = q < Q ? sub(zs[b * Q + q], zs[a * Q + q]) : Num<T>::zero();   // z_b - z_a
-        if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
-      }
-      const T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
-      const T m1 = Num<T>::ld(mab);
-      const T w = mul(m1, k);
-      const T ws = mul(add(m1, Num<T>::ld(mba)), k);
-      gs = w;
-#pragma unroll
-      for (int q = 0; q < QC; ++q) {
-        if (q < Q) {
-          const T dil = mul(d[q], il[q]);
-          gl[q] = mul(mul(w, d[q]), dil);
-          gz[q] = mul(ws, dil);
-        }
-      }
+  for (int i = 0; i < 1 + 2 * QC; ++i) v[i] = Num<T>::zero();
+  for (int b = threadIdx.x; b < M; b += blockDim.x) {
+    if (b != (int)threadIdx.x) {
+      mab = Mm[(size_t)a * M + b];
+      mba = Mm[(size_t)b * M + a];
     }
+    T r = Num<T>::zero();
+    T d[QC];
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      d[q] = q < Q ? sub(zs[b * Q + q], zs[a * Q + q]) : Num<T>::zero();   // z_b - z_a
+      if (q < Q) r = fma_(mul(d[q], d[q]), il[q], r);
+    }
+    const T k = exp_tab(sub(lsf, scale2(r, -1)), tab);
+    const T m1 = Num<T>::ld(mab);
+    const T w = mul(m1, k);
+    const T ws = mul(add(m1, Num<T>::ld(mba)), k);
+    v[0] = add(v[0], w);
 #pragma unroll
     for (int q = 0; q < QC; ++q) {
       if (q < Q) {
-        T v = warp_sum(gz[q]);
-        if (lane == 0) atomicAdd(&g_z[a * Q + q], (double)Num<T>::st(v));
+        const T dil = mul(d[q], il[q]);
+        v[1 + q] = fma_(mul(w, d[q]), dil, v[1 + q]);
+        v[1 + QC + q] = fma_(ws, dil, v[1 + QC + q]);
       }
     }
   }
-  // reduce gs and gl over the CTA
-  T v[1 + QC];
-  v[0] = gs;
 #pragma unroll
-  for (int q = 0; q < QC; ++q) v[1 + q] = gl[q];
-#pragma unroll
-  for (int i = 0; i < 1 + QC; ++i) {
-    T t = warp_sum(v[i]);
+  for (int i = 0; i < 1 + 2 * QC; ++i) {
+    const T t = warp_sum(v[i]);
     if (lane == 0) red[warp][i] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int i = 0; i < 1 + QC; ++i) {
+    for (int i = 0; i < 1 + 2 * QC; ++i) {
       T t = red[0][i];
-      for (int w = 1; w < TKW; ++w) t = add(t, red[w][i]);
+      for (int w = 1; w < nw; ++w) t = add(t, red[w][i]);
       v[i] = t;
     }
-    atomicAdd(g_sf, s_sf * (double)Num<T>::st(v[0]));
 #pragma unroll
     for (int q = 0; q < QC; ++q)
-      if (q < Q) atomicAdd(&g_ls[q], s_ls * 0.5 * (double)Num<T>::st(v[1 + q]));
+      if (q < Q) g_z[a * Q + q] += (double)Num<T>::st(v[1 + QC + q]);
+    const double vsf = s_sf * (double)Num<T>::st(v[0]);
+    if (part) part[(size_t)a * (1 + Q)] = vsf;
+    else atomicAdd(g_sf, vsf);
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      if (q < Q) {
+        const double vl = s_ls * 0.5 * (double)Num<T>::st(v[1 + q]);
+        if (part) part[(size_t)a * (1 + Q) + 1 + q] = vl;
+        else atomicAdd(&g_ls[q], vl);
+      }
+    }
   }
 }
 
@@ -843,6 +844,7 @@ int gemm_group_launch(int count, const gpk_gemm_t* pr, int nlc, const gpk_lincom
 extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
                         const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
                         void* C, int ldc, long strideC, void* stream) {
+  GPK_NVTX("gpk_gemm");
   GPK_REQUIRE(batch >= 0 && m >= 0 && n >= 0 && k >= 0, "gemm: negative size");
   GPK_REQUIRE(batch <= 65535, "gemm: batch %d > 65535", batch);
   GPK_REQUIRE(C && (k == 0 || (A && B)), "gemm: null pointer");
@@ -861,6 +863,7 @@ extern "C" int gpk_gemm(int prec, int batch, int m, int n, int k, int transA, in
 extern "C" int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB, double alpha,
                            const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
                            const void* E, int lde, long strideE, void* C, int ldc, long strideC, void* stream) {
+  GPK_NVTX("gpk_gemm_ex");
   GPK_REQUIRE(batch >= 0 && m >= 0 && n >= 0 && k >= 0, "gemm_ex: negative size");
   GPK_REQUIRE(batch <= 65535, "gemm_ex: batch %d > 65535", batch);
   GPK_REQUIRE(C && (k == 0 || (A && B)) && (beta == 0.0 || E), "gemm_ex: null pointer");
@@ -892,11 +895,13 @@ static int gemm_group_check(int count, const gpk_gemm_t* problems) {
 }
 
 extern "C" int gpk_gemm_group(int prec, int count, const gpk_gemm_t* problems, void* stream) {
+  GPK_NVTX("gpk_gemm_group");
   return gpk_level(prec, count, problems, 0, nullptr, stream);
 }
 
 extern "C" int gpk_level(int prec, int ngemm, const gpk_gemm_t* gemms, int nlc, const gpk_lincomb_t* lcs,
                          void* stream) {
+  GPK_NVTX("gpk_level");
   if (const int rc = gemm_group_check(ngemm, gemms)) return rc;
   GPK_REQUIRE(nlc >= 0 && nlc <= GPK_LC_GROUP && (nlc == 0 || lcs), "level: %d linear combinations (max %d)", nlc,
               GPK_LC_GROUP);
@@ -968,6 +973,7 @@ int chol_launch(int batch, int M, const void* A, void* Ainv, void* L, double* lo
 
 extern "C" int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet,
                                int* info, void* work, void* stream) {
+  GPK_NVTX("gpk_chol_inv_ws");
   GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "chol_inv: M=%d outside [1,4096]", M);
   GPK_REQUIRE(A, "chol_inv: null input");
   GPK_REQUIRE(M <= 128 || work, "chol_inv: M=%d > 128 needs a workspace of batch*M*M elements", M);
@@ -985,12 +991,14 @@ extern "C" int gpk_chol_inv_ws(int prec, int batch, int M, const void* A, void* 
 
 extern "C" int gpk_chol_inv(int prec, int batch, int M, const void* A, void* Ainv, void* L, double* logdet, int* info,
                             void* stream) {
+  GPK_NVTX("gpk_chol_inv");
   GPK_REQUIRE(M <= 128, "chol_inv: M=%d > 128 needs gpk_chol_inv_ws", M);
   return gpk_chol_inv_ws(prec, batch, M, A, Ainv, L, logdet, info, nullptr, stream);
 }
 
 extern "C" int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
                            void* work, void* stream) {
+  GPK_NVTX("gpk_spd_inv");
   GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 4096, "spd_inv: M=%d outside [1,4096]", M);
   GPK_REQUIRE(A && Ainv && info && work, "spd_inv: null pointer");
   if (batch == 0) return GPK_OK;
@@ -1005,41 +1013,33 @@ extern "C" int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv
 }
 
 // ---- gpk_spd_inv_static: gpk_spd_inv with its workspace in a file-scope device array ----
-// Limit: M <= 128 and batch * M * M <= SPD_STATIC_ELEMS (e.g. 8 matrices of 128 x 128).
-// Nothing in the array needs to start at zero (every element a call reads was written
-// earlier in the same call).  There is one array per device: calls that overlap on the
+// Limit: M <= 128, batch <= 65535 and batch * M * M <= SPD_STATIC_ELEMS (e.g. 8 matrices of
+// 128 x 128).  Nothing in the array needs to start at zero (every element a call reads was
+// written earlier in the same call).  There is one array per device: calls that overlap on the
 // device (different streams or host threads) race on it.
 constexpr long SPD_STATIC_ELEMS = 8L * 128 * 128;
+static_assert(sizeof(df64) <= 8 && sizeof(float) <= 8, "the array holds 2 SPD_STATIC_ELEMS elements of <= 8 bytes");
 static __device__ __align__(256) unsigned char g_spd_scratch[2 * SPD_STATIC_ELEMS * 8];
 
 namespace {
-constexpr int SPD_MAX_DEVICES = 64;
-void* g_spd_scratch_addr[SPD_MAX_DEVICES];
-std::mutex g_spd_scratch_mu;
-
-// device address of g_spd_scratch on the current device, looked up once per device
+// Device address of g_spd_scratch on the current device, looked up on every call: the lookup
+// is cheap once the module is loaded, and a cached address would go stale when the device's
+// context is torn down and created again (cudaDeviceReset), which reloads the module.
 int spd_scratch(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return gpk::fail(GPK_ECUDA, "spd_inv_static: cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= SPD_MAX_DEVICES)
-    return gpk::fail(GPK_EUNSUPPORTED, "spd_inv_static: device %d >= %d", dev, SPD_MAX_DEVICES);
-  std::lock_guard<std::mutex> lock(g_spd_scratch_mu);
-  if (!g_spd_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_spd_scratch);
-    if (e != cudaSuccess || !p)
-      return gpk::fail(GPK_ECUDA, "spd_inv_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_spd_scratch_addr[dev] = p;
-  }
-  *out = g_spd_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_spd_scratch);
+  if (e != cudaSuccess || !p)
+    return gpk::fail(GPK_ECUDA, "spd_inv_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  *out = p;
   return GPK_OK;
 }
 }  // namespace
 
 extern "C" int gpk_spd_inv_static(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
                                   void* stream) {
-  GPK_REQUIRE(batch >= 0 && M >= 1 && M <= 128, "spd_inv_static: M=%d outside [1,128]", M);
+  GPK_NVTX("gpk_spd_inv_static");
+  GPK_REQUIRE(batch >= 0 && batch <= 65535 && M >= 1 && M <= 128,
+              "spd_inv_static: batch=%d outside [0,65535] or M=%d outside [1,128]", batch, M);
   GPK_REQUIRE((long)batch * M * M <= SPD_STATIC_ELEMS, "spd_inv_static: batch*M*M = %ld > %ld",
               (long)batch * M * M, SPD_STATIC_ELEMS);
   GPK_REQUIRE(A && Ainv && info, "spd_inv_static: null pointer");
@@ -1055,35 +1055,52 @@ extern "C" int gpk_spd_inv_static(int prec, int batch, int M, const void* A, voi
 
 template <typename T, int QC>
 int trace_launch(int M, int Q, const void* Mm, const void* Z, const double* lls2, const double* lsf2, double s_sf,
-                 double s_ls, double* g_sf, double* g_ls, double* g_z, cudaStream_t st) {
+                 double s_ls, double* g_sf, double* g_ls, double* g_z, double* work, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
   const size_t sm = 256 * sizeof(float2) + (size_t)M * Q * sizeof(T);
   auto k = trace_kzz_kernel<T, QC>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  const int warps = M * gpk::ceil_div(M, 32);   // (a, block of 32 b)
-  k<<<gpk::ceil_div(warps, TKW), TKW * 32, sm, st>>>(M, Q, (const S*)Mm, (const S*)Z, lls2, lsf2, s_sf, s_ls, g_sf,
-                                                     g_ls, g_z);
-  return gpk::check_launch("trace_kzz");
+  k<<<M, 32 * std::min(TK_MAXW, gpk::ceil_div(M, 32)), sm, st>>>(M, Q, (const S*)Mm, (const S*)Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls,
+                                             g_z, work);
+  int rc = gpk::check_launch("trace_kzz");
+  if (rc != GPK_OK || !work) return rc;
+  gpk::RedPlan plan{};
+  plan.add(g_sf, 1);
+  plan.add(g_ls, Q);
+  return gpk::reduce_partials(work, M, plan, st);
 }
+
+long trace_kzz_work_elems(int M, int Q) { return (long)M * (1 + Q); }
 
 extern "C" int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
                              const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
                              void* stream) {
+  GPK_NVTX("gpk_trace_kzz");
+  return gpk_trace_kzz_ws(prec, M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, nullptr, 0, stream);
+}
+
+extern "C" int gpk_trace_kzz_ws(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
+                                const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
+                                double* work, long work_elems, void* stream) {
+  GPK_NVTX("gpk_trace_kzz_ws");
   GPK_REQUIRE(M >= 1 && Q >= 1 && Q <= 8, "trace_kzz: bad sizes M=%d Q=%d", M, Q);
   GPK_REQUIRE((size_t)M * Q * 8 <= 200 * 1024, "trace_kzz: M*Q=%d too large", M * Q);
   GPK_REQUIRE(Mm && Z && lls2 && lsf2 && g_sf && g_ls && g_z, "trace_kzz: null pointer");
+  GPK_REQUIRE(!work || work_elems >= trace_kzz_work_elems(M, Q), "trace_kzz: workspace of %ld doubles, %ld needed",
+              work_elems, trace_kzz_work_elems(M, Q));
   cudaStream_t st = gpk::as_stream(stream);
   if (prec == GPK_DF64)
-    return Q <= 2 ? trace_launch<df64, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st)
-                  : trace_launch<df64, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st);
+    return Q <= 2 ? trace_launch<df64, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, work, st)
+                  : trace_launch<df64, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, work, st);
   if (prec == GPK_FP32)
-    return Q <= 2 ? trace_launch<float, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st)
-                  : trace_launch<float, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, st);
+    return Q <= 2 ? trace_launch<float, 2>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, work, st)
+                  : trace_launch<float, 8>(M, Q, Mm, Z, lls2, lsf2, s_sf, s_ls, g_sf, g_ls, g_z, work, st);
   return gpk::fail(GPK_EINVAL, "trace_kzz: unknown precision %d", prec);
 }
 
 extern "C" int gpk_small_spd(int prec, int batch, int n, const void* A, void* Ainv, double* logdet, int* info,
                              void* stream) {
+  GPK_NVTX("gpk_small_spd");
   GPK_REQUIRE(batch >= 0 && n >= 1 && n <= 8, "small_spd: n=%d outside [1,8]", n);
   GPK_REQUIRE(A, "small_spd: null input");
   if (batch == 0) return GPK_OK;

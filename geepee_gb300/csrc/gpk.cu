@@ -17,5 +17,83 @@ int sm_count() {
 }
 }  // namespace gpk
 
-extern "C" int gpk_version(void) { return 1; }
+extern "C" int gpk_version(void) {
+  GPK_NVTX("gpk_version"); return 1; }
 extern "C" const char* gpk_last_error(void) { return gpk::g_err; }
+
+namespace {
+
+// Neumaier's compensated addition: (s, c) += x
+__device__ __forceinline__ void comp_add(double& s, double& c, double x) {
+  const double t = s + x;
+  c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
+// Eight lanes per output element j: lane l sums the partials c = l, l + 8, ... in order, then
+// the eight lane sums combine over a fixed butterfly (both partners compute the same sum, as
+// IEEE addition commutes), and lane 0 adds the total into the element's destination.
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const double* part, int nparts, long stride,
+                                                              gpk::RedPlan plan) {
+  const long j = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 3;
+  const int l = threadIdx.x & 7;
+  double s = 0.0, c = 0.0;
+  if (j < stride)
+    for (int k = l; k < nparts; k += 8) comp_add(s, c, part[(size_t)k * stride + j]);
+#pragma unroll
+  for (int m = 1; m < 8; m <<= 1) {
+    const double so = __shfl_xor_sync(0xffffffffu, s, m), co = __shfl_xor_sync(0xffffffffu, c, m);
+    const double t = s + so;
+    const double e = fabs(s) >= fabs(so) ? (s - t) + so : (so - t) + s;
+    s = t;
+    c = (c + co) + e;   // commutative in (c, co): both partners get the same value
+  }
+  if (l != 0 || j >= stride) return;
+  const double v = s + c;
+  long off = 0;
+  for (int i = 0; i < plan.nseg; ++i) {
+    const gpk::RedSeg& g = plan.seg[i];
+    if (j < off + g.len) {
+      if (!g.dst) return;
+      const long jj = j - off;
+      if (g.kind == 0) {
+        g.dst[jj] += v;
+      } else {
+        const long P = (long)g.M * (g.M + 1) / 2;
+        const long d = jj / P;
+        int a, b;
+        tri_pair((int)(jj - d * P), a, b);
+        double* m = g.dst + (size_t)d * g.M * g.M;
+        m[(size_t)a * g.M + b] += v;
+        if (a != b) m[(size_t)b * g.M + a] += v;
+      }
+      return;
+    }
+    off += g.len;
+  }
+}
+
+}  // namespace
+
+namespace gpk {
+int reduce_partials(const double* part, int nparts, const RedPlan& plan, cudaStream_t st) {
+  const long stride = plan.stride();
+  if (stride == 0 || nparts <= 0) return GPK_OK;
+  const long threads = stride * 8;
+  reduce_partials_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(part, nparts, stride, plan);
+  return check_launch("reduce_partials");
+}
+}  // namespace gpk
+
+extern "C" int gpk_work_elems(int op, int N, int M, int D, int Dout, long* elems) {
+  GPK_NVTX("gpk_work_elems");
+  GPK_REQUIRE(elems, "work_elems: null output");
+  GPK_REQUIRE(N >= 0 && M >= 1 && D >= 1 && Dout >= 1, "work_elems: bad sizes N=%d M=%d D=%d Dout=%d", N, M, D, Dout);
+  switch (op) {
+    case GPK_OP_PSI_BWD: *elems = psi_bwd_work_elems(M, D, Dout); return GPK_OK;
+    case GPK_OP_DET_BWD: *elems = det_bwd_work_elems(N, M, D, Dout); return GPK_OK;
+    case GPK_OP_GRAM: *elems = gram_work_elems(N, M, Dout); return GPK_OK;
+    case GPK_OP_TRACE_KZZ: *elems = trace_kzz_work_elems(M, D); return GPK_OK;
+    default: return gpk::fail(GPK_EINVAL, "work_elems: unknown operation %d", op);
+  }
+}

@@ -213,7 +213,8 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
                                                       const typename Num<T>::store_t* dv,
                                                       const typename Num<T>::store_t* dkfu, double* dsf2,
                                                       double* dl, double* dZ, double* dA,
-                                                      typename Num<T>::store_t* dx) {
+                                                      typename Num<T>::store_t* dx, double* part,
+                                                      long part_stride) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
@@ -301,7 +302,9 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
     }
     __syncthreads();
   }
-  // per-b sums over the row groups -> one atomic per CTA and (b, q) / (d, b)
+  // per-b sums over the row groups -> one write per CTA and (b, q) / (d, b): into this CTA's
+  // partial block ([dZ M*D | dA Dout*M | dsf2 | dl D], fixed-order path) or atomically
+  double* const pblk = part ? part + (size_t)blockIdx.x * part_stride : nullptr;
   T* pb = red;   // [RG][blockDim.x][DC + DO_MAX]
   const int W = DC + DO_MAX;
 #pragma unroll
@@ -315,17 +318,18 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
       if (q < D) {
         T sacc = pb[b * W + q];
         for (int r = 1; r < RG; ++r) sacc = add(sacc, pb[(r * blockDim.x + b) * W + q]);
-        atomicAdd(&dZ[(size_t)b * D + q], (double)Num<T>::st(sacc));
+        if (pblk) pblk[(size_t)b * D + q] = (double)Num<T>::st(sacc);
+        else atomicAdd(&dZ[(size_t)b * D + q], (double)Num<T>::st(sacc));
       }
     }
-    if (dA && !dkfu) {
+    const bool wantA = dA && !dkfu;
 #pragma unroll
-      for (int d = 0; d < DO_MAX; ++d) {
-        if (d < Dout) {
-          T sacc = pb[b * W + DC + d];
-          for (int r = 1; r < RG; ++r) sacc = add(sacc, pb[(r * blockDim.x + b) * W + DC + d]);
-          atomicAdd(&dA[(size_t)d * M + b], (double)Num<T>::st(sacc));
-        }
+    for (int d = 0; d < DO_MAX; ++d) {
+      if (d < (dkfu ? 0 : Dout)) {
+        T sacc = pb[b * W + DC + d];
+        for (int r = 1; r < RG; ++r) sacc = add(sacc, pb[(r * blockDim.x + b) * W + DC + d]);
+        if (pblk) pblk[(size_t)M * D + (size_t)d * M + b] = wantA ? (double)Num<T>::st(sacc) : 0.0;
+        else if (wantA) atomicAdd(&dA[(size_t)d * M + b], (double)Num<T>::st(sacc));
       }
     }
   }
@@ -347,13 +351,18 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
 #pragma unroll
     for (int i = 0; i < 1 + DC; ++i) vals[i] = warp_sum((tid & 31) < nw ? rw[(tid & 31) * (1 + DC) + i] : Num<T>::zero());
     if (tid == 0) {
-      atomicAdd(dsf2, (double)Num<T>::st(div(vals[0], h->sf2)));
+      const size_t o = (size_t)M * D + (size_t)(dkfu ? 0 : Dout) * M;
+      const double vsf = (double)Num<T>::st(div(vals[0], h->sf2));
+      if (pblk) pblk[o] = vsf;
+      else atomicAdd(dsf2, vsf);
 #pragma unroll
       for (int q = 0; q < DC; ++q) {
         if (q < D) {
           // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
           const T il = h->inv_l2[q];
-          atomicAdd(&dl[q], (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il)))));
+          const double vl = (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il))));
+          if (pblk) pblk[o + 1 + q] = vl;
+          else atomicAdd(&dl[q], vl);
         }
       }
     }
@@ -368,7 +377,8 @@ constexpr int GB = 32;
 template <typename T>
 __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
                                                    const typename Num<T>::store_t* v,
-                                                   const typename Num<T>::store_t* w, double* C, int sym) {
+                                                   const typename Num<T>::store_t* w, double* C, int sym,
+                                                   double* part) {
   typedef typename Num<T>::store_t S;
   __shared__ T su[GB][32], sv[GB][32], sw[GB][DO_MAX];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows of threads, 4 outputs each
@@ -435,8 +445,14 @@ __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const
         int i = i0 + ty * 4 + r, j = j0 + tx;
         if (i < M && j < M) {
           const double val = (double)Num<T>::st(acc[d][r]);
-          atomicAdd(&C[((size_t)d * M + i) * M + j], val);
-          if (sym && bi != bj) atomicAdd(&C[((size_t)d * M + j) * M + i], val);
+          if (part) {   // fixed-order path: this row chunk's partial matrices, plain stores
+            double* pc = part + (size_t)blockIdx.z * Dout * M * M;
+            pc[((size_t)d * M + i) * M + j] = val;
+            if (sym && bi != bj) pc[((size_t)d * M + j) * M + i] = val;
+          } else {
+            atomicAdd(&C[((size_t)d * M + i) * M + j], val);
+            if (sym && bi != bj) atomicAdd(&C[((size_t)d * M + j) * M + i], val);
+          }
         }
       }
     }
@@ -510,6 +526,7 @@ int kern_launch(int N, int M, int D, const void* x, int ldx, const void* z, int 
 
 extern "C" int gpk_kern(int prec, int N, int M, int D, const void* x, int ldx, const void* z, int ldz,
                         const double* lls2, const double* lsf2, double jitter, void* K, int ldk, void* stream) {
+  GPK_NVTX("gpk_kern");
   GPK_REQUIRE(N >= 0 && M >= 0 && D >= 1 && D <= DMAXK, "kern: bad sizes N=%d M=%d D=%d", N, M, D);
   GPK_REQUIRE(x && z && lls2 && lsf2 && K, "kern: null pointer");
   GPK_REQUIRE(ldx >= D && ldz >= D && ldk >= M, "kern: bad leading dimension");
@@ -523,6 +540,7 @@ extern "C" int gpk_kern(int prec, int N, int M, int D, const void* x, int ldx, c
 extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
                            const double* lls2, const double* lsf2, const void* A, const void* B, void* kfu,
                            void* Bk, void* m_out, void* v_out, void* stream) {
+  GPK_NVTX("gpk_det_fwd");
   GPK_REQUIRE(N >= 0 && M >= 1 && M <= 1024 && D >= 1 && D <= DMAXK, "det_fwd: bad sizes N=%d M=%d D=%d", N, M, D);
   GPK_REQUIRE(Dout >= 1 && Dout <= DO_MAX, "det_fwd: Dout=%d outside [1,%d]", Dout, DO_MAX);
   GPK_REQUIRE(x && Z && lls2 && lsf2 && A && B, "det_fwd: null input");
@@ -557,17 +575,57 @@ extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* 
                            const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
                            const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
                            double* dA, void* dx, void* stream) {
+  GPK_NVTX("gpk_det_bwd");
+  return gpk_det_bwd_ws(prec, N, M, D, Dout, x, ldx, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dkfu, dsf2, dl, dZ, dA, dx,
+                        nullptr, 0, stream);
+}
+
+namespace {
+// rows split over CTAs: threads are b (a multiple of 32 >= M) x row groups, 512 at most; CTAs of
+// two passes of the row groups (8 rows at rg = 4): 125 CTAs for 1000 rows, one per SM at most
+int det_bwd_grid(int N, int M) {
+  const int bx = 32 * gpk::ceil_div(M, 32), rg = bx <= 128 ? 4 : 2;
+  int grid = gpk::ceil_div(N, 2 * rg);
+  if (grid > gpk::sm_count()) grid = gpk::sm_count();
+  return grid;
+}
+long det_bwd_stride(int M, int D, int Dout, bool dkfu) { return (long)M * D + (long)(dkfu ? 0 : Dout) * M + 1 + D; }
+
+// gram: 32 x 32 output tiles (the upper ones only when C is symmetric), rows split over
+// gridDim.z chunks so that about two CTAs run per SM
+int gram_chunks(int N, int M, bool sym) {
+  const int nt = gpk::ceil_div(M, 32);
+  const int tiles = sym ? nt * (nt + 1) / 2 : nt * nt;
+  int chunks = gpk::ceil_div(gpk::sm_count() * 2, tiles);
+  if (chunks > gpk::ceil_div(N, 16)) chunks = gpk::ceil_div(N, 16);
+  if (chunks < 1) chunks = 1;
+  return chunks;
+}
+}  // namespace
+
+long det_bwd_work_elems(int N, int M, int D, int Dout) {
+  return (long)gpk::sm_count() * det_bwd_stride(M, D, Dout, false);
+}
+long gram_work_elems(int N, int M, int Dout) { return (long)gram_chunks(N, M, true) * Dout * M * M; }
+
+extern "C" int gpk_det_bwd_ws(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                              const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
+                              const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
+                              double* dA, void* dx, double* work, long work_elems, void* stream) {
+  GPK_NVTX("gpk_det_bwd_ws");
   GPK_REQUIRE(N >= 0 && M >= 1 && M <= 256 && D >= 1 && D <= 16, "det_bwd: bad sizes N=%d M=%d D=%d (M<=256, D<=16)", N, M, D);
   GPK_REQUIRE(dkfu || (Dout >= 1 && Dout <= DO_MAX), "det_bwd: Dout=%d outside [1,%d]", Dout, DO_MAX);
   GPK_REQUIRE(x && Z && lls2 && lsf2 && kfu && dsf2 && dl && dZ, "det_bwd: null");
   GPK_REQUIRE(dkfu || (A && Bk && dm && dv), "det_bwd: need dkfu or (A, Bk, dm, dv)");
+  const long stride = det_bwd_stride(M, D, Dout, dkfu != nullptr);
+  if (work) {
+    const long need = (long)gpk::sm_count() * stride;
+    GPK_REQUIRE(work_elems >= need, "det_bwd: workspace of %ld doubles, %ld needed", work_elems, need);
+  }
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  // threads: b (a multiple of 32 >= M) x row groups, 512 at most; CTAs of two passes of the row
-  // groups (8 rows at rg = 4): 125 CTAs for 1000 rows
   const int bx = 32 * gpk::ceil_div(M, 32), rg = bx <= 128 ? 4 : 2;
-  int grid = gpk::ceil_div(N, 2 * rg);
-  if (grid > gpk::sm_count()) grid = gpk::sm_count();
+  const int grid = det_bwd_grid(N, M);
   const dim3 threads(bx, rg);
   const int dc = D <= 8 ? 8 : 16;
   if (prec == GPK_DF64) {
@@ -576,45 +634,66 @@ extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* 
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
                                  (const double*)A, (const double*)kfu, (const double*)Bk, (const double*)dm,
-                                 (const double*)dv, (const double*)dkfu, dsf2, dl, dZ, dA, (double*)dx);
+                                 (const double*)dv, (const double*)dkfu, dsf2, dl, dZ, dA, (double*)dx, work, stride);
   } else if (prec == GPK_FP32) {
     const size_t sm = det_bwd_smem(bx, rg, dc, sizeof(float));
     auto k = dc == 8 ? det_bwd_kernel<float, 8> : det_bwd_kernel<float, 16>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
                                  (const float*)kfu, (const float*)Bk, (const float*)dm, (const float*)dv,
-                                 (const float*)dkfu, dsf2, dl, dZ, dA, (float*)dx);
+                                 (const float*)dkfu, dsf2, dl, dZ, dA, (float*)dx, work, stride);
   } else {
     return gpk::fail(GPK_EINVAL, "det_bwd: unknown precision %d", prec);
   }
-  return gpk::check_launch("det_bwd");
+  int rc = gpk::check_launch("det_bwd");
+  if (rc != GPK_OK || !work) return rc;
+  gpk::RedPlan plan{};
+  plan.add(dZ, M * D);
+  plan.add(dA, dkfu ? 0 : Dout * M);
+  plan.add(dsf2, 1);
+  plan.add(dl, D);
+  return gpk::reduce_partials(work, grid, plan, st);
 }
 
 extern "C" int gpk_gram(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
                         void* stream) {
+  GPK_NVTX("gpk_gram");
+  return gpk_gram_ws(prec, N, M, Dout, u, v, w, C, nullptr, 0, stream);
+}
+
+extern "C" int gpk_gram_ws(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
+                           double* work, long work_elems, void* stream) {
+  GPK_NVTX("gpk_gram_ws");
   GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1 && Dout <= DO_MAX, "gram: bad sizes");
   GPK_REQUIRE(u && v && w && C, "gram: null pointer");
+  const int sym = u == v;   // C symmetric: the upper tiles only
+  const int chunks = gram_chunks(N, M, sym);
+  if (work) {
+    const long need = (long)chunks * Dout * M * M;
+    GPK_REQUIRE(work_elems >= need, "gram: workspace of %ld doubles, %ld needed", work_elems, need);
+  }
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
   const int nt = gpk::ceil_div(M, 32);
-  const int sym = u == v;   // C symmetric: the upper tiles only
   const int tiles = sym ? nt * (nt + 1) / 2 : nt * nt;
-  int chunks = gpk::ceil_div(gpk::sm_count() * 2, tiles);
-  if (chunks > gpk::ceil_div(N, 16)) chunks = gpk::ceil_div(N, 16);
-  if (chunks < 1) chunks = 1;
   const dim3 grid(sym ? tiles : nt, sym ? 1 : nt, chunks);
   if (prec == GPK_DF64)
     gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C,
-                                            sym);
+                                            sym, work);
   else if (prec == GPK_FP32)
     gram_kernel<float><<<grid, 256, 0, st>>>(N, M, Dout, (const float*)u, (const float*)v, (const float*)w, C,
-                                             sym);
+                                             sym, work);
   else
     return gpk::fail(GPK_EINVAL, "gram: unknown precision %d", prec);
-  return gpk::check_launch("gram");
+  int rc = gpk::check_launch("gram");
+  if (rc != GPK_OK || !work) return rc;
+  gpk::RedPlan plan{};
+  plan.add(C, Dout * M * M);
+  return gpk::reduce_partials(work, chunks, plan, st);
 }
 
 extern "C" int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const void* w, double* c, void* stream) {
+  GPK_NVTX("gpk_wsum");
   GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1 && Dout <= DO_MAX, "wsum: bad sizes");
   GPK_REQUIRE(u && w && c, "wsum: null pointer");
   if (N == 0) return GPK_OK;

@@ -24,6 +24,7 @@ extern "C" int gpk_psi_fwd(int prec, int N, int M, int Q, int Dout, const void* 
                            const void* Z, const double* lls2, const double* lsf2, const void* A,
                            const void* B, void* psi1, void* psi2, double* psi2_sum, void* m_out,
                            void* v_out, void* stream) {
+  GPK_NVTX("gpk_psi_fwd");
   GPK_REQUIRE(N >= 0 && M >= 1 && Q >= 1 && Q <= QMAX, "psi_fwd: bad sizes N=%d M=%d Q=%d", N, M, Q);
   GPK_REQUIRE(Dout >= 0 && Dout <= DMAX, "psi_fwd: Dout=%d outside [0,%d]", Dout, DMAX);
   GPK_REQUIRE(mu && var && Z && lls2 && lsf2, "psi_fwd: null input");
@@ -46,6 +47,7 @@ extern "C" int gpk_psi_fwd(int prec, int N, int M, int Q, int Dout, const void* 
 extern "C" int gpk_psi_rollout(int prec, int T, int M, int Q, const void* mu0, const void* var0, const void* Z,
                                const double* lls2, const double* lsf2, const void* A, const void* B, void* m_out,
                                void* v_out, void* stream) {
+  GPK_NVTX("gpk_psi_rollout");
   GPK_REQUIRE(T >= 0 && M >= 1 && Q >= 1 && Q <= DMAX && Q <= QMAX, "psi_rollout: bad sizes T=%d M=%d Q=%d", T, M, Q);
   GPK_REQUIRE(mu0 && var0 && Z && lls2 && lsf2 && A && B && m_out && v_out, "psi_rollout: null pointer");
   cudaStream_t st = gpk::as_stream(stream);
@@ -76,6 +78,7 @@ extern "C" int gpk_psi_bwd(int prec, int N, int M, int Q, int Dout, const void* 
                            const void* B, const void* m, const void* dm, const void* dv, double* dsf2,
                            double* dl, double* dZ, double* dA, double* dB, void* dmu, void* dvar,
                            void* stream) {
+  GPK_NVTX("gpk_psi_bwd");
   return gpk_psi_bwd_ex(prec, N, M, Q, Dout, mu, var, Z, lls2, lsf2, A, B, m, dm, dv, nullptr, 0, dsf2, dl, dZ,
                         dA, dB, dmu, dvar, stream);
 }
@@ -85,6 +88,22 @@ extern "C" int gpk_psi_bwd_ex(int prec, int N, int M, int Q, int Dout, const voi
                               const void* B, const void* m, const void* dm, const void* dv, const void* dpsi1,
                               long b_stride, double* dsf2, double* dl, double* dZ, double* dA, double* dB,
                               void* dmu, void* dvar, void* stream) {
+  GPK_NVTX("gpk_psi_bwd_ex");
+  return gpk_psi_bwd_ws(prec, N, M, Q, Dout, mu, var, Z, lls2, lsf2, A, B, m, dm, dv, dpsi1, b_stride, dsf2, dl,
+                        dZ, dA, dB, dmu, dvar, nullptr, 0, stream);
+}
+
+long psi_bwd_work_elems(int M, int Q, int Dout) {
+  const long P = (long)M * (M + 1) / 2;
+  return (long)gpk::sm_count() * (Dout * P + (long)Dout * M + (long)M * Q + 1 + Q);
+}
+
+extern "C" int gpk_psi_bwd_ws(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
+                              const void* Z, const double* lls2, const double* lsf2, const void* A,
+                              const void* B, const void* m, const void* dm, const void* dv, const void* dpsi1,
+                              long b_stride, double* dsf2, double* dl, double* dZ, double* dA, double* dB,
+                              void* dmu, void* dvar, double* work, long work_elems, void* stream) {
+  GPK_NVTX("gpk_psi_bwd_ws");
   GPK_REQUIRE(N >= 0 && M >= 1 && Q >= 1 && Q <= QMAX, "psi_bwd: bad sizes N=%d M=%d Q=%d", N, M, Q);
   GPK_REQUIRE(Dout >= 1 && Dout <= DMAX, "psi_bwd: Dout=%d outside [1,%d]", Dout, DMAX);
   GPK_REQUIRE(b_stride == 0 || Dout == 1, "psi_bwd: per-point B needs Dout == 1");
@@ -92,13 +111,19 @@ extern "C" int gpk_psi_bwd_ex(int prec, int N, int M, int Q, int Dout, const voi
   GPK_REQUIRE(dpsi1 || (A && m && dm), "psi_bwd: need dpsi1 or (A, m, dm)");
   GPK_REQUIRE(b_stride != 0 || dv, "psi_bwd: need dv");
   GPK_REQUIRE(dsf2 && dl && dZ && dmu && dvar, "psi_bwd: null output");
+  if (work) {
+    const long need = psi_bwd_work_elems(M, Q, Dout);
+    GPK_REQUIRE(work_elems >= need, "psi_bwd: workspace of %ld doubles, %ld needed", work_elems, need);
+  }
   cudaStream_t st = gpk::as_stream(stream);
+  const long stride = (long)Dout * M * (M + 1) / 2 + (long)Dout * M + (long)M * Q + 1 + Q;
   if (prec == GPK_DF64) {
     auto a = make_args<double>(N, M, Q, Dout, mu, var, Z, lls2, lsf2, A, B);
     a.m = (const double*)m; a.dm = (const double*)dm; a.dv = (const double*)dv;
     a.dpsi1 = (const double*)dpsi1; a.b_stride = b_stride;
     a.dsf2 = dsf2; a.dl = dl; a.dZ = dZ; a.dA = dA; a.dB = dB;
     a.dmu = (double*)dmu; a.dvar = (double*)dvar;
+    a.part = work; a.part_stride = stride;
     return psi_bwd_df64(a, st);
   } else if (prec == GPK_FP32) {
     auto a = make_args<float>(N, M, Q, Dout, mu, var, Z, lls2, lsf2, A, B);
@@ -106,6 +131,7 @@ extern "C" int gpk_psi_bwd_ex(int prec, int N, int M, int Q, int Dout, const voi
     a.dpsi1 = (const float*)dpsi1; a.b_stride = b_stride;
     a.dsf2 = dsf2; a.dl = dl; a.dZ = dZ; a.dA = dA; a.dB = dB;
     a.dmu = (float*)dmu; a.dvar = (float*)dvar;
+    a.part = work; a.part_stride = stride;
     return psi_bwd_f32(a, st);
   }
   return gpk::fail(GPK_EINVAL, "psi_bwd: unknown precision %d", prec);

@@ -64,16 +64,12 @@ struct PsiArgs {
   double* dB;
   S* dmu;
   S* dvar;
+  double* part;      // backward, fixed-order path: this CTA's partial sums at part + blockIdx.x *
+                     // part_stride ([dB pairs D*P | dA D*M | dZ M*Q | dsf2 | dl Q]), no atomics
+  long part_stride;
 };
 
-__device__ __forceinline__ void pair_of(int p, int& a, int& b) {
-  // row-major lower triangle: p = a(a+1)/2 + b, 0 <= b <= a
-  int r = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
-  if ((r + 1) * (r + 2) / 2 <= p) ++r;
-  if (r * (r + 1) / 2 > p) --r;
-  a = r;
-  b = p - r * (r + 1) / 2;
-}
+__device__ __forceinline__ void pair_of(int p, int& a, int& b) { tri_pair(p, a, b); }
 
 // CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.  Only the
 // first `nact` warps hold non-zero values (the others skip the shuffles; default: all).
@@ -533,6 +529,9 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
   }
   if (s.accB)
     for (int i = threadIdx.x; i < D * P; i += NTB) s.accB[i] = Num<T>::zero();
+  double* const part = a.part ? a.part + (size_t)blockIdx.x * a.part_stride : nullptr;
+  if (part && !s.accB)   // dBhat accumulates in this CTA's partial block (each pair has one owner)
+    for (int i = threadIdx.x; i < D * P; i += NTB) part[i] = 0.0;
   __syncthreads();
   if (threadIdx.x < Q) {
     const int q = threadIdx.x;
@@ -755,6 +754,8 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
         if (d < D) {
           if (s.accB) {
             s.accB[d * P + p] = add(s.accB[d * P + p], ab[d]);
+          } else if (part) {   // no room for the accumulators: this thread's pair of the partial block
+            part[d * P + p] += (double)Num<T>::st(ab[d]);
           } else if (a.dB) {   // no room for the accumulators: straight into dB
             const double v = (double)Num<T>::st(ab[d]);
             atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
@@ -874,38 +875,54 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
     }
     __syncthreads();
   }
-  // ---- flush CTA accumulators
-  if (a.dB && s.accB) {
-    for (int p = threadIdx.x; p < P; p += NTB) {
-      int ia, ib;
-      pair_of(p, ia, ib);
-      for (int d = 0; d < D; ++d) {
-        const double v = (double)Num<T>::st(s.accB[d * P + p]);
-        atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
-        if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
-      }
-    }
-  }
-  if (threadIdx.x < M) {
-#pragma unroll
-    for (int d = 0; d < DB; ++d)
-      if (d < D && a.dA && !a.dpsi1) atomicAdd(&a.dA[d * M + threadIdx.x], (double)Num<T>::st(g_A[d]));
-  }
-  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) atomicAdd(&a.dZ[i], (double)Num<T>::st(s.dz[i]));
-  // dsf2 and dl need the ell / sf2 factors: (sum L1 + 2 sum L) / sf2 and ell * g_l
+  // ---- flush CTA accumulators: into the partial block (fixed-order path) or atomically
   T fin[1 + QC];
   fin[0] = g_sf;
 #pragma unroll
   for (int q = 0; q < QC; ++q) fin[1 + q] = g_l[q];
+  if (part) {
+    const bool wantA = a.dA && !a.dpsi1;
+    if (s.accB)
+      for (int i = threadIdx.x; i < D * P; i += NTB) part[i] = (double)Num<T>::st(s.accB[i]);
+    if (threadIdx.x < M) {
+#pragma unroll
+      for (int d = 0; d < DB; ++d)
+        if (d < D) part[D * P + d * M + threadIdx.x] = wantA ? (double)Num<T>::st(g_A[d]) : 0.0;
+    }
+    for (int i = threadIdx.x; i < M * Q; i += blockDim.x) part[D * P + D * M + i] = (double)Num<T>::st(s.dz[i]);
+  } else {
+    if (a.dB && s.accB) {
+      for (int p = threadIdx.x; p < P; p += NTB) {
+        int ia, ib;
+        pair_of(p, ia, ib);
+        for (int d = 0; d < D; ++d) {
+          const double v = (double)Num<T>::st(s.accB[d * P + p]);
+          atomicAdd(&a.dB[((size_t)d * M + ia) * M + ib], v);
+          if (ia != ib) atomicAdd(&a.dB[((size_t)d * M + ib) * M + ia], v);
+        }
+      }
+    }
+    if (threadIdx.x < M) {
+#pragma unroll
+      for (int d = 0; d < DB; ++d)
+        if (d < D && a.dA && !a.dpsi1) atomicAdd(&a.dA[d * M + threadIdx.x], (double)Num<T>::st(g_A[d]));
+    }
+    for (int i = threadIdx.x; i < M * Q; i += blockDim.x) atomicAdd(&a.dZ[i], (double)Num<T>::st(s.dz[i]));
+  }
+  // dsf2 and dl need the ell / sf2 factors: (sum L1 + 2 sum L) / sf2 and ell * g_l
   __syncthreads();
   block_sum<T, 1 + QC>(fin, s.red);
   if (threadIdx.x == 0) {
-    atomicAdd(a.dsf2, (double)Num<T>::st(div(fin[0], s.misc[1])));
+    const double vsf = (double)Num<T>::st(div(fin[0], s.misc[1]));
+    if (part) part[D * P + D * M + M * Q] = vsf;
+    else atomicAdd(a.dsf2, vsf);
 #pragma unroll
     for (int q = 0; q < QC; ++q) {
       if (q < Q) {
         T ell = sqrt_(s.ell2[q]);
-        atomicAdd(&a.dl[q], (double)Num<T>::st(mul(fin[1 + q], ell)));
+        const double vl = (double)Num<T>::st(mul(fin[1 + q], ell));
+        if (part) part[D * P + D * M + M * Q + 1 + q] = vl;
+        else atomicAdd(&a.dl[q], vl);
       }
     }
   }
@@ -964,6 +981,19 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   return fwd_variant<T, QMAX>(a, sum, contract, P, per_sm, sm, st);
 }
 
+// the destinations of the backward's partial block (layout in PsiArgs::part)
+template <typename S>
+gpk::RedPlan bwd_plan(const PsiArgs<S>& a) {
+  const int M = a.M, Q = a.Q, D = a.Dout, P = M * (M + 1) / 2;
+  gpk::RedPlan r{};
+  r.add(a.dB, D * P, 1, M);
+  r.add(a.dpsi1 ? nullptr : a.dA, D * M);
+  r.add(a.dZ, M * Q);
+  r.add(a.dsf2, 1);
+  r.add(a.dl, Q);
+  return r;
+}
+
 template <typename T, int NPB, int DB, int QC>
 int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t st) {
   auto k = psi_bwd_kernel<T, NPB, DB, QC>;
@@ -972,7 +1002,9 @@ int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t 
   if (grid > a.N) grid = a.N;
   if (grid < 1) return GPK_OK;
   k<<<grid, nt_bwd(QC), sm, st>>>(a);
-  return gpk::check_launch("psi_bwd");
+  int rc = gpk::check_launch("psi_bwd");
+  if (rc != GPK_OK || !a.part) return rc;
+  return gpk::reduce_partials(a.part, grid, bwd_plan(a), st);
 }
 
 template <typename T, int NPB, int QC>

@@ -51,15 +51,35 @@ def psi_fwd(mu, var, Z, lls2, lsf2, A=None, B=None, psi1=None, psi2=None, psi2_s
          stream())
 
 
+OP_PSI_BWD, OP_DET_BWD, OP_GRAM, OP_TRACE_KZZ = 1, 2, 3, 4   # GPK_OP_*
+
+
+def work_elems(op, N, M, D, Dout):
+    """Float64 workspace elements of the fixed-order form of operation `op` (gpk_work_elems)."""
+    n = ctypes.c_long(0)
+    call('gpk_work_elems', int(op), int(N), int(M), int(D), int(Dout), ctypes.addressof(n))
+    return int(n.value)
+
+
+def _ws(work):
+    return (ptr(work), 0 if work is None else work.numel())
+
+
 def psi_bwd(mu, var, Z, lls2, lsf2, A, B, m, dm, dv, dsf2, dl, dZ, dA, dB, dmu, dvar,
-            dpsi1=None, b_stride=0, Dout=None):
+            dpsi1=None, b_stride=0, Dout=None, work=None):
+    """work: a float64 workspace of work_elems(OP_PSI_BWD, ...) for the fixed-order
+    (bit-reproducible) sums; None adds with atomics."""
     N, Q = mu.shape
     M = Z.shape[0]
     if Dout is None:
         Dout = A.shape[0] if A is not None else 1
-    call('gpk_psi_bwd_ex', prec_of(mu.dtype), N, M, Q, Dout, ptr(mu), ptr(var), ptr(Z), ptr(lls2),
-         ptr(lsf2), ptr(A), ptr(B), ptr(m), ptr(dm), ptr(dv), ptr(dpsi1), int(b_stride), ptr(dsf2),
-         ptr(dl), ptr(dZ), ptr(dA), ptr(dB), ptr(dmu), ptr(dvar), stream())
+    args = (prec_of(mu.dtype), N, M, Q, Dout, ptr(mu), ptr(var), ptr(Z), ptr(lls2),
+            ptr(lsf2), ptr(A), ptr(B), ptr(m), ptr(dm), ptr(dv), ptr(dpsi1), int(b_stride), ptr(dsf2),
+            ptr(dl), ptr(dZ), ptr(dA), ptr(dB), ptr(dmu), ptr(dvar))
+    if work is None:
+        call('gpk_psi_bwd_ex', *args, stream())
+    else:
+        call('gpk_psi_bwd_ws', *args, *_ws(work), stream())
 
 
 def det_fwd(x, Z, lls2, lsf2, A, B, kfu=None, Bk=None, m_out=None, v_out=None):
@@ -70,19 +90,27 @@ def det_fwd(x, Z, lls2, lsf2, A, B, kfu=None, Bk=None, m_out=None, v_out=None):
          ptr(A), ptr(B), ptr(kfu), ptr(Bk), ptr(m_out), ptr(v_out), stream())
 
 
-def det_bwd(x, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dsf2, dl, dZ, dA, dx=None, dkfu=None, Dout=None):
+def det_bwd(x, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dsf2, dl, dZ, dA, dx=None, dkfu=None, Dout=None, work=None):
     N, D = x.shape
     M = Z.shape[0]
     if Dout is None:
         Dout = A.shape[0] if A is not None else 1
-    call('gpk_det_bwd', prec_of(x.dtype), N, M, D, Dout, ptr(x), D, ptr(Z), ptr(lls2), ptr(lsf2),
-         ptr(A), ptr(kfu), ptr(Bk), ptr(dm), ptr(dv), ptr(dkfu), ptr(dsf2), ptr(dl), ptr(dZ),
-         ptr(dA), ptr(dx), stream())
+    args = (prec_of(x.dtype), N, M, D, Dout, ptr(x), D, ptr(Z), ptr(lls2), ptr(lsf2),
+            ptr(A), ptr(kfu), ptr(Bk), ptr(dm), ptr(dv), ptr(dkfu), ptr(dsf2), ptr(dl), ptr(dZ),
+            ptr(dA), ptr(dx))
+    if work is None:
+        call('gpk_det_bwd', *args, stream())
+    else:
+        call('gpk_det_bwd_ws', *args, *_ws(work), stream())
 
 
-def gram(u, v, w, C):
+def gram(u, v, w, C, work=None):
     N, M = u.shape
-    call('gpk_gram', prec_of(u.dtype), N, M, w.shape[1], ptr(u), ptr(v), ptr(w), ptr(C), stream())
+    args = (prec_of(u.dtype), N, M, w.shape[1], ptr(u), ptr(v), ptr(w), ptr(C))
+    if work is None:
+        call('gpk_gram', *args, stream())
+    else:
+        call('gpk_gram_ws', *args, *_ws(work), stream())
 
 
 def wsum(u, w, c):
@@ -141,10 +169,14 @@ def chol_inv(A, Ainv=None, L=None, logdet=None, info=None, work=None):
          ptr(work), stream())
 
 
-def trace_kzz(Mm, Z, lls2, lsf2, g_sf, g_ls, g_z, s_sf=1.0, s_ls=1.0):
+def trace_kzz(Mm, Z, lls2, lsf2, g_sf, g_ls, g_z, s_sf=1.0, s_ls=1.0, work=None):
     M, Q = Z.shape
-    call('gpk_trace_kzz', prec_of(Z.dtype), M, Q, ptr(Mm), ptr(Z), ptr(lls2), ptr(lsf2), float(s_sf),
-         float(s_ls), ptr(g_sf), ptr(g_ls), ptr(g_z), stream())
+    args = (prec_of(Z.dtype), M, Q, ptr(Mm), ptr(Z), ptr(lls2), ptr(lsf2), float(s_sf),
+            float(s_ls), ptr(g_sf), ptr(g_ls), ptr(g_z))
+    if work is None:
+        call('gpk_trace_kzz', *args, stream())
+    else:
+        call('gpk_trace_kzz_ws', *args, *_ws(work), stream())
 
 
 def small_spd(A, Ainv=None, logdet=None, info=None):
@@ -164,7 +196,7 @@ class _GemmT(ctypes.Structure):
                 ('strideC', ctypes.c_long)]
 
 
-_GROUP = 8   # GPK_GEMM_GROUP
+_GROUP = 16   # GPK_GEMM_GROUP
 
 
 _LC_GROUP = 4   # GPK_LC_GROUP
@@ -281,6 +313,34 @@ def _lc_desc(out, terms, ranks, sum_batch, batch):
         d.sv[i] = cols if (v.dim() == 2 and v.shape[0] > 1) else 0
     d.out = ptr(out)
     return d, keep
+
+
+class _Forms(ctypes.Structure):
+    """gpk_forms_t (include/gpk.h)."""
+    _fields_ = [('D', ctypes.c_int), ('M', ctypes.c_int), ('beta', ctypes.c_double)] + \
+        [(n, ctypes.c_void_p) for n in ('T', 'Kinv', 't', 'Qh', 'KShK', 'Qu', 'KSuK', 'Tmh', 'Kmh', 'Tmu', 'Kmu',
+                                        'Bd', 'Bp', 'Bsto', 'Ah', 'A', 'regime')]
+
+
+_FORMS_MAX = 8   # GPK_FORMS_MAX
+
+
+def cavity_forms(items):
+    """gpk_cavity_forms over a list of dicts with the gpk_forms_t fields (tensors for the
+    pointers): each layer's posterior and cavity moments in the form accurate for its regime."""
+    for i in range(0, len(items), _FORMS_MAX):
+        chunk = items[i:i + _FORMS_MAX]
+        arr = (_Forms * len(chunk))()
+        keep = []
+        for a, it in zip(arr, chunk):
+            a.D, a.M, a.beta = int(it['D']), int(it['M']), float(it['beta'])
+            for n, _ in _Forms._fields_[3:]:
+                v = it.get(n)
+                if v is not None:
+                    v = v.contiguous()
+                    keep.append(v)
+                setattr(a, n, ptr(v))
+        call('gpk_cavity_forms', len(chunk), ctypes.addressof(arr), stream())
 
 
 def nat_prep(eta1, ls, sf, R, lls2, lsf2):

@@ -84,6 +84,16 @@ class DevLayer:
         self.prezeroed = False
         self.side = None
         self._dAh, self._dBh = views[2].view(Dout, M), views[3].view(Dout, M, M)
+        self._works = {}
+
+    def work(self, op):
+        """The layer's float64 workspace for the fixed-order (bit-reproducible) sums of
+        operation `op` (gpk.OP_*), sized for any number of rows and allocated on first use."""
+        w = self._works.get(op)
+        if w is None:
+            n = gpk.work_elems(op, 1 << 30, self.M, self.Din, self.Dout)
+            w = self._works[op] = torch.empty(n, dtype=F64, device=self.dev)
+        return w
 
     # ---------------------------------------------------------------- parameters
     def param_tensors(self):
@@ -128,17 +138,25 @@ class DevLayer:
         return out
 
     def set_s_factors(self, inv, logdet):
-        """Posterior and cavity moments from the inverted Su^-1, Suhat^-1, then the cavity
-        tail; the products of each stage are launched together."""
+        """Posterior and cavity moments from the inverted Su^-1, Suhat^-1; the products of each
+        stage are launched together."""
         with gpk.GemmGroup() as g:
             self._s_stage1(inv, logdet, g)
         with gpk.GemmGroup() as g:
             self._s_stage2(g)
-        with gpk.GemmGroup() as g:
-            self._s_stage3(g)
-        self._s_stage4()
+        gpk.cavity_forms([self._forms_item()])
 
-    # the four stages of set_s_factors (setup_layers interleaves them across layers)
+    # The three stages of set_s_factors (setup_layers interleaves them across layers).
+    #
+    # The cavity's Ahat = K^-1 muhat and Bhat_det = K^-1 Suhat K^-1 - K^-1 (aep_models.py:536-546)
+    # and the posterior's A, B (base_models.py:480-488) have two exact forms, from
+    # K^-1 Suhat = I - beta T Suhat (T = theta_1, t = theta_2, Suhat^-1 = K^-1 + beta T):
+    #     Bhat_det = beta^2 T Suhat T - beta T,   Ahat = beta t - beta T muhat,
+    # and each cancels in one regime.  When K^-1 dominates (Kuu ill-conditioned: entries ~1e5 at
+    # the deep GP's initialisation, cond ~7e6) the K^-1 products lose ~5 digits and the T form is
+    # exact to rounding; when T dominates (tight posteriors) the T form subtracts two matrices of
+    # size T.  Both forms' products are formed (stages 1-2) and gpk_cavity_forms keeps, per
+    # output, the one whose large operand is the smaller.
     def _s_stage1(self, inv, logdet, g):
         D = self.Dout
         self.Su, self.Sh = inv[:D], inv[D:]
@@ -148,23 +166,64 @@ class DevLayer:
         th2 = self.th2.unsqueeze(-1)
         self._mu3 = g.mm(self.Su, th2)                     # mu = Su theta_2
         self._mh3 = g.mm(self.Sh, th2, alpha=self.beta)    # muhat = Suhat beta theta_2
+        self._TSh, self._KSh = g.mm(self.th1, self.Sh), g.mm(self.Kinv, self.Sh)
+        self._TSu, self._KSu = g.mm(self.th1, self.Su), g.mm(self.Kinv, self.Su)
 
     def _s_stage2(self, g):
         self.mu, self.mh = self._mu3.squeeze(-1), self._mh3.squeeze(-1)
         self.Spmm = g.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
         self.Smm_h = g.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
-        self._Ah3 = g.mm(self.Kinv, self._mh3)             # Ahat = K^-1 muhat
-        self._KS2 = g.mm(self.Kinv, self.Sh)
+        self._Qh, self._KShK = g.mm(self._TSh, self.th1), g.mm(self._KSh, self.Kinv)
+        self._Qu, self._KSuK = g.mm(self._TSu, self.th1), g.mm(self._KSu, self.Kinv)
+        self._Tmh, self._Kmh = g.mm(self.th1, self._mh3), g.mm(self.Kinv, self._mh3)
+        self._Tmu, self._Kmu = g.mm(self.th1, self._mu3), g.mm(self.Kinv, self._mu3)
 
-    def _s_stage3(self, g):
-        self.Ah = self._Ah3.squeeze(-1)
-        # Bhat_det = K^-1 Suhat K^-1 - K^-1 (aep_models.py:536-546)
-        self.Bh_det = g.mm(self._KS2, self.Kinv, beta=-1.0, E=self.Kinv)
+    def _forms_item(self):
+        """The gpk_cavity_forms item of this layer; allocates its outputs (Bh_det, Bh_sto, Ahat
+        and the posterior's Bpost, Apost) and the per-output regime word."""
+        self.Bh_det = torch.empty_like(self._Qh)
+        self.Bpost = torch.empty_like(self._Qh)
+        self.Bh_sto = torch.empty_like(self._Qh)
+        self.Ah = torch.empty_like(self.mh)
+        self.Apost = torch.empty_like(self.mu)
+        if getattr(self, 'regime', None) is None:
+            self.regime = torch.zeros(self.Dout, dtype=torch.int32, device=self.dev)
+        sq = lambda v: v.reshape(v.shape[0], -1)
+        return dict(D=self.Dout, M=self.M, beta=self.beta, T=self.th1, Kinv=self.Kinv, t=self.th2, Qh=self._Qh,
+                    KShK=self._KShK, Qu=self._Qu, KSuK=self._KSuK, Tmh=sq(self._Tmh), Kmh=sq(self._Kmh),
+                    Tmu=sq(self._Tmu), Kmu=sq(self._Kmu), Bd=self.Bh_det, Bp=self.Bpost, Bsto=self.Bh_sto,
+                    Ah=self.Ah, A=self.Apost, regime=self.regime)
 
-    def _s_stage4(self, g=None):
-        # Bhat_sto = K^-1 (Suhat + mh mh^T) K^-1 - K^-1 = Bhat_det + Ahat Ahat^T
-        lc = g.lincomb if g is not None else gpk.lincomb
-        self.Bh_sto = lc(torch.empty_like(self.Bh_det), [(1.0, self.Bh_det)], [(1.0, self.Ah, self.Ah)])
+    def _kuu_grad_levels(self, dAh, dBh, sto, alpha):
+        """The gradient of the layer's energy w.r.t. Kuu, summed over outputs, without products
+        with K^-1 (natural-parameter layers): three dependency levels (a generator; each
+        `send(g)` adds one level's members to group g), the last writing `self.Mall`.  It equals
+        the reference's 1/2 (D K^-1 + K^-1 Minner K^-1) (aep_models.py:250-297, 453-505) up to an
+        antisymmetric part, which the trace gradient ignores:
+          sum_d [ Bd dBhat Bd + Bd a Ahat^T + s_post/2 (Bpost + A A^T) + s_cav/2 (Bd + Ahat Ahat^T) ]
+        with Bd = Bhat_det, A = K^-1 mu, s_post = N/alpha - 1, s_cav = -N/alpha, and a the gradient
+        reaching Ahat (dAhat, plus 2 dBhat Ahat when Bhat_sto carries Ahat Ahat^T).  The data part
+        follows from dAhat = Bd dK Ahat and dBd = Bd dK Bd (Ahat = beta G t, Bd = -beta G T,
+        G = (I + beta T K)^-1); the log-partitions' derivative is 1/2 (B + A A^T) for each of
+        prior-free posterior and cavity, their K^-1 terms summing to zero with the prior's."""
+        D, M = self.Dout, self.M
+        s_post, s_cav = self.N / alpha - 1.0, -self.N / alpha
+        g = yield
+        BdB = g.mm(self.Bh_det, dBh)
+        if sto:
+            a = g.mm(dBh, self.Ah.unsqueeze(-1), alpha=2.0, beta=1.0, E=dAh.unsqueeze(-1))
+        else:
+            a = dAh.unsqueeze(-1)
+        g = yield
+        data = g.mm(BdB, self.Bh_det)
+        Bda = g.mm(self.Bh_det, a).view(D, M)
+        g = yield
+        self.Mall = g.lincomb(torch.empty((M, M), dtype=F64, device=self.dev),
+                              [(1.0, data), (0.5 * s_post, self.Bpost), (0.5 * s_cav, self.Bh_det)],
+                              [(1.0, Bda, self.Ah), (0.5 * s_post, self.Apost, self.Apost),
+                               (0.5 * s_cav, self.Ah, self.Ah)],
+                              sum_batch=True, batch=D)
+        yield
 
     def setup_posterior(self):
         """update_hypers + compute_kuu + update_posterior (base_models.py:630-658,454-488)."""
@@ -277,7 +336,7 @@ class DevLayer:
 
     def _finish_hyp(self, Minner):
         gpk.trace_kzz(Minner.contiguous(), self.zu, self.lls2, self.lsf2, self.g['sf'], self.g['ls'],
-                      self.g['zu'], s_sf=2.0, s_ls=2.0)
+                      self.g['zu'], s_sf=2.0, s_ls=2.0, work=self.work(gpk.OP_TRACE_KZZ))
 
     def zero_accumulators(self):
         """Zero what the data-sized backward kernels add into: the kernel-hyperparameter and
@@ -306,7 +365,7 @@ class DevLayer:
         dmx = torch.empty((n, Q), dtype=F64, device=self.dev)
         dvx = torch.empty_like(dmx)
         gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.Ah, self.Bh_sto, m, dm, dv, self._dsf2, self._dl,
-                    dZ, self._dAh, self._dBh, dmx, dvx)
+                    dZ, self._dAh, self._dBh, dmx, dvx, work=self.work(gpk.OP_PSI_BWD))
         self._dv = dv   # for the hyperparameter chain rule, with the algebra
         return dmx, dvx
 
@@ -314,6 +373,49 @@ class DevLayer:
         """The M x M part of backprop_grads_lvm_mm (aep_models.py:250-304): cavity,
         natural-parameter and Kuu gradients.  Products of one dependency level are launched
         together; 2 dvcav muhat is formed as 2 (K^-1 dBhat) Ahat (K^-1 muhat = Ahat)."""
+        if not self.nat:
+            return self._bwd_mm_algebra_inv(alpha)
+        N, M, D = self.N, self.M, self.Dout
+        s_post, s_cav = N / alpha - 1.0, -N / alpha
+        beta = self.beta
+        dAh, dBh = self._dAh, self._dBh
+        K = self.Kinv
+        self._kernel_grads(self._dsf2, self._dl, self._dv)
+        kg = self._kuu_grad_levels(dAh, dBh, True, alpha)
+        next(kg)
+        with gpk.GemmGroup() as g:
+            KdB = g.mm(K, dBh)
+            U = g.mm(dAh, K, tB=True)
+            kg.send(g)
+        with gpk.GemmGroup() as g:
+            dvcav = g.mm(KdB, K)                                             # K^-1 dBhat K^-1
+            t = g.mm(KdB, self.Ah.unsqueeze(-1), alpha=2.0)                  # 2 dvcav muhat
+            kg.send(g)
+        # dmcav = U + t, and dvcav += beta dmcav th2^T as beta (U + t) th2^T (one level)
+        t2 = t.reshape(D, M)
+        with gpk.GemmGroup() as g:
+            dmcav = g.lincomb(torch.empty_like(U), [(1.0, U), (1.0, t2)])
+            g.lincomb(dvcav, [(1.0, dvcav)], [(beta, U, self.th2), (beta, t2, self.th2)])
+            kg.send(g)
+        self._finish_hyp(self.Mall)
+        with gpk.GemmGroup() as g:
+            SD = g.mm(self.Sh, dvcav)
+            dth2 = g.mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta)
+        dvcavinv = mm(SD, self.Sh, alpha=-1.0)
+        # sym = dth1 + dth1^T, dth1 = -s_post/2 Spmm - s_cav beta/2 Smm_h + beta dvcavinv
+        a1, a2 = -0.5 * s_post, -0.5 * s_cav * beta
+        sym = gpk.lincomb(torch.empty_like(dvcavinv), [(a1, self.Spmm), (a1, self.Spmm, True), (a2, self.Smm_h),
+                                                       (a2, self.Smm_h, True), (beta, dvcavinv),
+                                                       (beta, dvcavinv, True)])
+        with gpk.GemmGroup() as g:
+            dR = g.mm(self.R, sym)
+            g.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2.reshape(D, M))])
+        gpk.triu_pack(dR, self.R, self.g['eta1_R'])
+
+    def _bwd_mm_algebra_inv(self, alpha):
+        """bwd_mm_algebra for moment-parameterised layers (nat_param=False), through K^-1 as the
+        reference forms it (aep_models.py:250-304): cavity, parameter and Kuu gradients.
+        Products of one dependency level are launched together."""
         N, M, D = self.N, self.M, self.Dout
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
@@ -392,12 +494,13 @@ class DevLayer:
         dsf2, dl, dAh = z(1), z(Q), z(D, M)
         dZ = self.g['zu']
         dZ.zero_()
-        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh, dx=dx)
+        gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, dsf2, dl, dZ, dAh, dx=dx,
+                    work=self.work(gpk.OP_DET_BWD))
         self._kernel_grads(dsf2, dl, dv)
         # sum_n dm_nd (kfu_n K^-1) = dAhat_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T =
         # K^-1 dBhat_d K^-1: the M x M forms of the reference's kfu Kuuinv contractions
         dBh = z(D, M, M)
-        gpk.gram(kfu, kfu, dv, dBh)
+        gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
         dmucav = mm(dAh, K)
         dSucav = mm(mm(K, dBh), K)
         Sinv_mh = mv(self.Shinv, self.mh)
@@ -485,9 +588,9 @@ class DevLayer:
         self.zero_accumulators()
         dA, dB = self._dAh, self._dBh
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.A, kfu, Bk, dm, dv, self._dsf2, self._dl, self.g['zu'],
-                    dA, dx=dx)
+                    dA, dx=dx, work=self.work(gpk.OP_DET_BWD))
         self._kernel_grads(self._dsf2, self._dl, dv)
-        gpk.gram(kfu, kfu, dv, dB)
+        gpk.gram(kfu, kfu, dv, dB, work=self.work(gpk.OP_GRAM))
         # sum_n dm_nd (kfu_n K^-1) = dA_d K^-1 and sum_n dv_nd (K^-1 kfu_n)(K^-1 kfu_n)^T = K^-1 dB_d K^-1;
         # the KL adds K^-1 mu_d to dmu and (K^-1 - Su^-1)/2 to dSu
         dmu = mm(dA, K, beta=1.0, E=mm(self.mu, K))
@@ -511,7 +614,7 @@ class DevLayer:
         dmx = torch.empty_like(mx)
         dvx = torch.empty_like(vx)
         gpk.psi_bwd(mx, vx, self.zu, self.lls2, self.lsf2, self.A, self.B_sto, m, dm, dv, self._dsf2, self._dl,
-                    self.g['zu'], dA, dB, dmx, dvx)
+                    self.g['zu'], dA, dB, dmx, dvx, work=self.work(gpk.OP_PSI_BWD))
         self._kernel_grads(self._dsf2, self._dl, dv)
         # dSu = K^-1 dB K^-1 (+ the KL's (K^-1 - Su^-1)/2);  dmu = 2 dSu mu + K^-1 dA + K^-1 mu
         KdBK = mm(mm(K, dB), K)
@@ -541,7 +644,7 @@ class DevLayer:
         dZ = self.g['zu']
         dAh, dBh = self._dAh, self._dBh
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh,
-                    dx=dx)
+                    dx=dx, work=self.work(gpk.OP_DET_BWD))
         main = torch.cuda.current_stream()
         if self.side is not None:   # the chain rule beside the algebra; joined before trace_kzz
             self.side.wait_stream(main)
@@ -549,27 +652,33 @@ class DevLayer:
                 self._kernel_grads(self._dsf2, self._dl, dv)
         else:
             self._kernel_grads(self._dsf2, self._dl, dv)
-        gpk.gram(kfu, kfu, dv, dBh)
+        gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
+        kg = self._kuu_grad_levels(dAh, dBh, False, alpha)
+        next(kg)
         with gpk.GemmGroup() as g:
             Sinv_mh = g.mm(self.Shinv, self.mh.unsqueeze(-1))
             Sinv_mu = g.mm(self.Suinv, self.mu.unsqueeze(-1))
             KdB = g.mm(K, dBh)
-            KS = g.mm(K, self.Sh)
-            T1 = g.mm(dAh, self.mh, tA=True)
             U = g.mm(dAh, K)
+            kg.send(g)
         Sinv_mh, Sinv_mu = Sinv_mh.reshape(D, M), Sinv_mu.reshape(D, M)
         # cavity: dmucav = dAhat K^-1 + s_cav Suhat^-1 muhat (sum_n dm (kfu K^-1) = dAhat K^-1);
         # dSucav = K^-1 dBhat K^-1 + s_cav (Suhat^-1/2 - s s^T/2), plus the mean's beta dmucav th2^T
         # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
         with gpk.GemmGroup() as g:
             X = g.mm(KdB, K)
-            T2 = g.mm(KS.reshape(D * M, M), dBh.reshape(D * M, M), tA=True, alpha=2.0, beta=1.0, E=T1)
             e2p = g.mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
             dmucav = g.lincomb(torch.empty_like(U), [(1.0, U), (s_cav, Sinv_mh)])
             Y = g.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
                           [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
-        gpk.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
-                    [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
+            kg.send(g)
+        with gpk.GemmGroup() as g:
+            g.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
+                      [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
+            kg.send(g)
+        if self.side is not None:
+            main.wait_stream(self.side)
+        self._finish_hyp(self.Mall)
         with gpk.GemmGroup() as g:
             SX = g.mm(self.Sh, X)
             SY = g.mm(self.Su, Y)
@@ -578,21 +687,10 @@ class DevLayer:
         with gpk.GemmGroup() as g:
             dSinv_c = g.mm(SX, self.Sh, alpha=-1.0)
             dSinv_p = g.mm(SY, self.Su, alpha=-1.0)
-        # d eta1_R = pack(dth1 + dth1^T), dth1 = beta dSinv_c + dSinv_p;
-        # Kuu^-1 gradient: dAhat^T muhat + 2 sum_d (K^-1 Suhat)^T dBhat - sum_d dBhat
-        #                  + sum_d dSinv_c + sum_d dSinv_p - D/2 Kuu
-        with gpk.GemmGroup() as g:
-            sym = g.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (beta, dSinv_c, True), (1.0, dSinv_p),
-                                                        (1.0, dSinv_p, True)])
-            dK = g.lincomb(torch.empty_like(K), [(1.0, T2), (-1.0, dBh), (1.0, dSinv_c), (1.0, dSinv_p),
-                                                 (-0.5 * D, self.Kuu)], sum_batch=True, batch=D)
-        with gpk.GemmGroup() as g:
-            dR = g.mm(self.R, sym)
-            KdK = g.mm(K, dK)
-        Minner = mm(KdK, K, alpha=-1.0)
-        if self.side is not None:
-            main.wait_stream(self.side)
-        self._finish_hyp(Minner)
+        # d eta1_R = pack(dth1 + dth1^T), dth1 = beta dSinv_c + dSinv_p
+        sym = gpk.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (beta, dSinv_c, True), (1.0, dSinv_p),
+                                                      (1.0, dSinv_p, True)])
+        dR = mm(self.R, sym)
         gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 
 
@@ -704,11 +802,6 @@ def setup_layers(layers, alpha, streams=None):
         with gpk.GemmGroup() as g:
             for l in group:
                 l._s_stage2(g)
-        with gpk.GemmGroup() as g:
-            for l in group:
-                l._s_stage3(g)
-        with gpk.GemmGroup() as g:
-            for l in group:
-                l._s_stage4(g)
+        gpk.cavity_forms([l._forms_item() for l in group])
         statuses.append(info)
     return statuses

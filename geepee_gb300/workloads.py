@@ -106,6 +106,49 @@ def kink_ssm(seed: int = 0, T: int = 5000, Dx: int = 2, Dy: int = 4, M: int = 50
     return y, params
 
 
+def kink_ssm_ext(seed: int = 0, T: int = 40, Dx: int = 2, Dy: int = 3, M: int = 6, Dcon: int = 0,
+                 gp_emi: bool = False, control_to_emi: bool = True):
+    """The kink state-space data of `kink_ssm` with, optionally, control inputs u_t ~ N(0,1)
+    [T, Dcon] added to the dynamics through a random [Dx, Dcon] map, and parameters for a
+    sparse-GP emission (keys `_emission`, `sn_emission`) instead of the linear one.  The
+    transition's inputs are [x_{t-1}, u_{t-1}] (and the emission's [x_t, u_t] with
+    control_to_emi), as the reference's SGPSSM concatenates them.  Returns (y, x_control or
+    None, params)."""
+    rng = np.random.RandomState(seed)
+    mix = np.eye(Dx) + 0.3 * rng.randn(Dx, Dx)
+    Bc = 0.3 * rng.randn(Dx, Dcon) if Dcon else None
+    u = rng.randn(T, Dcon) if Dcon else None
+    x = np.zeros((T, Dx))
+    x[0] = rng.randn(Dx)
+    for t in range(T - 1):
+        f = 0.8 * x[t] + (x[t] + 0.2) * (1 - 5 / (1 + np.exp(-2 * x[t])))
+        if Dcon:
+            f = f + Bc @ u[t]
+        x[t + 1] = np.clip(mix @ f, -4, 4) + 0.05 * rng.randn(Dx)
+    C = rng.randn(Dy, Dx)
+    y = np.tanh(x @ C.T) + 0.1 * rng.randn(T, Dy) if gp_emi else x @ C.T + 0.1 * rng.randn(T, Dy)
+    post_m = x + 0.1 * rng.randn(T, Dx)
+    post_v = 0.1 * np.ones_like(post_m)
+    xin = np.hstack((x, u)) if Dcon else x
+    params = {'sn': np.log(0.05) * np.ones(1),
+              'x_factor_1': (post_m / post_v) / 3,
+              'x_factor_2': np.log((1.0 / post_v) / 3) / 2,
+              'ls_dynamic': np.log(np.std(xin, 0) + 0.5),
+              'sf_dynamic': np.zeros(1),
+              'zu_dynamic': xin[rng.permutation(T - 1)[:M]]}
+    params.update(natural_q_init(rng, M, Dx, '_dynamic'))
+    if gp_emi:
+        xe = np.hstack((x, u)) if (Dcon and control_to_emi) else x
+        params.update({'ls_emission': np.log(np.std(xe, 0) + 0.5), 'sf_emission': np.zeros(1),
+                       'zu_emission': xe[rng.permutation(T)[:M]], 'sn_emission': np.log(0.1) * np.ones(1)})
+        params.update(natural_q_init(rng, M, Dy, '_emission'))
+    else:
+        De = Dx + (Dcon if control_to_emi else 0)     # the linear emission also sees u_t
+        Ce = np.hstack((C, 0.1 * rng.randn(Dy, De - Dx))) if De > Dx else C
+        params.update({'C_emission': Ce + 0.05 * rng.randn(Dy, De), 'R_emission': np.log(0.1) * np.ones(Dy)})
+    return y, u, params
+
+
 def serving_models(seed: int = 0, n_models: int = 32, Ms=(50, 100, 200), D: int = 8, hidden: int = 2,
                    n_fit: int = 2000):
     """Parameters of `n_models` 2-layer deep GPs (input D, hidden width, 1 output) with M drawn in

@@ -164,7 +164,7 @@ typedef struct {
   int ldc;
   long strideC;
 } gpk_gemm_t;
-#define GPK_GEMM_GROUP 8
+#define GPK_GEMM_GROUP 16
 
 /* Up to GPK_GEMM_GROUP independent gpk_gemm_ex products in one launch (the products of one
  * dependency level of the AEP algebra, e.g. mu = Su theta_2 and muhat = beta Suhat theta_2 of
@@ -196,11 +196,13 @@ int gpk_spd_inv(int prec, int batch, int M, const void* A, void* Ainv, double* l
                 void* stream);
 
 /* gpk_spd_inv without a workspace argument and without allocating: the workspace is a
- * file-scope device array of the library (2 MiB), so the limit is M <= 128 and
- * batch*M*M <= 131072 (e.g. 8 matrices of 128 x 128); larger inputs are rejected with
+ * file-scope device array of the library (2 MiB), so the limit is M <= 128, batch <= 65535
+ * and batch*M*M <= 131072 (e.g. 8 matrices of 128 x 128); larger inputs are rejected with
  * GPK_EINVAL.  No counterpart in the reference (an interface of this library only).  The
  * array is one per device and needs no zeroing; calls that overlap on a device (other
- * streams or host threads) race on it. */
+ * streams or host threads) race on it.  The array's address is looked up on the current
+ * device at every call, so `stream` must belong to the current device; the first call on a
+ * device loads the library's module there and should come before any stream capture. */
 int gpk_spd_inv_static(int prec, int batch, int M, const void* A, void* Ainv, double* logdet, int* info,
                        void* stream);
 
@@ -232,6 +234,31 @@ typedef struct {
   double* out;
 } gpk_lincomb_t;
 int gpk_lincomb(const gpk_lincomb_t* desc, void* stream);
+
+/* The posterior and cavity moments of a natural-parameter layer (T = theta_1 [D,M,M],
+ * t = theta_2 [D,M], Su = (K^-1 + T)^-1, Suhat = (K^-1 + beta T)^-1, K = Kuu), in the form that
+ * is accurate for the layer's regime, chosen per output d on the device:
+ *   cavity, when beta max|T_d| <= max|K^-1| (prior-dominated; K^-1 products would cancel):
+ *     Bhat_det = beta^2 T Suhat T - beta T,  Ahat = beta t - beta T muhat
+ *   else (data-dominated; products with T would cancel):
+ *     Bhat_det = K^-1 Suhat K^-1 - K^-1,     Ahat = K^-1 muhat
+ *   posterior likewise with beta = 1: B = T Su T - T or K^-1 Su K^-1 - K^-1, A = t - T mu or K^-1 mu;
+ * and Bhat_sto = Bhat_det + Ahat Ahat^T.  The caller supplies the products of both forms
+ * (Qh = T Suhat T, KShK = K^-1 Suhat K^-1, Qu = T Su T, KSuK = K^-1 Su K^-1 [D,M,M]; Tmh = T muhat,
+ * Kmh = K^-1 muhat, Tmu = T mu, Kmu = K^-1 mu [D,M]); regime[d] (optional) gets bit 0 set for
+ * the cavity's T form and bit 1 for the posterior's.  Elementwise float64.  The same quantities
+ * as geepee/aep_models.py:536-546 and base_models.py:480-488 (which always take the K^-1 form). */
+typedef struct {
+  int D, M;
+  double beta;
+  const double *T, *Kinv, *t;
+  const double *Qh, *KShK, *Qu, *KSuK;
+  const double *Tmh, *Kmh, *Tmu, *Kmu;
+  double *Bd, *Bp, *Bsto, *Ah, *A;
+  int* regime;
+} gpk_forms_t;
+#define GPK_FORMS_MAX 8
+int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream);
 
 /* One dependency level of the AEP algebra in one launch: up to GPK_GEMM_GROUP products (as
  * gpk_gemm_group) and up to GPK_LC_GROUP linear combinations (as gpk_lincomb), all independent
@@ -319,6 +346,37 @@ int gpk_finish(int span, double* g, double divisor, int ninfo, const int* info, 
 int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
                   const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
                   void* stream);
+
+/* ---- fixed-order accumulation (bit-reproducible sums over data points) ----
+ * gpk_psi_bwd_ex, gpk_det_bwd, gpk_gram and gpk_trace_kzz add per-CTA partial sums into their
+ * float64 outputs with atomics, in an order that varies from run to run; the last bits of those
+ * sums vary with it (and the AEP gradients propagate them through ill-conditioned M x M
+ * algebra).  Each *_ws variant below takes a caller-owned float64 workspace instead: every CTA
+ * writes its partial sums there, and a second launch on the same stream adds them into the
+ * outputs in a fixed order with compensated summation, one writer per output element, so
+ * repeated calls on the same inputs give bit-identical outputs.  work = NULL gives the atomic
+ * form.  gpk_work_elems gives the workspace size in float64 elements for operation `op` at the
+ * given sizes on the current device (N rows; D = Q input dimensions; Dout outputs); it may
+ * exceed what one call uses.  No counterpart in the reference (numpy's sums are sequential). */
+#define GPK_OP_PSI_BWD 1
+#define GPK_OP_DET_BWD 2
+#define GPK_OP_GRAM 3
+#define GPK_OP_TRACE_KZZ 4
+int gpk_work_elems(int op, int N, int M, int D, int Dout, long* elems);
+int gpk_psi_bwd_ws(int prec, int N, int M, int Q, int Dout, const void* mu, const void* var,
+                   const void* Z, const double* lls2, const double* lsf2, const void* A,
+                   const void* B, const void* m, const void* dm, const void* dv, const void* dpsi1,
+                   long b_stride, double* dsf2, double* dl, double* dZ, double* dA, double* dB,
+                   void* dmu, void* dvar, double* work, long work_elems, void* stream);
+int gpk_det_bwd_ws(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
+                   const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
+                   const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
+                   double* dA, void* dx, double* work, long work_elems, void* stream);
+int gpk_gram_ws(int prec, int N, int M, int Dout, const void* u, const void* v, const void* w, double* C,
+                double* work, long work_elems, void* stream);
+int gpk_trace_kzz_ws(int prec, int M, int Q, const void* Mm, const void* Z, const double* lls2,
+                     const double* lsf2, double s_sf, double s_ls, double* g_sf, double* g_ls, double* g_z,
+                     double* work, long work_elems, void* stream);
 
 /* Batched inverse and log-determinant of many tiny SPD matrices A[b] (n x n, n <= 8), one
  * thread per matrix; info[b] as in gpk_chol_inv.  Replaces the per-time-step

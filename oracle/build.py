@@ -1,5 +1,7 @@
 """Build the oracle's C restatement (oracle/_build/libpsi_oracle.so) and, when the reference
-sources are mounted, oracle/_ref (the reference's own weave loop).  TEST INFRASTRUCTURE ONLY."""
+sources are present, oracle/_ref (the reference's own code and weave loop).  TEST
+INFRASTRUCTURE ONLY.  The reference checkout is $GEEPEE_REFERENCE, else the read-only mount
+this recipe was written for."""
 from __future__ import annotations
 
 import os
@@ -13,7 +15,12 @@ REF_DIR = os.path.join(HERE, '_ref')
 REF_LIB = os.path.join(REF_DIR, 'psi_weave_ref.so')
 
 
-def build(reference_src: str = '/root/reference') -> dict:
+MOUNT = '/root/reference'
+
+
+def build(reference_src: str | None = None) -> dict:
+    if reference_src is None:
+        reference_src = os.environ.get('GEEPEE_REFERENCE', MOUNT)
     os.makedirs(OUT_DIR, exist_ok=True)
     src = os.path.join(HERE, 'psi_c.c')
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):

@@ -899,12 +899,17 @@ def sgplvm_objective(y, p, alpha, idx=None, prior_mean=0.0, prior_var=1.0,
 
 
 def sgpssm_objective(y, p, alpha, start=None, mb_size=None, prior_mean=0.0, prior_var=1.0,
-                     fixed=()):
-    """``SGPSSM.objective_function`` aep_models.py:1024-1206, linear-Gaussian emission,
-    moment matching, no control inputs.  ``start`` is the window start when minibatching
-    (the reference draws it with ``np.random.randint``, aep_models.py:1051)."""
+                     fixed=(), x_control=None, gp_emi=False, control_to_emi=True):
+    """``SGPSSM.objective_function`` aep_models.py:1024-1206, moment matching.  The emission is
+    linear-Gaussian (Gauss_Emis) or, with ``gp_emi``, a sparse-GP layer (keys ``_emission``)
+    with a Gaussian likelihood (``sn_emission``); ``x_control`` [N, Dc] is appended to the
+    transition's inputs (and the emission's, with ``control_to_emi``) with zero variance
+    (aep_models.py:1069-1082).  ``start`` is the window start when minibatching (the reference
+    draws it with ``np.random.randint``, aep_models.py:1051)."""
     N, Dy = y.shape
     Mz, Dx = _layer_dims(p, '_dynamic')
+    Dcd = 0 if x_control is None else x_control.shape[1]
+    Dce = Dcd if control_to_emi else 0
     if mb_size is None or mb_size >= N:
         emi = np.arange(0, N)
         dyn = np.arange(0, N - 1)
@@ -931,6 +936,12 @@ def sgpssm_objective(y, p, alpha, start=None, mb_size=None, prior_mean=0.0, prio
     mt, vt = cm[dyn + 1], cv[dyn + 1]
     mtm1, vtm1 = cm[dyn], cv[dyn]
     mup, vup = cm[emi], cv[emi]
+    if Dcd:
+        mtm1 = np.hstack((mtm1, x_control[dyn]))
+        vtm1 = np.hstack((vtm1, np.zeros((dyn.shape[0], Dcd))))
+    if Dce:
+        mup = np.hstack((mup, x_control[emi]))
+        vup = np.hstack((vup, np.zeros((emi.shape[0], Dce))))
     mprop, vprop, p1, p2 = fwd_mm(L, mtm1, vtm1)
     # compute_transition_tilted aep_models.py:1317-1374 (2-D case)
     sn = _scalar(p['sn'])
@@ -946,8 +957,21 @@ def sgpssm_objective(y, p, alpha, start=None, mb_size=None, prior_mean=0.0, prio
     dmprop = -dmt
     dsn = dvt.sum() * 2 * sn2 / alpha + s_dyn * mprop.shape[0] * Dx * (1 - alpha)
     gh, gi = bwd_mm(L, N - 1, alpha, mprop, dmprop, dvprop, p1, p2, mtm1, vtm1)
-    logZ_emi, ge_in, ge_hyp = emission_tilted(np.asarray(p['C_emission'], dtype=float),
-                                              p['R_emission'], y[emi], mup, vup, alpha, s_emi)
+    E = None
+    if gp_emi:
+        # the emission factors through a sparse-GP layer and the Gaussian likelihood
+        # (aep_models.py:1100-1112)
+        Me, _ = _layer_dims(p, '_emission')
+        E = layer_cavity(layer_unpack(p, '_emission', Me, Dy), N, alpha)
+        mout, vout, p1e, p2e = fwd_mm(E, mup, vup)
+        lz, dme, dve = gauss_logZ(mout, vout, y[emi], p['sn_emission'], alpha)
+        logZ_emi = s_emi * lz
+        gh_e, ge_in = bwd_mm(E, N, alpha, mout, s_emi * dme, s_emi * dve, p1e, p2e, mup, vup)
+        ge_hyp = dict(gh_e)
+        ge_hyp['sn'] = gauss_dsn(dve, emi.shape[0], Dy, p['sn_emission'], alpha, s_emi)
+    else:
+        logZ_emi, ge_in, ge_hyp = emission_tilted(np.asarray(p['C_emission'], dtype=float),
+                                                  p['R_emission'], y[emi], mup, vup, alpha, s_emi)
     grads = {'sn': dsn}
     for k, val in gh.items():
         grads[k + '_dynamic'] = val
@@ -989,6 +1013,8 @@ def sgpssm_objective(y, p, alpha, start=None, mb_size=None, prior_mean=0.0, prio
     phi_post_x = np.sum(sp * 0.5 * (post1 ** 2 / post2 - np.log(post2)))
     phi_cav_x = np.sum(sc * 0.5 * (cav1 ** 2 / cav2 - np.log(cav2)))
     energy = logZ_dyn + logZ_emi + phi_prior_x + phi_post_x + phi_cav_x + layer_phi(L, N - 1, alpha)
+    if E is not None:
+        energy = energy + layer_phi(E, N, alpha)
     return _finish(energy, grads, N, fixed)
 
 

@@ -5,7 +5,7 @@ links or runs anything under ``oracle/``.
 
 The reference (thangbui/geepee) is Python 2 code whose only native part is a
 ``scipy.weave`` C++ loop; neither Python 2 nor weave exists in this image.  This
-script reads the reference sources from ``--src`` (default: the read-only mount)
+script reads the reference sources from ``--src`` (default: ``$GEEPEE_REFERENCE``)
 and writes two artefacts into ``oracle/_ref/`` (git-ignored, never committed):
 
 1. ``oracle/_ref/geepee_ref/`` - a Python 3 / numpy 2 package made from
@@ -28,7 +28,7 @@ and writes two artefacts into ``oracle/_ref/`` (git-ignored, never committed):
    wrapped in a C function with blitz-style ``a(i, j)`` accessors, so that the
    reference's own native loop can be compiled with g++ and timed/checked.
 
-Usage:  python oracle/make_ref.py [--src /path/to/reference]
+Usage:  python oracle/make_ref.py --src /path/to/reference   (or set GEEPEE_REFERENCE)
 """
 from __future__ import annotations
 
@@ -111,7 +111,8 @@ def _extract_weave_body(kernels_src: str) -> str:
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=os.environ.get("GEEPEE_REFERENCE"), required=not os.environ.get("GEEPEE_REFERENCE"),
+                    help="the reference checkout (default: $GEEPEE_REFERENCE)")
     args = ap.parse_args(argv)
     src = os.path.join(args.src, "geepee")
     if not os.path.isdir(src):

@@ -48,7 +48,8 @@ def _weave_psi(lib, lls2, lsf2, mu, S, Z):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('--src', default='/root/reference')
+    ap.add_argument('--src', default=os.environ.get('GEEPEE_REFERENCE'), required=not os.environ.get('GEEPEE_REFERENCE'),
+                    help='the reference checkout (default: $GEEPEE_REFERENCE)')
     args = ap.parse_args(argv)
     subprocess.check_call([sys.executable, os.path.join(ROOT, 'oracle', 'make_ref.py'),
                            '--src', args.src])

@@ -30,7 +30,8 @@ def _labels(rng, shape):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('--src', default='/root/reference')
+    ap.add_argument('--src', default=os.environ.get('GEEPEE_REFERENCE'), required=not os.environ.get('GEEPEE_REFERENCE'),
+                    help='the reference checkout (default: $GEEPEE_REFERENCE)')
     args = ap.parse_args(argv)
     if not os.path.isdir(os.path.join(REF, 'geepee_ref')):
         subprocess.check_call([sys.executable, os.path.join(ROOT, 'oracle', 'make_ref.py'), '--src', args.src])

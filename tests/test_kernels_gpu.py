@@ -56,6 +56,27 @@ def test_kfu_derivatives_and_trace_golden():
         assert_close(val, g['t_' + name], 1e-9, name)
 
 
+def test_single_point_and_gpy_aliases_golden():
+    """The reference's single-point, weave-variant and GPy-style entry points
+    (geepee/kernels.py:24-176, 243-299, 317-352) against the reference's own outputs
+    (tests/golden/make_aliases.py); the weave variants return the same quantities as the numpy
+    single-point functions."""
+    from geepee_gb300 import kernels as K
+    g = load('kernels_aliases.npz')
+    lls, lsf, z, xm, xv = g['lls'], g['lsf'], g['z'], g['xm'], g['xv']
+    assert_close(K.compute_kernel_diag(lls, lsf, g['x']), g['kdiag'], 1e-15, 'kdiag')
+    assert_close(K.grad_x(lls, lsf, g['x'], z), g['gradx'], DF64_TOL, 'grad_x')
+    assert_close(K.compute_psi1(lls, lsf, xm, xv, z), g['psi1'], DF64_TOL, 'psi1')
+    assert_close(K.compute_psi2(lls, lsf, xm, xv, z), g['psi2'], DF64_TOL, 'psi2')
+    assert_close(K.compute_psi1_weave(lls, lsf, xm, xv, z), g['psi1'][0], DF64_TOL, 'psi1 weave')
+    assert_close(K.compute_psi2_weave(lls, lsf, xm, xv, z), g['psi2'], DF64_TOL, 'psi2 weave')
+    p1, p2 = K.compute_psi_weave_single(lls, lsf, xm, xv, z)
+    assert_close(p1, g['psi1'][0], DF64_TOL, 'psi1 single')
+    assert_close(p2, g['psi2'], DF64_TOL, 'psi2 single')
+    assert_close(K.psi1computations(float(g['var']), g['ell'], z, g['mu'], g['S']), g['g_psi1'], DF64_TOL, 'gpy psi1')
+    assert_close(K.psi2computations(float(g['var']), g['ell'], z, g['mu'], g['S']), g['g_psi2'], DF64_TOL, 'gpy psi2')
+
+
 @pytest.mark.parametrize('M,Q,Dout,N', [(24, 5, 2, 200), (1, 1, 1, 3), (33, 3, 1, 17), (100, 2, 1, 300),
                                         (127, 8, 3, 40)])
 def test_psi_fused_fwd_bwd_vs_oracle(M, Q, Dout, N):
@@ -108,6 +129,54 @@ def test_psi_fp32_within_tolerance():
                 f(wl['Bhat']), psi1=psi1, psi2_sum=ssum, m_out=m, v_out=v)
     assert_close(psi1.double().cpu().numpy(), g['psi1'], FP32_TOL, 'psi1 fp32')
     assert_close(ssum.cpu().numpy(), g['psi2_sum'], FP32_TOL, 'psi2 sum fp32')
+
+
+# FP32 gradients of the psi statistics at the full workload: sums over 10000 points of terms
+# with mixed signs; FP32's unit roundoff (6e-8) times the sums' cancellation (~10^2 for dZ and
+# dl) bounds them near 1e-5, so 1e-4 is allowed there (the statistics themselves meet 1e-5)
+FP32_GRAD_TOL = 1e-4
+
+
+@pytest.mark.parametrize('prec', ['df64', 'fp32'])
+def test_psi_full_workload_vs_reference(prec):
+    """The psi-statistics workload at its full size (N=10000, Q=5, M=100, one output) against the
+    reference's own weave loop and compute_psi_derivatives (tests/golden/make_psi_c2.py): psi1,
+    sum_n psi2, the moment contraction m, v, and every gradient, the backward with fixed-order
+    sums.  df64 within 1e-10; FP32 statistics within 1e-5 and gradients within 1e-4."""
+    from geepee_gb300 import gpk, workloads as W
+    g = load('psi_c2.npz')
+    N, Q, M = int(g['N']), int(g['Q']), int(g['M'])
+    wl = W.psi_workload(seed=int(g['seed']), N=N, Q=Q, M=M, Dout=1)
+    dt = torch.float64 if prec == 'df64' else torch.float32
+    tol = DF64_TOL if prec == 'df64' else FP32_TOL
+    gtol = DF64_TOL if prec == 'df64' else FP32_GRAD_TOL
+    t = {k: dev(wl[k], dt) for k in ('mu', 'S', 'Z', 'Ahat', 'Bhat', 'dm', 'dv')}
+    l2, s2 = dev(2 * wl['ls']), dev(2 * wl['sf'])
+    psi1 = torch.empty((N, M), dtype=dt, device='cuda')
+    ssum = torch.zeros((M, M), dtype=torch.float64, device='cuda')
+    m = torch.empty((N, 1), dtype=dt, device='cuda')
+    v = torch.empty_like(m)
+    gpk.psi_fwd(t['mu'], t['S'], t['Z'], l2, s2, t['Ahat'], t['Bhat'], psi1=psi1, psi2_sum=ssum, m_out=m, v_out=v)
+    pick = np.arange(0, N, int(g['step']))
+    np64 = lambda x: x.double().cpu().numpy()
+    assert_close(np64(psi1)[pick], g['pt_psi1'], tol, 'psi1')
+    assert_close(np64(psi1).sum(0), g['psi1_sum'], tol, 'sum psi1')
+    assert_close(np64(ssum), g['psi2_sum'], tol, 'sum psi2')
+    assert_close(np64(m)[pick], g['pt_m'], tol, 'm')
+    assert_close(np64(v)[pick], g['pt_v'], tol, 'v')
+    assert abs(float(np64(v).sum()) - float(g['v_sum'])) <= tol * abs(float(g['v_sum']))
+    # the backward at the reference's m, so that both sides see the same upstream gradients
+    m_dev = dev(g['m_full'], dt)
+    z = lambda *sh: torch.zeros(sh, dtype=torch.float64, device='cuda')
+    out = dict(dsf2=z(1), dl=z(Q), dZ=z(M, Q), dA=z(1, M), dB=z(1, M, M))
+    dmu, dS = torch.empty((N, Q), dtype=dt, device='cuda'), torch.empty((N, Q), dtype=dt, device='cuda')
+    work = z(gpk.work_elems(gpk.OP_PSI_BWD, N, M, Q, 1))
+    gpk.psi_bwd(t['mu'], t['S'], t['Z'], l2, s2, t['Ahat'], t['Bhat'], m_dev, t['dm'], t['dv'], out['dsf2'],
+                out['dl'], out['dZ'], out['dA'], out['dB'], dmu, dS, work=work)
+    for name in ('dsf2', 'dl', 'dZ', 'dA', 'dB'):
+        assert_close(out[name].cpu().numpy(), g[name], gtol, name)
+    assert_close(np64(dmu)[pick], g['pt_dmu'], gtol, 'dmu')
+    assert_close(np64(dS)[pick], g['pt_dS'], gtol, 'dS')
 
 
 @pytest.mark.parametrize('with_L', [True, False])

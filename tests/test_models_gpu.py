@@ -1,13 +1,10 @@
 """GPU parity of the AEP models (objective, gradients, predictions) against the reference's
 golden fixtures.  Energies and predictive moments: rel <= 1e-6 (spec tolerance).
-Gradients: per key, error against the long-double truth within max(1e-6, 256 x the reference's
-own float64 error) - the reference is itself only accurate to ~1e-3 on ill-conditioned layers
-(cond(Kuu) ~ 1e7), and double-float's unit roundoff (2^-48) is 32x float64's (2^-53).  The
-pseudo-input gradients amplify rounding by ~1e11-1e13 and their per-CTA partial sums are added
-by float64 atomics in an order that varies from run to run: on the c1 SGPR the zu gradient's
-error against the truth was measured between 2.3e-3 and 4.6e-3 over eight evaluations of the
-same parameters (80-160x the reference's 2.9e-5; the energy was bit-identical), so the factor
-is 8x the unit-roundoff ratio.  Every other key is below 1e-6."""
+Gradients: per key, error against the long-double truth within max(1e-6, 4 x the reference's
+own float64 error).  The reference is itself only accurate to ~1e-3 on the deep GP's second
+layer (cond(Kuu) ~ 7e6): its gradient w.r.t. Kuu goes through products with Kuu^-1 that cancel
+by ~1e5.  The layers here form that gradient without Kuu^-1 and sum over data points in a fixed
+order, so their gradients are closer to the truth than the reference's and bit-reproducible."""
 import numpy as np
 import pytest
 import torch
@@ -20,7 +17,7 @@ pytestmark = pytest.mark.gpu
 E_TOL = 1e-6
 P_TOL = 1e-6
 G_TOL = 1e-6
-G_FACTOR = 256.0
+G_FACTOR = 4.0
 
 
 def _energy_ok(e, ref):
@@ -94,6 +91,29 @@ def test_sdgpr_c3_objective_predict():
         assert_close(v, g[k], P_TOL, k)
 
 
+@pytest.mark.parametrize('case', ['c1', 'c3'])
+def test_gradients_bit_reproducible(case):
+    """Eight evaluations of the same parameters (and minibatch) give bit-identical energies and
+    gradients: every sum over data points is formed in a fixed order."""
+    from geepee_gb300 import aep_models as A, workloads as W
+    if case == 'c1':
+        x, y, p, _ = W.sgpr_1d(seed=0)
+        mdl, mb = A.SGPR(x, y, 30), 1000
+    else:
+        x, y = W.dgp_regression(seed=0)
+        p = sub(load('sdgpr_c3.npz'), 'p_')
+        mdl, mb = A.SDGPR(x, y, 100, [2]), 1000
+    runs = []
+    for _ in range(8):
+        np.random.seed(2)
+        runs.append(mdl.objective_function({k: np.copy(v) for k, v in p.items()}, mb, alpha=0.5))
+    e0, g0 = runs[0]
+    for e, gr in runs[1:]:
+        assert e == e0
+        for k in g0:
+            assert np.array_equal(np.asarray(gr[k]), np.asarray(g0[k])), k
+
+
 def test_graph_replay_matches_eager_and_tracks_params():
     """The captured graph must recompute from the current parameter buffers."""
     from geepee_gb300 import aep_models as A
@@ -108,7 +128,7 @@ def test_graph_replay_matches_eager_and_tracks_params():
     e3, g3 = eager.objective_function(p2, 10, alpha=1.0)
     assert e1 != e2
     assert abs(e2 - e3) <= 1e-13 * abs(e3)
-    for k in g3:   # float64 atomics make the summation order (last bits) vary run to run
+    for k in g3:
         assert_close(g2[k], g3[k], 1e-10, k)
     ref = O.sdgpr_objective(g['x'], g['y'], p2, 1.0)
     assert abs(e2 - ref[0]) <= 1e-8 * abs(ref[0])
@@ -249,6 +269,88 @@ def test_sgpssm_small():
     ref = sub(g, 'gmb_')
     for k in ref:
         assert_close(gr[k], ref[k], 1e-5, 'sgpssm mb ' + k)
+
+
+def test_sgpssm_full_size():
+    """The GP state-space model at its full size: T=5000 steps of the kink dynamics, Dx=2, Dy=4,
+    M=50 transition pseudo-inputs, alpha=0.5, full batch, against the reference's own objective
+    (tests/golden/make_sgpssm_c4.py)."""
+    from geepee_gb300 import aep_models as A, workloads as W
+    g = load('sgpssm_c4.npz')
+    y, p = W.kink_ssm(seed=int(g['seed']), T=int(g['T']), Dx=int(g['Dx']), Dy=int(g['Dy']), M=int(g['M']))
+    mdl = A.SGPSSM(y, int(g['Dx']), int(g['M']), gp_emi=False)
+    e, gr = mdl.objective_function({k: np.copy(v) for k, v in p.items()}, int(g['T']), alpha=float(g['alpha']))
+    _energy_ok(e, g['energy'])
+    assert_truth_close(gr, sub(g, 'g_'), sub(g, 't_'), G_TOL, G_FACTOR, 'sgpssm c4')
+
+
+@pytest.mark.parametrize('case', ['gpemi', 'control', 'gpemi_control'])
+def test_sgpssm_gp_emission_and_control(case):
+    """The GP state-space model with a sparse-GP emission (the reference's
+    tests/test_grads_aep.py:393-410 case), with control inputs, and with both, against the
+    reference's own objective (tests/golden/make_sgpssm_ext.py): full batch and a window of 15
+    steps drawn as the reference draws it; the posterior emission predictions and, for the GP
+    emission, a 6-step forecast."""
+    from geepee_gb300 import aep_models as A, workloads as W
+    g = load('sgpssm_ext.npz')
+    seed, T, Dx, Dy, M, Dc, gp = (int(v) for v in g[case + '_case'])
+    y, u, p = W.kink_ssm_ext(seed=seed, T=T, Dx=Dx, Dy=Dy, M=M, Dcon=Dc, gp_emi=bool(gp))
+    mdl = A.SGPSSM(y, Dx, M, x_control=u, gp_emi=bool(gp))
+    cp = lambda q: {k: np.copy(v) for k, v in q.items()}
+    e, gr = mdl.objective_function(cp(p), T, alpha=0.5)
+    _energy_ok(e, float(np.ravel(g[case + '_energy'])[0]))
+    assert_truth_close(gr, sub(g, case + '_g_'), sub(g, case + '_t_'), G_TOL, G_FACTOR, case)
+    np.random.seed(31)
+    e, gr = mdl.objective_function(cp(p), 15, alpha=0.5)
+    _energy_ok(e, float(np.ravel(g[case + '_energy_mb'])[0]))
+    for k, ref in sub(g, case + '_gmb_').items():
+        assert_close(gr[k], ref, 1e-5, case + ' mb ' + k)
+    mdl.update_hypers(cp(p))
+    for k, val in zip(('py_m', 'py_vf', 'py_vy'), mdl.get_posterior_y()):
+        assert_close(val, g[case + '_' + k], P_TOL, case + ' ' + k)
+    if gp:
+        uf = g[case + '_fc_u'] if Dc else None
+        for k, val in zip(('fc_mx', 'fc_vx', 'fc_my', 'fc_vyn', 'fc_vy'), mdl.predict_forward(6, uf)):
+            assert_close(val, g[case + '_' + k], P_TOL, case + ' ' + k)
+
+
+def test_sdgpr_c3_finite_differences():
+    """Central finite differences (eps = 1e-6) on 50 random parameter coordinates of the deep GP
+    at its full configuration (N=20000, M=100, minibatch 1000, the same minibatch for every
+    evaluation), with the rule of the reference's check_grad (tests/test_utils.py:49-128 of the
+    reference): rel diff < 1e-4, or |numerical| < 1e-4 and rel diff <= 1.1; plus the
+    difference's own resolution, 8 x 2^-48 |E| / eps (the double-float energy resolves ~2^-46)."""
+    from geepee_gb300 import aep_models as A, workloads as W
+    g = load('sdgpr_c3.npz')
+    x, y = W.dgp_regression(seed=0)
+    mdl = A.SDGPR(x, y, 100, [2])
+    p = {k: np.array(v, dtype=float) for k, v in sub(g, 'p_').items()}
+    eps = 1e-6
+
+    def f(q):
+        np.random.seed(2)
+        return mdl.objective_function(q, 1000, alpha=0.5)
+
+    e0, gr = f(p)
+    res = 8 * 2.0 ** -48 * abs(e0) / eps
+    rng = np.random.RandomState(0)
+    keys = sorted(p)
+    sizes = [np.size(p[k]) for k in keys]
+    bad = []
+    for fl in rng.choice(sum(sizes), 50, replace=False):
+        ki = int(np.searchsorted(np.cumsum(sizes), fl, side='right'))
+        k = keys[ki]
+        j = fl - (np.cumsum(sizes)[ki - 1] if ki else 0)
+        pp = {kk: np.array(vv, copy=True) for kk, vv in p.items()}
+        pm = {kk: np.array(vv, copy=True) for kk, vv in p.items()}
+        pp[k].flat[j] += eps
+        pm[k].flat[j] -= eps
+        num = (f(pp)[0] - f(pm)[0]) / (2 * eps)
+        ana = float(np.ravel(gr[k])[j])
+        diff = (ana - num) / num if num != 0 else np.inf
+        if not (abs(diff) < 1e-4 or (abs(num) < 1e-4 and abs(diff) <= 1.1) or abs(ana - num) <= res):
+            bad.append((k, int(j), ana, num, diff))
+    assert not bad, bad
 
 
 @pytest.mark.parametrize('alpha', [1.0, 0.5])

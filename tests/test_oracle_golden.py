@@ -275,3 +275,61 @@ def test_sgpssm_forecast_mc_and_posterior_y():
         assert_close(got, g[name], 1e-10, name)
     for name, got in zip(('post_y_m', 'post_y_vf', 'post_y_vyn'), O.sgpssm_posterior_y(p)):
         assert_close(got, g[name], 1e-12, name)
+
+
+def test_oracle_psi_full_workload_points():
+    """The oracle's psi statistics and derivatives against the reference's (weave loop and
+    compute_psi_derivatives) on the sampled points of the full psi workload (N=10000, Q=5,
+    M=100; tests/golden/make_psi_c2.py).  The per-point quantities depend on their own point
+    only, so the sample is checked exactly as the full run computed it."""
+    from geepee_gb300 import workloads as W
+    g = load('psi_c2.npz')
+    N, Q, M = int(g['N']), int(g['Q']), int(g['M'])
+    wl = W.psi_workload(seed=int(g['seed']), N=N, Q=Q, M=M, Dout=1)
+    pick = np.arange(0, N, int(g['step']))
+    mu, S = wl['mu'][pick], wl['S'][pick]
+    p1, p2 = O.psi_stats(2 * wl['ls'], 2 * wl['sf'], mu, S, wl['Z'])
+    A, B = wl['Ahat'], wl['Bhat']
+    sf2 = float(np.exp(2 * wl['sf'][0]))
+    m = p1 @ A.T
+    v = sf2 + np.einsum('dab,nab->nd', B, p2) - m ** 2
+    assert_close(p1, g['pt_psi1'], 1e-12, 'psi1')
+    assert_close(m, g['pt_m'], 1e-12, 'm')
+    assert_close(v, g['pt_v'], 1e-12, 'v')
+    dm, dv = wl['dm'][pick], wl['dv'][pick]
+    dm_all = dm - 2 * dv * m
+    r = O.psi_derivatives(dm_all @ A, p1, np.einsum('nd,dab->nab', dv, B), p2, np.exp(wl['ls']), sf2, mu, S,
+                          wl['Z'])
+    assert_close(r[3], g['pt_dmu'], 1e-11, 'dmu')
+    assert_close(r[4], g['pt_dS'], 1e-11, 'dS')
+
+
+def test_oracle_sgpssm_full_size():
+    """The oracle's GP state-space objective at its full size (T=5000, Dx=2, Dy=4, M=50) against
+    the reference's (tests/golden/make_sgpssm_c4.py): the energy, and per gradient key an error
+    against the long-double truth no larger than the reference's own (or 1e-8)."""
+    from geepee_gb300 import workloads as W
+    g = load('sgpssm_c4.npz')
+    y, p = W.kink_ssm(seed=int(g['seed']), T=int(g['T']), Dx=int(g['Dx']), Dy=int(g['Dy']), M=int(g['M']))
+    e, gr = O.sgpssm_objective(y, p, float(g['alpha']))
+    assert abs(e - g['energy']) <= 1e-8 * abs(g['energy'])
+    assert_truth_close(gr, sub(g, 'g_'), sub(g, 't_'), 1e-8, 1.0, 'sgpssm c4 oracle')
+
+
+@pytest.mark.parametrize('case', ['gpemi', 'control', 'gpemi_control'])
+def test_oracle_sgpssm_gp_emission_and_control(case):
+    """The oracle's GP state-space objective with a sparse-GP emission and/or control inputs
+    against the reference's (tests/golden/make_sgpssm_ext.py): full batch and a window of 15."""
+    from geepee_gb300 import workloads as W
+    g = load('sgpssm_ext.npz')
+    seed, T, Dx, Dy, M, Dc, gp = (int(v) for v in g[case + '_case'])
+    y, u, p = W.kink_ssm_ext(seed=seed, T=T, Dx=Dx, Dy=Dy, M=M, Dcon=Dc, gp_emi=bool(gp))
+    e, gr = O.sgpssm_objective(y, p, 0.5, x_control=u, gp_emi=bool(gp))
+    ref = float(np.ravel(g[case + '_energy'])[0])
+    assert abs(e - ref) <= 1e-9 * abs(ref), (e, ref)
+    assert_truth_close(gr, sub(g, case + '_g_'), sub(g, case + '_t_'), 1e-8, 2.0, case)
+    start = int(g[case + '_mb_start'])
+    e, gr = O.sgpssm_objective(y, p, 0.5, start=start, mb_size=15, x_control=u, gp_emi=bool(gp))
+    ref = float(np.ravel(g[case + '_energy_mb'])[0])
+    assert abs(e - ref) <= 1e-9 * abs(ref), (e, ref)
+    assert_dict_close(gr, sub(g, case + '_gmb_'), 1e-5, case + ' mb')

@@ -18,27 +18,44 @@ def _spd(rng, batch, M):
     return K + np.stack([np.diag(rng.rand(M)) for _ in range(batch)])
 
 
-def test_spd_inv_static_matches_workspace_entry_twice():
-    from geepee_gb300._lib import call, ptr, stream, GPK_DF64
+@pytest.mark.parametrize('prec', ['df64', 'fp32'])
+def test_spd_inv_static_matches_workspace_entry_twice(prec):
+    """Several calls in a row (every size branch of the factor kernel: M <= 32, <= 64, <= 100,
+    128, and a many-matrix batch of small M) give the workspace entry point's results bit for
+    bit, and allocate no device memory."""
+    from geepee_gb300._lib import call, ptr, stream, GPK_DF64, GPK_FP32
+    p, dt = (GPK_DF64, torch.float64) if prec == 'df64' else (GPK_FP32, torch.float32)
     rng = np.random.RandomState(5)
-    for batch, M in ((3, 100), (8, 128)):   # two calls in a row, the second at the size limit
-        A = dev(_spd(rng, batch, M))
+    # one call before the memory checks: the driver loads the library's module data (the
+    # array itself) on first use of the symbol, which is not an allocation by the entry point
+    A0 = dev(_spd(rng, 1, 8)).to(dt)
+    out0 = torch.empty_like(A0)
+    ld0 = torch.empty(1, dtype=torch.float64, device='cuda')
+    info0 = torch.empty(1, dtype=torch.int32, device='cuda')
+    call('gpk_spd_inv_static', p, 1, 8, ptr(A0), ptr(out0), ptr(ld0), ptr(info0), stream())
+    for batch, M in ((3, 100), (8, 128), (512, 16), (20, 60), (64, 30)):
+        A = dev(_spd(rng, batch, M)).to(dt)
         inv_ref, inv = torch.empty_like(A), torch.empty_like(A)
         ld_ref = torch.empty(batch, dtype=torch.float64, device='cuda')
         ld = torch.empty_like(ld_ref)
         info_ref = torch.empty(batch, dtype=torch.int32, device='cuda')
         info = torch.empty_like(info_ref)
-        work = torch.empty((2 * batch, M, M), dtype=torch.float64, device='cuda')
-        call('gpk_spd_inv', GPK_DF64, batch, M, ptr(A), ptr(inv_ref), ptr(ld_ref), ptr(info_ref), ptr(work),
-             stream())
-        call('gpk_spd_inv_static', GPK_DF64, batch, M, ptr(A), ptr(inv), ptr(ld), ptr(info), stream())
+        work = torch.empty((2 * batch, M, M), dtype=dt, device='cuda')
+        call('gpk_spd_inv', p, batch, M, ptr(A), ptr(inv_ref), ptr(ld_ref), ptr(info_ref), ptr(work), stream())
         torch.cuda.synchronize()
+        used = torch.cuda.memory_allocated()
+        free0 = torch.cuda.mem_get_info()[0]
+        call('gpk_spd_inv_static', p, batch, M, ptr(A), ptr(inv), ptr(ld), ptr(info), stream())
+        torch.cuda.synchronize()
+        assert torch.cuda.memory_allocated() == used
+        assert torch.cuda.mem_get_info()[0] == free0
         assert info.cpu().tolist() == [0] * batch and info_ref.cpu().tolist() == [0] * batch
         assert torch.equal(inv, inv_ref)
         assert torch.equal(ld, ld_ref)
-        ref = np.linalg.inv(A.cpu().numpy())
-        err = np.abs(inv.cpu().numpy() - ref).max() / np.abs(ref).max()
-        assert err < 1e-13 * max(np.linalg.cond(A[0].cpu().numpy()), 1.0)
+        if prec == 'df64':
+            ref = np.linalg.inv(A.cpu().numpy())
+            err = np.abs(inv.cpu().numpy() - ref).max() / np.abs(ref).max()
+            assert err < 1e-13 * max(np.linalg.cond(A[0].cpu().numpy()), 1.0)
 
 
 def test_spd_inv_static_rejects_oversize():
@@ -46,3 +63,4 @@ def test_spd_inv_static_rejects_oversize():
     L = lib()
     assert L.gpk_spd_inv_static(GPK_DF64, 9, 128, None, None, None, None, None) == -1
     assert L.gpk_spd_inv_static(GPK_DF64, 1, 129, None, None, None, None, None) == -1
+    assert L.gpk_spd_inv_static(GPK_DF64, 65536, 1, None, None, None, None, None) == -1
