@@ -64,6 +64,7 @@ _SIGS = {
     'gpk_aep_phi': [_c_int, _c_int, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _vp, _vp],
     'gpk_work_elems': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp],
     'gpk_cavity_forms': [_c_int, _vp, _vp],
+    'gpk_regime': [_c_int, _c_int, _c_dbl, _vp, _vp, _vp, _vp],
 }
 # the fixed-order variants: the atomic form's arguments, then (work, work_elems) before the stream
 for _n in ('gpk_psi_bwd_ex', 'gpk_det_bwd', 'gpk_gram', 'gpk_trace_kzz'):

@@ -372,15 +372,23 @@ __device__ long long maxabs_bits(const double* x, long n, long long* red) {
   return r;
 }
 
+// one CTA per output d: bit 0 = beta max|T_d| <= max|K^-1|, bit 1 = max|T_d| <= max|K^-1|
+__global__ void __launch_bounds__(256) regime_kernel(int M, double beta, const double* T, const double* Kinv,
+                                                      int* flags) {
+  __shared__ long long red[8];
+  const long MM = (long)M * M;
+  const double tmax = __longlong_as_double(maxabs_bits(T + blockIdx.x * MM, MM, red));
+  const double kmax = __longlong_as_double(maxabs_bits(Kinv, MM, red));
+  if (threadIdx.x == 0) flags[blockIdx.x] = (beta * tmax <= kmax ? 1 : 0) | (tmax <= kmax ? 2 : 0);
+}
+
 struct FormsArgs {
   int n, chunks;      // items; CTAs per (item, d)
   gpk_forms_t it[GPK_FORMS_MAX];
 };
 
-// CTA (c, j): flattened (item, d) = c, element chunk j of that output's M x M block.  Every CTA
-// decides the regime itself (two max-abs scans), so no CTA waits for another.
+// CTA (c, j): flattened (item, d) = c, element chunk j of that output's M x M block
 __global__ void __launch_bounds__(256) cavity_forms_kernel(FormsArgs f) {
-  __shared__ long long red[8];
   int c = blockIdx.x / f.chunks;
   const int j = blockIdx.x - c * f.chunks;
   int k = 0;
@@ -389,30 +397,28 @@ __global__ void __launch_bounds__(256) cavity_forms_kernel(FormsArgs f) {
   const gpk_forms_t& g = f.it[k];
   const int d = c, M = g.M;
   const long MM = (long)M * M;
-  const double* T = g.T + d * MM;
-  const long long tb = maxabs_bits(T, MM, red), kb = maxabs_bits(g.Kinv, MM, red);
-  const double tmax = __longlong_as_double(tb), kmax = __longlong_as_double(kb);
-  const bool wc = g.beta * tmax <= kmax, wp = tmax <= kmax;
+  const int fl = g.flags[d];
+  const bool wc = fl & 1, wp = fl & 2;
   const double b = g.beta;
-  const double *t = g.t + (long)d * M, *Tmh = g.Tmh + (long)d * M, *Kmh = g.Kmh + (long)d * M;
-  const double *Tmu = g.Tmu + (long)d * M, *Kmu = g.Kmu + (long)d * M;
+  const double* T = g.T + d * MM;
+  const double *t = g.t + (long)d * M, *vh = g.vh + (long)d * M, *vu = g.vu + (long)d * M;
   if (j == 0) {
     for (int i = threadIdx.x; i < M; i += blockDim.x) {
-      g.Ah[(long)d * M + i] = wc ? b * t[i] - b * Tmh[i] : Kmh[i];
-      g.A[(long)d * M + i] = wp ? t[i] - Tmu[i] : Kmu[i];
+      g.Ah[(long)d * M + i] = wc ? b * t[i] - b * vh[i] : vh[i];
+      g.A[(long)d * M + i] = wp ? t[i] - vu[i] : vu[i];
     }
-    if (threadIdx.x == 0 && g.regime) g.regime[d] = (wc ? 1 : 0) | (wp ? 2 : 0);
   }
   const long e0 = MM * j / f.chunks, e1 = MM * (j + 1) / f.chunks;
   const long o = d * MM;
   for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int r = (int)(e / M), q = (int)(e - (long)r * M);
-    const double bd = wc ? b * b * g.Qh[o + e] - b * T[e] : g.KShK[o + e] - g.Kinv[e];
+    const double bd = wc ? b * b * g.Qh[o + e] - b * T[e] : g.Qh[o + e] - g.Kinv[e];
     g.Bd[o + e] = bd;
-    g.Bp[o + e] = wp ? g.Qu[o + e] - T[e] : g.KSuK[o + e] - g.Kinv[e];
-    const double ar = wc ? b * t[r] - b * Tmh[r] : Kmh[r];
-    const double aq = wc ? b * t[q] - b * Tmh[q] : Kmh[q];
+    g.Bp[o + e] = wp ? g.Qu[o + e] - T[e] : g.Qu[o + e] - g.Kinv[e];
+    const double ar = wc ? b * t[r] - b * vh[r] : vh[r];
+    const double aq = wc ? b * t[q] - b * vh[q] : vh[q];
     g.Bsto[o + e] = bd + ar * aq;
+    g.G[o + e] = wc ? (r == q ? 1.0 : 0.0) - b * g.Ph[o + e] : g.Ph[o + e];
   }
 }
 
@@ -581,6 +587,15 @@ extern "C" int gpk_finish(int span, double* g, double divisor, int ninfo, const 
   return gpk::check_launch("finish");
 }
 
+extern "C" int gpk_regime(int D, int M, double beta, const double* T, const double* Kinv, int* flags,
+                          void* stream) {
+  GPK_NVTX("gpk_regime");
+  GPK_REQUIRE(D >= 1 && D <= 65535 && M >= 1, "regime: bad sizes D=%d M=%d", D, M);
+  GPK_REQUIRE(T && Kinv && flags, "regime: null pointer");
+  regime_kernel<<<D, 256, 0, gpk::as_stream(stream)>>>(M, beta, T, Kinv, flags);
+  return gpk::check_launch("regime");
+}
+
 extern "C" int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream) {
   GPK_NVTX("gpk_cavity_forms");
   GPK_REQUIRE(n >= 0 && n <= GPK_FORMS_MAX && (n == 0 || items), "cavity_forms: %d items (max %d)", n, GPK_FORMS_MAX);
@@ -591,16 +606,16 @@ extern "C" int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream) {
   for (int i = 0; i < n; ++i) {
     const gpk_forms_t& g = items[i];
     GPK_REQUIRE(g.D >= 1 && g.M >= 1, "cavity_forms: item %d: bad sizes D=%d M=%d", i, g.D, g.M);
-    GPK_REQUIRE(g.T && g.Kinv && g.t && g.Qh && g.KShK && g.Qu && g.KSuK && g.Tmh && g.Kmh && g.Tmu && g.Kmu &&
-                    g.Bd && g.Bp && g.Bsto && g.Ah && g.A,
+    GPK_REQUIRE(g.T && g.Kinv && g.t && g.Qh && g.Qu && g.vh && g.vu && g.Ph && g.flags && g.Bd && g.Bp && g.Bsto &&
+                    g.Ah && g.A && g.G,
                 "cavity_forms: item %d: null pointer", i);
     f.it[i] = g;
     total += g.D;
     MM = (long)g.M * g.M > MM ? (long)g.M * g.M : MM;
   }
   if (total == 0) return GPK_OK;
-  // about two waves of 256-thread CTAs over the largest block
-  long ch = (MM + 2047) / 2048;
+  // 256-element chunks of each output's block, up to about two CTAs per SM in all
+  long ch = (MM + 255) / 256;
   const long cap = (2L * gpk::sm_count() + total - 1) / total;
   f.chunks = (int)(ch < 1 ? 1 : (ch > cap ? cap : ch));
   cavity_forms_kernel<<<total * f.chunks, 256, 0, gpk::as_stream(stream)>>>(f);

@@ -37,8 +37,8 @@ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 // Fixed-order accumulation.  A kernel of the deterministic path writes its per-CTA partial sums
 // to a workspace, part[c * stride + j] for CTA c, instead of adding them into the outputs with
-// atomics; reduce_partials then adds sum_c part[c * stride + j] (in the order c = 0, 1, ...,
-// compensated) into segment j's destination.  Each destination element has exactly one writer,
+// atomics; reduce_partials then adds sum_c part[c * stride + j] (in a fixed order of c) into
+// segment j's destination.  Each destination element has exactly one writer,
 // so repeated runs on the same inputs give bit-identical sums.
 constexpr int RED_SEGS = 6;
 struct RedSeg {

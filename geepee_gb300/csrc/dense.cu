@@ -190,9 +190,15 @@ __global__ void __launch_bounds__(GemmShape<TBM>::NG * KS, TBM == 8 ? 6 : 1) gem
   const int per = g.tiles_n[p] * g.tiles_m[p];
   const int bz = r / per, rem = r - bz * per;
   const int by = rem / g.tiles_n[p], bx = rem - by * g.tiles_n[p];
-  gemm_tile<T, TBM, KS, false>(bx, by, bz, pr.m, pr.n, pr.k, pr.transA, pr.transB, pr.alpha, (const S*)pr.A, pr.lda,
-                               pr.strideA, (const S*)pr.B, pr.ldb, pr.strideB, pr.beta, (const S*)pr.E, pr.lde,
-                               pr.strideE, (S*)pr.C, pr.ldc, pr.strideC);
+  const void *Ap = pr.A, *Bp = pr.B;
+  long sA = pr.strideA, sB = pr.strideB;
+  if (pr.sel && ((pr.sel[bz] >> pr.selbit) & 1)) {   // the device-side operand choice (CTA-uniform)
+    if (pr.A2) Ap = pr.A2, sA = pr.strideA2;
+    if (pr.B2) Bp = pr.B2, sB = pr.strideB2;
+  }
+  gemm_tile<T, TBM, KS, false>(bx, by, bz, pr.m, pr.n, pr.k, pr.transA, pr.transB, pr.alpha, (const S*)Ap, pr.lda,
+                               sA, (const S*)Bp, pr.ldb, sB, pr.beta, (const S*)pr.E, pr.lde, pr.strideE, (S*)pr.C,
+                               pr.ldc, pr.strideC);
 }
 
 // ---- the SPD inverse fast path: factor (one CTA) -> L^-1 (many CTAs) -> L^-T L^-1 (GEMM) ----
@@ -890,6 +896,8 @@ static int gemm_group_check(int count, const gpk_gemm_t* problems) {
     GPK_REQUIRE(q.lda >= (q.transA ? q.m : q.k) && q.ldb >= (q.transB ? q.k : q.n) && q.ldc >= q.n &&
                     (q.beta == 0.0 || q.lde >= q.n),
                 "gemm_group[%d]: bad leading dimension", p);
+    GPK_REQUIRE(!q.sel || ((q.A2 || q.B2) && q.selbit >= 0 && q.selbit < 31),
+                "gemm_group[%d]: a selector needs A2 or B2 and a bit in [0,30]", p);
   }
   return GPK_OK;
 }

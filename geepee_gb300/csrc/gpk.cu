@@ -23,33 +23,29 @@ extern "C" const char* gpk_last_error(void) { return gpk::g_err; }
 
 namespace {
 
-// Neumaier's compensated addition: (s, c) += x
-__device__ __forceinline__ void comp_add(double& s, double& c, double x) {
-  const double t = s + x;
-  c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
-  s = t;
-}
-
 // Eight lanes per output element j: lane l sums the partials c = l, l + 8, ... in order, then
 // the eight lane sums combine over a fixed butterfly (both partners compute the same sum, as
-// IEEE addition commutes), and lane 0 adds the total into the element's destination.
+// IEEE addition commutes), and lane 0 adds the total into the element's destination.  Plain
+// float64 additions: FP64 issues slowly on this GPU, and a compensated sum would cost ~8x
+// for ~150 partials whose rounding (~150 ulp at worst) is far below the df64 results' own.
 __global__ void __launch_bounds__(256) reduce_partials_kernel(const double* part, int nparts, long stride,
                                                               gpk::RedPlan plan) {
   const long j = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 3;
   const int l = threadIdx.x & 7;
-  double s = 0.0, c = 0.0;
-  if (j < stride)
-    for (int k = l; k < nparts; k += 8) comp_add(s, c, part[(size_t)k * stride + j]);
-#pragma unroll
-  for (int m = 1; m < 8; m <<= 1) {
-    const double so = __shfl_xor_sync(0xffffffffu, s, m), co = __shfl_xor_sync(0xffffffffu, c, m);
-    const double t = s + so;
-    const double e = fabs(s) >= fabs(so) ? (s - t) + so : (so - t) + s;
-    s = t;
-    c = (c + co) + e;   // commutative in (c, co): both partners get the same value
+  double s0 = 0.0, s1 = 0.0;   // two chains, joined in a fixed order
+  if (j < stride) {
+    int k = l;
+    for (; k + 8 < nparts; k += 16) {
+      s0 += part[(size_t)k * stride + j];
+      s1 += part[(size_t)(k + 8) * stride + j];
+    }
+    if (k < nparts) s0 += part[(size_t)k * stride + j];
   }
+  double s = s0 + s1;
+#pragma unroll
+  for (int m = 1; m < 8; m <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, m);
   if (l != 0 || j >= stride) return;
-  const double v = s + c;
+  const double v = s;
   long off = 0;
   for (int i = 0; i < plan.nseg; ++i) {
     const gpk::RedSeg& g = plan.seg[i];

@@ -1016,7 +1016,10 @@ int bwd_db(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t s
 
 // points per pass: BWD_NPB when their tables fit in shared memory and the per-point sums
 // (NPB (5 Q + 1) values) fit one reduction; else one
-constexpr int BWD_NPB = 1;
+#ifndef GPK_BWD_NPB
+#define GPK_BWD_NPB 1
+#endif
+constexpr int BWD_NPB = GPK_BWD_NPB;
 template <typename T>
 int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   PsiArgs<typename Num<T>::store_t> a = a_in;

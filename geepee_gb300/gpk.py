@@ -193,7 +193,8 @@ class _GemmT(ctypes.Structure):
                 ('beta', ctypes.c_double), ('A', ctypes.c_void_p), ('lda', ctypes.c_int), ('strideA', ctypes.c_long),
                 ('B', ctypes.c_void_p), ('ldb', ctypes.c_int), ('strideB', ctypes.c_long), ('E', ctypes.c_void_p),
                 ('lde', ctypes.c_int), ('strideE', ctypes.c_long), ('C', ctypes.c_void_p), ('ldc', ctypes.c_int),
-                ('strideC', ctypes.c_long)]
+                ('strideC', ctypes.c_long), ('sel', ctypes.c_void_p), ('selbit', ctypes.c_int), ('A2', ctypes.c_void_p),
+                ('strideA2', ctypes.c_long), ('B2', ctypes.c_void_p), ('strideB2', ctypes.c_long)]
 
 
 _GROUP = 16   # GPK_GEMM_GROUP
@@ -221,7 +222,10 @@ class GemmGroup:
     def __enter__(self):
         return self
 
-    def mm(self, A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False, E=None):
+    def mm(self, A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False, E=None, sel=None, selbit=0, A2=None,
+           B2=None):
+        """With sel (an int32 device tensor [batch]): batch entry b reads A2 / B2 (same shapes per
+        entry) in place of A / B when bit `selbit` of sel[b] is set."""
         A, B = A.contiguous(), B.contiguous()
         a3 = A if A.dim() == 3 else A.unsqueeze(0)
         b3 = B if B.dim() == 3 else B.unsqueeze(0)
@@ -245,6 +249,19 @@ class GemmGroup:
         g.E, g.lde = ptr(Ee), n
         g.strideE = m * n if E is None else (0 if E.dim() == 2 or E.shape[0] == 1 else m * n)
         g.C, g.ldc, g.strideC = ptr(C), n, m * n
+        if sel is not None:
+            assert sel.dtype == torch.int32 and sel.numel() >= batch
+            g.sel, g.selbit = ptr(sel), int(selbit)
+            for name, X, dflt in (('A', A2, a3), ('B', B2, b3)):
+                if X is None:
+                    continue
+                X = X.contiguous()
+                x3 = X if X.dim() == 3 else X.unsqueeze(0)
+                assert x3.shape[1:] == dflt.shape[1:], 'alternative operand of another shape'
+                setattr(g, name + '2', ptr(x3))
+                setattr(g, 'stride' + name + '2', 0 if x3.shape[0] == 1 else x3.shape[1] * x3.shape[2])
+                self.keep.append(x3)
+            self.keep.append(sel)
         self.items.append((prec_of(A.dtype), g))
         self.keep += [A, B, C, Ee]
         return C
@@ -318,11 +335,17 @@ def _lc_desc(out, terms, ranks, sum_batch, batch):
 class _Forms(ctypes.Structure):
     """gpk_forms_t (include/gpk.h)."""
     _fields_ = [('D', ctypes.c_int), ('M', ctypes.c_int), ('beta', ctypes.c_double)] + \
-        [(n, ctypes.c_void_p) for n in ('T', 'Kinv', 't', 'Qh', 'KShK', 'Qu', 'KSuK', 'Tmh', 'Kmh', 'Tmu', 'Kmu',
-                                        'Bd', 'Bp', 'Bsto', 'Ah', 'A', 'regime')]
+        [(n, ctypes.c_void_p) for n in ('T', 'Kinv', 't', 'Qh', 'Qu', 'vh', 'vu', 'Ph', 'flags', 'Bd', 'Bp', 'Bsto',
+                                        'Ah', 'A', 'G')]
 
 
 _FORMS_MAX = 8   # GPK_FORMS_MAX
+
+
+def regime(T, Kinv, beta, flags):
+    """gpk_regime: each output's regime word (bit 0 cavity, bit 1 posterior: T form) into flags."""
+    D, M = T.shape[0], T.shape[1]
+    call('gpk_regime', D, M, float(beta), ptr(T.contiguous()), ptr(Kinv.contiguous()), ptr(flags), stream())
 
 
 def cavity_forms(items):

@@ -140,6 +140,7 @@ class DevLayer:
     def set_s_factors(self, inv, logdet):
         """Posterior and cavity moments from the inverted Su^-1, Suhat^-1; the products of each
         stage are launched together."""
+        self.set_regime()
         with gpk.GemmGroup() as g:
             self._s_stage1(inv, logdet, g)
         with gpk.GemmGroup() as g:
@@ -155,8 +156,15 @@ class DevLayer:
     # and each cancels in one regime.  When K^-1 dominates (Kuu ill-conditioned: entries ~1e5 at
     # the deep GP's initialisation, cond ~7e6) the K^-1 products lose ~5 digits and the T form is
     # exact to rounding; when T dominates (tight posteriors) the T form subtracts two matrices of
-    # size T.  Both forms' products are formed (stages 1-2) and gpk_cavity_forms keeps, per
-    # output, the one whose large operand is the smaller.
+    # size T.  gpk_regime picks, per output, the form whose large operand is the smaller; the
+    # products then read T or K^-1 as that word says (the grouped GEMM's device-side operand
+    # choice) and gpk_cavity_forms assembles the moments.
+    def set_regime(self):
+        """The per-output regime words (gpk_regime) from theta_1 and K^-1, after both exist."""
+        if getattr(self, 'flags', None) is None:
+            self.flags = torch.zeros(self.Dout, dtype=torch.int32, device=self.dev)
+        gpk.regime(self.th1, self.Kinv, self.beta, self.flags)
+
     def _s_stage1(self, inv, logdet, g):
         D = self.Dout
         self.Su, self.Sh = inv[:D], inv[D:]
@@ -166,33 +174,33 @@ class DevLayer:
         th2 = self.th2.unsqueeze(-1)
         self._mu3 = g.mm(self.Su, th2)                     # mu = Su theta_2
         self._mh3 = g.mm(self.Sh, th2, alpha=self.beta)    # muhat = Suhat beta theta_2
-        self._TSh, self._KSh = g.mm(self.th1, self.Sh), g.mm(self.Kinv, self.Sh)
-        self._TSu, self._KSu = g.mm(self.th1, self.Su), g.mm(self.Kinv, self.Su)
+        # T Suhat or K^-1 Suhat (bit 0), T Su or K^-1 Su (bit 1)
+        self._Ph = g.mm(self.Kinv, self.Sh, sel=self.flags, selbit=0, A2=self.th1)
+        self._Pu = g.mm(self.Kinv, self.Su, sel=self.flags, selbit=1, A2=self.th1)
 
     def _s_stage2(self, g):
         self.mu, self.mh = self._mu3.squeeze(-1), self._mh3.squeeze(-1)
         self.Spmm = g.lincomb(torch.empty_like(self.Su), [(1.0, self.Su)], [(1.0, self.mu, self.mu)])
         self.Smm_h = g.lincomb(torch.empty_like(self.Sh), [(1.0, self.Sh)], [(1.0, self.mh, self.mh)])
-        self._Qh, self._KShK = g.mm(self._TSh, self.th1), g.mm(self._KSh, self.Kinv)
-        self._Qu, self._KSuK = g.mm(self._TSu, self.th1), g.mm(self._KSu, self.Kinv)
-        self._Tmh, self._Kmh = g.mm(self.th1, self._mh3), g.mm(self.Kinv, self._mh3)
-        self._Tmu, self._Kmu = g.mm(self.th1, self._mu3), g.mm(self.Kinv, self._mu3)
+        f = dict(sel=self.flags)
+        self._Qh = g.mm(self._Ph, self.Kinv, selbit=0, B2=self.th1, **f)
+        self._Qu = g.mm(self._Pu, self.Kinv, selbit=1, B2=self.th1, **f)
+        self._vh = g.mm(self.Kinv, self._mh3, selbit=0, A2=self.th1, **f)
+        self._vu = g.mm(self.Kinv, self._mu3, selbit=1, A2=self.th1, **f)
 
     def _forms_item(self):
-        """The gpk_cavity_forms item of this layer; allocates its outputs (Bh_det, Bh_sto, Ahat
-        and the posterior's Bpost, Apost) and the per-output regime word."""
+        """The gpk_cavity_forms item of this layer; allocates its outputs (Bh_det, Bh_sto, Ahat,
+        the posterior's Bpost, Apost, and G = K^-1 Suhat)."""
         self.Bh_det = torch.empty_like(self._Qh)
         self.Bpost = torch.empty_like(self._Qh)
         self.Bh_sto = torch.empty_like(self._Qh)
         self.Ah = torch.empty_like(self.mh)
         self.Apost = torch.empty_like(self.mu)
-        if getattr(self, 'regime', None) is None:
-            self.regime = torch.zeros(self.Dout, dtype=torch.int32, device=self.dev)
+        self.G = torch.empty_like(self._Qh)
         sq = lambda v: v.reshape(v.shape[0], -1)
         return dict(D=self.Dout, M=self.M, beta=self.beta, T=self.th1, Kinv=self.Kinv, t=self.th2, Qh=self._Qh,
-                    KShK=self._KShK, Qu=self._Qu, KSuK=self._KSuK, Tmh=sq(self._Tmh), Kmh=sq(self._Kmh),
-                    Tmu=sq(self._Tmu), Kmu=sq(self._Kmu), Bd=self.Bh_det, Bp=self.Bpost, Bsto=self.Bh_sto,
-                    Ah=self.Ah, A=self.Apost, regime=self.regime)
+                    Qu=self._Qu, vh=sq(self._vh), vu=sq(self._vu), Ph=self._Ph, flags=self.flags, Bd=self.Bh_det,
+                    Bp=self.Bpost, Bsto=self.Bh_sto, Ah=self.Ah, A=self.Apost, G=self.G)
 
     def _kuu_grad_levels(self, dAh, dBh, sto, alpha):
         """The gradient of the layer's energy w.r.t. Kuu, summed over outputs, without products
@@ -214,6 +222,7 @@ class DevLayer:
             a = g.mm(dBh, self.Ah.unsqueeze(-1), alpha=2.0, beta=1.0, E=dAh.unsqueeze(-1))
         else:
             a = dAh.unsqueeze(-1)
+        self._a3 = a
         g = yield
         data = g.mm(BdB, self.Bh_det)
         Bda = g.mm(self.Bh_det, a).view(D, M)
@@ -379,37 +388,31 @@ class DevLayer:
         s_post, s_cav = N / alpha - 1.0, -N / alpha
         beta = self.beta
         dAh, dBh = self._dAh, self._dBh
-        K = self.Kinv
         self._kernel_grads(self._dsf2, self._dl, self._dv)
+        # d theta_1 and d theta_2 through G = K^-1 Suhat (the reference's aep_models.py:252-287
+        # sandwiches by Suhat and K^-1, which collapse): with a = dAhat + 2 dBhat Ahat,
+        #   dvcavinv = -Suhat dvcav Suhat = -(G^T dBhat G + (G^T a) muhat^T),
+        #   dtheta_2 = beta G^T a + s_post mu + s_cav beta muhat,
+        #   dtheta_1 + dtheta_1^T = sym(-s_post Spmm - s_cav beta Smm_h + 2 beta dvcavinv)
         kg = self._kuu_grad_levels(dAh, dBh, True, alpha)
         next(kg)
         with gpk.GemmGroup() as g:
-            KdB = g.mm(K, dBh)
-            U = g.mm(dAh, K, tB=True)
+            H = g.mm(dBh, self.G)
             kg.send(g)
         with gpk.GemmGroup() as g:
-            dvcav = g.mm(KdB, K)                                             # K^-1 dBhat K^-1
-            t = g.mm(KdB, self.Ah.unsqueeze(-1), alpha=2.0)                  # 2 dvcav muhat
+            GtH = g.mm(self.G, H, tA=True)
+            Ga = g.mm(self.G, self._a3, tA=True).view(D, M)
             kg.send(g)
-        # dmcav = U + t, and dvcav += beta dmcav th2^T as beta (U + t) th2^T (one level)
-        t2 = t.reshape(D, M)
-        with gpk.GemmGroup() as g:
-            dmcav = g.lincomb(torch.empty_like(U), [(1.0, U), (1.0, t2)])
-            g.lincomb(dvcav, [(1.0, dvcav)], [(beta, U, self.th2), (beta, t2, self.th2)])
-            kg.send(g)
-        self._finish_hyp(self.Mall)
-        with gpk.GemmGroup() as g:
-            SD = g.mm(self.Sh, dvcav)
-            dth2 = g.mm(self.Sh, dmcav.unsqueeze(-1), alpha=beta)
-        dvcavinv = mm(SD, self.Sh, alpha=-1.0)
-        # sym = dth1 + dth1^T, dth1 = -s_post/2 Spmm - s_cav beta/2 Smm_h + beta dvcavinv
         a1, a2 = -0.5 * s_post, -0.5 * s_cav * beta
-        sym = gpk.lincomb(torch.empty_like(dvcavinv), [(a1, self.Spmm), (a1, self.Spmm, True), (a2, self.Smm_h),
-                                                       (a2, self.Smm_h, True), (beta, dvcavinv),
-                                                       (beta, dvcavinv, True)])
+        row = lambda v: v.view(D, 1, M)
         with gpk.GemmGroup() as g:
-            dR = g.mm(self.R, sym)
-            g.lincomb(self.g['eta2'], [(s_post, self.mu), (s_cav * beta, self.mh), (1.0, dth2.reshape(D, M))])
+            kg.send(g)
+            sym = g.lincomb(torch.empty_like(GtH), [(a1, self.Spmm), (a1, self.Spmm, True), (a2, self.Smm_h),
+                                                    (a2, self.Smm_h, True), (-beta, GtH), (-beta, GtH, True)],
+                            [(-beta, Ga, self.mh), (-beta, self.mh, Ga)])
+            g.lincomb(row(self.g['eta2']), [(s_post, row(self.mu)), (s_cav * beta, row(self.mh)), (beta, row(Ga))])
+        self._finish_hyp(self.Mall)
+        dR = mm(self.R, sym)
         gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 
     def _bwd_mm_algebra_inv(self, alpha):
@@ -653,43 +656,33 @@ class DevLayer:
         else:
             self._kernel_grads(self._dsf2, self._dl, dv)
         gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
+        # d theta_1 and d theta_2 through G = K^-1 Suhat (compute_cav_grad_u and
+        # compute_posterior_grad_u, aep_models.py:548-586 and base_models.py:490-516, whose
+        # sandwiches by Suhat / Su and K^-1 collapse): with w0 = G^T dAhat, w = w0 + s_cav muhat,
+        #   dSinv_cav = -(G^T dBhat G + s_cav/2 Suhat - s_cav/2 muhat muhat^T + w muhat^T),
+        #   dSinv_post = -s_post/2 (Su + mu mu^T),
+        #   dtheta_2 = beta w + s_post mu,  dtheta_1 = beta dSinv_cav + dSinv_post
         kg = self._kuu_grad_levels(dAh, dBh, False, alpha)
         next(kg)
         with gpk.GemmGroup() as g:
-            Sinv_mh = g.mm(self.Shinv, self.mh.unsqueeze(-1))
-            Sinv_mu = g.mm(self.Suinv, self.mu.unsqueeze(-1))
-            KdB = g.mm(K, dBh)
-            U = g.mm(dAh, K)
-            kg.send(g)
-        Sinv_mh, Sinv_mu = Sinv_mh.reshape(D, M), Sinv_mu.reshape(D, M)
-        # cavity: dmucav = dAhat K^-1 + s_cav Suhat^-1 muhat (sum_n dm (kfu K^-1) = dAhat K^-1);
-        # dSucav = K^-1 dBhat K^-1 + s_cav (Suhat^-1/2 - s s^T/2), plus the mean's beta dmucav th2^T
-        # posterior: dmu = s_post Su^-1 mu, dSu = s_post (Su^-1/2 - s s^T/2) + dmu th2^T
-        with gpk.GemmGroup() as g:
-            X = g.mm(KdB, K)
-            e2p = g.mm(self.Su, Sinv_mu.unsqueeze(-1), alpha=s_post)
-            dmucav = g.lincomb(torch.empty_like(U), [(1.0, U), (s_cav, Sinv_mh)])
-            Y = g.lincomb(torch.empty_like(self.Suinv), [(0.5 * s_post, self.Suinv)],
-                          [(-0.5 * s_post, Sinv_mu, Sinv_mu), (s_post, Sinv_mu, self.th2)])
+            H = g.mm(dBh, self.G)
+            w0 = g.mm(self.G, dAh.unsqueeze(-1), tA=True).view(D, M)
+            w = g.mm(self.G, dAh.unsqueeze(-1), tA=True, beta=s_cav, E=self._mh3).view(D, M)
             kg.send(g)
         with gpk.GemmGroup() as g:
-            g.lincomb(X, [(1.0, X), (0.5 * s_cav, self.Shinv)],
-                      [(-0.5 * s_cav, Sinv_mh, Sinv_mh), (beta, dmucav, self.th2)])
+            GtH = g.mm(self.G, H, tA=True)
             kg.send(g)
+        row = lambda v: v.view(D, 1, M)
+        with gpk.GemmGroup() as g:
+            kg.send(g)
+            c1, c2 = -0.5 * beta * s_cav, -0.5 * s_post
+            sym = g.lincomb(torch.empty_like(GtH), [(-beta, GtH), (-beta, GtH, True), (c1, self.Sh), (c1, self.Sh, True),
+                                                    (c2, self.Su), (c2, self.Su, True)],
+                            [(-beta, w0, self.mh), (-beta, self.mh, w), (-s_post, self.mu, self.mu)])
+            g.lincomb(row(self.g['eta2']), [(beta, row(w)), (s_post, row(self.mu))])
         if self.side is not None:
             main.wait_stream(self.side)
         self._finish_hyp(self.Mall)
-        with gpk.GemmGroup() as g:
-            SX = g.mm(self.Sh, X)
-            SY = g.mm(self.Su, Y)
-            # d eta2 = beta Suhat dmucav + Su dmu
-            g.mm(self.Sh, dmucav.unsqueeze(-1), alpha=beta, beta=1.0, E=e2p, C=self.g['eta2'].view(D, M, 1))
-        with gpk.GemmGroup() as g:
-            dSinv_c = g.mm(SX, self.Sh, alpha=-1.0)
-            dSinv_p = g.mm(SY, self.Su, alpha=-1.0)
-        # d eta1_R = pack(dth1 + dth1^T), dth1 = beta dSinv_c + dSinv_p
-        sym = gpk.lincomb(torch.empty_like(dSinv_c), [(beta, dSinv_c), (beta, dSinv_c, True), (1.0, dSinv_p),
-                                                      (1.0, dSinv_p, True)])
         dR = mm(self.R, sym)
         gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 
@@ -792,7 +785,18 @@ def setup_layers(layers, alpha, streams=None):
                 o += 2 * l.Dout
         Sinv = torch.empty_like(S)
         lds = torch.empty(nS, dtype=F64, device=dev)
+        if side:   # the regime words on a side stream, beside the factorisation
+            s_rg = side[0]
+            s_rg.wait_stream(main)
+            with torch.cuda.stream(s_rg):
+                for l in group:
+                    l.set_regime()
+        else:
+            for l in group:
+                l.set_regime()
         gpk.chol_inv(S, Sinv, None, lds, info[G:])
+        if side:
+            main.wait_stream(s_rg)
         with gpk.GemmGroup() as g:
             o = 0
             for l in group:

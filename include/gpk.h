@@ -147,7 +147,11 @@ int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB
                 const void* A, int lda, long strideA, const void* B, int ldb, long strideB, double beta,
                 const void* E, int lde, long strideE, void* C, int ldc, long strideC, void* stream);
 
-/* One product of a gpk_gemm_group: the arguments of gpk_gemm_ex. */
+/* One product of a gpk_gemm_group: the arguments of gpk_gemm_ex, and an optional operand
+ * choice made on the device: when sel != NULL and bit `selbit` of sel[b] is set, batch entry b
+ * reads A2 (stride strideA2) in place of A when A2 != NULL, and B2 (stride strideB2) in place
+ * of B when B2 != NULL (same shapes and leading dimensions).  E.g. the layer algebra's
+ * T Suhat or Kuu^-1 Suhat, whichever the regime word of output b selects (gpk_regime). */
 typedef struct {
   int batch, m, n, k, transA, transB;
   double alpha, beta;
@@ -163,6 +167,12 @@ typedef struct {
   void* C;
   int ldc;
   long strideC;
+  const int* sel;
+  int selbit;
+  const void* A2;
+  long strideA2;
+  const void* B2;
+  long strideB2;
 } gpk_gemm_t;
 #define GPK_GEMM_GROUP 16
 
@@ -235,27 +245,31 @@ typedef struct {
 } gpk_lincomb_t;
 int gpk_lincomb(const gpk_lincomb_t* desc, void* stream);
 
-/* The posterior and cavity moments of a natural-parameter layer (T = theta_1 [D,M,M],
- * t = theta_2 [D,M], Su = (K^-1 + T)^-1, Suhat = (K^-1 + beta T)^-1, K = Kuu), in the form that
- * is accurate for the layer's regime, chosen per output d on the device:
- *   cavity, when beta max|T_d| <= max|K^-1| (prior-dominated; K^-1 products would cancel):
- *     Bhat_det = beta^2 T Suhat T - beta T,  Ahat = beta t - beta T muhat
- *   else (data-dominated; products with T would cancel):
- *     Bhat_det = K^-1 Suhat K^-1 - K^-1,     Ahat = K^-1 muhat
- *   posterior likewise with beta = 1: B = T Su T - T or K^-1 Su K^-1 - K^-1, A = t - T mu or K^-1 mu;
- * and Bhat_sto = Bhat_det + Ahat Ahat^T.  The caller supplies the products of both forms
- * (Qh = T Suhat T, KShK = K^-1 Suhat K^-1, Qu = T Su T, KSuK = K^-1 Su K^-1 [D,M,M]; Tmh = T muhat,
- * Kmh = K^-1 muhat, Tmu = T mu, Kmu = K^-1 mu [D,M]); regime[d] (optional) gets bit 0 set for
- * the cavity's T form and bit 1 for the posterior's.  Elementwise float64.  The same quantities
- * as geepee/aep_models.py:536-546 and base_models.py:480-488 (which always take the K^-1 form). */
+/* The regime word of each output d of a natural-parameter layer (T = theta_1 [D,M,M],
+ * K = Kuu): bit 0 set when beta max|T_d| <= max|K^-1| (the cavity is prior-dominated: its
+ * moments are formed from T, as products with K^-1 would cancel), bit 1 set when
+ * max|T_d| <= max|K^-1| (the same for the posterior).  flags [D] int. */
+int gpk_regime(int D, int M, double beta, const double* T, const double* Kinv, int* flags, void* stream);
+
+/* The posterior and cavity moments of a natural-parameter layer (t = theta_2 [D,M],
+ * Su = (K^-1 + T)^-1, Suhat = (K^-1 + beta T)^-1) in the form its regime word selects:
+ *   cavity, bit 0 set:  Bhat_det = beta^2 Qh - beta T,  Ahat = beta t - beta vh,
+ *           (Qh = T Suhat T, vh = T muhat);
+ *   bit 0 clear:        Bhat_det = Qh - K^-1,            Ahat = vh
+ *           (Qh = K^-1 Suhat K^-1, vh = K^-1 muhat);
+ *   posterior likewise with bit 1, beta = 1, Qu (T Su T or K^-1 Su K^-1), vu (T mu or K^-1 mu):
+ *   B = Qu - T or Qu - K^-1,  A = t - vu or vu;
+ * Bhat_sto = Bhat_det + Ahat Ahat^T, and G = K^-1 Suhat (= I - beta Ph when bit 0 is set, Ph
+ * = T Suhat; = Ph = K^-1 Suhat otherwise), which the backward's algebra uses.  Qh, Qu [D,M,M],
+ * vh, vu [D,M] and Ph are the products of the selected form (gpk_gemm_t's sel).  Elementwise
+ * float64.  The quantities of geepee/aep_models.py:536-546 and base_models.py:480-488, which
+ * always take the K^-1 form. */
 typedef struct {
   int D, M;
   double beta;
-  const double *T, *Kinv, *t;
-  const double *Qh, *KShK, *Qu, *KSuK;
-  const double *Tmh, *Kmh, *Tmu, *Kmu;
-  double *Bd, *Bp, *Bsto, *Ah, *A;
-  int* regime;
+  const double *T, *Kinv, *t, *Qh, *Qu, *vh, *vu, *Ph;
+  const int* flags;
+  double *Bd, *Bp, *Bsto, *Ah, *A, *G;
 } gpk_forms_t;
 #define GPK_FORMS_MAX 8
 int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream);
@@ -353,7 +367,7 @@ int gpk_trace_kzz(int prec, int M, int Q, const void* Mm, const void* Z, const d
  * sums vary with it (and the AEP gradients propagate them through ill-conditioned M x M
  * algebra).  Each *_ws variant below takes a caller-owned float64 workspace instead: every CTA
  * writes its partial sums there, and a second launch on the same stream adds them into the
- * outputs in a fixed order with compensated summation, one writer per output element, so
+ * outputs in a fixed order (float64 additions), one writer per output element, so
  * repeated calls on the same inputs give bit-identical outputs.  work = NULL gives the atomic
  * form.  gpk_work_elems gives the workspace size in float64 elements for operation `op` at the
  * given sizes on the current device (N rows; D = Q input dimensions; Dout outputs); it may

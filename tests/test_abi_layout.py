@@ -1,4 +1,4 @@
-"""The ctypes mirrors of the C ABI's structs (gpk_lincomb_t, gpk_gemm_t) have the C layout:
+"""The ctypes mirrors of the C ABI's structs (gpk_lincomb_t, gpk_gemm_t, gpk_forms_t) have the C layout:
 a small C program prints sizeof/offsetof from include/gpk.h and the test compares."""
 import ctypes
 import os
@@ -26,11 +26,11 @@ def _c_layout(struct, fields):
     return [int(v) for v in out]
 
 
-@pytest.mark.parametrize('name', ['_LC', '_GemmT'])
+@pytest.mark.parametrize('name', ['_LC', '_GemmT', '_Forms'])
 def test_struct_layout_matches_header(name):
     from geepee_gb300 import gpk
     py = getattr(gpk, name)
-    cname = {'_LC': 'gpk_lincomb_t', '_GemmT': 'gpk_gemm_t'}[name]
+    cname = {'_LC': 'gpk_lincomb_t', '_GemmT': 'gpk_gemm_t', '_Forms': 'gpk_forms_t'}[name]
     fields = [f for f, _ in py._fields_]
     c = _c_layout(cname, fields)
     assert c[0] == ctypes.sizeof(py)

@@ -318,8 +318,15 @@ def test_sdgpr_c3_finite_differences():
     """Central finite differences (eps = 1e-6) on 50 random parameter coordinates of the deep GP
     at its full configuration (N=20000, M=100, minibatch 1000, the same minibatch for every
     evaluation), with the rule of the reference's check_grad (tests/test_utils.py:49-128 of the
-    reference): rel diff < 1e-4, or |numerical| < 1e-4 and rel diff <= 1.1; plus the
-    difference's own resolution, 8 x 2^-48 |E| / eps (the double-float energy resolves ~2^-46)."""
+    reference): rel diff < 1e-4, or |numerical| < 1e-4 and rel diff <= 1.1.
+
+    At this configuration the energy itself carries rounding noise far above its unit roundoff:
+    the cavity and posterior log-partitions enter with weights +-N/alpha = 4e4 and layer 2's Kuu
+    has condition number 7e6.  The reference's own float64 energy (the oracle) gives -0.0115 for
+    a derivative of -0.00846 at eps = 1e-6.  So the noise is measured: the standard deviation
+    sigma of the energy over eight random parameter perturbations of relative size 1e-13 (whose
+    true effect is below 1e-13 |E|), and a coordinate whose difference misses the rule must
+    agree within 4 sigma sqrt(2) / (2 eps), the difference's own noise."""
     from geepee_gb300 import aep_models as A, workloads as W
     g = load('sdgpr_c3.npz')
     x, y = W.dgp_regression(seed=0)
@@ -332,11 +339,13 @@ def test_sdgpr_c3_finite_differences():
         return mdl.objective_function(q, 1000, alpha=0.5)
 
     e0, gr = f(p)
-    res = 8 * 2.0 ** -48 * abs(e0) / eps
     rng = np.random.RandomState(0)
+    es = [f({k: v * (1 + 1e-13 * rng.randn(*np.shape(v))) for k, v in p.items()})[0] for _ in range(8)]
+    sigma = float(np.std(es))
+    res = 4 * sigma * np.sqrt(2) / (2 * eps)
     keys = sorted(p)
     sizes = [np.size(p[k]) for k in keys]
-    bad = []
+    bad, strict = [], 0
     for fl in rng.choice(sum(sizes), 50, replace=False):
         ki = int(np.searchsorted(np.cumsum(sizes), fl, side='right'))
         k = keys[ki]
@@ -348,8 +357,12 @@ def test_sdgpr_c3_finite_differences():
         num = (f(pp)[0] - f(pm)[0]) / (2 * eps)
         ana = float(np.ravel(gr[k])[j])
         diff = (ana - num) / num if num != 0 else np.inf
-        if not (abs(diff) < 1e-4 or (abs(num) < 1e-4 and abs(diff) <= 1.1) or abs(ana - num) <= res):
+        rule = abs(diff) < 1e-4 or (abs(num) < 1e-4 and abs(diff) <= 1.1)
+        strict += rule
+        if not (rule or abs(ana - num) <= res):
             bad.append((k, int(j), ana, num, diff))
+    print('\nc3 finite differences: energy noise %.2e, %d of 50 within the reference rule, the rest within '
+          '%.2e' % (sigma, strict, res))
     assert not bad, bad
 
 
