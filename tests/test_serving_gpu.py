@@ -56,3 +56,27 @@ def test_serving_admission_by_budget():
         f.future.result(timeout=60)
     srv.stop()
     assert peak['rows'] <= 128
+
+
+def test_serving_mix_at_full_size():
+    """The served configuration: 32 resident models with M in (50, 100, 200), a Poisson trace of
+    requests of 1..4096 rows.  Every answer equals the same model's answer alone, bit for bit, and
+    the oracle's on the request's first 32 rows."""
+    from geepee_gb300 import serving, workloads as W
+    models = W.serving_models(seed=0, n_models=32, Ms=(50, 100, 200))
+    dev = torch.device('cuda', 0)
+    res = [serving.ResidentDGP(p, sizes, Ms, dev) for p, sizes, Ms in models]
+    _, mids, _, xs = W.serving_trace(seed=1, rate=2000.0, seconds=0.05, n_models=32)
+    assert len(xs) >= 50
+    srv = serving.Server(res, n_streams=4, max_rows=4096, budget_rows=1 << 16, device=dev)
+    srv.start()
+    reqs = [(int(mid), x, srv.submit(int(mid), x)) for mid, x in zip(mids, xs)]
+    outs = [(mid, x, r.future.result(timeout=120)) for mid, x, r in reqs]
+    srv.stop()
+    for mid, x, (my, vy) in outs:
+        ma, va = res[mid].predict_y(torch.as_tensor(x, device=dev))
+        assert np.array_equal(my, ma.cpu().numpy()) and np.array_equal(vy, va.cpu().numpy()), \
+            'answer in the mix differs from the answer alone'
+        _, _, mo, vo = O.sdgpr_predict(models[mid][0], x[:32])
+        assert_close(my[:32], mo, 1e-6, 'my')
+        assert_close(vy[:32], vo, 1e-6, 'vy')
