@@ -183,8 +183,11 @@ def psi_bwd_bytes(N, M, Q, D):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one psi backward launch pair (kernel and
-# reduction) of the deep GP's layer 2 in one ncu capture of the same case
-PSI_BWD_TRAFFIC = None
+# reduction) of the deep GP's layer 2 in one ncu capture of the same case (1000 points, M=100,
+# Q=2): 281,088 bytes for the kernel (its inputs) and 6,605,568 for the reduction, which ncu
+# replays after flushing the caches, so that the 152 per-CTA partial blocks it reads come from
+# DRAM (in the evaluation they are still in L2)
+PSI_BWD_TRAFFIC = 281088 + 6605568
 
 
 def time_launches(fn, flush, reps=30):

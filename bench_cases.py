@@ -84,6 +84,15 @@ def case(name):
         kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
         m, v = z(1000, 2), z(1000, 2)
         return lambda: gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, m, v)
+    if name == 'det_contract_dgp':
+        # the first deep-GP layer's forward once its kernel rows exist: 1000 rows, M=100, Dout=2
+        rng = np.random.RandomState(0)
+        x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))
+        A, B = _d(rng.randn(2, 100)), _d(rng.randn(2, 100, 100))
+        l2, s2 = _d(np.zeros(8)), _d(np.zeros(1))
+        kfu = gpk.kern(x, Z, l2, s2)
+        Bk, m, v = z(1000, 2, 100), z(1000, 2), z(1000, 2)
+        return lambda: gpk.det_contract(kfu, s2, A, B, Bk, m, v)
     if name in ('det_bwd_dgp', 'gram_dgp'):
         rng = np.random.RandomState(0)
         x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))

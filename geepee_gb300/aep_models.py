@@ -429,15 +429,28 @@ class SDGPR(_PackedModel):
         nb = yb.shape[0]
         scale = -N / nb / alpha
         side = self._side_streams()
-        st = setup_layers(self.layers, alpha, streams=side)
+        # the first layer's kernel rows K(x_batch, Z) need only its hyperparameters: they are
+        # formed beside the factorisations, and its forward then runs only the contractions
+        # (allocated here, on the main stream, which is the last to use it)
+        lay0, k0 = self.layers[0], {}
+        kfu0 = torch.empty((nb, lay0.M), dtype=torch.float64, device=self.dev)
+
+        def kfu_ahead():
+            k0['kfu'] = lay0.kfu_rows(xb, out=kfu0)
+            k0['done'] = torch.cuda.Event()
+            k0['done'].record()
+        ahead = {lay0: kfu_ahead} if gpk.det_contract_supported(torch.float64, lay0.M, lay0.Dout) else None
+        st = setup_layers(self.layers, alpha, streams=side, ahead=ahead)
         # the backward's accumulators are zeroed on a side stream while the forward runs
         main = torch.cuda.current_stream()
+        if 'done' in k0:
+            main.wait_event(k0['done'])
         side[0].wait_stream(main)
         with torch.cuda.stream(side[0]):
             for lay in self.layers:
                 lay.zero_accumulators()
         ms, vs = [], []
-        m, v, kfu, Bk = self.layers[0].fwd_det(xb)
+        m, v, kfu, Bk = self.layers[0].fwd_det(xb, kfu=k0.get('kfu'))
         ms.append(m)
         vs.append(v)
         for i in range(1, L):

@@ -354,12 +354,30 @@ __global__ void __launch_bounds__(1024) sum_scaled_kernel(int nD, const double* 
 
 // max |x| over n float64 values as the integer order of their magnitude bits (positive IEEE
 // doubles order as their bit patterns), on the integer pipe; the CTA's result in all threads
+// max |x_i| over n doubles as the bit pattern of a non-negative double (integer order = value
+// order; a NaN's pattern exceeds every finite one), reduced over the CTA.  Four independent
+// loads per thread per pass, so that a thread's loads overlap.
 __device__ long long maxabs_bits(const double* x, long n, long long* red) {
-  long long m = 0;
-  for (long i = threadIdx.x; i < n; i += blockDim.x) {
-    const long long b = __double_as_longlong(x[i]) & 0x7fffffffffffffffLL;
-    m = b > m ? b : m;
+  constexpr long long MASK = 0x7fffffffffffffffLL;
+  long long m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  const long step = blockDim.x;
+  long i = threadIdx.x;
+  for (; i + 3 * step < n; i += 4 * step) {
+    const long long b0 = __double_as_longlong(x[i]) & MASK, b1 = __double_as_longlong(x[i + step]) & MASK;
+    const long long b2 = __double_as_longlong(x[i + 2 * step]) & MASK;
+    const long long b3 = __double_as_longlong(x[i + 3 * step]) & MASK;
+    m0 = b0 > m0 ? b0 : m0;
+    m1 = b1 > m1 ? b1 : m1;
+    m2 = b2 > m2 ? b2 : m2;
+    m3 = b3 > m3 ? b3 : m3;
   }
+  for (; i < n; i += step) {
+    const long long b = __double_as_longlong(x[i]) & MASK;
+    m0 = b > m0 ? b : m0;
+  }
+  long long m = m0 > m1 ? m0 : m1;
+  m2 = m2 > m3 ? m2 : m3;
+  m = m > m2 ? m : m2;
   for (int o = 16; o > 0; o >>= 1) {
     const long long v = __shfl_xor_sync(0xffffffffu, m, o);
     m = v > m ? v : m;
@@ -373,9 +391,10 @@ __device__ long long maxabs_bits(const double* x, long n, long long* red) {
 }
 
 // one CTA per output d: bit 0 = beta max|T_d| <= max|K^-1|, bit 1 = max|T_d| <= max|K^-1|
-__global__ void __launch_bounds__(256) regime_kernel(int M, double beta, const double* T, const double* Kinv,
-                                                      int* flags) {
-  __shared__ long long red[8];
+constexpr int RG_THREADS = 1024;
+__global__ void __launch_bounds__(RG_THREADS) regime_kernel(int M, double beta, const double* T, const double* Kinv,
+                                                            int* flags) {
+  __shared__ long long red[RG_THREADS / 32];
   const long MM = (long)M * M;
   const double tmax = __longlong_as_double(maxabs_bits(T + blockIdx.x * MM, MM, red));
   const double kmax = __longlong_as_double(maxabs_bits(Kinv, MM, red));
@@ -592,7 +611,7 @@ extern "C" int gpk_regime(int D, int M, double beta, const double* T, const doub
   GPK_NVTX("gpk_regime");
   GPK_REQUIRE(D >= 1 && D <= 65535 && M >= 1, "regime: bad sizes D=%d M=%d", D, M);
   GPK_REQUIRE(T && Kinv && flags, "regime: null pointer");
-  regime_kernel<<<D, 256, 0, gpk::as_stream(stream)>>>(M, beta, T, Kinv, flags);
+  regime_kernel<<<D, RG_THREADS, 0, gpk::as_stream(stream)>>>(M, beta, T, Kinv, flags);
   return gpk::check_launch("regime");
 }
 

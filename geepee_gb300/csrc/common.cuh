@@ -88,6 +88,35 @@ __host__ __device__ __forceinline__ void tri_pair(int p, int& a, int& b) {
   b = p - r * (r + 1) / 2;
 }
 
+// Copies n storage-type elements (8 or 4 bytes) from global memory into shared memory with
+// asynchronous copies issued by threads tid, tid + nth, ... (all in flight together), then
+// waits for this thread's copies; the caller's barrier makes them visible to the CTA.
+template <typename S>
+__device__ __forceinline__ void stage_async(S* dst, const S* src, long n, int tid, int nth) {
+  static_assert(sizeof(S) == 8 || sizeof(S) == 4, "8- or 4-byte elements");
+  for (long e = tid; e < n; e += nth) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + e);
+    if (sizeof(S) == 8)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src + e));
+    else
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src + e));
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Storage type -> compute type in place (the two have the same size), one element per
+// thread step; call between barriers.
+template <typename T>
+__device__ __forceinline__ void convert_in_place(T* buf, long n, int tid, int nth) {
+  typedef typename Num<T>::store_t S;
+  static_assert(sizeof(S) == sizeof(T), "in-place conversion needs equal sizes");
+  S* raw = reinterpret_cast<S*>(buf);
+  for (long e = tid; e < n; e += nth) {
+    const S x = raw[e];
+    buf[e] = Num<T>::ld(x);
+  }
+}
+
 #define GPK_REQUIRE(cond, ...) \
   do {                          \
     if (!(cond)) return gpk::fail(GPK_EINVAL, __VA_ARGS__); \

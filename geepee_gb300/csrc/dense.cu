@@ -634,9 +634,10 @@ __global__ void __launch_bounds__(TK_MAXW * 32) trace_kzz_kernel(int M, int Q, c
     mab = Mm[(size_t)a * M + threadIdx.x];
     mba = Mm[(size_t)threadIdx.x * M + a];
   }
+  stage_async(reinterpret_cast<S*>(zs), Z, (long)M * Q, threadIdx.x, blockDim.x);
   load_exp_table(tab);
-  for (int i = threadIdx.x; i < M * Q; i += blockDim.x) zs[i] = Num<T>::ld(Z[i]);
   __syncthreads();
+  convert_in_place(zs, (long)M * Q, threadIdx.x, blockDim.x);
   if (threadIdx.x < Q) il[threadIdx.x] = exp_tab(neg(Num<T>::ld(static_cast<S>(lls2[threadIdx.x]))), tab);
   if (threadIdx.x == 31) lsf = Num<T>::ld(static_cast<S>(lsf2[0]));   // Q <= 8: thread 31 is free
   __syncthreads();
@@ -669,32 +670,36 @@ __global__ void __launch_bounds__(TK_MAXW * 32) trace_kzz_kernel(int M, int Q, c
       }
     }
   }
+  // the 1 + 2 QC warp sums in butterflies of eight (lane l then holds value c0 + l / 4), then
+  // value i over the warps in order by thread i, which writes it
+  constexpr int NV = 1 + 2 * QC;
 #pragma unroll
-  for (int i = 0; i < 1 + 2 * QC; ++i) {
-    const T t = warp_sum(v[i]);
-    if (lane == 0) red[warp][i] = t;
+  for (int c0 = 0; c0 < NV; c0 += 8) {
+    T t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t[u] = c0 + u < NV ? v[(c0 + u) % NV] : Num<T>::zero();
+    warp_sum_many<8>(t);
+    if ((lane & 3) == 0 && c0 + (lane >> 2) < NV) red[warp][c0 + (lane >> 2)] = t[0];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int i = 0; i < 1 + 2 * QC; ++i) {
-      T t = red[0][i];
-      for (int w = 1; w < nw; ++w) t = add(t, red[w][i]);
-      v[i] = t;
-    }
-#pragma unroll
-    for (int q = 0; q < QC; ++q)
-      if (q < Q) g_z[a * Q + q] += (double)Num<T>::st(v[1 + QC + q]);
-    const double vsf = s_sf * (double)Num<T>::st(v[0]);
-    if (part) part[(size_t)a * (1 + Q)] = vsf;
-    else atomicAdd(g_sf, vsf);
-#pragma unroll
-    for (int q = 0; q < QC; ++q) {
+  const int i = threadIdx.x;
+  if (i < NV) {
+    T t = red[0][i];
+    for (int w = 1; w < nw; ++w) t = add(t, red[w][i]);
+    if (i == 0) {
+      const double vsf = s_sf * (double)Num<T>::st(t);
+      if (part) part[(size_t)a * (1 + Q)] = vsf;
+      else atomicAdd(g_sf, vsf);
+    } else if (i <= QC) {
+      const int q = i - 1;
       if (q < Q) {
-        const double vl = s_ls * 0.5 * (double)Num<T>::st(v[1 + q]);
+        const double vl = s_ls * 0.5 * (double)Num<T>::st(t);
         if (part) part[(size_t)a * (1 + Q) + 1 + q] = vl;
         else atomicAdd(&g_ls[q], vl);
       }
+    } else {
+      const int q = i - 1 - QC;
+      if (q < Q) g_z[a * Q + q] += (double)Num<T>::st(t);   // one writer per element (CTA a)
     }
   }
 }
@@ -954,6 +959,9 @@ int spd_inv_small(int batch, int M, const void* A, void* Ainv, double* logdet, i
   if (M <= 32) rc = spd_factor_launch<T, 1, 2, 16>(batch, M, A, Lw, logdet, info, st);
   else if (M <= 64) rc = spd_factor_launch<T, 2, 4, 16>(batch, M, A, Lw, logdet, info, st);
   else if (M <= 96) rc = spd_factor_launch<T, 3, 6, 16>(batch, M, A, Lw, logdet, info, st);
+#ifdef GPK_SPD_NW32
+  else if (M <= 128) rc = spd_factor_launch<T, 4, 4, 32>(batch, M, A, Lw, logdet, info, st);
+#endif
   else if (M <= 112) rc = spd_factor_launch<T, 4, 7, 16>(batch, M, A, Lw, logdet, info, st);
   else rc = spd_factor_launch<T, 4, 8, 16>(batch, M, A, Lw, logdet, info, st);
   if (rc) return rc;

@@ -265,7 +265,6 @@ __device__ __forceinline__ float warp_sum(float a) {
   for (int m = 16; m > 0; m >>= 1) a += __shfl_xor_sync(0xffffffffu, a, m);
   return a;
 }
-
 // ---- float overloads so templated kernels compile for T = float ----
 __device__ __forceinline__ float add(float a, float b) { return a + b; }
 __device__ __forceinline__ float sub(float a, float b) { return a - b; }
@@ -280,7 +279,38 @@ __device__ __forceinline__ float scale2(float a, int e) { return scale2f(a, e); 
 template <typename Tab> __device__ __forceinline__ float exp_tab(float x, const Tab&) { return expf(x); }
 template <typename Tab> __device__ __forceinline__ float log_tab(float x, const Tab&) { return logf(x); }
 
+// Warp sums of K values at once (K a power of two <= 32): in each of the first log2 K steps
+// of the butterfly a lane keeps half of its values and adds its partner's copies of them,
+// trading the other half, so the K sums take K - 1 + 5 - log2 K exchanges instead of 5 K.
+// On return v[0] of lane l holds the warp total of value l >> (5 - log2 K).
+template <int K, typename T>
+__device__ __forceinline__ void warp_sum_many(T (&v)[K]) {
+  static_assert(K >= 1 && K <= 32 && (K & (K - 1)) == 0, "K must be a power of two <= 32");
+  const int lane = threadIdx.x & 31;
+  int off = 16;
+#pragma unroll
+  for (int n = K; n > 1; n >>= 1, off >>= 1) {
+    const bool up = (lane & off) != 0;   // this lane keeps the upper half of the n values
+#pragma unroll
+    for (int i = 0; i < n / 2; ++i) {
+      const T keep = up ? v[i + n / 2] : v[i];
+      const T send = up ? v[i] : v[i + n / 2];
+      v[i] = add(keep, shfl_xor(send, off));
+    }
+  }
+#pragma unroll
+  for (; off > 0; off >>= 1) v[0] = add(v[0], shfl_xor(v[0], off));
+}
+
 // conversions between storage (double / float) and compute (df64 / float) types
+// A compute-type element read as one 8-byte access (df64) when its address is known to be
+// 8-byte aligned (df64 itself is only 4-byte aligned, so plain loads may split in two).
+__device__ __forceinline__ df64 ld_al8(const df64* p) {
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  return make_df(v.x, v.y);
+}
+__device__ __forceinline__ float ld_al8(const float* p) { return *p; }
+
 template <typename T> struct Num;
 template <> struct Num<df64> {
   typedef double store_t;

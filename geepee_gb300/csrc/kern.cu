@@ -193,6 +193,108 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
   }
 }
 
+// The deterministic-input layer's contractions from given kernel values kfu [N,M]:
+//   m_nd = kfu_n . A_d;  Bk_ndb = sum_a B_d[a,b] kfu_na;  v_nd = sf2 + kfu_n . Bk_nd
+// (geepee/aep_models.py:142-158 once Kfu is formed).  A CTA takes CR rows; warp w works on row
+// w % CR and column half w / CR, lane l on columns b = 64 h + l + 32 j (j < 2), for all DB
+// outputs, so each thread runs 2 DB independent sums over a.  All of B (Dout M^2) and the CTA's
+// kernel rows sit in shared memory (asynchronous copies, converted in place, 8-byte aligned so
+// that each element is one shared-memory access); m and v are warp sums, then the two halves'
+// sums are added in a fixed order.
+constexpr int CR = 8;              // rows per CTA
+constexpr int CT = CR * 2 * 32;    // threads: (row, column half) per warp
+template <typename T, int DB>
+__global__ void __launch_bounds__(CT) det_contract_kernel(int N, int M, int Dout,
+                                                          const typename Num<T>::store_t* kfu,
+                                                          const double* lsf2,
+                                                          const typename Num<T>::store_t* A,
+                                                          const typename Num<T>::store_t* B,
+                                                          typename Num<T>::store_t* Bk,
+                                                          typename Num<T>::store_t* m_out,
+                                                          typename Num<T>::store_t* v_out) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  T* Bs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [Dout][M][M]
+  T* kr = Bs + (size_t)Dout * M * M;                                 // [CR][M]
+  T* red = kr + (size_t)CR * M;                                      // [2][CR][DB][2] half sums
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int r = w % CR, h = w / CR;
+  const int n0 = blockIdx.x * CR, n = n0 + r;
+  const int nB = Dout * M * M, nr = min(CR, N - n0);
+  stage_async(reinterpret_cast<S*>(Bs), B, nB, tid, CT);
+  stage_async(reinterpret_cast<S*>(kr), kfu + (size_t)n0 * M, (long)nr * M, tid, CT);
+  load_exp_table(tab);
+  __syncthreads();
+  convert_in_place(Bs, nB, tid, CT);
+  convert_in_place(kr, (long)nr * M, tid, CT);
+  __syncthreads();
+  const bool live = n < N;   // warp-uniform; a dead row still reaches the barrier below
+  const T* k = kr + (size_t)(live ? r : 0) * M;
+  // columns past M read the row's last column (in bounds) and are never stored
+  const int c0 = min(64 * h + lane, M - 1), c1 = min(64 * h + lane + 32, M - 1);
+  T acc[DB][2];
+#pragma unroll
+  for (int d = 0; d < DB; ++d) acc[d][0] = acc[d][1] = Num<T>::zero();
+  // output d's columns of B; outputs past Dout (DB = 4 for Dout = 3) read output 0's, in
+  // bounds, and are never stored
+  const T* B0[DB];
+  const T* B1[DB];
+#pragma unroll
+  for (int d = 0; d < DB; ++d) {
+    const size_t off = (size_t)(d < Dout ? d : 0) * M * M;
+    B0[d] = Bs + off + c0;
+    B1[d] = Bs + off + c1;
+  }
+  for (int a = 0; a < M; ++a) {
+    const T ka = k[a];
+    const size_t ra = (size_t)a * M;
+#pragma unroll
+    for (int d = 0; d < DB; ++d) {
+      // det_fwd's operand order, so that the sums match its arithmetic
+      acc[d][0] = fma_(ld_al8(B0[d] + ra), ka, acc[d][0]);
+      acc[d][1] = fma_(ld_al8(B1[d] + ra), ka, acc[d][1]);
+    }
+  }
+  T pm[DB], pv[DB];
+#pragma unroll
+  for (int d = 0; d < DB; ++d) {
+    pm[d] = pv[d] = Num<T>::zero();
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int b = 64 * h + lane + 32 * j;
+      if (live && b < M && d < Dout) {
+        if (Bk) Bk[((size_t)n * Dout + d) * M + b] = Num<T>::st(acc[d][j]);
+        pm[d] = fma_(k[b], Num<T>::ld(A[(size_t)d * M + b]), pm[d]);
+        pv[d] = fma_(k[b], acc[d][j], pv[d]);
+      }
+    }
+    pm[d] = warp_sum(pm[d]);
+    pv[d] = warp_sum(pv[d]);
+    if (lane == 0) {
+      red[((h * CR + r) * DB + d) * 2] = pm[d];
+      red[((h * CR + r) * DB + d) * 2 + 1] = pv[d];
+    }
+  }
+  __syncthreads();
+  if (h == 0 && lane == 0 && live) {
+    const T sf2 = exp_tab(Num<T>::ld(static_cast<S>(lsf2[0])), tab);
+#pragma unroll
+    for (int d = 0; d < DB; ++d) {
+      if (d < Dout) {
+        const T mm = add(red[((0 * CR + r) * DB + d) * 2], red[((1 * CR + r) * DB + d) * 2]);
+        const T vv = add(red[((0 * CR + r) * DB + d) * 2 + 1], red[((1 * CR + r) * DB + d) * 2 + 1]);
+        if (m_out) m_out[(size_t)n * Dout + d] = Num<T>::st(mm);
+        if (v_out) v_out[(size_t)n * Dout + d] = Num<T>::st(add(sf2, vv));
+      }
+    }
+  }
+}
+
+size_t det_contract_smem(int M, int Dout, size_t tsz) {
+  return 256 * sizeof(float2) + ((size_t)Dout * M * M + (size_t)CR * M + 2 * CR * DO_MAX * 2) * tsz;
+}
+
 // Deterministic-input layer backward, per row (geepee/aep_models.py:451-460 with
 // kfucompDer, kernels.py:381-399):
 //   dkfu_nb = sum_d dm_nd A_db + 2 sum_d dv_nd Bk_ndb,   L_nb = dkfu_nb kfu_nb
@@ -202,7 +304,9 @@ __global__ void __launch_bounds__(256) det_fwd_kernel(int N, int M, int D, int D
 // groups; a CTA takes a contiguous range of rows, RG at a time.  Per-b sums (dZ, dA) are
 // reduced over the row groups in shared memory and flushed with one atomic per CTA; dsf2 and
 // dl by one CTA reduction.
-template <typename T, int DC>
+// DB outputs (Dout <= DB, every one of the first DB live unless DB = DO_MAX) and EX (D == DC)
+// are compile-time, so that the per-row loops carry no branch between independent sums.
+template <typename T, int DC, int DB, bool EX>
 __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int Dout,
                                                       const typename Num<T>::store_t* x, int ldx,
                                                       const typename Num<T>::store_t* z, const double* lls2,
@@ -241,6 +345,8 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
     ga[d] = Num<T>::zero();
   }
   T gsf = Num<T>::zero();
+  auto q_on = [&](int q) { return EX || q < D; };
+  auto d_on = [&](int d) { return d < DB && (DB < DO_MAX || d < Dout); };
   const int nbeg = (int)((long)N * blockIdx.x / gridDim.x), nend = (int)((long)N * (blockIdx.x + 1) / gridDim.x);
   __syncthreads();
   for (int n0 = nbeg; n0 < nend; n0 += RG) {
@@ -262,8 +368,8 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
         g = Num<T>::ld(dkfu[(size_t)n * M + b]);
       } else {
 #pragma unroll
-        for (int d = 0; d < DO_MAX; ++d) {
-          if (d < Dout) {
+        for (int d = 0; d < DB; ++d) {
+          if (d_on(d)) {
             const T dmd = gv[rg * 2 * DO_MAX + 2 * d], dvd = gv[rg * 2 * DO_MAX + 2 * d + 1];
             g = fma_(dmd, ab[d], g);
             g = fma_(scale2(dvd, 1), Num<T>::ld(Bk[((size_t)n * Dout + d) * M + b]), g);
@@ -275,7 +381,7 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
       gsf = add(gsf, L);
 #pragma unroll
       for (int q = 0; q < DC; ++q) {
-        if (q < D) {
+        if (q_on(q)) {
           const T df = sub(xs[rg * DC + q], zb[q]);
           const T t = mul(L, df);
           gz[q] = fma_(t, h->inv_l2[q], gz[q]);
@@ -284,14 +390,19 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
       }
     }
     if (dx) {
-      // dx_nq = -sum_b L (x_nq - z_bq) / l_q: warp sums over b, then over the group's warps
+      // dx_nq = -sum_b L (x_nq - z_bq) / l_q: warp sums over b (all q in one butterfly), then
+      // over the group's warps
 #pragma unroll
-      for (int q = 0; q < DC; ++q) {
-        if (q < D) {
-          T t = (row && b < M) ? mul(L, mul(sub(xs[rg * DC + q], zb[q]), h->inv_l2[q])) : Num<T>::zero();
-          t = warp_sum(t);
-          if (lane == 0) red[(rg * XW + xw) * DC + q] = t;
+      for (int c0 = 0; c0 < DC; c0 += 8) {   // eight dimensions per butterfly (register budget)
+        T t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int q = c0 + u;
+          t[u] = (q_on(q) && row && b < M) ? mul(L, mul(sub(xs[rg * DC + q], zb[q]), h->inv_l2[q])) : Num<T>::zero();
         }
+        warp_sum_many<8>(t);   // lane l now holds the warp total of dimension c0 + l / 4
+        const int q = c0 + (lane >> 2);
+        if ((lane & 3) == 0 && q < D) red[(rg * XW + xw) * DC + q] = t[0];
       }
       __syncthreads();
       if (row && b < D) {
@@ -334,37 +445,38 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
     }
   }
   __syncthreads();
-  // dsf2 and dl: CTA reduction (warp sums, then warp 0 of the CTA)
-  T vals[1 + DC];
-  vals[0] = gsf;
-#pragma unroll
-  for (int q = 0; q < DC; ++q) vals[1 + q] = gl[q];
-  const int wid = tid >> 5, nw = nth >> 5;
+  // dsf2 and dl: CTA reduction (the 1 + D warp sums in one butterfly, then lane i of warp 0
+  // adds value i over the warps in order)
+  const int wid = tid >> 5, nw = nth >> 5, ln = tid & 31;
   T* rw = red;   // [nw][1 + DC]
 #pragma unroll
-  for (int i = 0; i < 1 + DC; ++i) {
-    const T t = warp_sum(vals[i]);
-    if ((tid & 31) == 0) rw[wid * (1 + DC) + i] = t;
+  for (int c0 = 0; c0 < 1 + DC; c0 += 8) {   // values 0 (sf2) and 1 + q (dimension q), eight at a time
+    T vals[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = c0 + u;
+      vals[u] = i == 0 ? gsf : (i <= DC ? gl[(i - 1) & (DC - 1)] : Num<T>::zero());
+    }
+    warp_sum_many<8>(vals);
+    const int i = c0 + (ln >> 2);
+    if ((ln & 3) == 0 && i < 1 + DC) rw[wid * (1 + DC) + i] = vals[0];
   }
   __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int i = 0; i < 1 + DC; ++i) vals[i] = warp_sum((tid & 31) < nw ? rw[(tid & 31) * (1 + DC) + i] : Num<T>::zero());
-    if (tid == 0) {
-      const size_t o = (size_t)M * D + (size_t)(dkfu ? 0 : Dout) * M;
-      const double vsf = (double)Num<T>::st(div(vals[0], h->sf2));
+  if (wid == 0 && ln < 1 + DC) {
+    T tot = rw[ln];
+    for (int w = 1; w < nw; ++w) tot = add(tot, rw[w * (1 + DC) + ln]);
+    const size_t o = (size_t)M * D + (size_t)(dkfu ? 0 : Dout) * M;
+    if (ln == 0) {
+      const double vsf = (double)Num<T>::st(div(tot, h->sf2));
       if (pblk) pblk[o] = vsf;
       else atomicAdd(dsf2, vsf);
-#pragma unroll
-      for (int q = 0; q < DC; ++q) {
-        if (q < D) {
-          // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
-          const T il = h->inv_l2[q];
-          const double vl = (double)Num<T>::st(mul(vals[1 + q], mul(il, sqrt_(il))));
-          if (pblk) pblk[o + 1 + q] = vl;
-          else atomicAdd(&dl[q], vl);
-        }
-      }
+    } else if (ln - 1 < D) {
+      // d/d ell of exp(-(x-z)^2/(2 ell^2)) = (x-z)^2 / ell^3 = (x-z)^2 * (1/l)^{3/2}
+      const int q = ln - 1;
+      const T il = h->inv_l2[q];
+      const double vl = (double)Num<T>::st(mul(tot, mul(il, sqrt_(il))));
+      if (pblk) pblk[o + 1 + q] = vl;
+      else atomicAdd(&dl[q], vl);
     }
   }
 }
@@ -455,6 +567,73 @@ __global__ void __launch_bounds__(256) gram_kernel(int N, int M, int Dout, const
           }
         }
       }
+    }
+  }
+}
+
+// Symmetric weighted Gram reduction by unordered pairs:  C[d] += sum_n w[n,d] u_n u_n^T
+// (the dBhat einsum of geepee/aep_models.py:463-464 with u = kfu).  A CTA owns GP_PPT pairs
+// (a >= b, row-major lower-triangle order) per thread of one pair block and one chunk of rows
+// (blockIdx.y); the chunk's rows go through shared memory GR at a time, and each pair's sum
+// over the chunk is one product u_a u_b per row and one multiply-add per output.  Every pair is
+// computed once (no tile padding, no lower half of diagonal tiles); the chunk's sums leave as a
+// partial block of packed pairs for the fixed-order reduction.
+constexpr int GP_PPT = 2;
+constexpr int GP_T = 512;
+template <typename T, int DB>
+__global__ void __launch_bounds__(GP_T) gram_pairs_kernel(int N, int M, int Dout, const typename Num<T>::store_t* u,
+                                                          const typename Num<T>::store_t* w, double* part,
+                                                          long pstride, int GR) {
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  T* us = reinterpret_cast<T*>(smem_raw);   // [GR][M]
+  T* ws = us + (size_t)GR * M;              // [GR][DO_MAX]
+  const int tid = threadIdx.x, P = M * (M + 1) / 2;
+  int ia[GP_PPT], ib[GP_PPT], pp[GP_PPT];
+#pragma unroll
+  for (int k = 0; k < GP_PPT; ++k) {
+    pp[k] = blockIdx.x * (GP_T * GP_PPT) + tid + GP_T * k;
+    tri_pair(pp[k] < P ? pp[k] : 0, ia[k], ib[k]);   // pairs past P compute (0, 0), never stored
+  }
+  // DB (compile-time) outputs per pair, so that the loop below has no branch between the
+  // independent sums (DB = 4 serves Dout = 3 with a zero weight)
+  T acc[GP_PPT][DB];
+#pragma unroll
+  for (int k = 0; k < GP_PPT; ++k)
+#pragma unroll
+    for (int d = 0; d < DB; ++d) acc[k][d] = Num<T>::zero();
+  const int nbeg = (int)((long)N * blockIdx.y / gridDim.y), nend = (int)((long)N * (blockIdx.y + 1) / gridDim.y);
+  for (int n0 = nbeg; n0 < nend; n0 += GR) {
+    const int nr = min(GR, nend - n0);
+    stage_async(reinterpret_cast<S*>(us), u + (size_t)n0 * M, (long)nr * M, tid, GP_T);
+    for (int e = tid; e < nr * DO_MAX; e += GP_T) {
+      const int r = e / DO_MAX, d = e - r * DO_MAX;
+      ws[e] = d < Dout ? Num<T>::ld(w[(size_t)(n0 + r) * Dout + d]) : Num<T>::zero();
+    }
+    __syncthreads();
+    convert_in_place(us, (long)nr * M, tid, GP_T);
+    __syncthreads();
+    for (int rl = 0; rl < nr; ++rl) {
+      const T* ur = us + (size_t)rl * M;
+      T wd[DB];
+#pragma unroll
+      for (int d = 0; d < DB; ++d) wd[d] = ld_al8(ws + rl * DO_MAX + d);
+#pragma unroll
+      for (int k = 0; k < GP_PPT; ++k) {
+        const T kk = mul(ld_al8(ur + ia[k]), ld_al8(ur + ib[k]));
+#pragma unroll
+        for (int d = 0; d < DB; ++d) acc[k][d] = fma_(wd[d], kk, acc[k][d]);
+      }
+    }
+    __syncthreads();   // the rows are consumed before the next chunk overwrites them
+  }
+  double* pb = part + (size_t)blockIdx.y * pstride;
+#pragma unroll
+  for (int k = 0; k < GP_PPT; ++k) {
+    if (pp[k] < P) {
+#pragma unroll
+      for (int d = 0; d < DB; ++d)
+        if (d < Dout) pb[(size_t)d * P + pp[k]] = (double)Num<T>::st(acc[k][d]);
     }
   }
 }
@@ -571,6 +750,47 @@ extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* 
   return gpk::check_launch("det_fwd");
 }
 
+namespace {
+template <typename T, int DB>
+void contract_launch(int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A, const void* B,
+                     void* Bk, void* m_out, void* v_out, cudaStream_t st) {
+  typedef typename Num<T>::store_t S;
+  const size_t sm = det_contract_smem(M, Dout, sizeof(T));
+  auto k = det_contract_kernel<T, DB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<gpk::ceil_div(N, CR), CT, sm, st>>>(N, M, Dout, (const S*)kfu, lsf2, (const S*)A, (const S*)B, (S*)Bk,
+                                          (S*)m_out, (S*)v_out);
+}
+template <typename T>
+void contract_dispatch(int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A, const void* B,
+                       void* Bk, void* m_out, void* v_out, cudaStream_t st) {
+  if (Dout == 1) contract_launch<T, 1>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+  else if (Dout == 2) contract_launch<T, 2>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+  else contract_launch<T, 4>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+}
+}  // namespace
+
+extern "C" int gpk_det_contract_supported(int prec, int M, int Dout) {
+  const size_t tsz = prec == GPK_FP32 ? sizeof(float) : sizeof(df64);
+  return M >= 1 && M <= 128 && Dout >= 1 && Dout <= DO_MAX && det_contract_smem(M, Dout, tsz) <= 227 * 1024;
+}
+
+extern "C" int gpk_det_contract(int prec, int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A,
+                                const void* B, void* Bk, void* m_out, void* v_out, void* stream) {
+  GPK_NVTX("gpk_det_contract");
+  GPK_REQUIRE(prec == GPK_DF64 || prec == GPK_FP32, "det_contract: unknown precision %d", prec);
+  GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1, "det_contract: bad sizes N=%d M=%d Dout=%d", N, M, Dout);
+  if (!gpk_det_contract_supported(prec, M, Dout))
+    return gpk::fail(GPK_EUNSUPPORTED, "det_contract: M=%d, Dout=%d (needs M <= 128 and Dout M^2 in shared memory)",
+                     M, Dout);
+  GPK_REQUIRE(kfu && lsf2 && A && B, "det_contract: null input");
+  if (N == 0) return GPK_OK;
+  cudaStream_t st = gpk::as_stream(stream);
+  if (prec == GPK_DF64) contract_dispatch<df64>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+  else contract_dispatch<float>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+  return gpk::check_launch("det_contract");
+}
+
 extern "C" int gpk_det_bwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
                            const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
                            const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl, double* dZ,
@@ -603,10 +823,77 @@ int gram_chunks(int N, int M, bool sym) {
 }
 }  // namespace
 
+namespace {
+template <typename T, int DC, int DB, bool EX>
+void det_bwd_launch(int grid, dim3 threads, cudaStream_t st, int N, int M, int D, int Dout, const void* x, int ldx,
+                    const void* Z, const double* lls2, const double* lsf2, const void* A, const void* kfu,
+                    const void* Bk, const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl,
+                    double* dZ, double* dA, void* dx, double* work, long stride) {
+  typedef typename Num<T>::store_t S;
+  const size_t sm = det_bwd_smem(threads.x, threads.y, DC, sizeof(T));
+  auto k = det_bwd_kernel<T, DC, DB, EX>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const S*)x, ldx, (const S*)Z, lls2, lsf2, (const S*)A, (const S*)kfu,
+                               (const S*)Bk, (const S*)dm, (const S*)dv, (const S*)dkfu, dsf2, dl, dZ, dA, (S*)dx,
+                               work, stride);
+}
+// the exact forms for D = 8 inputs and 1 or 2 outputs given through A, Bk (the deep GP's first
+// layer and the 8-input regressions); everything else takes the general form
+template <typename T>
+void det_bwd_dispatch(int grid, dim3 threads, cudaStream_t st, int dc, int N, int M, int D, int Dout, const void* x,
+                      int ldx, const void* Z, const double* lls2, const double* lsf2, const void* A, const void* kfu,
+                      const void* Bk, const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl,
+                      double* dZ, double* dA, void* dx, double* work, long stride) {
+#define GPK_DET_BWD_ARGS grid, threads, st, N, M, D, Dout, x, ldx, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dkfu, dsf2, dl, \
+                         dZ, dA, dx, work, stride
+  if (D == 8 && !dkfu && Dout == 1) det_bwd_launch<T, 8, 1, true>(GPK_DET_BWD_ARGS);
+  else if (D == 8 && !dkfu && Dout == 2) det_bwd_launch<T, 8, 2, true>(GPK_DET_BWD_ARGS);
+  else if (dc == 8) det_bwd_launch<T, 8, DO_MAX, false>(GPK_DET_BWD_ARGS);
+  else det_bwd_launch<T, 16, DO_MAX, false>(GPK_DET_BWD_ARGS);
+#undef GPK_DET_BWD_ARGS
+}
+}  // namespace
+
 long det_bwd_work_elems(int N, int M, int D, int Dout) {
   return (long)gpk::sm_count() * det_bwd_stride(M, D, Dout, false);
 }
-long gram_work_elems(int N, int M, int Dout) { return (long)gram_chunks(N, M, true) * Dout * M * M; }
+namespace {
+// the pair-wise Gram reduction: pair blocks of GP_T * GP_PPT pairs, row chunks so that about one
+// CTA runs per SM, each chunk at least 8 rows; rows staged GR at a time (about 48 KB)
+int gram_pair_blocks(int M) { return gpk::ceil_div(M * (M + 1) / 2, GP_T * GP_PPT); }
+int gram_pair_chunks(int N, int M) {
+  int c = gpk::ceil_div(gpk::sm_count(), gram_pair_blocks(M));
+  const int cap = gpk::ceil_div(N, 8);
+  if (c > cap) c = cap;
+  return c < 1 ? 1 : c;
+}
+template <typename T, int DB>
+void gram_pairs_launch(dim3 grid, size_t sm, cudaStream_t st, int N, int M, int Dout, const void* u, const void* w,
+                       double* work, long pstride, int GR) {
+  typedef typename Num<T>::store_t S;
+  auto k = gram_pairs_kernel<T, DB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, GP_T, sm, st>>>(N, M, Dout, (const S*)u, (const S*)w, work, pstride, GR);
+}
+template <typename T>
+void gram_pairs_dispatch(dim3 grid, size_t sm, cudaStream_t st, int N, int M, int Dout, const void* u, const void* w,
+                         double* work, long pstride, int GR) {
+  if (Dout == 1) gram_pairs_launch<T, 1>(grid, sm, st, N, M, Dout, u, w, work, pstride, GR);
+  else if (Dout == 2) gram_pairs_launch<T, 2>(grid, sm, st, N, M, Dout, u, w, work, pstride, GR);
+  else gram_pairs_launch<T, 4>(grid, sm, st, N, M, Dout, u, w, work, pstride, GR);
+}
+
+int gram_pair_rows(int M, size_t tsz) {
+  const int r = (int)((48 * 1024) / ((size_t)M * tsz + DO_MAX * tsz));
+  return r < 1 ? 1 : (r > 32 ? 32 : r);
+}
+}  // namespace
+
+long gram_work_elems(int N, int M, int Dout) {
+  const long full = (long)gram_chunks(N, M, false) * Dout * M * M;   // u != v: full tiles
+  const long pairs = (long)gram_pair_chunks(N, M) * Dout * (M * (M + 1) / 2);
+  return full > pairs ? full : pairs;
+}
 
 extern "C" int gpk_det_bwd_ws(int prec, int N, int M, int D, int Dout, const void* x, int ldx, const void* Z,
                               const double* lls2, const double* lsf2, const void* A, const void* kfu, const void* Bk,
@@ -628,23 +915,14 @@ extern "C" int gpk_det_bwd_ws(int prec, int N, int M, int D, int Dout, const voi
   const int grid = det_bwd_grid(N, M);
   const dim3 threads(bx, rg);
   const int dc = D <= 8 ? 8 : 16;
-  if (prec == GPK_DF64) {
-    const size_t sm = det_bwd_smem(bx, rg, dc, sizeof(df64));
-    auto k = dc == 8 ? det_bwd_kernel<df64, 8> : det_bwd_kernel<df64, 16>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const double*)x, ldx, (const double*)Z, lls2, lsf2,
-                                 (const double*)A, (const double*)kfu, (const double*)Bk, (const double*)dm,
-                                 (const double*)dv, (const double*)dkfu, dsf2, dl, dZ, dA, (double*)dx, work, stride);
-  } else if (prec == GPK_FP32) {
-    const size_t sm = det_bwd_smem(bx, rg, dc, sizeof(float));
-    auto k = dc == 8 ? det_bwd_kernel<float, 8> : det_bwd_kernel<float, 16>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const float*)x, ldx, (const float*)Z, lls2, lsf2, (const float*)A,
-                                 (const float*)kfu, (const float*)Bk, (const float*)dm, (const float*)dv,
-                                 (const float*)dkfu, dsf2, dl, dZ, dA, (float*)dx, work, stride);
-  } else {
+  if (prec == GPK_DF64)
+    det_bwd_dispatch<df64>(grid, threads, st, dc, N, M, D, Dout, x, ldx, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dkfu,
+                           dsf2, dl, dZ, dA, dx, work, stride);
+  else if (prec == GPK_FP32)
+    det_bwd_dispatch<float>(grid, threads, st, dc, N, M, D, Dout, x, ldx, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dkfu,
+                            dsf2, dl, dZ, dA, dx, work, stride);
+  else
     return gpk::fail(GPK_EINVAL, "det_bwd: unknown precision %d", prec);
-  }
   int rc = gpk::check_launch("det_bwd");
   if (rc != GPK_OK || !work) return rc;
   gpk::RedPlan plan{};
@@ -667,16 +945,33 @@ extern "C" int gpk_gram_ws(int prec, int N, int M, int Dout, const void* u, cons
   GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1 && Dout <= DO_MAX, "gram: bad sizes");
   GPK_REQUIRE(u && v && w && C, "gram: null pointer");
   const int sym = u == v;   // C symmetric: the upper tiles only
-  const int chunks = gram_chunks(N, M, sym);
+  const int P = M * (M + 1) / 2;
+  const int chunks = sym ? gram_pair_chunks(N, M) : gram_chunks(N, M, false);
   if (work) {
-    const long need = (long)chunks * Dout * M * M;
+    const long need = (long)chunks * Dout * (sym ? P : M * M);
     GPK_REQUIRE(work_elems >= need, "gram: workspace of %ld doubles, %ld needed", work_elems, need);
   }
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
+  if (sym && work) {   // the fixed-order symmetric form: unordered pairs, packed partial blocks
+    const size_t tsz = prec == GPK_FP32 ? sizeof(float) : sizeof(df64);
+    const int GR = gram_pair_rows(M, tsz);
+    const size_t sm = (size_t)GR * (M + DO_MAX) * tsz;
+    const dim3 grid(gram_pair_blocks(M), chunks);
+    const long pstride = (long)Dout * P;
+    if (prec == GPK_DF64) gram_pairs_dispatch<df64>(grid, sm, st, N, M, Dout, u, w, work, pstride, GR);
+    else if (prec == GPK_FP32) gram_pairs_dispatch<float>(grid, sm, st, N, M, Dout, u, w, work, pstride, GR);
+    else return gpk::fail(GPK_EINVAL, "gram: unknown precision %d", prec);
+    int rc = gpk::check_launch("gram_pairs");
+    if (rc != GPK_OK) return rc;
+    gpk::RedPlan plan{};
+    plan.add(C, Dout * P, 1, M);
+    return gpk::reduce_partials(work, chunks, plan, st);
+  }
   const int nt = gpk::ceil_div(M, 32);
+  const int tchunks = gram_chunks(N, M, sym);   // the tiled form (atomic, or u != v)
   const int tiles = sym ? nt * (nt + 1) / 2 : nt * nt;
-  const dim3 grid(sym ? tiles : nt, sym ? 1 : nt, chunks);
+  const dim3 grid(sym ? tiles : nt, sym ? 1 : nt, tchunks);
   if (prec == GPK_DF64)
     gram_kernel<df64><<<grid, 256, 0, st>>>(N, M, Dout, (const double*)u, (const double*)v, (const double*)w, C,
                                             sym, work);
@@ -689,7 +984,7 @@ extern "C" int gpk_gram_ws(int prec, int N, int M, int Dout, const void* u, cons
   if (rc != GPK_OK || !work) return rc;
   gpk::RedPlan plan{};
   plan.add(C, Dout * M * M);
-  return gpk::reduce_partials(work, chunks, plan, st);
+  return gpk::reduce_partials(work, tchunks, plan, st);
 }
 
 extern "C" int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const void* w, double* c, void* stream) {

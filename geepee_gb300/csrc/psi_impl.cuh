@@ -71,6 +71,40 @@ struct PsiArgs {
 
 __device__ __forceinline__ void pair_of(int p, int& a, int& b) { tri_pair(p, a, b); }
 
+// The symmetrised weights of the packed pairs, Bs[d P + p] = B_d[a,b] + B_d[b,a] (a != b) or
+// B_d[a,a]: each thread keeps eight pairs' global loads in flight before converting them, so
+// the table costs a few memory latencies per CTA instead of one per pair.
+template <typename T, int NTH>
+__device__ void stage_sym_B(T* Bs, const typename Num<T>::store_t* B, int M, int D, int P) {
+  typedef typename Num<T>::store_t S;
+  constexpr int K = 8;
+  for (int d = 0; d < D; ++d) {
+    const S* Bd = B + (size_t)d * M * M;
+    for (int p0 = threadIdx.x; p0 < P; p0 += K * NTH) {
+      S x1[K], x2[K];
+      bool off[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int p = p0 + k * NTH;
+        int ia = 0, ib = 0;
+        if (p < P) pair_of(p, ia, ib);
+        off[k] = ia != ib;
+        x1[k] = p < P ? Bd[ia * M + ib] : S(0);
+        x2[k] = off[k] ? Bd[ib * M + ia] : S(0);
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int p = p0 + k * NTH;
+        if (p < P) {
+          T w = Num<T>::ld(x1[k]);
+          if (off[k]) w = add(w, Num<T>::ld(x2[k]));
+          Bs[d * P + p] = w;
+        }
+      }
+    }
+  }
+}
+
 // CTA-wide sum of K (<= RED) values per thread; the result is valid in warp 0.  Only the
 // first `nact` warps hold non-zero values (the others skip the shuffles; default: all).
 template <typename T, int K>
@@ -256,15 +290,8 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
       }
     }
     s.G[p] = neg(g);
-    if (s.Bs) {
-      for (int d = 0; d < D; ++d) {
-        const S* Bd = a.B + (size_t)d * M * M;
-        T w = Num<T>::ld(Bd[ia * M + ib]);
-        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
-        s.Bs[d * P + p] = w;
-      }
-    }
   }
+  if (s.Bs) stage_sym_B<T, NT>(s.Bs, a.B, M, D, P);
   constexpr int KP = PPT > 0 ? PPT : 1;
   T acc[KP];
   int pab[KP];
@@ -350,8 +377,9 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
         }
       }
     };
-    // the common configuration (a full pass of points, m and v only, Q == QC, Dout == DB, B in
-    // shared memory): the same sums without branches, so the NPB points' exps interleave
+    // the common configuration (m and v only, Q == QC, Dout == DB, B in shared memory): the same
+    // sums without branches, so the NPB points' exps interleave.  In a pass with fewer than NPB
+    // points the extra slots run on stale tables; their sums are never read.
     auto do_pair_fast = [&](int p, int ia, int ib) {
       const T gab = s.G[p];
       T w[DB];
@@ -374,7 +402,7 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
         for (int d = 0; d < DB; ++d) vacc[pt][d] = fma_(w[d], ps, vacc[pt][d]);
       }
     };
-    const bool fast = PPT == 0 && npts == NPB && contract && !a.psi2 && Q == QC && D == DB && s.Bs;
+    const bool fast = PPT == 0 && contract && !a.psi2 && Q == QC && D == DB && s.Bs;
     if (fast) {
       for (int p = threadIdx.x; p < P; p += NT) {
         int ia, ib;
@@ -560,15 +588,8 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
       }
     }
     s.G[p] = neg(g);
-    if (s.Bs) {
-      for (int d = 0; d < D; ++d) {
-        const S* Bd = a.B + (size_t)d * M * M;
-        T w = Num<T>::ld(Bd[ia * M + ib]);
-        if (ia != ib) w = add(w, Num<T>::ld(Bd[ib * M + ia]));
-        s.Bs[d * P + p] = w;
-      }
-    }
   }
+  if (s.Bs) stage_sym_B<T, NTB>(s.Bs, a.B, M, D, P);
   // per-thread accumulators over points
   T g_sf = Num<T>::zero();                 // sum L1 + 2 sum L (for dsf2 * sf2)
   T g_l[QC];                               // dl (before the ell factor)
@@ -780,21 +801,21 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
         T R1 = Num<T>::zero(), S1[QC];
 #pragma unroll
         for (int q = 0; q < QC; ++q) S1[q] = Num<T>::zero();
+        // branch-free: a second column past M contributes zero, and dimensions q >= Q reuse
+        // dimension 0's coordinate in sums that are never stored
         for (int ib = sl; ib < M; ib += 16) {
-          const int jb = ib + 8;
+          const int jb = ib + 8, jc = jb < M ? jb : ib;
           const int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
+          const int p1 = ia >= jc ? rowbase + jc : jc * (jc + 1) / 2 + ia;
           const T l = Lp[p];
+          const T l1 = jb < M ? Lp[p1] : Num<T>::zero();
           R = add(R, l);
+          R1 = add(R1, l1);
 #pragma unroll
-          for (int q = 0; q < QC; ++q)
-            if (q < Q) Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
-          if (jb < M) {
-            const int p1 = ia >= jb ? rowbase + jb : jb * (jb + 1) / 2 + ia;
-            const T l1 = Lp[p1];
-            R1 = add(R1, l1);
-#pragma unroll
-            for (int q = 0; q < QC; ++q)
-              if (q < Q) S1[q] = fma_(l1, s.z[jb * Q + q], S1[q]);
+          for (int q = 0; q < QC; ++q) {
+            const int qq = q < Q ? q : 0;
+            Sq[q] = fma_(l, s.z[ib * Q + qq], Sq[q]);
+            S1[q] = fma_(l1, s.z[jc * Q + qq], S1[q]);
           }
         }
         R = add(R, R1);

@@ -90,6 +90,19 @@ def det_fwd(x, Z, lls2, lsf2, A, B, kfu=None, Bk=None, m_out=None, v_out=None):
          ptr(A), ptr(B), ptr(kfu), ptr(Bk), ptr(m_out), ptr(v_out), stream())
 
 
+def det_contract_supported(dtype, M, Dout):
+    """Whether gpk_det_contract takes these sizes (M <= 128, Dout M^2 in shared memory)."""
+    from . import _lib
+    return bool(_lib.lib().gpk_det_contract_supported(prec_of(dtype), int(M), int(Dout)))
+
+
+def det_contract(kfu, lsf2, A, B, Bk=None, m_out=None, v_out=None):
+    """m = kfu A^T, Bk[n,d] = B_d^T kfu_n, v = sf2 + kfu_n . Bk[n,d] from given kernel values."""
+    N, M = kfu.shape
+    call('gpk_det_contract', prec_of(kfu.dtype), N, M, A.shape[0], ptr(kfu), ptr(lsf2), ptr(A), ptr(B), ptr(Bk),
+         ptr(m_out), ptr(v_out), stream())
+
+
 def det_bwd(x, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dsf2, dl, dZ, dA, dx=None, dkfu=None, Dout=None, work=None):
     N, D = x.shape
     M = Z.shape[0]

@@ -312,14 +312,28 @@ class DevLayer:
         return phi_prior + (N / alpha - 1.0) * phi_post - (N / alpha) * phi_cav
 
     # ---------------------------------------------------------------- forward
-    def fwd_det(self, x, cav=True):
+    def kfu_rows(self, x, out=None):
+        """K(x, Z) [n, M] (gpk_kern, into `out` when given): needs only the inputs and the
+        kernel hyperparameters, so a model can form it ahead, beside the factorisations."""
+        if out is None:
+            out = torch.empty((x.shape[0], self.M), dtype=F64, device=self.dev)
+        return gpk.kern(x, self.zu, self.lls2, self.lsf2, out=out)
+
+    def fwd_det(self, x, cav=True, kfu=None):
+        """Deterministic-input forward (aep_models.py:142-158): (m, v, kfu, Bk).  With kfu
+        given (kfu_rows of the same x) only the contractions run."""
         n = x.shape[0]
         A, B = (self.Ah, self.Bh_det) if cav else (self.A, self.B_det)
-        kfu = torch.empty((n, self.M), dtype=F64, device=self.dev)
         Bk = torch.empty((n, self.Dout, self.M), dtype=F64, device=self.dev)
         m = torch.empty((n, self.Dout), dtype=F64, device=self.dev)
         v = torch.empty_like(m)
-        gpk.det_fwd(x, self.zu, self.lls2, self.lsf2, A, B, kfu, Bk, m, v)
+        if gpk.det_contract_supported(F64, self.M, self.Dout):
+            if kfu is None:
+                kfu = self.kfu_rows(x)
+            gpk.det_contract(kfu, self.lsf2, A, B, Bk, m, v)
+        else:
+            kfu = torch.empty((n, self.M), dtype=F64, device=self.dev)
+            gpk.det_fwd(x, self.zu, self.lls2, self.lsf2, A, B, kfu, Bk, m, v)
         return m, v, kfu, Bk
 
     def fwd_mm(self, mx, vx, cav=True):
@@ -646,16 +660,25 @@ class DevLayer:
             self.zero_accumulators()
         dZ = self.g['zu']
         dAh, dBh = self._dAh, self._dBh
+        main = torch.cuda.current_stream()
+        if self.side is not None:
+            # dBhat = sum_n dv_n kfu_n kfu_n^T needs nothing of the row backward: it runs beside
+            # it on the side stream, and the algebra below waits for it alone
+            self.side.wait_stream(main)
+            with torch.cuda.stream(self.side):
+                gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
+                gram_done = torch.cuda.Event()
+                gram_done.record()
         gpk.det_bwd(x, self.zu, self.lls2, self.lsf2, self.Ah, kfu, Bk, dm, dv, self._dsf2, self._dl, dZ, dAh,
                     dx=dx, work=self.work(gpk.OP_DET_BWD))
-        main = torch.cuda.current_stream()
         if self.side is not None:   # the chain rule beside the algebra; joined before trace_kzz
             self.side.wait_stream(main)
             with torch.cuda.stream(self.side):
                 self._kernel_grads(self._dsf2, self._dl, dv)
+            main.wait_event(gram_done)
         else:
             self._kernel_grads(self._dsf2, self._dl, dv)
-        gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
+            gpk.gram(kfu, kfu, dv, dBh, work=self.work(gpk.OP_GRAM))
         # d theta_1 and d theta_2 through G = K^-1 Suhat (compute_cav_grad_u and
         # compute_posterior_grad_u, aep_models.py:548-586 and base_models.py:490-516, whose
         # sandwiches by Suhat / Su and K^-1 collapse): with w0 = G^T dAhat, w = w0 + s_cav muhat,
@@ -722,13 +745,17 @@ def gauss_dsn(dv, nb, D, sn, alpha, scale):
     return scale * (dv.sum() * 2 * sn2 / alpha + nb * D * (1 - alpha))
 
 
-def setup_layers(layers, alpha, streams=None):
+def setup_layers(layers, alpha, streams=None, ahead=None):
     """Posterior + cavity of several layers with batched factorisations: one SPD inverse for
     every layer's Kuu (grouped by M), then one for every Su^-1 and Suhat^-1 (natural-parameter
     layers; others take the per-layer path).  With side `streams`, each layer's parameter
     unpacking and Kuu run on its own stream, and theta_1 = R^T R alongside the Kuu inverse
-    (parallel branches of a captured graph).  Returns the int32 Cholesky status words of the
-    factorisations (0 = fine), for one reduction at the end of the evaluation."""
+    (parallel branches of a captured graph).  `ahead` maps a layer to a callable that is
+    issued right after that layer's hyperparameters are unpacked, on the same side stream
+    (beside the factorisations; the callable records what its consumer waits for).  Returns
+    the int32 Cholesky status words of the factorisations (0 = fine), for one reduction at the
+    end of the evaluation."""
+    ahead = ahead or {}
     nat = [l for l in layers if l.nat]
     statuses = []
     for l in layers:
@@ -736,6 +763,8 @@ def setup_layers(layers, alpha, streams=None):
             l.setup_posterior()
             l.setup_cavity(alpha)
             statuses.append(l.info)
+            if l in ahead:
+                ahead[l]()
     by_m = {}
     for l in nat:
         by_m.setdefault(l.M, []).append(l)
@@ -755,9 +784,13 @@ def setup_layers(layers, alpha, streams=None):
                 with torch.cuda.stream(s_i):
                     l.prep_r()
                     l.prep_k(out=K[i])
-                forked.append(s_i)
-            for s_i in forked:   # join only the branches forked here (graph-capture rule)
-                main.wait_stream(s_i)
+                    prepped = torch.cuda.Event()
+                    prepped.record()
+                    if l in ahead:   # stays on the branch: joined by its consumer or below
+                        ahead[l]()
+                forked.append((s_i, prepped))
+            for s_i, prepped in forked:   # the Kuu inverse waits for the preparations only
+                main.wait_event(prepped)
             s_th = side[0]
             s_th.wait_stream(main)
             with torch.cuda.stream(s_th), gpk.GemmGroup() as g:
@@ -771,6 +804,8 @@ def setup_layers(layers, alpha, streams=None):
                     l.prep_th1(g)
             for i, l in enumerate(group):
                 l.prep_k(out=K[i])
+                if l in ahead:
+                    ahead[l]()
         Kinv = torch.empty_like(K)
         ld = torch.empty(G, dtype=F64, device=dev)
         gpk.chol_inv(K, Kinv, None, ld, info[:G])

@@ -101,6 +101,17 @@ int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx,
                 const double* lls2, const double* lsf2, const void* A, const void* B, void* kfu,
                 void* Bk, void* m_out, void* v_out, void* stream);
 
+/* The contractions of gpk_det_fwd from given kernel values kfu [N,M] (e.g. from gpk_kern):
+ *   m[n,d] = kfu_n . A_d;  Bk[n,d,b] = sum_a B[d,a,b] kfu[n,a];  v[n,d] = sf2 + kfu_n . Bk[n,d]
+ * so that kfu, which needs only the inputs and the kernel hyperparameters, can be formed
+ * ahead (beside the factorisations that the cavity's A and B wait for).  Needs M <= 128 and
+ * Dout M^2 elements in shared memory (gpk_det_contract_supported says whether a size is
+ * supported; an unsupported one returns GPK_EUNSUPPORTED).  Bk, m_out, v_out optional.
+ * Replaces the Kfu contractions of geepee/aep_models.py:142-158 (base_models.py:265-284). */
+int gpk_det_contract_supported(int prec, int M, int Dout);
+int gpk_det_contract(int prec, int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A,
+                     const void* B, void* Bk, void* m_out, void* v_out, void* stream);
+
 /* Deterministic-input layer, backward through kfu:
  *   dkfu = dm A + 2 dv Bk   (or the given dkfu [N,M] when dkfu != NULL)
  * returns (+=, float64) dsf2 [1], dl [D] (w.r.t. ell), dZ [M,D], dA [Dout,M] += dm^T kfu,

@@ -300,6 +300,70 @@ def test_det_layer_fwd_bwd_vs_oracle(N, M, D, Dout):
     assert_close(c.cpu().numpy(), dm.T @ kfu, 1e-10, 'wsum')
 
 
+@pytest.mark.parametrize('N,M,Dout', [(1000, 100, 2), (301, 30, 2), (9, 128, 1), (17, 64, 3), (1, 1, 1), (8, 33, 4)])
+def test_det_contract_vs_oracle_and_det_fwd(N, M, Dout):
+    """The contractions from given kernel values (gpk_kern then gpk_det_contract) against the
+    oracle and against the fused gpk_det_fwd (the same sums over a in the same order; the fused
+    kernel keeps its kernel values in double-float, the contraction reads them back from
+    float64, so the two may differ in the last bits); ragged row tiles and column slots past M."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(11 + N + M)
+    D = 3
+    x, Z = rng.randn(N, D), rng.randn(M, D)
+    ls, sf = rng.uniform(-0.3, 0.5, D), np.array([0.2])
+    A, B = rng.randn(Dout, M), rng.randn(Dout, M, M)
+    kfu = O.ard_kernel(2 * ls, 2 * sf, x, Z)
+    m_ref = kfu @ A.T
+    v_ref = np.exp(2 * sf) + np.einsum('dab,na,nb->nd', B, kfu, kfu)
+    xt, Zt, At, Bt, l2, s2 = dev(x), dev(Z), dev(A), dev(B), dev(2 * ls), dev(2 * sf)
+    if not gpk.det_contract_supported(torch.float64, M, Dout):
+        pytest.skip('size outside the contraction kernel')
+    kt = gpk.kern(xt, Zt, l2, s2)
+    Bk = torch.empty((N, Dout, M), dtype=torch.float64, device='cuda')
+    m, v = torch.empty((N, Dout), dtype=torch.float64, device='cuda'), torch.empty((N, Dout), dtype=torch.float64, device='cuda')
+    gpk.det_contract(kt, s2, At, Bt, Bk, m, v)
+    assert_close(m.cpu().numpy(), m_ref, DF64_TOL, 'm')
+    assert_close(v.cpu().numpy(), v_ref, DF64_TOL, 'v')
+    assert_close(Bk.cpu().numpy(), np.einsum('dab,na->ndb', B, kfu), DF64_TOL, 'Bk')
+    k2, Bk2 = torch.empty_like(kt), torch.empty_like(Bk)
+    gpk.det_fwd(xt, Zt, l2, s2, At, Bt, k2, Bk2, torch.empty_like(m), torch.empty_like(v))
+    assert torch.equal(k2, kt), 'gpk_kern and gpk_det_fwd kernel values differ'
+    assert_close(Bk.cpu().numpy(), Bk2.cpu().numpy(), 1e-14, 'Bk vs the fused forward')
+
+
+@pytest.mark.parametrize('N,M,Dout', [(1000, 100, 2), (20000, 100, 1), (7, 1, 1), (33, 129, 3), (300, 64, 4), (5, 200, 2)])
+def test_gram_fixed_order_vs_oracle(N, M, Dout):
+    """The symmetric fixed-order Gram reduction (unordered pairs, packed partial blocks, then
+    the fixed-order sum that writes both triangles) against the oracle, bit-identical on
+    repetition; the non-symmetric fixed-order form too."""
+    from geepee_gb300 import gpk
+    rng = np.random.RandomState(N + M + Dout)
+    u, w = rng.randn(N, M), rng.randn(N, Dout)
+    ut, wt = dev(u), dev(w)
+    ref = np.einsum('nd,na,nb->dab', w, u, u)
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    work = z(gpk.work_elems(gpk.OP_GRAM, N, M, 1, Dout))
+    C1, C2 = z(Dout, M, M), z(Dout, M, M)
+    gpk.gram(ut, ut, wt, C1, work=work)
+    gpk.gram(ut, ut, wt, C2, work=work)
+    assert_close(C1.cpu().numpy(), ref, 1e-10, 'gram pairs')
+    assert torch.equal(C1, C2), 'fixed-order gram differs between calls'
+    v = rng.randn(N, M)
+    C3 = z(Dout, M, M)
+    gpk.gram(ut, dev(v), wt, C3, work=work)
+    assert_close(C3.cpu().numpy(), np.einsum('nd,na,nb->dab', w, u, v), 1e-10, 'gram u != v')
+
+
+def test_det_contract_rejects_unsupported_sizes():
+    from geepee_gb300 import gpk
+    from geepee_gb300._lib import GpkError
+    assert not gpk.det_contract_supported(torch.float64, 129, 1)
+    assert not gpk.det_contract_supported(torch.float64, 100, 4)
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    with pytest.raises(GpkError):
+        gpk.det_contract(z(4, 129), z(1), z(1, 129), z(1, 129, 129), z(4, 1, 129), z(4, 1), z(4, 1))
+
+
 def test_psi_size_limits_are_reported():
     """Sizes beyond the register-resident pair tables (forward sum_n psi2) or beyond shared
     memory (backward) are refused, not silently truncated."""
