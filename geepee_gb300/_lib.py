@@ -34,7 +34,7 @@ _SIGS = {
     'gpk_det_fwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _vp, _vp, _vp, _vp,
                     _vp, _vp, _vp, _vp, _vp],
     'gpk_det_contract_supported': [_c_int, _c_int, _c_int],
-    'gpk_det_contract': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    'gpk_det_contract': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
     'gpk_det_bwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _vp, _vp, _vp, _vp,
                     _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     'gpk_gram': [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],

@@ -433,6 +433,10 @@ __global__ void __launch_bounds__(256) cavity_forms_kernel(FormsArgs f) {
     const int r = (int)(e / M), q = (int)(e - (long)r * M);
     const double bd = wc ? b * b * g.Qh[o + e] - b * T[e] : g.Qh[o + e] - g.Kinv[e];
     g.Bd[o + e] = bd;
+    if (g.Bd_pair) {   // the same value as a double-float pair
+      const df64 v = df_from_double(bd);
+      reinterpret_cast<float2*>(g.Bd_pair)[o + e] = make_float2(v.hi, v.lo);
+    }
     g.Bp[o + e] = wp ? g.Qu[o + e] - T[e] : g.Qu[o + e] - g.Kinv[e];
     const double ar = wc ? b * t[r] - b * vh[r] : vh[r];
     const double aq = wc ? b * t[q] - b * vh[q] : vh[q];

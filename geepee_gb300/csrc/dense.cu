@@ -959,9 +959,6 @@ int spd_inv_small(int batch, int M, const void* A, void* Ainv, double* logdet, i
   if (M <= 32) rc = spd_factor_launch<T, 1, 2, 16>(batch, M, A, Lw, logdet, info, st);
   else if (M <= 64) rc = spd_factor_launch<T, 2, 4, 16>(batch, M, A, Lw, logdet, info, st);
   else if (M <= 96) rc = spd_factor_launch<T, 3, 6, 16>(batch, M, A, Lw, logdet, info, st);
-#ifdef GPK_SPD_NW32
-  else if (M <= 128) rc = spd_factor_launch<T, 4, 4, 32>(batch, M, A, Lw, logdet, info, st);
-#endif
   else if (M <= 112) rc = spd_factor_launch<T, 4, 7, 16>(batch, M, A, Lw, logdet, info, st);
   else rc = spd_factor_launch<T, 4, 8, 16>(batch, M, A, Lw, logdet, info, st);
   if (rc) return rc;

@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(CT) det_contract_kernel(int N, int M, int Dout
                                                           const typename Num<T>::store_t* B,
                                                           typename Num<T>::store_t* Bk,
                                                           typename Num<T>::store_t* m_out,
-                                                          typename Num<T>::store_t* v_out) {
+                                                          typename Num<T>::store_t* v_out, int b_pairs) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(CT) det_contract_kernel(int N, int M, int Dout
   stage_async(reinterpret_cast<S*>(kr), kfu + (size_t)n0 * M, (long)nr * M, tid, CT);
   load_exp_table(tab);
   __syncthreads();
-  convert_in_place(Bs, nB, tid, CT);
+  if (!b_pairs) convert_in_place(Bs, nB, tid, CT);   // pairs arrive in the compute type already
   convert_in_place(kr, (long)nr * M, tid, CT);
   __syncthreads();
   const bool live = n < N;   // warp-uniform; a dead row still reaches the barrier below
@@ -753,20 +753,20 @@ extern "C" int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* 
 namespace {
 template <typename T, int DB>
 void contract_launch(int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A, const void* B,
-                     void* Bk, void* m_out, void* v_out, cudaStream_t st) {
+                     int b_pairs, void* Bk, void* m_out, void* v_out, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
   const size_t sm = det_contract_smem(M, Dout, sizeof(T));
   auto k = det_contract_kernel<T, DB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<gpk::ceil_div(N, CR), CT, sm, st>>>(N, M, Dout, (const S*)kfu, lsf2, (const S*)A, (const S*)B, (S*)Bk,
-                                          (S*)m_out, (S*)v_out);
+                                          (S*)m_out, (S*)v_out, b_pairs);
 }
 template <typename T>
 void contract_dispatch(int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A, const void* B,
-                       void* Bk, void* m_out, void* v_out, cudaStream_t st) {
-  if (Dout == 1) contract_launch<T, 1>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
-  else if (Dout == 2) contract_launch<T, 2>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
-  else contract_launch<T, 4>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+                       int b_pairs, void* Bk, void* m_out, void* v_out, cudaStream_t st) {
+  if (Dout == 1) contract_launch<T, 1>(N, M, Dout, kfu, lsf2, A, B, b_pairs, Bk, m_out, v_out, st);
+  else if (Dout == 2) contract_launch<T, 2>(N, M, Dout, kfu, lsf2, A, B, b_pairs, Bk, m_out, v_out, st);
+  else contract_launch<T, 4>(N, M, Dout, kfu, lsf2, A, B, b_pairs, Bk, m_out, v_out, st);
 }
 }  // namespace
 
@@ -776,9 +776,10 @@ extern "C" int gpk_det_contract_supported(int prec, int M, int Dout) {
 }
 
 extern "C" int gpk_det_contract(int prec, int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A,
-                                const void* B, void* Bk, void* m_out, void* v_out, void* stream) {
+                                const void* B, int b_pairs, void* Bk, void* m_out, void* v_out, void* stream) {
   GPK_NVTX("gpk_det_contract");
   GPK_REQUIRE(prec == GPK_DF64 || prec == GPK_FP32, "det_contract: unknown precision %d", prec);
+  GPK_REQUIRE(!b_pairs || prec == GPK_DF64, "det_contract: double-float pairs need GPK_DF64");
   GPK_REQUIRE(N >= 0 && M >= 1 && Dout >= 1, "det_contract: bad sizes N=%d M=%d Dout=%d", N, M, Dout);
   if (!gpk_det_contract_supported(prec, M, Dout))
     return gpk::fail(GPK_EUNSUPPORTED, "det_contract: M=%d, Dout=%d (needs M <= 128 and Dout M^2 in shared memory)",
@@ -786,8 +787,8 @@ extern "C" int gpk_det_contract(int prec, int N, int M, int Dout, const void* kf
   GPK_REQUIRE(kfu && lsf2 && A && B, "det_contract: null input");
   if (N == 0) return GPK_OK;
   cudaStream_t st = gpk::as_stream(stream);
-  if (prec == GPK_DF64) contract_dispatch<df64>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
-  else contract_dispatch<float>(N, M, Dout, kfu, lsf2, A, B, Bk, m_out, v_out, st);
+  if (prec == GPK_DF64) contract_dispatch<df64>(N, M, Dout, kfu, lsf2, A, B, b_pairs, Bk, m_out, v_out, st);
+  else contract_dispatch<float>(N, M, Dout, kfu, lsf2, A, B, 0, Bk, m_out, v_out, st);
   return gpk::check_launch("det_contract");
 }
 

@@ -96,11 +96,12 @@ def det_contract_supported(dtype, M, Dout):
     return bool(_lib.lib().gpk_det_contract_supported(prec_of(dtype), int(M), int(Dout)))
 
 
-def det_contract(kfu, lsf2, A, B, Bk=None, m_out=None, v_out=None):
-    """m = kfu A^T, Bk[n,d] = B_d^T kfu_n, v = sf2 + kfu_n . Bk[n,d] from given kernel values."""
+def det_contract(kfu, lsf2, A, B, Bk=None, m_out=None, v_out=None, b_pairs=False):
+    """m = kfu A^T, Bk[n,d] = B_d^T kfu_n, v = sf2 + kfu_n . Bk[n,d] from given kernel values;
+    b_pairs: B holds double-float pairs (cavity_forms' Bd_pair) rather than float64 values."""
     N, M = kfu.shape
-    call('gpk_det_contract', prec_of(kfu.dtype), N, M, A.shape[0], ptr(kfu), ptr(lsf2), ptr(A), ptr(B), ptr(Bk),
-         ptr(m_out), ptr(v_out), stream())
+    call('gpk_det_contract', prec_of(kfu.dtype), N, M, A.shape[0], ptr(kfu), ptr(lsf2), ptr(A), ptr(B),
+         int(bool(b_pairs)), ptr(Bk), ptr(m_out), ptr(v_out), stream())
 
 
 def det_bwd(x, Z, lls2, lsf2, A, kfu, Bk, dm, dv, dsf2, dl, dZ, dA, dx=None, dkfu=None, Dout=None, work=None):
@@ -349,7 +350,7 @@ class _Forms(ctypes.Structure):
     """gpk_forms_t (include/gpk.h)."""
     _fields_ = [('D', ctypes.c_int), ('M', ctypes.c_int), ('beta', ctypes.c_double)] + \
         [(n, ctypes.c_void_p) for n in ('T', 'Kinv', 't', 'Qh', 'Qu', 'vh', 'vu', 'Ph', 'flags', 'Bd', 'Bp', 'Bsto',
-                                        'Ah', 'A', 'G')]
+                                        'Ah', 'A', 'G', 'Bd_pair')]
 
 
 _FORMS_MAX = 8   # GPK_FORMS_MAX

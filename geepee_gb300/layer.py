@@ -197,10 +197,13 @@ class DevLayer:
         self.Ah = torch.empty_like(self.mh)
         self.Apost = torch.empty_like(self.mu)
         self.G = torch.empty_like(self._Qh)
+        # Bhat_det again as double-float pairs (8 bytes an element, like float64): the first
+        # layer's contraction reads it without converting
+        self.Bh_det_pair = torch.empty_like(self._Qh)
         sq = lambda v: v.reshape(v.shape[0], -1)
         return dict(D=self.Dout, M=self.M, beta=self.beta, T=self.th1, Kinv=self.Kinv, t=self.th2, Qh=self._Qh,
                     Qu=self._Qu, vh=sq(self._vh), vu=sq(self._vu), Ph=self._Ph, flags=self.flags, Bd=self.Bh_det,
-                    Bp=self.Bpost, Bsto=self.Bh_sto, Ah=self.Ah, A=self.Apost, G=self.G)
+                    Bp=self.Bpost, Bsto=self.Bh_sto, Ah=self.Ah, A=self.Apost, G=self.G, Bd_pair=self.Bh_det_pair)
 
     def _kuu_grad_levels(self, dAh, dBh, sto, alpha):
         """The gradient of the layer's energy w.r.t. Kuu, summed over outputs, without products
@@ -330,7 +333,8 @@ class DevLayer:
         if gpk.det_contract_supported(F64, self.M, self.Dout):
             if kfu is None:
                 kfu = self.kfu_rows(x)
-            gpk.det_contract(kfu, self.lsf2, A, B, Bk, m, v)
+            pairs = cav and getattr(self, 'Bh_det_pair', None) is not None
+            gpk.det_contract(kfu, self.lsf2, A, self.Bh_det_pair if pairs else B, Bk, m, v, b_pairs=pairs)
         else:
             kfu = torch.empty((n, self.M), dtype=F64, device=self.dev)
             gpk.det_fwd(x, self.zu, self.lls2, self.lsf2, A, B, kfu, Bk, m, v)

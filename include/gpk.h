@@ -107,10 +107,12 @@ int gpk_det_fwd(int prec, int N, int M, int D, int Dout, const void* x, int ldx,
  * ahead (beside the factorisations that the cavity's A and B wait for).  Needs M <= 128 and
  * Dout M^2 elements in shared memory (gpk_det_contract_supported says whether a size is
  * supported; an unsupported one returns GPK_EUNSUPPORTED).  Bk, m_out, v_out optional.
+ * b_pairs != 0 (GPK_DF64 only): B holds double-float (hi, lo) float pairs, as gpk_cavity_forms
+ * writes them into Bd_pair, and is read without conversion.
  * Replaces the Kfu contractions of geepee/aep_models.py:142-158 (base_models.py:265-284). */
 int gpk_det_contract_supported(int prec, int M, int Dout);
 int gpk_det_contract(int prec, int N, int M, int Dout, const void* kfu, const double* lsf2, const void* A,
-                     const void* B, void* Bk, void* m_out, void* v_out, void* stream);
+                     const void* B, int b_pairs, void* Bk, void* m_out, void* v_out, void* stream);
 
 /* Deterministic-input layer, backward through kfu:
  *   dkfu = dm A + 2 dv Bk   (or the given dkfu [N,M] when dkfu != NULL)
@@ -271,7 +273,9 @@ int gpk_regime(int D, int M, double beta, const double* T, const double* Kinv, i
  *   posterior likewise with bit 1, beta = 1, Qu (T Su T or K^-1 Su K^-1), vu (T mu or K^-1 mu):
  *   B = Qu - T or Qu - K^-1,  A = t - vu or vu;
  * Bhat_sto = Bhat_det + Ahat Ahat^T, and G = K^-1 Suhat (= I - beta Ph when bit 0 is set, Ph
- * = T Suhat; = Ph = K^-1 Suhat otherwise), which the backward's algebra uses.  Qh, Qu [D,M,M],
+ * = T Suhat; = Ph = K^-1 Suhat otherwise), which the backward's algebra uses.  Bd_pair
+ * (optional, D M M pairs of floats) receives Bhat_det again as double-float (hi, lo) pairs, the
+ * form gpk_det_contract reads without converting.  Qh, Qu [D,M,M],
  * vh, vu [D,M] and Ph are the products of the selected form (gpk_gemm_t's sel).  Elementwise
  * float64.  The quantities of geepee/aep_models.py:536-546 and base_models.py:480-488, which
  * always take the K^-1 form. */
@@ -281,6 +285,7 @@ typedef struct {
   const double *T, *Kinv, *t, *Qh, *Qu, *vh, *vu, *Ph;
   const int* flags;
   double *Bd, *Bp, *Bsto, *Ah, *A, *G;
+  float* Bd_pair;
 } gpk_forms_t;
 #define GPK_FORMS_MAX 8
 int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream);

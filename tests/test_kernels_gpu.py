@@ -325,6 +325,14 @@ def test_det_contract_vs_oracle_and_det_fwd(N, M, Dout):
     assert_close(m.cpu().numpy(), m_ref, DF64_TOL, 'm')
     assert_close(v.cpu().numpy(), v_ref, DF64_TOL, 'v')
     assert_close(Bk.cpu().numpy(), np.einsum('dab,na->ndb', B, kfu), DF64_TOL, 'Bk')
+    # B as double-float pairs (hi = B rounded to float, lo = the rest rounded), the form the
+    # cavity kernel writes: the same results bit for bit
+    hi = B.astype(np.float32)
+    lo = (B - hi.astype(np.float64)).astype(np.float32)
+    pairs = torch.as_tensor(np.stack([hi, lo], -1), device='cuda').contiguous()
+    Bk3, m3, v3 = torch.empty_like(Bk), torch.empty_like(m), torch.empty_like(v)
+    gpk.det_contract(kt, s2, At, pairs, Bk3, m3, v3, b_pairs=True)
+    assert torch.equal(Bk3, Bk) and torch.equal(m3, m) and torch.equal(v3, v), 'pair input differs'
     k2, Bk2 = torch.empty_like(kt), torch.empty_like(Bk)
     gpk.det_fwd(xt, Zt, l2, s2, At, Bt, k2, Bk2, torch.empty_like(m), torch.empty_like(v))
     assert torch.equal(k2, kt), 'gpk_kern and gpk_det_fwd kernel values differ'
