@@ -258,15 +258,18 @@ class _PackedModel(Base_Model):
         first = next(k for k in keys if k in ('sn', 'x1', '__energy__'))
         return int(self.gpack.offsets[keys.index(first)])
 
-    def _energy_terms(self, layers, alpha, N, statuses):
+    def _energy_terms(self, layers, alpha, N, statuses, phi_sum=None):
         """energy += sum of the layers' weighted log-partitions / N (fused for natural-parameter
-        layers); then one launch divides the layer gradients by N and, for a single status
-        buffer, records the worst Cholesky status."""
-        for lay in layers:
-            if lay.nat:
-                lay.phi(alpha, out=self.energy, w=1.0 / N)
-            else:
-                self.energy.add_(lay.phi(alpha).reshape(1) / N)
+        layers; or the sum formed ahead, `phi_sum`); then one launch divides the layer gradients
+        by N and, for a single status buffer, records the worst Cholesky status."""
+        if phi_sum is not None:
+            self.energy.add_(phi_sum)
+        else:
+            for lay in layers:
+                if lay.nat:
+                    lay.phi(alpha, out=self.energy, w=1.0 / N)
+                else:
+                    self.energy.add_(lay.phi(alpha).reshape(1) / N)
         g = self.gpack.dev[:self._layer_grad_span()]
         if len(statuses) == 1:
             gpk.finish(g, N, statuses[0].reshape(-1), self.gpack.views['__info__'])
@@ -412,6 +415,7 @@ class SDGPR(_PackedModel):
         self.sgp_layers = self.layers
         self.x_dev = _to_dev(x_train, self.dev)
         self.y_dev = _to_dev(y_train, self.dev)
+        self._phi_sum = torch.zeros(1, dtype=torch.float64, device=self.dev)   # fixed address
 
     def init_hypers(self, y_train=None):
         """Base_SDGPR.init_hypers (base_models.py:1290-1312)."""
@@ -449,6 +453,10 @@ class SDGPR(_PackedModel):
         with torch.cuda.stream(side[0]):
             for lay in self.layers:
                 lay.zero_accumulators()
+            # the layers' log-partitions need only the setup: summed here, beside the forward
+            self._phi_sum.zero_()
+            for lay in self.layers:
+                lay.phi(alpha, out=self._phi_sum, w=1.0 / N)
         ms, vs = [], []
         m, v, kfu, Bk = self.layers[0].fwd_det(xb, kfu=k0.get('kfu'))
         ms.append(m)
@@ -491,7 +499,7 @@ class SDGPR(_PackedModel):
         for lay in self.layers:
             lay.prezeroed = False
         self.layers[0].side = None
-        self._energy_terms(self.layers, alpha, N, st)
+        self._energy_terms(self.layers, alpha, N, st, phi_sum=self._phi_sum)
         return self.energy
 
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):

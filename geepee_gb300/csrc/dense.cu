@@ -249,30 +249,38 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar) {
 
 // Right-looking Cholesky of one M x M SPD matrix per CTA (M <= min(32*RS, NW*CS)).  Element
 // (i, j) of the lower triangle lives in a register of lane i % 32 of warp j % NW (slot
-// [i/32][j/NW]), so a trailing update touches no shared memory except the column of L it
+// [i/32][j/NW]), so a trailing update touches no shared memory except the columns of L it
 // reads.  Column k of L is published by its owner warp through an mbarrier of its own (32
-// arrivals); a warp waits only for the column it applies next, so there is no CTA barrier in
-// the loop.  The warp owning column k+1 applies column k to it first, takes its pivot and
-// publishes it before updating its other columns.  Outputs: Lw (column-major L as raw (hi, lo)
-// pairs, 1/L_kk on the diagonal - the input of trinv_kernel), logdet = sum log L_kk^2,
-// info[b] = k+1 for a non-positive pivot (M+1 if a bounded wait ran out, never expected).
+// arrivals); a warp waits only for the columns it applies, so there is no CTA barrier in the
+// loop.  Step (k0, k1) = (2s, 2s+1) applies both columns to every column right of k1 (two
+// multiply-adds per register slot), so a warp waits, loads its row multipliers and walks its
+// columns once per two columns.  Look-ahead: the owner of k2 = k1 + 1 applies the pair to that
+// column and publishes it first; the owner of k3 = k2 + 1 applies the pair to k3, waits for k2,
+// applies it and publishes k3; then both take their other columns.  The pair (k2, k3) lies in
+// one segment of NW columns (NW even, pairs aligned), so its owners' register slot is a
+// compile-time index.  Row multipliers are read for every row slot without a predicate: rows at
+// or above the pair, and rows past M, only reach register slots above the diagonal or past M,
+// which are never read (the column stores cover rows k < i < M, the pivot row k itself); the
+// shared-memory area has slack for reads past the last column.  Outputs: Lw (column-major L as
+// raw (hi, lo) pairs, 1/L_kk on the diagonal - the input of trinv_kernel), logdet = sum log
+// L_kk^2, info[b] = k+1 for a non-positive pivot (M+1 if a bounded wait ran out, never expected).
 template <typename T, int RS, int CS, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typename Num<T>::store_t* A, long sA,
-                                                                T* Lw, double* logdet, int* info) {
+                                                                 T* Lw, double* logdet, int* info) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   const int LD = M | 1;
-  T* Ls = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][LD], column k at Ls + k*LD
-  T* dg = Ls + (size_t)M * LD;                                       // [M] L_kk
+  T* Ls = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][LD] + 32 RS slack
+  T* dg = Ls + (size_t)M * LD + 32 * RS;                             // [M] L_kk^2
   T* red = dg + M;                                                   // [NW]
   __shared__ int s_info, s_err;
   __shared__ __align__(8) unsigned long long s_bar[32 * RS];   // column k published (32 arrivals)
   const int b = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int NTH = NW * 32;
+  static_assert(32 % NW == 0 && NW >= 2 && NW % 2 == 0, "NW must be even and divide 32");
   A += b * sA;
   {
-    // stage A (row-major, storage type) in the Ls area with asynchronous copies
     S* raw = reinterpret_cast<S*>(Ls);
     for (int e = threadIdx.x; e < M * M; e += NTH) {
       const unsigned dst = (unsigned)__cvta_generic_to_shared(raw + e);
@@ -299,16 +307,14 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
       }
   }
   __syncthreads();   // the staging area becomes L
+  // the slack rows past the last column: defined values (zeros) for the predicate-free reads
+  for (int e = threadIdx.x; e < 32 * RS; e += NTH) Ls[(size_t)M * LD + e] = Num<T>::zero();
 
-  // column k of L from the registers of warp k % NW; CK = k / NW and RK = k / 32 are
-  // compile-time slot indices (warp-uniform caller)
   auto finalize = [&](int k, auto CK, auto RK) {
     const T p = shfl_idx(a[RK.value][CK.value], k & 31);
     if (!(Num<T>::approx(p) > 0.f)) {
       if (lane == 0) s_info = k + 1;
       __syncwarp();
-      // complete every remaining column's barrier: warps already waiting further on wake,
-      // see s_info and stop (no later column is published after a failure)
       for (int c = k; c < M; ++c) mbar_arrive(&s_bar[c]);
       return;
     }
@@ -320,76 +326,100 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     }
     if (lane == 0) {
       Ls[k * LD + k] = r;
-      dg[k] = p;   // L_kk^2
+      dg[k] = p;
     }
     __syncwarp();
-    mbar_arrive(&s_bar[k]);   // every lane arrives: each releases its own stores of column k
+    mbar_arrive(&s_bar[k]);
+  };
+  // -(column k) at this thread's row slots, every slot (see above)
+  auto multipliers = [&](int k, T (&l)[RS]) {
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) l[rr] = neg(Ls[k * LD + lane + 32 * rr]);
+  };
+  // bounded wait for column k; false: stop (a wait ran out, or a pivot failed)
+  auto await = [&](int k) {
+    if (!mbar_wait(&s_bar[k])) {
+      if (lane == 0) s_err = 1;
+      return false;
+    }
+    return s_info == 0;
   };
 
+  // columns 0 and 1 before the first step
   if (w == 0) finalize(0, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
-  // step k applies column k to the columns > k; the column k1 = k + 1 that its owner warp
-  // finalises after updating it is written k1 = 32 KB + NW H + kk (KB, H compile-time), so
-  // the owner's slots are compile-time indices too.  No CTA barrier: a warp waits only for the
-  // column it applies (its mbarrier), so warps drift apart and the owner of column k1 publishes
-  // it as soon as column k has reached it.
-  static_assert(32 % NW == 0 && NW > 1, "NW must divide 32");
-  const int last = w + NW * ((M - 1 - w) / NW);   // this warp's last column (w < M)
-  bool stop = w >= M;
+  if (w == 1 && M > 1) {
+    if (await(0)) {
+      T l0[RS];
+      multipliers(0, l0);
+      const T l01 = Ls[0 * LD + 1];
+#pragma unroll
+      for (int rr = 0; rr < RS; ++rr) a[rr][0] = fma_(l0[rr], l01, a[rr][0]);
+      finalize(1, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+    }
+  }
+  const int ncol = w < M ? (M - 1 - w) / NW + 1 : 0;   // this warp's columns
+  const int last = w + NW * (ncol - 1);
+  bool stop = ncol == 0;
   static_for<0, RS>([&](auto KB) {
     static_for<0, 32 / NW>([&](auto H) {
       constexpr int kb = KB.value;
-      constexpr int C1 = (32 * kb + NW * H.value) / NW;   // slot of column k1 in its owner warp
-      const int base = 32 * kb + NW * H.value;             // k1 = base + kk
-      for (int kk = 0; kk < NW && !stop; ++kk) {
-        const int k1 = base + kk, k = k1 - 1;
-        if (k1 == 0) continue;
-        if (k1 >= M || k >= last) {   // no column of this warp is right of column k
+      constexpr int C = (32 * kb + NW * H.value) / NW;   // slot of the look-ahead pair in its owners
+      const int base = 32 * kb + NW * H.value;
+      for (int kk = 0; kk < NW && !stop; kk += 2) {
+        const int k2 = base + kk, k3 = k2 + 1, k0 = k2 - 2, k1 = k2 - 1;
+        if (k2 == 0) continue;   // columns 0 and 1 were taken above
+        if (k1 >= M - 1 || last <= k1) {   // nothing of this warp right of the pair
           stop = true;
           break;
         }
-        if (!mbar_wait(&s_bar[k])) {   // bounded; never expected to run out
-          if (lane == 0) s_err = 1;
+        if (!await(k1)) {   // k1 published implies k0 published
           stop = true;
           break;
         }
-        if (s_info) {   // a pivot failed (written before its column's arrival)
-          stop = true;
-          break;
-        }
-        // slots wholly above row k + 1 meet no active column (rows < 32 rr + 32 <= k + 1 < j)
-        T li[RS];
+        T l0[RS], l1[RS];
+        multipliers(k0, l0);
+        multipliers(k1, l1);
+        const bool own2 = w == kk, own3 = w == kk + 1 && k3 < M;
+        if (own2) {   // look-ahead: column k2
+          const T x0 = Ls[k0 * LD + k2], x1 = Ls[k1 * LD + k2];
 #pragma unroll
-        for (int rr = 0; rr < RS; ++rr) {
-          const int i = lane + 32 * rr;
-          li[rr] = Num<T>::zero();
-          if (32 * rr + 31 > k && i > k && i < M) li[rr] = neg(Ls[k * LD + i]);
+          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][C]));
+          finalize(k2, std::integral_constant<int, C>{}, KB);
         }
-        if (w == kk) {   // owner of column k1: that column first, publish, then the others
-          const T ljk = Ls[k * LD + k1];
+        if (own3) {   // look-ahead: column k3, which also needs column k2
+          const T x0 = Ls[k0 * LD + k3], x1 = Ls[k1 * LD + k3];
 #pragma unroll
-          for (int rr = kb; rr < RS; ++rr) a[rr][C1] = fma_(li[rr], ljk, a[rr][C1]);
-          finalize(k1, std::integral_constant<int, C1>{}, KB);
+          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][C]));
+          if (!await(k2)) {
+            stop = true;
+            break;
+          }
+          T l2[RS];
+          multipliers(k2, l2);
+          const T x2 = Ls[k2 * LD + k3];
+#pragma unroll
+          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l2[rr], x2, a[rr][C]);
+          finalize(k3, std::integral_constant<int, C>{}, KB);
         }
+        // the pair on every other column of this warp right of k1
+        const int clo = k1 >= w ? (k1 - w) / NW + 1 : 0;   // first slot with column > k1
 #pragma unroll
         for (int cc = 0; cc < CS; ++cc) {
+          if (cc < clo || cc >= ncol || ((own2 || own3) && cc == C)) continue;   // warp-uniform
           const int j = w + NW * cc;
-          if (j <= k || j >= M || (w == kk && cc == C1)) continue;   // warp-uniform
-          const T ljk = Ls[k * LD + j];
-          // floor(j / 32) = floor(NW cc / 32) as NW divides 32 and w < NW: rows above the
-          // diagonal slot are skipped at compile time
+          const T x0 = Ls[k0 * LD + j], x1 = Ls[k1 * LD + j];
 #pragma unroll
-          for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(li[rr], ljk, a[rr][cc]);
+          for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][cc]));
         }
       }
     });
   });
   __syncthreads();
-  if (threadIdx.x == 0 && s_err && !s_info) s_info = M + 1;   // a wait ran out: reported as a failure
+  if (threadIdx.x == 0 && s_err && !s_info) s_info = M + 1;
   __syncthreads();
   const int bad = s_info;
   if (info && threadIdx.x == 0) info[b] = bad;
   if (bad) return;
-  // column-major L with 1/L_kk on the diagonal (rows >= k of column k; the rest unused)
   T* Lb = Lw + (size_t)b * M * M;
   for (int e = threadIdx.x; e < M * M; e += NTH) {
     const int k = e / M, i = e - k * M;
@@ -402,8 +432,8 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     if (lane == 0) red[w] = l;
     __syncthreads();
     if (w == 0) {
-      T s = warp_sum(lane < NW ? red[lane] : Num<T>::zero());
-      if (lane == 0) logdet[b] = (double)Num<T>::st(s);   // sum of log L_kk^2
+      T s2 = warp_sum(lane < NW ? red[lane] : Num<T>::zero());
+      if (lane == 0) logdet[b] = (double)Num<T>::st(s2);
     }
   }
 }
@@ -932,7 +962,7 @@ extern "C" int gpk_level(int prec, int ngemm, const gpk_gemm_t* gemms, int nlc, 
 template <typename T, int RS, int CS, int NW>
 int spd_factor_launch(int batch, int M, const void* A, T* Lw, double* logdet, int* info, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
-  const size_t sm = 256 * sizeof(float2) + ((size_t)M * (M | 1) + M + NW) * sizeof(T);
+  const size_t sm = 256 * sizeof(float2) + ((size_t)M * (M | 1) + 32 * RS + M + NW) * sizeof(T);
   auto k = spd_factor_kernel<T, RS, CS, NW>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<batch, NW * 32, sm, st>>>(M, (const S*)A, (long)M * M, Lw, logdet, info);

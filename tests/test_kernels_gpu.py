@@ -180,7 +180,7 @@ def test_psi_full_workload_vs_reference(prec):
 
 
 @pytest.mark.parametrize('with_L', [True, False])
-@pytest.mark.parametrize('M', [1, 7, 32, 33, 64, 65, 96, 100, 128, 129, 200])
+@pytest.mark.parametrize('M', [1, 7, 32, 33, 64, 65, 96, 97, 100, 111, 112, 128, 129, 200])
 def test_chol_inv_logdet(M, with_L):
     """with_L: factor, inverse and log-determinant in one kernel; without: the kernel returns
     L^-1 and the GEMM forms L^-T L^-1."""
