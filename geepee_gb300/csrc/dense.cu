@@ -256,9 +256,9 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar) {
 // multiply-adds per register slot), so a warp waits, loads its row multipliers and walks its
 // columns once per two columns.  Look-ahead: the owner of k2 = k1 + 1 applies the pair to that
 // column and publishes it first; the owner of k3 = k2 + 1 applies the pair to k3, waits for k2,
-// applies it and publishes k3; then both take their other columns.  The pair (k2, k3) lies in
-// one segment of NW columns (NW even, pairs aligned), so its owners' register slot is a
-// compile-time index.  Row multipliers are read for every row slot without a predicate: rows at
+// applies it and publishes k3; then both take their other columns.  The look-ahead column's
+// registers are picked by a select chain (runtime slot), so the step is one copy of code: the
+// compile-time form, eight copies, overflowed the instruction cache.  Row multipliers are read for every row slot without a predicate: rows at
 // or above the pair, and rows past M, only reach register slots above the diagonal or past M,
 // which are never read (the column stores cover rows k < i < M, the pivot row k itself); the
 // shared-memory area has slack for reads past the last column.  Outputs: Lw (column-major L as
@@ -310,8 +310,13 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   // the slack rows past the last column: defined values (zeros) for the predicate-free reads
   for (int e = threadIdx.x; e < 32 * RS; e += NTH) Ls[(size_t)M * LD + e] = Num<T>::zero();
 
-  auto finalize = [&](int k, auto CK, auto RK) {
-    const T p = shfl_idx(a[RK.value][CK.value], k & 31);
+  // column k of L from the register column `col` of its owner warp (RK = k / 32, runtime: the
+  // pivot is picked by a select chain, so one copy of this code serves every column)
+  auto finalize = [&](int k, const T (&col)[RS], int RK) {
+    T pv = col[0];
+#pragma unroll
+    for (int rr = 1; rr < RS; ++rr) pv = rr == RK ? col[rr] : pv;
+    const T p = shfl_idx(pv, k & 31);
     if (!(Num<T>::approx(p) > 0.f)) {
       if (lane == 0) s_info = k + 1;
       __syncwarp();
@@ -322,7 +327,7 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
 #pragma unroll
     for (int rr = 0; rr < RS; ++rr) {
       const int i = lane + 32 * rr;
-      if (i > k && i < M) Ls[k * LD + i] = mul(a[rr][CK.value], r);
+      if (i > k && i < M) Ls[k * LD + i] = mul(col[rr], r);
     }
     if (lane == 0) {
       Ls[k * LD + k] = r;
@@ -330,6 +335,15 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     }
     __syncwarp();
     mbar_arrive(&s_bar[k]);
+  };
+  // this thread's register column of slot c (runtime c: a select chain)
+  auto column = [&](int c, T (&col)[RS]) {
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+      col[rr] = a[rr][0];
+#pragma unroll
+      for (int cc = 1; cc < CS; ++cc) col[rr] = cc == c ? a[rr][cc] : col[rr];
+    }
   };
   // -(column k) at this thread's row slots, every slot (see above)
   auto multipliers = [&](int k, T (&l)[RS]) {
@@ -346,74 +360,62 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   };
 
   // columns 0 and 1 before the first step
-  if (w == 0) finalize(0, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+  if (w == 0) {
+    T col[RS];
+    column(0, col);
+    finalize(0, col, 0);
+  }
   if (w == 1 && M > 1) {
     if (await(0)) {
-      T l0[RS];
+      T l0[RS], col[RS];
       multipliers(0, l0);
+      column(0, col);
       const T l01 = Ls[0 * LD + 1];
 #pragma unroll
-      for (int rr = 0; rr < RS; ++rr) a[rr][0] = fma_(l0[rr], l01, a[rr][0]);
-      finalize(1, std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+      for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l0[rr], l01, col[rr]);
+      finalize(1, col, 0);
     }
   }
   const int ncol = w < M ? (M - 1 - w) / NW + 1 : 0;   // this warp's columns
   const int last = w + NW * (ncol - 1);
   bool stop = ncol == 0;
-  static_for<0, RS>([&](auto KB) {
-    static_for<0, 32 / NW>([&](auto H) {
-      constexpr int kb = KB.value;
-      constexpr int C = (32 * kb + NW * H.value) / NW;   // slot of the look-ahead pair in its owners
-      const int base = 32 * kb + NW * H.value;
-      for (int kk = 0; kk < NW && !stop; kk += 2) {
-        const int k2 = base + kk, k3 = k2 + 1, k0 = k2 - 2, k1 = k2 - 1;
-        if (k2 == 0) continue;   // columns 0 and 1 were taken above
-        if (k1 >= M - 1 || last <= k1) {   // nothing of this warp right of the pair
-          stop = true;
-          break;
-        }
-        if (!await(k1)) {   // k1 published implies k0 published
-          stop = true;
-          break;
-        }
-        T l0[RS], l1[RS];
-        multipliers(k0, l0);
-        multipliers(k1, l1);
-        const bool own2 = w == kk, own3 = w == kk + 1 && k3 < M;
-        if (own2) {   // look-ahead: column k2
-          const T x0 = Ls[k0 * LD + k2], x1 = Ls[k1 * LD + k2];
+  for (int k2 = 2; !stop; k2 += 2) {
+    const int k3 = k2 + 1, k0 = k2 - 2, k1 = k2 - 1;
+    if (k1 >= M - 1 || last <= k1) break;   // nothing of this warp right of the pair
+    if (!await(k1)) break;                  // k1 published implies k0 published
+    T l0[RS], l1[RS];
+    multipliers(k0, l0);
+    multipliers(k1, l1);
+    const int C = k2 / NW, KB = k2 >> 5;   // the look-ahead pair's slot in its owners, row block
+    const bool own2 = w == k2 % NW, own3 = w == k3 % NW && k3 < M;
+    if (own2 || own3) {   // look-ahead: column k2, or column k3 (which also needs column k2)
+      const int kx = own2 ? k2 : k3;
+      T col[RS];
+      column(C, col);
+      const T x0 = Ls[k0 * LD + kx], x1 = Ls[k1 * LD + kx];
 #pragma unroll
-          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][C]));
-          finalize(k2, std::integral_constant<int, C>{}, KB);
-        }
-        if (own3) {   // look-ahead: column k3, which also needs column k2
-          const T x0 = Ls[k0 * LD + k3], x1 = Ls[k1 * LD + k3];
+      for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l1[rr], x1, fma_(l0[rr], x0, col[rr]));
+      if (own3) {
+        if (!await(k2)) break;
+        T l2[RS];
+        multipliers(k2, l2);
+        const T x2 = Ls[k2 * LD + k3];
 #pragma unroll
-          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][C]));
-          if (!await(k2)) {
-            stop = true;
-            break;
-          }
-          T l2[RS];
-          multipliers(k2, l2);
-          const T x2 = Ls[k2 * LD + k3];
-#pragma unroll
-          for (int rr = kb; rr < RS; ++rr) a[rr][C] = fma_(l2[rr], x2, a[rr][C]);
-          finalize(k3, std::integral_constant<int, C>{}, KB);
-        }
-        // the pair on every other column of this warp right of k1
-        const int clo = k1 >= w ? (k1 - w) / NW + 1 : 0;   // first slot with column > k1
-#pragma unroll
-        for (int cc = 0; cc < CS; ++cc) {
-          if (cc < clo || cc >= ncol || ((own2 || own3) && cc == C)) continue;   // warp-uniform
-          const int j = w + NW * cc;
-          const T x0 = Ls[k0 * LD + j], x1 = Ls[k1 * LD + j];
-#pragma unroll
-          for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][cc]));
-        }
+        for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l2[rr], x2, col[rr]);
       }
-    });
-  });
+      finalize(kx, col, KB);   // the register column is dead afterwards
+    }
+    // the pair on every other column of this warp right of k1
+    const int clo = k1 >= w ? (k1 - w) / NW + 1 : 0;   // first slot with column > k1
+#pragma unroll
+    for (int cc = 0; cc < CS; ++cc) {
+      if (cc < clo || cc >= ncol || ((own2 || own3) && cc == C)) continue;   // warp-uniform
+      const int j = w + NW * cc;
+      const T x0 = Ls[k0 * LD + j], x1 = Ls[k1 * LD + j];
+#pragma unroll
+      for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][cc]));
+    }
+  }
   __syncthreads();
   if (threadIdx.x == 0 && s_err && !s_info) s_info = M + 1;
   __syncthreads();
