@@ -1002,6 +1002,328 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   return fwd_variant<T, QMAX>(a, sum, contract, P, per_sm, sm, st);
 }
 
+// ---------------------------------------------------------------------------------
+// Backward, software-pipelined over points (the common configuration: Q == QC, Dout == DB,
+// B and the dB-hat accumulators in shared memory, the fixed-order partial block).  Iteration
+// i overlaps point i's front half with point i-1's back half, so a point costs three CTA
+// barriers instead of six and the short phases share them:
+//   phase 1: row sums of point i-1 (8 threads a row)    | per-point constants of point i
+//   phase 2: dZ and totals of point i-1 (warps 4..7)     | psi1 terms of point i (warps 0..3)
+//            one CTA reduction of both; warp 0 then finalises point i-1 (dmu, dS)
+//   phase 3: the pair sweep of point i (L, dB-hat)
+// L, the row sums and the per-pseudo-input tables are read in the phase after the one that
+// writes them, so one copy of each suffices; the per-dimension constants, which point i-1's
+// finalisation still reads while point i's are formed, alternate between two slots.  The
+// psi1 part of a point's dmu, dS waits in shared memory (`carry`) for its finalisation.  The
+// arithmetic of every term is psi_bwd_kernel's.
+template <typename T>
+struct PSmem {
+  float2* tab;
+  T *z, *ell2, *lnl, *inv4l, *il, *misc;
+  T* pd;      // [2][5][QMAX]
+  T* pg;      // [2*DMAX] dm_all, dv of the current point
+  T* u;       // [M]
+  T* h;       // [M*Q]
+  T* G;       // [P]
+  T* Bs;      // [Dout*P]
+  T* L;       // [P]
+  T* rows;    // [M][1+QC]
+  T* dz;      // [M*Q] psi1 part of dZ
+  T* dzr;     // [M*Q] row-sum part of dZ
+  T* accB;    // [Dout*P]
+  T* carry;   // [2*QC] psi1 part of the previous point's dmu, dS
+  T* red;     // [32*RED]
+};
+
+__host__ __device__ inline size_t pipe_smem_bytes(int M, int Q, int QC, int P, int D, size_t tsz) {
+  const size_t n = (size_t)M * Q + 4 * QMAX + 4 + 2 * 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + P + (size_t)D * P + P +
+                   (size_t)M * (1 + QC) + 2 * (size_t)M * Q + (size_t)D * P + 2 * QC + 32 * RED;
+  return 256 * 8 + n * tsz;
+}
+
+template <typename T, int QC>
+__device__ PSmem<T> pcarve(char* base, int M, int Q, int P, int D) {
+  PSmem<T> s;
+  s.tab = reinterpret_cast<float2*>(base);
+  T* t = reinterpret_cast<T*>(base + 256 * sizeof(float2));
+  s.z = t; t += M * Q;
+  s.ell2 = t; t += QMAX;
+  s.lnl = t; t += QMAX;
+  s.inv4l = t; t += QMAX;
+  s.il = t; t += QMAX;
+  s.misc = t; t += 4;
+  s.pd = t; t += 2 * 5 * QMAX;
+  s.pg = t; t += 2 * DMAX;
+  s.u = t; t += M;
+  s.h = t; t += M * Q;
+  s.G = t; t += P;
+  s.Bs = t; t += D * P;
+  s.L = t; t += P;
+  s.rows = t; t += M * (1 + QC);
+  s.dz = t; t += M * Q;
+  s.dzr = t; t += M * Q;
+  s.accB = t; t += D * P;
+  s.carry = t; t += 2 * QC;
+  s.red = t;
+  return s;
+}
+
+template <typename T, int DB, int QC>
+__global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typename Num<T>::store_t> a) {
+  constexpr int NTB = nt_bwd(QC);
+  constexpr int Q = QC, D = DB;
+  constexpr int KV = 5 * QC + 1;   // [dmu, dS psi1 parts (2QC) | Rt, St (QC), Z2R (QC), ZS (QC)]
+  typedef typename Num<T>::store_t S;
+  static_assert(NTB >= 8 * 128, "the row phase takes 8 threads for each of up to 128 rows");
+  extern __shared__ __align__(16) char smem_raw[];
+  const int M = a.M;
+  const int P = M * (M + 1) / 2;
+  PSmem<T> s = pcarve<T, QC>(smem_raw, M, Q, P, D);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // ---- per-CTA tables (as psi_bwd_kernel)
+  load_exp_table(s.tab);
+  for (int i = tid; i < M * Q; i += NTB) {
+    s.z[i] = Num<T>::ld(a.Z[i]);
+    s.dz[i] = Num<T>::zero();
+    s.dzr[i] = Num<T>::zero();
+  }
+  for (int i = tid; i < D * P; i += NTB) s.accB[i] = Num<T>::zero();
+  __syncthreads();
+  if (tid < Q) {
+    const int q = tid;
+    T lnl = Num<T>::ld(static_cast<S>(a.lls2[q]));
+    T l2 = exp_tab(lnl, s.tab);
+    s.lnl[q] = lnl;
+    s.ell2[q] = l2;
+    s.il[q] = recip(l2);
+    s.inv4l[q] = recip(mul(l2, Num<T>::c(4.f)));
+  }
+  if (tid == 32) {
+    T lsf = Num<T>::ld(static_cast<S>(a.lsf2[0]));
+    s.misc[0] = lsf;
+    s.misc[1] = exp_tab(lsf, s.tab);
+  }
+  __syncthreads();
+  for (int p = tid; p < P; p += NTB) {
+    int ia, ib;
+    pair_of(p, ia, ib);
+    T g = Num<T>::zero();
+#pragma unroll
+    for (int q = 0; q < QC; ++q) {
+      T dd = sub(s.z[ia * Q + q], s.z[ib * Q + q]);
+      g = fma_(mul(dd, dd), s.inv4l[q], g);
+    }
+    s.G[p] = neg(g);
+  }
+  stage_sym_B<T, NTB>(s.Bs, a.B, M, D, P);
+  T g_sf = Num<T>::zero();
+  T g_l[QC], g_A[DB];
+#pragma unroll
+  for (int q = 0; q < QC; ++q) g_l[q] = Num<T>::zero();
+#pragma unroll
+  for (int d = 0; d < DB; ++d) g_A[d] = Num<T>::zero();
+  const T lsf = s.misc[0];
+  __syncthreads();
+
+  const int nbeg = (int)((long)a.N * blockIdx.x / gridDim.x);
+  const int nend = (int)((long)a.N * (blockIdx.x + 1) / gridDim.x);
+  const int cnt = nend - nbeg;
+  auto slot = [&](int i) {
+    T* pd = s.pd + (i & 1) * 5 * QMAX;
+    return PointSlot<T>{pd, pd + QMAX, pd + 2 * QMAX, pd + 3 * QMAX, pd + 4 * QMAX, s.u, s.h};
+  };
+  for (int i = 0; i <= cnt; ++i) {
+    const bool cur = i < cnt, prev = i > 0;
+    const int n = nbeg + i;
+    // ---- phase 1: row sums of the previous point | constants of this point.  Whole warps
+    // enter (the 8-lane sums below shuffle with a full mask); lanes of rows past M add nothing.
+    if (prev && warp < (8 * M + 31) / 32) {
+      const int ia = tid >> 3, sl = tid & 7;
+      const bool live = ia < M;
+      T R = Num<T>::zero(), R1 = Num<T>::zero(), Sq[QC], S1[QC];
+#pragma unroll
+      for (int q = 0; q < QC; ++q) Sq[q] = S1[q] = Num<T>::zero();
+      const int rowbase = ia * (ia + 1) / 2;
+      for (int ib = sl; live && ib < M; ib += 16) {
+        const int jb = ib + 8, jc = jb < M ? jb : ib;
+        const int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
+        const int p1 = ia >= jc ? rowbase + jc : jc * (jc + 1) / 2 + ia;
+        const T l = s.L[p];
+        const T l1 = jb < M ? s.L[p1] : Num<T>::zero();
+        R = add(R, l);
+        R1 = add(R1, l1);
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          Sq[q] = fma_(l, s.z[ib * Q + q], Sq[q]);
+          S1[q] = fma_(l1, s.z[jc * Q + q], S1[q]);
+        }
+      }
+      R = add(R, R1);
+#pragma unroll
+      for (int q = 0; q < QC; ++q) Sq[q] = add(Sq[q], S1[q]);
+#pragma unroll
+      for (int m = 1; m < 8; m <<= 1) {
+        R = add(R, shfl_xor(R, m));
+#pragma unroll
+        for (int q = 0; q < QC; ++q) Sq[q] = add(Sq[q], shfl_xor(Sq[q], m));
+      }
+      if (live && sl == 0) {
+        T* row = s.rows + ia * (1 + QC);
+        row[0] = R;
+#pragma unroll
+        for (int q = 0; q < QC; ++q) row[1 + q] = Sq[q];
+      }
+    }
+    if (cur) {
+      const int t = tid - (NTB - 64);   // the last two warps (beside the row threads while 8 M <= NTB - 64)
+      if (t >= 0 && t < 4 * Q) dims_of<T, S>(a, s.ell2, s.lnl, s.tab, slot(i), n, t >> 2, t & 3);
+      const int g = tid - (NTB - 32);
+      if (g >= 0 && g < D) {
+        const T dvv = Num<T>::ld(a.dv[(size_t)n * D + g]);
+        const T mm = Num<T>::ld(a.m[(size_t)n * D + g]);
+        const T dmv = Num<T>::ld(a.dm[(size_t)n * D + g]);
+        s.pg[g] = sub(dmv, mul(scale2(dvv, 1), mm));   // dm_all
+        s.pg[DMAX + g] = dvv;
+      }
+    }
+    __syncthreads();
+    // ---- phase 2: psi1 terms of this point (warps 0..3) | dZ and totals of the previous (4..7)
+    T vals[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) vals[k] = Num<T>::zero();
+    if (cur && tid < M) {
+      const int ia0 = tid;
+      const PointSlot<T> ps = slot(i);
+      const T p1 = rows_of<T, QC>(s.z, lsf, s.tab, ps, Q, ia0);
+      T dp1 = Num<T>::zero();
+#pragma unroll
+      for (int d = 0; d < DB; ++d) {
+        dp1 = fma_(s.pg[d], Num<T>::ld(a.A[d * M + ia0]), dp1);
+        g_A[d] = fma_(s.pg[d], p1, g_A[d]);
+      }
+      const T L1 = mul(dp1, p1);
+      g_sf = add(g_sf, L1);
+#pragma unroll
+      for (int q = 0; q < QC; ++q) {
+        const T dd = sub(ps.pmu[q], s.z[ia0 * Q + q]);
+        const T ds = mul(dd, ps.pis1[q]);
+        const T ds2 = mul(ds, ds);
+        const T L1ds = mul(L1, ds);
+        vals[q] = neg(L1ds);                                            // dmu
+        vals[QC + q] = scale2(mul(L1, sub(ds2, ps.pis1[q])), -1);       // dS
+        s.dz[ia0 * Q + q] = add(s.dz[ia0 * Q + q], L1ds);               // dZ (psi1)
+        g_l[q] = add(g_l[q], mul(L1, add(sub(s.il[q], ps.pis1[q]), ds2)));
+      }
+    }
+    if (prev && tid >= 128 && tid < 128 + M) {
+      const int ia0 = tid - 128;
+      const PointSlot<T> ps = slot(i - 1);
+      const T* row = s.rows + ia0 * (1 + QC);
+      const T R = row[0];
+      vals[2 * QC] = R;
+#pragma unroll
+      for (int q = 0; q < QC; ++q) {
+        const T zq = s.z[ia0 * Q + q], il = s.il[q], cq = ps.pc[q], Sa = row[1 + q];
+        const T t = sub(add(neg(mul(zq, il)), scale2(mul(cq, ps.pmu[q]), 1)), mul(cq, zq));
+        s.dzr[ia0 * Q + q] = add(s.dzr[ia0 * Q + q], add(mul(R, t), mul(Sa, sub(il, cq))));
+        vals[2 * QC + 1 + q] = Sa;                       // St
+        vals[3 * QC + 1 + q] = mul(mul(zq, zq), R);      // Z2R
+        vals[4 * QC + 1 + q] = mul(zq, Sa);              // ZS
+      }
+    }
+    block_sum<T, KV>(vals, s.red, (128 + M + 31) >> 5);   // warps past the dZ threads hold zeros
+    if (warp == 0) {
+      if (prev) {   // finalise the previous point with its carried psi1 part
+        const int np = n - 1;
+        const PointSlot<T> ps = slot(i - 1);
+        const T Rt = vals[2 * QC];
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          if (q == lane) {
+            const T St = vals[2 * QC + 1 + q], Z2R = vals[3 * QC + 1 + q], ZS = vals[4 * QC + 1 + q];
+            const T mu = ps.pmu[q], cq = ps.pc[q], il = s.il[q];
+            const T e2 = add(sub(mul(mul(mu, mu), Rt), scale2(mul(mu, St), 1)), scale2(add(Z2R, ZS), -1));
+            const T dmu = add(s.carry[q], mul(scale2(cq, 1), sub(St, mul(mu, Rt))));
+            const T dS = add(s.carry[QC + q], add(neg(mul(cq, Rt)), scale2(mul(mul(cq, cq), e2), 1)));
+            const T t = add(add(scale2(mul(Rt, sub(il, cq)), -1), scale2(mul(sub(Z2R, ZS), mul(il, il)), -1)),
+                            mul(mul(cq, cq), e2));
+            g_l[q] = add(g_l[q], scale2(t, 1));
+            a.dmu[(size_t)np * Q + q] = Num<T>::st(dmu);
+            a.dvar[(size_t)np * Q + q] = Num<T>::st(dS);
+          }
+        }
+        if (lane == 0) g_sf = add(g_sf, scale2(Rt, 1));
+      }
+      __syncwarp();
+      if (cur && lane < 2 * QC) s.carry[lane] = vals[lane];   // this point's psi1 part, for its finalisation
+    }
+    // ---- phase 3: the pair sweep of this point (as psi_bwd_kernel's branch-free loop)
+    if (cur) {
+      T dvr[DB];
+#pragma unroll
+      for (int d = 0; d < DB; ++d) dvr[d] = s.pg[DMAX + d];
+      for (int p0 = tid; p0 < P; p0 += 2 * NTB) {
+        int pp[2], ia[2], ib[2];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          ok[u] = p0 + u * NTB < P;
+          pp[u] = ok[u] ? p0 + u * NTB : p0;
+          pair_of(pp[u], ia[u], ib[u]);
+        }
+        T arg[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const T* hh = s.h + ia[u] * QC;
+          T cr = Num<T>::zero();
+#pragma unroll
+          for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
+          arg[u] = sub(add(add(s.u[ia[u]], s.u[ib[u]]), s.G[pp[u]]), cr);
+        }
+        T ps2[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) ps2[u] = exp_tab(arg[u], s.tab);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          T w = Num<T>::zero();
+          T ab[DB];
+#pragma unroll
+          for (int d = 0; d < DB; ++d) {
+            w = fma_(dvr[d], s.Bs[d * P + pp[u]], w);
+            ab[d] = mul(dvr[d], ps2[u]);
+          }
+          const T l = mul(w, ps2[u]);
+          if (ok[u]) {
+            s.L[pp[u]] = ia[u] == ib[u] ? l : scale2(l, -1);
+#pragma unroll
+            for (int d = 0; d < DB; ++d) s.accB[d * P + pp[u]] = add(s.accB[d * P + pp[u]], ab[d]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- flush into the partial block: [dB pairs D*P | dA D*M | dZ M*Q | dsf2 | dl Q]
+  double* const part = a.part + (size_t)blockIdx.x * a.part_stride;
+  for (int i = tid; i < D * P; i += NTB) part[i] = (double)Num<T>::st(s.accB[i]);
+  if (tid < M) {
+#pragma unroll
+    for (int d = 0; d < DB; ++d) part[D * P + d * M + tid] = a.dA ? (double)Num<T>::st(g_A[d]) : 0.0;
+  }
+  for (int i = tid; i < M * Q; i += NTB) part[D * P + D * M + i] = (double)Num<T>::st(add(s.dz[i], s.dzr[i]));
+  T fin[1 + QC];
+  fin[0] = g_sf;
+#pragma unroll
+  for (int q = 0; q < QC; ++q) fin[1 + q] = g_l[q];
+  __syncthreads();
+  block_sum<T, 1 + QC>(fin, s.red);
+  if (tid == 0) {
+    part[D * P + D * M + M * Q] = (double)Num<T>::st(div(fin[0], s.misc[1]));
+#pragma unroll
+    for (int q = 0; q < QC; ++q) part[D * P + D * M + M * Q + 1 + q] = (double)Num<T>::st(mul(fin[1 + q], sqrt_(s.ell2[q])));
+  }
+}
+
 // the destinations of the backward's partial block (layout in PsiArgs::part)
 template <typename S>
 gpk::RedPlan bwd_plan(const PsiArgs<S>& a) {
@@ -1028,6 +1350,19 @@ int run_bwd(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t 
   return gpk::reduce_partials(a.part, grid, bwd_plan(a), st);
 }
 
+template <typename T, int DB>
+int run_bwd_pipe(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t st) {
+  auto k = psi_bwd_pipe_kernel<T, DB, 2>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int grid = gpk::sm_count();
+  if (grid > a.N) grid = a.N;
+  if (grid < 1) return GPK_OK;
+  k<<<grid, nt_bwd(2), sm, st>>>(a);
+  int rc = gpk::check_launch("psi_bwd_pipe");
+  if (rc != GPK_OK) return rc;
+  return gpk::reduce_partials(a.part, grid, bwd_plan(a), st);
+}
+
 template <typename T, int NPB, int QC>
 int bwd_db(const PsiArgs<typename Num<T>::store_t>& a, size_t sm, cudaStream_t st) {
   if (a.Dout == 1) return run_bwd<T, NPB, 1, QC>(a, sm, st);
@@ -1048,6 +1383,11 @@ int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   if (a.M > nt_bwd(QMAX)) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: M=%d > %d", a.M, nt_bwd(QMAX));
   if (5 * (a.Q <= 2 ? 2 : QMAX) + 1 > RED) return gpk::fail(GPK_EUNSUPPORTED, "psi_bwd: Q=%d too large", a.Q);
   const size_t cap = 227 * 1024;
+  // the pipelined kernel: Q == 2, Dout <= 2, the fixed-order path, B in shared memory
+  if (a.Q == 2 && a.Dout <= 2 && a.part && !a.b_stride && !a.dpsi1 && a.A && a.m && a.dm && a.M <= 128) {
+    const size_t sm = pipe_smem_bytes(a.M, 2, 2, P, a.Dout, sizeof(T));
+    if (sm <= cap) return a.Dout == 1 ? run_bwd_pipe<T, 1>(a, sm, st) : run_bwd_pipe<T, 2>(a, sm, st);
+  }
   const int nbs = a.b_stride == 0 ? a.Dout * P : 0, nacc = a.Dout * P;
   for (int npb = (a.Q <= 2 ? BWD_NPB : 1); npb >= 1; --npb) {
     // preference: B and the dBhat accumulators both in shared memory, then without B, then

@@ -179,6 +179,42 @@ def test_psi_full_workload_vs_reference(prec):
     assert_close(np64(dS)[pick], g['pt_dS'], gtol, 'dS')
 
 
+@pytest.mark.parametrize('M,Dout,N', [(5, 1, 7), (6, 2, 40), (33, 1, 150), (50, 2, 500), (101, 1, 300),
+                                        (127, 2, 160), (128, 1, 200)])
+def test_psi_bwd_two_dims_fixed_order(M, Dout, N):
+    """The fixed-order psi backward at Q = 2 (the software-pipelined kernel: points overlapped,
+    row sums in 8-lane groups over whole warps) for ragged M, against the oracle, and
+    bit-identical on repetition."""
+    from geepee_gb300 import gpk, workloads as W
+    Q = 2
+    wl = W.psi_workload(seed=M + 7 * Dout, N=N, Q=Q, M=M, Dout=Dout)
+    lls2, lsf2 = 2 * wl['ls'], 2 * wl['sf']
+    p1, p2 = O.psi_stats(lls2, lsf2, wl['mu'], wl['S'], wl['Z'])
+    A, B = wl['Ahat'], wl['Bhat']
+    sf2 = float(np.exp(lsf2[0]))
+    m_ref = p1 @ A.T
+    dm, dv = wl['dm'], wl['dv']
+    dm_all = dm - 2 * dv * m_ref
+    r = O.psi_derivatives(dm_all @ A, p1, np.einsum('nd,dab->nab', dv, B), p2, np.exp(wl['ls']), sf2,
+                          wl['mu'], wl['S'], wl['Z'])
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device='cuda')
+    work = z(gpk.work_elems(gpk.OP_PSI_BWD, N, M, Q, Dout))
+    outs = []
+    for _ in range(2):
+        out = dict(dsf2=z(1), dl=z(Q), dZ=z(M, Q), dA=z(Dout, M), dB=z(Dout, M, M), dmu=z(N, Q), dS=z(N, Q))
+        gpk.psi_bwd(dev(wl['mu']), dev(wl['S']), dev(wl['Z']), dev(lls2), dev(lsf2), dev(A), dev(B), dev(m_ref),
+                    dev(dm), dev(dv), out['dsf2'], out['dl'], out['dZ'], out['dA'], out['dB'], out['dmu'], out['dS'],
+                    work=work)
+        outs.append(out)
+    out = outs[0]
+    for name, val in zip(('dsf2', 'dl', 'dZ', 'dmu', 'dS'), r):
+        assert_close(out[name].cpu().numpy(), val, 1e-9, name)
+    assert_close(out['dA'].cpu().numpy(), dm_all.T @ p1, 1e-9, 'dA')
+    assert_close(out['dB'].cpu().numpy(), np.einsum('nd,nab->dab', dv, p2), 1e-9, 'dB')
+    for name in out:
+        assert torch.equal(out[name], outs[1][name]), name + ' differs between calls'
+
+
 @pytest.mark.parametrize('with_L', [True, False])
 @pytest.mark.parametrize('M', [1, 7, 32, 33, 64, 65, 96, 97, 100, 111, 112, 128, 129, 200])
 def test_chol_inv_logdet(M, with_L):
@@ -418,8 +454,15 @@ def test_gemm_group_matches_single_products():
         c3 = g.mm(a, b, tA=True)
         c4 = g.mm(S, K, beta=-1.0, E=E)
         c5 = g.mm(S.reshape(300, 100), S.reshape(300, 100), tA=True, alpha=2.0, beta=1.0, E=E)
+        u3, w3 = dev(rng.randn(3, 100)), dev(rng.randn(3, 100))
+        c6 = g.mm(S, K, alpha=-2.0, beta=1.0, E=S, u=u3, v=w3, gamma=-0.5)   # rank-one addend, batched
+        u1, w1 = dev(rng.randn(100)), dev(rng.randn(100))
+        c7 = g.mm(K, K, u=u1, v=w1)                                           # unbatched
     Kn, Sn, vn, En = (t.cpu().numpy() for t in (K, S, v, E))
     an, bn = a.cpu().numpy(), b.cpu().numpy()
+    un3, wn3, un1, wn1 = (t.cpu().numpy() for t in (u3, w3, u1, w1))
+    assert_close(c6.cpu().numpy(), -2.0 * Sn @ Kn + Sn - 0.5 * np.einsum('bi,bj->bij', un3, wn3), 1e-12)
+    assert_close(c7.cpu().numpy(), Kn @ Kn + np.outer(un1, wn1), 1e-12)
     assert_close(c1.cpu().numpy(), Kn @ Sn, 1e-12)
     assert_close(c2.cpu().numpy(), 0.5 * Sn @ vn, 1e-12)
     assert_close(c3.cpu().numpy(), an.T @ bn, 1e-12)
