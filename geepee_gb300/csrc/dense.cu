@@ -36,7 +36,9 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
                                           const typename Num<T>::store_t* A, int lda, long sA,
                                           const typename Num<T>::store_t* B, int ldb, long sB, double beta,
                                           const typename Num<T>::store_t* E, int lde, long sE,
-                                          typename Num<T>::store_t* C, int ldc, long sC) {
+                                          typename Num<T>::store_t* C, int ldc, long sC, double gamma = 0.0,
+                                          const typename Num<T>::store_t* U = nullptr, long sU = 0,
+                                          const typename Num<T>::store_t* V = nullptr, long sV = 0) {
   typedef typename Num<T>::store_t S;
   constexpr int R = GemmShape<TBM>::R, TPD = GemmShape<TBM>::TPD, NG = GemmShape<TBM>::NG;
   constexpr int NT = NG * KS, NPT = KC * TBM / NT;
@@ -125,7 +127,11 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
   }
   // epilogue in the storage type (float64 for df64): the product is rounded once to it, and
   // alpha / beta E enter with that type's arithmetic, as separate BLAS-style operations would
-  const S al = static_cast<S>(alpha), be = static_cast<S>(beta);
+  const S al = static_cast<S>(alpha), be = static_cast<S>(beta), ga = static_cast<S>(gamma);
+  if (U) {
+    U += bz * sU;
+    V += bz * sV;
+  }
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -135,6 +141,7 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
         S v = Num<T>::st(acc[r][c]);
         if (alpha != 1.0) v = al * v;
         if (beta != 0.0) v = v + be * E[(size_t)gi * lde + gj];
+        if (U) v = v + ga * U[gi] * V[gj];   // the rank-one addend
         C[(size_t)gi * ldc + gj] = v;
       }
     }
@@ -198,7 +205,7 @@ __global__ void __launch_bounds__(GemmShape<TBM>::NG * KS, TBM == 8 ? 6 : 1) gem
   }
   gemm_tile<T, TBM, KS, false>(bx, by, bz, pr.m, pr.n, pr.k, pr.transA, pr.transB, pr.alpha, (const S*)Ap, pr.lda,
                                sA, (const S*)Bp, pr.ldb, sB, pr.beta, (const S*)pr.E, pr.lde, pr.strideE, (S*)pr.C,
-                               pr.ldc, pr.strideC);
+                               pr.ldc, pr.strideC, pr.gamma, (const S*)pr.u, pr.strideU, (const S*)pr.v, pr.strideV);
 }
 
 // ---- the SPD inverse fast path: factor (one CTA) -> L^-1 (many CTAs) -> L^-T L^-1 (GEMM) ----
@@ -935,6 +942,7 @@ static int gemm_group_check(int count, const gpk_gemm_t* problems) {
                 "gemm_group[%d]: bad leading dimension", p);
     GPK_REQUIRE(!q.sel || ((q.A2 || q.B2) && q.selbit >= 0 && q.selbit < 31),
                 "gemm_group[%d]: a selector needs A2 or B2 and a bit in [0,30]", p);
+    GPK_REQUIRE(!q.u == !q.v, "gemm_group[%d]: a rank-one addend needs both u and v", p);
   }
   return GPK_OK;
 }

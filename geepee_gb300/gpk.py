@@ -208,7 +208,9 @@ class _GemmT(ctypes.Structure):
                 ('B', ctypes.c_void_p), ('ldb', ctypes.c_int), ('strideB', ctypes.c_long), ('E', ctypes.c_void_p),
                 ('lde', ctypes.c_int), ('strideE', ctypes.c_long), ('C', ctypes.c_void_p), ('ldc', ctypes.c_int),
                 ('strideC', ctypes.c_long), ('sel', ctypes.c_void_p), ('selbit', ctypes.c_int), ('A2', ctypes.c_void_p),
-                ('strideA2', ctypes.c_long), ('B2', ctypes.c_void_p), ('strideB2', ctypes.c_long)]
+                ('strideA2', ctypes.c_long), ('B2', ctypes.c_void_p), ('strideB2', ctypes.c_long),
+                ('gamma', ctypes.c_double), ('u', ctypes.c_void_p), ('strideU', ctypes.c_long), ('v', ctypes.c_void_p),
+                ('strideV', ctypes.c_long)]
 
 
 _GROUP = 16   # GPK_GEMM_GROUP
@@ -237,9 +239,10 @@ class GemmGroup:
         return self
 
     def mm(self, A, B, C=None, alpha=1.0, beta=0.0, tA=False, tB=False, E=None, sel=None, selbit=0, A2=None,
-           B2=None):
+           B2=None, u=None, v=None, gamma=1.0):
         """With sel (an int32 device tensor [batch]): batch entry b reads A2 / B2 (same shapes per
-        entry) in place of A / B when bit `selbit` of sel[b] is set."""
+        entry) in place of A / B when bit `selbit` of sel[b] is set.  With u [batch, m] (or [m])
+        and v [batch, n] (or [n]): C += gamma u v^T per batch entry."""
         A, B = A.contiguous(), B.contiguous()
         a3 = A if A.dim() == 3 else A.unsqueeze(0)
         b3 = B if B.dim() == 3 else B.unsqueeze(0)
@@ -276,6 +279,12 @@ class GemmGroup:
                 setattr(g, 'stride' + name + '2', 0 if x3.shape[0] == 1 else x3.shape[1] * x3.shape[2])
                 self.keep.append(x3)
             self.keep.append(sel)
+        if u is not None:
+            u2, v2 = u.contiguous().reshape(-1, m), v.contiguous().reshape(-1, n)
+            g.gamma = float(gamma)
+            g.u, g.strideU = ptr(u2), 0 if u2.shape[0] == 1 else m
+            g.v, g.strideV = ptr(v2), 0 if v2.shape[0] == 1 else n
+            self.keep += [u2, v2]
         self.items.append((prec_of(A.dtype), g))
         self.keep += [A, B, C, Ee]
         return C

@@ -85,6 +85,7 @@ class DevLayer:
         self.side = None
         self._dAh, self._dBh = views[2].view(Dout, M), views[3].view(Dout, M, M)
         self._works = {}
+        self._consts_ready = False   # prep_det_bwd_consts issued for the current evaluation
 
     def work(self, op):
         """The layer's float64 workspace for the fixed-order (bit-reproducible) sums of
@@ -651,6 +652,29 @@ class DevLayer:
         self.g['eta2'].copy_(e2)
         return dmx, dvx
 
+    def prep_det_bwd_consts(self, alpha):
+        """The parts of the natural-parameter det layer's backward algebra that need only the
+        setup (a model may issue this beside the forward; _bwd_det_nat forms them itself
+        otherwise): E_sym = -s_post/2 (Su + Su^T) - beta s_cav/2 (Suhat + Suhat^T) - s_post mu
+        mu^T - beta s_cav muhat muhat^T, E_mall = sum_d [s_post/2 (Bpost + A A^T) + s_cav/2 (Bd +
+        Ahat Ahat^T)] and beta s_cav muhat + s_post mu (the constant part of d theta_2)."""
+        M, D = self.M, self.Dout
+        s_post, s_cav = self.N / alpha - 1.0, -self.N / alpha
+        beta = self.beta
+        c1, c2 = -0.5 * beta * s_cav, -0.5 * s_post
+        row = lambda v: v.view(D, 1, M)
+        with gpk.GemmGroup() as g:
+            self._E_sym = g.lincomb(torch.empty_like(self.Sh), [(c1, self.Sh), (c1, self.Sh, True), (c2, self.Su),
+                                                                (c2, self.Su, True)],
+                                    [(-beta * s_cav, self.mh, self.mh), (-s_post, self.mu, self.mu)])
+            self._E_mall = g.lincomb(torch.empty((M, M), dtype=F64, device=self.dev),
+                                     [(0.5 * s_post, self.Bpost), (0.5 * s_cav, self.Bh_det)],
+                                     [(0.5 * s_post, self.Apost, self.Apost), (0.5 * s_cav, self.Ah, self.Ah)],
+                                     sum_batch=True, batch=D)
+            self._c_eta2 = g.lincomb(torch.empty((D, 1, M), dtype=F64, device=self.dev),
+                                     [(beta * s_cav, row(self.mh)), (s_post, row(self.mu))])
+        self._consts_ready = True
+
     def _bwd_det_nat(self, alpha, dm, dv, kfu, Bk, x, dx=None):
         """backprop_grads_reg for natural parameters, with compute_cav_grad_u and
         compute_posterior_grad_u (aep_models.py:548-586, base_models.py:490-516) inlined so
@@ -688,30 +712,37 @@ class DevLayer:
         # sandwiches by Suhat / Su and K^-1 collapse): with w0 = G^T dAhat, w = w0 + s_cav muhat,
         #   dSinv_cav = -(G^T dBhat G + s_cav/2 Suhat - s_cav/2 muhat muhat^T + w muhat^T),
         #   dSinv_post = -s_post/2 (Su + mu mu^T),
-        #   dtheta_2 = beta w + s_post mu,  dtheta_1 = beta dSinv_cav + dSinv_post
-        kg = self._kuu_grad_levels(dAh, dBh, False, alpha)
-        next(kg)
+        #   dtheta_2 = beta w + s_post mu,  dtheta_1 = beta dSinv_cav + dSinv_post.
+        # dBhat is symmetric here, so with H2 = 2 dBhat G + dAhat muhat^T the symmetrised
+        # dtheta_1 is -beta G^T H2 - beta muhat w0^T + E_sym, and the Kuu gradient (see
+        # _kuu_grad_levels) is sum_d Bd (dBhat Bd + dAhat Ahat^T) + E_mall: two levels, the
+        # rank-one terms in the products' epilogues, E_sym, E_mall and the constant part of
+        # dtheta_2 formed ahead (prep_det_bwd_consts).
+        if not self._consts_ready:
+            self.prep_det_bwd_consts(alpha)
+        self._consts_ready = False
+        Bd, row = self.Bh_det, (lambda v: v.view(D, 1, M))
         with gpk.GemmGroup() as g:
-            H = g.mm(dBh, self.G)
+            H2 = g.mm(dBh, self.G, alpha=2.0, u=dAh, v=self.mh)
             w0 = g.mm(self.G, dAh.unsqueeze(-1), tA=True).view(D, M)
-            w = g.mm(self.G, dAh.unsqueeze(-1), tA=True, beta=s_cav, E=self._mh3).view(D, M)
-            kg.send(g)
+            Y = g.mm(dBh, Bd, u=dAh, v=self.Ah)
         with gpk.GemmGroup() as g:
-            GtH = g.mm(self.G, H, tA=True)
-            kg.send(g)
-        row = lambda v: v.view(D, 1, M)
-        with gpk.GemmGroup() as g:
-            kg.send(g)
-            c1, c2 = -0.5 * beta * s_cav, -0.5 * s_post
-            sym = g.lincomb(torch.empty_like(GtH), [(-beta, GtH), (-beta, GtH, True), (c1, self.Sh), (c1, self.Sh, True),
-                                                    (c2, self.Su), (c2, self.Su, True)],
-                            [(-beta, w0, self.mh), (-beta, self.mh, w), (-s_post, self.mu, self.mu)])
-            g.lincomb(row(self.g['eta2']), [(beta, row(w)), (s_post, row(self.mu))])
+            sym = g.mm(self.G, H2, tA=True, alpha=-beta, beta=1.0, E=self._E_sym, u=self.mh, v=w0, gamma=-beta)
+            self.Mall = g.mm(Bd.reshape(D * M, M), Y.reshape(D * M, M), tA=True, beta=1.0, E=self._E_mall)
+            g.lincomb(row(self.g['eta2']), [(beta, row(w0)), (1.0, self._c_eta2)])
         if self.side is not None:
+            # the trace gradient adds into what the chain rule on the side stream wrote: it
+            # follows it there, beside dR = R sym and its packing on the main stream
+            self.side.wait_stream(main)
+            with torch.cuda.stream(self.side):
+                self._finish_hyp(self.Mall)
+            dR = mm(self.R, sym)
+            gpk.triu_pack(dR, self.R, self.g['eta1_R'])
             main.wait_stream(self.side)
-        self._finish_hyp(self.Mall)
-        dR = mm(self.R, sym)
-        gpk.triu_pack(dR, self.R, self.g['eta1_R'])
+        else:
+            self._finish_hyp(self.Mall)
+            dR = mm(self.R, sym)
+            gpk.triu_pack(dR, self.R, self.g['eta1_R'])
 
 
 def gauss_logZ(m, v, y, sn, alpha):

@@ -164,7 +164,10 @@ int gpk_gemm_ex(int prec, int batch, int m, int n, int k, int transA, int transB
  * choice made on the device: when sel != NULL and bit `selbit` of sel[b] is set, batch entry b
  * reads A2 (stride strideA2) in place of A when A2 != NULL, and B2 (stride strideB2) in place
  * of B when B2 != NULL (same shapes and leading dimensions).  E.g. the layer algebra's
- * T Suhat or Kuu^-1 Suhat, whichever the regime word of output b selects (gpk_regime). */
+ * T Suhat or Kuu^-1 Suhat, whichever the regime word of output b selects (gpk_regime).  With
+ * u != NULL the epilogue also adds gamma u[b] v[b]^T (u: m elements at u + b strideU, v: n at
+ * v + b strideV, storage type): the rank-one terms of the layer algebra, e.g. the
+ * dAhat muhat^T beside dBhat G, without a separate linear combination. */
 typedef struct {
   int batch, m, n, k, transA, transB;
   double alpha, beta;
@@ -186,6 +189,11 @@ typedef struct {
   long strideA2;
   const void* B2;
   long strideB2;
+  double gamma;
+  const void* u;
+  long strideU;
+  const void* v;
+  long strideV;
 } gpk_gemm_t;
 #define GPK_GEMM_GROUP 16
 
