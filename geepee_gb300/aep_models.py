@@ -59,6 +59,17 @@ class _Graph:
         return self.out
 
 
+class _SplitGraph:
+    """An evaluation captured as two graphs replayed in order (front, then back)."""
+
+    def __init__(self, front, back):
+        self.front, self.back = front, back
+
+    def replay(self):
+        self.front.replay()
+        return self.back.replay()
+
+
 # ------------------------------------------------------------------------------------------
 # base behaviour (geepee/base_models.py:15-165)
 # ------------------------------------------------------------------------------------------
@@ -291,6 +302,11 @@ class _PackedModel(Base_Model):
             self._idx_host.numpy()[:] = idx
             self._idx_buf.copy_(self._idx_host, non_blocking=True)
             self._run(key, lambda: self.device_objective(self._idx_buf, alpha))
+        return self._host_result()
+
+    def _host_result(self):
+        """The evaluation's energy and gradients to the host (one D2H copy), as the reference
+        returns them."""
         out = self.gpack.download(self._shapes)
         energy, info = out.pop('__energy__'), out.pop('__info__')
         if info > 0:
@@ -428,37 +444,60 @@ class SDGPR(_PackedModel):
 
     def device_objective(self, idx, alpha):
         """Device-resident energy+gradient (aep_models.py:895-988); see SGPR.device_objective."""
-        N, L = self.N, self.L
         xb, yb = (self.x_dev, self.y_dev) if idx is None else gpk.gather_rows(idx, self.x_dev, self.y_dev)
-        nb = yb.shape[0]
-        scale = -N / nb / alpha
-        side = self._side_streams()
-        # the first layer's kernel rows K(x_batch, Z) need only its hyperparameters: they are
-        # formed beside the factorisations, and its forward then runs only the contractions
-        # (allocated here, on the main stream, which is the last to use it)
-        lay0, k0 = self.layers[0], {}
-        kfu0 = torch.empty((nb, lay0.M), dtype=torch.float64, device=self.dev)
+        st, kfu0 = self._dev_front(alpha, xb=xb)
+        return self._dev_back(xb, yb, alpha, st, kfu0)
 
-        def kfu_ahead():
-            k0['kfu'] = lay0.kfu_rows(xb, out=kfu0)
-            k0['done'] = torch.cuda.Event()
-            k0['done'].record()
-        ahead = {lay0: kfu_ahead} if gpk.det_contract_supported(torch.float64, lay0.M, lay0.Dout) else None
+    def _dev_front(self, alpha, xb=None, join=False):
+        """The part of an evaluation that does not depend on the minibatch: the layers' setup
+        (factorisations, posterior and cavity moments) and, beside the forward, the accumulator
+        fills, the layers' log-partitions and the first layer's backward constants.  With `xb`
+        the first layer's kernel rows K(xb, Z) are formed beside the factorisations (they need
+        only its hyperparameters); with `join` the side streams are joined at the end (the part
+        is then a graph of its own).  Returns (Cholesky statuses, kernel rows or None)."""
+        N = self.N
+        side = self._side_streams()
+        lay0, k0 = self.layers[0], {}
+        ahead = None
+        if xb is not None and gpk.det_contract_supported(torch.float64, lay0.M, lay0.Dout):
+            # (allocated here, on the main stream, which is the last to use it)
+            kfu0 = torch.empty((xb.shape[0], lay0.M), dtype=torch.float64, device=self.dev)
+
+            def kfu_ahead():
+                k0['kfu'] = lay0.kfu_rows(xb, out=kfu0)
+                k0['done'] = torch.cuda.Event()
+                k0['done'].record()
+            ahead = {lay0: kfu_ahead}
         st = setup_layers(self.layers, alpha, streams=side, ahead=ahead)
-        # the backward's accumulators are zeroed on a side stream while the forward runs
         main = torch.cuda.current_stream()
         if 'done' in k0:
             main.wait_event(k0['done'])
         side[0].wait_stream(main)
         with torch.cuda.stream(side[0]):
+            # the backward's accumulators are zeroed on a side stream while the forward runs
             for lay in self.layers:
                 lay.zero_accumulators()
             # the layers' log-partitions need only the setup: summed here, beside the forward
             self._phi_sum.zero_()
             for lay in self.layers:
                 lay.phi(alpha, out=self._phi_sum, w=1.0 / N)
+            # the first layer's backward constants (its algebra then takes two levels)
+            lay0.prep_det_bwd_consts(alpha)
+        if join:
+            main.wait_stream(side[0])
+        return st, k0.get('kfu')
+
+    def _dev_back(self, xb, yb, alpha, st, kfu0=None, joined=False):
+        """The minibatch part of an evaluation (after _dev_front): the forward through the
+        layers, the likelihood, the backward and the energy's terms.  `joined`: the front part
+        joined its side streams itself (it is a graph of its own)."""
+        N, L = self.N, self.L
+        nb = yb.shape[0]
+        scale = -N / nb / alpha
+        side = self._side_streams()
+        main = torch.cuda.current_stream()
         ms, vs = [], []
-        m, v, kfu, Bk = self.layers[0].fwd_det(xb, kfu=k0.get('kfu'))
+        m, v, kfu, Bk = self.layers[0].fwd_det(xb, kfu=kfu0)
         ms.append(m)
         vs.append(v)
         for i in range(1, L):
@@ -477,7 +516,8 @@ class SDGPR(_PackedModel):
             self._log_Z(ms[-1], vs[-1], yb, alpha, scale, 1.0 / N, dmi, dvi, self.energy)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
-        main.wait_stream(side[0])   # the zeroed accumulators
+        if not joined:
+            main.wait_stream(side[0])   # the zeroed accumulators
         for lay in self.layers:
             lay.prezeroed = True
         self.layers[0].side = side[0]
@@ -502,12 +542,50 @@ class SDGPR(_PackedModel):
         self._energy_terms(self.layers, alpha, N, st, phi_sum=self._phi_sum)
         return self.energy
 
+    def _split_graph(self, mb, alpha):
+        """The two captured graphs of a minibatch evaluation: the part independent of the
+        minibatch (_dev_front) and the rest (_dev_back), which reads the minibatch indices from a
+        fixed buffer.  Replaying both equals one evaluation."""
+        key = ('mb', mb, alpha, False)
+        if not hasattr(self, '_idx_bufs'):
+            self._idx_bufs = {}
+        if mb not in self._idx_bufs:   # one buffer pair per size, alive as long as its graphs
+            self._idx_bufs[mb] = (torch.zeros(mb, dtype=torch.int64, device=self.dev),
+                                  torch.zeros(mb, dtype=torch.int64, pin_memory=True))
+        self._idx_buf, self._idx_host = self._idx_bufs[mb]
+        g = self._graphs.get(key)
+        if isinstance(g, _SplitGraph):
+            return g
+        idx_buf = self._idx_buf
+
+        def front():
+            self._front_st, _ = self._dev_front(alpha, join=True)
+            return self._front_st
+
+        def back():
+            xb, yb = gpk.gather_rows(idx_buf, self.x_dev, self.y_dev)
+            return self._dev_back(xb, yb, alpha, self._front_st, joined=True)
+        g = self._graphs[key] = _SplitGraph(_Graph(front), _Graph(back))
+        return g
+
     def objective_function(self, params, mb_size, alpha=1.0, prop_mode=PROP_MM):
-        """aep_models.py:895-988."""
+        """aep_models.py:895-988.  A minibatch evaluation with graphs runs as two captured graphs:
+        the part that does not depend on the minibatch (the layers' setup) is launched first, and
+        the host draws the minibatch (the reference's np.random.choice(N, mb_size, replace=False),
+        the same call on the same RNG state: the parameters' upload does not touch it) while the
+        device works on that part."""
         N = self.N
-        idx = None if mb_size >= N else np.random.choice(N, mb_size, replace=False)
+        if mb_size >= N or not self.use_graphs or getattr(self, '_mc', False):
+            idx = None if mb_size >= N else np.random.choice(N, mb_size, replace=False)
+            self.update_hypers(params)
+            return self._objective_host(idx, alpha)
         self.update_hypers(params)
-        return self._objective_host(idx, alpha)
+        g = self._split_graph(mb_size, alpha)
+        g.front.replay()
+        self._idx_host.numpy()[:] = np.random.choice(N, mb_size, replace=False)
+        self._idx_buf.copy_(self._idx_host, non_blocking=True)
+        g.back.replay()
+        return self._host_result()
 
     def _prepare_predict(self):
         if not self.updated:
