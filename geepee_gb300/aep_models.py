@@ -448,14 +448,13 @@ class SDGPR(_PackedModel):
         st, kfu0 = self._dev_front(alpha, xb=xb)
         return self._dev_back(xb, yb, alpha, st, kfu0)
 
-    def _dev_front(self, alpha, xb=None, join=False):
+    def _dev_front(self, alpha, xb=None, side_work=True):
         """The part of an evaluation that does not depend on the minibatch: the layers' setup
-        (factorisations, posterior and cavity moments) and, beside the forward, the accumulator
-        fills, the layers' log-partitions and the first layer's backward constants.  With `xb`
-        the first layer's kernel rows K(xb, Z) are formed beside the factorisations (they need
-        only its hyperparameters); with `join` the side streams are joined at the end (the part
-        is then a graph of its own).  Returns (Cholesky statuses, kernel rows or None)."""
-        N = self.N
+        (factorisations, posterior and cavity moments) and, with `side_work`, the work issued
+        beside the forward (_side_work).  With `xb` the first layer's kernel rows K(xb, Z) are
+        formed beside the factorisations (they need only its hyperparameters).  Without
+        `side_work` the part joins every branch it forks (it is then a graph of its own).
+        Returns (Cholesky statuses, kernel rows or None)."""
         side = self._side_streams()
         lay0, k0 = self.layers[0], {}
         ahead = None
@@ -472,26 +471,32 @@ class SDGPR(_PackedModel):
         main = torch.cuda.current_stream()
         if 'done' in k0:
             main.wait_event(k0['done'])
-        side[0].wait_stream(main)
-        with torch.cuda.stream(side[0]):
-            # the backward's accumulators are zeroed on a side stream while the forward runs
-            for lay in self.layers:
-                lay.zero_accumulators()
-            # the layers' log-partitions need only the setup: summed here, beside the forward
-            self._phi_sum.zero_()
-            for lay in self.layers:
-                lay.phi(alpha, out=self._phi_sum, w=1.0 / N)
-            # the first layer's backward constants (its algebra then takes two levels)
-            lay0.prep_det_bwd_consts(alpha)
-        if join:
-            main.wait_stream(side[0])
+        if side_work:
+            self._side_work(alpha)
         return st, k0.get('kfu')
 
-    def _dev_back(self, xb, yb, alpha, st, kfu0=None, joined=False):
+    def _side_work(self, alpha):
+        """Issued on a side stream once the setup is done, beside the forward: the backward's
+        accumulator fills, the layers' log-partitions and the first layer's backward constants
+        (joined before the backward)."""
+        side, main = self._side_streams(), torch.cuda.current_stream()
+        side[0].wait_stream(main)
+        with torch.cuda.stream(side[0]):
+            for lay in self.layers:
+                lay.zero_accumulators()
+            self._phi_sum.zero_()
+            for lay in self.layers:
+                lay.phi(alpha, out=self._phi_sum, w=1.0 / self.N)
+            # the first layer's backward constants (its algebra then takes two levels)
+            self.layers[0].prep_det_bwd_consts(alpha)
+
+    def _dev_back(self, xb, yb, alpha, st, kfu0=None, side_work=False):
         """The minibatch part of an evaluation (after _dev_front): the forward through the
-        layers, the likelihood, the backward and the energy's terms.  `joined`: the front part
-        joined its side streams itself (it is a graph of its own)."""
+        layers, the likelihood, the backward and the energy's terms; with `side_work`, the work
+        beside the forward is issued here (when the front part is a graph of its own)."""
         N, L = self.N, self.L
+        if side_work:
+            self._side_work(alpha)
         nb = yb.shape[0]
         scale = -N / nb / alpha
         side = self._side_streams()
@@ -516,8 +521,7 @@ class SDGPR(_PackedModel):
             self._log_Z(ms[-1], vs[-1], yb, alpha, scale, 1.0 / N, dmi, dvi, self.energy)
         # the M x M algebra of layer i only needs layer i's own state: it runs on a side stream
         # while the backward continues into layer i-1 (a parallel branch of the captured graph)
-        if not joined:
-            main.wait_stream(side[0])   # the zeroed accumulators
+        main.wait_stream(side[0])   # the zeroed accumulators
         for lay in self.layers:
             lay.prezeroed = True
         self.layers[0].side = side[0]
@@ -559,12 +563,12 @@ class SDGPR(_PackedModel):
         idx_buf = self._idx_buf
 
         def front():
-            self._front_st, _ = self._dev_front(alpha, join=True)
+            self._front_st, _ = self._dev_front(alpha, side_work=False)
             return self._front_st
 
         def back():
             xb, yb = gpk.gather_rows(idx_buf, self.x_dev, self.y_dev)
-            return self._dev_back(xb, yb, alpha, self._front_st, joined=True)
+            return self._dev_back(xb, yb, alpha, self._front_st, side_work=True)
         g = self._graphs[key] = _SplitGraph(_Graph(front), _Graph(back))
         return g
 

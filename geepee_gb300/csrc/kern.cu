@@ -25,29 +25,57 @@ __device__ void load_hyp(Hyp<T>& h, const double* lls2, const double* lsf2, int 
   }
 }
 
-// K[n,m] = exp(lsf - 1/2 sum_d (x-z)^2 / l_d) (+ jitter on the diagonal)
+// K[n,m] = exp(lsf - 1/2 sum_d (x-z)^2 / l_d) (+ jitter on the diagonal).  A CTA takes KR rows
+// and KC columns: those rows of x and columns' Z arrive in shared memory by asynchronous copies
+// and are converted once (not once per element), then 256 threads sweep the KR x KC block.
+constexpr int KR = 8, KC = 128;
 template <typename T>
 __global__ void __launch_bounds__(256) kern_matrix_kernel(int N, int M, int D, const typename Num<T>::store_t* x,
                                                           int ldx, const typename Num<T>::store_t* z, int ldz,
                                                           const double* lls2, const double* lsf2, double jitter,
                                                           typename Num<T>::store_t* K, int ldk) {
-  __shared__ float2 tab[256];
-  __shared__ Hyp<T> h;
+  typedef typename Num<T>::store_t S;
+  extern __shared__ __align__(16) char smem_raw[];
+  float2* tab = reinterpret_cast<float2*>(smem_raw);
+  Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
+  T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [KR][D]
+  T* zs = xs + KR * D;                                                                  // [KC][D]
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.x * KC, n0 = blockIdx.y * KR;
+  const int nr = min(KR, N - n0), nc = min(KC, M - m0);
+  for (int e = tid; e < nr * D; e += 256) {
+    const int r = e / D, d = e - r * D;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<S*>(xs) + e);
+    const S* src = x + (size_t)(n0 + r) * ldx + d;
+    if (sizeof(S) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src));
+  }
+  for (int e = tid; e < nc * D; e += 256) {
+    const int c = e / D, d = e - c * D;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<S*>(zs) + e);
+    const S* src = z + (size_t)(m0 + c) * ldz + d;
+    if (sizeof(S) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src));
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   load_exp_table(tab);
   __syncthreads();
-  load_hyp(h, lls2, lsf2, D, tab);
+  convert_in_place(xs, (long)nr * D, tid, 256);
+  convert_in_place(zs, (long)nc * D, tid, 256);
+  load_hyp(*h, lls2, lsf2, D, tab);
   __syncthreads();
-  int m = blockIdx.x * 32 + threadIdx.x;
-  int n = blockIdx.y * 8 + threadIdx.y;
-  if (m >= M || n >= N) return;
-  T r = Num<T>::zero();
-  for (int d = 0; d < D; ++d) {
-    T df = sub(Num<T>::ld(x[(size_t)n * ldx + d]), Num<T>::ld(z[(size_t)m * ldz + d]));
-    r = fma_(mul(df, df), h.inv_l2[d], r);
+  for (int e = tid; e < nr * nc; e += 256) {
+    const int r = e / nc, c = e - r * nc;
+    const int n = n0 + r, m = m0 + c;
+    T rr = Num<T>::zero();
+    for (int d = 0; d < D; ++d) {
+      const T df = sub(xs[r * D + d], zs[c * D + d]);
+      rr = fma_(mul(df, df), h->inv_l2[d], rr);
+    }
+    T k = exp_tab(sub(h->lsf, scale2(rr, -1)), tab);
+    if (jitter != 0.0 && n == m) k = add(k, Num<T>::ld(static_cast<S>(jitter)));
+    K[(size_t)n * ldk + m] = Num<T>::st(k);
   }
-  T k = exp_tab(sub(h.lsf, scale2(r, -1)), tab);
-  if (jitter != 0.0 && n == m) k = add(k, Num<T>::ld(static_cast<typename Num<T>::store_t>(jitter)));
-  K[(size_t)n * ldk + m] = Num<T>::st(k);
 }
 
 // Deterministic-input layer forward for rows n:
@@ -695,9 +723,12 @@ template <typename T>
 int kern_launch(int N, int M, int D, const void* x, int ldx, const void* z, int ldz, const double* lls2,
                 const double* lsf2, double jitter, void* K, int ldk, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
-  dim3 grid(gpk::ceil_div(M, 32), gpk::ceil_div(N, 8));
-  kern_matrix_kernel<T><<<grid, dim3(32, 8), 0, st>>>(N, M, D, (const S*)x, ldx, (const S*)z, ldz, lls2, lsf2,
-                                                    jitter, (S*)K, ldk);
+  const dim3 grid(gpk::ceil_div(M, KC), gpk::ceil_div(N, KR));
+  GPK_REQUIRE(grid.y <= 65535, "kern: N=%d too large (at most %d rows)", N, 65535 * KR);
+  const size_t sm = 256 * sizeof(float2) + sizeof(Hyp<T>) + (size_t)(KR + KC) * D * sizeof(T);
+  auto k = kern_matrix_kernel<T>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, 256, sm, st>>>(N, M, D, (const S*)x, ldx, (const S*)z, ldz, lls2, lsf2, jitter, (S*)K, ldk);
   return gpk::check_launch("kern");
 }
 
