@@ -184,10 +184,11 @@ def psi_bwd_bytes(N, M, Q, D):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one psi backward launch pair (kernel and
 # reduction) of the deep GP's layer 2 in one ncu capture of the same case (1000 points, M=100,
-# Q=2): 281,088 bytes for the kernel (its inputs) and 6,605,568 for the reduction, which ncu
-# replays after flushing the caches, so that the 152 per-CTA partial blocks it reads come from
-# DRAM (in the evaluation they are still in L2)
-PSI_BWD_TRAFFIC = 281088 + 6605568
+# Q=2): 299,520 + 43,264 bytes for the pipelined kernel (its inputs; its outputs and partial
+# blocks stay in L2) and 6,605,568 for the reduction, which ncu replays after flushing the
+# caches, so that the 152 per-CTA partial blocks it reads come from DRAM (in the evaluation
+# they are still in L2)
+PSI_BWD_TRAFFIC = 299520 + 43264 + 6605568
 
 
 def time_launches(fn, flush, reps=30):
@@ -411,7 +412,7 @@ def run_ours(args, world, rank, local):
     except RuntimeError as exc:      # e.g. torch's linalg library not loadable under a profiler
         print('fp64 form skipped: %s' % exc, file=sys.stderr)
 
-    # ---- dominant kernel roofline: psi backward of layer 1 on this step's inputs
+    # ---- dominant kernel roofline: psi backward of the second layer on this step's inputs
     lay1 = mdl.layers[1]
     lay0 = mdl.layers[0]
     xb = xd.index_select(0, idx_all[W])
@@ -433,7 +434,7 @@ def run_ours(args, world, rank, local):
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = fp32_peak_tflops(n_sm, sm_mhz)
     achieved = F / t_k / 1e12
-    roofline = {'kernel': 'psi_bwd_kernel<df64> + its fixed-order reduction (layer 2, 1000 points, M=100, Q=2)',
+    roofline = {'kernel': 'psi_bwd_pipe_kernel<df64> + its fixed-order reduction (layer 2, 1000 points, M=100, Q=2)',
                 'bound': 'fp32-pipe', 'achieved': round(achieved, 4), 'peak': round(fp32_peak, 1),
                 'unit': 'TFLOP/s', 'frac': round(achieved / fp32_peak, 5),
                 'work': 'algorithmic: (8MQ + 20PQ + 4 Dout M^2) per point, P = M(M+1)/2, x 1000 points '

@@ -84,6 +84,13 @@ def case(name):
         kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
         m, v = z(1000, 2), z(1000, 2)
         return lambda: gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, m, v)
+    if name == 'kern_dgp':
+        # the first deep-GP layer's kernel rows K(x_batch, Z): 1000 rows, M=100, D=8
+        rng = np.random.RandomState(0)
+        x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))
+        l2, s2 = _d(np.zeros(8)), _d(np.zeros(1))
+        out = z(1000, 100)
+        return lambda: gpk.kern(x, Z, l2, s2, out=out)
     if name == 'det_contract_dgp':
         # the first deep-GP layer's forward once its kernel rows exist: 1000 rows, M=100, Dout=2
         rng = np.random.RandomState(0)
