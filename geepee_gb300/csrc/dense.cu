@@ -229,8 +229,7 @@ __device__ __forceinline__ void static_for(F&& f) {
   }
 }
 
-// mbarriers in shared memory (CTA scope): init with an arrival count; arrive (release);
-// wait for phase 0 to complete (acquire), bounded: false after ~2^31 SM cycles
+// mbarriers in shared memory (CTA scope): init with an arrival count; arrive (release)
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
@@ -239,10 +238,13 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a) : "memory");
 }
+// bounded wait for phase 0 of an mbarrier (acquire): false after ~2^31 SM cycles (about one
+// second).  try_wait may suspend the thread until the phase completes, so waiting warps spend
+// no issue slots (polling with test_wait measured slower, also for the critical-path warps).
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
   const long long t0 = clock64();
-  while (clock64() - t0 < (1LL << 31)) {   // about one second at the SM clock
+  do {
     unsigned done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -250,36 +252,53 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar) {
         : "r"(a)
         : "memory");
     if (done) return true;
-  }
+  } while (clock64() - t0 < (1LL << 31));
   return false;
 }
 
+// Two consecutive elements of the pair-interleaved L (one 16-byte load for df64, 8 for FP32)
+__device__ __forceinline__ void ld_pair(const df64* p, df64& a, df64& b) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = make_df(v.x, v.y);
+  b = make_df(v.z, v.w);
+}
+__device__ __forceinline__ void ld_pair(const float* p, float& a, float& b) {
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  a = v.x;
+  b = v.y;
+}
+
 // Right-looking Cholesky of one M x M SPD matrix per CTA (M <= min(32*RS, NW*CS)).  Element
-// (i, j) of the lower triangle lives in a register of lane i % 32 of warp j % NW (slot
-// [i/32][j/NW]), so a trailing update touches no shared memory except the columns of L it
+// (i, j) of the lower triangle lives in a register of warp j % NW (column slot j / NW), lane
+// (i - j) % 32, row slot (i - j) / 32: each column starts at lane 0 of row slot 0, so a column
+// of n rows fills ceil(n / 32) row slots and a trailing update walks only those (a layout
+// anchored at row 0 would walk the rows above the diagonal in the same 32-row block and, in
+// the last block, the rows past M: 2.3x the element updates of the triangle for M = 100,
+// against 1.5x here).  A trailing update touches no shared memory except the columns of L it
 // reads.  Column k of L is published by its owner warp through an mbarrier of its own (32
 // arrivals); a warp waits only for the columns it applies, so there is no CTA barrier in the
 // loop.  Step (k0, k1) = (2s, 2s+1) applies both columns to every column right of k1 (two
-// multiply-adds per register slot), so a warp waits, loads its row multipliers and walks its
-// columns once per two columns.  Look-ahead: the owner of k2 = k1 + 1 applies the pair to that
-// column and publishes it first; the owner of k3 = k2 + 1 applies the pair to k3, waits for k2,
-// applies it and publishes k3; then both take their other columns.  The look-ahead column's
-// registers are picked by a select chain (runtime slot), so the step is one copy of code: the
-// compile-time form, eight copies, overflowed the instruction cache.  Row multipliers are read for every row slot without a predicate: rows at
-// or above the pair, and rows past M, only reach register slots above the diagonal or past M,
-// which are never read (the column stores cover rows k < i < M, the pivot row k itself); the
-// shared-memory area has slack for reads past the last column.  Outputs: Lw (column-major L as
-// raw (hi, lo) pairs, 1/L_kk on the diagonal - the input of trinv_kernel), logdet = sum log
-// L_kk^2, info[b] = k+1 for a non-positive pivot (M+1 if a bounded wait ran out, never expected).
+// multiply-adds per register slot), so a warp waits, reads its multipliers and walks its
+// columns once per two columns.  L is kept in shared memory with the columns of a pair
+// interleaved (Lp[s][i][2], s = k / 2), so the two multipliers of a row, and the two
+// coefficients of a column, are one load.  Look-ahead: the owner of k2 = k1 + 1 applies the
+// pair to that column and publishes it first; the owner of k3 = k2 + 1 applies the pair to
+// k3, waits for k2, applies it and publishes k3; then both take their other columns.  The
+// look-ahead column's registers are picked by a select chain (runtime slot), so the step is
+// one copy of code.  Rows past M in a column's last row slot read the zeroed slack rows of Lp
+// and are never stored.  Outputs: Lw (column-major L as raw (hi, lo) pairs, 1/L_kk on the
+// diagonal - the input of trinv_kernel), logdet = sum log L_kk^2, info[b] = k+1 for a
+// non-positive pivot (M+1 if a bounded wait ran out, never expected).
 template <typename T, int RS, int CS, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typename Num<T>::store_t* A, long sA,
                                                                  T* Lw, double* logdet, int* info) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
   float2* tab = reinterpret_cast<float2*>(smem_raw);
-  const int LD = M | 1;
-  T* Ls = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [M][LD] + 32 RS slack
-  T* dg = Ls + (size_t)M * LD + 32 * RS;                             // [M] L_kk^2
+  const int LDP = M + 32;   // rows of a pair (32 slack rows past M)
+  const int NP = (M + 1) >> 1;
+  T* Lp = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2));   // [NP][LDP][2]
+  T* dg = Lp + (size_t)NP * LDP * 2;                                 // [M] L_kk^2
   T* red = dg + M;                                                   // [NW]
   __shared__ int s_info, s_err;
   __shared__ __align__(8) unsigned long long s_bar[32 * RS];   // column k published (32 arrivals)
@@ -288,7 +307,7 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   static_assert(32 % NW == 0 && NW >= 2 && NW % 2 == 0, "NW must be even and divide 32");
   A += b * sA;
   {
-    S* raw = reinterpret_cast<S*>(Ls);
+    S* raw = reinterpret_cast<S*>(Lp);   // the staging area (M*M <= NP*LDP*2 elements)
     for (int e = threadIdx.x; e < M * M; e += NTH) {
       const unsigned dst = (unsigned)__cvta_generic_to_shared(raw + e);
       if (sizeof(S) == 8)
@@ -304,26 +323,24 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   __syncthreads();
   T a[RS][CS];
   {
-    const S* raw = reinterpret_cast<const S*>(Ls);
+    const S* raw = reinterpret_cast<const S*>(Lp);
 #pragma unroll
-    for (int rr = 0; rr < RS; ++rr)
+    for (int cc = 0; cc < CS; ++cc)
 #pragma unroll
-      for (int cc = 0; cc < CS; ++cc) {
-        const int i = lane + 32 * rr, j = w + NW * cc;
-        a[rr][cc] = (i < M && j <= i) ? Num<T>::ld(raw[i * M + j]) : Num<T>::zero();
+      for (int rr = 0; rr < RS; ++rr) {
+        const int j = w + NW * cc, i = j + lane + 32 * rr;
+        a[rr][cc] = (i < M) ? Num<T>::ld(raw[i * M + j]) : Num<T>::zero();
       }
   }
-  __syncthreads();   // the staging area becomes L
-  // the slack rows past the last column: defined values (zeros) for the predicate-free reads
-  for (int e = threadIdx.x; e < 32 * RS; e += NTH) Ls[(size_t)M * LD + e] = Num<T>::zero();
+  __syncthreads();   // the staging area becomes Lp
+  // the slack rows past M of every pair: zeros, read by the rows past M of a last row slot
+  for (int e = threadIdx.x; e < NP * 64; e += NTH) Lp[((size_t)(e >> 6) * LDP + M) * 2 + (e & 63)] = Num<T>::zero();
+  __syncthreads();
+  auto at = [&](int k, int i) -> T* { return Lp + ((size_t)(k >> 1) * LDP + i) * 2 + (k & 1); };
 
-  // column k of L from the register column `col` of its owner warp (RK = k / 32, runtime: the
-  // pivot is picked by a select chain, so one copy of this code serves every column)
-  auto finalize = [&](int k, const T (&col)[RS], int RK) {
-    T pv = col[0];
-#pragma unroll
-    for (int rr = 1; rr < RS; ++rr) pv = rr == RK ? col[rr] : pv;
-    const T p = shfl_idx(pv, k & 31);
+  // column k of L from the register column `col` of its owner warp (row k in lane 0, slot 0)
+  auto finalize = [&](int k, const T (&col)[RS]) {
+    const T p = shfl_idx(col[0], 0);
     if (!(Num<T>::approx(p) > 0.f)) {
       if (lane == 0) s_info = k + 1;
       __syncwarp();
@@ -333,11 +350,11 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     const T r = rsqrt_(p);   // 1 / L_kk
 #pragma unroll
     for (int rr = 0; rr < RS; ++rr) {
-      const int i = lane + 32 * rr;
-      if (i > k && i < M) Ls[k * LD + i] = mul(col[rr], r);
+      const int i = k + lane + 32 * rr;
+      if (i > k && i < M) *at(k, i) = mul(col[rr], r);
     }
     if (lane == 0) {
-      Ls[k * LD + k] = r;
+      *at(k, k) = r;
       dg[k] = p;
     }
     __syncwarp();
@@ -352,11 +369,6 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
       for (int cc = 1; cc < CS; ++cc) col[rr] = cc == c ? a[rr][cc] : col[rr];
     }
   };
-  // -(column k) at this thread's row slots, every slot (see above)
-  auto multipliers = [&](int k, T (&l)[RS]) {
-#pragma unroll
-    for (int rr = 0; rr < RS; ++rr) l[rr] = neg(Ls[k * LD + lane + 32 * rr]);
-  };
   // bounded wait for column k; false: stop (a wait ran out, or a pivot failed)
   auto await = [&](int k) {
     if (!mbar_wait(&s_bar[k])) {
@@ -365,22 +377,35 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     }
     return s_info == 0;
   };
+  // the pair (k0, k0 + 1) applied to the rows of column j held in v (row slots below nr)
+  auto apply_pair = [&](int k0, int j, int nr, T* v) {
+    T x0, x1;
+    ld_pair(at(k0, j), x0, x1);
+#pragma unroll
+    for (int rr = 0; rr < RS; ++rr) {
+      if (rr > 0 && rr >= nr) break;   // warp-uniform
+      T l0, l1;
+      ld_pair(at(k0, j + lane + 32 * rr), l0, l1);
+      v[rr] = fma_(neg(l1), x1, fma_(neg(l0), x0, v[rr]));
+    }
+  };
 
   // columns 0 and 1 before the first step
   if (w == 0) {
     T col[RS];
     column(0, col);
-    finalize(0, col, 0);
+    finalize(0, col);
   }
   if (w == 1 && M > 1) {
     if (await(0)) {
-      T l0[RS], col[RS];
-      multipliers(0, l0);
+      T col[RS];
       column(0, col);
-      const T l01 = Ls[0 * LD + 1];
+      const T x = *at(0, 1);
+      const int nr = (M - 1 + 31) >> 5;
 #pragma unroll
-      for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l0[rr], l01, col[rr]);
-      finalize(1, col, 0);
+      for (int rr = 0; rr < RS; ++rr)
+        if (rr < nr) col[rr] = fma_(neg(*at(0, 1 + lane + 32 * rr)), x, col[rr]);
+      finalize(1, col);
     }
   }
   const int ncol = w < M ? (M - 1 - w) / NW + 1 : 0;   // this warp's columns
@@ -390,27 +415,24 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     const int k3 = k2 + 1, k0 = k2 - 2, k1 = k2 - 1;
     if (k1 >= M - 1 || last <= k1) break;   // nothing of this warp right of the pair
     if (!await(k1)) break;                  // k1 published implies k0 published
-    T l0[RS], l1[RS];
-    multipliers(k0, l0);
-    multipliers(k1, l1);
-    const int C = k2 / NW, KB = k2 >> 5;   // the look-ahead pair's slot in its owners, row block
+    const int C = k2 / NW;                  // the look-ahead pair's slot in its owners
     const bool own2 = w == k2 % NW, own3 = w == k3 % NW && k3 < M;
     if (own2 || own3) {   // look-ahead: column k2, or column k3 (which also needs column k2)
       const int kx = own2 ? k2 : k3;
+      const int nr = (M - kx + 31) >> 5;
       T col[RS];
       column(C, col);
-      const T x0 = Ls[k0 * LD + kx], x1 = Ls[k1 * LD + kx];
-#pragma unroll
-      for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l1[rr], x1, fma_(l0[rr], x0, col[rr]));
+      apply_pair(k0, kx, nr, col);
       if (own3) {
         if (!await(k2)) break;
-        T l2[RS];
-        multipliers(k2, l2);
-        const T x2 = Ls[k2 * LD + k3];
+        const T x2 = *at(k2, k3);
 #pragma unroll
-        for (int rr = 0; rr < RS; ++rr) col[rr] = fma_(l2[rr], x2, col[rr]);
+        for (int rr = 0; rr < RS; ++rr) {
+          if (rr > 0 && rr >= nr) break;
+          col[rr] = fma_(neg(*at(k2, k3 + lane + 32 * rr)), x2, col[rr]);
+        }
       }
-      finalize(kx, col, KB);   // the register column is dead afterwards
+      finalize(kx, col);   // the register column is dead afterwards
     }
     // the pair on every other column of this warp right of k1
     const int clo = k1 >= w ? (k1 - w) / NW + 1 : 0;   // first slot with column > k1
@@ -418,9 +440,17 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
     for (int cc = 0; cc < CS; ++cc) {
       if (cc < clo || cc >= ncol || ((own2 || own3) && cc == C)) continue;   // warp-uniform
       const int j = w + NW * cc;
-      const T x0 = Ls[k0 * LD + j], x1 = Ls[k1 * LD + j];
+      const int nr = (M - j + 31) >> 5;
+      T x0, x1;
+      ld_pair(at(k0, j), x0, x1);
+      // row slots past (32*RS - NW*cc) / 32 hold no row of any column of this slot
 #pragma unroll
-      for (int rr = (NW * cc) >> 5; rr < RS; ++rr) a[rr][cc] = fma_(l1[rr], x1, fma_(l0[rr], x0, a[rr][cc]));
+      for (int rr = 0; rr < RS - ((NW * cc) >> 5); ++rr) {
+        if (rr > 0 && rr >= nr) break;   // warp-uniform
+        T l0, l1;
+        ld_pair(at(k0, j + lane + 32 * rr), l0, l1);
+        a[rr][cc] = fma_(neg(l1), x1, fma_(neg(l0), x0, a[rr][cc]));
+      }
     }
   }
   __syncthreads();
@@ -432,7 +462,7 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   T* Lb = Lw + (size_t)b * M * M;
   for (int e = threadIdx.x; e < M * M; e += NTH) {
     const int k = e / M, i = e - k * M;
-    if (i >= k) Lb[e] = Ls[k * LD + i];
+    if (i >= k) Lb[e] = *at(k, i);
   }
   if (logdet) {
     T l = Num<T>::zero();
@@ -972,7 +1002,7 @@ extern "C" int gpk_level(int prec, int ngemm, const gpk_gemm_t* gemms, int nlc, 
 template <typename T, int RS, int CS, int NW>
 int spd_factor_launch(int batch, int M, const void* A, T* Lw, double* logdet, int* info, cudaStream_t st) {
   typedef typename Num<T>::store_t S;
-  const size_t sm = 256 * sizeof(float2) + ((size_t)M * (M | 1) + 32 * RS + M + NW) * sizeof(T);
+  const size_t sm = 256 * sizeof(float2) + ((size_t)((M + 1) >> 1) * (M + 32) * 2 + M + NW) * sizeof(T);
   auto k = spd_factor_kernel<T, RS, CS, NW>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<batch, NW * 32, sm, st>>>(M, (const S*)A, (long)M * M, Lw, logdet, info);

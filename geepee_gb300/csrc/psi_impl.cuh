@@ -128,6 +128,35 @@ __device__ __forceinline__ void block_sum(T* vals, T* red, int nact = 0) {
   }
 }
 
+// block_sum for a point's handful of values: each warp reduces them in multi-value butterflies
+// of eight (warp_sum_many; lane 4v then holds value c0 + v), lane i of warp 0 adds value i over
+// the warps in order and shuffles it to the warp.  Fixed order; K <= 32.
+template <typename T, int K>
+__device__ __forceinline__ void block_sum_many(T (&vals)[K], T* red, int nact) {
+  static_assert(K <= 32 && K <= RED, "K values per lane of warp 0");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < nact) {
+#pragma unroll
+    for (int c0 = 0; c0 < K; c0 += 8) {
+      T t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t[u] = c0 + u < K ? vals[c0 + u] : Num<T>::zero();
+      warp_sum_many<8>(t);
+      if ((lane & 3) == 0 && c0 + (lane >> 2) < K) red[warp * RED + c0 + (lane >> 2)] = t[0];
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    T s = Num<T>::zero();
+    if (lane < K) {
+      s = red[lane];
+      for (int w = 1; w < nact; ++w) s = add(s, red[w * RED + lane]);
+    }
+#pragma unroll
+    for (int i = 0; i < K; ++i) vals[i] = shfl_idx(s, i);
+  }
+}
+
 // Per-point tables of one data point n: per-dimension constants (pmu, pis1 = 1/(l+S),
 // pc = 1/(l+2S), pld1/pld2 = 1/2 log(l/(l+S)), 1/2 log(l/(l+2S))) and per-pseudo-input terms
 // (u_a, h_aq).  The backward keeps one point's tables, the forward NPB points' side by side.
@@ -1231,7 +1260,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         vals[4 * QC + 1 + q] = mul(zq, Sa);              // ZS
       }
     }
-    block_sum<T, KV>(vals, s.red, (128 + M + 31) >> 5);   // warps past the dZ threads hold zeros
+    block_sum_many<T, KV>(vals, s.red, (128 + M + 31) >> 5);   // warps past the dZ threads hold zeros
     if (warp == 0) {
       if (prev) {   // finalise the previous point with its carried psi1 part
         const int np = n - 1;
