@@ -14,6 +14,7 @@ Cases run one kernel of the deep-GP objective on its real input shapes:
   det_fwd_dgp   deterministic layer forward, 1000 rows, D=8, M=100, Dout=2, df64
   det_bwd_dgp   its backward (kfu derivatives, dAhat), df64
   gram_dgp      dBhat = sum_n dv_n kfu_n kfu_n^T for the same rows, df64
+                (det_bwd_dgp_n<rows>, gram_dgp_n<rows>: another row count)
   trace_m100    gradient of tr(M Kzz), M=100, Q=2, df64
   objective_dgp one full objective+gradient evaluation (eager, every kernel)
 With --time, prints the mean device time per launch (CUDA events).
@@ -100,20 +101,23 @@ def case(name):
         kfu = gpk.kern(x, Z, l2, s2)
         Bk, m, v = z(1000, 2, 100), z(1000, 2), z(1000, 2)
         return lambda: gpk.det_contract(kfu, s2, A, B, Bk, m, v)
-    if name in ('det_bwd_dgp', 'gram_dgp'):
+    if name.split('_n')[0] in ('det_bwd_dgp', 'gram_dgp'):
+        # 1000 rows, or the count after '_n' (e.g. det_bwd_dgp_n100)
+        n = int(name.split('_n')[1]) if '_n' in name else 1000
+        name = name.split('_n')[0]
         rng = np.random.RandomState(0)
-        x, Z = _d(rng.randn(1000, 8)), _d(rng.randn(100, 8))
+        x, Z = _d(rng.randn(n, 8)), _d(rng.randn(100, 8))
         A, B = _d(rng.randn(2, 100)), _d(rng.randn(2, 100, 100))
         l2, s2 = _d(np.zeros(8)), _d(np.zeros(1))
-        kfu, Bk = torch.empty((1000, 100), dtype=torch.float64, device='cuda'), z(1000, 2, 100)
-        gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, z(1000, 2), z(1000, 2))
-        dm, dv = _d(rng.randn(1000, 2)), _d(rng.randn(1000, 2))
+        kfu, Bk = torch.empty((n, 100), dtype=torch.float64, device='cuda'), z(n, 2, 100)
+        gpk.det_fwd(x, Z, l2, s2, A, B, kfu, Bk, z(n, 2), z(n, 2))
+        dm, dv = _d(rng.randn(n, 2)), _d(rng.randn(n, 2))
         if name == 'gram_dgp':
             C = z(2, 100, 100)
-            work = z(gpk.work_elems(gpk.OP_GRAM, 1000, 100, 8, 2))
+            work = z(gpk.work_elems(gpk.OP_GRAM, n, 100, 8, 2))
             return lambda: gpk.gram(kfu, kfu, dv, C, work=work)
         bufs = (z(1), z(8), z(100, 8), z(2, 100))
-        work = z(gpk.work_elems(gpk.OP_DET_BWD, 1000, 100, 8, 2))
+        work = z(gpk.work_elems(gpk.OP_DET_BWD, n, 100, 8, 2))
         return lambda: gpk.det_bwd(x, Z, l2, s2, A, kfu, Bk, dm, dv, *bufs, work=work)
     if name == 'trace_m100':
         rng = np.random.RandomState(0)

@@ -832,7 +832,9 @@ __global__ void __launch_bounds__(128) small_spd_kernel(int B, int n, const type
 // Tile edge for a set of products with t8 8-wide / t16 16-wide tiles: 8 (256-thread CTAs,
 // about four resident per SM) while the tiles fill at most two such waves, then 16 (one
 // 1024-thread CTA per SM) up to two waves, then 32.  Small products are latency-bound: more,
-// smaller CTAs start together and finish sooner.
+// smaller CTAs start together and finish sooner (16-wide tiles of 2 x 2 outputs a thread, which
+// convert each operand element half as often, measured slower: 9.6 against 6.2 us for one
+// M = 100 product, and no faster for a group of six).
 inline int gemm_tile_edge(long t8, long t16) {
   const long sms = gpk::sm_count();
   if (t8 <= 8 * sms) return 8;

@@ -323,15 +323,20 @@ size_t det_contract_smem(int M, int Dout, size_t tsz) {
   return 256 * sizeof(float2) + ((size_t)Dout * M * M + (size_t)CR * M + 2 * CR * DO_MAX * 2) * tsz;
 }
 
+// elements of one det_bwd row buffer: RG rows of kfu (or dkfu) and Bk, x, dm, dv
+__host__ __device__ inline int det_bwd_rowbuf(int RG, int M, int D, int Dk) { return RG * (M * (1 + Dk) + D + 2 * Dk); }
+
 // Deterministic-input layer backward, per row (geepee/aep_models.py:451-460 with
 // kfucompDer, kernels.py:381-399):
 //   dkfu_nb = sum_d dm_nd A_db + 2 sum_d dv_nd Bk_ndb,   L_nb = dkfu_nb kfu_nb
 //   dsf2 += sum L / sf2;  dl_q += sum L (x-z)^2 / l^{3/2};  dZ_bq += sum_n L (x_nq - z_bq)/l_q
 //   dA_db += sum_n dm_nd kfu_nb;   dx_nq = -sum_b L_nb (x_nq - z_bq)/l_q   (optional)
 // Threads are (b, row group): threadIdx.x is the pseudo-input b, threadIdx.y one of RG row
-// groups; a CTA takes a contiguous range of rows, RG at a time.  Per-b sums (dZ, dA) are
-// reduced over the row groups in shared memory and flushed with one atomic per CTA; dsf2 and
-// dl by one CTA reduction.
+// groups; a CTA takes a contiguous range of rows, RG at a time, whose kfu, Bk, x, dm, dv rows
+// are copied into shared memory (double-buffered: the next RG rows' copies are in flight while
+// these compute) and converted once; Z and A likewise at the start.  Per-b sums (dZ, dA) are
+// reduced over the row groups in shared memory and flushed with one write (or atomic) per CTA;
+// dsf2 and dl by one CTA reduction.
 // DB outputs (Dout <= DB, every one of the first DB live unless DB = DO_MAX) and EX (D == DC)
 // are compile-time, so that the per-row loops carry no branch between independent sums.
 template <typename T, int DC, int DB, bool EX>
@@ -352,65 +357,131 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
   float2* tab = reinterpret_cast<float2*>(smem_raw);
   Hyp<T>* h = reinterpret_cast<Hyp<T>*>(smem_raw + 256 * sizeof(float2));
   const int RG = blockDim.y, XW = blockDim.x >> 5;
-  T* xs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [RG][DC]
-  T* gv = xs + RG * DC;                      // [RG][2*DO_MAX]  dm_d, dv_d of the group's row
-  T* red = gv + RG * 2 * DO_MAX;             // [RG][XW][DC] (dx) / [RG][blockDim.x][DC+DO_MAX]
+  const int Dk = dkfu ? 0 : Dout;   // outputs whose A, Bk, dm, dv are read
+  const int BS = det_bwd_rowbuf(RG, M, D, Dk);
+  T* zs = reinterpret_cast<T*>(smem_raw + 256 * sizeof(float2) + sizeof(Hyp<T>));   // [M][D]
+  T* as = zs + (size_t)M * D;                // [Dk][M]
+  T* buf = as + (size_t)Dk * M;              // [2][BS]: RG rows of kfu (or dkfu), Bk, x, dm, dv
+  T* red = buf + 2 * (size_t)BS;             // [RG][XW][DC] (dx) / [RG][blockDim.x][DC+DO_MAX]
   const int b = threadIdx.x, rg = threadIdx.y, lane = threadIdx.x & 31, xw = threadIdx.x >> 5;
   const int tid = rg * blockDim.x + b, nth = blockDim.x * blockDim.y;
+  const int nbeg = (int)((long)N * blockIdx.x / gridDim.x), nend = (int)((long)N * (blockIdx.x + 1) / gridDim.x);
+  // The rows of a pass arrive by asynchronous copies into one of two buffers while the other
+  // pass computes; each thread converts the elements it copied (one conversion site for all
+  // of them), and a barrier publishes them.  Buffer layout (nr <= RG rows from n0):
+  //   [0, RG M) kfu or dkfu rows | [RG M, RG M (1+Dk)) Bk rows | RG D x rows | RG Dk dm | RG Dk dv
+  auto rowbuf = [&](int i, int n0, int nr, bool convert) {
+    T* B0 = buf + (size_t)(i & 1) * BS;
+    S* R0 = reinterpret_cast<S*>(B0);
+    const long nk = (long)nr * M, nb = (long)nr * Dk * M, nx = (long)nr * D, ng = (long)nr * Dk;
+    const long ob = (long)RG * M, ox = ob + (long)RG * Dk * M, om = ox + (long)RG * D, ov = om + (long)RG * Dk;
+    for (long e = tid; e < nk + nb + nx + 2 * ng; e += nth) {
+      long o;
+      const S* src;
+      if (e < nk) {
+        o = e;
+        src = (dkfu ? dkfu : kfu) + (size_t)n0 * M + e;
+      } else if (e < nk + nb) {
+        o = ob + (e - nk);
+        src = Bk + (size_t)n0 * Dk * M + (e - nk);
+      } else if (e < nk + nb + nx) {
+        const long t = e - nk - nb, r = t / D;
+        o = ox + t;
+        src = x + (size_t)(n0 + r) * ldx + (t - r * D);
+      } else if (e < nk + nb + nx + ng) {
+        o = om + (e - nk - nb - nx);
+        src = dm + (size_t)n0 * Dk + (e - nk - nb - nx);
+      } else {
+        o = ov + (e - nk - nb - nx - ng);
+        src = dv + (size_t)n0 * Dk + (e - nk - nb - nx - ng);
+      }
+      if (convert) {
+        B0[o] = Num<T>::ld(R0[o]);
+      } else {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(R0 + o);
+        if (sizeof(S) == 8)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+        else
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+      }
+    }
+  };
+  // Z and A the same way (with the first pass's rows)
+  auto zabuf = [&](bool convert) {
+    S* zr = reinterpret_cast<S*>(zs);
+    for (long e = tid; e < (long)M * D + (long)Dk * M; e += nth) {
+      const S* src = e < (long)M * D ? z + e : A + (e - (long)M * D);
+      if (convert) {
+        zs[e] = Num<T>::ld(zr[e]);
+      } else {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(zr + e);
+        if (sizeof(S) == 8)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+        else
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+      }
+    }
+  };
+  zabuf(false);
+  if (nbeg < nend) rowbuf(0, nbeg, min(RG, nend - nbeg), false);
   load_exp_table(tab);
   __syncthreads();
   load_hyp(*h, lls2, lsf2, D, tab);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  zabuf(true);
+  if (nbeg < nend) rowbuf(0, nbeg, min(RG, nend - nbeg), true);
+  __syncthreads();
   T zb[DC], gz[DC], gl[DC];
 #pragma unroll
   for (int q = 0; q < DC; ++q) {
-    zb[q] = (b < M && q < D) ? Num<T>::ld(z[(size_t)b * D + q]) : Num<T>::zero();
+    zb[q] = (b < M && q < D) ? zs[b * D + q] : Num<T>::zero();
     gz[q] = gl[q] = Num<T>::zero();
   }
   T ab[DO_MAX], ga[DO_MAX];
 #pragma unroll
   for (int d = 0; d < DO_MAX; ++d) {
-    ab[d] = (!dkfu && b < M && d < Dout) ? Num<T>::ld(A[(size_t)d * M + b]) : Num<T>::zero();
+    ab[d] = (b < M && d < Dk) ? as[d * M + b] : Num<T>::zero();
     ga[d] = Num<T>::zero();
   }
   T gsf = Num<T>::zero();
   auto q_on = [&](int q) { return EX || q < D; };
   auto d_on = [&](int d) { return d < DB && (DB < DO_MAX || d < Dout); };
-  const int nbeg = (int)((long)N * blockIdx.x / gridDim.x), nend = (int)((long)N * (blockIdx.x + 1) / gridDim.x);
-  __syncthreads();
-  for (int n0 = nbeg; n0 < nend; n0 += RG) {
+  for (int n0 = nbeg, it = 0; n0 < nend; n0 += RG, ++it) {
     const int n = n0 + rg;
     const bool row = n < nend;
-    if (row) {
-      if (b < D) xs[rg * DC + b] = Num<T>::ld(x[(size_t)n * ldx + b]);
-      if (!dkfu && b >= D && b < D + 2 * Dout) {   // D + 2 Dout <= 16 + 8 <= blockDim.x
-        const int t = b - D, d = t >> 1;
-        gv[rg * 2 * DO_MAX + t] = Num<T>::ld((t & 1) ? dv[(size_t)n * Dout + d] : dm[(size_t)n * Dout + d]);
-      }
-    }
-    __syncthreads();
+    const int nr = min(RG, nend - n0);
+    const bool more = n0 + RG < nend;
+    if (more) rowbuf(it + 1, n0 + RG, min(RG, nend - n0 - RG), false);   // the next pass's rows
+    const T* B0 = buf + (size_t)(it & 1) * BS;
+    const T* kr = B0 + (size_t)rg * M;
+    const T* bkr = B0 + (size_t)RG * M + (size_t)rg * Dk * M;
+    const T* xs = B0 + (size_t)RG * M * (1 + Dk) + (size_t)rg * D;
+    const T* dmr = B0 + (size_t)RG * (M * (1 + Dk) + D) + (size_t)rg * Dk;
+    const T* dvr = dmr + (size_t)RG * Dk;
     T L = Num<T>::zero();
     if (row && b < M) {
-      const T k = Num<T>::ld(kfu[(size_t)n * M + b]);
+      const T k = kr[b];
       T g = Num<T>::zero();
       if (dkfu) {
-        g = Num<T>::ld(dkfu[(size_t)n * M + b]);
+        g = k;   // the staged row holds dkfu here
       } else {
 #pragma unroll
         for (int d = 0; d < DB; ++d) {
           if (d_on(d)) {
-            const T dmd = gv[rg * 2 * DO_MAX + 2 * d], dvd = gv[rg * 2 * DO_MAX + 2 * d + 1];
+            const T dmd = dmr[d], dvd = dvr[d];
             g = fma_(dmd, ab[d], g);
-            g = fma_(scale2(dvd, 1), Num<T>::ld(Bk[((size_t)n * Dout + d) * M + b]), g);
+            g = fma_(scale2(dvd, 1), bkr[(size_t)d * M + b], g);
             ga[d] = fma_(dmd, k, ga[d]);
           }
         }
       }
-      L = mul(g, k);
+      const T kk = dkfu ? Num<T>::ld(kfu[(size_t)n * M + b]) : k;
+      L = mul(g, kk);
       gsf = add(gsf, L);
 #pragma unroll
       for (int q = 0; q < DC; ++q) {
         if (q_on(q)) {
-          const T df = sub(xs[rg * DC + q], zb[q]);
+          const T df = sub(xs[q], zb[q]);
           const T t = mul(L, df);
           gz[q] = fma_(t, h->inv_l2[q], gz[q]);
           gl[q] = fma_(t, df, gl[q]);
@@ -426,7 +497,7 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int q = c0 + u;
-          t[u] = (q_on(q) && row && b < M) ? mul(L, mul(sub(xs[rg * DC + q], zb[q]), h->inv_l2[q])) : Num<T>::zero();
+          t[u] = (q_on(q) && row && b < M) ? mul(L, mul(sub(xs[q], zb[q]), h->inv_l2[q])) : Num<T>::zero();
         }
         warp_sum_many<8>(t);   // lane l now holds the warp total of dimension c0 + l / 4
         const int q = c0 + (lane >> 2);
@@ -438,6 +509,11 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
         for (int w = 0; w < XW; ++w) sacc = add(sacc, red[(rg * XW + w) * DC + b]);
         dx[(size_t)n * D + b] = Num<T>::st(neg(sacc));
       }
+    }
+    (void)nr;
+    if (more) {   // the next pass's rows: this thread's copies landed; convert them, publish
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
+      rowbuf(it + 1, n0 + RG, min(RG, nend - n0 - RG), true);
     }
     __syncthreads();
   }
@@ -714,9 +790,10 @@ __global__ void __launch_bounds__(256) wsum_kernel(int N, int M, int Dout, const
 size_t det_fwd_smem(int M, int D, bool zstage, size_t tsz) {
   return 256 * 8 + sizeof(Hyp<df64>) + ((size_t)FT * M + FKA * FCB + 8 * DO_MAX * FT + FT * D + (zstage ? (size_t)M * D : 0)) * tsz;
 }
-size_t det_bwd_smem(int bx, int rg, int dc, size_t tsz) {
+size_t det_bwd_smem(int bx, int rg, int dc, int M, int D, int Dk, size_t tsz) {
   const size_t red = (size_t)rg * bx * (dc + DO_MAX);   // the largest of the three uses of the area
-  return 256 * 8 + sizeof(Hyp<df64>) + ((size_t)rg * dc + (size_t)rg * 2 * DO_MAX + red) * tsz;
+  return 256 * 8 + sizeof(Hyp<df64>) +
+         ((size_t)M * D + (size_t)Dk * M + 2 * (size_t)det_bwd_rowbuf(rg, M, D, Dk) + red) * tsz;
 }
 
 template <typename T>
@@ -862,7 +939,7 @@ void det_bwd_launch(int grid, dim3 threads, cudaStream_t st, int N, int M, int D
                     const void* Bk, const void* dm, const void* dv, const void* dkfu, double* dsf2, double* dl,
                     double* dZ, double* dA, void* dx, double* work, long stride) {
   typedef typename Num<T>::store_t S;
-  const size_t sm = det_bwd_smem(threads.x, threads.y, DC, sizeof(T));
+  const size_t sm = det_bwd_smem(threads.x, threads.y, DC, M, D, dkfu ? 0 : Dout, sizeof(T));
   auto k = det_bwd_kernel<T, DC, DB, EX>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<grid, threads, sm, st>>>(N, M, D, Dout, (const S*)x, ldx, (const S*)Z, lls2, lsf2, (const S*)A, (const S*)kfu,
