@@ -31,6 +31,9 @@ constexpr int NT = 512;        // threads per CTA (forward)
 // threads per CTA of the backward (one CTA per SM): 32 warps when Q <= 2 (64 registers a
 // thread, no spills), 16 when the per-dimension sums of Q <= 8 need more registers
 __host__ __device__ constexpr int nt_bwd(int QC) { return QC <= 2 ? 1024 : 512; }
+// Q is QC itself in an exact instantiation (every width other than the two catch-all ones, 2
+// for Q <= 2 and QMAX above): the per-dimension loops then carry no runtime test
+__host__ __device__ constexpr bool exact_q(int QC) { return QC != 2 && QC != QMAX; }
 constexpr int PPT_MAX = 16;    // pairs per thread for register-resident per-pair sums
 constexpr int RED = 48;        // reduction slots per warp
 
@@ -283,7 +286,7 @@ template <typename T, int NPB, int PPT, int QC, int DB>
 __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::store_t> a) {
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
-  const int M = a.M, Q = a.Q, D = a.Dout;
+  const int M = a.M, Q = exact_q(QC) ? QC : a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
   const bool contract = (a.A != nullptr) && (a.B != nullptr) && (a.m_out != nullptr || a.v_out != nullptr);
   FSmem<T> s = fcarve<T>(smem_raw, M, Q, P, contract ? D : 0, NPB, a.bs_smem ? D * P : 0);
@@ -575,7 +578,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
   constexpr int NTB = nt_bwd(QC);
   typedef typename Num<T>::store_t S;
   extern __shared__ __align__(16) char smem_raw[];
-  const int M = a.M, Q = a.Q, D = a.Dout;
+  const int M = a.M, Q = exact_q(QC) ? QC : a.Q, D = a.Dout;
   const int P = M * (M + 1) / 2;
   BSmem<T> s = bcarve<T>(smem_raw, M, Q, P, a.accb_smem ? D * P : 0, NPB, a.bs_smem ? D * P : 0);
   // ---- per-CTA tables: exp table, Z, lengthscales, sf2, G_ab and the symmetrised B
@@ -1028,6 +1031,10 @@ int launch_fwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 2) per_sm = 2;
   if (a.Q <= 2) return fwd_variant<T, 2>(a, sum, contract, P, per_sm, sm, st);
+  // five input dimensions, one output, moments only (the psi-statistics workload's shape): an
+  // exact instantiation, so that the pair loop is the branch-free one (Q == QC)
+  if (a.Q == 5 && !sum && !a.chain && contract && a.Dout == 1 && !a.psi2 && a.bs_smem)
+    return run_fwd<T, 4, 0, 5, 1>(a, per_sm, sm, st);
   return fwd_variant<T, QMAX>(a, sum, contract, P, per_sm, sm, st);
 }
 
@@ -1429,6 +1436,7 @@ int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
       a.accb_smem = opts[o][1] > 0;
       if (npb == 2) return bwd_db<T, 2, 2>(a, sm, st);
       if (a.Q <= 2) return bwd_db<T, 1, 2>(a, sm, st);
+      if (a.Q == 5) return bwd_db<T, 1, 5>(a, sm, st);   // the psi-statistics workload's width, exact
       return bwd_db<T, 1, QMAX>(a, sm, st);
     }
   }

@@ -165,6 +165,13 @@ def test_psi_full_workload_vs_reference(prec):
     assert_close(np64(m)[pick], g['pt_m'], tol, 'm')
     assert_close(np64(v)[pick], g['pt_v'], tol, 'v')
     assert abs(float(np64(v).sum()) - float(g['v_sum'])) <= tol * abs(float(g['v_sum']))
+    # the moments alone (no psi1 / psi2 outputs): the exact five-dimension kernel's branch-free
+    # pair loop, against the same reference values
+    m2, v2 = torch.empty_like(m), torch.empty_like(v)
+    gpk.psi_fwd(t['mu'], t['S'], t['Z'], l2, s2, t['Ahat'], t['Bhat'], m_out=m2, v_out=v2)
+    assert_close(np64(m2)[pick], g['pt_m'], tol, 'm (moments only)')
+    assert_close(np64(v2)[pick], g['pt_v'], tol, 'v (moments only)')
+    assert abs(float(np64(v2).sum()) - float(g['v_sum'])) <= tol * abs(float(g['v_sum']))
     # the backward at the reference's m, so that both sides see the same upstream gradients
     m_dev = dev(g['m_full'], dt)
     z = lambda *sh: torch.zeros(sh, dtype=torch.float64, device='cuda')
