@@ -278,6 +278,12 @@ __device__ __forceinline__ float rsqrt_(float a) { return __frsqrt_rn(a); }
 __device__ __forceinline__ float scale2(float a, int e) { return scale2f(a, e); }
 template <typename Tab> __device__ __forceinline__ float exp_tab(float x, const Tab&) { return expf(x); }
 template <typename Tab> __device__ __forceinline__ float log_tab(float x, const Tab&) { return logf(x); }
+// The exp of the psi2 pair sweeps (one per pair and point, the bulk of those kernels): the
+// double-float exp_tab, or in FP32 CUDA's __expf intrinsic (documented maximum error
+// 2 + floor(|1.173 x|) ulp; the terms that dominate a sweep's sums have |x| near 0, and the
+// FP32 path's statistics are held to 1e-5 and its gradients to 1e-4 relative).
+template <typename Tab> __device__ __forceinline__ df64 exp_pair(df64 x, const Tab& tab) { return exp_tab(x, tab); }
+template <typename Tab> __device__ __forceinline__ float exp_pair(float x, const Tab&) { return __expf(x); }
 
 // Warp sums of K values at once (K a power of two <= 32): in each of the first log2 K steps
 // of the butterfly a lane keeps half of its values and adds its partner's copies of them,

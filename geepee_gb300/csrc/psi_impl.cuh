@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
 #pragma unroll
           for (int q = 0; q < QC; ++q)
             if (q < Q) cr = fma_(hh[q], zb[q], cr);
-          const T ps = exp_tab(sub(x, cr), s.tab);
+          const T ps = exp_pair(sub(x, cr), s.tab);
           if (a.psi2) {
             const S v = Num<T>::st(ps);
             const size_t o = (size_t)(n0 + pt) * M;
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
       }
 #pragma unroll
       for (int pt = 0; pt < NPB; ++pt) {
-        const T ps = exp_tab(arg[pt], s.tab);
+        const T ps = exp_pair(arg[pt], s.tab);
 #pragma unroll
         for (int d = 0; d < DB; ++d) vacc[pt][d] = fma_(w[d], ps, vacc[pt][d]);
       }
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
         }
         T ps[2];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) ps[u] = exp_tab(arg[u], s.tab);
+        for (int u = 0; u < 2; ++u) ps[u] = exp_pair(arg[u], s.tab);
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           T w = Num<T>::zero();
@@ -788,7 +788,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
 #pragma unroll
           for (int q = 0; q < QC; ++q)
             if (q < Q) cr = fma_(hh[q], zb[q], cr);
-          const T ps = exp_tab(sub(x, cr), s.tab);
+          const T ps = exp_pair(sub(x, cr), s.tab);
           T w = Num<T>::zero();
 #pragma unroll
           for (int d = 0; d < DB; ++d) {
@@ -1318,7 +1318,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         }
         T ps2[2];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) ps2[u] = exp_tab(arg[u], s.tab);
+        for (int u = 0; u < 2; ++u) ps2[u] = exp_pair(arg[u], s.tab);
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           T w = Num<T>::zero();
