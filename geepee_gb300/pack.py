@@ -24,23 +24,32 @@ class Pack:
         self.views = {}
         for (k, s), a, b in zip(self.spec, self.offsets[:-1], self.offsets[1:]):
             self.views[k] = self.dev[a:b].view(s if len(s) else (1,))
+        # (key, start, end, shape) as plain ints: the per-call loops below are host time on the
+        # objective's critical path
+        self._keys = [k for k, _ in self.spec]
+        self._sizes = sizes
+        self._bounds = [(k, int(a), int(b), s) for (k, s), a, b in zip(self.spec, self.offsets[:-1], self.offsets[1:])]
 
     def nbytes(self):
         return self.n * 8
 
     def upload(self, params):
         """numpy dict -> device (one pinned H2D copy, asynchronous on the current stream)."""
-        for (k, s), a, b in zip(self.spec, self.offsets[:-1], self.offsets[1:]):
-            self.host_np[a:b] = np.ravel(np.asarray(params[k], dtype=np.float64))
+        parts = [np.ravel(params[k]) for k in self._keys]
+        for k, p, n in zip(self._keys, parts, self._sizes):
+            if p.size != n:
+                raise ValueError('parameter %s has %d elements, %d expected' % (k, p.size, n))
+        np.concatenate(parts, out=self.host_np)
         self.dev.copy_(self.host, non_blocking=True)
 
     def download(self, shapes=None):
-        """device -> numpy dict (one D2H copy into pinned memory, then a synchronize)."""
+        """device -> numpy dict (one D2H copy into pinned memory, then a synchronize): the
+        arrays are views into one fresh copy of the pinned buffer."""
         self.host.copy_(self.dev, non_blocking=True)
         torch.cuda.current_stream().synchronize()
+        flat = self.host_np.copy()
         out = {}
-        for (k, s), a, b in zip(self.spec, self.offsets[:-1], self.offsets[1:]):
+        for k, a, b, s in self._bounds:
             shp = shapes[k] if shapes is not None and k in shapes else s
-            v = self.host_np[a:b].copy()
-            out[k] = float(v[0]) if shp == () else v.reshape(shp)
+            out[k] = float(flat[a]) if shp == () else flat[a:b].reshape(shp)
         return out
