@@ -422,9 +422,9 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
       for (int pt = 0; pt < NPB; ++pt) {
         const T* hu = s.u + pt * M;
         const T* hh = s.h + pt * M * QC + ia * QC;
-        T cr = Num<T>::zero();
+        T cr = mul(hh[0], s.z[ib * QC]);   // = fma_ from zero, bit for bit
 #pragma unroll
-        for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib * QC + q], cr);
+        for (int q = 1; q < QC; ++q) cr = fma_(hh[q], s.z[ib * QC + q], cr);
         arg[pt] = sub(add(add(hu[ia], hu[ib]), gab), cr);
       }
 #pragma unroll
@@ -725,9 +725,9 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const T* hh = s.h + ia[u] * QC;
-          T cr = Num<T>::zero();
+          T cr = mul(hh[0], s.z[ib[u] * QC]);   // = fma_ from zero, bit for bit
 #pragma unroll
-          for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
+          for (int q = 1; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
           arg[u] = sub(add(add(hu[ia[u]], hu[ib[u]]), s.G[pp[u]]), cr);
         }
         T ps[2];
@@ -735,15 +735,20 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
         for (int u = 0; u < 2; ++u) ps[u] = exp_pair(arg[u], s.tab);
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          T w = Num<T>::zero();
           T ab[DB];
 #pragma unroll
-          for (int d = 0; d < DB; ++d) {
-            w = fma_(dvr[0][d], s.Bs[d * P + pp[u]], w);
-            ab[d] = mul(dvr[0][d], ps[u]);
+          for (int d = 0; d < DB; ++d) ab[d] = mul(dvr[0][d], ps[u]);
+          // L~ (half weight off the diagonal: the symmetric matrix entry) = psi2 sum_d dv_d Bs_d:
+          // for one output (dv psi2) Bs, reusing the dB-hat term
+          T l;
+          if (DB == 1) {
+            l = mul(ab[0], s.Bs[pp[u]]);
+          } else {
+            T w = mul(dvr[0][0], s.Bs[pp[u]]);
+#pragma unroll
+            for (int d = 1; d < DB; ++d) w = fma_(dvr[0][d], s.Bs[d * P + pp[u]], w);
+            l = mul(w, ps[u]);
           }
-          // L~ (half weight off the diagonal: the symmetric matrix entry)
-          const T l = mul(w, ps[u]);
           if (ok[u]) {
             s.L[pp[u]] = ia[u] == ib[u] ? l : scale2(l, -1);
 #pragma unroll
@@ -1311,9 +1316,9 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const T* hh = s.h + ia[u] * QC;
-          T cr = Num<T>::zero();
+          T cr = mul(hh[0], s.z[ib[u] * QC]);   // = fma_ from zero, bit for bit
 #pragma unroll
-          for (int q = 0; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
+          for (int q = 1; q < QC; ++q) cr = fma_(hh[q], s.z[ib[u] * QC + q], cr);
           arg[u] = sub(add(add(s.u[ia[u]], s.u[ib[u]]), s.G[pp[u]]), cr);
         }
         T ps2[2];
@@ -1321,14 +1326,19 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         for (int u = 0; u < 2; ++u) ps2[u] = exp_pair(arg[u], s.tab);
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          T w = Num<T>::zero();
           T ab[DB];
 #pragma unroll
-          for (int d = 0; d < DB; ++d) {
-            w = fma_(dvr[d], s.Bs[d * P + pp[u]], w);
-            ab[d] = mul(dvr[d], ps2[u]);
+          for (int d = 0; d < DB; ++d) ab[d] = mul(dvr[d], ps2[u]);
+          // L = psi2 sum_d dv_d Bs_d: for one output (dv psi2) Bs, reusing the dB-hat term
+          T l;
+          if (DB == 1) {
+            l = mul(ab[0], s.Bs[pp[u]]);
+          } else {
+            T w = mul(dvr[0], s.Bs[pp[u]]);
+#pragma unroll
+            for (int d = 1; d < DB; ++d) w = fma_(dvr[d], s.Bs[d * P + pp[u]], w);
+            l = mul(w, ps2[u]);
           }
-          const T l = mul(w, ps2[u]);
           if (ok[u]) {
             s.L[pp[u]] = ia[u] == ib[u] ? l : scale2(l, -1);
 #pragma unroll
