@@ -214,9 +214,12 @@ __device__ __forceinline__ df64 rsqrt_(df64 a) {
 // ln2/256 = 0.0027076061740622863 as a df64 (hi + lo exact to 3.4e-19)
 __device__ __forceinline__ df64 ln2_over_256() { return make_df(2.707606182e-03f, -7.440055516e-12f); }
 
-template <typename Tab>
+// NARROW: the domain [-87, 88]; below it the result (< 1.6e-38, already subnormal in its high
+// word) is flushed to zero, so that the final scaling 2^m has m in [-126, 126] and takes one
+// multiply per word instead of the two-step range-checked one
+template <bool NARROW = false, typename Tab>
 __device__ __forceinline__ df64 exp_tab(df64 x, const Tab& tab) {
-  if (x.hi < -103.0f) return make_df(0.f);
+  if (x.hi < (NARROW ? -87.0f : -103.0f)) return make_df(0.f);
   if (x.hi > 88.0f) return make_df(__int_as_float(0x7f800000), 0.f);
   const float inv = 369.32993f;  // 256 / ln 2
   // k = round(x / (ln2/256)) by the 1.5*2^23 magic addition (|x * inv| < 2^22 here): the
@@ -234,6 +237,10 @@ __device__ __forceinline__ df64 exp_tab(df64 x, const Tab& tab) {
   int m = k >> 8;  // arithmetic shift: floor(k / 256)
   float2 tj = tab[j];
   df64 res = mul(make_df(tj.x, tj.y), e);
+  if (NARROW) {
+    const float s2m = pow2f(m);
+    return make_df(res.hi * s2m, res.lo * s2m);
+  }
   return scale2(res, m);
 }
 
@@ -282,7 +289,7 @@ template <typename Tab> __device__ __forceinline__ float log_tab(float x, const 
 // double-float exp_tab, or in FP32 CUDA's __expf intrinsic (documented maximum error
 // 2 + floor(|1.173 x|) ulp; the terms that dominate a sweep's sums have |x| near 0, and the
 // FP32 path's statistics are held to 1e-5 and its gradients to 1e-4 relative).
-template <typename Tab> __device__ __forceinline__ df64 exp_pair(df64 x, const Tab& tab) { return exp_tab(x, tab); }
+template <typename Tab> __device__ __forceinline__ df64 exp_pair(df64 x, const Tab& tab) { return exp_tab<true>(x, tab); }
 template <typename Tab> __device__ __forceinline__ float exp_pair(float x, const Tab&) { return __expf(x); }
 
 // Warp sums of K values at once (K a power of two <= 32): in each of the first log2 K steps
