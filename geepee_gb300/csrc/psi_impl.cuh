@@ -1074,12 +1074,13 @@ struct PSmem {
   T* accB;    // [Dout*P]
   T* carry;   // [2*QC] psi1 part of the previous point's dmu, dS
   T* red;     // [32*RED]
+  int* pab;   // [P] the pairs (a << 16 | b), the same for every point
 };
 
 __host__ __device__ inline size_t pipe_smem_bytes(int M, int Q, int QC, int P, int D, size_t tsz) {
   const size_t n = (size_t)M * Q + 4 * QMAX + 4 + 2 * 5 * QMAX + 2 * DMAX + M + (size_t)M * Q + P + (size_t)D * P + P +
                    (size_t)M * (1 + QC) + 2 * (size_t)M * Q + (size_t)D * P + 2 * QC + 32 * RED;
-  return 256 * 8 + n * tsz;
+  return 256 * 8 + n * tsz + (size_t)P * sizeof(int);
 }
 
 template <typename T, int QC>
@@ -1105,7 +1106,8 @@ __device__ PSmem<T> pcarve(char* base, int M, int Q, int P, int D) {
   s.dzr = t; t += M * Q;
   s.accB = t; t += D * P;
   s.carry = t; t += 2 * QC;
-  s.red = t;
+  s.red = t; t += 32 * RED;
+  s.pab = reinterpret_cast<int*>(t);
   return s;
 }
 
@@ -1148,6 +1150,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
   for (int p = tid; p < P; p += NTB) {
     int ia, ib;
     pair_of(p, ia, ib);
+    s.pab[p] = (ia << 16) | ib;
     T g = Num<T>::zero();
 #pragma unroll
     for (int q = 0; q < QC; ++q) {
@@ -1310,7 +1313,9 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         for (int u = 0; u < 2; ++u) {
           ok[u] = p0 + u * NTB < P;
           pp[u] = ok[u] ? p0 + u * NTB : p0;
-          pair_of(pp[u], ia[u], ib[u]);
+          const int ab = s.pab[pp[u]];
+          ia[u] = ab >> 16;
+          ib[u] = ab & 0xffff;
         }
         T arg[2];
 #pragma unroll
