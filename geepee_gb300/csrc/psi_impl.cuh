@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
           vals[(pt * DB + d) * 2] = mm;
           vals[(pt * DB + d) * 2 + 1] = vacc[pt][d];
         }
-      block_sum<T, 2 * NPB * DB>(vals, s.red);
+      block_sum_many<T, 2 * NPB * DB>(vals, s.red, NT / 32);
       if (threadIdx.x == 0) {
 #pragma unroll
         for (int pt = 0; pt < NPB; ++pt)
