@@ -184,11 +184,11 @@ def psi_bwd_bytes(N, M, Q, D):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one psi backward launch pair (kernel and
 # reduction) of the deep GP's layer 2 in one ncu capture of the same case (1000 points, M=100,
-# Q=2): 282,624 + 41,472 bytes for the pipelined kernel (its inputs; its outputs and partial
-# blocks stay in L2) and 6,604,544 for the reduction, which ncu replays after flushing the
+# Q=2): 280,064 + 41,216 bytes for the pipelined kernel (its inputs; its outputs and partial
+# blocks stay in L2) and 6,605,312 for the reduction, which ncu replays after flushing the
 # caches, so that the 152 per-CTA partial blocks it reads come from DRAM (in the evaluation
 # they are still in L2)
-PSI_BWD_TRAFFIC = 282624 + 41472 + 6604544
+PSI_BWD_TRAFFIC = 280064 + 41216 + 6605312
 
 
 def time_launches(fn, flush, reps=30):
