@@ -9,7 +9,7 @@ from tests._helpers import load, assert_close
 pytestmark = pytest.mark.gpu
 
 DF64_TOL = 1e-10   # double-float (~48-bit) arithmetic against float64
-FP32_TOL = 1e-5    # FP32 psi statistics (spec tolerance)
+FP32_TOL = 1e-5    # FP32 psi statistics (the stated tolerance for that path)
 
 
 def dev(a, dtype=torch.float64):

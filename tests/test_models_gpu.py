@@ -1,5 +1,5 @@
 """GPU parity of the AEP models (objective, gradients, predictions) against the reference's
-golden fixtures.  Energies and predictive moments: rel <= 1e-6 (spec tolerance).
+golden fixtures.  Energies and predictive moments: rel <= 1e-6 (the stated tolerance).
 Gradients: per key, error against the long-double truth within max(1e-6, 4 x the reference's
 own float64 error).  The reference is itself only accurate to ~1e-3 on the deep GP's second
 layer (cond(Kuu) ~ 7e6): its gradient w.r.t. Kuu goes through products with Kuu^-1 that cancel

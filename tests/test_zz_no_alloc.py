@@ -26,7 +26,7 @@ def test_spd_inv_static_matches_workspace_entry_twice(prec):
     from geepee_gb300._lib import call, ptr, stream, GPK_DF64, GPK_FP32
     p, dt = (GPK_DF64, torch.float64) if prec == 'df64' else (GPK_FP32, torch.float32)
     rng = np.random.RandomState(5)
-    # one call before the memory checks: the driver loads the library's module data (the
+    # one call before the memory checks: the CUDA driver loads the library's module data (the
     # array itself) on first use of the symbol, which is not an allocation by the entry point
     A0 = dev(_spd(rng, 1, 8)).to(dt)
     out0 = torch.empty_like(A0)
