@@ -11,7 +11,9 @@ import os
 import torch
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, 'libgpk.so')
+# GPK_LIBRARY selects another build of the same ABI (e.g. libgpk_debug.so, the bounds-checked
+# build)
+LIB_PATH = os.environ.get('GPK_LIBRARY') or os.path.join(_HERE, 'libgpk.so')
 
 GPK_DF64 = 0
 GPK_FP32 = 1
@@ -23,6 +25,7 @@ _vp = ctypes.c_void_p
 # name -> argtypes (all return int)
 _SIGS = {
     'gpk_version': [],
+    'gpk_debug_bounds': [_vp],
     'gpk_kern': [_c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _c_int, _vp, _vp, _c_dbl, _vp, _c_int, _vp],
     'gpk_psi_fwd': [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                     _vp, _vp, _vp, _vp, _vp, _vp],

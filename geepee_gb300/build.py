@@ -35,7 +35,13 @@ def _stale(src: str, obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in [src] + deps)
 
 
-def build(verbose: bool = False, extra=()) -> str:
+def build(verbose: bool = False, extra=(), debug_bounds: bool = False) -> str:
+    """Compile and link libgpk.so; with debug_bounds, the index-checked build (-DGPK_DEBUG_BOUNDS)
+    into libgpk_debug.so, from objects of its own."""
+    OBJ = os.path.join(HERE, '_build_debug' if debug_bounds else '_build')
+    OUT = os.path.join(HERE, 'libgpk_debug.so' if debug_bounds else 'libgpk.so')
+    if debug_bounds:
+        extra = tuple(extra) + ('-DGPK_DEBUG_BOUNDS',)
     os.makedirs(OBJ, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, '*.cu')))
     deps = glob.glob(os.path.join(CSRC, '*.cuh')) + glob.glob(os.path.join(HERE, '..', 'include', '*.h'))
@@ -43,7 +49,7 @@ def build(verbose: bool = False, extra=()) -> str:
     jobs = []
     for s in srcs:
         o = os.path.join(OBJ, os.path.basename(s)[:-3] + '.o')
-        if _stale(s, o, deps) or extra:
+        if _stale(s, o, deps) or (extra and not debug_bounds):
             jobs.append([cc, *ARCH, *FLAGS, *extra, '-c', s, '-o', o])
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -63,4 +69,4 @@ def build(verbose: bool = False, extra=()) -> str:
 
 
 if __name__ == '__main__':
-    print(build(verbose='-v' in sys.argv))
+    print(build(verbose='-v' in sys.argv, debug_bounds='--debug-bounds' in sys.argv))

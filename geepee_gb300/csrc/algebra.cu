@@ -644,3 +644,6 @@ extern "C" int gpk_cavity_forms(int n, const gpk_forms_t* items, void* stream) {
   cavity_forms_kernel<<<total * f.chunks, 256, 0, gpk::as_stream(stream)>>>(f);
   return gpk::check_launch("cavity_forms");
 }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(algebra)

@@ -9,6 +9,35 @@
 #include "../../include/gpk.h"
 #include "df64.cuh"
 
+// Debug build (-DGPK_DEBUG_BOUNDS; build(debug_bounds=True) -> libgpk_debug.so): the hot
+// kernels' indexed accesses go through GPK_IDX(i, n, code).  An index outside [0, n) sets bit
+// `code` of this translation unit's error word and is replaced by 0 (an element that exists),
+// so the kernel completes and the host reads the word (gpk_debug_bounds).  The release build
+// compiles the checks away.  Codes: 0 factor L, 1 GEMM tile staging, 2 psi backward pair
+// table / L / accumulators, 3 psi forward pair tables, 4 det backward row buffer, 5 det
+// contraction B, 6 psi backward row sums.
+#ifdef GPK_DEBUG_BOUNDS
+static __device__ unsigned int g_gpk_bounds_word;
+__device__ __forceinline__ long gpk_idx(long i, long n, int code) {
+  if (i >= 0 && i < n) return i;
+  atomicOr(&g_gpk_bounds_word, 1u << code);
+  return 0;
+}
+#define GPK_IDX(i, n, code) gpk_idx((long)(i), (long)(n), (code))
+// this translation unit's word, cleared after reading (host side)
+#define GPK_BOUNDS_READER(name)                                           \
+  unsigned gpk_bounds_word_##name() {                                     \
+    unsigned w = 0, z = 0;                                                \
+    cudaMemcpyFromSymbol(&w, g_gpk_bounds_word, sizeof(w));               \
+    cudaMemcpyToSymbol(g_gpk_bounds_word, &z, sizeof(z));                 \
+    return w;                                                             \
+  }
+#else
+#define GPK_IDX(i, n, code) (i)
+#define GPK_BOUNDS_READER(name) \
+  unsigned gpk_bounds_word_##name() { return 0u; }
+#endif
+
 namespace gpk {
 
 // per-thread text of the last error (read by gpk_last_error)

@@ -88,8 +88,8 @@ __device__ __forceinline__ void gemm_tile(int bx, int by, int bz, int m, int n, 
     }
 #pragma unroll
     for (int u = 0; u < NPT; ++u) {
-      if (oa[u] >= 0) As[oa[u]] = P2 ? pair_bits<T>(ra[u]) : Num<T>::ld(ra[u]);
-      if (ob[u] >= 0) Bs[ob[u]] = P2 ? pair_bits<T>(rb[u]) : Num<T>::ld(rb[u]);
+      if (oa[u] >= 0) As[GPK_IDX(oa[u], KC * TBM, 1)] = P2 ? pair_bits<T>(ra[u]) : Num<T>::ld(ra[u]);
+      if (ob[u] >= 0) Bs[GPK_IDX(ob[u], KC * TBM, 1)] = P2 ? pair_bits<T>(rb[u]) : Num<T>::ld(rb[u]);
     }
     __syncthreads();
 #pragma unroll 4
@@ -336,7 +336,9 @@ __global__ void __launch_bounds__(NW * 32, 1) spd_factor_kernel(int M, const typ
   // the slack rows past M of every pair: zeros, read by the rows past M of a last row slot
   for (int e = threadIdx.x; e < NP * 64; e += NTH) Lp[((size_t)(e >> 6) * LDP + M) * 2 + (e & 63)] = Num<T>::zero();
   __syncthreads();
-  auto at = [&](int k, int i) -> T* { return Lp + ((size_t)(k >> 1) * LDP + i) * 2 + (k & 1); };
+  auto at = [&](int k, int i) -> T* {
+    return Lp + GPK_IDX(((size_t)(k >> 1) * LDP + i) * 2 + (k & 1), (size_t)NP * LDP * 2, 0);
+  };
 
   // column k of L from the register column `col` of its owner warp (row k in lane 0, slot 0)
   auto finalize = [&](int k, const T (&col)[RS]) {
@@ -1199,3 +1201,6 @@ extern "C" int gpk_small_spd(int prec, int batch, int n, const void* A, void* Ai
     return gpk::fail(GPK_EINVAL, "small_spd: unknown precision %d", prec);
   return gpk::check_launch("small_spd");
 }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(dense)

@@ -21,6 +21,29 @@ extern "C" int gpk_version(void) {
   GPK_NVTX("gpk_version"); return 1; }
 extern "C" const char* gpk_last_error(void) { return gpk::g_err; }
 
+// the other translation units' bounds words (common.cuh, GPK_BOUNDS_READER)
+unsigned gpk_bounds_word_algebra();
+unsigned gpk_bounds_word_dense();
+unsigned gpk_bounds_word_kern();
+unsigned gpk_bounds_word_psi_api();
+unsigned gpk_bounds_word_psi_bwd_df64();
+unsigned gpk_bounds_word_psi_bwd_f32();
+unsigned gpk_bounds_word_psi_fwd_df64();
+unsigned gpk_bounds_word_psi_fwd_f32();
+
+extern "C" int gpk_debug_bounds(unsigned int* word) {
+  GPK_NVTX("gpk_debug_bounds");
+  if (!word) return gpk::fail(GPK_EINVAL, "debug_bounds: null output");
+  *word = gpk_bounds_word_algebra() | gpk_bounds_word_dense() | gpk_bounds_word_kern() | gpk_bounds_word_psi_api() |
+          gpk_bounds_word_psi_bwd_df64() | gpk_bounds_word_psi_bwd_f32() | gpk_bounds_word_psi_fwd_df64() |
+          gpk_bounds_word_psi_fwd_f32();
+#ifdef GPK_DEBUG_BOUNDS
+  return 1;
+#else
+  return 0;
+#endif
+}
+
 namespace {
 
 // Eight lanes per output element j: lane l sums the partials c = l, l + 8, ... in order, then

@@ -395,6 +395,7 @@ __global__ void __launch_bounds__(512) det_bwd_kernel(int N, int M, int D, int D
         o = ov + (e - nk - nb - nx - ng);
         src = dv + (size_t)n0 * Dk + (e - nk - nb - nx - ng);
       }
+      o = GPK_IDX(o, BS, 4);
       if (convert) {
         B0[o] = Num<T>::ld(R0[o]);
       } else {
@@ -1113,3 +1114,6 @@ extern "C" int gpk_wsum(int prec, int N, int M, int Dout, const void* u, const v
     return gpk::fail(GPK_EINVAL, "wsum: unknown precision %d", prec);
   return gpk::check_launch("wsum");
 }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(kern)

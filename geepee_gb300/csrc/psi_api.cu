@@ -136,3 +136,6 @@ extern "C" int gpk_psi_bwd_ws(int prec, int N, int M, int Q, int Dout, const voi
   }
   return gpk::fail(GPK_EINVAL, "psi_bwd: unknown precision %d", prec);
 }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(psi_api)

@@ -3,3 +3,6 @@
 #include "psi_impl.cuh"
 
 int psi_bwd_f32(const psi_impl::PsiArgs<float>& a, cudaStream_t st) { return psi_impl::launch_bwd<float>(a, st); }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(psi_bwd_f32)

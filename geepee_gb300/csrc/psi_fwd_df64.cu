@@ -3,3 +3,6 @@
 #include "psi_impl.cuh"
 
 int psi_fwd_df64(const psi_impl::PsiArgs<double>& a, cudaStream_t st) { return psi_impl::launch_fwd<df64>(a, st); }
+
+// the translation unit's bounds word (debug build; 0 otherwise)
+GPK_BOUNDS_READER(psi_fwd_df64)

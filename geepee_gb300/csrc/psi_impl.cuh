@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(NT) psi_fwd_kernel(PsiArgs<typename Num<T>::st
     // sums without branches, so the NPB points' exps interleave.  In a pass with fewer than NPB
     // points the extra slots run on stale tables; their sums are never read.
     auto do_pair_fast = [&](int p, int ia, int ib) {
+      p = GPK_IDX(p, P, 3);
       const T gab = s.G[p];
       T w[DB];
 #pragma unroll
@@ -1192,8 +1193,8 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         const int jb = ib + 8, jc = jb < M ? jb : ib;
         const int p = ia >= ib ? rowbase + ib : ib * (ib + 1) / 2 + ia;
         const int p1 = ia >= jc ? rowbase + jc : jc * (jc + 1) / 2 + ia;
-        const T l = s.L[p];
-        const T l1 = jb < M ? s.L[p1] : Num<T>::zero();
+        const T l = s.L[GPK_IDX(p, P, 6)];
+        const T l1 = jb < M ? s.L[GPK_IDX(p1, P, 6)] : Num<T>::zero();
         R = add(R, l);
         R1 = add(R1, l1);
 #pragma unroll
@@ -1313,6 +1314,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_pipe_kernel(PsiArgs<typena
         for (int u = 0; u < 2; ++u) {
           ok[u] = p0 + u * NTB < P;
           pp[u] = ok[u] ? p0 + u * NTB : p0;
+          pp[u] = GPK_IDX(pp[u], P, 2);
           const int ab = s.pab[pp[u]];
           ia[u] = ab >> 16;
           ib[u] = ab & 0xffff;

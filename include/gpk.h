@@ -37,6 +37,16 @@ extern "C" {
 int gpk_version(void);
 const char* gpk_last_error(void);
 
+/* Index checks of the debug build.  A library built with -DGPK_DEBUG_BOUNDS (the build
+ * script's debug_bounds option, libgpk_debug.so) checks the hot kernels' indexed accesses; an
+ * index out of range sets a bit of an error word (the access then goes to element 0) and the
+ * kernel completes.  Writes the OR of the words (bit 0 factor L, 1 GEMM tile staging, 2 psi
+ * backward pair table / L / accumulators, 3 psi forward pair tables, 4 det backward row
+ * buffer, 6 psi backward row sums) into *word and clears them; synchronous.  Returns 1 for a
+ * debug build, 0 for a release build (*word = 0), <0 for a null pointer.  (No counterpart in
+ * the reference; a debugging aid.) */
+int gpk_debug_bounds(unsigned int* word);
+
 /* ARD exponentiated-quadratic kernel matrix
  *   K[n,m] = sf2 * exp(-1/2 sum_d (x[n,d]-z[m,d])^2 / ell2[d])  (+ jitter if n == m)
  * x: [N,D] (row stride ldx), z: [M,D] (row stride ldz), K: [N,M] (row stride ldk).

@@ -59,3 +59,31 @@ def test_python_binding_argument_counts_match_header():
     assert set(L._SIGS) <= set(protos)
     bad = {n: (len(L._SIGS[n]), protos[n]) for n in L._SIGS if len(L._SIGS[n]) != protos[n]}
     assert not bad, f'(binding, header) argument counts differ: {bad}'
+
+
+def test_release_library_reports_no_bounds_checks():
+    """gpk_debug_bounds in the release build: 0 (no checks compiled in), word 0; a host-only
+    call."""
+    lib = _lib()
+    w = ctypes.c_uint(7)
+    assert lib.gpk_debug_bounds(ctypes.byref(w)) == 0
+    assert w.value == 0
+    assert lib.gpk_debug_bounds(None) < 0
+
+
+def test_debug_bounds_unit_compiles():
+    """The index-checked variant (-DGPK_DEBUG_BOUNDS) of the unit that aggregates the words and
+    of the SPD factor / GEMM unit compiles for sm_103a."""
+    import shutil
+    import subprocess
+    import tempfile
+    nvcc = shutil.which('nvcc') or '/usr/local/cuda/bin/nvcc'
+    if not os.path.exists(nvcc):
+        pytest.skip('no nvcc here')
+    from geepee_gb300 import build
+    with tempfile.TemporaryDirectory() as d:
+        for unit in ('gpk.cu', 'dense.cu'):
+            r = subprocess.run([nvcc, *build.ARCH, *build.FLAGS, '-DGPK_DEBUG_BOUNDS', '-c',
+                                os.path.join(build.CSRC, unit), '-o', os.path.join(d, unit + '.o')],
+                               capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr[-2000:]
