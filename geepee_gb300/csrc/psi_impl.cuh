@@ -132,11 +132,11 @@ __device__ __forceinline__ void block_sum(T* vals, T* red, int nact = 0) {
 }
 
 // block_sum for a point's handful of values: each warp reduces them in multi-value butterflies
-// of eight (warp_sum_many; lane 4v then holds value c0 + v), lane i of warp 0 adds value i over
-// the warps in order and shuffles it to the warp.  Fixed order; K <= 32.
+// of eight (warp_sum_many; lane 4v then holds value c0 + v), lane i of warp 0 adds value i (and
+// i + 32) over the warps in order and shuffles it to the warp.  Fixed order; K <= RED.
 template <typename T, int K>
 __device__ __forceinline__ void block_sum_many(T (&vals)[K], T* red, int nact) {
-  static_assert(K <= 32 && K <= RED, "K values per lane of warp 0");
+  static_assert(K <= RED, "K values per warp slot");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp < nact) {
 #pragma unroll
@@ -150,13 +150,16 @@ __device__ __forceinline__ void block_sum_many(T (&vals)[K], T* red, int nact) {
   }
   __syncthreads();
   if (warp == 0) {
-    T s = Num<T>::zero();
-    if (lane < K) {
-      s = red[lane];
-      for (int w = 1; w < nact; ++w) s = add(s, red[w * RED + lane]);
-    }
 #pragma unroll
-    for (int i = 0; i < K; ++i) vals[i] = shfl_idx(s, i);
+    for (int c0 = 0; c0 < K; c0 += 32) {
+      T s = Num<T>::zero();
+      if (c0 + lane < K) {
+        s = red[c0 + lane];
+        for (int w = 1; w < nact; ++w) s = add(s, red[w * RED + c0 + lane]);
+      }
+#pragma unroll
+      for (int i = c0; i < K && i < c0 + 32; ++i) vals[i] = shfl_idx(s, i - c0);
+    }
   }
 }
 
@@ -903,7 +906,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
       }
     }
     // ---- per-point totals: one CTA reduction, then lane q of warp 0 finalises dimension q
-    block_sum<T, NPB * KV>(vals, s.red, (M + 31) >> 5);   // vals live in the row threads ia0 < M
+    block_sum_many<T, NPB * KV>(vals, s.red, (M + 31) >> 5);   // vals live in the row threads ia0 < M
     if (threadIdx.x < 32) {
 #pragma unroll
       for (int pt = 0; pt < NPB; ++pt) {
