@@ -59,6 +59,7 @@ struct PsiArgs {
   int chain;         // forward rollout: point n > 0 takes point n-1's (m, v) as its (mu, var)
   int bs_smem;       // symmetrised B staged in shared memory (set by the launcher)
   int accb_smem;     // backward: dBhat accumulates in shared memory (else atomically in dB)
+  int pab_smem;      // backward: the pair table fits in shared memory (set by the launcher)
   long b_stride;     // != 0: B is per point (B + n*b_stride), dv treated as 1
   double* dsf2;
   double* dl;
@@ -538,6 +539,7 @@ struct BSmem {
   T* dz;     // [M*Q]
   T* accB;   // [Dout*P] sum over the CTA's points of dv psi2 (dBhat)
   T* red;    // [32*RED]
+  int* pab;  // [P] the pairs (a << 16 | b), the same for every point
 };
 
 __host__ __device__ inline size_t bwd_smem_bytes(int M, int Q, int P, int nacc, int npb, size_t tsz, int nbs) {
@@ -567,7 +569,8 @@ __device__ BSmem<T> bcarve(char* base, int M, int Q, int P, int nacc, int npb, i
   s.rows = t; t += npb * M * (1 + QMAX);
   s.dz = t; t += M * Q;
   s.accB = nacc ? t : nullptr; t += nacc;
-  s.red = t;
+  s.red = t; t += 32 * RED;
+  s.pab = reinterpret_cast<int*>(t);
   return s;
 }
 
@@ -615,6 +618,7 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
   for (int p = threadIdx.x; p < P; p += NTB) {
     int ia, ib;
     pair_of(p, ia, ib);
+    if (a.pab_smem) s.pab[p] = (ia << 16) | ib;
     T g = Num<T>::zero();
 #pragma unroll
     for (int q = 0; q < QC; ++q) {
@@ -722,8 +726,14 @@ __global__ void __launch_bounds__(nt_bwd(QC)) psi_bwd_kernel(PsiArgs<typename Nu
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           ok[u] = p0 + u * NTB < P;
-          pp[u] = ok[u] ? p0 + u * NTB : p0;
-          pair_of(pp[u], ia[u], ib[u]);
+          pp[u] = GPK_IDX(ok[u] ? p0 + u * NTB : p0, P, 2);
+          if (a.pab_smem) {   // the pair's (a, b) from the per-CTA table (CTA-uniform test)
+            const int ab = s.pab[pp[u]];
+            ia[u] = ab >> 16;
+            ib[u] = ab & 0xffff;
+          } else {
+            pair_of(pp[u], ia[u], ib[u]);
+          }
         }
         T arg[2];
 #pragma unroll
@@ -1450,10 +1460,14 @@ int launch_bwd(const PsiArgs<typename Num<T>::store_t>& a_in, cudaStream_t st) {
     // without either (dBhat then accumulates with atomics in global memory)
     const int opts[3][2] = {{nbs, nacc}, {0, nacc}, {0, 0}};
     for (int o = 0; o < 3; ++o) {
-      const size_t sm = bwd_smem_bytes(a.M, a.Q, P, opts[o][1], npb, sizeof(T), opts[o][0]);
+      size_t sm = bwd_smem_bytes(a.M, a.Q, P, opts[o][1], npb, sizeof(T), opts[o][0]);
       if (sm > cap) continue;
       a.bs_smem = opts[o][0] > 0;
       a.accb_smem = opts[o][1] > 0;
+      // the pair table only where it fits on top of this option (it never displaces B or the
+      // dB-hat accumulators)
+      a.pab_smem = sm + (size_t)P * sizeof(int) <= cap;
+      if (a.pab_smem) sm += (size_t)P * sizeof(int);
       if (npb == 2) return bwd_db<T, 2, 2>(a, sm, st);
       if (a.Q <= 2) return bwd_db<T, 1, 2>(a, sm, st);
       if (a.Q == 5) return bwd_db<T, 1, 5>(a, sm, st);   // the psi-statistics workload's width, exact
