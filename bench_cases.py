@@ -8,6 +8,7 @@ Cases run one kernel of the deep-GP objective on its real input shapes:
   psi_fwd_dgp   psi forward, same shapes, df64
   psi_fwd_c2    psi forward with sum_n psi2, N=10000, Q=5, M=100, df64
   psi_fwd_c2_f32  the same in FP32
+  psi_fwd_c2m_f32 psi forward, moments only (m, v; the bench line's form), N=10000, Q=5, M=100, FP32
   psi_bwd_c2    psi backward, N=10000, Q=5, M=100, df64
   chol_m100     SPD Cholesky + inverse + logdet of one 100x100 Kuu, df64
   gemm_m100     one 100x100x100 df64 GEMM (the M x M algebra)
@@ -56,13 +57,13 @@ def case(name):
         work = z(gpk.work_elems(gpk.OP_PSI_BWD, N, M, Q, 1))
         return lambda: gpk.psi_bwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'], m,
                                    t['dm'], t['dv'], *bufs, work=work)
-    if name in ('psi_fwd_dgp', 'psi_fwd_c2', 'psi_fwd_c2_f32'):
+    if name in ('psi_fwd_dgp', 'psi_fwd_c2', 'psi_fwd_c2_f32', 'psi_fwd_c2m_f32'):
         N, Q, M = (1000, 2, 100) if name == 'psi_fwd_dgp' else (10000, 5, 100)
         dtype = torch.float32 if name.endswith('f32') else torch.float64
         t = _psi_case(N, Q, M, 1, dtype)
         m = torch.empty((N, 1), dtype=dtype, device='cuda')
         v = torch.empty_like(m)
-        s = z(M, M) if name != 'psi_fwd_dgp' else None
+        s = z(M, M) if name in ('psi_fwd_c2', 'psi_fwd_c2_f32') else None
         return lambda: gpk.psi_fwd(t['mu'], t['S'], t['Z'], t['lls2'], t['lsf2'], t['Ahat'], t['Bhat'],
                                    psi2_sum=s, m_out=m, v_out=v)
     if name == 'chol_m100':
